@@ -1,0 +1,398 @@
+"""GB300 spectral Ewald summation for the doubly-periodic 2-D Stokeslet and stresslet.
+
+Python mirror of annabroms/FastTools2D's spectral Ewald interface, backed by
+the CUDA library ``_build/libfte_gb300.so`` (C ABI in ``include/fasttools2d.h``):
+
+* ``StokesSLP_ewald_2p`` / ``StokesDLP_ewald_2p`` mirror the MATLAB drivers
+  (PeriodicEwald/src/matlab/StokesSLP_ewald_2p.m:1-2, StokesDLP_ewald_2p.m:1-2):
+  same positional arguments, the options ``P``, ``Nb``, ``tol``, ``verbose``,
+  and the outputs ``(u1, u2, ur, uk, xi)``.
+* ``mex_stokes_slp_real``, ``mex_stokes_slp_kspace``, ``mex_stokes_dlp_real``,
+  ``mex_stokes_dlp_kspace`` mirror the four MEX gateways (argument order of
+  PeriodicEwald/src/mex/StokesSLP/mex_stokes_slp_real.cpp:65-83, ..._kspace.cpp:19-45,
+  PeriodicEwald/src/mex/StokesDLP/mex_stokes_dlp_real.cpp:36-52, ..._kspace.cpp:239-264);
+  2 x N arrays are given as (N, 2) arrays (x/y interleaved, the same memory).
+
+Arrays may be numpy arrays (host memory; copied to the GPU inside the call) or
+CUDA torch tensors (used in place).  There is no CPU fallback: if the library
+is missing or no GPU is present the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libfte_gb300.so")
+
+FTE_OK = 0
+FTE_ERR_INVALID = 1
+FTE_ERR_CUDA = 2
+FTE_ERR_ALLOC = 3
+FTE_ERR_UNSUPPORTED = 4
+FTE_ERR_DEVICE = 5
+FTE_DEVICE_POINTERS = 1
+FORM_PLAIN = 0
+FORM_MIXED = 1
+KIND_SLP = 0
+KIND_DLP = 1
+
+
+class FteError(RuntimeError):
+    """A call into the GPU library failed; ``code`` is the FTE_ERR_* status."""
+
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[fte status {code}] {msg}")
+        self.code = code
+
+
+class Params(C.Structure):
+    _fields_ = [("P", C.c_int), ("Nb", C.c_double), ("tol", C.c_double), ("Q", C.c_double),
+                ("A", C.c_int), ("B", C.c_int), ("nside_x", C.c_int), ("nside_y", C.c_int),
+                ("rc", C.c_double), ("xi", C.c_double), ("kinf", C.c_int), ("Mx", C.c_int), ("My", C.c_int),
+                ("w", C.c_double), ("eta", C.c_double)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+class Options(C.Structure):
+    _fields_ = [("P", C.c_int), ("Nb", C.c_double), ("tol", C.c_double), ("xi", C.c_double),
+                ("Mx", C.c_int), ("My", C.c_int), ("nside_x", C.c_int), ("nside_y", C.c_int),
+                ("weights", C.c_void_p), ("form", C.c_int)]
+
+
+class Info(C.Structure):
+    _fields_ = [("params", Params), ("ms_total", C.c_double), ("ms_cells", C.c_double), ("ms_near", C.c_double),
+                ("ms_spread", C.c_double), ("ms_fft", C.c_double), ("ms_gather", C.c_double),
+                ("near_pairs", C.c_longlong), ("kernels_launched", C.c_int)]
+
+    def as_dict(self):
+        d = {n: getattr(self, n) for n, _ in self._fields_ if n != "params"}
+        d["params"] = self.params.as_dict()
+        return d
+
+
+_lock = threading.Lock()
+_lib = None
+_default_ctx = None
+
+_vp = C.c_void_p
+_i64 = C.c_int64
+_d = C.c_double
+_i = C.c_int
+_u = C.c_uint
+
+# exported symbol -> (restype, argtypes)
+SIGNATURES = {
+    "fte_last_error": (C.c_char_p, []),
+    "fte_version": (_i, []),
+    "fte_create": (_i, [C.POINTER(_vp), _i]),
+    "fte_destroy": (_i, [_vp]),
+    "fte_set_stream": (_i, [_vp, _vp]),
+    "fte_set_timing": (_i, [_vp, _i]),
+    "fte_kernel_count": (C.c_longlong, [_vp]),
+    "fte_slp_real": (_i, [_vp, _vp, _i64, _vp, _i64, _vp, _d, _i, _i, _d, _d, _vp, _u]),
+    "fte_dlp_real": (_i, [_vp, _vp, _i64, _vp, _i64, _vp, _vp, _d, _i, _i, _d, _d, _vp, _u]),
+    "fte_slp_kspace": (_i, [_vp, _vp, _i64, _vp, _i64, _d, _d, _vp, _i, _i, _d, _d, _d, _i, _vp, _u]),
+    "fte_dlp_kspace": (_i, [_vp, _vp, _i64, _vp, _i64, _d, _d, _vp, _vp, _i, _i, _d, _d, _d, _i, _vp, _u]),
+    "fte_stokes_slp_ewald_2p": (_i, [_vp, _vp, _vp, _i64, _vp, _vp, _i64, _vp, _vp, _d, _d, C.POINTER(Options),
+                                     _vp, _vp, _vp, _vp, C.POINTER(Info), _u]),
+    "fte_stokes_dlp_ewald_2p": (_i, [_vp, _vp, _vp, _i64, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _d, _d,
+                                     C.POINTER(Options), _vp, _vp, _vp, _vp, C.POINTER(Info), _u]),
+    "fte_choose_params": (_i, [_i, _i64, _i64, _vp, _vp, _d, _d, C.POINTER(Options), C.POINTER(Params)]),
+}
+
+
+def build(verbose: bool = False) -> str:
+    """Compile the CUDA library for sm_103a (see buildlib.py)."""
+    from . import buildlib
+
+    return buildlib.build(verbose=verbose)
+
+
+def lib():
+    """Load the GPU library (raises if it has not been built)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                raise FteError(FTE_ERR_UNSUPPORTED,
+                               f"GPU library not built: {LIB_PATH} is missing (run fasttools2d_gb300.build())")
+            L = C.CDLL(LIB_PATH)
+            for name, (res, args) in SIGNATURES.items():
+                fn = getattr(L, name)
+                fn.restype = res
+                fn.argtypes = args
+            _lib = L
+    return _lib
+
+
+def _check(status: int):
+    if status != FTE_OK:
+        msg = lib().fte_last_error()
+        raise FteError(status, msg.decode() if msg else "")
+
+
+class Context:
+    """Owns a CUDA stream and the device workspace of the library."""
+
+    def __init__(self, device: int = 0):
+        h = _vp()
+        _check(lib().fte_create(C.byref(h), int(device)))
+        self.h = h
+        self.device = device
+
+    def close(self):
+        if self.h:
+            lib().fte_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_handle: int | None):
+        _check(lib().fte_set_stream(self.h, _vp(stream_handle) if stream_handle else None))
+
+    def set_timing(self, on: bool):
+        _check(lib().fte_set_timing(self.h, 1 if on else 0))
+
+    @property
+    def kernel_count(self) -> int:
+        return lib().fte_kernel_count(self.h)
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+# ---- argument marshalling ----------------------------------------------------
+
+def _is_cuda_tensor(a) -> bool:
+    return hasattr(a, "is_cuda") and getattr(a, "is_cuda")
+
+
+class _Args:
+    """Collects pointers for one call; all arrays must be on the same side."""
+
+    def __init__(self):
+        self.keep = []
+        self.device = None
+
+    def arr(self, a, ncomp: int, n: int | None = None):
+        if a is None:
+            return None, 0
+        if _is_cuda_tensor(a):
+            import torch
+
+            t = a.to(torch.float64).contiguous()
+            if self.device is False:
+                raise ValueError("mixing host and device arrays in one call")
+            self.device = True
+            self.keep.append(t)
+            cnt = t.numel() // ncomp
+            return t.data_ptr(), cnt
+        x = np.ascontiguousarray(np.asarray(a, dtype=np.float64))
+        if ncomp == 2 and x.ndim == 2 and x.shape[1] != 2 and x.shape[0] == 2:
+            x = np.ascontiguousarray(x.T)  # accept MATLAB-shaped 2 x N
+        if self.device is True:
+            raise ValueError("mixing host and device arrays in one call")
+        self.device = False
+        self.keep.append(x)
+        return x.ctypes.data, x.size // ncomp
+
+    def out(self, shape):
+        if self.device:
+            import torch
+
+            t = torch.empty(shape, dtype=torch.float64, device="cuda")
+            self.keep.append(t)
+            return t, t.data_ptr()
+        x = np.empty(shape, dtype=np.float64)
+        self.keep.append(x)
+        return x, x.ctypes.data
+
+    @property
+    def flags(self) -> int:
+        return FTE_DEVICE_POINTERS if self.device else 0
+
+
+# ---- MEX-shaped entries --------------------------------------------------------
+
+def mex_stokes_slp_real(psrc, ptar, f, xi, nside_x, nside_y, Lx, Ly, ctx: Context | None = None):
+    ctx = ctx or default_context()
+    A = _Args()
+    ps, ns = A.arr(psrc, 2)
+    pt, nt = A.arr(ptar, 2)
+    pf, nf = A.arr(f, 2)
+    if nf != ns:
+        raise ValueError("psrc and f must be the same size.")
+    out, po = A.out((nt, 2))
+    _check(lib().fte_slp_real(ctx.h, ps, ns, pt, nt, pf, float(xi), int(nside_x), int(nside_y), float(Lx), float(Ly),
+                              po, A.flags))
+    return out
+
+
+def mex_stokes_dlp_real(psrc, ptar, f, n, xi, nside_x, nside_y, Lx, Ly, ctx: Context | None = None):
+    ctx = ctx or default_context()
+    A = _Args()
+    ps, ns = A.arr(psrc, 2)
+    pt, nt = A.arr(ptar, 2)
+    pf, nf = A.arr(f, 2)
+    pn, nn = A.arr(n, 2)
+    if nf != ns:
+        raise ValueError("psrc and f must be the same size.")
+    if nn != ns:
+        raise ValueError("psrc and n must be the same size.")
+    out, po = A.out((nt, 2))
+    _check(lib().fte_dlp_real(ctx.h, ps, ns, pt, nt, pf, pn, float(xi), int(nside_x), int(nside_y), float(Lx),
+                              float(Ly), po, A.flags))
+    return out
+
+
+def mex_stokes_slp_kspace(psrc, ptar, xi, eta, f, Mx, My, Lx, Ly, w, P, ctx: Context | None = None):
+    ctx = ctx or default_context()
+    A = _Args()
+    ps, ns = A.arr(psrc, 2)
+    pt, nt = A.arr(ptar, 2)
+    pf, nf = A.arr(f, 2)
+    if nf != ns:
+        raise ValueError("psrc and f must be the same size.")
+    out, po = A.out((nt, 2))
+    _check(lib().fte_slp_kspace(ctx.h, ps, ns, pt, nt, float(xi), float(eta), pf, int(Mx), int(My), float(Lx),
+                                float(Ly), float(w), int(P), po, A.flags))
+    return out
+
+
+def mex_stokes_dlp_kspace(psrc, ptar, xi, eta, f, n, Mx, My, Lx, Ly, w, P, ctx: Context | None = None):
+    ctx = ctx or default_context()
+    A = _Args()
+    ps, ns = A.arr(psrc, 2)
+    pt, nt = A.arr(ptar, 2)
+    pf, nf = A.arr(f, 2)
+    pn, nn = A.arr(n, 2)
+    if nf != ns:
+        raise ValueError("psrc and f must be the same size.")
+    if nn != ns:
+        raise ValueError("psrc and n must be the same size.")
+    out, po = A.out((nt, 2))
+    _check(lib().fte_dlp_kspace(ctx.h, ps, ns, pt, nt, float(xi), float(eta), pf, pn, int(Mx), int(My), float(Lx),
+                                float(Ly), float(w), int(P), po, A.flags))
+    return out
+
+
+# ---- driver-shaped entries -----------------------------------------------------
+
+def _options(P=24, Nb=None, tol=1e-16, xi=None, Mx=None, My=None, nside_x=None, nside_y=None, weights_ptr=None,
+             form=FORM_PLAIN) -> Options:
+    o = Options()
+    o.P = int(P or 0)
+    o.Nb = float(Nb) if Nb else 0.0
+    o.tol = float(tol) if tol else 0.0
+    o.xi = float(xi) if xi else 0.0
+    o.Mx = int(Mx or 0)
+    o.My = int(My or 0)
+    o.nside_x = int(nside_x or 0)
+    o.nside_y = int(nside_y or 0)
+    o.weights = weights_ptr
+    o.form = int(form)
+    return o
+
+
+def _print_verbose(kind: str, ns: int, nt: int, info: Info):
+    p = info.params
+    print("*********************************************************")
+    print(f"SPECTRAL EWALD FOR THE STOKES {kind} POTENTIAL (GB300)\n")
+    print(f"NUMBER OF SOURCES: {ns}\nNUMBER OF TARGETS: {nt}\nTOLERANCE: {p.tol:.3e}\nP: {p.P}\n"
+          f"Points per box: {p.Nb:g}")
+    print(f"\nPARAMETER INFORMATION:\n\txi: {p.xi:.3f}\n\trc: {p.rc:.3f}\n\tkinf: {p.kinf}\n\tMx: {p.Mx}\n"
+          f"\tMy: {p.My}\n\tw: {p.w:.3f}\n\teta: {p.eta:.3f}")
+    print(f"TIME: total {info.ms_total:.3f} ms (near {info.ms_near:.3f}, spread {info.ms_spread:.3f}, "
+          f"fft+filter {info.ms_fft:.3f}, gather {info.ms_gather:.3f})")
+    print("*********************************************************\n")
+
+
+def StokesSLP_ewald_2p(xsrc, ysrc, xtar, ytar, f1, f2, Lx, Ly, P=24, Nb=None, tol=1e-16, verbose=0,
+                       weights=None, xi=None, Mx=None, My=None, nside_x=None, nside_y=None, form=FORM_PLAIN,
+                       ctx: Context | None = None, return_info: bool = False):
+    """Spectral Ewald evaluation of the doubly-periodic Stokeslet.
+
+    Returns (u1, u2, ur, uk, xi) like the MATLAB driver; ur and uk are (Ntar, 2).
+    """
+    ctx = ctx or default_context()
+    A = _Args()
+    pxs, ns = A.arr(xsrc, 1)
+    pys, _ = A.arr(ysrc, 1)
+    pxt, nt = A.arr(xtar, 1)
+    pyt, _ = A.arr(ytar, 1)
+    pf1, _ = A.arr(f1, 1)
+    pf2, _ = A.arr(f2, 1)
+    pw, _ = A.arr(weights, 1)
+    u1, pu1 = A.out((nt,))
+    u2, pu2 = A.out((nt,))
+    ur, pur = A.out((nt, 2))
+    uk, puk = A.out((nt, 2))
+    opt = _options(P, Nb, tol, xi, Mx, My, nside_x, nside_y, pw, form)
+    info = Info()
+    if verbose:
+        ctx.set_timing(True)
+    _check(lib().fte_stokes_slp_ewald_2p(ctx.h, pxs, pys, ns, pxt, pyt, nt, pf1, pf2, float(Lx), float(Ly),
+                                         C.byref(opt), pu1, pu2, pur, puk, C.byref(info), A.flags))
+    if verbose:
+        _print_verbose("SINGLE-LAYER", ns, nt, info)
+    out = (u1, u2, ur, uk, info.params.xi)
+    return (out, info) if return_info else out
+
+
+def StokesDLP_ewald_2p(xsrc, ysrc, xtar, ytar, n1, n2, f1, f2, Lx, Ly, P=24, Nb=None, tol=1e-16, verbose=0,
+                       weights=None, xi=None, Mx=None, My=None, nside_x=None, nside_y=None, form=FORM_PLAIN,
+                       ctx: Context | None = None, return_info: bool = False):
+    """Spectral Ewald evaluation of the doubly-periodic stresslet (double layer).
+
+    Returns (u1, u2, ur, uk, xi); uk includes the k = 0 mode like the MATLAB driver.
+    """
+    ctx = ctx or default_context()
+    A = _Args()
+    pxs, ns = A.arr(xsrc, 1)
+    pys, _ = A.arr(ysrc, 1)
+    pxt, nt = A.arr(xtar, 1)
+    pyt, _ = A.arr(ytar, 1)
+    pn1, _ = A.arr(n1, 1)
+    pn2, _ = A.arr(n2, 1)
+    pf1, _ = A.arr(f1, 1)
+    pf2, _ = A.arr(f2, 1)
+    pw, _ = A.arr(weights, 1)
+    u1, pu1 = A.out((nt,))
+    u2, pu2 = A.out((nt,))
+    ur, pur = A.out((nt, 2))
+    uk, puk = A.out((nt, 2))
+    opt = _options(P, Nb, tol, xi, Mx, My, nside_x, nside_y, pw, form)
+    info = Info()
+    if verbose:
+        ctx.set_timing(True)
+    _check(lib().fte_stokes_dlp_ewald_2p(ctx.h, pxs, pys, ns, pxt, pyt, nt, pn1, pn2, pf1, pf2, float(Lx),
+                                         float(Ly), C.byref(opt), pu1, pu2, pur, puk, C.byref(info), A.flags))
+    if verbose:
+        _print_verbose("DOUBLE-LAYER", ns, nt, info)
+    out = (u1, u2, ur, uk, info.params.xi)
+    return (out, info) if return_info else out
+
+
+def choose_params(kind, f1, f2, ntar, Lx, Ly, P=24, Nb=None, tol=1e-16, **kw) -> Params:
+    """The drivers' analytic parameter choice (host only, no GPU needed)."""
+    f1 = np.ascontiguousarray(f1, dtype=np.float64)
+    f2 = np.ascontiguousarray(f2, dtype=np.float64)
+    opt = _options(P, Nb, tol, **kw)
+    prm = Params()
+    _check(lib().fte_choose_params(int(kind), len(f1), int(ntar), f1.ctypes.data, f2.ctypes.data, float(Lx),
+                                   float(Ly), C.byref(opt), C.byref(prm)))
+    return prm

@@ -1,0 +1,954 @@
+// api.cu -- C ABI, context, workspace, FFT plans, parameter selection and the
+// driver-level orchestration of the GB300 spectral Ewald library.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <complex>
+#include <vector>
+
+#include "fte_internal.cuh"
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+static thread_local char g_err[1024] = "";
+
+void fte_set_error(const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+}
+
+extern "C" const char* fte_last_error(void) { return g_err; }
+extern "C" int fte_version(void) { return FTE_VERSION; }
+
+// ---------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------
+extern "C" int fte_create(fte_context** out, int device) {
+    if (!out) {
+        fte_set_error("fte_create: null output pointer");
+        return FTE_ERR_INVALID;
+    }
+    *out = nullptr;
+    int ndev = 0;
+    FTE_CUDA_TRY(cudaGetDeviceCount(&ndev));
+    if (device < 0 || device >= ndev) {
+        fte_set_error("fte_create: device %d not present (%d devices)", device, ndev);
+        return FTE_ERR_INVALID;
+    }
+    FTE_CUDA_TRY(cudaSetDevice(device));
+    fte_context* c = new (std::nothrow) fte_context();
+    if (!c) {
+        fte_set_error("fte_create: out of host memory");
+        return FTE_ERR_ALLOC;
+    }
+    c->device = device;
+    cudaDeviceProp prop;
+    FTE_CUDA_TRY(cudaGetDeviceProperties(&prop, device));
+    c->max_smem_optin = (int)prop.sharedMemPerBlockOptin;
+    c->num_sms = prop.multiProcessorCount;
+    FTE_CUDA_TRY(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking));
+    c->stream = c->own_stream;
+    for (int i = 0; i < 8; i++) FTE_CUDA_TRY(cudaEventCreate(&c->ev[i]));
+    FTE_CUDA_TRY(cudaMallocHost(&c->host_scalars, 64 * sizeof(double)));
+    *out = c;
+    return FTE_OK;
+}
+
+static void plan_free(FftPlan* p) {
+    if (!p) return;
+    cudaFree(p->tw);
+    cudaFree(p->chirp);
+    cudaFree(p->bhat);
+    cudaFree(p->tw32);
+    cudaFree(p->chirp32);
+    cudaFree(p->bhat32);
+    delete p;
+}
+
+extern "C" int fte_destroy(fte_context* c) {
+    if (!c) return FTE_OK;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (auto& kv : c->plans) plan_free(kv.second);
+    if (c->ws) cudaFree(c->ws);
+    if (c->ws2) cudaFree(c->ws2);
+    if (c->host_scalars) cudaFreeHost(c->host_scalars);
+    for (int i = 0; i < 8; i++)
+        if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+    if (c->own_stream) cudaStreamDestroy(c->own_stream);
+    delete c;
+    return FTE_OK;
+}
+
+extern "C" int fte_set_stream(fte_context* c, void* stream) {
+    if (!c) {
+        fte_set_error("fte_set_stream: null context");
+        return FTE_ERR_INVALID;
+    }
+    c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+    return FTE_OK;
+}
+
+extern "C" int fte_set_timing(fte_context* c, int enable) {
+    if (!c) {
+        fte_set_error("fte_set_timing: null context");
+        return FTE_ERR_INVALID;
+    }
+    c->timing = enable ? 1 : 0;
+    return FTE_OK;
+}
+
+extern "C" long long fte_kernel_count(const fte_context* c) { return c ? c->kernels : 0; }
+
+int fte_ws_reserve(fte_context* c, size_t bytes) {
+    if (bytes <= c->ws_size) return FTE_OK;
+    if (c->ws) {
+        FTE_CUDA_TRY(cudaStreamSynchronize(c->stream));
+        cudaFree(c->ws);
+        c->ws = nullptr;
+        c->ws_size = 0;
+    }
+    size_t want = bytes + bytes / 8 + (1 << 20);
+    cudaError_t e = cudaMalloc(&c->ws, want);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        fte_set_error("device workspace of %zu bytes could not be allocated: %s", want, cudaGetErrorString(e));
+        return FTE_ERR_ALLOC;
+    }
+    c->ws_size = want;
+    return FTE_OK;
+}
+
+int fte_ws2_reserve(fte_context* c, size_t bytes) {
+    if (bytes <= c->ws2_size) return FTE_OK;
+    if (c->ws2) {
+        FTE_CUDA_TRY(cudaStreamSynchronize(c->stream));
+        cudaFree(c->ws2);
+        c->ws2 = nullptr;
+        c->ws2_size = 0;
+    }
+    size_t want = bytes + bytes / 8 + (1 << 20);
+    cudaError_t e = cudaMalloc(&c->ws2, want);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        fte_set_error("device workspace of %zu bytes could not be allocated: %s", want, cudaGetErrorString(e));
+        return FTE_ERR_ALLOC;
+    }
+    c->ws2_size = want;
+    return FTE_OK;
+}
+
+int fte_record(fte_context* c, int slot) {
+    if (!c->timing) return FTE_OK;
+    FTE_CUDA_TRY(cudaEventRecord(c->ev[slot], c->stream));
+    return FTE_OK;
+}
+
+double fte_elapsed(fte_context* c, int a, int b) {
+    if (!c->timing) return 0.0;
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, c->ev[a], c->ev[b]) != cudaSuccess) {
+        cudaGetLastError();
+        return 0.0;
+    }
+    return ms;
+}
+
+// ---------------------------------------------------------------------------
+// FFT plans
+// ---------------------------------------------------------------------------
+static bool smooth7(int n, std::vector<int>* rad) {
+    int v = n;
+    int c8 = 0, c2 = 0, c3 = 0, c5 = 0, c7 = 0;
+    while (v % 2 == 0) {
+        v /= 2;
+        c2++;
+    }
+    while (v % 3 == 0) {
+        v /= 3;
+        c3++;
+    }
+    while (v % 5 == 0) {
+        v /= 5;
+        c5++;
+    }
+    while (v % 7 == 0) {
+        v /= 7;
+        c7++;
+    }
+    if (v != 1) return false;
+    if (rad) {
+        rad->clear();
+        c8 = c2 / 3;
+        c2 -= 3 * c8;
+        for (int i = 0; i < c8; i++) rad->push_back(8);
+        if (c2 == 2) rad->push_back(4);
+        if (c2 == 1) rad->push_back(2);
+        for (int i = 0; i < c3; i++) rad->push_back(3);
+        for (int i = 0; i < c5; i++) rad->push_back(5);
+        for (int i = 0; i < c7; i++) rad->push_back(7);
+    }
+    return true;
+}
+
+// exp(-2 pi i num/den) with the numerator reduced first
+static std::complex<double> unit_root(long long num, long long den) {
+    num %= den;
+    if (num < 0) num += den;
+    double ang;
+    if (2 * num <= den)
+        ang = -2.0 * FTE_PI * (double)num / (double)den;
+    else
+        ang = 2.0 * FTE_PI * (double)(den - num) / (double)den;
+    return {std::cos(ang), std::sin(ang)};
+}
+
+// host recursive mixed-radix DFT (for the Bluestein kernel only)
+static void host_dft(std::vector<std::complex<double>>& a) {
+    size_t n = a.size();
+    if (n <= 1) return;
+    size_t p = 0;
+    for (size_t q : {2, 3, 5, 7})
+        if (n % q == 0) {
+            p = q;
+            break;
+        }
+    if (p == 0) {
+        std::vector<std::complex<double>> o(n);
+        for (size_t k = 0; k < n; k++) {
+            std::complex<double> s = 0;
+            for (size_t j = 0; j < n; j++) s += a[j] * unit_root((long long)(j * k % n), (long long)n);
+            o[k] = s;
+        }
+        a = o;
+        return;
+    }
+    size_t m = n / p;
+    std::vector<std::vector<std::complex<double>>> sub(p, std::vector<std::complex<double>>(m));
+    for (size_t q = 0; q < p; q++)
+        for (size_t j = 0; j < m; j++) sub[q][j] = a[j * p + q];
+    for (size_t q = 0; q < p; q++) host_dft(sub[q]);
+    for (size_t k = 0; k < n; k++) {
+        std::complex<double> s = 0;
+        for (size_t q = 0; q < p; q++) s += sub[q][k % m] * unit_root((long long)(q * k % n), (long long)n);
+        a[k] = s;
+    }
+}
+
+template <typename T>
+static int upload(T** dst, const std::vector<T>& v) {
+    FTE_CUDA_TRY(cudaMalloc(dst, v.size() * sizeof(T)));
+    FTE_CUDA_TRY(cudaMemcpy(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return FTE_OK;
+}
+
+int fte_get_plan(fte_context* c, int n, FftDev* out) {
+    auto it = c->plans.find(n);
+    FftPlan* p = nullptr;
+    if (it != c->plans.end()) {
+        p = it->second;
+    } else {
+        p = new FftPlan();
+        p->n = n;
+        std::vector<int> rad;
+        if (smooth7(n, &rad)) {
+            p->m = n;
+        } else {
+            p->bluestein = 1;
+            int m = 2 * n - 1;
+            while (!smooth7(m, nullptr)) m++;
+            smooth7(m, &rad);
+            p->m = m;
+        }
+        if (rad.size() > 24) {
+            delete p;
+            fte_set_error("FFT length %d has too many factors", n);
+            return FTE_ERR_UNSUPPORTED;
+        }
+        p->nrad = (int)rad.size();
+        for (size_t i = 0; i < rad.size(); i++) p->rad[i] = rad[i];
+        const int m = p->m;
+        std::vector<double2> tw(m);
+        std::vector<float2> tw32(m);
+        for (int t = 0; t < m; t++) {
+            auto z = unit_root(t, m);
+            tw[t] = make_double2(z.real(), z.imag());
+            tw32[t] = make_float2((float)z.real(), (float)z.imag());
+        }
+        int st = upload(&p->tw, tw);
+        if (!st) st = upload(&p->tw32, tw32);
+        if (!st && p->bluestein) {
+            std::vector<double2> ch(n);
+            std::vector<float2> ch32(n);
+            std::vector<std::complex<double>> b(m, 0.0);
+            for (int k = 0; k < n; k++) {
+                long long k2 = ((long long)k * k) % (2LL * n);
+                auto z = unit_root(k2, 2LL * n);  // exp(-i pi k^2 / n)
+                ch[k] = make_double2(z.real(), z.imag());
+                ch32[k] = make_float2((float)z.real(), (float)z.imag());
+                b[k] = std::conj(z);
+                if (k > 0) b[m - k] = std::conj(z);
+            }
+            host_dft(b);
+            std::vector<double2> bh(m);
+            std::vector<float2> bh32(m);
+            for (int k = 0; k < m; k++) {
+                auto z = b[k] / (double)m;
+                bh[k] = make_double2(z.real(), z.imag());
+                bh32[k] = make_float2((float)z.real(), (float)z.imag());
+            }
+            st = upload(&p->chirp, ch);
+            if (!st) st = upload(&p->chirp32, ch32);
+            if (!st) st = upload(&p->bhat, bh);
+            if (!st) st = upload(&p->bhat32, bh32);
+        }
+        if (st) {
+            plan_free(p);
+            return st;
+        }
+        c->plans[n] = p;
+    }
+    out->n = p->n;
+    out->m = p->m;
+    out->nrad = p->nrad;
+    out->bluestein = p->bluestein;
+    for (int i = 0; i < 24; i++) out->rad[i] = p->rad[i];
+    out->tw = p->tw;
+    out->chirp = p->chirp;
+    out->bhat = p->bhat;
+    out->tw32 = p->tw32;
+    out->chirp32 = p->chirp32;
+    out->bhat32 = p->bhat32;
+    return FTE_OK;
+}
+
+// ---------------------------------------------------------------------------
+// parameter selection: the MATLAB drivers' analytic choice
+// (StokesSLP_ewald_2p.m:27-35,85-104 and find_kinfb :147-173, find_xi :178-202;
+//  StokesDLP_ewald_2p.m:27-38,307-327 and find_kinfb :373-399, find_xi :404-427).
+// Estimates of Palsson & Tornberg 2019; Newton iterations with the step in
+// the negative direction limited to 0.9 of the iterate, at most 101 steps.
+// find_kinfb is called with Lx in place of Ly, as the drivers do.
+// ---------------------------------------------------------------------------
+namespace {
+
+// MATLAB rat with tolerance 1e-6 |x| (nearest-integer continued fraction)
+void matlab_rat(double x, int* num, int* den) {
+    double tol = 1e-6 * std::fabs(x);
+    double lastn = 1, lastd = 0, n = std::round(x), d = 1, frac = x - n;
+    for (int guard = 0; std::fabs(x - n / d) >= tol && guard < 64; guard++) {
+        double flip = 1 / frac, step = std::round(flip);
+        frac = flip - step;
+        double sn = n;
+        n = n * step + lastn;
+        lastn = sn;
+        double sd = d;
+        d = d * step + lastd;
+        lastd = sd;
+    }
+    *num = (int)(n * (d > 0 ? 1 : (d < 0 ? -1 : 0)));
+    *den = (int)std::fabs(d);
+}
+
+template <typename F, typename FP>
+double newton(double x, double tol, F f, FP fp) {
+    for (int it = 0;; it++) {
+        double fx = f(x);
+        if (!(std::fabs(fx) > tol)) break;
+        if (it > 100) break;
+        double d = fx / fp(x);
+        if (0.9 * x < d) d = 0.9 * x;
+        x -= d;
+    }
+    return x;
+}
+
+int matlab_length(int64_t n) { return n == 0 ? 0 : (n > 2 ? (int)n : 2); }
+
+}  // namespace
+
+static int choose_params_q(int kind, int64_t nsrc, int64_t ntar, double Q, double Lx, double Ly,
+                           const fte_options* opt, fte_params* o) {
+    std::memset(o, 0, sizeof(*o));
+    int P = (opt && opt->P > 0) ? opt->P : 24;
+    double tol = (opt && opt->tol > 0) ? opt->tol : 1e-16;
+    double npts = (double)nsrc + (double)ntar;
+    double Nb = (opt && opt->Nb > 0) ? opt->Nb : std::fmin(P * std::round(std::log2(npts)), npts / 4);
+    int A, B;
+    matlab_rat(Lx / Ly, &A, &B);
+    if (A <= 0 || B <= 0) {
+        fte_set_error("box aspect ratio Lx/Ly = %g has no usable rational approximation", Lx / Ly);
+        return FTE_ERR_INVALID;
+    }
+    if (kind == FTE_KIND_DLP) npts = (double)matlab_length(nsrc) + (double)matlab_length(ntar);
+    int a = (int)std::ceil(std::sqrt(npts / (Nb * A * B)));
+    if (a < 1) a = 1;
+    const double m = 0.95 * std::sqrt(FTE_PI * P);
+    o->P = P;
+    o->Nb = Nb;
+    o->tol = tol;
+    o->Q = Q;
+    o->A = A;
+    o->B = B;
+    o->nside_x = (opt && opt->nside_x > 0) ? opt->nside_x : a * A;
+    o->nside_y = (opt && opt->nside_y > 0) ? opt->nside_y : a * B;
+    double rc = Lx / o->nside_x;
+    o->rc = rc;
+    double xi;
+    if (opt && opt->xi > 0) {
+        xi = opt->xi;
+    } else if (kind == FTE_KIND_SLP) {
+        xi = newton(
+            4 / rc, tol,
+            [&](double x) { return std::sqrt(Q * FTE_PI / (4 * Lx * Ly * x)) * std::exp(-x * x * rc * rc) - tol; },
+            [&](double x) {
+                return -std::sqrt(Q * FTE_PI / (4 * Lx * Ly)) * std::exp(-x * x * rc * rc) *
+                       (0.5 * std::pow(x, -1.5) + 2 * rc * rc * x * std::sqrt(1 / x));
+            });
+    } else {
+        xi = newton(
+            1 / rc, tol,
+            [&](double x) { return std::exp(-x * x * rc * rc) * x * rc * std::sqrt(2 * FTE_PI * Q / (Lx * Ly)) - tol; },
+            [&](double x) {
+                return (1 - 2 * x * x * rc * rc) * std::exp(-x * x * rc * rc) * std::sqrt(2 * FTE_PI * Q / (Lx * Ly)) * rc;
+            });
+    }
+    o->xi = xi;
+    const double L1 = Lx, L2 = Lx;  // find_kinfb(Q, Lx, Lx, xi, tol)
+    const double mx = L1 > L2 ? L1 : L2;
+    double k;
+    if (kind == FTE_KIND_SLP) {
+        k = newton(
+            std::round(5 * xi), tol,
+            [&](double k) {
+                return std::sqrt(4 * Q * FTE_PI * mx / (L1 * L1 * L1 * L2 * L2 * L2 * k)) * std::exp(-k * k / (4 * xi * xi)) - tol;
+            },
+            [&](double k) {
+                return -std::sqrt(4 * Q * FTE_PI * mx / (L1 * L1 * L1 * L2 * L2 * L2)) * std::exp(-k * k / (4 * xi * xi)) *
+                       (0.5 * std::pow(k, -1.5) + std::sqrt(1 / k) * 2 * k / (4 * xi * xi));
+            });
+    } else {
+        // left-to-right as in MATLAB: k*8*pi*Q*max(Lx,Ly)/Lx^3*Ly^3
+        k = newton(
+            std::round(5 * xi), tol,
+            [&](double k) {
+                return std::sqrt(k * 8 * FTE_PI * Q * mx / (L1 * L1 * L1) * (L2 * L2 * L2)) * std::exp(-k * k / (4 * xi * xi)) - tol;
+            },
+            [&](double k) {
+                return std::sqrt(8 * FTE_PI * Q * mx / (L1 * L1 * L1) * (L2 * L2 * L2)) * std::exp(-k * k / (4 * xi * xi)) *
+                       (0.5 * std::pow(k, -0.5) - 2 * std::pow(k, 1.5) / (4 * xi * xi));
+            });
+    }
+    int kinf = (int)std::round(Lx * k / (2 * FTE_PI));
+    o->kinf = kinf;
+    int M = 2 * kinf < 10000 ? 2 * kinf : 10000;
+    o->Mx = (opt && opt->Mx > 0) ? opt->Mx : A * M;
+    o->My = (opt && opt->My > 0) ? opt->My : B * M;
+    o->w = P * Lx / o->Mx / 2;
+    o->eta = (2 * xi * o->w / m) * (2 * xi * o->w / m);
+    return FTE_OK;
+}
+
+extern "C" int fte_choose_params(int kind, int64_t nsrc, int64_t ntar, const double* f1, const double* f2, double Lx,
+                                 double Ly, const fte_options* opt, fte_params* out) {
+    if (!out || (nsrc > 0 && (!f1 || !f2))) {
+        fte_set_error("fte_choose_params: null argument");
+        return FTE_ERR_INVALID;
+    }
+    if (!(Lx > 0) || !(Ly > 0) || !std::isfinite(Lx) || !std::isfinite(Ly)) {
+        fte_set_error("fte_choose_params: box lengths must be positive and finite");
+        return FTE_ERR_INVALID;
+    }
+    double Q = 0;
+    const double* w = opt ? opt->weights : nullptr;
+    for (int64_t j = 0; j < nsrc; j++) {
+        double a = f1[j] * (w ? w[j] : 1.0);
+        Q += a * a;
+    }
+    for (int64_t j = 0; j < nsrc; j++) {
+        double a = f2[j] * (w ? w[j] : 1.0);
+        Q += a * a;
+    }
+    return choose_params_q(kind, nsrc, ntar, Q + 1, Lx, Ly, opt, out);
+}
+
+// ---------------------------------------------------------------------------
+// small device kernels of the drivers
+// ---------------------------------------------------------------------------
+namespace {
+
+// MATLAB mod(a, L) - L/2 with mod's round-off compensation
+// (StokesSLP_ewald_2p.m:75-78): exactly 0 when a/L is an integer to within eps.
+__device__ __forceinline__ double wrap_coord(double v, double L) {
+    double a = __dadd_rn(v, __ddiv_rn(L, 2.0));
+    double q = __ddiv_rn(a, L);
+    double rq = round(q);
+    double r;
+    if (fabs(__dsub_rn(q, rq)) <= 2.220446049250313e-16 * fabs(q))
+        r = 0.0;
+    else
+        r = __dsub_rn(a, __dmul_rn(floor(q), L));
+    return __dsub_rn(r, __ddiv_rn(L, 2.0));
+}
+
+__global__ void k_wrap_pack(const double* __restrict__ x, const double* __restrict__ y, int64_t n, double Lx,
+                            double Ly, double* __restrict__ p) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        p[2 * i] = wrap_coord(x[i], Lx);
+        p[2 * i + 1] = wrap_coord(y[i], Ly);
+    }
+}
+
+__global__ void k_pack(const double* __restrict__ a, const double* __restrict__ b, int64_t n, double* __restrict__ p) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        p[2 * i] = a[i];
+        p[2 * i + 1] = b[i];
+    }
+}
+
+// acc[0] += sum (w f1)^2 + (w f2)^2 ;  DLP also acc[1..2] += sum (f.n) (xs, ys)
+template <int KIND>
+__global__ void k_reduce(const double* __restrict__ p, const double* __restrict__ f, const double* __restrict__ nrm,
+                         const double* __restrict__ wts, int64_t n, double* __restrict__ acc) {
+    double q = 0, zx = 0, zy = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double w = wts ? wts[i] : 1.0;
+        double f1 = f[2 * i] * w, f2 = f[2 * i + 1] * w;
+        q += f1 * f1 + f2 * f2;
+        if (KIND == FTE_KIND_DLP) {
+            double fn = f1 * nrm[2 * i] + f2 * nrm[2 * i + 1];
+            zx += fn * p[2 * i];
+            zy += fn * p[2 * i + 1];
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        q += __shfl_down_sync(0xffffffffu, q, o);
+        zx += __shfl_down_sync(0xffffffffu, zx, o);
+        zy += __shfl_down_sync(0xffffffffu, zy, o);
+    }
+    __shared__ double sq[32], sx[32], sy[32];
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+        sq[warp] = q;
+        sx[warp] = zx;
+        sy[warp] = zy;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        int nw = blockDim.x >> 5;
+        q = lane < nw ? sq[lane] : 0;
+        zx = lane < nw ? sx[lane] : 0;
+        zy = lane < nw ? sy[lane] : 0;
+        for (int o = 16; o > 0; o >>= 1) {
+            q += __shfl_down_sync(0xffffffffu, q, o);
+            zx += __shfl_down_sync(0xffffffffu, zx, o);
+            zy += __shfl_down_sync(0xffffffffu, zy, o);
+        }
+        if (lane == 0) {
+            atomicAdd(&acc[0], q);
+            if (KIND == FTE_KIND_DLP) {
+                atomicAdd(&acc[1], zx);
+                atomicAdd(&acc[2], zy);
+            }
+        }
+    }
+}
+
+// u = ur + uk (+ zero mode); optional interleaved copies of ur and uk (with the zero mode in uk)
+__global__ void k_combine(const double2* __restrict__ ur, const double2* __restrict__ uk, int64_t n,
+                          const double* __restrict__ zero, double inv_area, double* __restrict__ u1,
+                          double* __restrict__ u2, double* __restrict__ ur_out, double* __restrict__ uk_out) {
+    double zx = zero ? zero[1] * inv_area : 0.0, zy = zero ? zero[2] * inv_area : 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double2 r = ur[i], k = uk[i];
+        k.x += zx;
+        k.y += zy;
+        u1[i] = r.x + k.x;
+        u2[i] = r.y + k.y;
+        if (ur_out) {
+            ur_out[2 * i] = r.x;
+            ur_out[2 * i + 1] = r.y;
+        }
+        if (uk_out) {
+            uk_out[2 * i] = k.x;
+            uk_out[2 * i + 1] = k.y;
+        }
+    }
+}
+
+int grid1d(fte_context* c, int64_t n, int threads = 256) {
+    int64_t b = (n + threads - 1) / threads;
+    int64_t mx = (int64_t)c->num_sms * 8;
+    if (b > mx) b = mx;
+    if (b < 1) b = 1;
+    return (int)b;
+}
+
+// ---- validation -------------------------------------------------------------
+int check_box(double Lx, double Ly) {
+    if (!(Lx > 0) || !(Ly > 0) || !std::isfinite(Lx) || !std::isfinite(Ly)) {
+        fte_set_error("box lengths must be positive and finite (Lx=%g, Ly=%g)", Lx, Ly);
+        return FTE_ERR_INVALID;
+    }
+    return FTE_OK;
+}
+
+int check_counts(int64_t nsrc, int64_t ntar) {
+    if (nsrc < 0 || ntar < 0 || nsrc > 2000000000LL || ntar > 2000000000LL) {
+        fte_set_error("point counts out of range (nsrc=%lld, ntar=%lld)", (long long)nsrc, (long long)ntar);
+        return FTE_ERR_INVALID;
+    }
+    return FTE_OK;
+}
+
+int check_real_params(double xi, int nsx, int nsy) {
+    if (!(xi > 0) || !std::isfinite(xi)) {
+        fte_set_error("xi must be positive and finite (xi=%g)", xi);
+        return FTE_ERR_INVALID;
+    }
+    if (nsx < 1 || nsy < 1 || (int64_t)nsx * nsy > 100000000LL) {
+        fte_set_error("cell counts out of range (nside_x=%d, nside_y=%d)", nsx, nsy);
+        return FTE_ERR_INVALID;
+    }
+    return FTE_OK;
+}
+
+int check_kspace_params(double xi, double eta, int Mx, int My, double Lx, double Ly, double w, int P) {
+    if (!(xi > 0) || !std::isfinite(xi) || !(eta > 0) || !std::isfinite(eta) || !std::isfinite(w)) {
+        fte_set_error("xi, eta must be positive and w finite (xi=%g, eta=%g, w=%g)", xi, eta, w);
+        return FTE_ERR_INVALID;
+    }
+    if (P < 2 || P % 2 != 0 || P > 64) {
+        fte_set_error("window support P must be even and in [2, 64] (P=%d)", P);
+        return FTE_ERR_INVALID;
+    }
+    if (Mx < 2 || My < 2 || Mx % 2 || My % 2) {
+        fte_set_error("grid sizes must be even and >= 2 (Mx=%d, My=%d)", Mx, My);
+        return FTE_ERR_INVALID;
+    }
+    if (P + 1 > Mx || P + 1 > My) {
+        fte_set_error("window support P+1=%d exceeds the grid (Mx=%d, My=%d)", P + 1, Mx, My);
+        return FTE_ERR_INVALID;
+    }
+    double hx = Lx / Mx, hy = Ly / My;
+    if (std::fabs(hx - hy) > 1e-12 * std::fmax(hx, hy)) {
+        fte_set_error("grid spacing must be equal in x and y (Lx/Mx=%.17g, Ly/My=%.17g)", hx, hy);
+        return FTE_ERR_INVALID;
+    }
+    return FTE_OK;
+}
+
+// Stage host arrays in device workspace when the call uses host pointers.
+struct Stager {
+    fte_context* c;
+    WsCarver* wc;
+    bool host;
+    int put(const double* src, size_t count, const double** dst) {
+        if (!host || !src) {
+            *dst = src;
+            return FTE_OK;
+        }
+        double* d = wc->take<double>(count);
+        if (count) FTE_CUDA_TRY(cudaMemcpyAsync(d, src, count * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+        *dst = d;
+        return FTE_OK;
+    }
+};
+
+int finish_output(fte_context* c, bool host, double* user, const double* dev, size_t count) {
+    if (host && user && count)
+        FTE_CUDA_TRY(cudaMemcpyAsync(user, dev, count * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    return FTE_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// gateway-level entries
+// ---------------------------------------------------------------------------
+static int real_entry(fte_context* c, int kind, const double* psrc, int64_t nsrc, const double* ptar, int64_t ntar,
+                      const double* f, const double* nrm, double xi, int nsx, int nsy, double Lx, double Ly,
+                      double* ur, unsigned flags) {
+    if (!c) {
+        fte_set_error("null context");
+        return FTE_ERR_INVALID;
+    }
+    FTE_TRY(check_counts(nsrc, ntar));
+    FTE_TRY(check_box(Lx, Ly));
+    FTE_TRY(check_real_params(xi, nsx, nsy));
+    if ((nsrc > 0 && (!psrc || !f || (kind == FTE_KIND_DLP && !nrm))) || (ntar > 0 && (!ptar || !ur))) {
+        fte_set_error("null array argument");
+        return FTE_ERR_INVALID;
+    }
+    FTE_CUDA_TRY(cudaSetDevice(c->device));
+    const bool host = !(flags & FTE_DEVICE_POINTERS);
+    int nb = nsx * nsy;
+    size_t need = fte_cells_ws(nsrc, ntar, nb) + ws_bytes(2 * (ntar + 1), sizeof(double));
+    if (host) need += ws_bytes(2 * (nsrc + 1), 8) * 3 + ws_bytes(2 * (ntar + 1), 8);
+    FTE_TRY(fte_ws_reserve(c, need));
+    WsCarver wc{c->ws, 0, c->ws_size};
+    Stager st{c, &wc, host};
+    const double *dps, *dpt, *df, *dn;
+    FTE_TRY(st.put(psrc, 2 * (size_t)nsrc, &dps));
+    FTE_TRY(st.put(ptar, 2 * (size_t)ntar, &dpt));
+    FTE_TRY(st.put(f, 2 * (size_t)nsrc, &df));
+    FTE_TRY(st.put(kind == FTE_KIND_DLP ? nrm : nullptr, 2 * (size_t)nsrc, &dn));
+    double2* dur = host ? wc.take<double2>(ntar + 1) : reinterpret_cast<double2*>(ur);
+    FTE_WS_CHECK(wc);
+    if (ntar > 0) {
+        CellList cl;
+        FTE_TRY(fte_cells_build(c, wc, kind, dps, nsrc, dpt, ntar, df, dn, nullptr, nsx, nsy, Lx, Ly, &cl));
+        FTE_TRY(fte_near_launch(c, kind, cl, xi, Lx, Ly, dur));
+        FTE_TRY(finish_output(c, host, ur, reinterpret_cast<const double*>(dur), 2 * (size_t)ntar));
+    }
+    FTE_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return FTE_OK;
+}
+
+extern "C" int fte_slp_real(fte_context* c, const double* psrc, int64_t nsrc, const double* ptar, int64_t ntar,
+                            const double* f, double xi, int nside_x, int nside_y, double Lx, double Ly, double* ur,
+                            unsigned flags) {
+    return real_entry(c, FTE_KIND_SLP, psrc, nsrc, ptar, ntar, f, nullptr, xi, nside_x, nside_y, Lx, Ly, ur, flags);
+}
+
+extern "C" int fte_dlp_real(fte_context* c, const double* psrc, int64_t nsrc, const double* ptar, int64_t ntar,
+                            const double* f, const double* n, double xi, int nside_x, int nside_y, double Lx,
+                            double Ly, double* ur, unsigned flags) {
+    return real_entry(c, FTE_KIND_DLP, psrc, nsrc, ptar, ntar, f, n, xi, nside_x, nside_y, Lx, Ly, ur, flags);
+}
+
+static int kspace_entry(fte_context* c, int kind, const double* psrc, int64_t nsrc, const double* ptar, int64_t ntar,
+                        double xi, double eta, const double* f, const double* nrm, int Mx, int My, double Lx,
+                        double Ly, double w, int P, double* uk, unsigned flags) {
+    if (!c) {
+        fte_set_error("null context");
+        return FTE_ERR_INVALID;
+    }
+    FTE_TRY(check_counts(nsrc, ntar));
+    FTE_TRY(check_box(Lx, Ly));
+    FTE_TRY(check_kspace_params(xi, eta, Mx, My, Lx, Ly, w, P));
+    if ((nsrc > 0 && (!psrc || !f || (kind == FTE_KIND_DLP && !nrm))) || (ntar > 0 && (!ptar || !uk))) {
+        fte_set_error("null array argument");
+        return FTE_ERR_INVALID;
+    }
+    FTE_CUDA_TRY(cudaSetDevice(c->device));
+    const bool host = !(flags & FTE_DEVICE_POINTERS);
+    size_t need = fte_kspace_ws(kind, FTE_FORM_PLAIN, Mx, My) + ws_bytes(2 * (ntar + 1), 8);
+    if (host) need += ws_bytes(2 * (nsrc + 1), 8) * 3 + ws_bytes(2 * (ntar + 1), 8);
+    FTE_TRY(fte_ws_reserve(c, need));
+    WsCarver wc{c->ws, 0, c->ws_size};
+    Stager st{c, &wc, host};
+    const double *dps, *dpt, *df, *dn;
+    FTE_TRY(st.put(psrc, 2 * (size_t)nsrc, &dps));
+    FTE_TRY(st.put(ptar, 2 * (size_t)ntar, &dpt));
+    FTE_TRY(st.put(f, 2 * (size_t)nsrc, &df));
+    FTE_TRY(st.put(kind == FTE_KIND_DLP ? nrm : nullptr, 2 * (size_t)nsrc, &dn));
+    double2* duk = host ? wc.take<double2>(ntar + 1) : reinterpret_cast<double2*>(uk);
+    FTE_WS_CHECK(wc);
+    KspaceArgs a;
+    a.kind = kind;
+    a.form = FTE_FORM_PLAIN;
+    a.nsrc = nsrc;
+    a.ntar = ntar;
+    a.psrc = dps;
+    a.ptar = dpt;
+    a.f = df;
+    a.nrm = dn;
+    a.wts = nullptr;
+    a.xi = xi;
+    a.eta = eta;
+    a.w = w;
+    a.Lx = Lx;
+    a.Ly = Ly;
+    a.Mx = Mx;
+    a.My = My;
+    a.P = P;
+    a.uk = duk;
+    FTE_TRY(fte_kspace_run(c, wc, a, nullptr));
+    FTE_TRY(finish_output(c, host, uk, reinterpret_cast<const double*>(duk), 2 * (size_t)ntar));
+    FTE_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return FTE_OK;
+}
+
+extern "C" int fte_slp_kspace(fte_context* c, const double* psrc, int64_t nsrc, const double* ptar, int64_t ntar,
+                              double xi, double eta, const double* f, int Mx, int My, double Lx, double Ly, double w,
+                              int P, double* uk, unsigned flags) {
+    return kspace_entry(c, FTE_KIND_SLP, psrc, nsrc, ptar, ntar, xi, eta, f, nullptr, Mx, My, Lx, Ly, w, P, uk, flags);
+}
+
+extern "C" int fte_dlp_kspace(fte_context* c, const double* psrc, int64_t nsrc, const double* ptar, int64_t ntar,
+                              double xi, double eta, const double* f, const double* n, int Mx, int My, double Lx,
+                              double Ly, double w, int P, double* uk, unsigned flags) {
+    return kspace_entry(c, FTE_KIND_DLP, psrc, nsrc, ptar, ntar, xi, eta, f, n, Mx, My, Lx, Ly, w, P, uk, flags);
+}
+
+// ---------------------------------------------------------------------------
+// driver-level entries
+// ---------------------------------------------------------------------------
+static int ewald_entry(fte_context* c, int kind, const double* xsrc, const double* ysrc, int64_t nsrc,
+                       const double* xtar, const double* ytar, int64_t ntar, const double* n1, const double* n2,
+                       const double* f1, const double* f2, double Lx, double Ly, const fte_options* opt, double* u1,
+                       double* u2, double* ur, double* uk, fte_info* info, unsigned flags) {
+    if (!c) {
+        fte_set_error("null context");
+        return FTE_ERR_INVALID;
+    }
+    FTE_TRY(check_counts(nsrc, ntar));
+    FTE_TRY(check_box(Lx, Ly));
+    if ((nsrc > 0 && (!xsrc || !ysrc || !f1 || !f2 || (kind == FTE_KIND_DLP && (!n1 || !n2)))) ||
+        (ntar > 0 && (!xtar || !ytar || !u1 || !u2))) {
+        fte_set_error("null array argument");
+        return FTE_ERR_INVALID;
+    }
+    fte_options defaults;
+    std::memset(&defaults, 0, sizeof(defaults));
+    if (!opt) opt = &defaults;
+    if (opt->P != 0 && (opt->P < 2 || opt->P % 2 || opt->P > 64)) {
+        fte_set_error("window support P must be even and in [2, 64] (P=%d)", opt->P);
+        return FTE_ERR_INVALID;
+    }
+    if (opt->form != FTE_FORM_PLAIN) {
+        fte_set_error("form %d is not available in this build", opt->form);
+        return FTE_ERR_UNSUPPORTED;
+    }
+    FTE_CUDA_TRY(cudaSetDevice(c->device));
+    const bool host = !(flags & FTE_DEVICE_POINTERS);
+    long long k0 = c->kernels;
+    FTE_TRY(fte_record(c, 0));
+
+    // workspace (first pass: everything except the grids, which need the parameters)
+    size_t base = 0;
+    base += ws_bytes(2 * (nsrc + 1), 8) * 3 + ws_bytes(2 * (ntar + 1), 8) * 3;  // packed inputs + ur/uk
+    if (host) base += ws_bytes(nsrc + 1, 8) * 7 + ws_bytes(ntar + 1, 8) * 8;
+    base += 4096;
+    FTE_TRY(fte_ws_reserve(c, base));
+    // host inputs are staged first so that Q can be reduced on the device
+    WsCarver wc{c->ws, 0, c->ws_size};
+    Stager st{c, &wc, host};
+    const double *dxs, *dys, *dxt, *dyt, *df1, *df2, *dn1 = nullptr, *dn2 = nullptr, *dw = nullptr;
+    FTE_TRY(st.put(xsrc, nsrc, &dxs));
+    FTE_TRY(st.put(ysrc, nsrc, &dys));
+    FTE_TRY(st.put(xtar, ntar, &dxt));
+    FTE_TRY(st.put(ytar, ntar, &dyt));
+    FTE_TRY(st.put(f1, nsrc, &df1));
+    FTE_TRY(st.put(f2, nsrc, &df2));
+    if (kind == FTE_KIND_DLP) {
+        FTE_TRY(st.put(n1, nsrc, &dn1));
+        FTE_TRY(st.put(n2, nsrc, &dn2));
+    }
+    FTE_TRY(st.put(opt->weights, nsrc, &dw));
+    double* ps = wc.take<double>(2 * (nsrc + 1));
+    double* pt = wc.take<double>(2 * (ntar + 1));
+    double* pf = wc.take<double>(2 * (nsrc + 1));
+    double* pn = kind == FTE_KIND_DLP ? wc.take<double>(2 * (nsrc + 1)) : nullptr;
+    double2* dur = wc.take<double2>(ntar + 1);
+    double2* duk = wc.take<double2>(ntar + 1);
+    double* acc = wc.take<double>(8);
+    FTE_WS_CHECK(wc);
+    if (nsrc > 0) {
+        FTE_LAUNCH(c, k_wrap_pack, grid1d(c, nsrc), 256, 0, dxs, dys, nsrc, Lx, Ly, ps);
+        FTE_LAUNCH(c, k_pack, grid1d(c, nsrc), 256, 0, df1, df2, nsrc, pf);
+        if (pn) FTE_LAUNCH(c, k_pack, grid1d(c, nsrc), 256, 0, dn1, dn2, nsrc, pn);
+    }
+    if (ntar > 0) FTE_LAUNCH(c, k_wrap_pack, grid1d(c, ntar), 256, 0, dxt, dyt, ntar, Lx, Ly, pt);
+    FTE_CUDA_TRY(cudaMemsetAsync(acc, 0, 8 * sizeof(double), c->stream));
+    if (nsrc > 0) {
+        if (kind == FTE_KIND_SLP)
+            FTE_LAUNCH(c, k_reduce<FTE_KIND_SLP>, grid1d(c, nsrc), 256, 0, (const double*)ps, (const double*)pf,
+                       (const double*)pn, dw, nsrc, acc);
+        else
+            FTE_LAUNCH(c, k_reduce<FTE_KIND_DLP>, grid1d(c, nsrc), 256, 0, (const double*)ps, (const double*)pf,
+                       (const double*)pn, dw, nsrc, acc);
+    }
+    FTE_CUDA_TRY(cudaMemcpyAsync(c->host_scalars, acc, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    FTE_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    double Q = c->host_scalars[0] + 1.0;
+    fte_params prm;
+    FTE_TRY(choose_params_q(kind, nsrc, ntar, Q, Lx, Ly, opt, &prm));
+    FTE_TRY(check_real_params(prm.xi, prm.nside_x, prm.nside_y));
+    FTE_TRY(check_kspace_params(prm.xi, prm.eta, prm.Mx, prm.My, Lx, Ly, prm.w, prm.P));
+    // second workspace: cell list, grids and outputs (the staged point data stays in the first)
+    size_t need = fte_cells_ws(nsrc, ntar, prm.nside_x * prm.nside_y) +
+                  fte_kspace_ws(kind, FTE_FORM_PLAIN, prm.Mx, prm.My) + ws_bytes(2 * (ntar + 1), 8) * 3 + 8192;
+    FTE_TRY(fte_ws2_reserve(c, need));
+    WsCarver wc2{c->ws2, 0, c->ws2_size};
+    FTE_TRY(fte_record(c, 1));
+    if (ntar > 0) {
+        CellList cl;
+        FTE_TRY(fte_cells_build(c, wc2, kind, ps, nsrc, pt, ntar, pf, pn, dw, prm.nside_x, prm.nside_y, Lx, Ly, &cl));
+        FTE_TRY(fte_record(c, 6));
+        FTE_TRY(fte_near_launch(c, kind, cl, prm.xi, Lx, Ly, dur));
+        FTE_TRY(fte_record(c, 7));
+        KspaceArgs a;
+        a.kind = kind;
+        a.form = opt->form;
+        a.nsrc = nsrc;
+        a.ntar = ntar;
+        a.psrc = ps;
+        a.ptar = pt;
+        a.f = pf;
+        a.nrm = pn;
+        a.wts = dw;
+        a.xi = prm.xi;
+        a.eta = prm.eta;
+        a.w = prm.w;
+        a.Lx = Lx;
+        a.Ly = Ly;
+        a.Mx = prm.Mx;
+        a.My = prm.My;
+        a.P = prm.P;
+        a.uk = duk;
+        FTE_TRY(fte_kspace_run(c, wc2, a, info));
+        double* ou1 = host ? wc2.take<double>(ntar + 1) : u1;
+        double* ou2 = host ? wc2.take<double>(ntar + 1) : u2;
+        double* our = (ur && host) ? wc2.take<double>(2 * (ntar + 1)) : ur;
+        double* ouk = (uk && host) ? wc2.take<double>(2 * (ntar + 1)) : uk;
+        FTE_WS_CHECK(wc2);
+        FTE_LAUNCH(c, k_combine, grid1d(c, ntar), 256, 0, (const double2*)dur, (const double2*)duk, ntar,
+                   kind == FTE_KIND_DLP ? (const double*)acc : nullptr, 1.0 / (Lx * Ly), ou1, ou2, our, ouk);
+        FTE_TRY(fte_record(c, 5));
+        if (host) {
+            FTE_TRY(finish_output(c, true, u1, ou1, ntar));
+            FTE_TRY(finish_output(c, true, u2, ou2, ntar));
+            FTE_TRY(finish_output(c, true, ur, our, 2 * (size_t)ntar));
+            FTE_TRY(finish_output(c, true, uk, ouk, 2 * (size_t)ntar));
+        }
+    }
+    FTE_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    if (info) {
+        std::memset(info, 0, sizeof(*info));
+        info->params = prm;
+        info->kernels_launched = (int)(c->kernels - k0);
+        if (c->timing && ntar > 0) {
+            info->ms_total = fte_elapsed(c, 0, 5);
+            info->ms_cells = fte_elapsed(c, 1, 6);
+            info->ms_near = fte_elapsed(c, 6, 7);
+            info->ms_spread = fte_elapsed(c, 2, 3);
+            info->ms_fft = fte_elapsed(c, 3, 4);
+            info->ms_gather = fte_elapsed(c, 4, 5);
+        }
+    }
+    return FTE_OK;
+}
+
+extern "C" int fte_stokes_slp_ewald_2p(fte_context* c, const double* xsrc, const double* ysrc, int64_t nsrc,
+                                       const double* xtar, const double* ytar, int64_t ntar, const double* f1,
+                                       const double* f2, double Lx, double Ly, const fte_options* opt, double* u1,
+                                       double* u2, double* ur, double* uk, fte_info* info, unsigned flags) {
+    return ewald_entry(c, FTE_KIND_SLP, xsrc, ysrc, nsrc, xtar, ytar, ntar, nullptr, nullptr, f1, f2, Lx, Ly, opt, u1,
+                       u2, ur, uk, info, flags);
+}
+
+extern "C" int fte_stokes_dlp_ewald_2p(fte_context* c, const double* xsrc, const double* ysrc, int64_t nsrc,
+                                       const double* xtar, const double* ytar, int64_t ntar, const double* n1,
+                                       const double* n2, const double* f1, const double* f2, double Lx, double Ly,
+                                       const fte_options* opt, double* u1, double* u2, double* ur, double* uk,
+                                       fte_info* info, unsigned flags) {
+    return ewald_entry(c, FTE_KIND_DLP, xsrc, ysrc, nsrc, xtar, ytar, ntar, n1, n2, f1, f2, Lx, Ly, opt, u1, u2, ur,
+                       uk, info, flags);
+}

@@ -1,0 +1,210 @@
+// fte_internal.cuh -- shared declarations of the GB300 spectral Ewald library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <map>
+#include <vector>
+
+#include "../../include/fasttools2d.h"
+
+#define FTE_PI 3.14159265358979323846
+#define FTE_EULER 0.57721566490153286060651209008240243
+
+// ---------------------------------------------------------------------------
+// Errors: every internal routine returns an FTE_* status and records a message
+// in a thread-local buffer read by fte_last_error().
+// ---------------------------------------------------------------------------
+void fte_set_error(const char* fmt, ...);
+
+#define FTE_CUDA_TRY(expr)                                                                         \
+    do {                                                                                           \
+        cudaError_t e_ = (expr);                                                                   \
+        if (e_ != cudaSuccess) {                                                                   \
+            fte_set_error("%s failed: %s (%s:%d)", #expr, cudaGetErrorString(e_), __FILE__, __LINE__); \
+            return FTE_ERR_CUDA;                                                                   \
+        }                                                                                          \
+    } while (0)
+
+#define FTE_TRY(expr)          \
+    do {                       \
+        int s_ = (expr);       \
+        if (s_ != FTE_OK) return s_; \
+    } while (0)
+
+// launch a kernel on ctx->stream and count it
+#define FTE_LAUNCH(ctx, kernel, grid, block, smem, ...)                                       \
+    do {                                                                                      \
+        kernel<<<(grid), (block), (smem), (ctx)->stream>>>(__VA_ARGS__);                      \
+        cudaError_t e_ = cudaGetLastError();                                                  \
+        if (e_ != cudaSuccess) {                                                              \
+            fte_set_error("launch of %s failed: %s (%s:%d)", #kernel, cudaGetErrorString(e_), \
+                          __FILE__, __LINE__);                                                \
+            return FTE_ERR_CUDA;                                                              \
+        }                                                                                     \
+        (ctx)->kernels++;                                                                     \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// FFT plan for one transform length (device tables are owned by the plan).
+// ---------------------------------------------------------------------------
+struct FftPlan {
+    int n = 0;           // transform length
+    int nrad = 0;        // Stockham passes of the inner transform
+    int rad[24] = {0};   // radices (2, 3, 4, 5, 7, 8)
+    int bluestein = 0;   // 1: chirp-z over the 7-smooth length m
+    int m = 0;           // inner transform length (n, or m >= 2n-1 for Bluestein)
+    double2* tw = nullptr;     // W_m^t = exp(-2 pi i t / m), t < m   (device, FP64)
+    double2* chirp = nullptr;  // exp(-i pi k^2 / n), k < n           (Bluestein)
+    double2* bhat = nullptr;   // DFT_m of the conjugate chirp / m    (Bluestein)
+    float2* tw32 = nullptr;    // FP32 copies for the mixed form
+    float2* chirp32 = nullptr;
+    float2* bhat32 = nullptr;
+};
+
+// Device view of a plan passed by value to kernels.
+struct FftDev {
+    int n, m, nrad, bluestein;
+    int rad[24];
+    const double2* tw;
+    const double2* chirp;
+    const double2* bhat;
+    const float2* tw32;
+    const float2* chirp32;
+    const float2* bhat32;
+};
+
+struct fte_context {
+    int device = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    int timing = 0;
+    long long kernels = 0;
+    // workspace (grown on demand, reused across calls)
+    char* ws = nullptr;   // point data staged for one call
+    size_t ws_size = 0;
+    char* ws2 = nullptr;  // cell list, grids and outputs
+    size_t ws2_size = 0;
+    // small pinned host buffer for scalar read-backs
+    double* host_scalars = nullptr;
+    std::map<int, FftPlan*> plans;
+    cudaEvent_t ev[8] = {nullptr};
+    int max_smem_optin = 0;
+    int num_sms = 0;
+};
+
+// Bump allocator over the context workspace.  Sizes are rounded to 256 B.
+struct WsCarver {
+    char* base;
+    size_t off = 0;
+    size_t cap;
+    template <typename T>
+    T* take(size_t count) {
+        size_t bytes = (count * sizeof(T) + 255) & ~size_t(255);
+        T* p = reinterpret_cast<T*>(base + off);
+        off += bytes;
+        return p;
+    }
+    bool ok() const { return off <= cap; }
+};
+// Fails the call (before any kernel touches the carved memory) when the
+// workspace estimate was too small.
+#define FTE_WS_CHECK(wc)                                                                        \
+    do {                                                                                        \
+        if (!(wc).ok()) {                                                                       \
+            fte_set_error("internal: workspace estimate too small (%zu > %zu) at %s:%d",        \
+                          (size_t)(wc).off, (size_t)(wc).cap, __FILE__, __LINE__);              \
+            return FTE_ERR_ALLOC;                                                               \
+        }                                                                                       \
+    } while (0)
+inline size_t ws_bytes(size_t count, size_t elem) { return (count * elem + 255) & ~size_t(255); }
+
+int fte_ws_reserve(fte_context* ctx, size_t bytes);
+int fte_ws2_reserve(fte_context* ctx, size_t bytes);
+int fte_get_plan(fte_context* ctx, int n, FftDev* out);
+int fte_record(fte_context* ctx, int slot);
+double fte_elapsed(fte_context* ctx, int a, int b);
+
+// ---------------------------------------------------------------------------
+// Device helpers shared by the kernels.
+// ---------------------------------------------------------------------------
+
+// First window node (mx, my) and in-cell offsets (px, py) of a point: the
+// reference's FindClosestNode (PeriodicEwald/src/mex/common/ewald_tools.cpp:116-144).
+// Written with explicitly rounded operations so that no multiply-add is fused:
+// the tie-break below depends on the exact rounding of each step.
+__device__ __forceinline__ void fte_closest_node(double x, double y, double Lx, double Ly, double h, int P, int* mx,
+                                                 int* my, double* px, double* py) {
+    const double TOL = 1e-13;
+    double qx = __ddiv_rn(x, h), qy = __ddiv_rn(y, h);
+    double ppx = __dsub_rn(x, __dmul_rn(h, floor(qx)));
+    double ppy = __dsub_rn(y, __dmul_rn(h, floor(qy)));
+    double lhx = __ddiv_rn(Lx, 2.0), lhy = __ddiv_rn(Ly, 2.0);
+    double ax = __ddiv_rn(__dadd_rn(x, lhx), h), ay = __ddiv_rn(__dadd_rn(y, lhy), h);
+    int half = P / 2;
+    int ix = (int)__dsub_rn(floor(ax), (double)half);
+    int iy = (int)__dsub_rn(floor(ay), (double)half);
+    if (fabs(ppx) < TOL || fabs(__dsub_rn(ppx, h)) < TOL) ppx = 0;
+    if (fabs(ppy) < TOL || fabs(__dsub_rn(ppy, h)) < TOL) ppy = 0;
+    if (ppx == 0 && remainder(__dsub_rn(ax, (double)half), 1.0) < 0) ix++;
+    if (ppy == 0 && remainder(__dsub_rn(ay, (double)half), 1.0) < 0) iy++;
+    *mx = ix;
+    *my = iy;
+    *px = ppx;
+    *py = ppy;
+}
+
+__device__ __forceinline__ int fte_wrap_index(int i, int M) {
+    int r = i % M;
+    return r < 0 ? r + M : r;
+}
+
+// Cell of a point: floor(nside (x/L + 0.5)) clamped to [0, nside-1]
+// (PeriodicEwald/src/mex/common/ewald_tools.cpp:57-64).
+__device__ __forceinline__ int fte_cell_1d(double x, double L, int nside) {
+    int b = (int)floor(__dmul_rn((double)nside, __dadd_rn(__ddiv_rn(x, L), 0.5)));
+    if (b < 0) b = 0;
+    if (b >= nside) b = nside - 1;
+    return b;
+}
+
+// Host launchers (one translation unit each).
+struct CellList {
+    int nsx, nsy, nb;
+    // sources sorted by cell
+    int* src_off;   // nb + 1
+    double2* spos;  // sorted source positions
+    double* q0;     // SLP: f1 ; DLP: S11 = f1 n1
+    double* q1;     // SLP: f2 ; DLP: S12 + S21
+    double* q2;     // DLP: S22
+    // targets sorted by cell
+    int* tar_off;   // nb + 1
+    double2* tpos;
+    int* tidx;      // original index of each sorted target
+    int max_neigh;  // upper bound of sources in a 3x3 neighbourhood (0 = unknown)
+};
+
+size_t fte_cells_ws(int64_t nsrc, int64_t ntar, int nb);
+int fte_cells_build(fte_context* ctx, WsCarver& wc, int kind, const double* psrc, int64_t nsrc, const double* ptar,
+                    int64_t ntar, const double* f, const double* nrm, const double* wts, int nsx, int nsy, double Lx,
+                    double Ly, CellList* cl);
+int fte_scan_exclusive(fte_context* ctx, WsCarver& wc, const int* in, int* out, int n);
+
+int fte_near_launch(fte_context* ctx, int kind, const CellList& cl, double xi, double Lx, double Ly, double2* ur);
+
+struct KspaceArgs {
+    int kind;
+    int form;
+    int64_t nsrc, ntar;
+    const double* psrc;  // interleaved
+    const double* ptar;
+    const double* f;     // interleaved
+    const double* nrm;   // interleaved (DLP)
+    const double* wts;   // optional weights (driver option)
+    double xi, eta, w, Lx, Ly;
+    int Mx, My, P;
+    double2* uk;         // output, interleaved
+};
+size_t fte_kspace_ws(int kind, int form, int Mx, int My);
+int fte_kspace_run(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, fte_info* info);

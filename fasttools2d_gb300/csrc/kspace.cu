@@ -1,0 +1,397 @@
+// kspace.cu -- Fourier-space part of the spectral Ewald sums (FP64 form).
+//
+// Restates the reference's k-space gateways
+//   SLP: PeriodicEwald/src/mex/StokesSLP/mex_stokes_slp_kspace.cpp:47-209
+//   DLP: PeriodicEwald/src/mex/StokesDLP/mex_stokes_dlp_kspace.cpp:266-487
+// and the shared Spread/Gather (PeriodicEwald/src/mex/common/ewald_tools.cpp:150-301):
+//
+//   1. spread: every source adds omega(node) q_c to (P+1)^2 nodes of each
+//      grid, omega the fast-Gaussian-gridding window of the reference
+//      (e1[j] = exp(-2 xi^2 h^2 j^2 / eta) and four exps per point);
+//   2. forward 2-D FFT of each real grid;
+//   3. the Stokeslet / stresslet multiplier with the reference's index ->
+//      wave-number map (index <= M/2 counted positive) and k = 0 set to 0;
+//   4. inverse FFT, real part;
+//   5. gather with the same window, scaled by (4 xi^2/eta)^2 h^2/pi/(4 pi).
+//
+// Layout in HBM: real grids [g][x][y] (y fastest, the reference's column-major
+// My x Mx); half spectra [g][x][ky], ky = 0..My/2.  The 2-D transform is a
+// real-to-complex FFT along y (two real columns packed in one complex FFT),
+// complex FFTs along x, the multiplier, inverse FFTs along x and a
+// complex-to-real FFT along y.  Because the reference multiplies the Nyquist
+// column/row with +k on both the k and -k copies and then keeps only the real
+// part of the inverse transform, the half-spectrum multiplier is the average
+// of the multiplier at (k1, k2) and at the Nyquist-mirrored wave vector
+// (k1', k2') (k' = -k on a Nyquist index, k' = k elsewhere); this reproduces
+// real(ifft2(.)) of the full-grid reference exactly.
+#include "fft.cuh"
+#include "fte_internal.cuh"
+
+namespace {
+
+constexpr int kPtThreads = 128;
+
+struct WinParams {
+    double Lx, Ly, h, xi, eta, w;
+    int P, Mx, My;
+};
+
+// per-point window factors, as in ewald_tools.cpp:182-190 / 256-262
+struct Win {
+    int mx, my;
+    double ex, e4y, e3x, e3y;
+};
+
+__device__ __forceinline__ Win window_of(double x, double y, const WinParams& wp) {
+    Win o;
+    double px, py;
+    fte_closest_node(x, y, wp.Lx, wp.Ly, wp.h, wp.P, &o.mx, &o.my, &px, &py);
+    double t = -2 * wp.xi * wp.xi / wp.eta;
+    o.ex = exp(t * (px * px + py * py + 2 * wp.w * px));
+    o.e4y = exp(2 * t * wp.w * py);
+    o.e3x = exp(-2 * t * wp.h * px);
+    o.e3y = exp(-2 * t * wp.h * py);
+    return o;
+}
+
+// e1[j] = exp(-2 xi^2/eta h^2 (j - P/2)^2)   (ewald_tools.cpp:155-157)
+__device__ __forceinline__ void load_e1(double* e1, const WinParams& wp) {
+    double t0 = -2 * wp.xi * wp.xi / wp.eta * wp.h * wp.h;
+    for (int j = threadIdx.x; j <= wp.P; j += blockDim.x) {
+        int jj = j - wp.P / 2;
+        e1[j] = exp(t0 * jj * jj);
+    }
+}
+
+// ---- spread: one thread per source, FP64 atomics into the global grids ------
+template <int NG>
+__global__ void __launch_bounds__(kPtThreads) k_spread(const double* __restrict__ p, const double* __restrict__ f,
+                                                      const double* __restrict__ nrm, const double* __restrict__ wts,
+                                                      int64_t n, WinParams wp, double* __restrict__ H) {
+    extern __shared__ double sh[];
+    double* e1 = sh;
+    const int P1 = wp.P + 1;
+    double* wyb = e1 + ((P1 + 1) & ~1) + threadIdx.x * P1;
+    load_e1(e1, wp);
+    __syncthreads();
+    const size_t G = (size_t)wp.Mx * wp.My;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double x = p[2 * i], y = p[2 * i + 1];
+        Win wn = window_of(x, y, wp);
+        double q[4];
+        double f1 = f[2 * i], f2 = f[2 * i + 1];
+        if (wts) {
+            f1 *= wts[i];
+            f2 *= wts[i];
+        }
+        if (NG == 2) {
+            q[0] = f1;
+            q[1] = f2;
+        } else {
+            // (f1 n1, f2 n1, f1 n2, f2 n2): mex_stokes_dlp_kspace.cpp:290-298
+            double n1 = nrm[2 * i], n2 = nrm[2 * i + 1];
+            q[0] = f1 * n1;
+            q[1] = f2 * n1;
+            q[2] = f1 * n2;
+            q[3] = f2 * n2;
+        }
+        // y factors e1[y] e3y^y
+        double ey = 1.0;
+        for (int j = 0; j < P1; j++) {
+            wyb[j] = ey * e1[j];
+            ey *= wn.e3y;
+        }
+        bool ywrap = !(wn.my >= 0 && wn.my + wp.P < wp.My);
+        double ex = wn.ex * wn.e4y;
+        for (int a = 0; a < P1; a++) {
+            double wxa = ex * e1[a];
+            ex *= wn.e3x;
+            int col = fte_wrap_index(wn.mx + a, wp.Mx);
+            size_t base = (size_t)col * wp.My;
+            double fw[NG];
+#pragma unroll
+            for (int g = 0; g < NG; g++) fw[g] = q[g] * wxa;
+            for (int j = 0; j < P1; j++) {
+                int row = ywrap ? fte_wrap_index(wn.my + j, wp.My) : wn.my + j;
+                double wyj = wyb[j];
+#pragma unroll
+                for (int g = 0; g < NG; g++) atomicAdd(&H[g * G + base + row], fw[g] * wyj);
+            }
+        }
+    }
+}
+
+// ---- gather: one thread per target -------------------------------------------
+__global__ void __launch_bounds__(kPtThreads) k_gather(const double* __restrict__ p, int64_t n, WinParams wp,
+                                                       const double* __restrict__ G0, const double* __restrict__ G1,
+                                                       double scale, double2* __restrict__ out) {
+    extern __shared__ double sh[];
+    double* e1 = sh;
+    const int P1 = wp.P + 1;
+    double* wyb = e1 + ((P1 + 1) & ~1) + threadIdx.x * P1;
+    load_e1(e1, wp);
+    __syncthreads();
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double x = p[2 * i], y = p[2 * i + 1];
+        Win wn = window_of(x, y, wp);
+        double ey = 1.0;
+        for (int j = 0; j < P1; j++) {
+            wyb[j] = ey * e1[j];
+            ey *= wn.e3y;
+        }
+        bool ywrap = !(wn.my >= 0 && wn.my + wp.P < wp.My);
+        double ex = wn.ex * wn.e4y;
+        double acc0 = 0.0, acc1 = 0.0;
+        for (int a = 0; a < P1; a++) {
+            double wxa = ex * e1[a];
+            ex *= wn.e3x;
+            int col = fte_wrap_index(wn.mx + a, wp.Mx);
+            const double* c0 = G0 + (size_t)col * wp.My;
+            const double* c1 = G1 + (size_t)col * wp.My;
+            double s0 = 0.0, s1 = 0.0;
+            if (!ywrap) {
+                for (int j = 0; j < P1; j++) {
+                    double wyj = wyb[j];
+                    s0 = fma(wyj, __ldg(c0 + wn.my + j), s0);
+                    s1 = fma(wyj, __ldg(c1 + wn.my + j), s1);
+                }
+            } else {
+                for (int j = 0; j < P1; j++) {
+                    int row = fte_wrap_index(wn.my + j, wp.My);
+                    double wyj = wyb[j];
+                    s0 = fma(wyj, __ldg(c0 + row), s0);
+                    s1 = fma(wyj, __ldg(c1 + row), s1);
+                }
+            }
+            acc0 = fma(wxa, s0, acc0);
+            acc1 = fma(wxa, s1, acc1);
+        }
+        out[i] = make_double2(acc0 * scale, acc1 * scale);
+    }
+}
+
+// ---- FFT along y: real -> half spectrum (two columns per complex FFT) -------
+__global__ void k_fft_y_r2c(const double* __restrict__ H, double2* __restrict__ Hh, int Mx, int My, FftDev plan) {
+    extern __shared__ double2 shc[];
+    double2* A = shc;
+    double2* B = shc + plan.m;
+    const int c = blockIdx.x, g = blockIdx.y;
+    const int Kh = My / 2 + 1;
+    const double* h0 = H + ((size_t)g * Mx + 2 * c) * My;
+    const double* h1 = h0 + My;
+    for (int y = threadIdx.x; y < My; y += blockDim.x) A[y] = make_double2(h0[y], h1[y]);
+    double2* R = fft_block<double>(A, B, plan, false);
+    double2* o0 = Hh + ((size_t)g * Mx + 2 * c) * Kh;
+    double2* o1 = o0 + Kh;
+    for (int k = threadIdx.x; k < Kh; k += blockDim.x) {
+        double2 zk = R[k], zm = R[(My - k) % My];
+        // A_k = (Z_k + conj Z_{-k})/2,  B_k = (Z_k - conj Z_{-k})/(2i)
+        o0[k] = make_double2(0.5 * (zk.x + zm.x), 0.5 * (zk.y - zm.y));
+        o1[k] = make_double2(0.5 * (zk.y + zm.y), -0.5 * (zk.x - zm.x));
+    }
+}
+
+// ---- FFT along x of half spectra, in place: one block per (ky, grid) ---------
+__global__ void k_fft_x(double2* __restrict__ Hh, int Mx, int Kh, FftDev plan, int inv) {
+    extern __shared__ double2 shc[];
+    double2* A = shc;
+    double2* B = shc + plan.m;
+    const int k = blockIdx.x, g = blockIdx.y;
+    double2* base = Hh + (size_t)g * Mx * Kh + k;
+    for (int x = threadIdx.x; x < Mx; x += blockDim.x) A[x] = base[(size_t)x * Kh];
+    double2* R = fft_block<double>(A, B, plan, inv != 0);
+    for (int x = threadIdx.x; x < Mx; x += blockDim.x) base[(size_t)x * Kh] = R[x];
+}
+
+// ---- FFT along y: half spectrum -> real, two columns per complex FFT --------
+__global__ void k_fft_y_c2r(const double2* __restrict__ Hh, double* __restrict__ H, int Mx, int My, FftDev plan) {
+    extern __shared__ double2 shc[];
+    double2* A = shc;
+    double2* B = shc + plan.m;
+    const int c = blockIdx.x, g = blockIdx.y;
+    const int Kh = My / 2 + 1;
+    const double2* i0 = Hh + ((size_t)g * Mx + 2 * c) * Kh;
+    const double2* i1 = i0 + Kh;
+    for (int k = threadIdx.x; k < Kh; k += blockDim.x) {
+        double2 a = i0[k], b = i1[k];
+        if (k == 0 || 2 * k == My) {
+            a.y = 0.0;
+            b.y = 0.0;
+        }
+        // Z_k = a + i b ; Z_{My-k} = conj(a) + i conj(b)
+        A[k] = make_double2(a.x - b.y, a.y + b.x);
+        if (k > 0 && 2 * k < My) A[My - k] = make_double2(a.x + b.y, -a.y + b.x);
+    }
+    double2* R = fft_block<double>(A, B, plan, true);
+    double* o0 = H + ((size_t)g * Mx + 2 * c) * My;
+    double* o1 = o0 + My;
+    for (int y = threadIdx.x; y < My; y += blockDim.x) {
+        double2 z = R[y];
+        o0[y] = z.x;
+        o1[y] = z.y;
+    }
+}
+
+// ---- k-space multipliers ------------------------------------------------------
+// SLP (mex_stokes_slp_kspace.cpp:128-139): G = (K^2 H - k (k.H)) (1/K^4 + 1/(4 xi^2 K^2)) e^{-(1-eta)K^2/(4xi^2)}
+__device__ __forceinline__ void slp_mult(double k1, double k2, double xi, double eta, double2 q1, double2 q2,
+                                         double2& g1, double2& g2) {
+    double K = k1 * k1 + k2 * k2;
+    double e = (1.0 / (K * K) + 0.25 / (K * xi * xi)) * exp(-0.25 * (1 - eta) / (xi * xi) * K);
+    double kqr = k1 * q1.x + k2 * q2.x, kqi = k1 * q1.y + k2 * q2.y;
+    g1 = make_double2((K * q1.x - k1 * kqr) * e, (K * q1.y - k1 * kqi) * e);
+    g2 = make_double2((K * q2.x - k2 * kqr) * e, (K * q2.y - k2 * kqi) * e);
+}
+
+// DLP (mex_stokes_dlp_kspace.cpp:372-402) on the spectra of S11, S21, S12, S22
+__device__ __forceinline__ void dlp_mult(double k1, double k2, double xi, double eta, double2 a, double2 s21,
+                                         double2 s12, double2 d, double2& g1, double2& g2) {
+    double K = k1 * k1 + k2 * k2;
+    double e = exp(-K * (1 - eta) / (4 * xi * xi)) * (1 + K / (4 * xi * xi)) / K;
+    double sr = s21.x + s12.x, si = s21.y + s12.y;
+    double qr = (k1 * k1 * a.x + k1 * k2 * sr + k2 * k2 * d.x) / K;
+    double qi = (k1 * k1 * a.y + k1 * k2 * si + k2 * k2 * d.y) / K;
+    double x1r = 2 * a.x * k1 + k2 * sr + k1 * (a.x + d.x) - 2 * k1 * qr;
+    double x1i = 2 * a.y * k1 + k2 * si + k1 * (a.y + d.y) - 2 * k1 * qi;
+    double x2r = 2 * d.x * k2 + k1 * sr + k2 * (a.x + d.x) - 2 * k2 * qr;
+    double x2i = 2 * d.y * k2 + k1 * si + k2 * (a.y + d.y) - 2 * k2 * qi;
+    g1 = make_double2(-x1i * e, x1r * e);
+    g2 = make_double2(-x2i * e, x2r * e);
+}
+
+template <int KIND>
+__global__ void k_filter(double2* __restrict__ Hh, int Mx, int My, double Lx, double Ly, double xi, double eta) {
+    const int Kh = My / 2 + 1;
+    const size_t GS = (size_t)Mx * Kh;
+    const size_t tot = GS;
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < tot; idx += (size_t)gridDim.x * blockDim.x) {
+        int j = (int)(idx / Kh), k = (int)(idx % Kh);
+        double2* p0 = Hh + idx;
+        if (j == 0 && k == 0) {
+            p0[0] = make_double2(0, 0);
+            p0[GS] = make_double2(0, 0);
+            continue;
+        }
+        double k1 = (j <= Mx / 2) ? 2.0 * FTE_PI / Lx * j : 2.0 * FTE_PI / Lx * (j - Mx);
+        double k2 = 2.0 * FTE_PI / Ly * k;
+        bool nyq_x = (2 * j == Mx), nyq_y = (2 * k == My);
+        double2 g1, g2;
+        if (KIND == FTE_KIND_SLP) {
+            double2 q1 = p0[0], q2 = p0[GS];
+            slp_mult(k1, k2, xi, eta, q1, q2, g1, g2);
+            if (nyq_x || nyq_y) {
+                double2 h1, h2;
+                slp_mult(nyq_x ? -k1 : k1, nyq_y ? -k2 : k2, xi, eta, q1, q2, h1, h2);
+                g1 = make_double2(0.5 * (g1.x + h1.x), 0.5 * (g1.y + h1.y));
+                g2 = make_double2(0.5 * (g2.x + h2.x), 0.5 * (g2.y + h2.y));
+            }
+        } else {
+            double2 a = p0[0], s21 = p0[GS], s12 = p0[2 * GS], d = p0[3 * GS];
+            dlp_mult(k1, k2, xi, eta, a, s21, s12, d, g1, g2);
+            if (nyq_x || nyq_y) {
+                double2 h1, h2;
+                dlp_mult(nyq_x ? -k1 : k1, nyq_y ? -k2 : k2, xi, eta, a, s21, s12, d, h1, h2);
+                g1 = make_double2(0.5 * (g1.x + h1.x), 0.5 * (g1.y + h1.y));
+                g2 = make_double2(0.5 * (g2.x + h2.x), 0.5 * (g2.y + h2.y));
+            }
+        }
+        p0[0] = g1;
+        p0[GS] = g2;
+    }
+}
+
+inline int pt_grid(fte_context* ctx, int64_t n) {
+    int64_t b = (n + kPtThreads - 1) / kPtThreads;
+    int64_t maxb = (int64_t)ctx->num_sms * 16;
+    if (b > maxb) b = maxb;
+    if (b < 1) b = 1;
+    return (int)b;
+}
+
+int fft_threads(int m) {
+    int t = 64;
+    while (t < 512 && t * 8 < m) t *= 2;
+    return t;
+}
+
+}  // namespace
+
+size_t fte_kspace_ws(int kind, int form, int Mx, int My) {
+    (void)form;
+    int ng = kind == FTE_KIND_SLP ? 2 : 4;
+    size_t G = (size_t)Mx * My;
+    size_t Gh = (size_t)Mx * (My / 2 + 1);
+    return ws_bytes(ng * G, sizeof(double)) + ws_bytes(ng * Gh, sizeof(double2)) + 4096;
+}
+
+int fte_kspace_run(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, fte_info* info) {
+    const int ng = a.kind == FTE_KIND_SLP ? 2 : 4;
+    const int Mx = a.Mx, My = a.My;
+    const size_t G = (size_t)Mx * My;
+    const int Kh = My / 2 + 1;
+    double* H = wc.take<double>(ng * G);
+    double2* Hh = wc.take<double2>(ng * (size_t)Mx * Kh);
+    FTE_WS_CHECK(wc);
+    WinParams wp;
+    wp.Lx = a.Lx;
+    wp.Ly = a.Ly;
+    wp.h = a.Lx / Mx;
+    wp.xi = a.xi;
+    wp.eta = a.eta;
+    wp.w = a.w;
+    wp.P = a.P;
+    wp.Mx = Mx;
+    wp.My = My;
+    FftDev py, px;
+    FTE_TRY(fte_get_plan(ctx, My, &py));
+    FTE_TRY(fte_get_plan(ctx, Mx, &px));
+    size_t sm_y = 2 * (size_t)py.m * sizeof(double2);
+    size_t sm_x = 2 * (size_t)px.m * sizeof(double2);
+    if (sm_y > (size_t)ctx->max_smem_optin || sm_x > (size_t)ctx->max_smem_optin) {
+        fte_set_error("grid %d x %d needs FFT lengths (%d, %d) beyond this build's shared-memory transform", Mx, My,
+                      px.m, py.m);
+        return FTE_ERR_UNSUPPORTED;
+    }
+    const int P1 = a.P + 1;
+    size_t sm_pt = (size_t)(((P1 + 1) & ~1) + kPtThreads * P1) * sizeof(double);
+
+    FTE_TRY(fte_record(ctx, 2));
+    FTE_CUDA_TRY(cudaMemsetAsync(H, 0, sizeof(double) * ng * G, ctx->stream));
+    if (a.nsrc > 0) {
+        if (ng == 2) {
+            FTE_CUDA_TRY(cudaFuncSetAttribute(k_spread<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_pt));
+            FTE_LAUNCH(ctx, k_spread<2>, pt_grid(ctx, a.nsrc), kPtThreads, sm_pt, a.psrc, a.f, a.nrm, a.wts, a.nsrc,
+                       wp, H);
+        } else {
+            FTE_CUDA_TRY(cudaFuncSetAttribute(k_spread<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_pt));
+            FTE_LAUNCH(ctx, k_spread<4>, pt_grid(ctx, a.nsrc), kPtThreads, sm_pt, a.psrc, a.f, a.nrm, a.wts, a.nsrc,
+                       wp, H);
+        }
+    }
+    FTE_TRY(fte_record(ctx, 3));
+    FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_y_r2c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_y));
+    FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_y_c2r, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_y));
+    FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_x));
+    FTE_LAUNCH(ctx, k_fft_y_r2c, dim3(Mx / 2, ng), fft_threads(py.m), sm_y, (const double*)H, Hh, Mx, My, py);
+    FTE_LAUNCH(ctx, k_fft_x, dim3(Kh, ng), fft_threads(px.m), sm_x, Hh, Mx, Kh, px, 0);
+    int fb = (int)(((size_t)Mx * Kh + 255) / 256);
+    if (fb > ctx->num_sms * 32) fb = ctx->num_sms * 32;
+    if (a.kind == FTE_KIND_SLP)
+        FTE_LAUNCH(ctx, k_filter<FTE_KIND_SLP>, fb, 256, 0, Hh, Mx, My, a.Lx, a.Ly, a.xi, a.eta);
+    else
+        FTE_LAUNCH(ctx, k_filter<FTE_KIND_DLP>, fb, 256, 0, Hh, Mx, My, a.Lx, a.Ly, a.xi, a.eta);
+    FTE_LAUNCH(ctx, k_fft_x, dim3(Kh, 2), fft_threads(px.m), sm_x, Hh, Mx, Kh, px, 1);
+    FTE_LAUNCH(ctx, k_fft_y_c2r, dim3(Mx / 2, 2), fft_threads(py.m), sm_y, (const double2*)Hh, H, Mx, My, py);
+    FTE_TRY(fte_record(ctx, 4));
+    double s = 4 * a.xi * a.xi / a.eta;
+    s = s * s * wp.h * wp.h / FTE_PI;
+    double scale = s / (4 * FTE_PI) / ((double)Mx * (double)My);
+    if (a.ntar > 0) {
+        FTE_CUDA_TRY(cudaFuncSetAttribute(k_gather, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_pt));
+        FTE_LAUNCH(ctx, k_gather, pt_grid(ctx, a.ntar), kPtThreads, sm_pt, a.ptar, a.ntar, wp, (const double*)H,
+                   (const double*)(H + G), scale, a.uk);
+    }
+    FTE_TRY(fte_record(ctx, 5));
+    (void)info;
+    return FTE_OK;
+}

@@ -1,0 +1,156 @@
+/*
+ * fasttools2d.h -- C ABI of the GB300 implementation of the doubly-periodic
+ * spectral Ewald (SE) summation for the 2-D Stokeslet (single layer, SLP)
+ * and stresslet (double layer, DLP).
+ *
+ * The entry points replace annabroms/FastTools2D's spectral Ewald path
+ * (paths relative to that project):
+ *
+ *   fte_slp_real      <- mex_stokes_slp_real     PeriodicEwald/src/mex/StokesSLP/mex_stokes_slp_real.cpp:58-83,340-346
+ *   fte_slp_kspace    <- mex_stokes_slp_kspace   PeriodicEwald/src/mex/StokesSLP/mex_stokes_slp_kspace.cpp:7-48,205-209
+ *   fte_dlp_real      <- mex_stokes_dlp_real     PeriodicEwald/src/mex/StokesDLP/mex_stokes_dlp_real.cpp:15-52,193-200
+ *   fte_dlp_kspace    <- mex_stokes_dlp_kspace   PeriodicEwald/src/mex/StokesDLP/mex_stokes_dlp_kspace.cpp:10-53,272-276
+ *   fte_stokes_slp_ewald_2p <- StokesSLP_ewald_2p PeriodicEwald/src/matlab/StokesSLP_ewald_2p.m:1-138
+ *   fte_stokes_dlp_ewald_2p <- StokesDLP_ewald_2p PeriodicEwald/src/matlab/StokesDLP_ewald_2p.m:1-163
+ *   fte_choose_params       <- the drivers' parameter selection and find_xi/find_kinfb
+ *                              (StokesSLP_ewald_2p.m:27-35,85-104,147-202;
+ *                               StokesDLP_ewald_2p.m:27-38,307-327,373-427)
+ *
+ * Conventions (as the MEX gateways): point, density and normal arrays given
+ * as one pointer are 2 x N column-major doubles, i.e. x/y interleaved
+ * (p[2*j], p[2*j+1]); the driver-level entries take separate x and y arrays
+ * like the MATLAB functions.  Outputs are caller-allocated and written in the
+ * caller's target order.  Quadrature weights are not a separate argument in
+ * the reference (callers fold them into f); fte_options.weights offers the
+ * same folding as a convenience.
+ *
+ * Pointers are host pointers unless FTE_DEVICE_POINTERS is set in `flags`,
+ * in which case every array argument of that call is device memory of the
+ * context's device.  Every entry returns FTE_OK or an FTE_ERR_* status; the
+ * message of the last failure on the calling thread is fte_last_error().
+ * A context owns one CUDA stream and its workspace; calls on one context
+ * must not overlap, calls on different contexts are independent.
+ */
+#ifndef FASTTOOLS2D_H
+#define FASTTOOLS2D_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FTE_VERSION 100
+
+/* status codes */
+#define FTE_OK 0
+#define FTE_ERR_INVALID 1     /* argument rejected by validation */
+#define FTE_ERR_CUDA 2        /* a CUDA runtime call failed */
+#define FTE_ERR_ALLOC 3       /* device or host allocation failed */
+#define FTE_ERR_UNSUPPORTED 4 /* valid input outside what this build implements */
+#define FTE_ERR_DEVICE 5      /* a kernel reported an error status */
+
+/* flags */
+#define FTE_DEVICE_POINTERS 1u /* all array arguments are device pointers */
+
+/* arithmetic forms */
+#define FTE_FORM_PLAIN 0  /* FP64 everywhere (the drop-in) */
+#define FTE_FORM_MIXED 1  /* FP32 spread/FFT/filter/gather (compensated), FP64 near sums */
+
+/* kinds */
+#define FTE_KIND_SLP 0
+#define FTE_KIND_DLP 1
+
+typedef struct fte_context fte_context;
+
+/* Parameters of one SE evaluation (what the MATLAB drivers compute). */
+typedef struct {
+    int P;          /* window support: P+1 grid nodes per direction */
+    double Nb;      /* average points per cell used to size the cell list */
+    double tol;     /* requested tolerance */
+    double Q;       /* sum |f|^2 + 1 */
+    int A, B;       /* rat(Lx/Ly) */
+    int nside_x, nside_y;
+    double rc;      /* real-space cutoff Lx/nside_x */
+    double xi;      /* Ewald parameter */
+    int kinf;       /* Fourier truncation from find_kinfb */
+    int Mx, My;     /* grid size */
+    double w;       /* window half-width P*h/2 */
+    double eta;     /* window shape (2 xi w / m)^2, m = 0.95 sqrt(pi P) */
+} fte_params;
+
+/* Options of the driver-level entries; zero-initialise for the reference
+ * defaults (P = 24, Nb = min(P round(log2 npts), npts/4), tol = 1e-16). */
+typedef struct {
+    int P;
+    double Nb;
+    double tol;
+    double xi;             /* > 0: override xi */
+    int Mx, My;            /* > 0: override the grid */
+    int nside_x, nside_y;  /* > 0: override the cell list (cutoff = sqrt(Lx Ly/(nside_x nside_y))) */
+    const double* weights; /* optional quadrature weights, multiplied into f (length nsrc) */
+    int form;              /* FTE_FORM_PLAIN or FTE_FORM_MIXED */
+} fte_options;
+
+/* Per-call diagnostics (optional output of the driver entries). */
+typedef struct {
+    fte_params params;
+    double ms_total;       /* device time of the whole evaluation (CUDA events) */
+    double ms_cells;       /* cell list */
+    double ms_near;        /* real-space sum */
+    double ms_spread;
+    double ms_fft;         /* forward + inverse FFTs and the filter */
+    double ms_gather;
+    long long near_pairs;  /* pairs evaluated in the real-space sum (when counted) */
+    int kernels_launched;
+} fte_info;
+
+const char* fte_last_error(void);
+int fte_version(void);
+
+int fte_create(fte_context** ctx, int device);
+int fte_destroy(fte_context* ctx);
+/* Use an existing cudaStream_t for subsequent calls (NULL restores the
+ * context's own stream). */
+int fte_set_stream(fte_context* ctx, void* stream);
+/* Collect per-stage CUDA-event timings into fte_info (adds syncs). */
+int fte_set_timing(fte_context* ctx, int enable);
+/* Number of kernels this context launched so far. */
+long long fte_kernel_count(const fte_context* ctx);
+
+/* ---- gateway-level entries (2 x N interleaved arrays) -------------------- */
+int fte_slp_real(fte_context* ctx, const double* psrc, int64_t nsrc, const double* ptar, int64_t ntar,
+                 const double* f, double xi, int nside_x, int nside_y, double Lx, double Ly, double* ur,
+                 unsigned flags);
+int fte_dlp_real(fte_context* ctx, const double* psrc, int64_t nsrc, const double* ptar, int64_t ntar,
+                 const double* f, const double* n, double xi, int nside_x, int nside_y, double Lx, double Ly,
+                 double* ur, unsigned flags);
+int fte_slp_kspace(fte_context* ctx, const double* psrc, int64_t nsrc, const double* ptar, int64_t ntar, double xi,
+                   double eta, const double* f, int Mx, int My, double Lx, double Ly, double w, int P, double* uk,
+                   unsigned flags);
+int fte_dlp_kspace(fte_context* ctx, const double* psrc, int64_t nsrc, const double* ptar, int64_t ntar, double xi,
+                   double eta, const double* f, const double* n, int Mx, int My, double Lx, double Ly, double w,
+                   int P, double* uk, unsigned flags);
+
+/* ---- driver-level entries (separate x/y arrays) ------------------------- */
+/* u1, u2: length ntar; ur, uk: 2 x ntar interleaved or NULL; info may be NULL. */
+int fte_stokes_slp_ewald_2p(fte_context* ctx, const double* xsrc, const double* ysrc, int64_t nsrc,
+                            const double* xtar, const double* ytar, int64_t ntar, const double* f1,
+                            const double* f2, double Lx, double Ly, const fte_options* opt, double* u1, double* u2,
+                            double* ur, double* uk, fte_info* info, unsigned flags);
+int fte_stokes_dlp_ewald_2p(fte_context* ctx, const double* xsrc, const double* ysrc, int64_t nsrc,
+                            const double* xtar, const double* ytar, int64_t ntar, const double* n1,
+                            const double* n2, const double* f1, const double* f2, double Lx, double Ly,
+                            const fte_options* opt, double* u1, double* u2, double* ur, double* uk, fte_info* info,
+                            unsigned flags);
+
+/* Parameter selection alone (host arrays f1, f2 of length nsrc; Q is
+ * computed from them). */
+int fte_choose_params(int kind, int64_t nsrc, int64_t ntar, const double* f1, const double* f2, double Lx,
+                      double Ly, const fte_options* opt, fte_params* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
