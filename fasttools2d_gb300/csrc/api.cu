@@ -631,10 +631,8 @@ int check_kspace_params(double xi, double eta, int Mx, int My, double Lx, double
         fte_set_error("grid sizes must be even and >= 2 (Mx=%d, My=%d)", Mx, My);
         return FTE_ERR_INVALID;
     }
-    if (P + 1 > Mx || P + 1 > My) {
-        fte_set_error("window support P+1=%d exceeds the grid (Mx=%d, My=%d)", P + 1, Mx, My);
-        return FTE_ERR_INVALID;
-    }
+    // P + 1 > M is allowed: the window then wraps around the periodic grid
+    // more than once, as it does in the reference.
     double hx = Lx / Mx, hy = Ly / My;
     if (std::fabs(hx - hy) > 1e-12 * std::fmax(hx, hy)) {
         fte_set_error("grid spacing must be equal in x and y (Lx/Mx=%.17g, Ly/My=%.17g)", hx, hy);
