@@ -1,0 +1,408 @@
+#!/usr/bin/env python
+"""Benchmark of the doubly-periodic spectral Ewald Stokeslet + stresslet on GB300.
+
+Metric: targets/s at 1M points (10^6 sources, 10^6 targets uniform in [0,1]^2,
+zero-mean N(0,1) densities, unit normals at random angles), one step = one
+Stokeslet (SLP) plus one stresslet (DLP) evaluation of all targets, parameter
+selection included.  Reported per tolerance (1e-10 headline, 1e-6 alongside)
+with max and RMS relative error against the converged FP64 Ewald sums of
+10,000 sampled targets (tests/golden/truth_config3.npz).
+
+Arms:
+  default            the GPU library through its public API (C ABI, ctypes)
+  --impl reference   the reference's CPU spectral Ewald path on this host's
+                     cores: the reference's own gateways (oracle/_ref) where
+                     they were compiled for this machine, else the oracle's C
+                     restatement (oracle/or_ewald.c), OpenMP over all cores.
+
+Multi-GPU (torchrun): replicas only -- every rank evaluates the same
+configuration on its own GPU, no collective on the data path; value = total
+targets of all ranks / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import platform
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "targets/s at 1M pts, tol 1e-6 & 1e-10: chosen vs plain GPU form; max rel err"
+UNIT = "targets/s"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=1_000_000, help="sources = targets")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--quick", action="store_true", help="headline only (for profiling runs)")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        import numpy as np
+
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# reference arm: CPU
+# ---------------------------------------------------------------------------
+def reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    import numpy as np
+
+    from fasttools2d_gb300 import workloads as wl
+    from oracle import pyoracle as po
+
+    use_ref = platform.machine() in ("x86_64", "AMD64") and po.ref_available("O3")
+    if not os.path.exists(po.LIB_PATH):
+        po.build()
+
+    def run(cfg, n, tol):
+        sl = slice(0, n)
+        a = [cfg[k][sl] for k in ("xsrc", "ysrc", "xtar", "ytar")]
+        if use_ref:
+            po.ref_stokes_slp_ewald_2p(*a, cfg["f1"][sl], cfg["f2"][sl], 1.0, 1.0, tol=tol)
+            po.ref_stokes_dlp_ewald_2p(*a, cfg["n1"][sl], cfg["n2"][sl], cfg["f1"][sl], cfg["f2"][sl], 1.0, 1.0,
+                                       tol=tol)
+        else:
+            po.stokes_slp_ewald_2p(*a, cfg["f1"][sl], cfg["f2"][sl], 1.0, 1.0, tol=tol)
+            po.stokes_dlp_ewald_2p(*a, cfg["n1"][sl], cfg["n2"][sl], cfg["f1"][sl], cfg["f2"][sl], 1.0, 1.0, tol=tol)
+
+    cfg = wl.config3(n=args.n)
+    # size the per-step sample so that warmup + steps stay within ~3 minutes
+    probe_n = min(20000, args.n)
+    t = time.perf_counter()
+    run(wl.config3(n=probe_n), probe_n, 1e-10)
+    per_target = (time.perf_counter() - t) / probe_n
+    budget = 180.0 / max(1, args.steps + args.warmup)
+    n = int(min(args.n, max(probe_n, budget / per_target)))
+    sub = wl.config3(n=n)
+    for _ in range(args.warmup):
+        run(sub, n, 1e-10)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        run(sub, n, 1e-10)
+    dt = (time.perf_counter() - t0) / args.steps
+    value = n / dt
+    kind = "reference" if use_ref else "port"
+    sample = (f"config-3 layout at N = {n} sources and {n} targets (uniform [0,1]^2, zero-mean N(0,1) densities), "
+              f"one SLP + one DLP evaluation at tol 1e-10 per step, P = 24, analytic parameters")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "config3: SLP+DLP spectral Ewald, 1e6 sources / 1e6 targets, unit box, tol 1e-10",
+                   "sample_n": n, "l2": "n/a (CPU)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": int(os.environ.get("OMP_NUM_THREADS", cores)),
+                         "kind": kind, "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline(n_full):
+    """Oracle (or reference) on a bounded sample, ~10-30 s of CPU work."""
+    cores = os.cpu_count() or 1
+    from fasttools2d_gb300 import workloads as wl
+    from oracle import pyoracle as po
+
+    use_ref = platform.machine() in ("x86_64", "AMD64") and po.ref_available("O3")
+    if not os.path.exists(po.LIB_PATH):
+        po.build()
+    n = min(n_full, 100_000)
+    cfg = wl.config3(n=n)
+    a = [cfg[k] for k in ("xsrc", "ysrc", "xtar", "ytar")]
+    t = time.perf_counter()
+    if use_ref:
+        po.ref_stokes_slp_ewald_2p(*a, cfg["f1"], cfg["f2"], 1.0, 1.0, tol=1e-10)
+        po.ref_stokes_dlp_ewald_2p(*a, cfg["n1"], cfg["n2"], cfg["f1"], cfg["f2"], 1.0, 1.0, tol=1e-10)
+    else:
+        po.stokes_slp_ewald_2p(*a, cfg["f1"], cfg["f2"], 1.0, 1.0, tol=1e-10)
+        po.stokes_dlp_ewald_2p(*a, cfg["n1"], cfg["n2"], cfg["f1"], cfg["f2"], 1.0, 1.0, tol=1e-10)
+    dt = time.perf_counter() - t
+    return {"value": n / dt, "unit": UNIT, "cores": po.num_threads(), "kind": "reference" if use_ref else "port",
+            "sample": f"one SLP + one DLP evaluation, config-3 layout at N = {n} sources/targets, tol 1e-10, "
+                      f"{dt:.1f} s"}
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        reference_arm(args)
+        return
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
+    import numpy as np
+    import torch
+
+    import fasttools2d_gb300 as ft
+    from fasttools2d_gb300 import workloads as wl
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local_rank)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def max_over_ranks(x: float) -> float:
+        if dist is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    if not os.path.exists(ft.LIB_PATH):
+        ft.build()
+    ctx = ft.Context(local_rank)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+
+    cfg = wl.config3(n=args.n)
+    N = args.n
+    keys = ("xsrc", "ysrc", "xtar", "ytar", "f1", "f2", "n1", "n2")
+    dev = {k: torch.tensor(cfg[k], dtype=torch.float64, device="cuda") for k in keys}
+    outs = [torch.empty(N, dtype=torch.float64, device="cuda") for _ in range(4)]
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
+
+    def step(tol, form, arrays=None, out=None):
+        a = arrays or dev
+        o = out or outs
+        ft.StokesSLP_ewald_2p(a["xsrc"], a["ysrc"], a["xtar"], a["ytar"], a["f1"], a["f2"], 1.0, 1.0, tol=tol,
+                              form=form, ctx=ctx, out=(o[0], o[1]), parts=False)
+        ft.StokesDLP_ewald_2p(a["xsrc"], a["ysrc"], a["xtar"], a["ytar"], a["n1"], a["n2"], a["f1"], a["f2"], 1.0,
+                              1.0, tol=tol, form=form, ctx=ctx, out=(o[2], o[3]), parts=False)
+
+    def timed(tol, form, steps, arrays=None, out=None, flush_l2=True):
+        """Mean device time per step (CUDA events on the library's stream),
+        L2 flushed before every step outside the timed events."""
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        k0 = ctx.kernel_count
+        barrier()
+        torch.cuda.synchronize()
+        for i in range(steps):
+            if flush_l2:
+                flush.fill_(float(i))
+            ev[i][0].record(stream)
+            step(tol, form, arrays, out)
+            ev[i][1].record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        ms = sum(a.elapsed_time(b) for a, b in ev) / steps
+        return max_over_ranks(ms), ctx.kernel_count - k0
+
+    forms = {"plain": ft.FORM_PLAIN}
+    try:
+        # the mixed-precision form is reported when this build provides it
+        ft.StokesSLP_ewald_2p(cfg["xsrc"][:64], cfg["ysrc"][:64], cfg["xtar"][:64], cfg["ytar"][:64],
+                              cfg["f1"][:64], cfg["f2"][:64], 1.0, 1.0, tol=1e-6, form=ft.FORM_MIXED, ctx=ctx)
+        forms["mixed"] = ft.FORM_MIXED
+    except ft.FteError:
+        pass
+
+    truth = None
+    tpath = os.path.join(ROOT, "tests", "golden", "truth_config3.npz")
+    if N == 1_000_000 and os.path.exists(tpath):
+        z = np.load(tpath)
+        truth = {k: z[k] for k in z.files}
+        ck = wl.checksum(*(cfg[k] for k in keys))
+        if abs(ck - float(truth["checksum"])) > 1e-9 * abs(float(truth["checksum"])):
+            truth = None  # regenerated inputs differ: no error figures
+    idx_t = torch.tensor(truth["idx"], device="cuda") if truth is not None else None
+
+    def errors():
+        if truth is None:
+            return None
+        res = {}
+        for name, (a, b) in (("slp", (outs[0], outs[1])), ("dlp", (outs[2], outs[3]))):
+            u = torch.stack([a[idx_t], b[idx_t]], 1).cpu().numpy()
+            t = truth[name]
+            d = np.abs(u - t)
+            res[name] = {"max_rel": float(d.max() / np.abs(t).max()),
+                         "rms_rel": float(np.sqrt((d ** 2).sum() / (t ** 2).sum()))}
+        return res
+
+    results = {}
+    tols = [1e-10] if args.quick else [1e-10, 1e-6]
+    # warm up every variant (plans, workspaces)
+    for form in forms.values():
+        for tol in tols:
+            for _ in range(args.warmup):
+                step(tol, form)
+    torch.cuda.synchronize()
+
+    clocks = ClockSampler(local_rank)
+    headline_form = "mixed" if "mixed" in forms else "plain"
+    for fname, form in forms.items():
+        for tol in tols:
+            is_head = (fname == headline_form and tol == 1e-10)
+            if is_head:
+                clocks.start()
+            ms, launches = timed(tol, form, args.steps)
+            clk = clocks.stop() if is_head else None
+            err = errors()
+            results[(fname, tol)] = {"ms": ms, "launches": launches, "targets_per_s": world * N / (ms / 1e3),
+                                     "err": err, "clocks": clk}
+
+    # per-stage timings of the headline form (separate pass, events inside the library)
+    ctx.set_timing(True)
+    stage = {"near": [], "spread": [], "fft": [], "gather": [], "cells": [], "total": []}
+    info_params = {}
+    for _ in range(max(3, min(args.steps, 5))):
+        for kind in (ft.KIND_SLP, ft.KIND_DLP):
+            fn = ft.StokesSLP_ewald_2p if kind == ft.KIND_SLP else ft.StokesDLP_ewald_2p
+            a = dev
+            extra = (a["n1"], a["n2"]) if kind == ft.KIND_DLP else ()
+            (_, info) = fn(a["xsrc"], a["ysrc"], a["xtar"], a["ytar"], *extra, a["f1"], a["f2"], 1.0, 1.0, tol=1e-10,
+                           form=forms[headline_form], ctx=ctx, out=(outs[0], outs[1]), parts=False,
+                           return_info=True)
+            key = "slp" if kind == ft.KIND_SLP else "dlp"
+            info_params[key] = info.params.as_dict()
+            for s, v in (("near", info.ms_near), ("spread", info.ms_spread), ("fft", info.ms_fft),
+                         ("gather", info.ms_gather), ("cells", info.ms_cells), ("total", info.ms_total)):
+                stage[s].append((key, v))
+    ctx.set_timing(False)
+
+    def mean_stage(s, key):
+        v = [x for k, x in stage[s] if k == key]
+        return float(np.mean(v)) if v else 0.0
+
+    # e2e: the same public API on pinned host buffers (H2D of inputs and D2H of
+    # the velocities inside the timed region)
+    pin = {k: torch.from_numpy(cfg[k]).pin_memory() for k in keys}
+    hin = {k: v.numpy() for k, v in pin.items()}
+    hout = [torch.empty(N, dtype=torch.float64).pin_memory().numpy() for _ in range(4)]
+    for _ in range(2):
+        step(1e-10, forms[headline_form], hin, hout)
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step(1e-10, forms[headline_form], hin, hout)
+    torch.cuda.synchronize()
+    barrier()
+    e2e_ms = max_over_ranks((time.perf_counter() - t0) / args.steps * 1e3)
+    h2d = 8 * N * (6 + 8)  # SLP: xs, ys, xt, yt, f1, f2 ; DLP: + n1, n2
+    d2h = 8 * N * 4
+
+    head = results[(headline_form, 1e-10)]
+    # roofline of the dominant kernel (the real-space sum): algorithmic bytes
+    # per launch = sorted sources (position + densities) and targets (position,
+    # index, output) read/written once.
+    near_ms = {k: mean_stage("near", k) for k in ("slp", "dlp")}
+    bytes_near = {"slp": N * (16 + 16) + N * (16 + 4 + 16), "dlp": N * (16 + 24) + N * (16 + 4 + 16)}
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    hbm_peak, peak_src = 6800.0, "fallback"
+    if os.path.exists(peaks_path):
+        hbm_peak, peak_src = float(json.load(open(peaks_path))["hbm_gbs"]), "measured"
+    dom = "dlp" if near_ms["dlp"] > near_ms["slp"] else "slp"
+    achieved = bytes_near[dom] / (near_ms[dom] / 1e3) / 1e9 if near_ms[dom] > 0 else 0.0
+    traffic = None
+    tr_path = os.path.join(ROOT, "profiles", "roofline_traffic.json")
+    if os.path.exists(tr_path):
+        traffic = json.load(open(tr_path)).get(f"near_{dom}_bytes_per_launch_1M")
+
+    line = {
+        "metric": METRIC, "value": head["targets_per_s"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": head["ms"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if headline_form == "plain" else "f64/f32", "data": "synthetic",
+        "config": {"workload": f"config3: SLP+DLP spectral Ewald, {N} sources / {N} targets uniform in [0,1]^2, "
+                               f"zero-mean N(0,1) densities, random unit normals, tol 1e-10, {headline_form} form",
+                   "l2": "flushed before every step (256 MB write, outside the timed events)",
+                   "parallelism": f"replicas x{world}", "params": info_params},
+        "forms": {f"{f}@{t:g}": {"targets_per_s": r["targets_per_s"], "ms_per_step": r["ms"], "err": r["err"]}
+                  for (f, t), r in results.items()},
+        "stages_ms": {k: {s: mean_stage(s, k) for s in stage} for k in ("slp", "dlp")},
+        "e2e": {"value": world * N / (e2e_ms / 1e3), "unit": UNIT, "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": head["launches"],
+        "roofline": {"bound": "hbm", "kernel": f"k_near<{dom.upper()}>", "achieved": achieved, "peak": hbm_peak,
+                     "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
+                     "peak_source": peak_src,
+                     "note": "FP64-ALU-bound kernel; HBM fraction reported as required, see fp64 pipe figures"},
+        "clocks": head["clocks"],
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(N)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -210,7 +210,21 @@ class _Args:
         self.keep.append(x)
         return x.ctypes.data, x.size // ncomp
 
-    def out(self, shape):
+    def out(self, shape, given=None):
+        if given is not None:
+            if _is_cuda_tensor(given) != bool(self.device):
+                raise ValueError("output buffer on the wrong side")
+            if tuple(given.shape) != tuple(shape):
+                raise ValueError(f"output buffer has shape {tuple(given.shape)}, expected {tuple(shape)}")
+            if _is_cuda_tensor(given):
+                import torch
+
+                if given.dtype != torch.float64 or not given.is_contiguous():
+                    raise ValueError("output buffer must be contiguous float64")
+                return given, given.data_ptr()
+            if given.dtype != np.float64 or not given.flags["C_CONTIGUOUS"]:
+                raise ValueError("output buffer must be contiguous float64")
+            return given, given.ctypes.data
         if self.device:
             import torch
 
@@ -321,45 +335,8 @@ def _print_verbose(kind: str, ns: int, nt: int, info: Info):
     print("*********************************************************\n")
 
 
-def StokesSLP_ewald_2p(xsrc, ysrc, xtar, ytar, f1, f2, Lx, Ly, P=24, Nb=None, tol=1e-16, verbose=0,
-                       weights=None, xi=None, Mx=None, My=None, nside_x=None, nside_y=None, form=FORM_PLAIN,
-                       ctx: Context | None = None, return_info: bool = False):
-    """Spectral Ewald evaluation of the doubly-periodic Stokeslet.
-
-    Returns (u1, u2, ur, uk, xi) like the MATLAB driver; ur and uk are (Ntar, 2).
-    """
-    ctx = ctx or default_context()
-    A = _Args()
-    pxs, ns = A.arr(xsrc, 1)
-    pys, _ = A.arr(ysrc, 1)
-    pxt, nt = A.arr(xtar, 1)
-    pyt, _ = A.arr(ytar, 1)
-    pf1, _ = A.arr(f1, 1)
-    pf2, _ = A.arr(f2, 1)
-    pw, _ = A.arr(weights, 1)
-    u1, pu1 = A.out((nt,))
-    u2, pu2 = A.out((nt,))
-    ur, pur = A.out((nt, 2))
-    uk, puk = A.out((nt, 2))
-    opt = _options(P, Nb, tol, xi, Mx, My, nside_x, nside_y, pw, form)
-    info = Info()
-    if verbose:
-        ctx.set_timing(True)
-    _check(lib().fte_stokes_slp_ewald_2p(ctx.h, pxs, pys, ns, pxt, pyt, nt, pf1, pf2, float(Lx), float(Ly),
-                                         C.byref(opt), pu1, pu2, pur, puk, C.byref(info), A.flags))
-    if verbose:
-        _print_verbose("SINGLE-LAYER", ns, nt, info)
-    out = (u1, u2, ur, uk, info.params.xi)
-    return (out, info) if return_info else out
-
-
-def StokesDLP_ewald_2p(xsrc, ysrc, xtar, ytar, n1, n2, f1, f2, Lx, Ly, P=24, Nb=None, tol=1e-16, verbose=0,
-                       weights=None, xi=None, Mx=None, My=None, nside_x=None, nside_y=None, form=FORM_PLAIN,
-                       ctx: Context | None = None, return_info: bool = False):
-    """Spectral Ewald evaluation of the doubly-periodic stresslet (double layer).
-
-    Returns (u1, u2, ur, uk, xi); uk includes the k = 0 mode like the MATLAB driver.
-    """
+def _ewald(kind, xsrc, ysrc, xtar, ytar, n1, n2, f1, f2, Lx, Ly, P, Nb, tol, verbose, weights, xi, Mx, My,
+           nside_x, nside_y, form, ctx, return_info, out, parts):
     ctx = ctx or default_context()
     A = _Args()
     pxs, ns = A.arr(xsrc, 1)
@@ -371,20 +348,53 @@ def StokesDLP_ewald_2p(xsrc, ysrc, xtar, ytar, n1, n2, f1, f2, Lx, Ly, P=24, Nb=
     pf1, _ = A.arr(f1, 1)
     pf2, _ = A.arr(f2, 1)
     pw, _ = A.arr(weights, 1)
-    u1, pu1 = A.out((nt,))
-    u2, pu2 = A.out((nt,))
-    ur, pur = A.out((nt, 2))
-    uk, puk = A.out((nt, 2))
+    u1, pu1 = A.out((nt,), out[0] if out is not None else None)
+    u2, pu2 = A.out((nt,), out[1] if out is not None else None)
+    ur = uk = None
+    pur = puk = None
+    if parts:
+        ur, pur = A.out((nt, 2))
+        uk, puk = A.out((nt, 2))
     opt = _options(P, Nb, tol, xi, Mx, My, nside_x, nside_y, pw, form)
     info = Info()
     if verbose:
         ctx.set_timing(True)
-    _check(lib().fte_stokes_dlp_ewald_2p(ctx.h, pxs, pys, ns, pxt, pyt, nt, pn1, pn2, pf1, pf2, float(Lx),
-                                         float(Ly), C.byref(opt), pu1, pu2, pur, puk, C.byref(info), A.flags))
+    if kind == KIND_SLP:
+        st = lib().fte_stokes_slp_ewald_2p(ctx.h, pxs, pys, ns, pxt, pyt, nt, pf1, pf2, float(Lx), float(Ly),
+                                           C.byref(opt), pu1, pu2, pur, puk, C.byref(info), A.flags)
+    else:
+        st = lib().fte_stokes_dlp_ewald_2p(ctx.h, pxs, pys, ns, pxt, pyt, nt, pn1, pn2, pf1, pf2, float(Lx),
+                                           float(Ly), C.byref(opt), pu1, pu2, pur, puk, C.byref(info), A.flags)
+    _check(st)
     if verbose:
-        _print_verbose("DOUBLE-LAYER", ns, nt, info)
-    out = (u1, u2, ur, uk, info.params.xi)
-    return (out, info) if return_info else out
+        _print_verbose("SINGLE-LAYER" if kind == KIND_SLP else "DOUBLE-LAYER", ns, nt, info)
+    res = (u1, u2, ur, uk, info.params.xi)
+    return (res, info) if return_info else res
+
+
+def StokesSLP_ewald_2p(xsrc, ysrc, xtar, ytar, f1, f2, Lx, Ly, P=24, Nb=None, tol=1e-16, verbose=0,
+                       weights=None, xi=None, Mx=None, My=None, nside_x=None, nside_y=None, form=FORM_PLAIN,
+                       ctx: Context | None = None, return_info: bool = False, out=None, parts: bool = True):
+    """Spectral Ewald evaluation of the doubly-periodic Stokeslet.
+
+    Returns (u1, u2, ur, uk, xi) like the MATLAB driver; ur and uk are
+    (Ntar, 2) (None when parts=False).  ``out=(u1, u2)`` supplies the output
+    buffers (same side as the inputs).
+    """
+    return _ewald(KIND_SLP, xsrc, ysrc, xtar, ytar, None, None, f1, f2, Lx, Ly, P, Nb, tol, verbose, weights, xi, Mx,
+                  My, nside_x, nside_y, form, ctx, return_info, out, parts)
+
+
+def StokesDLP_ewald_2p(xsrc, ysrc, xtar, ytar, n1, n2, f1, f2, Lx, Ly, P=24, Nb=None, tol=1e-16, verbose=0,
+                       weights=None, xi=None, Mx=None, My=None, nside_x=None, nside_y=None, form=FORM_PLAIN,
+                       ctx: Context | None = None, return_info: bool = False, out=None, parts: bool = True):
+    """Spectral Ewald evaluation of the doubly-periodic stresslet (double layer).
+
+    Returns (u1, u2, ur, uk, xi); uk includes the k = 0 mode like the MATLAB
+    driver.  Options as for StokesSLP_ewald_2p.
+    """
+    return _ewald(KIND_DLP, xsrc, ysrc, xtar, ytar, n1, n2, f1, f2, Lx, Ly, P, Nb, tol, verbose, weights, xi, Mx,
+                  My, nside_x, nside_y, form, ctx, return_info, out, parts)
 
 
 def choose_params(kind, f1, f2, ntar, Lx, Ly, P=24, Nb=None, tol=1e-16, **kw) -> Params:
