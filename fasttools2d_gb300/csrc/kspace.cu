@@ -24,6 +24,9 @@
 // of the multiplier at (k1, k2) and at the Nyquist-mirrored wave vector
 // (k1', k2') (k' = -k on a Nyquist index, k' = k elsewhere); this reproduces
 // real(ifft2(.)) of the full-grid reference exactly.
+#include <cmath>
+#include <mutex>
+
 #include "fft.cuh"
 #include "fte_internal.cuh"
 
@@ -393,5 +396,261 @@ int fte_kspace_run(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, fte_info
     }
     FTE_TRY(fte_record(ctx, 5));
     (void)info;
+    return FTE_OK;
+}
+
+// ===========================================================================
+// Stokeslet k-space sum without device allocation.
+//
+// Some callers cannot call cudaMalloc: solvers embedded in a host application
+// that owns every byte of device memory through its own pool, real-time loops
+// where an allocation (and the device synchronisation cudaMalloc/cudaFree can
+// imply) is not allowed after start-up, and plugins whose host forbids
+// allocation outside its initialisation phase.  fte_slp_kspace_noalloc serves
+// them: it computes exactly what fte_slp_kspace computes, but takes every
+// byte of scratch (the two real grids, their half spectra and the FFT tables)
+// from one file-scope device array of fixed size instead of a context
+// workspace.  The caller passes device pointers to the inputs and the output
+// and a stream; nothing is allocated on the device or the host.
+//
+// Limits: Mx, My <= FTE_NOALLOC_MAX_SIDE (512) and Mx*My <= FTE_NOALLOC_MAX_NODES
+// (512*512); larger grids are rejected with FTE_ERR_UNSUPPORTED.  The array
+// (about 8.5 MB) stays resident on every GPU that loads the library until the
+// process exits.  All calls share it and it keeps the previous call's
+// contents, so calls that overlap on the GPU (different streams, or different
+// host threads on one device) race and must be serialised by the caller.
+// ===========================================================================
+namespace {
+
+constexpr long kNaMaxSide = FTE_NOALLOC_MAX_SIDE;
+constexpr long kNaMaxNodes = FTE_NOALLOC_MAX_NODES;
+constexpr long kNaMaxFft = 1024;  // inner FFT length for any side <= 512 (7-smooth m >= 2n-1)
+// doubles: 2 real grids, 2 half spectra (Mx (My/2+1) complex each), and per
+// direction the twiddle, chirp and Bluestein tables (complex, <= kNaMaxFft each)
+constexpr long kNaGrid = 2 * kNaMaxNodes;
+constexpr long kNaSpec = 2 * 2 * (kNaMaxNodes / 2 + kNaMaxSide);
+constexpr long kNaTables = 2 * 3 * 2 * kNaMaxFft;
+constexpr long kNaDoubles = kNaGrid + kNaSpec + kNaTables;
+
+static __device__ __align__(256) double g_fte_noalloc_scratch[kNaDoubles];
+
+// Device address of the array per device ordinal, looked up once per device.
+std::mutex g_na_mu;
+double* g_na_ptr[256] = {nullptr};
+
+int na_scratch(double** out) {
+    int dev = 0;
+    FTE_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 256) {
+        fte_set_error("fte_slp_kspace_noalloc: device ordinal %d out of range", dev);
+        return FTE_ERR_UNSUPPORTED;
+    }
+    std::lock_guard<std::mutex> lk(g_na_mu);
+    if (!g_na_ptr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_fte_noalloc_scratch);
+        if (e != cudaSuccess || p == nullptr) {
+            fte_set_error("fte_slp_kspace_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+            return FTE_ERR_CUDA;
+        }
+        g_na_ptr[dev] = static_cast<double*>(p);
+    }
+    *out = g_na_ptr[dev];
+    return FTE_OK;
+}
+
+// radices of a 7-smooth length (8s first), no heap
+bool na_radices(int n, int* rad, int* nrad) {
+    int c2 = 0, c3 = 0, c5 = 0, c7 = 0, v = n;
+    while (v % 2 == 0) { v /= 2; c2++; }
+    while (v % 3 == 0) { v /= 3; c3++; }
+    while (v % 5 == 0) { v /= 5; c5++; }
+    while (v % 7 == 0) { v /= 7; c7++; }
+    if (v != 1) return false;
+    int k = 0;
+    for (; c2 >= 3; c2 -= 3) rad[k++] = 8;
+    if (c2 == 2) rad[k++] = 4;
+    if (c2 == 1) rad[k++] = 2;
+    for (int i = 0; i < c3; i++) rad[k++] = 3;
+    for (int i = 0; i < c5; i++) rad[k++] = 5;
+    for (int i = 0; i < c7; i++) rad[k++] = 7;
+    *nrad = k;
+    return k <= 24;
+}
+
+// FFT plan of length n with its tables at `tab` (3 * kNaMaxFft complex).
+bool na_plan(int n, double2* tab, FftDev* p) {
+    int rad[32], nrad = 0;
+    p->n = n;
+    if (na_radices(n, rad, &nrad)) {
+        p->bluestein = 0;
+        p->m = n;
+    } else {
+        int m = 2 * n - 1;
+        while (!na_radices(m, rad, &nrad)) m++;
+        p->bluestein = 1;
+        p->m = m;
+    }
+    if (p->m > kNaMaxFft) return false;
+    p->nrad = nrad;
+    for (int i = 0; i < 24; i++) p->rad[i] = i < nrad ? rad[i] : 0;
+    p->tw = tab;
+    p->chirp = tab + kNaMaxFft;
+    p->bhat = tab + 2 * kNaMaxFft;
+    p->tw32 = nullptr;
+    p->chirp32 = nullptr;
+    p->bhat32 = nullptr;
+    return true;
+}
+
+// twiddles exp(-2 pi i t/m) and the chirp exp(-i pi k^2/n), from sincospi
+__global__ void k_na_tables(double2* tw, double2* chirp, int n, int m, int bluestein) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < m; t += gridDim.x * blockDim.x) {
+        double s, c;
+        if (2 * t <= m)
+            sincospi(-2.0 * (double)t / (double)m, &s, &c);
+        else
+            sincospi(2.0 * (double)(m - t) / (double)m, &s, &c);
+        tw[t] = make_double2(c, s);
+        if (bluestein && t < n) {
+            long long k2 = ((long long)t * t) % (2LL * n);
+            sincospi(-(double)k2 / (double)n, &s, &c);
+            chirp[t] = make_double2(c, s);
+        }
+    }
+}
+
+// Bluestein kernel: DFT_m of the wrapped conjugate chirp, divided by m
+__global__ void k_na_bhat(FftDev p, double2* bhat) {
+    extern __shared__ double2 shc[];
+    double2* A = shc;
+    double2* B = shc + p.m;
+    for (int k = threadIdx.x; k < p.m; k += blockDim.x) {
+        double2 v = make_double2(0.0, 0.0);
+        int j = k < p.n ? k : (k > p.m - p.n ? p.m - k : -1);
+        if (j >= 0) {
+            double2 c = p.chirp[j];
+            v = make_double2(c.x, -c.y);
+        }
+        A[k] = v;
+    }
+    double2* R = fft_inner<double>(A, B, p, false);
+    double inv = 1.0 / p.m;
+    for (int k = threadIdx.x; k < p.m; k += blockDim.x) bhat[k] = make_double2(R[k].x * inv, R[k].y * inv);
+}
+
+#define NA_LAUNCH(kernel, grid, block, smem, stream, ...)                                          \
+    do {                                                                                           \
+        kernel<<<(grid), (block), (smem), (stream)>>>(__VA_ARGS__);                                \
+        cudaError_t e_ = cudaGetLastError();                                                       \
+        if (e_ != cudaSuccess) {                                                                   \
+            fte_set_error("fte_slp_kspace_noalloc: launch of %s failed: %s", #kernel,              \
+                          cudaGetErrorString(e_));                                                 \
+            return FTE_ERR_CUDA;                                                                   \
+        }                                                                                          \
+    } while (0)
+
+}  // namespace
+
+extern "C" int fte_slp_kspace_noalloc(const double* psrc, int64_t nsrc, const double* ptar, int64_t ntar, double xi,
+                                      double eta, const double* f, int Mx, int My, double Lx, double Ly, double w,
+                                      int P, double* uk, void* stream_handle) {
+    cudaStream_t stream = (cudaStream_t)stream_handle;
+    if (nsrc < 0 || ntar < 0 || nsrc > 2000000000LL || ntar > 2000000000LL) {
+        fte_set_error("fte_slp_kspace_noalloc: point counts out of range");
+        return FTE_ERR_INVALID;
+    }
+    if ((nsrc > 0 && (!psrc || !f)) || (ntar > 0 && (!ptar || !uk))) {
+        fte_set_error("fte_slp_kspace_noalloc: null array argument");
+        return FTE_ERR_INVALID;
+    }
+    if (!(Lx > 0) || !(Ly > 0) || !isfinite(Lx) || !isfinite(Ly) || !(xi > 0) || !isfinite(xi) || !(eta > 0) ||
+        !isfinite(eta) || !isfinite(w)) {
+        fte_set_error("fte_slp_kspace_noalloc: Lx, Ly, xi, eta must be positive and finite, w finite");
+        return FTE_ERR_INVALID;
+    }
+    if (P < 2 || P % 2 != 0 || P > 64) {
+        fte_set_error("fte_slp_kspace_noalloc: window support P must be even and in [2, 64] (P=%d)", P);
+        return FTE_ERR_INVALID;
+    }
+    if (Mx < 2 || My < 2 || Mx % 2 || My % 2) {
+        fte_set_error("fte_slp_kspace_noalloc: grid sizes must be even and >= 2 (Mx=%d, My=%d)", Mx, My);
+        return FTE_ERR_INVALID;
+    }
+    double hx = Lx / Mx, hy = Ly / My;
+    if (fabs(hx - hy) > 1e-12 * fmax(hx, hy)) {
+        fte_set_error("fte_slp_kspace_noalloc: grid spacing must be equal in x and y");
+        return FTE_ERR_INVALID;
+    }
+    if (Mx > kNaMaxSide || My > kNaMaxSide || (long)Mx * My > kNaMaxNodes) {
+        fte_set_error("fte_slp_kspace_noalloc: grid %d x %d exceeds the fixed scratch (sides <= %ld, Mx*My <= %ld); "
+                      "use fte_slp_kspace",
+                      Mx, My, kNaMaxSide, kNaMaxNodes);
+        return FTE_ERR_UNSUPPORTED;
+    }
+    double* base = nullptr;
+    FTE_TRY(na_scratch(&base));
+    const int Kh = My / 2 + 1;
+    const size_t G = (size_t)Mx * My;
+    double* H = base;                                           // 2 real grids
+    double2* Hh = reinterpret_cast<double2*>(base + kNaGrid);   // 2 half spectra
+    double2* tab = reinterpret_cast<double2*>(base + kNaGrid + kNaSpec);
+    FftDev py, px;
+    if (!na_plan(My, tab, &py) || !na_plan(Mx, tab + 3 * kNaMaxFft, &px)) {
+        fte_set_error("fte_slp_kspace_noalloc: FFT length beyond the fixed tables");
+        return FTE_ERR_UNSUPPORTED;
+    }
+    // FFT tables of this call's sizes (the previous call may have used others)
+    NA_LAUNCH(k_na_tables, 4, 256, 0, stream, const_cast<double2*>(py.tw), const_cast<double2*>(py.chirp), My, py.m,
+              py.bluestein);
+    NA_LAUNCH(k_na_tables, 4, 256, 0, stream, const_cast<double2*>(px.tw), const_cast<double2*>(px.chirp), Mx, px.m,
+              px.bluestein);
+    if (py.bluestein)
+        NA_LAUNCH(k_na_bhat, 1, fft_threads(py.m), 2 * py.m * sizeof(double2), stream, py,
+                  const_cast<double2*>(py.bhat));
+    if (px.bluestein)
+        NA_LAUNCH(k_na_bhat, 1, fft_threads(px.m), 2 * px.m * sizeof(double2), stream, px,
+                  const_cast<double2*>(px.bhat));
+    // the spread accumulates with atomics: the grids must start at zero
+    FTE_CUDA_TRY(cudaMemsetAsync(H, 0, sizeof(double) * 2 * G, stream));
+    WinParams wp;
+    wp.Lx = Lx;
+    wp.Ly = Ly;
+    wp.h = Lx / Mx;
+    wp.xi = xi;
+    wp.eta = eta;
+    wp.w = w;
+    wp.P = P;
+    wp.Mx = Mx;
+    wp.My = My;
+    const int P1 = P + 1;
+    const size_t sm_pt = (size_t)(((P1 + 1) & ~1) + kPtThreads * P1) * sizeof(double);
+    const size_t sm_y = 2 * (size_t)py.m * sizeof(double2), sm_x = 2 * (size_t)px.m * sizeof(double2);
+    auto blocks = [](int64_t n) {
+        int64_t b = (n + kPtThreads - 1) / kPtThreads;
+        return (int)(b < 1 ? 1 : (b > 4096 ? 4096 : b));
+    };
+    // The dynamic shared-memory ceiling is a per-kernel attribute that other
+    // entries set to their own sizes; raise it to what these launches need.
+    FTE_CUDA_TRY(cudaFuncSetAttribute(k_spread<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_pt));
+    FTE_CUDA_TRY(cudaFuncSetAttribute(k_gather, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_pt));
+    FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_y_r2c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_y));
+    FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_y_c2r, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_y));
+    FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_x));
+    if (nsrc > 0)
+        NA_LAUNCH(k_spread<2>, blocks(nsrc), kPtThreads, sm_pt, stream, psrc, f, (const double*)nullptr,
+                  (const double*)nullptr, nsrc, wp, H);
+    NA_LAUNCH(k_fft_y_r2c, dim3(Mx / 2, 2), fft_threads(py.m), sm_y, stream, (const double*)H, Hh, Mx, My, py);
+    NA_LAUNCH(k_fft_x, dim3(Kh, 2), fft_threads(px.m), sm_x, stream, Hh, Mx, Kh, px, 0);
+    int fb = (int)(((size_t)Mx * Kh + 255) / 256);
+    NA_LAUNCH(k_filter<FTE_KIND_SLP>, fb, 256, 0, stream, Hh, Mx, My, Lx, Ly, xi, eta);
+    NA_LAUNCH(k_fft_x, dim3(Kh, 2), fft_threads(px.m), sm_x, stream, Hh, Mx, Kh, px, 1);
+    NA_LAUNCH(k_fft_y_c2r, dim3(Mx / 2, 2), fft_threads(py.m), sm_y, stream, (const double2*)Hh, H, Mx, My, py);
+    double s = 4 * xi * xi / eta;
+    s = s * s * wp.h * wp.h / FTE_PI;
+    double scale = s / (4 * FTE_PI) / ((double)Mx * (double)My);
+    if (ntar > 0)
+        NA_LAUNCH(k_gather, blocks(ntar), kPtThreads, sm_pt, stream, ptar, ntar, wp, (const double*)H,
+                  (const double*)(H + G), scale, reinterpret_cast<double2*>(uk));
     return FTE_OK;
 }

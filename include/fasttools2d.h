@@ -150,6 +150,29 @@ int fte_stokes_dlp_ewald_2p(fte_context* ctx, const double* xsrc, const double* 
 int fte_choose_params(int kind, int64_t nsrc, int64_t ntar, const double* f1, const double* f2, double Lx,
                       double Ly, const fte_options* opt, fte_params* out);
 
+/* ---- allocation-free variant --------------------------------------------- */
+/* No counterpart in the reference.  The Stokeslet k-space sum of
+ * fte_slp_kspace (same arguments and results) for callers that may not
+ * allocate device memory: an application that hands all GPU memory to its own
+ * pool, a real-time loop that must not allocate (or risk the implicit
+ * synchronisation of cudaMalloc/cudaFree) after start-up, a plugin host that
+ * forbids allocation outside initialisation.  It needs no context: every
+ * pointer is a device pointer, `stream` is a cudaStream_t (NULL = default
+ * stream), and all scratch (grids, spectra, FFT tables) lives in one fixed
+ * device array of about 8.5 MB that the library holds on each GPU that loads
+ * it until the process exits.  The grid is limited to
+ * Mx, My <= FTE_NOALLOC_MAX_SIDE and Mx*My <= FTE_NOALLOC_MAX_NODES; larger
+ * grids return FTE_ERR_UNSUPPORTED.  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress), so make that first call
+ * before any stream capture.  Calls share the array: calls that overlap on the
+ * GPU (other streams, other threads on the same device) race and must be
+ * serialised by the caller.  The call is asynchronous on `stream`. */
+#define FTE_NOALLOC_MAX_SIDE 512
+#define FTE_NOALLOC_MAX_NODES (512 * 512)
+int fte_slp_kspace_noalloc(const double* psrc, int64_t nsrc, const double* ptar, int64_t ntar, double xi,
+                           double eta, const double* f, int Mx, int My, double Lx, double Ly, double w, int P,
+                           double* uk, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
