@@ -17,6 +17,13 @@ in the interval-local variable t in [-1, 1] for Horner evaluation:
 The piece for x >= 1 is selected from the binary exponent k and the top two
 mantissa bits q of x.  For x >= 1024, E1(x) < 1e-447 underflows to 0.
 
+The Stokeslet real-space weight 0.5 E1(x) - exp(-x) is evaluated for x >= 1 as
+exp(-x) K(x) with K(x) = 0.5 e^x E1(x) - 1 on eighth-octave pieces (80 pieces,
+degree 10).  exp(-x) itself is evaluated from 2^(-n/64) (a 64-entry table),
+n = round(64 x / ln 2), times the degree-6 Taylor polynomial of exp(-r),
+r = x - n ln2/64 (Cody-Waite split of ln2/64); this header holds the table and
+the constants.
+
 Run:  python fasttools2d_gb300/csrc/gen_e1_coeffs.py   (needs mpmath; the
 generated header is committed so the build does not.)
 """
@@ -27,6 +34,7 @@ import mpmath as mp
 mp.mp.dps = 60
 DEG_R = 11
 DEG_G = 12
+DEG_K = 10
 
 
 def cheb_fit(fun, a, b, deg):
@@ -69,6 +77,10 @@ def g_fun(x):
     return x * mp.exp(x) * mp.e1(x)
 
 
+def k_fun(x):
+    return mp.exp(x) * mp.e1(x) / 2 - 1
+
+
 def horner(mono, t):
     acc = mp.mpf(0)
     for a in reversed(mono):
@@ -107,10 +119,48 @@ def main():
             out.append("    {" + ", ".join(mp.nstr(v, 20, min_fixed=-1, max_fixed=-1) for v in m) + "},")
     out.append("};")
     out.append(f"/* worst relative truncation error of the G pieces: {worst:.3e} */")
+
+    # K(x) = 0.5 e^x E1(x) - 1 on eighth-octave pieces of [1, 1024): the
+    # Stokeslet real-space weight 0.5 E1(x) - e^-x equals e^-x K(x).
+    out.append(f"#define FTE_K_DEG {DEG_K}")
+    out.append("#define FTE_K_NPIECE 80")
+    out.append("/* K(x) = 0.5 e^x E1(x) - 1 on [2^k (1 + q/8), 2^k (1 + (q+1)/8)), k = 0..9, q = 0..7;")
+    out.append(" * t = (x - mid)/half */")
+    out.append("FTE_E1_STORAGE_G double fte_k_coef[FTE_K_NPIECE][FTE_K_DEG + 1] = {")
+    worst_k = 0.0
+    for k in range(10):
+        for q in range(8):
+            a = mp.mpf(2) ** k * (1 + mp.mpf(q) / 8)
+            b = mp.mpf(2) ** k * (1 + mp.mpf(q + 1) / 8)
+            c = cheb_fit(k_fun, a, b, DEG_K)
+            m = cheb_to_mono(c)
+            mid, half = (a + b) / 2, (b - a) / 2
+            e = max(abs(horner(m, (x - mid) / half) / k_fun(x) - 1) for x in [a + (b - a) * i / 99 for i in range(100)])
+            worst_k = max(worst_k, float(e))
+            out.append("    {" + ", ".join(mp.nstr(v, 20, min_fixed=-1, max_fixed=-1) for v in m) + "},")
+    out.append("};")
+    out.append(f"/* worst relative truncation error of the K pieces: {worst_k:.3e} */")
+
+    # exp(-x) = 2^(-n/64) exp(-r): table 2^(-j/64), Cody-Waite split of ln2/64
+    # (the high part has 36 significant bits so n * hi is exact for n < 2^17),
+    # and the Taylor coefficients (-1)^k / k! of exp(-r), |r| <= ln2/128.
+    ln2_64 = mp.log(2) / 64
+    hi = mp.mpf(int(mp.nint(ln2_64 * mp.mpf(2) ** 42))) / mp.mpf(2) ** 42
+    lo = ln2_64 - hi
+    out.append("/* exp(-x) = 2^(-n/64) exp(-r), n = round(64 x / ln 2), r = x - n ln2/64 */")
+    out.append(f"#define FTE_EXP_INV_LN2_64 {mp.nstr(1 / ln2_64, 20, min_fixed=-1, max_fixed=-1)}")
+    out.append(f"#define FTE_EXP_LN2_64_HI {mp.nstr(hi, 20, min_fixed=-1, max_fixed=-1)}")
+    out.append(f"#define FTE_EXP_LN2_64_LO {mp.nstr(lo, 20, min_fixed=-1, max_fixed=-1)}")
+    out.append("FTE_E1_STORAGE_G double fte_exp_tab[64] = {")
+    out.append("    " + ", ".join(mp.nstr(mp.mpf(2) ** (-mp.mpf(j) / 64), 20, min_fixed=-1, max_fixed=-1)
+                                  for j in range(64)) + "};")
+    out.append("FTE_E1_STORAGE_R double fte_exp_poly[7] = {")
+    out.append("    " + ", ".join(mp.nstr(mp.mpf(-1) ** k / mp.factorial(k), 20, min_fixed=-1, max_fixed=-1)
+                                  for k in range(7)) + "};")
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "fte_e1_coeffs.h")
     with open(path, "w") as fh:
         fh.write("\n".join(out) + "\n")
-    print("wrote", path, "R err", float(err_r), "G worst rel err", worst)
+    print("wrote", path, "R err", float(err_r), "G worst rel err", worst, "K worst rel err", worst_k)
 
 
 if __name__ == "__main__":

@@ -30,6 +30,7 @@ constexpr int kNearThreads = 256;
 constexpr int kNearWarps = kNearThreads / 32;
 constexpr int kQueue = 64;
 constexpr int kGtab = FTE_E1_NPIECE_G * (FTE_E1_DEG_G + 1);
+constexpr int kKtab = FTE_K_NPIECE * (FTE_K_DEG + 1);
 
 struct NearParams {
     int nsx, nsy, nb;
@@ -41,7 +42,7 @@ struct NearParams {
     const int* __restrict__ tar_off;
     const double2* __restrict__ tpos;
     const int* __restrict__ tidx;
-    double Lx, Ly, xi, xi2, inv_xi2, selfc, cutoffsq;
+    double Lx, Ly, xi, xi2, inv_xi2, selfc, cutoffsq, pf;
     float cut32;
     int cap;
     double2* __restrict__ ur;
@@ -80,28 +81,90 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
+// exp(-x) for x >= 0 (0 beyond 700): 2^(-n/64) exp(-r) with n = round(64 x / ln 2),
+// r = x - n ln2/64 (Cody-Waite), exp(-r) by its degree-6 Taylor polynomial
+// (|r| <= ln2/128, truncation < 3e-20), 2^(-j/64) from a 64-entry table and
+// the power of two applied to the exponent field.  11 FP64 operations.
+__device__ __forceinline__ double fte_expm(double x, const double* __restrict__ tab) {
+    const double magic = 6755399441055744.0;  // 1.5 * 2^52
+    double t = fma(x, FTE_EXP_INV_LN2_64, magic);
+    double nd = t - magic;
+    int n = __double2loint(t);
+    double r = fma(nd, -FTE_EXP_LN2_64_HI, x);
+    r = fma(nd, -FTE_EXP_LN2_64_LO, r);
+    double p = fte_exp_poly[6];
+#pragma unroll
+    for (int k = 5; k >= 0; k--) p = fma(p, r, fte_exp_poly[k]);
+    double v = p * tab[n & 63];
+    v = __hiloint2double(__double2hiint(v) - ((n >> 6) << 20), __double2loint(v));
+    return x > 700.0 ? 0.0 : v;
+}
+
+// 1/a from the FP32 hardware reciprocal and two Newton steps in FP64.
+__device__ __forceinline__ double fte_rcp(double a) {
+    float af = __double2float_rn(a);
+    float yf;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(yf) : "f"(af));
+    double y = (double)yf;
+    double e = fma(-a, y, 1.0);
+    y = fma(y, e, y);
+    e = fma(-a, y, 1.0);
+    return fma(y, e, y);
+}
+
+// K(x) = 0.5 e^x E1(x) - 1 for x >= 1 (eighth-octave pieces; a value marginally
+// below 1, from the FP32 classification, extrapolates the first piece).
+__device__ __forceinline__ double fte_kfun(double x, const double* __restrict__ ktab) {
+    long long bits = __double_as_longlong(x);
+    int e = (int)(bits >> 52) - 1023;
+    int q = (int)((bits >> 49) & 7);
+    double mant = __longlong_as_double((bits & 0x000FFFFFFFFFFFFFLL) | 0x3FF0000000000000LL);
+    if (e < 0) {
+        e = 0;
+        q = 0;
+        mant = x;
+    } else if (e > 9) {  // exp(-x) underflows there; stay inside the table
+        e = 9;
+        q = 7;
+        mant = 2.0;
+    }
+    double mid = __longlong_as_double(0x3FF0000000000000LL | ((long long)q << 49) | (1LL << 48));
+    double t = (mant - mid) * 16.0;
+    const double* c = ktab + (8 * e + q) * (FTE_K_DEG + 1);
+    double k = c[FTE_K_DEG];
+#pragma unroll
+    for (int j = FTE_K_DEG - 1; j >= 0; j--) k = fma(k, t, c[j]);
+    return k;
+}
+
 template <int KIND>
-__global__ void __launch_bounds__(kNearThreads) k_near(const NearParams prm) {
+__global__ void __launch_bounds__(kNearThreads, 2) k_near(const NearParams prm) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int cap = prm.cap;
-    double* gtab = reinterpret_cast<double*>(smem_raw);
-    double* sx = gtab + kGtab;
+    double* ktab = reinterpret_cast<double*>(smem_raw);
+    double* etab = ktab + kKtab;
+    double* sx = etab + 64;
     double* sy = sx + cap;
     double* a0 = sy + cap;
     double* a1 = a0 + cap;
-    double* a2 = a1 + cap;  // DLP only (allocated for both)
-    float2* s32 = reinterpret_cast<float2*>(a2 + (KIND == FTE_KIND_DLP ? cap : 0));
+    double* a2 = a1 + cap;  // DLP only
+    double* a3 = a2 + (KIND == FTE_KIND_DLP ? cap : 0);  // DLP only
+    float2* s32 = reinterpret_cast<float2*>(a3 + (KIND == FTE_KIND_DLP ? cap : 0));
     int* qbuf = reinterpret_cast<int*>(s32 + cap);
     __shared__ int nb_box[9];
     __shared__ int nb_start[10];
     __shared__ double nb_shx[9], nb_shy[9];
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    int* myq = qbuf + warp * kQueue;
+    // per warp: queue 0 = pairs with x >= 1 (all DLP pairs), queue 1 = x < 1 (SLP)
+    int* qf = qbuf + warp * 2 * kQueue;
+    int* qn = qf + kQueue;
     const unsigned lt_mask = (1u << lane) - 1u;
     const double inv4pi = 1.0 / (4.0 * FTE_PI);
+    const float xi2f = (float)prm.xi2;
 
-    for (int i = tid; i < kGtab; i += kNearThreads) gtab[i] = (&fte_e1_coef_g[0][0])[i];
+    for (int i = tid; i < kKtab; i += kNearThreads) ktab[i] = (&fte_k_coef[0][0])[i];
+    for (int i = tid; i < 64; i += kNearThreads) etab[i] = fte_exp_tab[i];
 
     for (int b = blockIdx.x; b < prm.nb; b += gridDim.x) {
         const int t0 = prm.tar_off[b];
@@ -153,9 +216,17 @@ __global__ void __launch_bounds__(kNearThreads) k_near(const NearParams prm) {
                 double xs = p.x + nb_shx[e], ys = p.y + nb_shy[e];
                 sx[i] = xs;
                 sy[i] = ys;
-                a0[i] = prm.q0[si];
-                a1[i] = prm.q1[si];
-                if (KIND == FTE_KIND_DLP) a2[i] = prm.q2[si];
+                if (KIND == FTE_KIND_SLP) {
+                    a0[i] = prm.q0[si];
+                    a1[i] = prm.q1[si];
+                } else {
+                    // S11, (S12 + S21)/2, S22, S11 + S22
+                    double s11 = prm.q0[si], ssym = prm.q1[si], s22 = prm.q2[si];
+                    a0[i] = s11;
+                    a1[i] = 0.5 * ssym;
+                    a2[i] = s22;
+                    a3[i] = s11 + s22;
+                }
                 s32[i] = make_float2((float)(xs - cx), (float)(ys - cy));
             }
             __syncthreads();
@@ -165,66 +236,120 @@ __global__ void __launch_bounds__(kNearThreads) k_near(const NearParams prm) {
                 const double2 tp = prm.tpos[t0 + t];
                 const float tx32 = (float)(tp.x - cx), ty32 = (float)(tp.y - cy);
                 double acc0 = 0.0, acc1 = 0.0;
-                int qhead = 0, qcount = 0;
+                int hf = 0, cf = 0, hn = 0, cn = 0;  // ring heads and counts
 
-                auto eval = [&](int s) {
+                // Stokeslet pair (mex_stokes_slp_real.cpp:161-225 / 264-323):
+                //   u += (0.5 E1(x) - e^-x) f + e^-x (r.f) r / r^2,   x = xi^2 r^2
+                auto eval_slp = [&](int s, bool small_x) {
                     double dx = tp.x - sx[s], dy = tp.y - sy[s];
-                    double r2 = dx * dx + dy * dy;
+                    double r2 = fma(dx, dx, dy * dy);
                     bool own = s < own_lim;
-                    if (KIND == FTE_KIND_SLP) {
-                        double fx = a0[s], fy = a1[s];
-                        if (own && fabs(r2) < 1e-15) {
-                            acc0 += prm.selfc * fx;
-                            acc1 += prm.selfc * fy;
-                        } else if (own || r2 < prm.cutoffsq) {
-                            double x = r2 * prm.xi2;
-                            double emx = exp(-x);
-                            double ir2 = 1.0 / r2;
-                            double E = fte_e1(x, emx, ir2 * prm.inv_xi2, gtab);
-                            double g2 = emx * ir2;
-                            double hE = 0.5 * E;
-                            double dxy = dx * dy;
-                            acc0 += hE * fx + (dxy * fy - dy * dy * fx) * g2;
-                            acc1 += hE * fy + (dxy * fx - dx * dx * fy) * g2;
-                        }
-                    } else {
-                        if ((own && r2 != 0.0) || (!own && r2 < prm.cutoffsq)) {
-                            double s11 = a0[s], ssym = a1[s], s22 = a2[s];
-                            double e2 = exp(-prm.xi2 * r2);
-                            double ir2 = 1.0 / r2;
-                            double facb = -4.0 * (1.0 + prm.xi2 * r2) * ir2 * ir2;
-                            double Q = dx * dx * s11 + dx * dy * ssym + dy * dy * s22;
-                            double pf = 2.0 * prm.xi2;
-                            acc0 += e2 * (facb * dx * Q + pf * (3.0 * dx * s11 + dy * ssym + dx * s22));
-                            acc1 += e2 * (facb * dy * Q + pf * (dx * ssym + 3.0 * dy * s22 + dy * s11));
-                        }
+                    double fx = a0[s], fy = a1[s];
+                    if (own && fabs(r2) < 1e-15) {
+                        acc0 = fma(prm.selfc, fx, acc0);
+                        acc1 = fma(prm.selfc, fy, acc1);
+                        return;
                     }
+                    if (!own && !(r2 < prm.cutoffsq)) return;
+                    double x = r2 * prm.xi2;
+                    double emx = fte_expm(x, etab);
+                    double A;
+                    if (small_x) {
+                        double tt = fma(2.0, x, -1.0);
+                        double R = fte_e1_coef_r[FTE_E1_DEG_R];
+#pragma unroll
+                        for (int k = FTE_E1_DEG_R - 1; k >= 0; k--) R = fma(R, tt, fte_e1_coef_r[k]);
+                        double E = fma(x, R, -FTE_EULER - log(x));
+                        A = fma(0.5, E, -emx);
+                    } else {
+                        A = emx * fte_kfun(x, ktab);
+                    }
+                    double ir2 = fte_rcp(r2);
+                    double c = emx * ir2 * fma(dx, fx, dy * fy);
+                    acc0 = fma(A, fx, fma(c, dx, acc0));
+                    acc1 = fma(A, fy, fma(c, dy, acc1));
+                };
+                // stresslet pair (mex_stokes_dlp_real.cpp:117-138 / 162-181):
+                //   u_i += e^-x [ -4 (1+x) r_i (r.S.r)/r^4 + 2 xi^2 (f_i (r.n) + n_i (r.f) + (f.n) r_i) ]
+                auto eval_dlp = [&](int s) {
+                    double dx = tp.x - sx[s], dy = tp.y - sy[s];
+                    double r2 = fma(dx, dx, dy * dy);
+                    bool own = s < own_lim;
+                    if (own ? (r2 == 0.0) : !(r2 < prm.cutoffsq)) return;
+                    double x = r2 * prm.xi2;
+                    double e2 = fte_expm(x, etab);
+                    double ir2 = fte_rcp(r2);
+                    double facb = -4.0 * (1.0 + x) * ir2 * ir2;
+                    double s11 = a0[s], h = a1[s], s22 = a2[s], tr = a3[s];
+                    double u = fma(dx, s11, dy * h);  // (S r)_1 with S symmetrised
+                    double v = fma(dy, s22, dx * h);  // (S r)_2
+                    double Q = fma(dx, u, dy * v);    // r.S.r
+                    double fQ = facb * Q;
+                    double w1 = fma(dx, tr, u + u);   // f_1 (r.n) + n_1 (r.f) + (f.n) r_1
+                    double w2 = fma(dy, tr, v + v);
+                    acc0 = fma(e2, fma(fQ, dx, prm.pf * w1), acc0);
+                    acc1 = fma(e2, fma(fQ, dy, prm.pf * w2), acc1);
                 };
 
                 for (int base = 0; base < clen; base += 32) {
                     int s = base + lane;
-                    bool pass = false;
+                    bool pass = false, small_x = false;
                     if (s < clen) {
-                        if (s < own_lim) {
-                            pass = true;
-                        } else {
-                            float2 q = s32[s];
-                            float dx = q.x - tx32, dy = q.y - ty32;
-                            pass = dx * dx + dy * dy < prm.cut32;
+                        float2 q = s32[s];
+                        float dx = q.x - tx32, dy = q.y - ty32;
+                        float r2f = dx * dx + dy * dy;
+                        pass = (s < own_lim) || (r2f < prm.cut32);
+                        small_x = r2f * xi2f < 1.0f;
+                    }
+                    if (KIND == FTE_KIND_SLP) {
+                        bool pf_ = pass && !small_x, pn_ = pass && small_x;
+                        unsigned mf = __ballot_sync(0xffffffffu, pf_);
+                        unsigned mn = __ballot_sync(0xffffffffu, pn_);
+                        if (pf_) qf[(hf + cf + __popc(mf & lt_mask)) & (kQueue - 1)] = s;
+                        if (pn_) qn[(hn + cn + __popc(mn & lt_mask)) & (kQueue - 1)] = s;
+                        cf += __popc(mf);
+                        cn += __popc(mn);
+                        __syncwarp();
+                        if (cf >= 32) {
+                            eval_slp(qf[(hf + lane) & (kQueue - 1)], false);
+                            hf = (hf + 32) & (kQueue - 1);
+                            cf -= 32;
+                            __syncwarp();
+                        }
+                        if (cn >= 32) {
+                            eval_slp(qn[(hn + lane) & (kQueue - 1)], true);
+                            hn = (hn + 32) & (kQueue - 1);
+                            cn -= 32;
+                            __syncwarp();
+                        }
+                    } else {
+                        unsigned mf = __ballot_sync(0xffffffffu, pass);
+                        if (pass) qf[(hf + cf + __popc(mf & lt_mask)) & (kQueue - 1)] = s;
+                        cf += __popc(mf);
+                        __syncwarp();
+                        if (cf >= 32) {
+                            eval_dlp(qf[(hf + lane) & (kQueue - 1)]);
+                            hf = (hf + 32) & (kQueue - 1);
+                            cf -= 32;
+                            __syncwarp();
                         }
                     }
-                    unsigned m = __ballot_sync(0xffffffffu, pass);
-                    if (pass) myq[(qhead + qcount + __popc(m & lt_mask)) & (kQueue - 1)] = s;
-                    qcount += __popc(m);
-                    __syncwarp();
-                    if (qcount >= 32) {
-                        eval(myq[(qhead + lane) & (kQueue - 1)]);
-                        qhead = (qhead + 32) & (kQueue - 1);
-                        qcount -= 32;
-                        __syncwarp();
-                    }
                 }
-                if (lane < qcount) eval(myq[(qhead + lane) & (kQueue - 1)]);
+                if (KIND == FTE_KIND_SLP) {
+                    // the two partial queues share one pass: lanes [0, cf) take far
+                    // pairs, lanes [cf, cf+cn) near pairs when they fit in a warp
+                    if (cf + cn <= 32) {
+                        if (lane < cf)
+                            eval_slp(qf[(hf + lane) & (kQueue - 1)], false);
+                        else if (lane < cf + cn)
+                            eval_slp(qn[(hn + lane - cf) & (kQueue - 1)], true);
+                    } else {
+                        if (lane < cf) eval_slp(qf[(hf + lane) & (kQueue - 1)], false);
+                        if (lane < cn) eval_slp(qn[(hn + lane) & (kQueue - 1)], true);
+                    }
+                } else {
+                    if (lane < cf) eval_dlp(qf[(hf + lane) & (kQueue - 1)]);
+                }
                 __syncwarp();
                 acc0 = warp_sum(acc0);
                 acc1 = warp_sum(acc1);
@@ -244,8 +369,8 @@ __global__ void __launch_bounds__(kNearThreads) k_near(const NearParams prm) {
 }
 
 size_t near_smem_bytes(int kind, int cap) {
-    size_t per = (kind == FTE_KIND_DLP ? 5 : 4) * sizeof(double) + sizeof(float2);
-    return kGtab * sizeof(double) + (size_t)cap * per + kNearWarps * kQueue * sizeof(int) + 64;
+    size_t per = (kind == FTE_KIND_DLP ? 6 : 4) * sizeof(double) + sizeof(float2);
+    return (kKtab + 64) * sizeof(double) + (size_t)cap * per + kNearWarps * 2 * kQueue * sizeof(int) + 64;
 }
 
 }  // namespace
@@ -270,6 +395,7 @@ int fte_near_launch(fte_context* ctx, int kind, const CellList& cl, double xi, d
     p.inv_xi2 = 1.0 / (xi * xi);
     p.selfc = -(1.0 + 0.5 * FTE_EULER) - log(xi);
     p.cutoffsq = Lx * Ly / cl.nsx / cl.nsy;
+    p.pf = 2.0 * xi * xi;
     double bsx = Lx / cl.nsx, bsy = Ly / cl.nsy;
     double bmax = bsx > bsy ? bsx : bsy;
     p.cut32 = (float)(p.cutoffsq + 1e-4 * bmax * bmax);
@@ -295,22 +421,59 @@ int fte_near_launch(fte_context* ctx, int kind, const CellList& cl, double xi, d
     return FTE_OK;
 }
 
-// ---- diagnostics: E1 on the device (test hook) ------------------------------
+// ---- diagnostics: the special functions on the device (test hook) ------------
 namespace {
-__global__ void k_e1_probe(const double* __restrict__ x, double* __restrict__ out, int n) {
+__global__ void k_special_probe(int which, const double* __restrict__ x, double* __restrict__ out, int n) {
     __shared__ double gtab[kGtab];
+    __shared__ double ktab[kKtab];
+    __shared__ double etab[64];
     for (int i = threadIdx.x; i < kGtab; i += blockDim.x) gtab[i] = (&fte_e1_coef_g[0][0])[i];
+    for (int i = threadIdx.x; i < kKtab; i += blockDim.x) ktab[i] = (&fte_k_coef[0][0])[i];
+    for (int i = threadIdx.x; i < 64; i += blockDim.x) etab[i] = fte_exp_tab[i];
     __syncthreads();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) {
-        double v = x[i];
-        out[i] = fte_e1(v, exp(-v), 1.0 / v, gtab);
+    if (i >= n) return;
+    double v = x[i];
+    double r;
+    switch (which) {
+        case 0:  // E1(x)
+            r = fte_e1(v, exp(-v), 1.0 / v, gtab);
+            break;
+        case 1:  // exp(-x), this project's evaluation
+            r = fte_expm(v, etab);
+            break;
+        case 2: {  // 0.5 E1(x) - exp(-x) as the Stokeslet kernel evaluates it
+            double emx = fte_expm(v, etab);
+            if (v < 1.0) {
+                double tt = fma(2.0, v, -1.0);
+                double R = fte_e1_coef_r[FTE_E1_DEG_R];
+                for (int k = FTE_E1_DEG_R - 1; k >= 0; k--) R = fma(R, tt, fte_e1_coef_r[k]);
+                r = fma(0.5, fma(v, R, -FTE_EULER - log(v)), -emx);
+            } else {
+                r = emx * fte_kfun(v, ktab);
+            }
+            break;
+        }
+        default:  // 1/x
+            r = fte_rcp(v);
+            break;
     }
+    out[i] = r;
 }
 }  // namespace
 
-int fte_e1_device(fte_context* ctx, const double* x_dev, double* out_dev, int n) {
+extern "C" int fte_debug_special(int which, const double* x_dev, double* out_dev, int n) {
     if (n <= 0) return FTE_OK;
-    FTE_LAUNCH(ctx, k_e1_probe, (n + 255) / 256, 256, 0, x_dev, out_dev, n);
+    if (which < 0 || which > 3 || !x_dev || !out_dev) {
+        fte_set_error("fte_debug_special: bad arguments");
+        return FTE_ERR_INVALID;
+    }
+    k_special_probe<<<(n + 255) / 256, 256>>>(which, x_dev, out_dev, n);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+        fte_set_error("fte_debug_special: %s", cudaGetErrorString(e));
+        return FTE_ERR_CUDA;
+    }
     return FTE_OK;
 }

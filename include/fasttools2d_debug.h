@@ -1,0 +1,21 @@
+/*
+ * fasttools2d_debug.h -- diagnostic entry of the GB300 spectral Ewald library.
+ * No counterpart in the reference: it exposes the device evaluation of the
+ * special functions used by the real-space kernels so that tests can compare
+ * them with CUDA's exp/division and with a reference E1.
+ */
+#ifndef FASTTOOLS2D_DEBUG_H
+#define FASTTOOLS2D_DEBUG_H
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Evaluate on the current device, for device arrays x[n] -> out[n]:
+ * which = 0: E1(x); 1: exp(-x); 2: 0.5 E1(x) - exp(-x); 3: 1/x.
+ * Synchronises the device. */
+int fte_debug_special(int which, const double* x_dev, double* out_dev, int n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
