@@ -736,7 +736,7 @@ static int kspace_entry(fte_context* c, int kind, const double* psrc, int64_t ns
     }
     FTE_CUDA_TRY(cudaSetDevice(c->device));
     const bool host = !(flags & FTE_DEVICE_POINTERS);
-    size_t need = fte_kspace_ws(kind, FTE_FORM_PLAIN, Mx, My) + ws_bytes(2 * (ntar + 1), 8);
+    size_t need = fte_kspace_ws(kind, FTE_FORM_PLAIN, Mx, My, nsrc, ntar) + ws_bytes(2 * (ntar + 1), 8);
     if (host) need += ws_bytes(2 * (nsrc + 1), 8) * 3 + ws_bytes(2 * (ntar + 1), 8);
     FTE_TRY(fte_ws_reserve(c, need));
     WsCarver wc{c->ws, 0, c->ws_size};
@@ -872,7 +872,7 @@ static int ewald_entry(fte_context* c, int kind, const double* xsrc, const doubl
     FTE_TRY(check_kspace_params(prm.xi, prm.eta, prm.Mx, prm.My, Lx, Ly, prm.w, prm.P));
     // second workspace: cell list, grids and outputs (the staged point data stays in the first)
     size_t need = fte_cells_ws(nsrc, ntar, prm.nside_x * prm.nside_y) +
-                  fte_kspace_ws(kind, FTE_FORM_PLAIN, prm.Mx, prm.My) + ws_bytes(2 * (ntar + 1), 8) * 3 + 8192;
+                  fte_kspace_ws(kind, FTE_FORM_PLAIN, prm.Mx, prm.My, nsrc, ntar) + ws_bytes(2 * (ntar + 1), 8) * 3 + 8192;
     FTE_TRY(fte_ws2_reserve(c, need));
     WsCarver wc2{c->ws2, 0, c->ws2_size};
     FTE_TRY(fte_record(c, 1));

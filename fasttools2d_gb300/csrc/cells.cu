@@ -107,6 +107,30 @@ __global__ void k_scatter_tar(const double* __restrict__ p, int64_t n, const int
     }
 }
 
+// Grid tile of a point for the k-space kernels: floor((x + L/2)/h), the node
+// index FindClosestNode starts from, divided by the tile size, clamped.
+__global__ void k_tile_assign(const double* __restrict__ p, int64_t n, double Lx, double Ly, double h, int ts,
+                              int ntx, int nty, int* __restrict__ tile, int* __restrict__ rank,
+                              int* __restrict__ counts) {
+    const double lhx = __ddiv_rn(Lx, 2.0), lhy = __ddiv_rn(Ly, 2.0);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double ax = floor(__ddiv_rn(__dadd_rn(p[2 * i], lhx), h));
+        double ay = floor(__ddiv_rn(__dadd_rn(p[2 * i + 1], lhy), h));
+        ax = fmin(fmax(ax, 0.0), (double)(ntx * ts - 1));
+        ay = fmin(fmax(ay, 0.0), (double)(nty * ts - 1));
+        int tx = min((int)ax / ts, ntx - 1), ty = min((int)ay / ts, nty - 1);
+        int t = ty * ntx + tx;
+        tile[i] = t;
+        rank[i] = atomicAdd(&counts[t], 1);
+    }
+}
+
+__global__ void k_tile_scatter(int64_t n, const int* __restrict__ tile, const int* __restrict__ rank,
+                               const int* __restrict__ off, int* __restrict__ perm) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        perm[off[tile[i]] + rank[i]] = (int)i;
+}
+
 inline int grid_for(int64_t n, int threads, int max_blocks) {
     int64_t b = (n + threads - 1) / threads;
     if (b < 1) b = 1;
@@ -189,5 +213,34 @@ int fte_cells_build(fte_context* ctx, WsCarver& wc, int kind, const double* psrc
     if (ntar > 0)
         FTE_LAUNCH(ctx, k_scatter_tar, grid_for(ntar, 256, maxb), 256, 0, ptar, ntar, (const int*)tbox,
                    (const int*)trank, (const int*)cl->tar_off, cl->tpos, cl->tidx);
+    return FTE_OK;
+}
+
+size_t fte_tiles_ws(int64_t n, int ntiles) {
+    return 4 * ws_bytes(ntiles + 1, sizeof(int)) + 3 * ws_bytes((size_t)(n + 1), sizeof(int)) +
+           4 * ws_bytes((size_t)(ntiles + 1) / 4096 + 8, sizeof(int)) + 4096;
+}
+
+int fte_tiles_build(fte_context* ctx, WsCarver& wc, const double* p, int64_t n, double Lx, double Ly, double h,
+                    int ts, int ntx, int nty, TileBins* out) {
+    int nt = ntx * nty;
+    out->ntx = ntx;
+    out->nty = nty;
+    out->ts = ts;
+    int* cnt = wc.take<int>(nt + 1);
+    out->off = wc.take<int>(nt + 1);
+    int* tile = wc.take<int>(n + 1);
+    int* rank = wc.take<int>(n + 1);
+    out->perm = wc.take<int>(n + 1);
+    FTE_WS_CHECK(wc);
+    FTE_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(int) * (nt + 1), ctx->stream));
+    int maxb = ctx->num_sms * 8;
+    if (n > 0)
+        FTE_LAUNCH(ctx, k_tile_assign, grid_for(n, 256, maxb), 256, 0, p, n, Lx, Ly, h, ts, ntx, nty, tile, rank,
+                   cnt);
+    FTE_TRY(fte_scan_exclusive(ctx, wc, cnt, out->off, nt + 1));
+    if (n > 0)
+        FTE_LAUNCH(ctx, k_tile_scatter, grid_for(n, 256, maxb), 256, 0, n, (const int*)tile, (const int*)rank,
+                   (const int*)out->off, out->perm);
     return FTE_OK;
 }

@@ -191,6 +191,16 @@ int fte_cells_build(fte_context* ctx, WsCarver& wc, int kind, const double* psrc
                     double Ly, CellList* cl);
 int fte_scan_exclusive(fte_context* ctx, WsCarver& wc, const int* in, int* out, int n);
 
+// points binned by k-space grid tile (ts x ts nodes)
+struct TileBins {
+    int ntx, nty, ts;
+    int* off;   // ntx*nty + 1
+    int* perm;  // original index of the k-th point in tile order
+};
+size_t fte_tiles_ws(int64_t n, int ntiles);
+int fte_tiles_build(fte_context* ctx, WsCarver& wc, const double* p, int64_t n, double Lx, double Ly, double h,
+                    int ts, int ntx, int nty, TileBins* out);
+
 int fte_near_launch(fte_context* ctx, int kind, const CellList& cl, double xi, double Lx, double Ly, double2* ur);
 
 struct KspaceArgs {
@@ -206,5 +216,5 @@ struct KspaceArgs {
     int Mx, My, P;
     double2* uk;         // output, interleaved
 };
-size_t fte_kspace_ws(int kind, int form, int Mx, int My);
+size_t fte_kspace_ws(int kind, int form, int Mx, int My, int64_t nsrc, int64_t ntar);
 int fte_kspace_run(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, fte_info* info);

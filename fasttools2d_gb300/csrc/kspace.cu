@@ -173,6 +173,177 @@ __global__ void __launch_bounds__(kPtThreads) k_gather(const double* __restrict_
     }
 }
 
+// ---- tiled spread / gather ------------------------------------------------------
+// Points are binned by grid tile (ts x ts nodes).  A CTA owns one tile and a
+// shared-memory region of W x W nodes per grid, W = ts + P + 4, starting at
+// node (tx ts - P/2 - 2, ty ts - P/2 - 2): every window of a point binned in
+// the tile lies inside it.  The spread accumulates with shared-memory atomics
+// and flushes the region to the global grids (wrapped, atomics only where
+// regions of neighbouring tiles overlap); the gather stages the region once
+// and reads every target's window from shared memory.  A point whose window
+// is not inside the region (a caller passing points outside [-L/2, L/2))
+// takes the global, wrapped path.
+constexpr int kTileThreads = 128;
+
+__host__ __device__ inline int tile_region(int ts, int P) { return ts + P + 4; }
+
+template <int NG>
+__global__ void __launch_bounds__(kTileThreads) k_spread_tiled(const double* __restrict__ p, const double* __restrict__ f,
+                                                              const double* __restrict__ nrm,
+                                                              const double* __restrict__ wts,
+                                                              const int* __restrict__ toff, const int* __restrict__ perm,
+                                                              int ts, int ntx, int nty, WinParams wp,
+                                                              double* __restrict__ H) {
+    extern __shared__ double sh[];
+    const int P1 = wp.P + 1, W = tile_region(ts, wp.P), WW = W * W;
+    double* buf = sh;
+    double* e1 = buf + NG * WW;
+    double* wyb = e1 + ((P1 + 1) & ~1) + threadIdx.x * P1;
+    load_e1(e1, wp);
+    const size_t G = (size_t)wp.Mx * wp.My;
+    for (int tile = blockIdx.x; tile < ntx * nty; tile += gridDim.x) {
+        const int k0 = toff[tile], k1 = toff[tile + 1];
+        if (k0 == k1) continue;
+        const int ox = (tile % ntx) * ts - wp.P / 2 - 2, oy = (tile / ntx) * ts - wp.P / 2 - 2;
+        __syncthreads();
+        for (int i = threadIdx.x; i < NG * WW; i += blockDim.x) buf[i] = 0.0;
+        __syncthreads();
+        for (int k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
+            const int i = perm[k];
+            Win wn = window_of(p[2 * i], p[2 * i + 1], wp);
+            double q[4];
+            double f1 = f[2 * i], f2 = f[2 * i + 1];
+            if (wts) {
+                f1 *= wts[i];
+                f2 *= wts[i];
+            }
+            if (NG == 2) {
+                q[0] = f1;
+                q[1] = f2;
+            } else {
+                double n1 = nrm[2 * i], n2 = nrm[2 * i + 1];
+                q[0] = f1 * n1;
+                q[1] = f2 * n1;
+                q[2] = f1 * n2;
+                q[3] = f2 * n2;
+            }
+            double ey = 1.0;
+            for (int j = 0; j < P1; j++) {
+                wyb[j] = ey * e1[j];
+                ey *= wn.e3y;
+            }
+            const int lx = wn.mx - ox, ly = wn.my - oy;
+            double ex = wn.ex * wn.e4y;
+            if (lx >= 0 && ly >= 0 && lx + wp.P < W && ly + wp.P < W) {
+                for (int a = 0; a < P1; a++) {
+                    double wxa = ex * e1[a];
+                    ex *= wn.e3x;
+                    double* row = buf + (lx + a) * W + ly;
+                    double fw[NG];
+#pragma unroll
+                    for (int g = 0; g < NG; g++) fw[g] = q[g] * wxa;
+                    for (int j = 0; j < P1; j++) {
+                        double wyj = wyb[j];
+#pragma unroll
+                        for (int g = 0; g < NG; g++) atomicAdd(row + g * WW + j, fw[g] * wyj);
+                    }
+                }
+            } else {
+                for (int a = 0; a < P1; a++) {
+                    double wxa = ex * e1[a];
+                    ex *= wn.e3x;
+                    size_t base = (size_t)fte_wrap_index(wn.mx + a, wp.Mx) * wp.My;
+                    for (int j = 0; j < P1; j++) {
+                        size_t at = base + fte_wrap_index(wn.my + j, wp.My);
+#pragma unroll
+                        for (int g = 0; g < NG; g++) atomicAdd(&H[g * G + at], q[g] * wxa * wyb[j]);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < NG * WW; idx += blockDim.x) {
+            double v = buf[idx];
+            if (v == 0.0) continue;
+            int g = idx / WW, r = idx - g * WW;
+            int xx = r / W, yy = r - xx * W;
+            size_t at = (size_t)fte_wrap_index(ox + xx, wp.Mx) * wp.My + fte_wrap_index(oy + yy, wp.My);
+            atomicAdd(&H[g * G + at], v);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kTileThreads) k_gather_tiled(const double* __restrict__ p,
+                                                              const int* __restrict__ toff,
+                                                              const int* __restrict__ perm, int ts, int ntx, int nty,
+                                                              WinParams wp, const double* __restrict__ G0,
+                                                              const double* __restrict__ G1, double scale,
+                                                              double2* __restrict__ out) {
+    extern __shared__ double sh[];
+    const int P1 = wp.P + 1, W = tile_region(ts, wp.P), WW = W * W;
+    double* r0 = sh;
+    double* r1 = r0 + WW;
+    double* e1 = r1 + WW;
+    double* wyb = e1 + ((P1 + 1) & ~1) + threadIdx.x * P1;
+    load_e1(e1, wp);
+    for (int tile = blockIdx.x; tile < ntx * nty; tile += gridDim.x) {
+        const int k0 = toff[tile], k1 = toff[tile + 1];
+        if (k0 == k1) continue;
+        const int ox = (tile % ntx) * ts - wp.P / 2 - 2, oy = (tile / ntx) * ts - wp.P / 2 - 2;
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < WW; idx += blockDim.x) {
+            int xx = idx / W, yy = idx - xx * W;
+            size_t at = (size_t)fte_wrap_index(ox + xx, wp.Mx) * wp.My + fte_wrap_index(oy + yy, wp.My);
+            r0[idx] = __ldg(G0 + at);
+            r1[idx] = __ldg(G1 + at);
+        }
+        __syncthreads();
+        for (int k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
+            const int i = perm[k];
+            Win wn = window_of(p[2 * i], p[2 * i + 1], wp);
+            double ey = 1.0;
+            for (int j = 0; j < P1; j++) {
+                wyb[j] = ey * e1[j];
+                ey *= wn.e3y;
+            }
+            const int lx = wn.mx - ox, ly = wn.my - oy;
+            double ex = wn.ex * wn.e4y;
+            double acc0 = 0.0, acc1 = 0.0;
+            if (lx >= 0 && ly >= 0 && lx + wp.P < W && ly + wp.P < W) {
+                for (int a = 0; a < P1; a++) {
+                    double wxa = ex * e1[a];
+                    ex *= wn.e3x;
+                    const double* c0 = r0 + (lx + a) * W + ly;
+                    const double* c1 = r1 + (lx + a) * W + ly;
+                    double s0 = 0.0, s1 = 0.0;
+                    for (int j = 0; j < P1; j++) {
+                        double wyj = wyb[j];
+                        s0 = fma(wyj, c0[j], s0);
+                        s1 = fma(wyj, c1[j], s1);
+                    }
+                    acc0 = fma(wxa, s0, acc0);
+                    acc1 = fma(wxa, s1, acc1);
+                }
+            } else {
+                for (int a = 0; a < P1; a++) {
+                    double wxa = ex * e1[a];
+                    ex *= wn.e3x;
+                    size_t base = (size_t)fte_wrap_index(wn.mx + a, wp.Mx) * wp.My;
+                    double s0 = 0.0, s1 = 0.0;
+                    for (int j = 0; j < P1; j++) {
+                        size_t at = base + fte_wrap_index(wn.my + j, wp.My);
+                        s0 = fma(wyb[j], __ldg(G0 + at), s0);
+                        s1 = fma(wyb[j], __ldg(G1 + at), s1);
+                    }
+                    acc0 = fma(wxa, s0, acc0);
+                    acc1 = fma(wxa, s1, acc1);
+                }
+            }
+            out[i] = make_double2(acc0 * scale, acc1 * scale);
+        }
+    }
+}
+
 // ---- FFT along y: real -> half spectrum (two columns per complex FFT) -------
 __global__ void k_fft_y_r2c(const double* __restrict__ H, double2* __restrict__ Hh, int Mx, int My, FftDev plan) {
     extern __shared__ double2 shc[];
@@ -319,12 +490,33 @@ int fft_threads(int m) {
 
 }  // namespace
 
-size_t fte_kspace_ws(int kind, int form, int Mx, int My) {
+namespace {
+// largest tile (multiple of 4 nodes, <= 64) whose region and per-thread
+// weight buffers fit the shared-memory budget; 0 when none does
+int pick_tile(int ng, int P, size_t budget) {
+    const int P1 = P + 1;
+    size_t per = (size_t)(((P1 + 1) & ~1) + kTileThreads * P1) * sizeof(double);
+    for (int ts = 64; ts >= 8; ts -= 4) {
+        size_t W = tile_region(ts, P);
+        if ((size_t)ng * W * W * sizeof(double) + per <= budget) return ts;
+    }
+    return 0;
+}
+size_t tile_budget(const fte_context* ctx) {
+    size_t b = 110 * 1024;  // two CTAs per SM
+    return b < (size_t)ctx->max_smem_optin ? b : (size_t)ctx->max_smem_optin;
+}
+}  // namespace
+
+size_t fte_kspace_ws(int kind, int form, int Mx, int My, int64_t nsrc, int64_t ntar) {
     (void)form;
     int ng = kind == FTE_KIND_SLP ? 2 : 4;
     size_t G = (size_t)Mx * My;
     size_t Gh = (size_t)Mx * (My / 2 + 1);
-    return ws_bytes(ng * G, sizeof(double)) + ws_bytes(ng * Gh, sizeof(double2)) + 4096;
+    // tiles no smaller than 8 nodes
+    int ntiles = ((Mx + 7) / 8) * ((My + 7) / 8);
+    return ws_bytes(ng * G, sizeof(double)) + ws_bytes(ng * Gh, sizeof(double2)) + fte_tiles_ws(nsrc, ntiles) +
+           fte_tiles_ws(ntar, ntiles) + 4096;
 }
 
 int fte_kspace_run(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, fte_info* info) {
@@ -358,9 +550,35 @@ int fte_kspace_run(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, fte_info
     const int P1 = a.P + 1;
     size_t sm_pt = (size_t)(((P1 + 1) & ~1) + kPtThreads * P1) * sizeof(double);
 
+    // tile the grid for the shared-memory spread and gather
+    const int ts_s = pick_tile(ng, a.P, tile_budget(ctx));
+    const int ts_g = pick_tile(2, a.P, tile_budget(ctx));
+    TileBins tb_s, tb_g;
+    tb_s.ntx = tb_g.ntx = 0;
+    if (ts_s > 0 && a.nsrc > 0)
+        FTE_TRY(fte_tiles_build(ctx, wc, a.psrc, a.nsrc, a.Lx, a.Ly, wp.h, ts_s, (Mx + ts_s - 1) / ts_s,
+                                (My + ts_s - 1) / ts_s, &tb_s));
+    if (ts_g > 0 && a.ntar > 0)
+        FTE_TRY(fte_tiles_build(ctx, wc, a.ptar, a.ntar, a.Lx, a.Ly, wp.h, ts_g, (Mx + ts_g - 1) / ts_g,
+                                (My + ts_g - 1) / ts_g, &tb_g));
+
     FTE_TRY(fte_record(ctx, 2));
     FTE_CUDA_TRY(cudaMemsetAsync(H, 0, sizeof(double) * ng * G, ctx->stream));
-    if (a.nsrc > 0) {
+    if (a.nsrc > 0 && ts_s > 0) {
+        const int W = tile_region(ts_s, a.P);
+        size_t sm = (size_t)ng * W * W * sizeof(double) + sm_pt;
+        int nt = tb_s.ntx * tb_s.nty;
+        int grid = nt < ctx->num_sms * 8 ? nt : ctx->num_sms * 8;
+        if (ng == 2) {
+            FTE_CUDA_TRY(cudaFuncSetAttribute(k_spread_tiled<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+            FTE_LAUNCH(ctx, k_spread_tiled<2>, grid, kTileThreads, sm, a.psrc, a.f, a.nrm, a.wts,
+                       (const int*)tb_s.off, (const int*)tb_s.perm, ts_s, tb_s.ntx, tb_s.nty, wp, H);
+        } else {
+            FTE_CUDA_TRY(cudaFuncSetAttribute(k_spread_tiled<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+            FTE_LAUNCH(ctx, k_spread_tiled<4>, grid, kTileThreads, sm, a.psrc, a.f, a.nrm, a.wts,
+                       (const int*)tb_s.off, (const int*)tb_s.perm, ts_s, tb_s.ntx, tb_s.nty, wp, H);
+        }
+    } else if (a.nsrc > 0) {
         if (ng == 2) {
             FTE_CUDA_TRY(cudaFuncSetAttribute(k_spread<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_pt));
             FTE_LAUNCH(ctx, k_spread<2>, pt_grid(ctx, a.nsrc), kPtThreads, sm_pt, a.psrc, a.f, a.nrm, a.wts, a.nsrc,
@@ -389,7 +607,15 @@ int fte_kspace_run(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, fte_info
     double s = 4 * a.xi * a.xi / a.eta;
     s = s * s * wp.h * wp.h / FTE_PI;
     double scale = s / (4 * FTE_PI) / ((double)Mx * (double)My);
-    if (a.ntar > 0) {
+    if (a.ntar > 0 && ts_g > 0) {
+        const int W = tile_region(ts_g, a.P);
+        size_t sm = 2 * (size_t)W * W * sizeof(double) + sm_pt;
+        int nt = tb_g.ntx * tb_g.nty;
+        int grid = nt < ctx->num_sms * 8 ? nt : ctx->num_sms * 8;
+        FTE_CUDA_TRY(cudaFuncSetAttribute(k_gather_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        FTE_LAUNCH(ctx, k_gather_tiled, grid, kTileThreads, sm, a.ptar, (const int*)tb_g.off, (const int*)tb_g.perm,
+                   ts_g, tb_g.ntx, tb_g.nty, wp, (const double*)H, (const double*)(H + G), scale, a.uk);
+    } else if (a.ntar > 0) {
         FTE_CUDA_TRY(cudaFuncSetAttribute(k_gather, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_pt));
         FTE_LAUNCH(ctx, k_gather, pt_grid(ctx, a.ntar), kPtThreads, sm_pt, a.ptar, a.ntar, wp, (const double*)H,
                    (const double*)(H + G), scale, a.uk);

@@ -104,6 +104,31 @@ def test_driver_matches_oracle(gpu_ctx, case):
     assert np.max(np.abs(g[3] - o[3])) <= TOL_FP64 * scale
 
 
+@pytest.mark.parametrize("kind", ["slp", "dlp"])
+def test_kspace_gateway_points_outside_box(gpu_ctx, kind):
+    """Gateway-level callers may pass points outside [-L/2, L/2) (the drivers
+    wrap, the gateways do not): windows then leave their tile's region."""
+    ft = _ft()
+    rng = np.random.default_rng(21)
+    ns, nt = 3000, 2000
+    ps = (rng.random((ns, 2)) - 0.5) * 1.8
+    pt = (rng.random((nt, 2)) - 0.5) * 1.8
+    f = rng.standard_normal((ns, 2))
+    th = rng.random(ns) * 2 * np.pi
+    n = np.stack([np.cos(th), np.sin(th)], 1)
+    Mx = My = 96
+    P, xi = 24, 30.0
+    w = P * (1.0 / Mx) / 2
+    eta = (2 * xi * w / (0.95 * np.sqrt(np.pi * P))) ** 2
+    if kind == "slp":
+        ref = po.slp_kspace(ps, pt, xi, eta, f, Mx, My, 1.0, 1.0, w, P)
+        out = ft.mex_stokes_slp_kspace(ps, pt, xi, eta, f, Mx, My, 1.0, 1.0, w, P, ctx=gpu_ctx)
+    else:
+        ref = po.dlp_kspace(ps, pt, xi, eta, f, n, Mx, My, 1.0, 1.0, w, P)
+        out = ft.mex_stokes_dlp_kspace(ps, pt, xi, eta, f, n, Mx, My, 1.0, 1.0, w, P, ctx=gpu_ctx)
+    assert rel_max(out, ref) <= TOL_FP64
+
+
 def test_device_pointers_match_host(gpu_ctx):
     import torch
 
