@@ -273,6 +273,125 @@ __global__ void __launch_bounds__(kTileThreads) k_spread_tiled(const double* __r
     }
 }
 
+// Column-owned spread of two grids without atomics.  For a chunk of the
+// tile's sources, threads first compute each source's window origin and its
+// factors fw_g[a] = q_g ex e4y e1[a] e3x^a and wy[j] = e1[j] e3y^j into
+// shared memory; then warp w adds the products for every region column
+// c = w (mod warps) of every source of the chunk, lane j owning window row j,
+// so every update is one FMA on an address no other thread touches.
+// mode 0: (f1, f2) [Stokeslet]; 1: (f1 n1, f2 n1); 2: (f1 n2, f2 n2) [stresslet].
+constexpr int kColThreads = 256;
+constexpr int kColChunk = 32;
+
+__global__ void __launch_bounds__(kColThreads) k_spread_cols(int mode, const double* __restrict__ p,
+                                                            const double* __restrict__ f,
+                                                            const double* __restrict__ nrm,
+                                                            const double* __restrict__ wts,
+                                                            const int* __restrict__ toff,
+                                                            const int* __restrict__ perm, int ts, int ntx, int nty,
+                                                            WinParams wp, double* __restrict__ H0,
+                                                            double* __restrict__ H1) {
+    extern __shared__ double sh[];
+    const int P1 = wp.P + 1, W = tile_region(ts, wp.P), WW = W * W;
+    const int P1e = (P1 + 1) & ~1;
+    double* buf = sh;                     // 2 * WW
+    double* e1 = buf + 2 * WW;            // P1e
+    double* fw = e1 + P1e;                // kColChunk * 2 * P1
+    double* wy = fw + kColChunk * 2 * P1; // kColChunk * P1
+    int* org = reinterpret_cast<int*>(wy + kColChunk * P1);  // kColChunk * 2 (lx, ly; lx < 0: global path)
+    load_e1(e1, wp);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int tile = blockIdx.x; tile < ntx * nty; tile += gridDim.x) {
+        const int k0 = toff[tile], k1 = toff[tile + 1];
+        if (k0 == k1) continue;
+        const int ox = (tile % ntx) * ts - wp.P / 2 - 2, oy = (tile / ntx) * ts - wp.P / 2 - 2;
+        __syncthreads();
+        for (int i = threadIdx.x; i < 2 * WW; i += blockDim.x) buf[i] = 0.0;
+        for (int c0 = k0; c0 < k1; c0 += kColChunk) {
+            const int cn = min(kColChunk, k1 - c0);
+            __syncthreads();
+            if (threadIdx.x < cn) {
+                const int s = threadIdx.x;
+                const int i = perm[c0 + s];
+                Win wn = window_of(p[2 * i], p[2 * i + 1], wp);
+                double f1 = f[2 * i], f2 = f[2 * i + 1];
+                if (wts) {
+                    f1 *= wts[i];
+                    f2 *= wts[i];
+                }
+                double q0 = f1, q1 = f2;
+                if (mode == 1) {
+                    q0 = f1 * nrm[2 * i];
+                    q1 = f2 * nrm[2 * i];
+                } else if (mode == 2) {
+                    q0 = f1 * nrm[2 * i + 1];
+                    q1 = f2 * nrm[2 * i + 1];
+                }
+                double ey = 1.0;
+                for (int j = 0; j < P1; j++) {
+                    wy[s * P1 + j] = ey * e1[j];
+                    ey *= wn.e3y;
+                }
+                double ex = wn.ex * wn.e4y;
+                for (int a = 0; a < P1; a++) {
+                    double wxa = ex * e1[a];
+                    ex *= wn.e3x;
+                    fw[(s * 2 + 0) * P1 + a] = q0 * wxa;
+                    fw[(s * 2 + 1) * P1 + a] = q1 * wxa;
+                }
+                const int lx = wn.mx - ox, ly = wn.my - oy;
+                if (lx >= 0 && ly >= 0 && lx + wp.P < W && ly + wp.P < W) {
+                    org[2 * s] = lx;
+                    org[2 * s + 1] = ly;
+                } else {
+                    // window outside the region: add straight into the global grids
+                    org[2 * s] = -1;
+                    for (int a = 0; a < P1; a++) {
+                        size_t base = (size_t)fte_wrap_index(wn.mx + a, wp.Mx) * wp.My;
+                        for (int j = 0; j < P1; j++) {
+                            size_t at = base + fte_wrap_index(wn.my + j, wp.My);
+                            atomicAdd(&H0[at], fw[(s * 2 + 0) * P1 + a] * wy[s * P1 + j]);
+                            atomicAdd(&H1[at], fw[(s * 2 + 1) * P1 + a] * wy[s * P1 + j]);
+                        }
+                    }
+                }
+            }
+            __syncthreads();
+            for (int s = 0; s < cn; s++) {
+                const int lx = org[2 * s];
+                if (lx < 0) continue;
+                const int ly = org[2 * s + 1];
+                // first column >= lx owned by this warp
+                int c = lx + ((warp - lx) % nw + nw) % nw;
+                if (lane < P1) {
+                    const double wyj = wy[s * P1 + lane];
+                    const double* fa = fw + (s * 2) * P1;
+                    const double* fb = fa + P1;
+                    for (; c <= lx + wp.P; c += nw) {
+                        double* b0 = buf + c * W + ly + lane;
+                        b0[0] = fma(fa[c - lx], wyj, b0[0]);
+                        b0[WW] = fma(fb[c - lx], wyj, b0[WW]);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < 2 * WW; idx += blockDim.x) {
+            double v = buf[idx];
+            if (v == 0.0) continue;
+            int g = idx >= WW, r = idx - g * WW;
+            int xx = r / W, yy = r - xx * W;
+            size_t at = (size_t)fte_wrap_index(ox + xx, wp.Mx) * wp.My + fte_wrap_index(oy + yy, wp.My);
+            atomicAdd(g ? &H1[at] : &H0[at], v);
+        }
+    }
+}
+
+size_t spread_cols_smem(int ts, int P) {
+    const int P1 = P + 1, W = tile_region(ts, P);
+    return (size_t)(2 * W * W + ((P1 + 1) & ~1) + kColChunk * 3 * P1) * sizeof(double) + kColChunk * 2 * sizeof(int);
+}
+
 __global__ void __launch_bounds__(kTileThreads) k_gather_tiled(const double* __restrict__ p,
                                                               const int* __restrict__ toff,
                                                               const int* __restrict__ perm, int ts, int ntx, int nty,
@@ -551,7 +670,9 @@ int fte_kspace_run(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, fte_info
     size_t sm_pt = (size_t)(((P1 + 1) & ~1) + kPtThreads * P1) * sizeof(double);
 
     // tile the grid for the shared-memory spread and gather
-    const int ts_s = pick_tile(ng, a.P, tile_budget(ctx));
+    int ts_s = 0;  // column-owned spread: largest tile whose region fits
+    for (int ts = 64; ts >= 8 && !ts_s; ts -= 4)
+        if (spread_cols_smem(ts, a.P) <= tile_budget(ctx)) ts_s = ts;
     const int ts_g = pick_tile(2, a.P, tile_budget(ctx));
     TileBins tb_s, tb_g;
     tb_s.ntx = tb_g.ntx = 0;
@@ -565,18 +686,15 @@ int fte_kspace_run(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, fte_info
     FTE_TRY(fte_record(ctx, 2));
     FTE_CUDA_TRY(cudaMemsetAsync(H, 0, sizeof(double) * ng * G, ctx->stream));
     if (a.nsrc > 0 && ts_s > 0) {
-        const int W = tile_region(ts_s, a.P);
-        size_t sm = (size_t)ng * W * W * sizeof(double) + sm_pt;
+        size_t sm = spread_cols_smem(ts_s, a.P);
         int nt = tb_s.ntx * tb_s.nty;
         int grid = nt < ctx->num_sms * 8 ? nt : ctx->num_sms * 8;
-        if (ng == 2) {
-            FTE_CUDA_TRY(cudaFuncSetAttribute(k_spread_tiled<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-            FTE_LAUNCH(ctx, k_spread_tiled<2>, grid, kTileThreads, sm, a.psrc, a.f, a.nrm, a.wts,
-                       (const int*)tb_s.off, (const int*)tb_s.perm, ts_s, tb_s.ntx, tb_s.nty, wp, H);
-        } else {
-            FTE_CUDA_TRY(cudaFuncSetAttribute(k_spread_tiled<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-            FTE_LAUNCH(ctx, k_spread_tiled<4>, grid, kTileThreads, sm, a.psrc, a.f, a.nrm, a.wts,
-                       (const int*)tb_s.off, (const int*)tb_s.perm, ts_s, tb_s.ntx, tb_s.nty, wp, H);
+        FTE_CUDA_TRY(cudaFuncSetAttribute(k_spread_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        for (int pass = 0; pass < ng / 2; pass++) {
+            int mode = ng == 2 ? 0 : 1 + pass;
+            FTE_LAUNCH(ctx, k_spread_cols, grid, kColThreads, sm, mode, a.psrc, a.f, a.nrm, a.wts,
+                       (const int*)tb_s.off, (const int*)tb_s.perm, ts_s, tb_s.ntx, tb_s.nty, wp, H + 2 * pass * G,
+                       H + (2 * pass + 1) * G);
         }
     } else if (a.nsrc > 0) {
         if (ng == 2) {
