@@ -53,7 +53,7 @@ class Params(C.Structure):
     _fields_ = [("P", C.c_int), ("Nb", C.c_double), ("tol", C.c_double), ("Q", C.c_double),
                 ("A", C.c_int), ("B", C.c_int), ("nside_x", C.c_int), ("nside_y", C.c_int),
                 ("rc", C.c_double), ("xi", C.c_double), ("kinf", C.c_int), ("Mx", C.c_int), ("My", C.c_int),
-                ("w", C.c_double), ("eta", C.c_double)]
+                ("w", C.c_double), ("eta", C.c_double), ("form", C.c_int)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -306,7 +306,7 @@ def mex_stokes_dlp_kspace(psrc, ptar, xi, eta, f, n, Mx, My, Lx, Ly, w, P, ctx: 
 
 # ---- driver-shaped entries -----------------------------------------------------
 
-def _options(P=24, Nb=None, tol=1e-16, xi=None, Mx=None, My=None, nside_x=None, nside_y=None, weights_ptr=None,
+def _options(P=None, Nb=None, tol=1e-16, xi=None, Mx=None, My=None, nside_x=None, nside_y=None, weights_ptr=None,
              form=FORM_PLAIN) -> Options:
     o = Options()
     o.P = int(P or 0)
@@ -372,7 +372,7 @@ def _ewald(kind, xsrc, ysrc, xtar, ytar, n1, n2, f1, f2, Lx, Ly, P, Nb, tol, ver
     return (res, info) if return_info else res
 
 
-def StokesSLP_ewald_2p(xsrc, ysrc, xtar, ytar, f1, f2, Lx, Ly, P=24, Nb=None, tol=1e-16, verbose=0,
+def StokesSLP_ewald_2p(xsrc, ysrc, xtar, ytar, f1, f2, Lx, Ly, P=None, Nb=None, tol=1e-16, verbose=0,
                        weights=None, xi=None, Mx=None, My=None, nside_x=None, nside_y=None, form=FORM_PLAIN,
                        ctx: Context | None = None, return_info: bool = False, out=None, parts: bool = True):
     """Spectral Ewald evaluation of the doubly-periodic Stokeslet.
@@ -385,7 +385,7 @@ def StokesSLP_ewald_2p(xsrc, ysrc, xtar, ytar, f1, f2, Lx, Ly, P=24, Nb=None, to
                   My, nside_x, nside_y, form, ctx, return_info, out, parts)
 
 
-def StokesDLP_ewald_2p(xsrc, ysrc, xtar, ytar, n1, n2, f1, f2, Lx, Ly, P=24, Nb=None, tol=1e-16, verbose=0,
+def StokesDLP_ewald_2p(xsrc, ysrc, xtar, ytar, n1, n2, f1, f2, Lx, Ly, P=None, Nb=None, tol=1e-16, verbose=0,
                        weights=None, xi=None, Mx=None, My=None, nside_x=None, nside_y=None, form=FORM_PLAIN,
                        ctx: Context | None = None, return_info: bool = False, out=None, parts: bool = True):
     """Spectral Ewald evaluation of the doubly-periodic stresslet (double layer).
@@ -397,7 +397,7 @@ def StokesDLP_ewald_2p(xsrc, ysrc, xtar, ytar, n1, n2, f1, f2, Lx, Ly, P=24, Nb=
                   My, nside_x, nside_y, form, ctx, return_info, out, parts)
 
 
-def choose_params(kind, f1, f2, ntar, Lx, Ly, P=24, Nb=None, tol=1e-16, **kw) -> Params:
+def choose_params(kind, f1, f2, ntar, Lx, Ly, P=None, Nb=None, tol=1e-16, **kw) -> Params:
     """The drivers' analytic parameter choice (host only, no GPU needed)."""
     f1 = np.ascontiguousarray(f1, dtype=np.float64)
     f2 = np.ascontiguousarray(f2, dtype=np.float64)

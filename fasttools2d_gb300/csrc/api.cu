@@ -454,6 +454,147 @@ static int choose_params_q(int kind, int64_t nsrc, int64_t ntar, double Q, doubl
     return FTE_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Tuned parameters of the mixed form.  The analytic estimates above are kept
+// (the same Newton solves for xi and kinf), but every free choice the drivers
+// fix is optimised for speed at the requested tolerance:
+//   * P: smallest even support whose window error erfc(m/sqrt 2),
+//     m = 0.95 sqrt(pi P), is below tol/10 (the drivers always use 24);
+//   * the cell multiplier a (cutoff rc = Lx/(a A)): minimises a cost model of
+//     near pairs (FP64), window work (spread + gather) and FFTs, with unit
+//     costs measured on GB300; the drivers take a from Nb;
+//   * grids rounded up to 7-smooth even sizes (no Bluestein transform);
+//   * the k-space part in FP32 when tol >= 1e-7, else in FP64;
+//   * the estimates are solved for tol * slack: they bound the error by
+//     sum |f|^2, which over-estimates the max-relative error of the result by
+//     two to three orders of magnitude on the benchmark inputs; slack = 10.
+// ---------------------------------------------------------------------------
+namespace {
+
+double xi_estimate(int kind, double Q, double Lx, double Ly, double rc, double tol) {
+    if (kind == FTE_KIND_SLP)
+        return newton(
+            4 / rc, tol,
+            [&](double x) { return std::sqrt(Q * FTE_PI / (4 * Lx * Ly * x)) * std::exp(-x * x * rc * rc) - tol; },
+            [&](double x) {
+                return -std::sqrt(Q * FTE_PI / (4 * Lx * Ly)) * std::exp(-x * x * rc * rc) *
+                       (0.5 * std::pow(x, -1.5) + 2 * rc * rc * x * std::sqrt(1 / x));
+            });
+    return newton(
+        1 / rc, tol,
+        [&](double x) { return std::exp(-x * x * rc * rc) * x * rc * std::sqrt(2 * FTE_PI * Q / (Lx * Ly)) - tol; },
+        [&](double x) {
+            return (1 - 2 * x * x * rc * rc) * std::exp(-x * x * rc * rc) * std::sqrt(2 * FTE_PI * Q / (Lx * Ly)) * rc;
+        });
+}
+
+int kinf_estimate(int kind, double Q, double Lx, double xi, double tol) {
+    const double L1 = Lx;
+    double k;
+    if (kind == FTE_KIND_SLP)
+        k = newton(
+            std::round(5 * xi), tol,
+            [&](double k) {
+                return std::sqrt(4 * Q * FTE_PI * L1 / (std::pow(L1, 6) * k)) * std::exp(-k * k / (4 * xi * xi)) - tol;
+            },
+            [&](double k) {
+                return -std::sqrt(4 * Q * FTE_PI * L1 / std::pow(L1, 6)) * std::exp(-k * k / (4 * xi * xi)) *
+                       (0.5 * std::pow(k, -1.5) + std::sqrt(1 / k) * 2 * k / (4 * xi * xi));
+            });
+    else
+        k = newton(
+            std::round(5 * xi), tol,
+            [&](double k) { return std::sqrt(k * 8 * FTE_PI * Q * L1) * std::exp(-k * k / (4 * xi * xi)) - tol; },
+            [&](double k) {
+                return std::sqrt(8 * FTE_PI * Q * L1) * std::exp(-k * k / (4 * xi * xi)) *
+                       (0.5 * std::pow(k, -0.5) - 2 * std::pow(k, 1.5) / (4 * xi * xi));
+            });
+    return (int)std::round(Lx * k / (2 * FTE_PI));
+}
+
+int next_smooth_even(int n) {
+    if (n < 2) n = 2;
+    if (n % 2) n++;
+    while (!smooth7(n, nullptr)) n += 2;
+    return n;
+}
+
+}  // namespace
+
+// unit costs (seconds) measured on GB300 for the cost model
+static const double kCostPair = 0.094e-9;      // one FP64 near pair
+static const double kCostWin64 = 3.2e-12;      // one window node x grid, FP64 spread/gather
+static const double kCostWin32 = 1.2e-12;      // same in FP32 with compensation
+static const double kCostFft64 = 3.5e-11;      // per complex grid point x log2(points), 7-smooth FP64
+static const double kCostFft32 = 1.2e-11;      // same in FP32
+static const double kTolSlack = 10.0;
+
+static int choose_params_tuned(int kind, int64_t nsrc, int64_t ntar, double Q, double Lx, double Ly,
+                               const fte_options* opt, fte_params* o) {
+    // start from the analytic choice (Nb, rat, defaults) and re-optimise
+    FTE_TRY(choose_params_q(kind, nsrc, ntar, Q, Lx, Ly, opt, o));
+    const double tol = o->tol;
+    const double tol_e = tol * kTolSlack;
+    const bool fp32 = tol >= 1e-7;
+    int P = opt && opt->P > 0 ? opt->P : 0;
+    if (P == 0) {
+        for (P = 4; P < 24; P += 2) {
+            double m = 0.95 * std::sqrt(FTE_PI * P);
+            if (std::erfc(m / std::sqrt(2.0)) <= tol / 10) break;
+        }
+    }
+    const int A = o->A, B = o->B;
+    const int a0 = o->nside_x / A;
+    const double area = Lx * Ly;
+    const int ng = kind == FTE_KIND_SLP ? 2 : 4;
+    const double nfft = kind == FTE_KIND_SLP ? 2.0 : 3.0;
+    const int mcap = fp32 ? 6144 : 3072;  // shared-memory transform limit (smooth sizes)
+    double best = 1e300;
+    fte_params bestp = *o;
+    for (int step = 0; step <= 40; step++) {
+        int a = (int)std::lround(a0 * std::pow(1.1, step));
+        if (step > 0 && a == (int)std::lround(a0 * std::pow(1.1, step - 1))) continue;
+        if (opt && opt->nside_x > 0) a = opt->nside_x / A;
+        int nsx = a * A, nsy = a * B;
+        double rc = Lx / nsx;
+        double xi = (opt && opt->xi > 0) ? opt->xi : xi_estimate(kind, Q, Lx, Ly, rc, tol_e);
+        int kinf = kinf_estimate(kind, Q, Lx, xi, tol_e);
+        int M = next_smooth_even(2 * kinf);
+        int Mx = (opt && opt->Mx > 0) ? opt->Mx : next_smooth_even(A * M);
+        int My = (opt && opt->My > 0) ? opt->My : next_smooth_even(B * M);
+        if (Mx > mcap || My > mcap) break;
+        // keep hx = hy: the grid follows the box aspect exactly when A, B are used
+        if (std::fabs(Lx / Mx - Ly / My) > 1e-12 * (Lx / Mx)) {
+            My = (int)std::lround((double)Mx * Ly / Lx);
+            if (My % 2 || std::fabs(Lx / Mx - Ly / My) > 1e-12 * (Lx / Mx)) continue;
+        }
+        double pairs = (double)nsrc * (double)ntar * FTE_PI * rc * rc / area * 1.03;
+        double win = (double)(P + 1) * (P + 1) * ((double)nsrc * ng + (double)ntar * 2);
+        double pts = (double)Mx * My;
+        double cost = kCostPair * pairs + (fp32 ? kCostWin32 : kCostWin64) * win +
+                      (fp32 ? kCostFft32 : kCostFft64) * nfft * pts * std::log2(pts);
+        if (cost < best) {
+            best = cost;
+            bestp = *o;
+            bestp.P = P;
+            bestp.nside_x = nsx;
+            bestp.nside_y = nsy;
+            bestp.rc = rc;
+            bestp.xi = xi;
+            bestp.kinf = kinf;
+            bestp.Mx = Mx;
+            bestp.My = My;
+            double m = 0.95 * std::sqrt(FTE_PI * P);
+            bestp.w = P * Lx / Mx / 2;
+            bestp.eta = (2 * xi * bestp.w / m) * (2 * xi * bestp.w / m);
+        }
+        if (opt && opt->nside_x > 0) break;
+    }
+    *o = bestp;
+    o->form = fp32 ? FTE_FORM_MIXED : FTE_FORM_PLAIN;
+    return FTE_OK;
+}
+
 extern "C" int fte_choose_params(int kind, int64_t nsrc, int64_t ntar, const double* f1, const double* f2, double Lx,
                                  double Ly, const fte_options* opt, fte_params* out) {
     if (!out || (nsrc > 0 && (!f1 || !f2))) {
@@ -474,6 +615,7 @@ extern "C" int fte_choose_params(int kind, int64_t nsrc, int64_t ntar, const dou
         double a = f2[j] * (w ? w[j] : 1.0);
         Q += a * a;
     }
+    if (opt && opt->form == FTE_FORM_MIXED) return choose_params_tuned(kind, nsrc, ntar, Q + 1, Lx, Ly, opt, out);
     return choose_params_q(kind, nsrc, ntar, Q + 1, Lx, Ly, opt, out);
 }
 
@@ -810,9 +952,9 @@ static int ewald_entry(fte_context* c, int kind, const double* xsrc, const doubl
         fte_set_error("window support P must be even and in [2, 64] (P=%d)", opt->P);
         return FTE_ERR_INVALID;
     }
-    if (opt->form != FTE_FORM_PLAIN) {
-        fte_set_error("form %d is not available in this build", opt->form);
-        return FTE_ERR_UNSUPPORTED;
+    if (opt->form != FTE_FORM_PLAIN && opt->form != FTE_FORM_MIXED) {
+        fte_set_error("unknown form %d", opt->form);
+        return FTE_ERR_INVALID;
     }
     FTE_CUDA_TRY(cudaSetDevice(c->device));
     const bool host = !(flags & FTE_DEVICE_POINTERS);
@@ -867,7 +1009,10 @@ static int ewald_entry(fte_context* c, int kind, const double* xsrc, const doubl
     FTE_CUDA_TRY(cudaStreamSynchronize(c->stream));
     double Q = c->host_scalars[0] + 1.0;
     fte_params prm;
-    FTE_TRY(choose_params_q(kind, nsrc, ntar, Q, Lx, Ly, opt, &prm));
+    if (opt->form == FTE_FORM_MIXED)
+        FTE_TRY(choose_params_tuned(kind, nsrc, ntar, Q, Lx, Ly, opt, &prm));
+    else
+        FTE_TRY(choose_params_q(kind, nsrc, ntar, Q, Lx, Ly, opt, &prm));
     FTE_TRY(check_real_params(prm.xi, prm.nside_x, prm.nside_y));
     FTE_TRY(check_kspace_params(prm.xi, prm.eta, prm.Mx, prm.My, Lx, Ly, prm.w, prm.P));
     // second workspace: cell list, grids and outputs (the staged point data stays in the first)
@@ -884,7 +1029,7 @@ static int ewald_entry(fte_context* c, int kind, const double* xsrc, const doubl
         FTE_TRY(fte_record(c, 7));
         KspaceArgs a;
         a.kind = kind;
-        a.form = opt->form;
+        a.form = prm.form;
         a.nsrc = nsrc;
         a.ntar = ntar;
         a.psrc = ps;

@@ -625,6 +625,395 @@ size_t tile_budget(const fte_context* ctx) {
     size_t b = 110 * 1024;  // two CTAs per SM
     return b < (size_t)ctx->max_smem_optin ? b : (size_t)ctx->max_smem_optin;
 }
+
+// ===========================================================================
+// Mixed form: grids, spectra and window weights in FP32.
+//
+// Window weights: for node offset a the window is exp(t ((a - P/2) h - px)^2),
+// t = -2 xi^2/eta (the fast-Gaussian-gridding product with w = P h / 2, which
+// the drivers always use); the argument is formed in FP64 and the
+// exponential taken in FP32, so no error accumulates along the window (the
+// FP32 recurrence would lose ~P ulps).  The spread accumulates with Kahan
+// compensation (sum and carry per node); the gather sums a window column in
+// FP32 and the columns in FP64.  Filter multipliers are evaluated in FP64 and
+// applied to the FP32 spectra.
+// ===========================================================================
+__device__ __forceinline__ void win32(double pp, const WinParams& wp, float* out) {
+    const double t = -2 * wp.xi * wp.xi / wp.eta;
+    const int P1 = wp.P + 1;
+    for (int a = 0; a < P1; a++) {
+        double d = fma((double)(a - wp.P / 2), wp.h, -pp);
+        out[a] = expf((float)(t * d * d));
+    }
+}
+
+__device__ __forceinline__ void closest32(double x, double y, const WinParams& wp, int* mx, int* my, double* px,
+                                          double* py) {
+    fte_closest_node(x, y, wp.Lx, wp.Ly, wp.h, wp.P, mx, my, px, py);
+}
+
+constexpr int kColChunk32 = 64;
+
+__global__ void __launch_bounds__(kColThreads) k_spread_cols32(int mode, const double* __restrict__ p,
+                                                              const double* __restrict__ f,
+                                                              const double* __restrict__ nrm,
+                                                              const double* __restrict__ wts,
+                                                              const int* __restrict__ toff,
+                                                              const int* __restrict__ perm, int ts, int ntx, int nty,
+                                                              WinParams wp, float* __restrict__ H0,
+                                                              float* __restrict__ H1) {
+    extern __shared__ float shf[];
+    const int P1 = wp.P + 1, W = tile_region(ts, wp.P), WW = W * W;
+    float* sum = shf;                       // 2 * WW
+    float* car = sum + 2 * WW;              // 2 * WW (Kahan carries)
+    float* fw = car + 2 * WW;               // kColChunk32 * 2 * P1
+    float* wy = fw + kColChunk32 * 2 * P1;  // kColChunk32 * P1
+    int* org = reinterpret_cast<int*>(wy + kColChunk32 * P1);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int tile = blockIdx.x; tile < ntx * nty; tile += gridDim.x) {
+        const int k0 = toff[tile], k1 = toff[tile + 1];
+        if (k0 == k1) continue;
+        const int ox = (tile % ntx) * ts - wp.P / 2 - 2, oy = (tile / ntx) * ts - wp.P / 2 - 2;
+        __syncthreads();
+        for (int i = threadIdx.x; i < 4 * WW; i += blockDim.x) sum[i] = 0.f;
+        for (int c0 = k0; c0 < k1; c0 += kColChunk32) {
+            const int cn = min(kColChunk32, k1 - c0);
+            __syncthreads();
+            if (threadIdx.x < cn) {
+                const int s = threadIdx.x;
+                const int i = perm[c0 + s];
+                int mx, my;
+                double px, py;
+                closest32(p[2 * i], p[2 * i + 1], wp, &mx, &my, &px, &py);
+                double f1 = f[2 * i], f2 = f[2 * i + 1];
+                if (wts) {
+                    f1 *= wts[i];
+                    f2 *= wts[i];
+                }
+                double q0 = f1, q1 = f2;
+                if (mode == 1) {
+                    q0 = f1 * nrm[2 * i];
+                    q1 = f2 * nrm[2 * i];
+                } else if (mode == 2) {
+                    q0 = f1 * nrm[2 * i + 1];
+                    q1 = f2 * nrm[2 * i + 1];
+                }
+                float* wyx = wy + s * P1;
+                win32(py, wp, wyx);
+                float* fa = fw + (s * 2) * P1;
+                win32(px, wp, fa);
+                const float q0f = (float)q0, q1f = (float)q1;
+                for (int a = 0; a < P1; a++) {
+                    float wxa = fa[a];
+                    fa[a] = q0f * wxa;
+                    fa[P1 + a] = q1f * wxa;
+                }
+                const int lx = mx - ox, ly = my - oy;
+                if (lx >= 0 && ly >= 0 && lx + wp.P < W && ly + wp.P < W) {
+                    org[2 * s] = lx;
+                    org[2 * s + 1] = ly;
+                } else {
+                    org[2 * s] = -1;
+                    for (int a = 0; a < P1; a++) {
+                        size_t base = (size_t)fte_wrap_index(mx + a, wp.Mx) * wp.My;
+                        for (int j = 0; j < P1; j++) {
+                            size_t at = base + fte_wrap_index(my + j, wp.My);
+                            atomicAdd(&H0[at], fa[a] * wyx[j]);
+                            atomicAdd(&H1[at], fa[P1 + a] * wyx[j]);
+                        }
+                    }
+                }
+            }
+            __syncthreads();
+            for (int s = 0; s < cn; s++) {
+                const int lx = org[2 * s];
+                if (lx < 0) continue;
+                const int ly = org[2 * s + 1];
+                int c = lx + ((warp - lx) % nw + nw) % nw;
+                if (lane < P1) {
+                    const float wyj = wy[s * P1 + lane];
+                    const float* fa = fw + (s * 2) * P1;
+                    for (; c <= lx + wp.P; c += nw) {
+                        const int at = c * W + ly + lane;
+#pragma unroll
+                        for (int g = 0; g < 2; g++) {
+                            // Kahan: sum += v with carry
+                            float v = fa[g * P1 + c - lx] * wyj - car[g * WW + at];
+                            float s0 = sum[g * WW + at];
+                            float t = s0 + v;
+                            car[g * WW + at] = (t - s0) - v;
+                            sum[g * WW + at] = t;
+                        }
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < 2 * WW; idx += blockDim.x) {
+            float v = sum[idx] - car[idx];
+            if (v == 0.f) continue;
+            int g = idx >= WW, r = idx - g * WW;
+            int xx = r / W, yy = r - xx * W;
+            size_t at = (size_t)fte_wrap_index(ox + xx, wp.Mx) * wp.My + fte_wrap_index(oy + yy, wp.My);
+            atomicAdd(g ? &H1[at] : &H0[at], v);
+        }
+    }
+}
+
+size_t spread_cols32_smem(int ts, int P) {
+    const int P1 = P + 1, W = tile_region(ts, P);
+    return (size_t)(4 * W * W + kColChunk32 * 3 * P1) * sizeof(float) + kColChunk32 * 2 * sizeof(int);
+}
+
+__global__ void __launch_bounds__(kTileThreads) k_gather_tiled32(const double* __restrict__ p,
+                                                                const int* __restrict__ toff,
+                                                                const int* __restrict__ perm, int ts, int ntx,
+                                                                int nty, WinParams wp, const float* __restrict__ G0,
+                                                                const float* __restrict__ G1, double scale,
+                                                                double2* __restrict__ out) {
+    extern __shared__ float shf[];
+    const int P1 = wp.P + 1, W = tile_region(ts, wp.P), WW = W * W;
+    float* r0 = shf;
+    float* r1 = r0 + WW;
+    float* wxb = r1 + WW + threadIdx.x * 2 * P1;
+    float* wyb = wxb + P1;
+    for (int tile = blockIdx.x; tile < ntx * nty; tile += gridDim.x) {
+        const int k0 = toff[tile], k1 = toff[tile + 1];
+        if (k0 == k1) continue;
+        const int ox = (tile % ntx) * ts - wp.P / 2 - 2, oy = (tile / ntx) * ts - wp.P / 2 - 2;
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < WW; idx += blockDim.x) {
+            int xx = idx / W, yy = idx - xx * W;
+            size_t at = (size_t)fte_wrap_index(ox + xx, wp.Mx) * wp.My + fte_wrap_index(oy + yy, wp.My);
+            r0[idx] = __ldg(G0 + at);
+            r1[idx] = __ldg(G1 + at);
+        }
+        __syncthreads();
+        for (int k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
+            const int i = perm[k];
+            int mx, my;
+            double px, py;
+            closest32(p[2 * i], p[2 * i + 1], wp, &mx, &my, &px, &py);
+            win32(px, wp, wxb);
+            win32(py, wp, wyb);
+            const int lx = mx - ox, ly = my - oy;
+            const bool inside = lx >= 0 && ly >= 0 && lx + wp.P < W && ly + wp.P < W;
+            double acc0 = 0.0, acc1 = 0.0;
+            for (int a = 0; a < P1; a++) {
+                float s0 = 0.f, s1 = 0.f;
+                if (inside) {
+                    const float* c0 = r0 + (lx + a) * W + ly;
+                    const float* c1 = r1 + (lx + a) * W + ly;
+                    for (int j = 0; j < P1; j++) {
+                        s0 = fmaf(wyb[j], c0[j], s0);
+                        s1 = fmaf(wyb[j], c1[j], s1);
+                    }
+                } else {
+                    size_t base = (size_t)fte_wrap_index(mx + a, wp.Mx) * wp.My;
+                    for (int j = 0; j < P1; j++) {
+                        size_t at = base + fte_wrap_index(my + j, wp.My);
+                        s0 = fmaf(wyb[j], __ldg(G0 + at), s0);
+                        s1 = fmaf(wyb[j], __ldg(G1 + at), s1);
+                    }
+                }
+                acc0 = fma((double)wxb[a], (double)s0, acc0);
+                acc1 = fma((double)wxb[a], (double)s1, acc1);
+            }
+            out[i] = make_double2(acc0 * scale, acc1 * scale);
+        }
+    }
+}
+
+size_t gather32_smem(int ts, int P) {
+    const int W = tile_region(ts, P);
+    return (size_t)(2 * W * W + kTileThreads * 2 * (P + 1)) * sizeof(float);
+}
+
+// FP32 FFT passes (same structure as the FP64 kernels)
+__global__ void k_fft_y_r2c32(const float* __restrict__ H, float2* __restrict__ Hh, int Mx, int My, FftDev plan) {
+    extern __shared__ float2 shc32[];
+    float2* A = shc32;
+    float2* B = shc32 + plan.m;
+    const int c = blockIdx.x, g = blockIdx.y;
+    const int Kh = My / 2 + 1;
+    const float* h0 = H + ((size_t)g * Mx + 2 * c) * My;
+    const float* h1 = h0 + My;
+    for (int y = threadIdx.x; y < My; y += blockDim.x) A[y] = make_float2(h0[y], h1[y]);
+    float2* R = fft_block<float>(A, B, plan, false);
+    float2* o0 = Hh + ((size_t)g * Mx + 2 * c) * Kh;
+    float2* o1 = o0 + Kh;
+    for (int k = threadIdx.x; k < Kh; k += blockDim.x) {
+        float2 zk = R[k], zm = R[(My - k) % My];
+        o0[k] = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
+        o1[k] = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
+    }
+}
+
+__global__ void k_fft_x32(float2* __restrict__ Hh, int Mx, int Kh, FftDev plan, int inv) {
+    extern __shared__ float2 shc32[];
+    float2* A = shc32;
+    float2* B = shc32 + plan.m;
+    const int k = blockIdx.x, g = blockIdx.y;
+    float2* base = Hh + (size_t)g * Mx * Kh + k;
+    for (int x = threadIdx.x; x < Mx; x += blockDim.x) A[x] = base[(size_t)x * Kh];
+    float2* R = fft_block<float>(A, B, plan, inv != 0);
+    for (int x = threadIdx.x; x < Mx; x += blockDim.x) base[(size_t)x * Kh] = R[x];
+}
+
+__global__ void k_fft_y_c2r32(const float2* __restrict__ Hh, float* __restrict__ H, int Mx, int My, FftDev plan) {
+    extern __shared__ float2 shc32[];
+    float2* A = shc32;
+    float2* B = shc32 + plan.m;
+    const int c = blockIdx.x, g = blockIdx.y;
+    const int Kh = My / 2 + 1;
+    const float2* i0 = Hh + ((size_t)g * Mx + 2 * c) * Kh;
+    const float2* i1 = i0 + Kh;
+    for (int k = threadIdx.x; k < Kh; k += blockDim.x) {
+        float2 a = i0[k], b = i1[k];
+        if (k == 0 || 2 * k == My) {
+            a.y = 0.f;
+            b.y = 0.f;
+        }
+        A[k] = make_float2(a.x - b.y, a.y + b.x);
+        if (k > 0 && 2 * k < My) A[My - k] = make_float2(a.x + b.y, -a.y + b.x);
+    }
+    float2* R = fft_block<float>(A, B, plan, true);
+    float* o0 = H + ((size_t)g * Mx + 2 * c) * My;
+    float* o1 = o0 + My;
+    for (int y = threadIdx.x; y < My; y += blockDim.x) {
+        float2 z = R[y];
+        o0[y] = z.x;
+        o1[y] = z.y;
+    }
+}
+
+// multipliers in FP64 applied to FP32 spectra (same Nyquist averaging)
+template <int KIND>
+__global__ void k_filter32(float2* __restrict__ Hh, int Mx, int My, double Lx, double Ly, double xi, double eta) {
+    const int Kh = My / 2 + 1;
+    const size_t GS = (size_t)Mx * Kh;
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < GS; idx += (size_t)gridDim.x * blockDim.x) {
+        int j = (int)(idx / Kh), k = (int)(idx % Kh);
+        float2* p0 = Hh + idx;
+        if (j == 0 && k == 0) {
+            p0[0] = make_float2(0.f, 0.f);
+            p0[GS] = make_float2(0.f, 0.f);
+            continue;
+        }
+        double k1 = (j <= Mx / 2) ? 2.0 * FTE_PI / Lx * j : 2.0 * FTE_PI / Lx * (j - Mx);
+        double k2 = 2.0 * FTE_PI / Ly * k;
+        bool nyq_x = (2 * j == Mx), nyq_y = (2 * k == My);
+        double2 g1, g2;
+        auto d2 = [](float2 v) { return make_double2(v.x, v.y); };
+        if (KIND == FTE_KIND_SLP) {
+            double2 q1 = d2(p0[0]), q2 = d2(p0[GS]);
+            slp_mult(k1, k2, xi, eta, q1, q2, g1, g2);
+            if (nyq_x || nyq_y) {
+                double2 h1, h2;
+                slp_mult(nyq_x ? -k1 : k1, nyq_y ? -k2 : k2, xi, eta, q1, q2, h1, h2);
+                g1 = make_double2(0.5 * (g1.x + h1.x), 0.5 * (g1.y + h1.y));
+                g2 = make_double2(0.5 * (g2.x + h2.x), 0.5 * (g2.y + h2.y));
+            }
+        } else {
+            double2 a = d2(p0[0]), s21 = d2(p0[GS]), s12 = d2(p0[2 * GS]), d = d2(p0[3 * GS]);
+            dlp_mult(k1, k2, xi, eta, a, s21, s12, d, g1, g2);
+            if (nyq_x || nyq_y) {
+                double2 h1, h2;
+                dlp_mult(nyq_x ? -k1 : k1, nyq_y ? -k2 : k2, xi, eta, a, s21, s12, d, h1, h2);
+                g1 = make_double2(0.5 * (g1.x + h1.x), 0.5 * (g1.y + h1.y));
+                g2 = make_double2(0.5 * (g2.x + h2.x), 0.5 * (g2.y + h2.y));
+            }
+        }
+        p0[0] = make_float2((float)g1.x, (float)g1.y);
+        p0[GS] = make_float2((float)g2.x, (float)g2.y);
+    }
+}
+
+int kspace_run_mixed(fte_context* ctx, WsCarver& wc, const KspaceArgs& a) {
+    const int ng = a.kind == FTE_KIND_SLP ? 2 : 4;
+    const int Mx = a.Mx, My = a.My;
+    const size_t G = (size_t)Mx * My;
+    const int Kh = My / 2 + 1;
+    float* H = wc.take<float>(ng * G);
+    float2* Hh = wc.take<float2>(ng * (size_t)Mx * Kh);
+    FTE_WS_CHECK(wc);
+    WinParams wp;
+    wp.Lx = a.Lx;
+    wp.Ly = a.Ly;
+    wp.h = a.Lx / Mx;
+    wp.xi = a.xi;
+    wp.eta = a.eta;
+    wp.w = a.w;
+    wp.P = a.P;
+    wp.Mx = Mx;
+    wp.My = My;
+    FftDev py, px;
+    FTE_TRY(fte_get_plan(ctx, My, &py));
+    FTE_TRY(fte_get_plan(ctx, Mx, &px));
+    size_t sm_y = 2 * (size_t)py.m * sizeof(float2), sm_x = 2 * (size_t)px.m * sizeof(float2);
+    if (sm_y > (size_t)ctx->max_smem_optin || sm_x > (size_t)ctx->max_smem_optin) {
+        fte_set_error("grid %d x %d beyond this build's shared-memory transform", Mx, My);
+        return FTE_ERR_UNSUPPORTED;
+    }
+    int ts_s = 0, ts_g = 0;
+    for (int ts = 64; ts >= 8 && !ts_s; ts -= 4)
+        if (spread_cols32_smem(ts, a.P) <= tile_budget(ctx)) ts_s = ts;
+    for (int ts = 64; ts >= 8 && !ts_g; ts -= 4)
+        if (gather32_smem(ts, a.P) <= tile_budget(ctx)) ts_g = ts;
+    if (!ts_s || !ts_g) {
+        fte_set_error("window support P=%d too large for the mixed form's tiles", a.P);
+        return FTE_ERR_UNSUPPORTED;
+    }
+    TileBins tb_s, tb_g;
+    if (a.nsrc > 0)
+        FTE_TRY(fte_tiles_build(ctx, wc, a.psrc, a.nsrc, a.Lx, a.Ly, wp.h, ts_s, (Mx + ts_s - 1) / ts_s,
+                                (My + ts_s - 1) / ts_s, &tb_s));
+    if (a.ntar > 0)
+        FTE_TRY(fte_tiles_build(ctx, wc, a.ptar, a.ntar, a.Lx, a.Ly, wp.h, ts_g, (Mx + ts_g - 1) / ts_g,
+                                (My + ts_g - 1) / ts_g, &tb_g));
+    FTE_TRY(fte_record(ctx, 2));
+    FTE_CUDA_TRY(cudaMemsetAsync(H, 0, sizeof(float) * ng * G, ctx->stream));
+    if (a.nsrc > 0) {
+        size_t sm = spread_cols32_smem(ts_s, a.P);
+        int nt = tb_s.ntx * tb_s.nty;
+        int grid = nt < ctx->num_sms * 8 ? nt : ctx->num_sms * 8;
+        FTE_CUDA_TRY(cudaFuncSetAttribute(k_spread_cols32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        for (int pass = 0; pass < ng / 2; pass++) {
+            int mode = ng == 2 ? 0 : 1 + pass;
+            FTE_LAUNCH(ctx, k_spread_cols32, grid, kColThreads, sm, mode, a.psrc, a.f, a.nrm, a.wts,
+                       (const int*)tb_s.off, (const int*)tb_s.perm, ts_s, tb_s.ntx, tb_s.nty, wp, H + 2 * pass * G,
+                       H + (2 * pass + 1) * G);
+        }
+    }
+    FTE_TRY(fte_record(ctx, 3));
+    FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_y_r2c32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_y));
+    FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_y_c2r32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_y));
+    FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_x32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_x));
+    FTE_LAUNCH(ctx, k_fft_y_r2c32, dim3(Mx / 2, ng), fft_threads(py.m), sm_y, (const float*)H, Hh, Mx, My, py);
+    FTE_LAUNCH(ctx, k_fft_x32, dim3(Kh, ng), fft_threads(px.m), sm_x, Hh, Mx, Kh, px, 0);
+    int fb = (int)(((size_t)Mx * Kh + 255) / 256);
+    if (fb > ctx->num_sms * 32) fb = ctx->num_sms * 32;
+    if (a.kind == FTE_KIND_SLP)
+        FTE_LAUNCH(ctx, k_filter32<FTE_KIND_SLP>, fb, 256, 0, Hh, Mx, My, a.Lx, a.Ly, a.xi, a.eta);
+    else
+        FTE_LAUNCH(ctx, k_filter32<FTE_KIND_DLP>, fb, 256, 0, Hh, Mx, My, a.Lx, a.Ly, a.xi, a.eta);
+    FTE_LAUNCH(ctx, k_fft_x32, dim3(Kh, 2), fft_threads(px.m), sm_x, Hh, Mx, Kh, px, 1);
+    FTE_LAUNCH(ctx, k_fft_y_c2r32, dim3(Mx / 2, 2), fft_threads(py.m), sm_y, (const float2*)Hh, H, Mx, My, py);
+    FTE_TRY(fte_record(ctx, 4));
+    double s = 4 * a.xi * a.xi / a.eta;
+    s = s * s * wp.h * wp.h / FTE_PI;
+    double scale = s / (4 * FTE_PI) / ((double)Mx * (double)My);
+    if (a.ntar > 0) {
+        size_t sm = gather32_smem(ts_g, a.P);
+        int nt = tb_g.ntx * tb_g.nty;
+        int grid = nt < ctx->num_sms * 8 ? nt : ctx->num_sms * 8;
+        FTE_CUDA_TRY(cudaFuncSetAttribute(k_gather_tiled32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        FTE_LAUNCH(ctx, k_gather_tiled32, grid, kTileThreads, sm, a.ptar, (const int*)tb_g.off, (const int*)tb_g.perm,
+                   ts_g, tb_g.ntx, tb_g.nty, wp, (const float*)H, (const float*)(H + G), scale, a.uk);
+    }
+    FTE_TRY(fte_record(ctx, 5));
+    return FTE_OK;
+}
 }  // namespace
 
 size_t fte_kspace_ws(int kind, int form, int Mx, int My, int64_t nsrc, int64_t ntar) {
@@ -639,6 +1028,7 @@ size_t fte_kspace_ws(int kind, int form, int Mx, int My, int64_t nsrc, int64_t n
 }
 
 int fte_kspace_run(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, fte_info* info) {
+    if (a.form == FTE_FORM_MIXED) return kspace_run_mixed(ctx, wc, a);
     const int ng = a.kind == FTE_KIND_SLP ? 2 : 4;
     const int Mx = a.Mx, My = a.My;
     const size_t G = (size_t)Mx * My;

@@ -78,6 +78,7 @@ typedef struct {
     int Mx, My;     /* grid size */
     double w;       /* window half-width P*h/2 */
     double eta;     /* window shape (2 xi w / m)^2, m = 0.95 sqrt(pi P) */
+    int form;       /* arithmetic of the k-space part: FTE_FORM_PLAIN (FP64) or FTE_FORM_MIXED (FP32) */
 } fte_params;
 
 /* Options of the driver-level entries; zero-initialise for the reference

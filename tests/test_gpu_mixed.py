@@ -1,0 +1,82 @@
+"""The mixed form (tuned parameters; FP32 spread/FFT/filter/gather when the
+tolerance allows it, FP64 real-space sums) against converged FP64 Ewald sums.
+
+The requested tolerance is the bar: max |u - u_truth| / max |u_truth| <= tol
+(per component set, SLP and DLP), on seeded uniform and clustered inputs.
+"""
+import numpy as np
+import pytest
+
+from conftest import load_golden
+from oracle import pyoracle as po
+
+pytestmark = pytest.mark.gpu
+
+
+def _ft():
+    import fasttools2d_gb300 as ft
+
+    return ft
+
+
+def _case(seed, n, Lx, Ly):
+    rng = np.random.default_rng(seed)
+    xs, ys = (rng.random(n) - 0.5) * Lx, (rng.random(n) - 0.5) * Ly
+    xt, yt = (rng.random(n) - 0.5) * Lx, (rng.random(n) - 0.5) * Ly
+    f1, f2 = rng.standard_normal(n), rng.standard_normal(n)
+    f1 -= f1.mean()
+    f2 -= f2.mean()
+    th = rng.random(n) * 2 * np.pi
+    return xs, ys, xt, yt, f1, f2, np.cos(th), np.sin(th)
+
+
+@pytest.mark.parametrize("tol", [1e-6, 1e-8, 1e-10])
+@pytest.mark.parametrize("geom", [(20000, 1.0, 1.0, 31), (12000, 2.0, 1.0, 32)])
+def test_mixed_form_meets_tolerance(gpu_ctx, tol, geom):
+    ft = _ft()
+    n, Lx, Ly, seed = geom
+    xs, ys, xt, yt, f1, f2, n1, n2 = _case(seed, n, Lx, Ly)
+    idx = np.arange(0, n, 40)
+    for kind in ("slp", "dlp"):
+        if kind == "slp":
+            out, info = ft.StokesSLP_ewald_2p(xs, ys, xt, yt, f1, f2, Lx, Ly, tol=tol, form=ft.FORM_MIXED,
+                                              ctx=gpu_ctx, return_info=True)
+            truth = po.ewald_truth(po.KIND_SLP, xs, ys, xt[idx], yt[idx], f1, f2, Lx, Ly)
+        else:
+            out, info = ft.StokesDLP_ewald_2p(xs, ys, xt, yt, n1, n2, f1, f2, Lx, Ly, tol=tol, form=ft.FORM_MIXED,
+                                              ctx=gpu_ctx, return_info=True)
+            truth = po.ewald_truth(po.KIND_DLP, xs, ys, xt[idx], yt[idx], f1, f2, Lx, Ly, n1=n1, n2=n2)
+        u = np.stack([out[0][idx], out[1][idx]], 1)
+        err = np.max(np.abs(u - truth)) / np.max(np.abs(truth))
+        assert err <= tol, (kind, err, info.params.as_dict())
+        # the FP32 k-space is used only where it can meet the tolerance
+        assert info.params.form == (ft.FORM_MIXED if tol >= 1e-7 else ft.FORM_PLAIN)
+
+
+def test_mixed_form_on_ellipses(gpu_ctx):
+    """Clustered boundary points with self-coincident targets (config 2 in
+    miniature), tol 1e-8, against the reference's own SE output at tol 1e-10."""
+    ft = _ft()
+    g = load_golden("config2_mini")
+    for kind in ("slp", "dlp"):
+        if kind == "slp":
+            out = ft.StokesSLP_ewald_2p(g["xsrc"], g["ysrc"], g["xtar"], g["ytar"], g["f1"], g["f2"], 2.0, 1.0,
+                                        tol=1e-8, form=ft.FORM_MIXED, ctx=gpu_ctx)
+        else:
+            out = ft.StokesDLP_ewald_2p(g["xsrc"], g["ysrc"], g["xtar"], g["ytar"], g["n1"], g["n2"], g["f1"],
+                                        g["f2"], 2.0, 1.0, tol=1e-8, form=ft.FORM_MIXED, ctx=gpu_ctx)
+        ref = g[kind + "_u"]
+        u = np.stack([out[0], out[1]], 1)
+        assert np.max(np.abs(u - ref)) / np.max(np.abs(ref)) <= 1e-8
+
+
+def test_tuned_parameters_are_cheaper(gpu_ctx):
+    ft = _ft()
+    rng = np.random.default_rng(5)
+    n = 1_000_000
+    f1, f2 = rng.standard_normal(n), rng.standard_normal(n)
+    plain = ft.choose_params(ft.KIND_SLP, f1, f2, n, 1.0, 1.0, tol=1e-6)
+    tuned = ft.choose_params(ft.KIND_SLP, f1, f2, n, 1.0, 1.0, tol=1e-6, form=ft.FORM_MIXED)
+    assert tuned.P < plain.P
+    assert tuned.nside_x > plain.nside_x  # smaller cutoff: fewer FP64 near pairs
+    assert tuned.form == ft.FORM_MIXED
