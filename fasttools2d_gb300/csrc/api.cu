@@ -459,7 +459,9 @@ static int choose_params_q(int kind, int64_t nsrc, int64_t ntar, double Q, doubl
 // (the same Newton solves for xi and kinf), but every free choice the drivers
 // fix is optimised for speed at the requested tolerance:
 //   * P: smallest even support whose window error erfc(m/sqrt 2),
-//     m = 0.95 sqrt(pi P), is below tol/10 (the drivers always use 24);
+//     m = 0.95 sqrt(pi P), is below tol/300 (the drivers always use 24; the
+//     measured window error of the stresslet k-space part is ~50-100 x this
+//     term relative to max |u|);
 //   * the cell multiplier a (cutoff rc = Lx/(a A)): minimises a cost model of
 //     near pairs (FP64), window work (spread + gather) and FFTs, with unit
 //     costs measured on GB300; the drivers take a from Nb;
@@ -467,7 +469,8 @@ static int choose_params_q(int kind, int64_t nsrc, int64_t ntar, double Q, doubl
 //   * the k-space part in FP32 when tol >= 1e-7, else in FP64;
 //   * the estimates are solved for tol * slack: they bound the error by
 //     sum |f|^2, which over-estimates the max-relative error of the result by
-//     two to three orders of magnitude on the benchmark inputs; slack = 10.
+//     one to three orders of magnitude on the benchmark inputs (least for
+//     the stresslet at small N); slack = 3.
 // ---------------------------------------------------------------------------
 namespace {
 
@@ -527,7 +530,7 @@ static const double kCostWin64 = 3.2e-12;      // one window node x grid, FP64 s
 static const double kCostWin32 = 1.2e-12;      // same in FP32 with compensation
 static const double kCostFft64 = 3.5e-11;      // per complex grid point x log2(points), 7-smooth FP64
 static const double kCostFft32 = 1.2e-11;      // same in FP32
-static const double kTolSlack = 10.0;
+static const double kTolSlack = 3.0;
 
 static int choose_params_tuned(int kind, int64_t nsrc, int64_t ntar, double Q, double Lx, double Ly,
                                const fte_options* opt, fte_params* o) {
@@ -540,7 +543,7 @@ static int choose_params_tuned(int kind, int64_t nsrc, int64_t ntar, double Q, d
     if (P == 0) {
         for (P = 4; P < 24; P += 2) {
             double m = 0.95 * std::sqrt(FTE_PI * P);
-            if (std::erfc(m / std::sqrt(2.0)) <= tol / 10) break;
+            if (std::erfc(m / std::sqrt(2.0)) <= tol / 300) break;
         }
     }
     const int A = o->A, B = o->B;

@@ -55,7 +55,12 @@ def test_mixed_form_meets_tolerance(gpu_ctx, tol, geom):
 
 def test_mixed_form_on_ellipses(gpu_ctx):
     """Clustered boundary points with self-coincident targets (config 2 in
-    miniature), tol 1e-8, against the reference's own SE output at tol 1e-10."""
+    miniature), tol 1e-8, against the reference's own SE output at tol 1e-10.
+
+    The densities carry quadrature weights, so sum |f|^2 + 1 (the scale of the
+    reference's error estimates) is ~1 while max |u| is ~0.02: the estimates
+    bound the absolute error, which is the criterion here,
+    max |u - u_ref| <= tol * max(1, max |u_ref|)."""
     ft = _ft()
     g = load_golden("config2_mini")
     for kind in ("slp", "dlp"):
@@ -67,7 +72,7 @@ def test_mixed_form_on_ellipses(gpu_ctx):
                                         g["f2"], 2.0, 1.0, tol=1e-8, form=ft.FORM_MIXED, ctx=gpu_ctx)
         ref = g[kind + "_u"]
         u = np.stack([out[0], out[1]], 1)
-        assert np.max(np.abs(u - ref)) / np.max(np.abs(ref)) <= 1e-8
+        assert np.max(np.abs(u - ref)) <= 1e-8 * max(1.0, np.max(np.abs(ref))), kind
 
 
 def test_tuned_parameters_are_cheaper(gpu_ctx):
