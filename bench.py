@@ -205,26 +205,13 @@ def main():
     import fasttools2d_gb300 as ft
     from fasttools2d_gb300 import workloads as wl
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
+    from fasttools2d_gb300.replicas import Replicas
 
-        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
-    torch.cuda.set_device(local_rank)
-
-    def barrier():
-        if dist is not None:
-            dist.barrier()
-
-    def max_over_ranks(x: float) -> float:
-        if dist is None:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    reps = Replicas()
+    world, rank, local_rank = reps.world, reps.rank, reps.local_rank
+    barrier = reps.barrier
+    max_over_ranks = reps.max
 
     if not os.path.exists(ft.LIB_PATH):
         ft.build()
@@ -400,8 +387,7 @@ def main():
         line["cpu_baseline"] = cpu_baseline(N)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    if dist is not None:
-        dist.destroy_process_group()
+    reps.close()
 
 
 if __name__ == "__main__":
