@@ -104,6 +104,16 @@ SIGNATURES = {
     "fte_stokes_dlp_ewald_2p": (_i, [_vp, _vp, _vp, _i64, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _d, _d,
                                      C.POINTER(Options), _vp, _vp, _vp, _vp, C.POINTER(Info), _u]),
     "fte_choose_params": (_i, [_i, _i64, _i64, _vp, _vp, _d, _d, C.POINTER(Options), C.POINTER(Params)]),
+    "fte_plan_create": (_i, [_vp, _i, _vp, _vp, _i64, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _d, _d,
+                             C.POINTER(Options), _i, C.POINTER(_vp), _u]),
+    "fte_plan_params": (_i, [_vp, C.POINTER(Params)]),
+    "fte_plan_execute": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _u]),
+    "fte_plan_destroy": (_i, [_vp]),
+    "fte_batch_create": (_i, [_vp, C.POINTER(_vp), _i, _i, C.POINTER(_vp)]),
+    "fte_batch_launch": (_i, [_vp, _i]),
+    "fte_batch_destroy": (_i, [_vp]),
+    "fte_batch_set_density": (_i, [_vp, _i, _vp, _vp, _u]),
+    "fte_batch_get_velocity": (_i, [_vp, _i, _vp, _vp, _u]),
 }
 
 
@@ -406,3 +416,100 @@ def choose_params(kind, f1, f2, ntar, Lx, Ly, P=None, Nb=None, tol=1e-16, **kw) 
     _check(lib().fte_choose_params(int(kind), len(f1), int(ntar), f1.ctypes.data, f2.ctypes.data, float(Lx),
                                    float(Ly), C.byref(opt), C.byref(prm)))
     return prm
+
+
+# ---- plans and batches -----------------------------------------------------------
+
+class Plan:
+    """Geometry of one SE evaluation reused across density vectors (a GMRES
+    loop): parameters, cell list, tile bins and scratch are set up once.
+
+    ``execute(f1s, f2s)`` takes arrays of shape (nv, nsrc) (numpy or CUDA
+    tensors) and returns velocities of shape (nv, ntar)."""
+
+    def __init__(self, kind, xsrc, ysrc, xtar, ytar, f1, f2, Lx, Ly, n1=None, n2=None, P=None, Nb=None,
+                 tol=1e-16, form=FORM_PLAIN, weights=None, nvmax=4, ctx: Context | None = None, **kw):
+        self.ctx = ctx or default_context()
+        A = _Args()
+        pxs, ns = A.arr(xsrc, 1)
+        pys, _ = A.arr(ysrc, 1)
+        pxt, nt = A.arr(xtar, 1)
+        pyt, _ = A.arr(ytar, 1)
+        pn1, _ = A.arr(n1, 1)
+        pn2, _ = A.arr(n2, 1)
+        pf1, _ = A.arr(f1, 1)
+        pf2, _ = A.arr(f2, 1)
+        pw, _ = A.arr(weights, 1)
+        opt = _options(P, Nb, tol, weights_ptr=pw, form=form, **kw)
+        h = _vp()
+        _check(lib().fte_plan_create(self.ctx.h, int(kind), pxs, pys, ns, pxt, pyt, nt, pn1, pn2, pf1, pf2,
+                                     float(Lx), float(Ly), C.byref(opt), int(nvmax), C.byref(h), A.flags))
+        self.h = h
+        self.kind, self.nsrc, self.ntar, self.nvmax = int(kind), ns, nt, int(nvmax)
+
+    @property
+    def params(self) -> Params:
+        p = Params()
+        _check(lib().fte_plan_params(self.h, C.byref(p)))
+        return p
+
+    def execute(self, f1s, f2s):
+        A = _Args()
+        pf1, n1 = A.arr(f1s, 1)
+        pf2, _ = A.arr(f2s, 1)
+        nv = n1 // max(self.nsrc, 1) if self.nsrc else 1
+        u1, pu1 = A.out((nv, self.ntar))
+        u2, pu2 = A.out((nv, self.ntar))
+        _check(lib().fte_plan_execute(self.h, nv, pf1, pf2, pu1, pu2, A.flags))
+        return u1, u2
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().fte_plan_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Many plans evaluated by one launch (a replayed CUDA graph)."""
+
+    def __init__(self, plans, nv: int, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        self.plans = list(plans)
+        self.nv = int(nv)
+        arr = (_vp * len(self.plans))(*[p.h for p in self.plans])
+        h = _vp()
+        _check(lib().fte_batch_create(self.ctx.h, arr, len(self.plans), self.nv, C.byref(h)))
+        self.h = h
+
+    def set_density(self, i, f1s, f2s):
+        A = _Args()
+        pf1, _ = A.arr(f1s, 1)
+        pf2, _ = A.arr(f2s, 1)
+        _check(lib().fte_batch_set_density(self.h, int(i), pf1, pf2, A.flags))
+
+    def launch(self, use_graph: bool = True):
+        _check(lib().fte_batch_launch(self.h, 1 if use_graph else 0))
+
+    def velocity(self, i):
+        p = self.plans[i]
+        u1 = np.empty((self.nv, p.ntar))
+        u2 = np.empty((self.nv, p.ntar))
+        _check(lib().fte_batch_get_velocity(self.h, int(i), u1.ctypes.data, u2.ctypes.data, 0))
+        return u1, u2
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().fte_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

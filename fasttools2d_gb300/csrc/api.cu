@@ -598,6 +598,12 @@ static int choose_params_tuned(int kind, int64_t nsrc, int64_t ntar, double Q, d
     return FTE_OK;
 }
 
+int fte_choose_params_ex(int kind, int64_t nsrc, int64_t ntar, double Q, double Lx, double Ly, const fte_options* opt,
+                         fte_params* out) {
+    if (opt && opt->form == FTE_FORM_MIXED) return choose_params_tuned(kind, nsrc, ntar, Q, Lx, Ly, opt, out);
+    return choose_params_q(kind, nsrc, ntar, Q, Lx, Ly, opt, out);
+}
+
 extern "C" int fte_choose_params(int kind, int64_t nsrc, int64_t ntar, const double* f1, const double* f2, double Lx,
                                  double Ly, const fte_options* opt, fte_params* out) {
     if (!out || (nsrc > 0 && (!f1 || !f2))) {

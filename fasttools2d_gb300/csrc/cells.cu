@@ -76,10 +76,11 @@ __global__ void k_scatter_src(const double* __restrict__ p, const double* __rest
                               const double* __restrict__ nrm, const double* __restrict__ wts, int64_t n,
                               const int* __restrict__ box, const int* __restrict__ rank, const int* __restrict__ off,
                               double2* __restrict__ spos, double* __restrict__ q0, double* __restrict__ q1,
-                              double* __restrict__ q2) {
+                              double* __restrict__ q2, int* __restrict__ sidx) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         int d = off[box[i]] + rank[i];
         spos[d] = make_double2(p[2 * i], p[2 * i + 1]);
+        sidx[d] = (int)i;
         double f1 = f[2 * i], f2 = f[2 * i + 1];
         if (wts) {
             f1 *= wts[i];
@@ -166,6 +167,7 @@ size_t fte_cells_ws(int64_t nsrc, int64_t ntar, int nb) {
     s += 3 * ws_bytes((size_t)(nsrc + 1), sizeof(double));       // q0..q2
     s += ws_bytes((size_t)(ntar + 1), sizeof(double2));          // tpos
     s += ws_bytes((size_t)(ntar + 1), sizeof(int));              // tidx
+    s += ws_bytes((size_t)(nsrc + 1), sizeof(int));              // sidx
     s += 4 * ws_bytes((size_t)(nb + 1) / 4096 + 8, sizeof(int)); // scan partials
     return s + 4096;
 }
@@ -192,6 +194,9 @@ int fte_cells_build(fte_context* ctx, WsCarver& wc, int kind, const double* psrc
     cl->tpos = wc.take<double2>(ntar + 1);
     cl->tidx = wc.take<int>(ntar + 1);
     cl->max_neigh = 0;
+    cl->qstride = 0;
+    cl->sidx = wc.take<int>(nsrc + 1);
+    FTE_WS_CHECK(wc);
     FTE_WS_CHECK(wc);
     FTE_CUDA_TRY(cudaMemsetAsync(scnt, 0, sizeof(int) * (nb + 1), ctx->stream));
     FTE_CUDA_TRY(cudaMemsetAsync(tcnt, 0, sizeof(int) * (nb + 1), ctx->stream));
@@ -205,10 +210,12 @@ int fte_cells_build(fte_context* ctx, WsCarver& wc, int kind, const double* psrc
     if (nsrc > 0) {
         if (kind == FTE_KIND_SLP)
             FTE_LAUNCH(ctx, k_scatter_src<FTE_KIND_SLP>, grid_for(nsrc, 256, maxb), 256, 0, psrc, f, nrm, wts, nsrc,
-                       (const int*)sbox, (const int*)srank, (const int*)cl->src_off, cl->spos, cl->q0, cl->q1, cl->q2);
+                       (const int*)sbox, (const int*)srank, (const int*)cl->src_off, cl->spos, cl->q0, cl->q1, cl->q2,
+                       cl->sidx);
         else
             FTE_LAUNCH(ctx, k_scatter_src<FTE_KIND_DLP>, grid_for(nsrc, 256, maxb), 256, 0, psrc, f, nrm, wts, nsrc,
-                       (const int*)sbox, (const int*)srank, (const int*)cl->src_off, cl->spos, cl->q0, cl->q1, cl->q2);
+                       (const int*)sbox, (const int*)srank, (const int*)cl->src_off, cl->spos, cl->q0, cl->q1, cl->q2,
+                       cl->sidx);
     }
     if (ntar > 0)
         FTE_LAUNCH(ctx, k_scatter_tar, grid_for(ntar, 256, maxb), 256, 0, ptar, ntar, (const int*)tbox,

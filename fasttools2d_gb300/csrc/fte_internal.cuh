@@ -183,6 +183,8 @@ struct CellList {
     double2* tpos;
     int* tidx;      // original index of each sorted target
     int max_neigh;  // upper bound of sources in a 3x3 neighbourhood (0 = unknown)
+    long long qstride;  // distance between density vectors in q0..q2 (0: one vector)
+    int* sidx;          // original index of each sorted source (plans only; may be null)
 };
 
 size_t fte_cells_ws(int64_t nsrc, int64_t ntar, int nb);
@@ -202,6 +204,19 @@ int fte_tiles_build(fte_context* ctx, WsCarver& wc, const double* p, int64_t n, 
                     int ts, int ntx, int nty, TileBins* out);
 
 int fte_near_launch(fte_context* ctx, int kind, const CellList& cl, double xi, double Lx, double Ly, double2* ur);
+// Near-field launch description, opaque outside near.cu.
+struct NearParamsHost {
+    alignas(16) unsigned char raw[256];
+};
+void fte_near_fill_params(int kind, const CellList& cl, double xi, double Lx, double Ly, NearParamsHost* hp);
+size_t fte_near_params_size();
+int fte_near_cap(const fte_context* ctx, int kind, int nv);
+// nv (1..4) density vectors at q* + v*cl.qstride; outputs at ur + v*ustride
+int fte_near_launch_nv(fte_context* ctx, int kind, int nv, const NearParamsHost& hp, double2* ur, long long ustride);
+// many problems in one launch: plist_dev = device array of the filled
+// descriptions (ur/ustride/cap set), items = (problem, box) pairs
+int fte_near_launch_batch(fte_context* ctx, int kind, int nv, const void* plist_dev, const int2* items, int nitems);
+void fte_near_set_output(NearParamsHost* hp, double2* ur, long long ustride, int cap);
 
 struct KspaceArgs {
     int kind;
@@ -215,6 +230,11 @@ struct KspaceArgs {
     double xi, eta, w, Lx, Ly;
     int Mx, My, P;
     double2* uk;         // output, interleaved
+    // tile bins built beforehand (plans); null: built by the call
+    const TileBins* pre_src = nullptr;
+    const TileBins* pre_tar = nullptr;
 };
 size_t fte_kspace_ws(int kind, int form, int Mx, int My, int64_t nsrc, int64_t ntar);
+// build the spread/gather tile bins that fte_kspace_run would build for `a`
+int fte_kspace_tiles(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, TileBins* src, TileBins* tar);
 int fte_kspace_run(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, fte_info* info);

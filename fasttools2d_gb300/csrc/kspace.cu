@@ -965,12 +965,20 @@ int kspace_run_mixed(fte_context* ctx, WsCarver& wc, const KspaceArgs& a) {
         return FTE_ERR_UNSUPPORTED;
     }
     TileBins tb_s, tb_g;
-    if (a.nsrc > 0)
+    if (a.pre_src && a.nsrc > 0)
+        tb_s = *a.pre_src;
+    else if (a.nsrc > 0)
         FTE_TRY(fte_tiles_build(ctx, wc, a.psrc, a.nsrc, a.Lx, a.Ly, wp.h, ts_s, (Mx + ts_s - 1) / ts_s,
                                 (My + ts_s - 1) / ts_s, &tb_s));
-    if (a.ntar > 0)
+    if (a.pre_tar && a.ntar > 0)
+        tb_g = *a.pre_tar;
+    else if (a.ntar > 0)
         FTE_TRY(fte_tiles_build(ctx, wc, a.ptar, a.ntar, a.Lx, a.Ly, wp.h, ts_g, (Mx + ts_g - 1) / ts_g,
                                 (My + ts_g - 1) / ts_g, &tb_g));
+    if ((a.nsrc > 0 && tb_s.ts != ts_s) || (a.ntar > 0 && tb_g.ts != ts_g)) {
+        fte_set_error("internal: prebuilt tiles do not match the mixed-form tile sizes");
+        return FTE_ERR_INVALID;
+    }
     FTE_TRY(fte_record(ctx, 2));
     FTE_CUDA_TRY(cudaMemsetAsync(H, 0, sizeof(float) * ng * G, ctx->stream));
     if (a.nsrc > 0) {
@@ -1015,6 +1023,32 @@ int kspace_run_mixed(fte_context* ctx, WsCarver& wc, const KspaceArgs& a) {
     return FTE_OK;
 }
 }  // namespace
+
+int fte_kspace_tiles(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, TileBins* src, TileBins* tar) {
+    const int ng = a.kind == FTE_KIND_SLP ? 2 : 4;
+    int ts_s = 0, ts_g = 0;
+    if (a.form == FTE_FORM_MIXED) {
+        for (int ts = 64; ts >= 8 && !ts_s; ts -= 4)
+            if (spread_cols32_smem(ts, a.P) <= tile_budget(ctx)) ts_s = ts;
+        for (int ts = 64; ts >= 8 && !ts_g; ts -= 4)
+            if (gather32_smem(ts, a.P) <= tile_budget(ctx)) ts_g = ts;
+    } else {
+        for (int ts = 64; ts >= 8 && !ts_s; ts -= 4)
+            if (spread_cols_smem(ts, a.P) <= tile_budget(ctx)) ts_s = ts;
+        ts_g = pick_tile(2, a.P, tile_budget(ctx));
+    }
+    (void)ng;
+    src->ts = tar->ts = 0;
+    src->ntx = tar->ntx = 0;
+    const double h = a.Lx / a.Mx;
+    if (ts_s > 0 && a.nsrc > 0)
+        FTE_TRY(fte_tiles_build(ctx, wc, a.psrc, a.nsrc, a.Lx, a.Ly, h, ts_s, (a.Mx + ts_s - 1) / ts_s,
+                                (a.My + ts_s - 1) / ts_s, src));
+    if (ts_g > 0 && a.ntar > 0)
+        FTE_TRY(fte_tiles_build(ctx, wc, a.ptar, a.ntar, a.Lx, a.Ly, h, ts_g, (a.Mx + ts_g - 1) / ts_g,
+                                (a.My + ts_g - 1) / ts_g, tar));
+    return FTE_OK;
+}
 
 size_t fte_kspace_ws(int kind, int form, int Mx, int My, int64_t nsrc, int64_t ntar) {
     (void)form;
@@ -1066,12 +1100,21 @@ int fte_kspace_run(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, fte_info
     const int ts_g = pick_tile(2, a.P, tile_budget(ctx));
     TileBins tb_s, tb_g;
     tb_s.ntx = tb_g.ntx = 0;
-    if (ts_s > 0 && a.nsrc > 0)
+    tb_s.ts = tb_g.ts = 0;
+    if (a.pre_src && ts_s > 0 && a.nsrc > 0)
+        tb_s = *a.pre_src;
+    else if (ts_s > 0 && a.nsrc > 0)
         FTE_TRY(fte_tiles_build(ctx, wc, a.psrc, a.nsrc, a.Lx, a.Ly, wp.h, ts_s, (Mx + ts_s - 1) / ts_s,
                                 (My + ts_s - 1) / ts_s, &tb_s));
-    if (ts_g > 0 && a.ntar > 0)
+    if (a.pre_tar && ts_g > 0 && a.ntar > 0)
+        tb_g = *a.pre_tar;
+    else if (ts_g > 0 && a.ntar > 0)
         FTE_TRY(fte_tiles_build(ctx, wc, a.ptar, a.ntar, a.Lx, a.Ly, wp.h, ts_g, (Mx + ts_g - 1) / ts_g,
                                 (My + ts_g - 1) / ts_g, &tb_g));
+    if ((a.nsrc > 0 && tb_s.ts != ts_s) || (a.ntar > 0 && tb_g.ts != ts_g)) {
+        fte_set_error("internal: prebuilt tiles do not match the FP64 tile sizes");
+        return FTE_ERR_INVALID;
+    }
 
     FTE_TRY(fte_record(ctx, 2));
     FTE_CUDA_TRY(cudaMemsetAsync(H, 0, sizeof(double) * ng * G, ctx->stream));

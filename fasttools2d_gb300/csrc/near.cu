@@ -36,16 +36,19 @@ struct NearParams {
     int nsx, nsy, nb;
     const int* __restrict__ src_off;
     const double2* __restrict__ spos;
-    const double* __restrict__ q0;
-    const double* __restrict__ q1;
-    const double* __restrict__ q2;
+    // densities of the sorted sources; vector v at q* + v * qstride
+    const double* __restrict__ q0;  // SLP: f1 ; DLP: S11 = f1 n1
+    const double* __restrict__ q1;  // SLP: f2 ; DLP: S12 + S21
+    const double* __restrict__ q2;  // DLP: S22
+    long long qstride;
     const int* __restrict__ tar_off;
     const double2* __restrict__ tpos;
     const int* __restrict__ tidx;
     double Lx, Ly, xi, xi2, inv_xi2, selfc, cutoffsq, pf;
     float cut32;
     int cap;
-    double2* __restrict__ ur;
+    double2* __restrict__ ur;  // vector v at ur + v * ustride
+    long long ustride;
 };
 
 // E1(x) for x > 0 from the piecewise polynomials of gen_e1_coeffs.py:
@@ -137,230 +140,257 @@ __device__ __forceinline__ double fte_kfun(double x, const double* __restrict__ 
     return k;
 }
 
-template <int KIND>
-__global__ void __launch_bounds__(kNearThreads, 2) k_near(const NearParams prm) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+// Shared-memory layout of the near-field kernels (per CTA):
+//   K(x) table, exp table, then per staged source: x, y (FP64), NV density
+//   sets (SLP: f1, f2; DLP: S11, (S12+S21)/2, S22, S11+S22), FP32 box-relative
+//   position; then two 64-entry rings per warp.
+template <int KIND, int NV>
+struct NearSmem {
+    static constexpr int kDen = KIND == FTE_KIND_SLP ? 2 : 4;
+    __host__ __device__ static size_t bytes(int cap) {
+        return (kKtab + 64) * sizeof(double) + (size_t)cap * ((2 + kDen * NV) * sizeof(double) + sizeof(float2)) +
+               kNearWarps * 2 * kQueue * sizeof(int) + 64;
+    }
+};
+
+// All targets of box b against the 3x3 neighbourhood of sources, for NV
+// density vectors at once: the pair geometry and the special functions are
+// evaluated once per pair and shared by the vectors.
+template <int KIND, int NV>
+__device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned char* smem_raw, int* nb_box,
+                                         int* nb_start, double* nb_shx, double* nb_shy) {
+    constexpr int kDen = NearSmem<KIND, NV>::kDen;
     const int cap = prm.cap;
-    double* ktab = reinterpret_cast<double*>(smem_raw);
-    double* etab = ktab + kKtab;
-    double* sx = etab + 64;
+    const double* ktab = reinterpret_cast<const double*>(smem_raw);
+    const double* etab = ktab + kKtab;
+    double* sx = const_cast<double*>(etab) + 64;
     double* sy = sx + cap;
-    double* a0 = sy + cap;
-    double* a1 = a0 + cap;
-    double* a2 = a1 + cap;  // DLP only
-    double* a3 = a2 + (KIND == FTE_KIND_DLP ? cap : 0);  // DLP only
-    float2* s32 = reinterpret_cast<float2*>(a3 + (KIND == FTE_KIND_DLP ? cap : 0));
+    double* den = sy + cap;  // den[(v * kDen + c) * cap + i]
+    float2* s32 = reinterpret_cast<float2*>(den + (size_t)kDen * NV * cap);
     int* qbuf = reinterpret_cast<int*>(s32 + cap);
-    __shared__ int nb_box[9];
-    __shared__ int nb_start[10];
-    __shared__ double nb_shx[9], nb_shy[9];
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    // per warp: queue 0 = pairs with x >= 1 (all DLP pairs), queue 1 = x < 1 (SLP)
+    // per warp: ring 0 = pairs with x >= 1 (all stresslet pairs), ring 1 = x < 1 (Stokeslet)
     int* qf = qbuf + warp * 2 * kQueue;
     int* qn = qf + kQueue;
     const unsigned lt_mask = (1u << lane) - 1u;
     const double inv4pi = 1.0 / (4.0 * FTE_PI);
     const float xi2f = (float)prm.xi2;
 
-    for (int i = tid; i < kKtab; i += kNearThreads) ktab[i] = (&fte_k_coef[0][0])[i];
-    for (int i = tid; i < 64; i += kNearThreads) etab[i] = fte_exp_tab[i];
-
-    for (int b = blockIdx.x; b < prm.nb; b += gridDim.x) {
-        const int t0 = prm.tar_off[b];
-        const int nt = prm.tar_off[b + 1] - t0;
-        if (nt == 0) continue;
-        const int bx = b % prm.nsx, by = b / prm.nsx;
-        __syncthreads();  // previous box finished with the staging buffers
-        if (tid < 9) {
-            // own box first, then the reference's neighbour order (ilist_x/ilist_y)
-            const int ox_tab[9] = {0, -1, -1, -1, 0, 0, 1, 1, 1};
-            const int oy_tab[9] = {0, -1, 0, 1, -1, 1, -1, 0, 1};
-            int psx = bx + ox_tab[tid], psy = by + oy_tab[tid];
-            int tx = (psx + prm.nsx) % prm.nsx, ty = (psy + prm.nsy) % prm.nsy;
-            int sb = ty * prm.nsx + tx;
-            nb_box[tid] = sb;
-            nb_shx[tid] = (prm.Lx * (psx - tx)) / prm.nsx;
-            nb_shy[tid] = (prm.Ly * (psy - ty)) / prm.nsy;
+    const int t0 = prm.tar_off[b];
+    const int nt = prm.tar_off[b + 1] - t0;
+    if (nt == 0) return;
+    const int bx = b % prm.nsx, by = b / prm.nsx;
+    __syncthreads();  // the previous box is done with the staging buffers
+    if (tid < 9) {
+        // own box first, then the reference's neighbour order (ilist_x/ilist_y)
+        const int ox = tid == 0 ? 0 : (tid <= 3 ? -1 : (tid <= 5 ? 0 : 1));
+        const int oy = tid == 0 ? 0 : ((tid == 1 || tid == 4 || tid == 6) ? -1 : ((tid == 2 || tid == 7) ? 0 : 1));
+        int psx = bx + ox, psy = by + oy;
+        int tx = (psx + prm.nsx) % prm.nsx, ty = (psy + prm.nsy) % prm.nsy;
+        int sb = ty * prm.nsx + tx;
+        nb_box[tid] = sb;
+        nb_shx[tid] = (prm.Lx * (psx - tx)) / prm.nsx;
+        nb_shy[tid] = (prm.Ly * (psy - ty)) / prm.nsy;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        int s = 0;
+        for (int e = 0; e < 9; e++) {
+            nb_start[e] = s;
+            s += prm.src_off[nb_box[e] + 1] - prm.src_off[nb_box[e]];
         }
-        __syncthreads();
-        if (tid == 0) {
-            int s = 0;
-            for (int e = 0; e < 9; e++) {
-                nb_start[e] = s;
-                s += prm.src_off[nb_box[e] + 1] - prm.src_off[nb_box[e]];
-            }
-            nb_start[9] = s;
-        }
-        __syncthreads();
-        const int S = nb_start[9];
-        const int n_own = nb_start[1];
-        const double cx = -prm.Lx / 2 + (bx + 0.5) * prm.Lx / prm.nsx;
-        const double cy = -prm.Ly / 2 + (by + 0.5) * prm.Ly / prm.nsy;
+        nb_start[9] = s;
+    }
+    __syncthreads();
+    const int S = nb_start[9];
+    const int n_own = nb_start[1];
+    const double cx = -prm.Lx / 2 + (bx + 0.5) * prm.Lx / prm.nsx;
+    const double cy = -prm.Ly / 2 + (by + 0.5) * prm.Ly / prm.nsy;
 
-        if (S == 0) {
-            for (int t = tid; t < nt; t += kNearThreads) prm.ur[prm.tidx[t0 + t]] = make_double2(0.0, 0.0);
-            continue;
-        }
+    if (S == 0) {
+        for (int t = tid; t < nt; t += kNearThreads)
+            for (int v = 0; v < NV; v++) prm.ur[v * prm.ustride + prm.tidx[t0 + t]] = make_double2(0.0, 0.0);
+        return;
+    }
 
-        for (int chunk = 0; chunk < S; chunk += cap) {
-            const int clen = min(cap, S - chunk);
-            if (chunk > 0) __syncthreads();
-            for (int i = tid; i < clen; i += kNearThreads) {
-                int g = chunk + i;
-                int e = 0;
+    for (int chunk = 0; chunk < S; chunk += cap) {
+        const int clen = min(cap, S - chunk);
+        if (chunk > 0) __syncthreads();
+        for (int i = tid; i < clen; i += kNearThreads) {
+            int g = chunk + i;
+            int e = 0;
 #pragma unroll
-                for (int k = 1; k < 9; k++) e += (g >= nb_start[k]);
-                int si = prm.src_off[nb_box[e]] + (g - nb_start[e]);
-                double2 p = prm.spos[si];
-                double xs = p.x + nb_shx[e], ys = p.y + nb_shy[e];
-                sx[i] = xs;
-                sy[i] = ys;
+            for (int k = 1; k < 9; k++) e += (g >= nb_start[k]);
+            int si = prm.src_off[nb_box[e]] + (g - nb_start[e]);
+            double2 p = prm.spos[si];
+            double xs = p.x + nb_shx[e], ys = p.y + nb_shy[e];
+            sx[i] = xs;
+            sy[i] = ys;
+#pragma unroll
+            for (int v = 0; v < NV; v++) {
+                const long long o = v * prm.qstride + si;
+                double* d = den + (size_t)v * kDen * cap + i;
                 if (KIND == FTE_KIND_SLP) {
-                    a0[i] = prm.q0[si];
-                    a1[i] = prm.q1[si];
+                    d[0] = prm.q0[o];
+                    d[cap] = prm.q1[o];
                 } else {
                     // S11, (S12 + S21)/2, S22, S11 + S22
-                    double s11 = prm.q0[si], ssym = prm.q1[si], s22 = prm.q2[si];
-                    a0[i] = s11;
-                    a1[i] = 0.5 * ssym;
-                    a2[i] = s22;
-                    a3[i] = s11 + s22;
+                    double s11 = prm.q0[o], ssym = prm.q1[o], s22 = prm.q2[o];
+                    d[0] = s11;
+                    d[cap] = 0.5 * ssym;
+                    d[2 * cap] = s22;
+                    d[3 * cap] = s11 + s22;
                 }
-                s32[i] = make_float2((float)(xs - cx), (float)(ys - cy));
             }
-            __syncthreads();
-            const int own_lim = n_own - chunk;  // local index < own_lim: own box
+            s32[i] = make_float2((float)(xs - cx), (float)(ys - cy));
+        }
+        __syncthreads();
+        const int own_lim = n_own - chunk;  // local index < own_lim: own box
 
-            for (int t = warp; t < nt; t += kNearWarps) {
-                const double2 tp = prm.tpos[t0 + t];
-                const float tx32 = (float)(tp.x - cx), ty32 = (float)(tp.y - cy);
-                double acc0 = 0.0, acc1 = 0.0;
-                int hf = 0, cf = 0, hn = 0, cn = 0;  // ring heads and counts
-
-                // Stokeslet pair (mex_stokes_slp_real.cpp:161-225 / 264-323):
-                //   u += (0.5 E1(x) - e^-x) f + e^-x (r.f) r / r^2,   x = xi^2 r^2
-                auto eval_slp = [&](int s, bool small_x) {
-                    double dx = tp.x - sx[s], dy = tp.y - sy[s];
-                    double r2 = fma(dx, dx, dy * dy);
-                    bool own = s < own_lim;
-                    double fx = a0[s], fy = a1[s];
-                    if (own && fabs(r2) < 1e-15) {
-                        acc0 = fma(prm.selfc, fx, acc0);
-                        acc1 = fma(prm.selfc, fy, acc1);
-                        return;
-                    }
-                    if (!own && !(r2 < prm.cutoffsq)) return;
-                    double x = r2 * prm.xi2;
-                    double emx = fte_expm(x, etab);
-                    double A;
-                    if (small_x) {
-                        double tt = fma(2.0, x, -1.0);
-                        double R = fte_e1_coef_r[FTE_E1_DEG_R];
+        for (int t = warp; t < nt; t += kNearWarps) {
+            const double2 tp = prm.tpos[t0 + t];
+            const float tx32 = (float)(tp.x - cx), ty32 = (float)(tp.y - cy);
+            double acc[NV][2];
 #pragma unroll
-                        for (int k = FTE_E1_DEG_R - 1; k >= 0; k--) R = fma(R, tt, fte_e1_coef_r[k]);
-                        double E = fma(x, R, -FTE_EULER - log(x));
-                        A = fma(0.5, E, -emx);
-                    } else {
-                        A = emx * fte_kfun(x, ktab);
+            for (int v = 0; v < NV; v++) acc[v][0] = acc[v][1] = 0.0;
+            int hf = 0, cf = 0, hn = 0, cn = 0;  // ring heads and counts
+
+            // Stokeslet pair (mex_stokes_slp_real.cpp:161-225 / 264-323):
+            //   u += (0.5 E1(x) - e^-x) f + e^-x (r.f) r / r^2,   x = xi^2 r^2
+            auto eval_slp = [&](int s, bool small_x) {
+                double dx = tp.x - sx[s], dy = tp.y - sy[s];
+                double r2 = fma(dx, dx, dy * dy);
+                bool own = s < own_lim;
+                if (own && fabs(r2) < 1e-15) {
+#pragma unroll
+                    for (int v = 0; v < NV; v++) {
+                        const double* d = den + (size_t)v * 2 * cap + s;
+                        acc[v][0] = fma(prm.selfc, d[0], acc[v][0]);
+                        acc[v][1] = fma(prm.selfc, d[cap], acc[v][1]);
                     }
-                    double ir2 = fte_rcp(r2);
-                    double c = emx * ir2 * fma(dx, fx, dy * fy);
-                    acc0 = fma(A, fx, fma(c, dx, acc0));
-                    acc1 = fma(A, fy, fma(c, dy, acc1));
-                };
-                // stresslet pair (mex_stokes_dlp_real.cpp:117-138 / 162-181):
-                //   u_i += e^-x [ -4 (1+x) r_i (r.S.r)/r^4 + 2 xi^2 (f_i (r.n) + n_i (r.f) + (f.n) r_i) ]
-                auto eval_dlp = [&](int s) {
-                    double dx = tp.x - sx[s], dy = tp.y - sy[s];
-                    double r2 = fma(dx, dx, dy * dy);
-                    bool own = s < own_lim;
-                    if (own ? (r2 == 0.0) : !(r2 < prm.cutoffsq)) return;
-                    double x = r2 * prm.xi2;
-                    double e2 = fte_expm(x, etab);
-                    double ir2 = fte_rcp(r2);
-                    double facb = -4.0 * (1.0 + x) * ir2 * ir2;
-                    double s11 = a0[s], h = a1[s], s22 = a2[s], tr = a3[s];
+                    return;
+                }
+                if (!own && !(r2 < prm.cutoffsq)) return;
+                double x = r2 * prm.xi2;
+                double emx = fte_expm(x, etab);
+                double A;
+                if (small_x) {
+                    double tt = fma(2.0, x, -1.0);
+                    double R = fte_e1_coef_r[FTE_E1_DEG_R];
+#pragma unroll
+                    for (int k = FTE_E1_DEG_R - 1; k >= 0; k--) R = fma(R, tt, fte_e1_coef_r[k]);
+                    double E = fma(x, R, -FTE_EULER - log(x));
+                    A = fma(0.5, E, -emx);
+                } else {
+                    A = emx * fte_kfun(x, ktab);
+                }
+                double gr = emx * fte_rcp(r2);
+#pragma unroll
+                for (int v = 0; v < NV; v++) {
+                    const double* d = den + (size_t)v * 2 * cap + s;
+                    double fx = d[0], fy = d[cap];
+                    double c = gr * fma(dx, fx, dy * fy);
+                    acc[v][0] = fma(A, fx, fma(c, dx, acc[v][0]));
+                    acc[v][1] = fma(A, fy, fma(c, dy, acc[v][1]));
+                }
+            };
+            // stresslet pair (mex_stokes_dlp_real.cpp:117-138 / 162-181):
+            //   u_i += e^-x [ -4 (1+x) r_i (r.S.r)/r^4 + 2 xi^2 (f_i (r.n) + n_i (r.f) + (f.n) r_i) ]
+            auto eval_dlp = [&](int s) {
+                double dx = tp.x - sx[s], dy = tp.y - sy[s];
+                double r2 = fma(dx, dx, dy * dy);
+                bool own = s < own_lim;
+                if (own ? (r2 == 0.0) : !(r2 < prm.cutoffsq)) return;
+                double x = r2 * prm.xi2;
+                double e2 = fte_expm(x, etab);
+                double ir2 = fte_rcp(r2);
+                double facb = -4.0 * (1.0 + x) * ir2 * ir2;
+#pragma unroll
+                for (int v = 0; v < NV; v++) {
+                    const double* d = den + (size_t)v * 4 * cap + s;
+                    double s11 = d[0], h = d[cap], s22 = d[2 * cap], tr = d[3 * cap];
                     double u = fma(dx, s11, dy * h);  // (S r)_1 with S symmetrised
-                    double v = fma(dy, s22, dx * h);  // (S r)_2
-                    double Q = fma(dx, u, dy * v);    // r.S.r
+                    double w = fma(dy, s22, dx * h);  // (S r)_2
+                    double Q = fma(dx, u, dy * w);    // r.S.r
                     double fQ = facb * Q;
                     double w1 = fma(dx, tr, u + u);   // f_1 (r.n) + n_1 (r.f) + (f.n) r_1
-                    double w2 = fma(dy, tr, v + v);
-                    acc0 = fma(e2, fma(fQ, dx, prm.pf * w1), acc0);
-                    acc1 = fma(e2, fma(fQ, dy, prm.pf * w2), acc1);
-                };
+                    double w2 = fma(dy, tr, w + w);
+                    acc[v][0] = fma(e2, fma(fQ, dx, prm.pf * w1), acc[v][0]);
+                    acc[v][1] = fma(e2, fma(fQ, dy, prm.pf * w2), acc[v][1]);
+                }
+            };
 
-                for (int base = 0; base < clen; base += 32) {
-                    int s = base + lane;
-                    bool pass = false, small_x = false;
-                    if (s < clen) {
-                        float2 q = s32[s];
-                        float dx = q.x - tx32, dy = q.y - ty32;
-                        float r2f = dx * dx + dy * dy;
-                        pass = (s < own_lim) || (r2f < prm.cut32);
-                        small_x = r2f * xi2f < 1.0f;
-                    }
-                    if (KIND == FTE_KIND_SLP) {
-                        bool pf_ = pass && !small_x, pn_ = pass && small_x;
-                        unsigned mf = __ballot_sync(0xffffffffu, pf_);
-                        unsigned mn = __ballot_sync(0xffffffffu, pn_);
-                        if (pf_) qf[(hf + cf + __popc(mf & lt_mask)) & (kQueue - 1)] = s;
-                        if (pn_) qn[(hn + cn + __popc(mn & lt_mask)) & (kQueue - 1)] = s;
-                        cf += __popc(mf);
-                        cn += __popc(mn);
-                        __syncwarp();
-                        if (cf >= 32) {
-                            eval_slp(qf[(hf + lane) & (kQueue - 1)], false);
-                            hf = (hf + 32) & (kQueue - 1);
-                            cf -= 32;
-                            __syncwarp();
-                        }
-                        if (cn >= 32) {
-                            eval_slp(qn[(hn + lane) & (kQueue - 1)], true);
-                            hn = (hn + 32) & (kQueue - 1);
-                            cn -= 32;
-                            __syncwarp();
-                        }
-                    } else {
-                        unsigned mf = __ballot_sync(0xffffffffu, pass);
-                        if (pass) qf[(hf + cf + __popc(mf & lt_mask)) & (kQueue - 1)] = s;
-                        cf += __popc(mf);
-                        __syncwarp();
-                        if (cf >= 32) {
-                            eval_dlp(qf[(hf + lane) & (kQueue - 1)]);
-                            hf = (hf + 32) & (kQueue - 1);
-                            cf -= 32;
-                            __syncwarp();
-                        }
-                    }
+            for (int base = 0; base < clen; base += 32) {
+                int s = base + lane;
+                bool pass = false, small_x = false;
+                if (s < clen) {
+                    float2 q = s32[s];
+                    float dx = q.x - tx32, dy = q.y - ty32;
+                    float r2f = dx * dx + dy * dy;
+                    pass = (s < own_lim) || (r2f < prm.cut32);
+                    small_x = r2f * xi2f < 1.0f;
                 }
                 if (KIND == FTE_KIND_SLP) {
-                    // the two partial queues share one pass: lanes [0, cf) take far
-                    // pairs, lanes [cf, cf+cn) near pairs when they fit in a warp
-                    if (cf + cn <= 32) {
-                        if (lane < cf)
-                            eval_slp(qf[(hf + lane) & (kQueue - 1)], false);
-                        else if (lane < cf + cn)
-                            eval_slp(qn[(hn + lane - cf) & (kQueue - 1)], true);
-                    } else {
-                        if (lane < cf) eval_slp(qf[(hf + lane) & (kQueue - 1)], false);
-                        if (lane < cn) eval_slp(qn[(hn + lane) & (kQueue - 1)], true);
+                    bool pf_ = pass && !small_x, pn_ = pass && small_x;
+                    unsigned mf = __ballot_sync(0xffffffffu, pf_);
+                    unsigned mn = __ballot_sync(0xffffffffu, pn_);
+                    if (pf_) qf[(hf + cf + __popc(mf & lt_mask)) & (kQueue - 1)] = s;
+                    if (pn_) qn[(hn + cn + __popc(mn & lt_mask)) & (kQueue - 1)] = s;
+                    cf += __popc(mf);
+                    cn += __popc(mn);
+                    __syncwarp();
+                    if (cf >= 32) {
+                        eval_slp(qf[(hf + lane) & (kQueue - 1)], false);
+                        hf = (hf + 32) & (kQueue - 1);
+                        cf -= 32;
+                        __syncwarp();
+                    }
+                    if (cn >= 32) {
+                        eval_slp(qn[(hn + lane) & (kQueue - 1)], true);
+                        hn = (hn + 32) & (kQueue - 1);
+                        cn -= 32;
+                        __syncwarp();
                     }
                 } else {
-                    if (lane < cf) eval_dlp(qf[(hf + lane) & (kQueue - 1)]);
+                    unsigned mf = __ballot_sync(0xffffffffu, pass);
+                    if (pass) qf[(hf + cf + __popc(mf & lt_mask)) & (kQueue - 1)] = s;
+                    cf += __popc(mf);
+                    __syncwarp();
+                    if (cf >= 32) {
+                        eval_dlp(qf[(hf + lane) & (kQueue - 1)]);
+                        hf = (hf + 32) & (kQueue - 1);
+                        cf -= 32;
+                        __syncwarp();
+                    }
                 }
-                __syncwarp();
-                acc0 = warp_sum(acc0);
-                acc1 = warp_sum(acc1);
+            }
+            if (KIND == FTE_KIND_SLP) {
+                // the two partial rings share one pass when they fit in a warp
+                if (cf + cn <= 32) {
+                    if (lane < cf)
+                        eval_slp(qf[(hf + lane) & (kQueue - 1)], false);
+                    else if (lane < cf + cn)
+                        eval_slp(qn[(hn + lane - cf) & (kQueue - 1)], true);
+                } else {
+                    if (lane < cf) eval_slp(qf[(hf + lane) & (kQueue - 1)], false);
+                    if (lane < cn) eval_slp(qn[(hn + lane) & (kQueue - 1)], true);
+                }
+            } else {
+                if (lane < cf) eval_dlp(qf[(hf + lane) & (kQueue - 1)]);
+            }
+            __syncwarp();
+#pragma unroll
+            for (int v = 0; v < NV; v++) {
+                double a0 = warp_sum(acc[v][0]), a1 = warp_sum(acc[v][1]);
                 if (lane == 0) {
-                    int oi = prm.tidx[t0 + t];
-                    double2 v = make_double2(acc0 * inv4pi, acc1 * inv4pi);
+                    double2* o = prm.ur + v * prm.ustride + prm.tidx[t0 + t];
+                    double2 val = make_double2(a0 * inv4pi, a1 * inv4pi);
                     if (chunk == 0) {
-                        prm.ur[oi] = v;
+                        *o = val;
                     } else {
-                        double2 o = prm.ur[oi];
-                        prm.ur[oi] = make_double2(o.x + v.x, o.y + v.y);
+                        double2 old = *o;
+                        *o = make_double2(old.x + val.x, old.y + val.y);
                     }
                 }
             }
@@ -368,15 +398,55 @@ __global__ void __launch_bounds__(kNearThreads, 2) k_near(const NearParams prm) 
     }
 }
 
-size_t near_smem_bytes(int kind, int cap) {
-    size_t per = (kind == FTE_KIND_DLP ? 6 : 4) * sizeof(double) + sizeof(float2);
-    return (kKtab + 64) * sizeof(double) + (size_t)cap * per + kNearWarps * 2 * kQueue * sizeof(int) + 64;
+template <int KIND, int NV>
+__device__ __forceinline__ void near_load_tables(unsigned char* smem_raw) {
+    double* ktab = reinterpret_cast<double*>(smem_raw);
+    double* etab = ktab + kKtab;
+    for (int i = threadIdx.x; i < kKtab; i += kNearThreads) ktab[i] = (&fte_k_coef[0][0])[i];
+    for (int i = threadIdx.x; i < 64; i += kNearThreads) etab[i] = fte_exp_tab[i];
+}
+
+// one problem: grid-stride over its boxes
+template <int KIND, int NV>
+__global__ void __launch_bounds__(kNearThreads, 2) k_near(const NearParams prm) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int nb_box[9], nb_start[10];
+    __shared__ double nb_shx[9], nb_shy[9];
+    near_load_tables<KIND, NV>(smem_raw);
+    for (int b = blockIdx.x; b < prm.nb; b += gridDim.x)
+        near_box<KIND, NV>(prm, b, smem_raw, nb_box, nb_start, nb_shx, nb_shy);
+}
+
+// many problems: grid-stride over a (problem, box) work list; descriptions
+// are stored in NearParamsHost slots (kParamStride bytes apart)
+constexpr int kParamStride = sizeof(NearParamsHost);
+
+template <int KIND, int NV>
+__global__ void __launch_bounds__(kNearThreads, 2) k_near_batch(const unsigned char* __restrict__ plist,
+                                                                const int2* __restrict__ items, int nitems) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int nb_box[9], nb_start[10];
+    __shared__ double nb_shx[9], nb_shy[9];
+    near_load_tables<KIND, NV>(smem_raw);
+    for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+        const int2 w = items[it];
+        const NearParams prm = *reinterpret_cast<const NearParams*>(plist + (size_t)w.x * kParamStride);
+        near_box<KIND, NV>(prm, w.y, smem_raw, nb_box, nb_start, nb_shx, nb_shy);
+    }
+}
+
+template <int KIND, int NV>
+int near_cap(const fte_context* ctx) {
+    int cap = 2048;
+    const size_t budget = 110 * 1024 < (size_t)ctx->max_smem_optin ? 110 * 1024 : (size_t)ctx->max_smem_optin;
+    while (cap > 128 && NearSmem<KIND, NV>::bytes(cap) > budget) cap -= 64;
+    return cap;
 }
 
 }  // namespace
 
-int fte_near_launch(fte_context* ctx, int kind, const CellList& cl, double xi, double Lx, double Ly, double2* ur) {
-    NearParams p;
+void fte_near_fill_params(int kind, const CellList& cl, double xi, double Lx, double Ly, NearParamsHost* hp) {
+    NearParams& p = *reinterpret_cast<NearParams*>(hp->raw);
     p.nsx = cl.nsx;
     p.nsy = cl.nsy;
     p.nb = cl.nb;
@@ -385,6 +455,7 @@ int fte_near_launch(fte_context* ctx, int kind, const CellList& cl, double xi, d
     p.q0 = cl.q0;
     p.q1 = cl.q1;
     p.q2 = cl.q2;
+    p.qstride = cl.qstride;
     p.tar_off = cl.tar_off;
     p.tpos = cl.tpos;
     p.tidx = cl.tidx;
@@ -399,26 +470,100 @@ int fte_near_launch(fte_context* ctx, int kind, const CellList& cl, double xi, d
     double bsx = Lx / cl.nsx, bsy = Ly / cl.nsy;
     double bmax = bsx > bsy ? bsx : bsy;
     p.cut32 = (float)(p.cutoffsq + 1e-4 * bmax * bmax);
-    p.ur = ur;
-    int cap = kind == FTE_KIND_DLP ? 1792 : 2048;
-    size_t smem = near_smem_bytes(kind, cap);
-    while (smem > (size_t)ctx->max_smem_optin && cap > 256) {
-        cap -= 256;
-        smem = near_smem_bytes(kind, cap);
-    }
-    p.cap = cap;
-    int grid = cl.nb;
-    int maxgrid = ctx->num_sms * 16;
-    if (grid > maxgrid) grid = maxgrid;
+    p.cap = 0;
+    p.ur = nullptr;
+    p.ustride = 0;
+    (void)kind;
+}
+
+size_t fte_near_params_size() { return sizeof(NearParams); }
+
+namespace {
+template <int KIND, int NV>
+int near_launch_one(fte_context* ctx, NearParams p) {
+    p.cap = near_cap<KIND, NV>(ctx);
+    size_t smem = NearSmem<KIND, NV>::bytes(p.cap);
+    int grid = p.nb < ctx->num_sms * 16 ? p.nb : ctx->num_sms * 16;
     if (grid < 1) grid = 1;
-    if (kind == FTE_KIND_SLP) {
-        FTE_CUDA_TRY(cudaFuncSetAttribute(k_near<FTE_KIND_SLP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        FTE_LAUNCH(ctx, k_near<FTE_KIND_SLP>, grid, kNearThreads, smem, p);
-    } else {
-        FTE_CUDA_TRY(cudaFuncSetAttribute(k_near<FTE_KIND_DLP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        FTE_LAUNCH(ctx, k_near<FTE_KIND_DLP>, grid, kNearThreads, smem, p);
-    }
+    FTE_CUDA_TRY(cudaFuncSetAttribute(k_near<KIND, NV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    FTE_LAUNCH(ctx, (k_near<KIND, NV>), grid, kNearThreads, smem, p);
     return FTE_OK;
+}
+
+template <int KIND, int NV>
+int near_launch_batch(fte_context* ctx, const unsigned char* plist_dev, const int2* items, int nitems) {
+    size_t smem = NearSmem<KIND, NV>::bytes(near_cap<KIND, NV>(ctx));
+    int grid = nitems < ctx->num_sms * 16 ? nitems : ctx->num_sms * 16;
+    if (grid < 1) return FTE_OK;
+    FTE_CUDA_TRY(cudaFuncSetAttribute(k_near_batch<KIND, NV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    FTE_LAUNCH(ctx, (k_near_batch<KIND, NV>), grid, kNearThreads, smem, plist_dev, items, nitems);
+    return FTE_OK;
+}
+}  // namespace
+
+int fte_near_cap(const fte_context* ctx, int kind, int nv) {
+    if (kind == FTE_KIND_SLP) {
+        switch (nv) {
+            case 1: return near_cap<FTE_KIND_SLP, 1>(ctx);
+            case 2: return near_cap<FTE_KIND_SLP, 2>(ctx);
+            case 3: return near_cap<FTE_KIND_SLP, 3>(ctx);
+            default: return near_cap<FTE_KIND_SLP, 4>(ctx);
+        }
+    }
+    switch (nv) {
+        case 1: return near_cap<FTE_KIND_DLP, 1>(ctx);
+        case 2: return near_cap<FTE_KIND_DLP, 2>(ctx);
+        case 3: return near_cap<FTE_KIND_DLP, 3>(ctx);
+        default: return near_cap<FTE_KIND_DLP, 4>(ctx);
+    }
+}
+
+int fte_near_launch_nv(fte_context* ctx, int kind, int nv, const NearParamsHost& hp, double2* ur, long long ustride) {
+    NearParams p = *reinterpret_cast<const NearParams*>(hp.raw);
+    p.ur = ur;
+    p.ustride = ustride;
+    if (nv < 1 || nv > 4) {
+        fte_set_error("1 to 4 density vectors per near-field launch (got %d)", nv);
+        return FTE_ERR_INVALID;
+    }
+    if (kind == FTE_KIND_SLP) {
+        switch (nv) {
+            case 1: return near_launch_one<FTE_KIND_SLP, 1>(ctx, p);
+            case 2: return near_launch_one<FTE_KIND_SLP, 2>(ctx, p);
+            case 3: return near_launch_one<FTE_KIND_SLP, 3>(ctx, p);
+            default: return near_launch_one<FTE_KIND_SLP, 4>(ctx, p);
+        }
+    }
+    switch (nv) {
+        case 1: return near_launch_one<FTE_KIND_DLP, 1>(ctx, p);
+        case 2: return near_launch_one<FTE_KIND_DLP, 2>(ctx, p);
+        case 3: return near_launch_one<FTE_KIND_DLP, 3>(ctx, p);
+        default: return near_launch_one<FTE_KIND_DLP, 4>(ctx, p);
+    }
+}
+
+int fte_near_launch_batch(fte_context* ctx, int kind, int nv, const void* plist_dev, const int2* items, int nitems) {
+    const unsigned char* pl = static_cast<const unsigned char*>(plist_dev);
+    if (kind == FTE_KIND_SLP) {
+        switch (nv) {
+            case 1: return near_launch_batch<FTE_KIND_SLP, 1>(ctx, pl, items, nitems);
+            case 2: return near_launch_batch<FTE_KIND_SLP, 2>(ctx, pl, items, nitems);
+            case 3: return near_launch_batch<FTE_KIND_SLP, 3>(ctx, pl, items, nitems);
+            default: return near_launch_batch<FTE_KIND_SLP, 4>(ctx, pl, items, nitems);
+        }
+    }
+    switch (nv) {
+        case 1: return near_launch_batch<FTE_KIND_DLP, 1>(ctx, pl, items, nitems);
+        case 2: return near_launch_batch<FTE_KIND_DLP, 2>(ctx, pl, items, nitems);
+        case 3: return near_launch_batch<FTE_KIND_DLP, 3>(ctx, pl, items, nitems);
+        default: return near_launch_batch<FTE_KIND_DLP, 4>(ctx, pl, items, nitems);
+    }
+}
+
+int fte_near_launch(fte_context* ctx, int kind, const CellList& cl, double xi, double Lx, double Ly, double2* ur) {
+    NearParamsHost hp;
+    fte_near_fill_params(kind, cl, xi, Lx, Ly, &hp);
+    return fte_near_launch_nv(ctx, kind, 1, hp, ur, 0);
 }
 
 // ---- diagnostics: the special functions on the device (test hook) ------------
@@ -476,4 +621,12 @@ extern "C" int fte_debug_special(int which, const double* x_dev, double* out_dev
         return FTE_ERR_CUDA;
     }
     return FTE_OK;
+}
+
+void fte_near_set_output(NearParamsHost* hp, double2* ur, long long ustride, int cap) {
+    static_assert(sizeof(NearParams) <= sizeof(NearParamsHost::raw), "NearParamsHost too small");
+    NearParams& p = *reinterpret_cast<NearParams*>(hp->raw);
+    p.ur = ur;
+    p.ustride = ustride;
+    p.cap = cap;
 }

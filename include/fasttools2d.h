@@ -151,6 +151,48 @@ int fte_stokes_dlp_ewald_2p(fte_context* ctx, const double* xsrc, const double* 
 int fte_choose_params(int kind, int64_t nsrc, int64_t ntar, const double* f1, const double* f2, double Lx,
                       double Ly, const fte_options* opt, fte_params* out);
 
+/* ---- plans: geometry reused across density vectors ------------------------ */
+/* No single counterpart in the reference, which recomputes the cell list
+ * (PeriodicEwald/src/mex/common/ewald_tools.cpp:37-110) and the parameters
+ * (PeriodicEwald/src/matlab/StokesSLP_ewald_2p.m:85-104) on every call.  A
+ * plan does the density-independent work of a driver call once: wrapping,
+ * the parameter choice (from f1, f2, a representative density, and opt; the
+ * mixed form's tuned choice when opt->form == FTE_FORM_MIXED), the cell list,
+ * the k-space tile bins and all scratch.  fte_plan_execute then evaluates
+ * u = SLP[f] (kind FTE_KIND_SLP) or DLP[f] (FTE_KIND_DLP, normals fixed at
+ * creation) for nv <= nvmax density vectors, stored as nv consecutive blocks
+ * of nsrc (f1s, f2s) and ntar (u1s, u2s) values; the real-space pair geometry
+ * and special functions are shared by the nv vectors.  Results equal the
+ * driver entries' with the same parameters. */
+typedef struct fte_plan fte_plan;
+int fte_plan_create(fte_context* ctx, int kind, const double* xsrc, const double* ysrc, int64_t nsrc,
+                    const double* xtar, const double* ytar, int64_t ntar, const double* n1, const double* n2,
+                    const double* f1, const double* f2, double Lx, double Ly, const fte_options* opt, int nvmax,
+                    fte_plan** plan, unsigned flags);
+int fte_plan_params(const fte_plan* plan, fte_params* out);
+int fte_plan_execute(fte_plan* plan, int nv, const double* f1s, const double* f2s, double* u1s, double* u2s,
+                     unsigned flags);
+int fte_plan_destroy(fte_plan* plan);
+
+/* ---- batches: many plans in one graph launch ------------------------------ */
+/* No counterpart in the reference.  A batch binds plans of one context (any
+ * sizes, both kinds) and nv density vectors each to device buffers
+ * (fte_batch_buffers: plan i's f1s, f2s, u1s, u2s, laid out as in
+ * fte_plan_execute).  fte_batch_launch evaluates all of them: one persistent
+ * real-space launch per kind over every plan's cells, the k-space parts on
+ * forked streams; with use_graph = 1 it replays the CUDA graph captured at
+ * creation (one graph launch per step of an iterative solver).  Asynchronous
+ * on the context's stream. */
+typedef struct fte_batch fte_batch;
+int fte_batch_create(fte_context* ctx, fte_plan* const* plans, int nplans, int nv, fte_batch** batch);
+int fte_batch_buffers(const fte_batch* batch, int i, double** f1s, double** f2s, double** u1s, double** u2s);
+int fte_batch_launch(fte_batch* batch, int use_graph);
+int fte_batch_destroy(fte_batch* batch);
+/* copy plan i's nv density vectors in / velocities out (host or, with
+ * FTE_DEVICE_POINTERS, device arrays; host copies synchronise) */
+int fte_batch_set_density(fte_batch* batch, int i, const double* f1s, const double* f2s, unsigned flags);
+int fte_batch_get_velocity(fte_batch* batch, int i, double* u1s, double* u2s, unsigned flags);
+
 /* ---- allocation-free variant --------------------------------------------- */
 /* No counterpart in the reference.  The Stokeslet k-space sum of
  * fte_slp_kspace (same arguments and results) for callers that may not
