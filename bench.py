@@ -46,6 +46,7 @@ def parse_args():
     ap.add_argument("--n", type=int, default=1_000_000, help="sources = targets")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--quick", action="store_true", help="headline only (for profiling runs)")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched 64-configuration section")
     return ap.parse_args()
 
 
@@ -193,6 +194,157 @@ def cpu_baseline(n_full):
 # ---------------------------------------------------------------------------
 # our arm
 # ---------------------------------------------------------------------------
+def batched_section(ft, wl, ctx, stream, steps, warmup, flush):
+    """Batched form on the 64-configuration workload (config 4): every
+    configuration evaluated with the Stokeslet and the stresslet for 4
+    density vectors, at tolerance 1e-8.
+
+    ours:     one plan per (configuration, kernel) with the tuned parameter
+              choice and autotuned spread/gather tiles, all bound into one
+              batch; a step is one replay of its CUDA graph.
+    baseline: the untuned plain per-instance loop -- one FP64 driver call per
+              (configuration, kernel, vector) with the analytic parameters.
+    Both with inputs resident on the GPU; L2 flushed before every step."""
+    import numpy as np
+    import torch
+
+    cfgs = wl.config4()
+    nv, tol = 4, 1e-8
+    kinds = (ft.KIND_SLP, ft.KIND_DLP)
+    dev = []
+    for c in cfgs:
+        d = {k: torch.tensor(c[k], dtype=torch.float64, device="cuda") for k in ("xsrc", "ysrc", "n1", "n2")}
+        d["f1"] = torch.tensor(np.stack([f[0] for f in c["f"][:nv]]), dtype=torch.float64, device="cuda")
+        d["f2"] = torch.tensor(np.stack([f[1] for f in c["f"][:nv]]), dtype=torch.float64, device="cuda")
+        d["Lx"], d["Ly"] = c["Lx"], c["Ly"]
+        dev.append(d)
+    npts = sum(len(c["xsrc"]) for c in cfgs)
+    targets_per_step = npts * nv * len(kinds)
+
+    def events(n):
+        return [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
+
+    # ---- baseline: plain per-instance loop
+    loop_out = [[(torch.empty_like(d["f1"]), torch.empty_like(d["f1"])) for _ in kinds] for d in dev]
+
+    def loop_step():
+        for d, outs in zip(dev, loop_out):
+            for kind, (u1, u2) in zip(kinds, outs):
+                for v in range(nv):
+                    if kind == ft.KIND_SLP:
+                        ft.StokesSLP_ewald_2p(d["xsrc"], d["ysrc"], d["xsrc"], d["ysrc"], d["f1"][v], d["f2"][v],
+                                              d["Lx"], d["Ly"], tol=tol, ctx=ctx, out=(u1[v], u2[v]), parts=False)
+                    else:
+                        ft.StokesDLP_ewald_2p(d["xsrc"], d["ysrc"], d["xsrc"], d["ysrc"], d["n1"], d["n2"],
+                                              d["f1"][v], d["f2"][v], d["Lx"], d["Ly"], tol=tol, ctx=ctx,
+                                              out=(u1[v], u2[v]), parts=False)
+
+    loop_step()
+    lsteps = 1
+    ev = events(lsteps)
+    torch.cuda.synchronize()
+    for i in range(lsteps):
+        flush.fill_(float(i))
+        ev[i][0].record(stream)
+        loop_step()
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    loop_ms = sum(a.elapsed_time(b) for a, b in ev) / lsteps
+
+    # ---- ours: plans + batch + graph
+    t0 = time.perf_counter()
+    plans = []
+    for d in dev:
+        for kind in kinds:
+            plans.append(ft.Plan(kind, d["xsrc"], d["ysrc"], d["xsrc"], d["ysrc"], d["f1"][0], d["f2"][0], d["Lx"],
+                                 d["Ly"], n1=d["n1"], n2=d["n2"], tol=tol, form=ft.FORM_MIXED, nvmax=nv, tune=True,
+                                 ctx=ctx))
+    batch = ft.Batch(plans, nv, ctx=ctx)
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    for i, p in enumerate(plans):
+        d = dev[i // len(kinds)]
+        batch.set_density(i, d["f1"], d["f2"])
+    k0 = ctx.kernel_count
+    batch.launch(False)
+    launches = ctx.kernel_count - k0
+    for _ in range(warmup):
+        batch.launch(True)
+    bsteps = max(3, min(steps, 10))
+    ev = events(bsteps)
+    torch.cuda.synchronize()
+    for i in range(bsteps):
+        flush.fill_(float(i))
+        ev[i][0].record(stream)
+        batch.launch(True)
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    graph_ms = sum(a.elapsed_time(b) for a, b in ev) / bsteps
+
+    # agreement with the FP64 plain loop (both at tolerance 1e-8)
+    worst = 0.0
+    for i, p in enumerate(plans):
+        b1, b2 = batch.velocity(i)
+        u1, u2 = loop_out[i // len(kinds)][i % len(kinds)]
+        ref = np.stack([u1.cpu().numpy(), u2.cpu().numpy()])
+        worst = max(worst, float(np.abs(np.stack([b1, b2]) - ref).max() / np.abs(ref).max()))
+
+    # end to end through the public API: densities from pinned host memory in,
+    # velocities out to pinned host memory, every step
+    hf = [(dev[i // len(kinds)]["f1"].cpu().pin_memory(), dev[i // len(kinds)]["f2"].cpu().pin_memory())
+          for i in range(len(plans))]
+    hu = [torch.empty((nv, p.ntar), dtype=torch.float64).pin_memory() for p in plans]
+    hu2 = [torch.empty((nv, p.ntar), dtype=torch.float64).pin_memory() for p in plans]
+    import ctypes as C
+
+    lib = ft.lib()
+
+    def e2e_step():
+        for i in range(len(plans)):
+            batch.set_density(i, hf[i][0].numpy(), hf[i][1].numpy())
+        batch.launch(True)
+        for i in range(len(plans)):
+            ft._check(lib.fte_batch_get_velocity(batch.h, i, C.c_void_p(hu[i].data_ptr()),
+                                                 C.c_void_p(hu2[i].data_ptr()), 0))
+
+    e2e_step()
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for _ in range(bsteps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_ms = (time.perf_counter() - t1) / bsteps * 1e3
+    h2d = sum(2 * 8 * nv * p.nsrc for p in plans)
+    d2h = sum(2 * 8 * nv * p.ntar for p in plans)
+
+    tiles = {}
+    forms = {}
+    for p in plans:
+        q = p.params
+        key = f"{q.ts_spread}/{q.ts_gather}"
+        tiles[key] = tiles.get(key, 0) + 1
+        forms[q.form] = forms.get(q.form, 0) + 1
+    batch.close()
+    for p in plans:
+        p.close()
+    return {
+        "workload": f"config4: {len(cfgs)} configurations, {npts} points in total (N log-uniform in [2e3, 2e5]), "
+                    f"aspect p/4 in [1, 4], half uniform / half on ellipses, SLP and DLP, {nv} density vectors, "
+                    f"tol {tol:g}",
+        "targets_per_s": targets_per_step / (graph_ms / 1e3), "ms_per_step": graph_ms,
+        "plain_loop": {"targets_per_s": targets_per_step / (loop_ms / 1e3), "ms_per_step": loop_ms,
+                       "calls_per_step": len(cfgs) * len(kinds) * nv},
+        "speedup_vs_plain_loop": loop_ms / graph_ms,
+        "setup_s": setup_s, "gpu_launches_per_step": launches,
+        "max_rel_diff_vs_plain_loop": worst,
+        "tiles_spread_gather": tiles, "kspace_forms": {("fp32" if k == ft.FORM_MIXED else "fp64"): v
+                                                       for k, v in forms.items()},
+        "e2e": {"targets_per_s": targets_per_step / (e2e_ms / 1e3), "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "l2": "flushed before every step",
+    }
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
@@ -216,7 +368,9 @@ def main():
     if not os.path.exists(ft.LIB_PATH):
         ft.build()
     ctx = ft.Context(local_rank)
-    stream = torch.cuda.current_stream()
+    # one non-default stream shared by torch (L2 flush, events) and the library
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
 
     cfg = wl.config3(n=args.n)
@@ -383,6 +537,8 @@ def main():
                      "note": "FP64-ALU-bound kernel; HBM fraction reported as required, see fp64 pipe figures"},
         "clocks": head["clocks"],
     }
+    if not (args.quick or args.no_batch):
+        line["batched"] = batched_section(ft, wl, ctx, stream, args.steps, args.warmup, flush)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(N)
     if rank == 0:

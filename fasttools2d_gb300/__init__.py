@@ -53,7 +53,8 @@ class Params(C.Structure):
     _fields_ = [("P", C.c_int), ("Nb", C.c_double), ("tol", C.c_double), ("Q", C.c_double),
                 ("A", C.c_int), ("B", C.c_int), ("nside_x", C.c_int), ("nside_y", C.c_int),
                 ("rc", C.c_double), ("xi", C.c_double), ("kinf", C.c_int), ("Mx", C.c_int), ("My", C.c_int),
-                ("w", C.c_double), ("eta", C.c_double), ("form", C.c_int)]
+                ("w", C.c_double), ("eta", C.c_double), ("form", C.c_int), ("ts_spread", C.c_int),
+                ("ts_gather", C.c_int)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -62,7 +63,7 @@ class Params(C.Structure):
 class Options(C.Structure):
     _fields_ = [("P", C.c_int), ("Nb", C.c_double), ("tol", C.c_double), ("xi", C.c_double),
                 ("Mx", C.c_int), ("My", C.c_int), ("nside_x", C.c_int), ("nside_y", C.c_int),
-                ("weights", C.c_void_p), ("form", C.c_int)]
+                ("weights", C.c_void_p), ("form", C.c_int), ("tune", C.c_int)]
 
 
 class Info(C.Structure):
@@ -317,7 +318,7 @@ def mex_stokes_dlp_kspace(psrc, ptar, xi, eta, f, n, Mx, My, Lx, Ly, w, P, ctx: 
 # ---- driver-shaped entries -----------------------------------------------------
 
 def _options(P=None, Nb=None, tol=1e-16, xi=None, Mx=None, My=None, nside_x=None, nside_y=None, weights_ptr=None,
-             form=FORM_PLAIN) -> Options:
+             form=FORM_PLAIN, tune=False) -> Options:
     o = Options()
     o.P = int(P or 0)
     o.Nb = float(Nb) if Nb else 0.0
@@ -329,6 +330,7 @@ def _options(P=None, Nb=None, tol=1e-16, xi=None, Mx=None, My=None, nside_x=None
     o.nside_y = int(nside_y or 0)
     o.weights = weights_ptr
     o.form = int(form)
+    o.tune = 1 if tune else 0
     return o
 
 

@@ -75,6 +75,12 @@ extern "C" int fte_destroy(fte_context* c) {
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     for (auto& kv : c->plans) plan_free(kv.second);
+    for (auto& kv : c->lplans) {
+        cudaFree(kv.second->tw);
+        cudaFree(kv.second->chirp);
+        cudaFree(kv.second->bhat);
+        delete kv.second;
+    }
     if (c->ws) cudaFree(c->ws);
     if (c->ws2) cudaFree(c->ws2);
     if (c->host_scalars) cudaFreeHost(c->host_scalars);
@@ -327,6 +333,133 @@ int fte_get_plan(fte_context* c, int n, FftDev* out) {
     return FTE_OK;
 }
 
+// ---- long transforms -----------------------------------------------------------
+// inner length of the block transform of n: n when 7-smooth, else the
+// Bluestein length (smallest 7-smooth m >= 2n - 1)
+static long long block_inner(int n) {
+    std::vector<int> rad;
+    if (smooth7(n, &rad)) return rad.size() <= 24 ? n : -1;
+    long long m = 2LL * n - 1;
+    while (!smooth7((int)m, nullptr)) m++;
+    return m;
+}
+
+bool fte_fft_fits_block(int n, int complex_bytes) {
+    if (n < 1) return false;
+    long long m = block_inner(n);
+    return m > 0 && 2 * m * complex_bytes <= kFftSmemCap;
+}
+
+// L = n1 * n2 with both factors block-transformable in FP64: prefer 7-smooth
+// factors (no in-block Bluestein), then the most balanced split.
+static bool split_factors(int L, bool smooth_only, int* n1, int* n2) {
+    int best = 0;
+    for (int a = 2; (long long)a * a <= L; a++) {
+        if (L % a) continue;
+        int b = L / a;
+        if (smooth_only && !(smooth7(a, nullptr) && smooth7(b, nullptr))) continue;
+        if (!fte_fft_fits_block(a, 16) || !fte_fft_fits_block(b, 16)) continue;
+        best = a;  // increasing a: the last fit is the most balanced
+    }
+    if (!best) return false;
+    // the contiguous second pass transforms n1: give it the larger factor
+    *n1 = L / best;
+    *n2 = best;
+    return true;
+}
+
+bool fte_long_shape(int n, int* mode, int* L, int* n1, int* n2) {
+    if (n < 4) return false;
+    if (split_factors(n, true, n1, n2) || split_factors(n, false, n1, n2)) {
+        *mode = 1;
+        *L = n;
+        return true;
+    }
+    for (long long m = 2LL * n - 1; m < (1LL << 30); m++) {
+        if (!smooth7((int)m, nullptr)) continue;
+        if (split_factors((int)m, true, n1, n2)) {
+            *mode = 2;
+            *L = (int)m;
+            return true;
+        }
+    }
+    return false;
+}
+
+size_t fte_long_scratch(int n, long long nl) {
+    int mode, L, n1, n2;
+    if (!fte_long_shape(n, &mode, &L, &n1, &n2)) return 0;
+    return (size_t)(mode == 1 ? 1 : 2) * (size_t)nl * (size_t)L;
+}
+
+int fte_get_long_plan(fte_context* c, int n, LongFft* out) {
+    auto it = c->lplans.find(n);
+    if (it != c->lplans.end()) {
+        *out = it->second->dev;
+        return FTE_OK;
+    }
+    int mode, L, n1, n2;
+    if (!fte_long_shape(n, &mode, &L, &n1, &n2)) {
+        fte_set_error("FFT length %d: no block factorisation", n);
+        return FTE_ERR_UNSUPPORTED;
+    }
+    LongPlan* p = new LongPlan();
+    p->dev.n = n;
+    p->dev.mode = mode;
+    p->dev.L = L;
+    p->dev.n1 = n1;
+    p->dev.n2 = n2;
+    int st = fte_get_plan(c, n1, &p->dev.d1);
+    if (!st) st = fte_get_plan(c, n2, &p->dev.d2);
+    std::vector<double2> tw(L);
+    for (int t = 0; t < L; t++) {
+        auto z = unit_root(t, L);
+        tw[t] = make_double2(z.real(), z.imag());
+    }
+    if (!st) st = upload(&p->tw, tw);
+    if (!st && mode == 2) {
+        std::vector<double2> ch(n);
+        std::vector<std::complex<double>> b(L, 0.0);
+        for (int k = 0; k < n; k++) {
+            long long k2 = ((long long)k * k) % (2LL * n);
+            auto z = unit_root(k2, 2LL * n);  // exp(-i pi k^2 / n)
+            ch[k] = make_double2(z.real(), z.imag());
+            b[k] = std::conj(z);
+            if (k > 0) b[L - k] = std::conj(z);
+        }
+        host_dft(b);
+        std::vector<double2> bh(L);
+        for (int k = 0; k < L; k++) {
+            auto z = b[k] / (double)L;
+            bh[k] = make_double2(z.real(), z.imag());
+        }
+        st = upload(&p->chirp, ch);
+        if (!st) st = upload(&p->bhat, bh);
+    }
+    if (st) {
+        cudaFree(p->tw);
+        cudaFree(p->chirp);
+        cudaFree(p->bhat);
+        delete p;
+        return st;
+    }
+    p->dev.tw = p->tw;
+    p->dev.chirp = p->chirp;
+    p->dev.bhat = p->bhat;
+    c->lplans[n] = p;
+    *out = p->dev;
+    return FTE_OK;
+}
+
+int fte_fft_prepare(fte_context* c, int n) {
+    if (fte_fft_fits_block(n, 16)) {
+        FftDev d;
+        return fte_get_plan(c, n, &d);
+    }
+    LongFft f;
+    return fte_get_long_plan(c, n, &f);
+}
+
 // ---------------------------------------------------------------------------
 // parameter selection: the MATLAB drivers' analytic choice
 // (StokesSLP_ewald_2p.m:27-35,85-104 and find_kinfb :147-173, find_xi :178-202;
@@ -522,6 +655,35 @@ int next_smooth_even(int n) {
     return n;
 }
 
+// transform work of a length-n line relative to a 7-smooth line of n points:
+// Bluestein runs two transforms of a smooth length m >= 2n - 1 (about 2.2 n)
+double fft_weight(int n) { return smooth7(n, nullptr) ? (double)n : 5.5 * (double)n; }
+
+// Grid resolving kinf modes along Lx with square cells (hx = hy):
+// Mx = A t, My = B t (Lx / Ly = A / B), t >= 2 kinf / A, both even; among
+// the t in a short range the one with the least transform work.  (The
+// drivers use Mx = A * 2 kinf, which over-resolves by A along each side.)
+void pick_grid(int A, int B, int kinf, int* Mx, int* My) {
+    int t0 = (int)std::ceil(2.0 * kinf / A);
+    if (t0 < 2) t0 = 2;
+    double best = 1e300;
+    int bt = t0;
+    int span = t0 / 8 > 16 ? t0 / 8 : 16;
+    if (span > 128) span = 128;
+    for (int t = t0; t <= t0 + span; t++) {
+        int mx = A * t, my = B * t;
+        if (mx % 2 || my % 2) continue;
+        double w = fft_weight(mx) * my * std::log2((double)mx) + fft_weight(my) * mx * std::log2((double)my);
+        if (w < best) {
+            best = w;
+            bt = t;
+        }
+    }
+    if (A * bt % 2 || B * bt % 2) bt += 1;
+    *Mx = A * bt;
+    *My = B * bt;
+}
+
 }  // namespace
 
 // unit costs (seconds) measured on GB300 for the cost model
@@ -551,31 +713,36 @@ static int choose_params_tuned(int kind, int64_t nsrc, int64_t ntar, double Q, d
     const double area = Lx * Ly;
     const int ng = kind == FTE_KIND_SLP ? 2 : 4;
     const double nfft = kind == FTE_KIND_SLP ? 2.0 : 3.0;
-    const int mcap = fp32 ? 6144 : 3072;  // shared-memory transform limit (smooth sizes)
     double best = 1e300;
     fte_params bestp = *o;
-    for (int step = 0; step <= 40; step++) {
+    int best_form = FTE_FORM_PLAIN;
+    int last_a = -1;
+    for (int step = -12; step <= 40; step++) {
         int a = (int)std::lround(a0 * std::pow(1.1, step));
-        if (step > 0 && a == (int)std::lround(a0 * std::pow(1.1, step - 1))) continue;
         if (opt && opt->nside_x > 0) a = opt->nside_x / A;
+        if (a < 1 || a == last_a) continue;
+        last_a = a;
         int nsx = a * A, nsy = a * B;
         double rc = Lx / nsx;
         double xi = (opt && opt->xi > 0) ? opt->xi : xi_estimate(kind, Q, Lx, Ly, rc, tol_e);
         int kinf = kinf_estimate(kind, Q, Lx, xi, tol_e);
-        int M = next_smooth_even(2 * kinf);
-        int Mx = (opt && opt->Mx > 0) ? opt->Mx : next_smooth_even(A * M);
-        int My = (opt && opt->My > 0) ? opt->My : next_smooth_even(B * M);
-        if (Mx > mcap || My > mcap) break;
-        // keep hx = hy: the grid follows the box aspect exactly when A, B are used
-        if (std::fabs(Lx / Mx - Ly / My) > 1e-12 * (Lx / Mx)) {
-            My = (int)std::lround((double)Mx * Ly / Lx);
-            if (My % 2 || std::fabs(Lx / Mx - Ly / My) > 1e-12 * (Lx / Mx)) continue;
-        }
+        int Mx, My;
+        pick_grid(A, B, kinf, &Mx, &My);
+        if (opt && opt->Mx > 0) Mx = opt->Mx;
+        if (opt && opt->My > 0) My = opt->My;
+        if (std::fabs(Lx / Mx - Ly / My) > 1e-12 * (Lx / Mx)) continue;
+        if ((double)Mx * My > 4.0e8) continue;  // 4 grids of 4e8 nodes: 13 GB
+        if (P + 1 > Mx || P + 1 > My) continue;
+        // FP32 k-space where the tolerance allows it and lines fit a block
+        // transform; FP64 lines longer than a block take the long transform
+        const bool f32 = fp32 && fte_fft_fits_block(Mx, 8) && fte_fft_fits_block(My, 8);
+        const bool long64 = !f32 && (!fte_fft_fits_block(Mx, 16) || !fte_fft_fits_block(My, 16));
         double pairs = (double)nsrc * (double)ntar * FTE_PI * rc * rc / area * 1.03;
         double win = (double)(P + 1) * (P + 1) * ((double)nsrc * ng + (double)ntar * 2);
         double pts = (double)Mx * My;
-        double cost = kCostPair * pairs + (fp32 ? kCostWin32 : kCostWin64) * win +
-                      (fp32 ? kCostFft32 : kCostFft64) * nfft * pts * std::log2(pts);
+        double fftw = (fft_weight(Mx) * My + fft_weight(My) * Mx) / 2 * std::log2(pts);
+        double cost = kCostPair * pairs + (f32 ? kCostWin32 : kCostWin64) * win +
+                      (f32 ? kCostFft32 : kCostFft64) * (long64 ? 2.5 : 1.0) * nfft * fftw;
         if (cost < best) {
             best = cost;
             bestp = *o;
@@ -590,11 +757,16 @@ static int choose_params_tuned(int kind, int64_t nsrc, int64_t ntar, double Q, d
             double m = 0.95 * std::sqrt(FTE_PI * P);
             bestp.w = P * Lx / Mx / 2;
             bestp.eta = (2 * xi * bestp.w / m) * (2 * xi * bestp.w / m);
+            best_form = f32 ? FTE_FORM_MIXED : FTE_FORM_PLAIN;
         }
         if (opt && opt->nside_x > 0) break;
     }
+    if (best >= 1e300) {
+        fte_set_error("no tuned parameters within the grid limits (%d x %d boxes)", o->nside_x, o->nside_y);
+        return FTE_ERR_UNSUPPORTED;
+    }
     *o = bestp;
-    o->form = fp32 ? FTE_FORM_MIXED : FTE_FORM_PLAIN;
+    o->form = best_form;
     return FTE_OK;
 }
 

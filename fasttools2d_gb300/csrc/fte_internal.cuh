@@ -75,6 +75,35 @@ struct FftDev {
     const float2* bhat32;
 };
 
+// Long 1-D transforms: lines whose block transform does not fit one block's
+// shared memory.  Four-step (Bailey 1990) over L = n1 * n2 with block
+// transforms of n1 and n2 -- on L = n directly (mode 1), or (mode 2), when n
+// has no such factorisation, as Bluestein's chirp-z convolution in global
+// memory over a factorable 7-smooth L >= 2n - 1.
+struct LongFft {
+    int n = 0;
+    int mode = 0;  // 1: four-step on n; 2: Bluestein over L
+    int L = 0, n1 = 0, n2 = 0;
+    FftDev d1, d2;                   // block plans of n1 and n2
+    const double2* tw = nullptr;     // W_L^t, t < L
+    const double2* chirp = nullptr;  // mode 2: exp(-i pi k^2 / n), k < n
+    const double2* bhat = nullptr;   // mode 2: DFT_L of the conjugate chirp, / L
+};
+struct LongPlan {
+    LongFft dev;
+    double2* tw = nullptr;
+    double2* chirp = nullptr;
+    double2* bhat = nullptr;
+};
+// Lines of a batch: element j of line l sits at
+//   (l / lpg) * gs + (l % lpg) * ls + j * es   (complex elements)
+struct LineMap {
+    long long gs, ls, es;
+    int lpg;
+};
+// opt-in shared memory per block on sm_100 / sm_103 (227 KB)
+constexpr int kFftSmemCap = 232448;
+
 struct fte_context {
     int device = 0;
     cudaStream_t own_stream = nullptr;
@@ -89,6 +118,7 @@ struct fte_context {
     // small pinned host buffer for scalar read-backs
     double* host_scalars = nullptr;
     std::map<int, FftPlan*> plans;
+    std::map<int, LongPlan*> lplans;
     cudaEvent_t ev[8] = {nullptr};
     int max_smem_optin = 0;
     int num_sms = 0;
@@ -121,6 +151,19 @@ struct WsCarver {
 inline size_t ws_bytes(size_t count, size_t elem) { return (count * elem + 255) & ~size_t(255); }
 
 int fte_ws_reserve(fte_context* ctx, size_t bytes);
+
+// FFT lengths: does one block transform a line of n complex values of
+// `complex_bytes` each (two buffers of the inner length in shared memory)?
+bool fte_fft_fits_block(int n, int complex_bytes);
+// shape of the long transform of length n (FP64); false when none exists
+bool fte_long_shape(int n, int* mode, int* L, int* n1, int* n2);
+int fte_get_long_plan(fte_context* c, int n, LongFft* out);
+// scratch (complex elements) of fte_long_fft for nl lines of length n
+size_t fte_long_scratch(int n, long long nl);
+// in-place FP64 transform of nl lines (unnormalised; inv: exp(+i...))
+int fte_long_fft(fte_context* c, const LongFft& f, double2* X, LineMap mx, long long nl, bool inv, double2* scratch);
+// block plan or long plan of length n, whichever the FP64 kernels will use
+int fte_fft_prepare(fte_context* c, int n);
 int fte_ws2_reserve(fte_context* ctx, size_t bytes);
 int fte_get_plan(fte_context* ctx, int n, FftDev* out);
 int fte_record(fte_context* ctx, int slot);
@@ -233,8 +276,15 @@ struct KspaceArgs {
     // tile bins built beforehand (plans); null: built by the call
     const TileBins* pre_src = nullptr;
     const TileBins* pre_tar = nullptr;
+    // spread / gather tile sizes (grid nodes a side); 0: the default rule
+    int ts_spread = 0, ts_gather = 0;
 };
 size_t fte_kspace_ws(int kind, int form, int Mx, int My, int64_t nsrc, int64_t ntar);
 // build the spread/gather tile bins that fte_kspace_run would build for `a`
 int fte_kspace_tiles(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, TileBins* src, TileBins* tar);
 int fte_kspace_run(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, fte_info* info);
+// time every fitting spread and gather tile size on a's points; sets
+// a.ts_spread / a.ts_gather to the fastest (grid: ng grids of scratch; bins:
+// scratch for one candidate's tile bins, fte_tiles_ws(max(nsrc, ntar), tiles
+// of 8 nodes))
+int fte_kspace_tune(fte_context* ctx, void* grid, WsCarver bins, KspaceArgs& a, float* ms_spread, float* ms_gather);

@@ -609,18 +609,199 @@ int fft_threads(int m) {
 
 }  // namespace
 
+// ===========================================================================
+// Long FP64 transforms (grids whose lines do not fit one block's shared
+// memory: the drivers' analytic grids reach A * 10000 nodes along x).
+//
+// Four-step (Bailey 1990) over L = n1 n2, x_j = x[j1 + n1 j2]:
+//   pass 1, per (line, j1):  v[k2] = W_L^{j1 k2} * DFT_{n2}(x[j1 + n1 j2])[k2]
+//                            stored at Y[line][j1 + n1 k2]
+//   pass 2, per (line, k2):  X[k2 + n2 k1] = DFT_{n1}(Y[line][j1 + n1 k2])[k1]
+// The inverse uses the conjugate roots throughout.  Lengths without a
+// block-sized factorisation run Bluestein's convolution in global memory
+// over a factorable L >= 2n - 1 (chirp, forward four-step, multiply by the
+// transformed conjugate chirp, inverse four-step, chirp).
+// ===========================================================================
 namespace {
-// largest tile (multiple of 4 nodes, <= 64) whose region and per-thread
-// weight buffers fit the shared-memory budget; 0 when none does
-int pick_tile(int ng, int P, size_t budget) {
-    const int P1 = P + 1;
-    size_t per = (size_t)(((P1 + 1) & ~1) + kTileThreads * P1) * sizeof(double);
-    for (int ts = 64; ts >= 8; ts -= 4) {
-        size_t W = tile_region(ts, P);
-        if ((size_t)ng * W * W * sizeof(double) + per <= budget) return ts;
-    }
-    return 0;
+__device__ __forceinline__ size_t lm_off(const LineMap& m, long long l) {
+    return (size_t)(l / m.lpg) * m.gs + (size_t)(l % m.lpg) * m.ls;
 }
+
+__global__ void k_lf_pass1(const double2* __restrict__ X, LineMap mx, int L, int n1, int n2, FftDev d2,
+                           const double2* __restrict__ tw, double2* __restrict__ Y, int inv) {
+    extern __shared__ double2 shc[];
+    double2* A = shc;
+    double2* B = shc + d2.m;
+    const long long line = blockIdx.x;
+    const int j1 = blockIdx.y;
+    const double2* x = X + lm_off(mx, line);
+    for (int j2 = threadIdx.x; j2 < n2; j2 += blockDim.x) A[j2] = x[(size_t)(j1 + (long long)n1 * j2) * mx.es];
+    double2* R = fft_block<double>(A, B, d2, inv != 0);
+    double2* y = Y + (size_t)line * L;
+    for (int k2 = threadIdx.x; k2 < n2; k2 += blockDim.x) {
+        double2 w = __ldg(tw + (long long)j1 * k2 % L);
+        if (inv) w.y = -w.y;
+        y[j1 + (size_t)n1 * k2] = cmul(R[k2], w);
+    }
+}
+
+__global__ void k_lf_pass2(const double2* __restrict__ Y, int L, int n1, int n2, FftDev d1, double2* __restrict__ X,
+                           LineMap mx, int inv) {
+    extern __shared__ double2 shc[];
+    double2* A = shc;
+    double2* B = shc + d1.m;
+    const long long line = blockIdx.x;
+    const int k2 = blockIdx.y;
+    const double2* y = Y + (size_t)line * L + (size_t)n1 * k2;
+    for (int j1 = threadIdx.x; j1 < n1; j1 += blockDim.x) A[j1] = y[j1];
+    double2* R = fft_block<double>(A, B, d1, inv != 0);
+    double2* x = X + lm_off(mx, line);
+    for (int k1 = threadIdx.x; k1 < n1; k1 += blockDim.x) x[(size_t)(k2 + (long long)n2 * k1) * mx.es] = R[k1];
+}
+
+__global__ void k_lb_pre(const double2* __restrict__ X, LineMap mx, int n, int L, const double2* __restrict__ chirp,
+                         double2* __restrict__ Z, long long nl, int inv) {
+    const long long total = nl * L;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long l = i / L;
+        const int k = (int)(i - l * L);
+        double2 v = make_double2(0.0, 0.0);
+        if (k < n) {
+            double2 x = X[lm_off(mx, l) + (size_t)k * mx.es];
+            if (inv) x.y = -x.y;
+            v = cmul(x, __ldg(chirp + k));
+        }
+        Z[i] = v;
+    }
+}
+
+__global__ void k_lb_mul(double2* __restrict__ Z, const double2* __restrict__ bhat, int L, long long total) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x)
+        Z[i] = cmul(Z[i], __ldg(bhat + i % L));
+}
+
+__global__ void k_lb_post(const double2* __restrict__ Z, int n, int L, const double2* __restrict__ chirp,
+                          double2* __restrict__ X, LineMap mx, long long nl, int inv) {
+    const long long total = nl * n;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long l = i / n;
+        const int k = (int)(i - l * n);
+        double2 y = cmul(Z[(size_t)l * L + k], __ldg(chirp + k));
+        if (inv) y.y = -y.y;
+        X[lm_off(mx, l) + (size_t)k * mx.es] = y;
+    }
+}
+
+// y direction through a staging buffer S of complex lines (two real rows each)
+__global__ void k_ly_pack_r2c(const double* __restrict__ H, double2* __restrict__ S, int Mx, int My, int ng) {
+    const long long total = (long long)ng * (Mx / 2) * My;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long line = i / My;
+        const int y = (int)(i - line * My);
+        const long long g = line / (Mx / 2), c = line - g * (Mx / 2);
+        const double* h0 = H + ((size_t)g * Mx + 2 * c) * My;
+        S[i] = make_double2(h0[y], h0[My + y]);
+    }
+}
+
+__global__ void k_ly_unpack_r2c(const double2* __restrict__ S, double2* __restrict__ Hh, int Mx, int My, int ng) {
+    const int Kh = My / 2 + 1;
+    const long long total = (long long)ng * (Mx / 2) * Kh;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long line = i / Kh;
+        const int k = (int)(i - line * Kh);
+        const long long g = line / (Mx / 2), c = line - g * (Mx / 2);
+        const double2* R = S + (size_t)line * My;
+        double2 zk = R[k], zm = R[(My - k) % My];
+        double2* o0 = Hh + ((size_t)g * Mx + 2 * c) * Kh;
+        o0[k] = make_double2(0.5 * (zk.x + zm.x), 0.5 * (zk.y - zm.y));
+        o0[Kh + k] = make_double2(0.5 * (zk.y + zm.y), -0.5 * (zk.x - zm.x));
+    }
+}
+
+__global__ void k_ly_pack_c2r(const double2* __restrict__ Hh, double2* __restrict__ S, int Mx, int My, int ng) {
+    const int Kh = My / 2 + 1;
+    const long long total = (long long)ng * (Mx / 2) * Kh;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long line = i / Kh;
+        const int k = (int)(i - line * Kh);
+        const long long g = line / (Mx / 2), c = line - g * (Mx / 2);
+        const double2* i0 = Hh + ((size_t)g * Mx + 2 * c) * Kh;
+        double2 a = i0[k], b = i0[Kh + k];
+        if (k == 0 || 2 * k == My) {
+            a.y = 0.0;
+            b.y = 0.0;
+        }
+        double2* A = S + (size_t)line * My;
+        A[k] = make_double2(a.x - b.y, a.y + b.x);
+        if (k > 0 && 2 * k < My) A[My - k] = make_double2(a.x + b.y, -a.y + b.x);
+    }
+}
+
+__global__ void k_ly_unpack_c2r(const double2* __restrict__ S, double* __restrict__ H, int Mx, int My, int ng) {
+    const long long total = (long long)ng * (Mx / 2) * My;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long line = i / My;
+        const int y = (int)(i - line * My);
+        const long long g = line / (Mx / 2), c = line - g * (Mx / 2);
+        double* o0 = H + ((size_t)g * Mx + 2 * c) * My;
+        double2 z = S[i];
+        o0[y] = z.x;
+        o0[My + y] = z.y;
+    }
+}
+
+int ew_grid(const fte_context* c, long long total) {
+    long long b = (total + 255) / 256;
+    if (b < 1) b = 1;
+    if (b > c->num_sms * 16) b = c->num_sms * 16;
+    return (int)b;
+}
+}  // namespace
+
+int fte_long_fft(fte_context* c, const LongFft& f, double2* X, LineMap mx, long long nl, bool inv, double2* scratch) {
+    if (nl <= 0) return FTE_OK;
+    if (nl > 0x7fffffffLL || f.n1 > 65535 || f.n2 > 65535) {
+        fte_set_error("long FFT: %lld lines of %d beyond the launch limits", nl, f.n);
+        return FTE_ERR_UNSUPPORTED;
+    }
+    const size_t sm1 = 2 * (size_t)f.d2.m * sizeof(double2), sm2 = 2 * (size_t)f.d1.m * sizeof(double2);
+    if (sm1 > (size_t)c->max_smem_optin || sm2 > (size_t)c->max_smem_optin) {
+        fte_set_error("long FFT: block transforms of %d / %d exceed shared memory", f.n2, f.n1);
+        return FTE_ERR_UNSUPPORTED;
+    }
+    FTE_CUDA_TRY(cudaFuncSetAttribute(k_lf_pass1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1));
+    FTE_CUDA_TRY(cudaFuncSetAttribute(k_lf_pass2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2));
+    const LineMap flat{(long long)f.L, 0, 1, 1};
+    auto four_step = [&](double2* data, LineMap m, double2* Y, bool iv) -> int {
+        FTE_LAUNCH(c, k_lf_pass1, dim3((unsigned)nl, f.n1), fft_threads(f.d2.m), sm1, (const double2*)data, m, f.L,
+                   f.n1, f.n2, f.d2, f.tw, Y, iv ? 1 : 0);
+        FTE_LAUNCH(c, k_lf_pass2, dim3((unsigned)nl, f.n2), fft_threads(f.d1.m), sm2, (const double2*)Y, f.L, f.n1,
+                   f.n2, f.d1, data, m, iv ? 1 : 0);
+        return FTE_OK;
+    };
+    if (f.mode == 1) return four_step(X, mx, scratch, inv);
+    // Bluestein over L: Z = chirp * x (zero padded), Z <- IDFT(DFT(Z) * bhat), x = chirp * Z
+    double2* Z = scratch;
+    double2* Y = scratch + (size_t)nl * f.L;
+    const long long total = nl * (long long)f.L;
+    FTE_LAUNCH(c, k_lb_pre, ew_grid(c, total), 256, 0, (const double2*)X, mx, f.n, f.L, f.chirp, Z, nl, inv ? 1 : 0);
+    FTE_TRY(four_step(Z, flat, Y, false));
+    FTE_LAUNCH(c, k_lb_mul, ew_grid(c, total), 256, 0, Z, f.bhat, f.L, total);
+    FTE_TRY(four_step(Z, flat, Y, true));
+    FTE_LAUNCH(c, k_lb_post, ew_grid(c, nl * (long long)f.n), 256, 0, (const double2*)Z, f.n, f.L, f.chirp, X, mx, nl,
+               inv ? 1 : 0);
+    return FTE_OK;
+}
+
+namespace {
 size_t tile_budget(const fte_context* ctx) {
     size_t b = 110 * 1024;  // two CTAs per SM
     return b < (size_t)ctx->max_smem_optin ? b : (size_t)ctx->max_smem_optin;
@@ -929,6 +1110,124 @@ __global__ void k_filter32(float2* __restrict__ Hh, int Mx, int My, double Lx, d
     }
 }
 
+// ---- tile sizes -------------------------------------------------------------
+// Spread and gather tiles are ts x ts grid nodes (ts >= 8); a tile's shared-
+// memory region (ts + P + 4 nodes a side) must fit the two-CTAs-per-SM budget.
+// The default is the largest fitting multiple of 4 up to 64; a plan may carry
+// a tuned size instead (fte_kspace_tune).
+size_t gather64_smem(int ts, int P) {
+    const int P1 = P + 1, W = tile_region(ts, P);
+    return 2 * (size_t)W * W * sizeof(double) + (size_t)(((P1 + 1) & ~1) + kPtThreads * P1) * sizeof(double);
+}
+bool spread_fits(const fte_context* ctx, int form, int ts, int P) {
+    if (ts < 8 || ts > 256) return false;
+    size_t sm = form == FTE_FORM_MIXED ? spread_cols32_smem(ts, P) : spread_cols_smem(ts, P);
+    return sm <= tile_budget(ctx);
+}
+bool gather_fits(const fte_context* ctx, int form, int ts, int P) {
+    if (ts < 8 || ts > 256) return false;
+    size_t sm = form == FTE_FORM_MIXED ? gather32_smem(ts, P) : gather64_smem(ts, P);
+    return sm <= tile_budget(ctx);
+}
+int resolve_tiles(const fte_context* ctx, const KspaceArgs& a, int* ts_s, int* ts_g) {
+    *ts_s = 0;
+    *ts_g = 0;
+    if (a.ts_spread > 0) {
+        if (!spread_fits(ctx, a.form, a.ts_spread, a.P)) {
+            fte_set_error("spread tile %d does not fit shared memory at P=%d", a.ts_spread, a.P);
+            return FTE_ERR_INVALID;
+        }
+        *ts_s = a.ts_spread;
+    } else {
+        for (int ts = 64; ts >= 8 && !*ts_s; ts -= 4)
+            if (spread_fits(ctx, a.form, ts, a.P)) *ts_s = ts;
+    }
+    if (a.ts_gather > 0) {
+        if (!gather_fits(ctx, a.form, a.ts_gather, a.P)) {
+            fte_set_error("gather tile %d does not fit shared memory at P=%d", a.ts_gather, a.P);
+            return FTE_ERR_INVALID;
+        }
+        *ts_g = a.ts_gather;
+    } else {
+        for (int ts = 64; ts >= 8 && !*ts_g; ts -= 4)
+            if (gather_fits(ctx, a.form, ts, a.P)) *ts_g = ts;
+    }
+    return FTE_OK;
+}
+
+WinParams win_params(const KspaceArgs& a) {
+    WinParams wp;
+    wp.Lx = a.Lx;
+    wp.Ly = a.Ly;
+    wp.h = a.Lx / a.Mx;
+    wp.xi = a.xi;
+    wp.eta = a.eta;
+    wp.w = a.w;
+    wp.P = a.P;
+    wp.Mx = a.Mx;
+    wp.My = a.My;
+    return wp;
+}
+
+// tiled spread of all source grids (H holds ng grids of G nodes, FP64 or FP32)
+int launch_spread_tiled(fte_context* ctx, const KspaceArgs& a, const TileBins& tb, const WinParams& wp, void* H) {
+    const int ng = a.kind == FTE_KIND_SLP ? 2 : 4;
+    const size_t G = (size_t)a.Mx * a.My;
+    const bool f32 = a.form == FTE_FORM_MIXED;
+    const size_t sm = f32 ? spread_cols32_smem(tb.ts, a.P) : spread_cols_smem(tb.ts, a.P);
+    const int nt = tb.ntx * tb.nty;
+    const int grid = nt < ctx->num_sms * 8 ? nt : ctx->num_sms * 8;
+    if (f32) {
+        float* Hf = static_cast<float*>(H);
+        FTE_CUDA_TRY(cudaFuncSetAttribute(k_spread_cols32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        for (int pass = 0; pass < ng / 2; pass++) {
+            int mode = ng == 2 ? 0 : 1 + pass;
+            FTE_LAUNCH(ctx, k_spread_cols32, grid, kColThreads, sm, mode, a.psrc, a.f, a.nrm, a.wts,
+                       (const int*)tb.off, (const int*)tb.perm, tb.ts, tb.ntx, tb.nty, wp, Hf + 2 * pass * G,
+                       Hf + (2 * pass + 1) * G);
+        }
+    } else {
+        double* Hd = static_cast<double*>(H);
+        FTE_CUDA_TRY(cudaFuncSetAttribute(k_spread_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        for (int pass = 0; pass < ng / 2; pass++) {
+            int mode = ng == 2 ? 0 : 1 + pass;
+            FTE_LAUNCH(ctx, k_spread_cols, grid, kColThreads, sm, mode, a.psrc, a.f, a.nrm, a.wts,
+                       (const int*)tb.off, (const int*)tb.perm, tb.ts, tb.ntx, tb.nty, wp, Hd + 2 * pass * G,
+                       Hd + (2 * pass + 1) * G);
+        }
+    }
+    return FTE_OK;
+}
+
+// tiled gather of the two velocity grids at the targets
+int launch_gather_tiled(fte_context* ctx, const KspaceArgs& a, const TileBins& tb, const WinParams& wp,
+                        const void* H, double scale) {
+    const size_t G = (size_t)a.Mx * a.My;
+    const int nt = tb.ntx * tb.nty;
+    const int grid = nt < ctx->num_sms * 8 ? nt : ctx->num_sms * 8;
+    if (a.form == FTE_FORM_MIXED) {
+        const float* Hf = static_cast<const float*>(H);
+        size_t sm = gather32_smem(tb.ts, a.P);
+        FTE_CUDA_TRY(cudaFuncSetAttribute(k_gather_tiled32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        FTE_LAUNCH(ctx, k_gather_tiled32, grid, kTileThreads, sm, a.ptar, (const int*)tb.off, (const int*)tb.perm,
+                   tb.ts, tb.ntx, tb.nty, wp, Hf, Hf + G, scale, a.uk);
+    } else {
+        const double* Hd = static_cast<const double*>(H);
+        size_t sm = gather64_smem(tb.ts, a.P);
+        FTE_CUDA_TRY(cudaFuncSetAttribute(k_gather_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        FTE_LAUNCH(ctx, k_gather_tiled, grid, kTileThreads, sm, a.ptar, (const int*)tb.off, (const int*)tb.perm,
+                   tb.ts, tb.ntx, tb.nty, wp, Hd, Hd + G, scale, a.uk);
+    }
+    return FTE_OK;
+}
+
+double gather_scale(const KspaceArgs& a) {
+    const double h = a.Lx / a.Mx;
+    double s = 4 * a.xi * a.xi / a.eta;
+    s = s * s * h * h / FTE_PI;
+    return s / (4 * FTE_PI) / ((double)a.Mx * (double)a.My);
+}
+
 int kspace_run_mixed(fte_context* ctx, WsCarver& wc, const KspaceArgs& a) {
     const int ng = a.kind == FTE_KIND_SLP ? 2 : 4;
     const int Mx = a.Mx, My = a.My;
@@ -937,16 +1236,7 @@ int kspace_run_mixed(fte_context* ctx, WsCarver& wc, const KspaceArgs& a) {
     float* H = wc.take<float>(ng * G);
     float2* Hh = wc.take<float2>(ng * (size_t)Mx * Kh);
     FTE_WS_CHECK(wc);
-    WinParams wp;
-    wp.Lx = a.Lx;
-    wp.Ly = a.Ly;
-    wp.h = a.Lx / Mx;
-    wp.xi = a.xi;
-    wp.eta = a.eta;
-    wp.w = a.w;
-    wp.P = a.P;
-    wp.Mx = Mx;
-    wp.My = My;
+    const WinParams wp = win_params(a);
     FftDev py, px;
     FTE_TRY(fte_get_plan(ctx, My, &py));
     FTE_TRY(fte_get_plan(ctx, Mx, &px));
@@ -956,10 +1246,7 @@ int kspace_run_mixed(fte_context* ctx, WsCarver& wc, const KspaceArgs& a) {
         return FTE_ERR_UNSUPPORTED;
     }
     int ts_s = 0, ts_g = 0;
-    for (int ts = 64; ts >= 8 && !ts_s; ts -= 4)
-        if (spread_cols32_smem(ts, a.P) <= tile_budget(ctx)) ts_s = ts;
-    for (int ts = 64; ts >= 8 && !ts_g; ts -= 4)
-        if (gather32_smem(ts, a.P) <= tile_budget(ctx)) ts_g = ts;
+    FTE_TRY(resolve_tiles(ctx, a, &ts_s, &ts_g));
     if (!ts_s || !ts_g) {
         fte_set_error("window support P=%d too large for the mixed form's tiles", a.P);
         return FTE_ERR_UNSUPPORTED;
@@ -981,18 +1268,7 @@ int kspace_run_mixed(fte_context* ctx, WsCarver& wc, const KspaceArgs& a) {
     }
     FTE_TRY(fte_record(ctx, 2));
     FTE_CUDA_TRY(cudaMemsetAsync(H, 0, sizeof(float) * ng * G, ctx->stream));
-    if (a.nsrc > 0) {
-        size_t sm = spread_cols32_smem(ts_s, a.P);
-        int nt = tb_s.ntx * tb_s.nty;
-        int grid = nt < ctx->num_sms * 8 ? nt : ctx->num_sms * 8;
-        FTE_CUDA_TRY(cudaFuncSetAttribute(k_spread_cols32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        for (int pass = 0; pass < ng / 2; pass++) {
-            int mode = ng == 2 ? 0 : 1 + pass;
-            FTE_LAUNCH(ctx, k_spread_cols32, grid, kColThreads, sm, mode, a.psrc, a.f, a.nrm, a.wts,
-                       (const int*)tb_s.off, (const int*)tb_s.perm, ts_s, tb_s.ntx, tb_s.nty, wp, H + 2 * pass * G,
-                       H + (2 * pass + 1) * G);
-        }
-    }
+    if (a.nsrc > 0) FTE_TRY(launch_spread_tiled(ctx, a, tb_s, wp, H));
     FTE_TRY(fte_record(ctx, 3));
     FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_y_r2c32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_y));
     FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_y_c2r32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_y));
@@ -1008,36 +1284,15 @@ int kspace_run_mixed(fte_context* ctx, WsCarver& wc, const KspaceArgs& a) {
     FTE_LAUNCH(ctx, k_fft_x32, dim3(Kh, 2), fft_threads(px.m), sm_x, Hh, Mx, Kh, px, 1);
     FTE_LAUNCH(ctx, k_fft_y_c2r32, dim3(Mx / 2, 2), fft_threads(py.m), sm_y, (const float2*)Hh, H, Mx, My, py);
     FTE_TRY(fte_record(ctx, 4));
-    double s = 4 * a.xi * a.xi / a.eta;
-    s = s * s * wp.h * wp.h / FTE_PI;
-    double scale = s / (4 * FTE_PI) / ((double)Mx * (double)My);
-    if (a.ntar > 0) {
-        size_t sm = gather32_smem(ts_g, a.P);
-        int nt = tb_g.ntx * tb_g.nty;
-        int grid = nt < ctx->num_sms * 8 ? nt : ctx->num_sms * 8;
-        FTE_CUDA_TRY(cudaFuncSetAttribute(k_gather_tiled32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        FTE_LAUNCH(ctx, k_gather_tiled32, grid, kTileThreads, sm, a.ptar, (const int*)tb_g.off, (const int*)tb_g.perm,
-                   ts_g, tb_g.ntx, tb_g.nty, wp, (const float*)H, (const float*)(H + G), scale, a.uk);
-    }
+    if (a.ntar > 0) FTE_TRY(launch_gather_tiled(ctx, a, tb_g, wp, H, gather_scale(a)));
     FTE_TRY(fte_record(ctx, 5));
     return FTE_OK;
 }
 }  // namespace
 
 int fte_kspace_tiles(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, TileBins* src, TileBins* tar) {
-    const int ng = a.kind == FTE_KIND_SLP ? 2 : 4;
     int ts_s = 0, ts_g = 0;
-    if (a.form == FTE_FORM_MIXED) {
-        for (int ts = 64; ts >= 8 && !ts_s; ts -= 4)
-            if (spread_cols32_smem(ts, a.P) <= tile_budget(ctx)) ts_s = ts;
-        for (int ts = 64; ts >= 8 && !ts_g; ts -= 4)
-            if (gather32_smem(ts, a.P) <= tile_budget(ctx)) ts_g = ts;
-    } else {
-        for (int ts = 64; ts >= 8 && !ts_s; ts -= 4)
-            if (spread_cols_smem(ts, a.P) <= tile_budget(ctx)) ts_s = ts;
-        ts_g = pick_tile(2, a.P, tile_budget(ctx));
-    }
-    (void)ng;
+    FTE_TRY(resolve_tiles(ctx, a, &ts_s, &ts_g));
     src->ts = tar->ts = 0;
     src->ntx = tar->ntx = 0;
     const double h = a.Lx / a.Mx;
@@ -1050,15 +1305,107 @@ int fte_kspace_tiles(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, TileBi
     return FTE_OK;
 }
 
+// Autotuner of the spread and gather tiles.  Small tiles give more CTAs (a
+// 256 x 256 grid has only 16 tiles of 64 x 64 for 152 SMs) but re-read more
+// halo nodes per grid node; the best size depends on the grid, the window
+// support and how the points cluster, so it is measured: every candidate size
+// that fits shared memory is timed (bins built, one warm-up, then the median
+// of three launches, CUDA events on the context's stream) on the plan's own
+// points and densities.  `grid` holds the plan's grids (ng grids of Mx*My
+// nodes, FP64 or FP32 by form) and `bins` scratch for one candidate's tile
+// bins; a.uk receives junk velocities.
+int fte_kspace_tune(fte_context* ctx, void* grid, WsCarver bins, KspaceArgs& a, float* ms_spread,
+                    float* ms_gather) {
+    static const int cand[] = {8, 12, 16, 20, 24, 32, 40, 48, 56, 64};
+    const WinParams wp = win_params(a);
+    const int ng = a.kind == FTE_KIND_SLP ? 2 : 4;
+    const size_t gbytes = (size_t)ng * a.Mx * a.My * (a.form == FTE_FORM_MIXED ? sizeof(float) : sizeof(double));
+    cudaEvent_t e[4];
+    for (int i = 0; i < 4; i++) FTE_CUDA_TRY(cudaEventCreate(&e[i]));
+    auto time3 = [&](auto&& launch, float* out) -> int {
+        FTE_TRY(launch());  // warm-up
+        float t[3];
+        for (int r = 0; r < 3; r++) {
+            FTE_CUDA_TRY(cudaEventRecord(e[0], ctx->stream));
+            FTE_TRY(launch());
+            FTE_CUDA_TRY(cudaEventRecord(e[1], ctx->stream));
+            FTE_CUDA_TRY(cudaEventSynchronize(e[1]));
+            FTE_CUDA_TRY(cudaEventElapsedTime(&t[r], e[0], e[1]));
+        }
+        float lo = fminf(t[0], fminf(t[1], t[2])), hi = fmaxf(t[0], fmaxf(t[1], t[2]));
+        *out = t[0] + t[1] + t[2] - lo - hi;
+        return FTE_OK;
+    };
+    int rc = FTE_OK;
+    float best_s = 1e30f, best_g = 1e30f;
+    int ts_s = 0, ts_g = 0;
+    for (int ts : cand) {
+        if (rc || a.nsrc == 0 || !spread_fits(ctx, a.form, ts, a.P)) continue;
+        WsCarver w = bins;
+        TileBins tb;
+        rc = fte_tiles_build(ctx, w, a.psrc, a.nsrc, a.Lx, a.Ly, wp.h, ts, (a.Mx + ts - 1) / ts,
+                             (a.My + ts - 1) / ts, &tb);
+        if (!rc && !w.ok()) {
+            fte_set_error("internal: tuner bin scratch too small");
+            rc = FTE_ERR_ALLOC;
+        }
+        float ms = 0;
+        if (!rc)
+            rc = time3(
+                [&]() -> int {
+                    FTE_CUDA_TRY(cudaMemsetAsync(grid, 0, gbytes, ctx->stream));
+                    return launch_spread_tiled(ctx, a, tb, wp, grid);
+                },
+                &ms);
+        if (!rc && ms < best_s) {
+            best_s = ms;
+            ts_s = ts;
+        }
+    }
+    const double scale = gather_scale(a);
+    for (int ts : cand) {
+        if (rc || a.ntar == 0 || !gather_fits(ctx, a.form, ts, a.P)) continue;
+        WsCarver w = bins;
+        TileBins tb;
+        rc = fte_tiles_build(ctx, w, a.ptar, a.ntar, a.Lx, a.Ly, wp.h, ts, (a.Mx + ts - 1) / ts,
+                             (a.My + ts - 1) / ts, &tb);
+        if (!rc && !w.ok()) {
+            fte_set_error("internal: tuner bin scratch too small");
+            rc = FTE_ERR_ALLOC;
+        }
+        float ms = 0;
+        if (!rc) rc = time3([&]() -> int { return launch_gather_tiled(ctx, a, tb, wp, grid, scale); }, &ms);
+        if (!rc && ms < best_g) {
+            best_g = ms;
+            ts_g = ts;
+        }
+    }
+    for (int i = 0; i < 4; i++) cudaEventDestroy(e[i]);
+    if (rc) return rc;
+    a.ts_spread = ts_s;
+    a.ts_gather = ts_g;
+    if (ms_spread) *ms_spread = ts_s ? best_s : 0.f;
+    if (ms_gather) *ms_gather = ts_g ? best_g : 0.f;
+    return FTE_OK;
+}
+
 size_t fte_kspace_ws(int kind, int form, int Mx, int My, int64_t nsrc, int64_t ntar) {
-    (void)form;
     int ng = kind == FTE_KIND_SLP ? 2 : 4;
     size_t G = (size_t)Mx * My;
     size_t Gh = (size_t)Mx * (My / 2 + 1);
     // tiles no smaller than 8 nodes
     int ntiles = ((Mx + 7) / 8) * ((My + 7) / 8);
-    return ws_bytes(ng * G, sizeof(double)) + ws_bytes(ng * Gh, sizeof(double2)) + fte_tiles_ws(nsrc, ntiles) +
-           fte_tiles_ws(ntar, ntiles) + 4096;
+    size_t s = ws_bytes(ng * G, sizeof(double)) + ws_bytes(ng * Gh, sizeof(double2)) + fte_tiles_ws(nsrc, ntiles) +
+               fte_tiles_ws(ntar, ntiles) + 4096;
+    if (form != FTE_FORM_MIXED) {
+        // long FP64 transforms: staging lines along y and the four-step scratch
+        const bool ly = !fte_fft_fits_block(My, sizeof(double2)), lx = !fte_fft_fits_block(Mx, sizeof(double2));
+        if (ly) s += ws_bytes((size_t)ng * (Mx / 2) * My, sizeof(double2));
+        size_t a = ly ? fte_long_scratch(My, (long long)ng * (Mx / 2)) : 0;
+        size_t b = lx ? fte_long_scratch(Mx, (long long)ng * (My / 2 + 1)) : 0;
+        if (a || b) s += ws_bytes(a > b ? a : b, sizeof(double2));
+    }
+    return s;
 }
 
 int fte_kspace_run(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, fte_info* info) {
@@ -1070,34 +1417,41 @@ int fte_kspace_run(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, fte_info
     double* H = wc.take<double>(ng * G);
     double2* Hh = wc.take<double2>(ng * (size_t)Mx * Kh);
     FTE_WS_CHECK(wc);
-    WinParams wp;
-    wp.Lx = a.Lx;
-    wp.Ly = a.Ly;
-    wp.h = a.Lx / Mx;
-    wp.xi = a.xi;
-    wp.eta = a.eta;
-    wp.w = a.w;
-    wp.P = a.P;
-    wp.Mx = Mx;
-    wp.My = My;
-    FftDev py, px;
-    FTE_TRY(fte_get_plan(ctx, My, &py));
-    FTE_TRY(fte_get_plan(ctx, Mx, &px));
+    const WinParams wp = win_params(a);
+    // block transforms where a line fits shared memory, long ones elsewhere
+    const bool long_y = !fte_fft_fits_block(My, sizeof(double2));
+    const bool long_x = !fte_fft_fits_block(Mx, sizeof(double2));
+    FftDev py{}, px{};
+    LongFft ly, lx;
+    if (long_y)
+        FTE_TRY(fte_get_long_plan(ctx, My, &ly));
+    else
+        FTE_TRY(fte_get_plan(ctx, My, &py));
+    if (long_x)
+        FTE_TRY(fte_get_long_plan(ctx, Mx, &lx));
+    else
+        FTE_TRY(fte_get_plan(ctx, Mx, &px));
     size_t sm_y = 2 * (size_t)py.m * sizeof(double2);
     size_t sm_x = 2 * (size_t)px.m * sizeof(double2);
     if (sm_y > (size_t)ctx->max_smem_optin || sm_x > (size_t)ctx->max_smem_optin) {
-        fte_set_error("grid %d x %d needs FFT lengths (%d, %d) beyond this build's shared-memory transform", Mx, My,
-                      px.m, py.m);
+        fte_set_error("grid %d x %d needs FFT lengths (%d, %d) beyond this device's shared memory", Mx, My, px.m,
+                      py.m);
         return FTE_ERR_UNSUPPORTED;
     }
+    double2* S = long_y ? wc.take<double2>((size_t)ng * (Mx / 2) * My) : nullptr;
+    const size_t lsy = long_y ? fte_long_scratch(My, (long long)ng * (Mx / 2)) : 0;
+    const size_t lsx = long_x ? fte_long_scratch(Mx, (long long)ng * Kh) : 0;
+    double2* LS = (lsy || lsx) ? wc.take<double2>(lsy > lsx ? lsy : lsx) : nullptr;
+    FTE_WS_CHECK(wc);
+    const LineMap rows{(long long)My, 0, 1, 1};
+    const LineMap cols{(long long)Mx * Kh, 1, (long long)Kh, Kh};
     const int P1 = a.P + 1;
     size_t sm_pt = (size_t)(((P1 + 1) & ~1) + kPtThreads * P1) * sizeof(double);
 
-    // tile the grid for the shared-memory spread and gather
-    int ts_s = 0;  // column-owned spread: largest tile whose region fits
-    for (int ts = 64; ts >= 8 && !ts_s; ts -= 4)
-        if (spread_cols_smem(ts, a.P) <= tile_budget(ctx)) ts_s = ts;
-    const int ts_g = pick_tile(2, a.P, tile_budget(ctx));
+    // tile the grid for the shared-memory spread and gather (0: window too
+    // wide for any tile; the per-point kernels with global atomics are used)
+    int ts_s = 0, ts_g = 0;
+    FTE_TRY(resolve_tiles(ctx, a, &ts_s, &ts_g));
     TileBins tb_s, tb_g;
     tb_s.ntx = tb_g.ntx = 0;
     tb_s.ts = tb_g.ts = 0;
@@ -1119,16 +1473,7 @@ int fte_kspace_run(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, fte_info
     FTE_TRY(fte_record(ctx, 2));
     FTE_CUDA_TRY(cudaMemsetAsync(H, 0, sizeof(double) * ng * G, ctx->stream));
     if (a.nsrc > 0 && ts_s > 0) {
-        size_t sm = spread_cols_smem(ts_s, a.P);
-        int nt = tb_s.ntx * tb_s.nty;
-        int grid = nt < ctx->num_sms * 8 ? nt : ctx->num_sms * 8;
-        FTE_CUDA_TRY(cudaFuncSetAttribute(k_spread_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        for (int pass = 0; pass < ng / 2; pass++) {
-            int mode = ng == 2 ? 0 : 1 + pass;
-            FTE_LAUNCH(ctx, k_spread_cols, grid, kColThreads, sm, mode, a.psrc, a.f, a.nrm, a.wts,
-                       (const int*)tb_s.off, (const int*)tb_s.perm, ts_s, tb_s.ntx, tb_s.nty, wp, H + 2 * pass * G,
-                       H + (2 * pass + 1) * G);
-        }
+        FTE_TRY(launch_spread_tiled(ctx, a, tb_s, wp, H));
     } else if (a.nsrc > 0) {
         if (ng == 2) {
             FTE_CUDA_TRY(cudaFuncSetAttribute(k_spread<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_pt));
@@ -1141,31 +1486,44 @@ int fte_kspace_run(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, fte_info
         }
     }
     FTE_TRY(fte_record(ctx, 3));
-    FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_y_r2c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_y));
-    FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_y_c2r, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_y));
-    FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_x));
-    FTE_LAUNCH(ctx, k_fft_y_r2c, dim3(Mx / 2, ng), fft_threads(py.m), sm_y, (const double*)H, Hh, Mx, My, py);
-    FTE_LAUNCH(ctx, k_fft_x, dim3(Kh, ng), fft_threads(px.m), sm_x, Hh, Mx, Kh, px, 0);
+    if (!long_y) {
+        FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_y_r2c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_y));
+        FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_y_c2r, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_y));
+        FTE_LAUNCH(ctx, k_fft_y_r2c, dim3(Mx / 2, ng), fft_threads(py.m), sm_y, (const double*)H, Hh, Mx, My, py);
+    } else {
+        const long long tot = (long long)ng * (Mx / 2) * My;
+        FTE_LAUNCH(ctx, k_ly_pack_r2c, ew_grid(ctx, tot), 256, 0, (const double*)H, S, Mx, My, ng);
+        FTE_TRY(fte_long_fft(ctx, ly, S, rows, (long long)ng * (Mx / 2), false, LS));
+        FTE_LAUNCH(ctx, k_ly_unpack_r2c, ew_grid(ctx, (long long)ng * (Mx / 2) * Kh), 256, 0, (const double2*)S, Hh,
+                   Mx, My, ng);
+    }
+    if (!long_x) {
+        FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_x));
+        FTE_LAUNCH(ctx, k_fft_x, dim3(Kh, ng), fft_threads(px.m), sm_x, Hh, Mx, Kh, px, 0);
+    } else {
+        FTE_TRY(fte_long_fft(ctx, lx, Hh, cols, (long long)ng * Kh, false, LS));
+    }
     int fb = (int)(((size_t)Mx * Kh + 255) / 256);
     if (fb > ctx->num_sms * 32) fb = ctx->num_sms * 32;
     if (a.kind == FTE_KIND_SLP)
         FTE_LAUNCH(ctx, k_filter<FTE_KIND_SLP>, fb, 256, 0, Hh, Mx, My, a.Lx, a.Ly, a.xi, a.eta);
     else
         FTE_LAUNCH(ctx, k_filter<FTE_KIND_DLP>, fb, 256, 0, Hh, Mx, My, a.Lx, a.Ly, a.xi, a.eta);
-    FTE_LAUNCH(ctx, k_fft_x, dim3(Kh, 2), fft_threads(px.m), sm_x, Hh, Mx, Kh, px, 1);
-    FTE_LAUNCH(ctx, k_fft_y_c2r, dim3(Mx / 2, 2), fft_threads(py.m), sm_y, (const double2*)Hh, H, Mx, My, py);
+    if (!long_x)
+        FTE_LAUNCH(ctx, k_fft_x, dim3(Kh, 2), fft_threads(px.m), sm_x, Hh, Mx, Kh, px, 1);
+    else
+        FTE_TRY(fte_long_fft(ctx, lx, Hh, cols, 2LL * Kh, true, LS));
+    if (!long_y) {
+        FTE_LAUNCH(ctx, k_fft_y_c2r, dim3(Mx / 2, 2), fft_threads(py.m), sm_y, (const double2*)Hh, H, Mx, My, py);
+    } else {
+        FTE_LAUNCH(ctx, k_ly_pack_c2r, ew_grid(ctx, 2LL * (Mx / 2) * Kh), 256, 0, (const double2*)Hh, S, Mx, My, 2);
+        FTE_TRY(fte_long_fft(ctx, ly, S, rows, 2LL * (Mx / 2), true, LS));
+        FTE_LAUNCH(ctx, k_ly_unpack_c2r, ew_grid(ctx, 2LL * (Mx / 2) * My), 256, 0, (const double2*)S, H, Mx, My, 2);
+    }
     FTE_TRY(fte_record(ctx, 4));
-    double s = 4 * a.xi * a.xi / a.eta;
-    s = s * s * wp.h * wp.h / FTE_PI;
-    double scale = s / (4 * FTE_PI) / ((double)Mx * (double)My);
+    const double scale = gather_scale(a);
     if (a.ntar > 0 && ts_g > 0) {
-        const int W = tile_region(ts_g, a.P);
-        size_t sm = 2 * (size_t)W * W * sizeof(double) + sm_pt;
-        int nt = tb_g.ntx * tb_g.nty;
-        int grid = nt < ctx->num_sms * 8 ? nt : ctx->num_sms * 8;
-        FTE_CUDA_TRY(cudaFuncSetAttribute(k_gather_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        FTE_LAUNCH(ctx, k_gather_tiled, grid, kTileThreads, sm, a.ptar, (const int*)tb_g.off, (const int*)tb_g.perm,
-                   ts_g, tb_g.ntx, tb_g.nty, wp, (const double*)H, (const double*)(H + G), scale, a.uk);
+        FTE_TRY(launch_gather_tiled(ctx, a, tb_g, wp, H, scale));
     } else if (a.ntar > 0) {
         FTE_CUDA_TRY(cudaFuncSetAttribute(k_gather, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_pt));
         FTE_LAUNCH(ctx, k_gather, pt_grid(ctx, a.ntar), kPtThreads, sm_pt, a.ptar, a.ntar, wp, (const double*)H,

@@ -217,6 +217,8 @@ static int plan_exec_body(fte_plan* p, int nv, const double* f1s, const double* 
         a.uk = p->uk + v * nt;
         a.pre_src = &p->tb_src;
         a.pre_tar = &p->tb_tar;
+        a.ts_spread = p->prm.ts_spread;
+        a.ts_gather = p->prm.ts_gather;
         FTE_TRY(fte_kspace_run(c, wc, a, nullptr));
     }
     if (p->kind == FTE_KIND_DLP && ns > 0)
@@ -334,24 +336,23 @@ extern "C" int fte_plan_create(fte_context* c, int kind, const double* xsrc, con
         return FTE_ERR_ALLOC;
     }
     p->mem_size = need;
+    // frees the plan on every early return below
+    struct Guard {
+        fte_plan* p;
+        ~Guard() {
+            if (p) {
+                cudaStreamSynchronize(p->ctx->stream);
+                cudaFree(p->mem);
+                delete p;
+            }
+        }
+    } guard{p};
     WsCarver pm{p->mem, 0, need};
     p->ps = pm.take<double>(2 * (nsrc + 1));
     p->pt = pm.take<double>(2 * (ntar + 1));
     double* pf = pm.take<double>(2 * (nsrc + 1));
     p->nrm = kind == FTE_KIND_DLP ? pm.take<double>(2 * (nsrc + 1)) : nullptr;
     p->wts = dw ? pm.take<double>(nsrc + 1) : nullptr;
-    if (nsrc > 0) {
-        FTE_LAUNCH(c, k_plan_wrap, grid_of(c, nsrc), 256, 0, dxs, dys, nsrc, Lx, Ly, p->ps);
-        FTE_LAUNCH(c, k_plan_pack, grid_of(c, nsrc), 256, 0, df1, df2, nsrc, pf);
-        if (p->nrm) FTE_LAUNCH(c, k_plan_pack, grid_of(c, nsrc), 256, 0, dn1, dn2, nsrc, p->nrm);
-        if (p->wts) FTE_CUDA_TRY(cudaMemcpyAsync(p->wts, dw, nsrc * 8, cudaMemcpyDeviceToDevice, c->stream));
-    }
-    if (ntar > 0) FTE_LAUNCH(c, k_plan_wrap, grid_of(c, ntar), 256, 0, dxt, dyt, ntar, Lx, Ly, p->pt);
-    FTE_TRY(fte_cells_build(c, pm, kind, p->ps, nsrc, p->pt, ntar, pf, p->nrm, p->wts, prm.nside_x, prm.nside_y, Lx,
-                            Ly, &p->cl));
-    ka.psrc = p->ps;
-    ka.ptar = p->pt;
-    FTE_TRY(fte_kspace_tiles(c, pm, ka, &p->tb_src, &p->tb_tar));
     p->q0 = pm.take<double>(nv * (nsrc + 1));
     p->q1 = pm.take<double>(nv * (nsrc + 1));
     p->q2 = pm.take<double>(nv * (nsrc + 1));
@@ -361,6 +362,39 @@ extern "C" int fte_plan_create(fte_context* c, int kind, const double* xsrc, con
     p->uk = pm.take<double2>(nv * (ntar + 1));
     p->kscratch = pm.take<char>(p->kscratch_size);
     FTE_WS_CHECK(pm);
+    if (nsrc > 0) {
+        FTE_LAUNCH(c, k_plan_wrap, grid_of(c, nsrc), 256, 0, dxs, dys, nsrc, Lx, Ly, p->ps);
+        FTE_LAUNCH(c, k_plan_pack, grid_of(c, nsrc), 256, 0, df1, df2, nsrc, pf);
+        if (p->nrm) FTE_LAUNCH(c, k_plan_pack, grid_of(c, nsrc), 256, 0, dn1, dn2, nsrc, p->nrm);
+        if (p->wts) FTE_CUDA_TRY(cudaMemcpyAsync(p->wts, dw, nsrc * 8, cudaMemcpyDeviceToDevice, c->stream));
+    }
+    if (ntar > 0) FTE_LAUNCH(c, k_plan_wrap, grid_of(c, ntar), 256, 0, dxt, dyt, ntar, Lx, Ly, p->pt);
+    FTE_TRY(fte_cells_build(c, pm, kind, p->ps, nsrc, p->pt, ntar, pf, p->nrm, p->wts, prm.nside_x, prm.nside_y, Lx,
+                            Ly, &p->cl));
+    FTE_WS_CHECK(pm);
+    ka.psrc = p->ps;
+    ka.ptar = p->pt;
+    ka.f = pf;
+    ka.nrm = p->nrm;
+    ka.wts = p->wts;
+    ka.xi = prm.xi;
+    ka.eta = prm.eta;
+    ka.w = prm.w;
+    ka.uk = p->uk;
+    if (opt->tune && (nsrc > 0 || ntar > 0)) {
+        // the staged inputs are no longer needed: the context workspace holds
+        // one candidate's tile bins at a time
+        const int ntiles8 = ((prm.Mx + 7) / 8) * ((prm.My + 7) / 8);
+        const size_t bins = fte_tiles_ws(nsrc > ntar ? nsrc : ntar, ntiles8) + 4096;
+        FTE_CUDA_TRY(cudaStreamSynchronize(c->stream));
+        FTE_TRY(fte_ws_reserve(c, bins));
+        WsCarver bw{c->ws, 0, c->ws_size};
+        FTE_TRY(fte_kspace_tune(c, p->kscratch, bw, ka, nullptr, nullptr));
+    }
+    FTE_TRY(fte_kspace_tiles(c, pm, ka, &p->tb_src, &p->tb_tar));
+    FTE_WS_CHECK(pm);
+    p->prm.ts_spread = nsrc > 0 ? p->tb_src.ts : ka.ts_spread;
+    p->prm.ts_gather = ntar > 0 ? p->tb_tar.ts : ka.ts_gather;
     CellList cl = p->cl;
     cl.q0 = p->q0;
     cl.q1 = p->q1;
@@ -369,10 +403,10 @@ extern "C" int fte_plan_create(fte_context* c, int kind, const double* xsrc, con
     fte_near_fill_params(kind, cl, prm.xi, Lx, Ly, &p->near);
     fte_near_set_output(&p->near, p->ur, ntar, fte_near_cap(c, kind, nv));
     // warm the FFT tables so that executions (and graph capture) allocate nothing
-    FftDev tmp;
-    FTE_TRY(fte_get_plan(c, prm.Mx, &tmp));
-    FTE_TRY(fte_get_plan(c, prm.My, &tmp));
+    FTE_TRY(fte_fft_prepare(c, prm.Mx));
+    FTE_TRY(fte_fft_prepare(c, prm.My));
     FTE_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    guard.p = nullptr;
     *out = p;
     return FTE_OK;
 }
@@ -493,6 +527,8 @@ static int batch_run(fte_batch* b) {
                 a.uk = p->uk + v * p->ntar;
                 a.pre_src = &p->tb_src;
                 a.pre_tar = &p->tb_tar;
+                a.ts_spread = p->prm.ts_spread;
+                a.ts_gather = p->prm.ts_gather;
                 rc = fte_kspace_run(c, wc, a, nullptr);
             }
             if (rc == FTE_OK && p->kind == FTE_KIND_DLP && p->nsrc > 0) {

@@ -79,6 +79,8 @@ typedef struct {
     double w;       /* window half-width P*h/2 */
     double eta;     /* window shape (2 xi w / m)^2, m = 0.95 sqrt(pi P) */
     int form;       /* arithmetic of the k-space part: FTE_FORM_PLAIN (FP64) or FTE_FORM_MIXED (FP32) */
+    int ts_spread;  /* k-space spread / gather tile sizes in grid nodes (plans; 0: the default rule) */
+    int ts_gather;
 } fte_params;
 
 /* Options of the driver-level entries; zero-initialise for the reference
@@ -92,6 +94,7 @@ typedef struct {
     int nside_x, nside_y;  /* > 0: override the cell list (cutoff = sqrt(Lx Ly/(nside_x nside_y))) */
     const double* weights; /* optional quadrature weights, multiplied into f (length nsrc) */
     int form;              /* FTE_FORM_PLAIN or FTE_FORM_MIXED */
+    int tune;              /* plans: 1 = time the k-space tile sizes on the plan's points at creation */
 } fte_options;
 
 /* Per-call diagnostics (optional output of the driver entries). */

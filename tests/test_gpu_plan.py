@@ -188,3 +188,28 @@ def test_batch_new_density_between_launches(gpu_ctx):
             e1, e2 = p.execute(*dens[i])
             assert rel_max(np.stack([b1, b2]), np.stack([e1, e2])) <= 1e-12, (step, i)
     batch.close()
+
+
+@pytest.mark.parametrize("form,tol", [(0, 1e-12), (1, 1e-6)])
+def test_tuned_tiles_give_same_result(gpu_ctx, form, tol):
+    """Tile sizes chosen by the autotuner change the work decomposition only:
+    results agree with the default tiles (FP64 form to 1e-12; FP32 k-space
+    within its tolerance) and the chosen sizes are reported."""
+    ft = _ft()
+    Lx, Ly = 1.5, 1.0
+    g = _geom(51, 30000, Lx, Ly)
+    f1s, f2s = _dens(52, 2, 30000)
+    for kind in (ft.KIND_SLP, ft.KIND_DLP):
+        base = ft.Plan(kind, *g[:4], f1s[0], f2s[0], Lx, Ly, n1=g[4], n2=g[5], tol=tol, form=form, nvmax=2,
+                       ctx=gpu_ctx)
+        tuned = ft.Plan(kind, *g[:4], f1s[0], f2s[0], Lx, Ly, n1=g[4], n2=g[5], tol=tol, form=form, nvmax=2,
+                        tune=True, ctx=gpu_ctx)
+        pb, pt = base.params, tuned.params
+        assert (pb.Mx, pb.My, pb.P, pb.form) == (pt.Mx, pt.My, pt.P, pt.form)
+        assert pt.ts_spread in (8, 12, 16, 20, 24, 32, 40, 48, 56, 64)
+        assert pt.ts_gather in (8, 12, 16, 20, 24, 32, 40, 48, 56, 64)
+        assert pb.ts_spread > 0 and pb.ts_gather > 0
+        b1, b2 = base.execute(f1s, f2s)
+        t1, t2 = tuned.execute(f1s, f2s)
+        bar = 1e-12 if pb.form == ft.FORM_PLAIN else tol
+        assert rel_max(np.stack([t1, t2]), np.stack([b1, b2])) <= bar, (kind, pt.ts_spread, pt.ts_gather)
