@@ -63,7 +63,7 @@ class Params(C.Structure):
 class Options(C.Structure):
     _fields_ = [("P", C.c_int), ("Nb", C.c_double), ("tol", C.c_double), ("xi", C.c_double),
                 ("Mx", C.c_int), ("My", C.c_int), ("nside_x", C.c_int), ("nside_y", C.c_int),
-                ("weights", C.c_void_p), ("form", C.c_int), ("tune", C.c_int)]
+                ("weights", C.c_void_p), ("form", C.c_int), ("tune", C.c_int), ("slack", C.c_double)]
 
 
 class Info(C.Structure):
@@ -115,6 +115,11 @@ SIGNATURES = {
     "fte_batch_destroy": (_i, [_vp]),
     "fte_batch_set_density": (_i, [_vp, _i, _vp, _vp, _u]),
     "fte_batch_get_velocity": (_i, [_vp, _i, _vp, _vp, _u]),
+    "fte_mlp_param_count": (_i, []),
+    "fte_mlp_scratch_floats": (C.c_size_t, [_i]),
+    "fte_mlp_forward": (_i, [_vp, _vp, _i, _vp, _vp]),
+    "fte_mlp_loss_grad": (_i, [_vp, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp]),
+    "fte_mlp_adam": (_i, [_vp, _vp, _vp, _vp, _i, C.c_float, C.c_float, C.c_float, C.c_float, _vp]),
 }
 
 
@@ -318,7 +323,7 @@ def mex_stokes_dlp_kspace(psrc, ptar, xi, eta, f, n, Mx, My, Lx, Ly, w, P, ctx: 
 # ---- driver-shaped entries -----------------------------------------------------
 
 def _options(P=None, Nb=None, tol=1e-16, xi=None, Mx=None, My=None, nside_x=None, nside_y=None, weights_ptr=None,
-             form=FORM_PLAIN, tune=False) -> Options:
+             form=FORM_PLAIN, tune=False, slack=None) -> Options:
     o = Options()
     o.P = int(P or 0)
     o.Nb = float(Nb) if Nb else 0.0
@@ -331,6 +336,7 @@ def _options(P=None, Nb=None, tol=1e-16, xi=None, Mx=None, My=None, nside_x=None
     o.weights = weights_ptr
     o.form = int(form)
     o.tune = 1 if tune else 0
+    o.slack = float(slack) if slack else 0.0
     return o
 
 
@@ -348,7 +354,7 @@ def _print_verbose(kind: str, ns: int, nt: int, info: Info):
 
 
 def _ewald(kind, xsrc, ysrc, xtar, ytar, n1, n2, f1, f2, Lx, Ly, P, Nb, tol, verbose, weights, xi, Mx, My,
-           nside_x, nside_y, form, ctx, return_info, out, parts):
+           nside_x, nside_y, form, ctx, return_info, out, parts, slack=None):
     ctx = ctx or default_context()
     A = _Args()
     pxs, ns = A.arr(xsrc, 1)
@@ -367,7 +373,7 @@ def _ewald(kind, xsrc, ysrc, xtar, ytar, n1, n2, f1, f2, Lx, Ly, P, Nb, tol, ver
     if parts:
         ur, pur = A.out((nt, 2))
         uk, puk = A.out((nt, 2))
-    opt = _options(P, Nb, tol, xi, Mx, My, nside_x, nside_y, pw, form)
+    opt = _options(P, Nb, tol, xi, Mx, My, nside_x, nside_y, pw, form, slack=slack)
     info = Info()
     if verbose:
         ctx.set_timing(True)
@@ -386,7 +392,8 @@ def _ewald(kind, xsrc, ysrc, xtar, ytar, n1, n2, f1, f2, Lx, Ly, P, Nb, tol, ver
 
 def StokesSLP_ewald_2p(xsrc, ysrc, xtar, ytar, f1, f2, Lx, Ly, P=None, Nb=None, tol=1e-16, verbose=0,
                        weights=None, xi=None, Mx=None, My=None, nside_x=None, nside_y=None, form=FORM_PLAIN,
-                       ctx: Context | None = None, return_info: bool = False, out=None, parts: bool = True):
+                       ctx: Context | None = None, return_info: bool = False, out=None, parts: bool = True,
+                       slack=None):
     """Spectral Ewald evaluation of the doubly-periodic Stokeslet.
 
     Returns (u1, u2, ur, uk, xi) like the MATLAB driver; ur and uk are
@@ -394,19 +401,20 @@ def StokesSLP_ewald_2p(xsrc, ysrc, xtar, ytar, f1, f2, Lx, Ly, P=None, Nb=None, 
     buffers (same side as the inputs).
     """
     return _ewald(KIND_SLP, xsrc, ysrc, xtar, ytar, None, None, f1, f2, Lx, Ly, P, Nb, tol, verbose, weights, xi, Mx,
-                  My, nside_x, nside_y, form, ctx, return_info, out, parts)
+                  My, nside_x, nside_y, form, ctx, return_info, out, parts, slack)
 
 
 def StokesDLP_ewald_2p(xsrc, ysrc, xtar, ytar, n1, n2, f1, f2, Lx, Ly, P=None, Nb=None, tol=1e-16, verbose=0,
                        weights=None, xi=None, Mx=None, My=None, nside_x=None, nside_y=None, form=FORM_PLAIN,
-                       ctx: Context | None = None, return_info: bool = False, out=None, parts: bool = True):
+                       ctx: Context | None = None, return_info: bool = False, out=None, parts: bool = True,
+                       slack=None):
     """Spectral Ewald evaluation of the doubly-periodic stresslet (double layer).
 
     Returns (u1, u2, ur, uk, xi); uk includes the k = 0 mode like the MATLAB
     driver.  Options as for StokesSLP_ewald_2p.
     """
     return _ewald(KIND_DLP, xsrc, ysrc, xtar, ytar, n1, n2, f1, f2, Lx, Ly, P, Nb, tol, verbose, weights, xi, Mx,
-                  My, nside_x, nside_y, form, ctx, return_info, out, parts)
+                  My, nside_x, nside_y, form, ctx, return_info, out, parts, slack)
 
 
 def choose_params(kind, f1, f2, ntar, Lx, Ly, P=None, Nb=None, tol=1e-16, **kw) -> Params:

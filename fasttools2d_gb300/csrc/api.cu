@@ -692,20 +692,28 @@ static const double kCostWin64 = 3.2e-12;      // one window node x grid, FP64 s
 static const double kCostWin32 = 1.2e-12;      // same in FP32 with compensation
 static const double kCostFft64 = 3.5e-11;      // per complex grid point x log2(points), 7-smooth FP64
 static const double kCostFft32 = 1.2e-11;      // same in FP32
-static const double kTolSlack = 3.0;
+// Calibration of the tuned choice against converged FP64 sums on 2000
+// generated configurations (uniform and clustered points, aspect 1..4,
+// tolerances 1e-12..1e-4): the stresslet's estimates meet the tolerance with
+// slack 3 and the window rule erfc(m / sqrt 2) <= tol / 300, the Stokeslet
+// needs no slack and one more window step (tol / 3000), and FP32 grids bottom
+// out near 2.5e-7 (Stokeslet) and 4e-8 (stresslet) relative.
+static const double kTolSlack[2] = {1.0, 3.0};
+static const double kWinRatio[2] = {3000.0, 300.0};
+static const double kFp32Floor[2] = {1e-6, 2e-7};
 
 static int choose_params_tuned(int kind, int64_t nsrc, int64_t ntar, double Q, double Lx, double Ly,
                                const fte_options* opt, fte_params* o) {
     // start from the analytic choice (Nb, rat, defaults) and re-optimise
     FTE_TRY(choose_params_q(kind, nsrc, ntar, Q, Lx, Ly, opt, o));
     const double tol = o->tol;
-    const double tol_e = tol * kTolSlack;
-    const bool fp32 = tol >= 1e-7;
+    const double tol_e = tol * (opt && opt->slack > 0 ? opt->slack : kTolSlack[kind]);
+    const bool fp32 = tol >= kFp32Floor[kind];
     int P = opt && opt->P > 0 ? opt->P : 0;
     if (P == 0) {
         for (P = 4; P < 24; P += 2) {
             double m = 0.95 * std::sqrt(FTE_PI * P);
-            if (std::erfc(m / std::sqrt(2.0)) <= tol / 300) break;
+            if (std::erfc(m / std::sqrt(2.0)) <= tol / kWinRatio[kind]) break;
         }
     }
     const int A = o->A, B = o->B;
@@ -1206,7 +1214,10 @@ static int ewald_entry(fte_context* c, int kind, const double* xsrc, const doubl
         CellList cl;
         FTE_TRY(fte_cells_build(c, wc2, kind, ps, nsrc, pt, ntar, pf, pn, dw, prm.nside_x, prm.nside_y, Lx, Ly, &cl));
         FTE_TRY(fte_record(c, 6));
-        FTE_TRY(fte_near_launch(c, kind, cl, prm.xi, Lx, Ly, dur));
+        // the mixed form evaluates the pairs whose terms are far below the
+        // tolerance in FP32
+        const double x32 = opt->form == FTE_FORM_MIXED ? fte_near_fp32_threshold(prm.tol) : HUGE_VAL;
+        FTE_TRY(fte_near_launch(c, kind, cl, prm.xi, Lx, Ly, dur, x32));
         FTE_TRY(fte_record(c, 7));
         KspaceArgs a;
         a.kind = kind;

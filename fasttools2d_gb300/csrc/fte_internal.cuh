@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <cmath>
 #include <stdint.h>
 
 #include <map>
@@ -246,12 +247,17 @@ size_t fte_tiles_ws(int64_t n, int ntiles);
 int fte_tiles_build(fte_context* ctx, WsCarver& wc, const double* p, int64_t n, double Lx, double Ly, double h,
                     int ts, int ntx, int nty, TileBins* out);
 
-int fte_near_launch(fte_context* ctx, int kind, const CellList& cl, double xi, double Lx, double Ly, double2* ur);
+int fte_near_launch(fte_context* ctx, int kind, const CellList& cl, double xi, double Lx, double Ly, double2* ur,
+                    double x32 = HUGE_VAL);
+// xi^2 r^2 above which a pair's terms are small enough for FP32 at tolerance
+// tol (mixed form); HUGE_VAL: every pair in FP64
+double fte_near_fp32_threshold(double tol);
 // Near-field launch description, opaque outside near.cu.
 struct NearParamsHost {
     alignas(16) unsigned char raw[256];
 };
-void fte_near_fill_params(int kind, const CellList& cl, double xi, double Lx, double Ly, NearParamsHost* hp);
+void fte_near_fill_params(int kind, const CellList& cl, double xi, double Lx, double Ly, NearParamsHost* hp,
+                          double x32 = HUGE_VAL);
 size_t fte_near_params_size();
 int fte_near_cap(const fte_context* ctx, int kind, int nv);
 // nv (1..4) density vectors at q* + v*cl.qstride; outputs at ur + v*ustride

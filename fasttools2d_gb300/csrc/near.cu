@@ -46,6 +46,9 @@ struct NearParams {
     const int* __restrict__ tidx;
     double Lx, Ly, xi, xi2, inv_xi2, selfc, cutoffsq, pf;
     float cut32;
+    // pairs with xi^2 r^2 >= x32 are evaluated in FP32 (their terms are
+    // below the tolerance's reach of FP32 rounding); +inf: all FP64
+    float x32;
     int cap;
     double2* __restrict__ ur;  // vector v at ur + v * ustride
     long long ustride;
@@ -140,16 +143,43 @@ __device__ __forceinline__ double fte_kfun(double x, const double* __restrict__ 
     return k;
 }
 
+// The same K(x) in FP32 from an FP32 copy of the table (pairs of the FP32
+// class only: x >= 1, relative error ~1e-7).
+__device__ __forceinline__ float fte_kfun32(float x, const float* __restrict__ ktab) {
+    int bits = __float_as_int(x);
+    int e = (bits >> 23) - 127;
+    int q = (bits >> 20) & 7;
+    float mant = __int_as_float((bits & 0x007FFFFF) | 0x3F800000);
+    if (e < 0) {
+        e = 0;
+        q = 0;
+        mant = x;
+    } else if (e > 9) {
+        e = 9;
+        q = 7;
+        mant = 2.0f;
+    }
+    float mid = __int_as_float(0x3F800000 | (q << 20) | (1 << 19));
+    float t = (mant - mid) * 16.0f;
+    const float* c = ktab + (8 * e + q) * (FTE_K_DEG + 1);
+    float k = c[FTE_K_DEG];
+#pragma unroll
+    for (int j = FTE_K_DEG - 1; j >= 0; j--) k = fmaf(k, t, c[j]);
+    return k;
+}
+
 // Shared-memory layout of the near-field kernels (per CTA):
-//   K(x) table, exp table, then per staged source: x, y (FP64), NV density
-//   sets (SLP: f1, f2; DLP: S11, (S12+S21)/2, S22, S11+S22), FP32 box-relative
-//   position; then two 64-entry rings per warp.
+//   K(x) table, exp table, FP32 K(x) table, then per staged source: x, y
+//   (FP64), NV density sets (SLP: f1, f2; DLP: S11, (S12+S21)/2, S22,
+//   S11+S22) in FP64 and in FP32, FP32 box-relative position; then three
+//   64-entry rings per warp.
 template <int KIND, int NV>
 struct NearSmem {
     static constexpr int kDen = KIND == FTE_KIND_SLP ? 2 : 4;
     __host__ __device__ static size_t bytes(int cap) {
-        return (kKtab + 64) * sizeof(double) + (size_t)cap * ((2 + kDen * NV) * sizeof(double) + sizeof(float2)) +
-               kNearWarps * 2 * kQueue * sizeof(int) + 64;
+        return (kKtab + 64) * sizeof(double) + kKtab * sizeof(float) +
+               (size_t)cap * ((2 + kDen * NV) * sizeof(double) + sizeof(float2) + kDen * NV * sizeof(float)) +
+               kNearWarps * 3 * kQueue * sizeof(int) + 64;
     }
 };
 
@@ -163,16 +193,23 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
     const int cap = prm.cap;
     const double* ktab = reinterpret_cast<const double*>(smem_raw);
     const double* etab = ktab + kKtab;
-    double* sx = const_cast<double*>(etab) + 64;
+    const float* ktab32 = reinterpret_cast<const float*>(etab + 64);
+    double* sx = reinterpret_cast<double*>(smem_raw) + kKtab + 64 + kKtab / 2 + 1;
     double* sy = sx + cap;
     double* den = sy + cap;  // den[(v * kDen + c) * cap + i]
     float2* s32 = reinterpret_cast<float2*>(den + (size_t)kDen * NV * cap);
-    int* qbuf = reinterpret_cast<int*>(s32 + cap);
+    float* den32 = reinterpret_cast<float*>(s32 + cap);  // den32[(v * kDen + c) * cap + i]
+    int* qbuf = reinterpret_cast<int*>(den32 + (size_t)kDen * NV * cap);
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    // per warp: ring 0 = pairs with x >= 1 (all stresslet pairs), ring 1 = x < 1 (Stokeslet)
-    int* qf = qbuf + warp * 2 * kQueue;
+    // per warp: ring 0 = FP64 pairs with x >= 1 (all FP64 stresslet pairs),
+    // ring 1 = x < 1 (Stokeslet), ring 2 = the FP32 class (x >= x32)
+    int* qf = qbuf + warp * 3 * kQueue;
     int* qn = qf + kQueue;
+    int* qs = qn + kQueue;
+    const float x32 = prm.x32;
+    const float cutf = (float)prm.cutoffsq;
+    const float pf32 = (float)prm.pf;
     const unsigned lt_mask = (1u << lane) - 1u;
     const double inv4pi = 1.0 / (4.0 * FTE_PI);
     const float xi2f = (float)prm.xi2;
@@ -231,9 +268,12 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
             for (int v = 0; v < NV; v++) {
                 const long long o = v * prm.qstride + si;
                 double* d = den + (size_t)v * kDen * cap + i;
+                float* d32 = den32 + (size_t)v * kDen * cap + i;
                 if (KIND == FTE_KIND_SLP) {
                     d[0] = prm.q0[o];
                     d[cap] = prm.q1[o];
+                    d32[0] = (float)d[0];
+                    d32[cap] = (float)d[cap];
                 } else {
                     // S11, (S12 + S21)/2, S22, S11 + S22
                     double s11 = prm.q0[o], ssym = prm.q1[o], s22 = prm.q2[o];
@@ -241,6 +281,10 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
                     d[cap] = 0.5 * ssym;
                     d[2 * cap] = s22;
                     d[3 * cap] = s11 + s22;
+                    d32[0] = (float)s11;
+                    d32[cap] = (float)(0.5 * ssym);
+                    d32[2 * cap] = (float)s22;
+                    d32[3 * cap] = (float)(s11 + s22);
                 }
             }
             s32[i] = make_float2((float)(xs - cx), (float)(ys - cy));
@@ -252,9 +296,54 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
             const double2 tp = prm.tpos[t0 + t];
             const float tx32 = (float)(tp.x - cx), ty32 = (float)(tp.y - cy);
             double acc[NV][2];
+            float acc32[NV][2];
 #pragma unroll
-            for (int v = 0; v < NV; v++) acc[v][0] = acc[v][1] = 0.0;
-            int hf = 0, cf = 0, hn = 0, cn = 0;  // ring heads and counts
+            for (int v = 0; v < NV; v++) acc[v][0] = acc[v][1] = 0.0, acc32[v][0] = acc32[v][1] = 0.0f;
+            int hf = 0, cf = 0, hn = 0, cn = 0, hs = 0, cs = 0;  // ring heads and counts
+
+            // FP32 class: the same pair terms in FP32 from box-relative
+            // positions, accumulated per lane in FP32 and added to the FP64
+            // sum once per target
+            auto eval_slp32 = [&](int s) {
+                const float2 q = s32[s];
+                const float dx = tx32 - q.x, dy = ty32 - q.y;
+                const float r2 = fmaf(dx, dx, dy * dy);
+                if (!(s < own_lim) && !(r2 < cutf)) return;
+                const float x = r2 * xi2f;
+                const float e = expf(-x);
+                const float A = e * fte_kfun32(x, ktab32);
+                const float gr = __fdividef(e, r2);
+#pragma unroll
+                for (int v = 0; v < NV; v++) {
+                    const float* d = den32 + (size_t)v * 2 * cap + s;
+                    const float fx = d[0], fy = d[cap];
+                    const float c = gr * fmaf(dx, fx, dy * fy);
+                    acc32[v][0] = fmaf(A, fx, fmaf(c, dx, acc32[v][0]));
+                    acc32[v][1] = fmaf(A, fy, fmaf(c, dy, acc32[v][1]));
+                }
+            };
+            auto eval_dlp32 = [&](int s) {
+                const float2 q = s32[s];
+                const float dx = tx32 - q.x, dy = ty32 - q.y;
+                const float r2 = fmaf(dx, dx, dy * dy);
+                if (!(s < own_lim) && !(r2 < cutf)) return;
+                const float x = r2 * xi2f;
+                const float e2 = expf(-x);
+                const float ir2 = __frcp_rn(r2);
+                const float facb = -4.0f * (1.0f + x) * ir2 * ir2;
+#pragma unroll
+                for (int v = 0; v < NV; v++) {
+                    const float* d = den32 + (size_t)v * 4 * cap + s;
+                    const float s11 = d[0], h = d[cap], s22 = d[2 * cap], tr = d[3 * cap];
+                    const float u = fmaf(dx, s11, dy * h);
+                    const float w = fmaf(dy, s22, dx * h);
+                    const float fQ = facb * fmaf(dx, u, dy * w);
+                    const float w1 = fmaf(dx, tr, u + u);
+                    const float w2 = fmaf(dy, tr, w + w);
+                    acc32[v][0] = fmaf(e2, fmaf(fQ, dx, pf32 * w1), acc32[v][0]);
+                    acc32[v][1] = fmaf(e2, fmaf(fQ, dy, pf32 * w2), acc32[v][1]);
+                }
+            };
 
             // Stokeslet pair (mex_stokes_slp_real.cpp:161-225 / 264-323):
             //   u += (0.5 E1(x) - e^-x) f + e^-x (r.f) r / r^2,   x = xi^2 r^2
@@ -323,13 +412,32 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
 
             for (int base = 0; base < clen; base += 32) {
                 int s = base + lane;
-                bool pass = false, small_x = false;
+                bool pass = false, small_x = false, single = false;
                 if (s < clen) {
                     float2 q = s32[s];
                     float dx = q.x - tx32, dy = q.y - ty32;
                     float r2f = dx * dx + dy * dy;
                     pass = (s < own_lim) || (r2f < prm.cut32);
-                    small_x = r2f * xi2f < 1.0f;
+                    const float xf = r2f * xi2f;
+                    small_x = xf < 1.0f;
+                    single = xf >= x32;
+                }
+                {
+                    const bool ps_ = pass && single;
+                    const unsigned ms = __ballot_sync(0xffffffffu, ps_);
+                    if (ps_) qs[(hs + cs + __popc(ms & lt_mask)) & (kQueue - 1)] = s;
+                    cs += __popc(ms);
+                    pass = pass && !single;
+                    __syncwarp();
+                    if (cs >= 32) {
+                        if (KIND == FTE_KIND_SLP)
+                            eval_slp32(qs[(hs + lane) & (kQueue - 1)]);
+                        else
+                            eval_dlp32(qs[(hs + lane) & (kQueue - 1)]);
+                        hs = (hs + 32) & (kQueue - 1);
+                        cs -= 32;
+                        __syncwarp();
+                    }
                 }
                 if (KIND == FTE_KIND_SLP) {
                     bool pf_ = pass && !small_x, pn_ = pass && small_x;
@@ -379,9 +487,17 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
             } else {
                 if (lane < cf) eval_dlp(qf[(hf + lane) & (kQueue - 1)]);
             }
+            if (lane < cs) {
+                if (KIND == FTE_KIND_SLP)
+                    eval_slp32(qs[(hs + lane) & (kQueue - 1)]);
+                else
+                    eval_dlp32(qs[(hs + lane) & (kQueue - 1)]);
+            }
             __syncwarp();
 #pragma unroll
             for (int v = 0; v < NV; v++) {
+                acc[v][0] += (double)acc32[v][0];
+                acc[v][1] += (double)acc32[v][1];
                 double a0 = warp_sum(acc[v][0]), a1 = warp_sum(acc[v][1]);
                 if (lane == 0) {
                     double2* o = prm.ur + v * prm.ustride + prm.tidx[t0 + t];
@@ -402,7 +518,11 @@ template <int KIND, int NV>
 __device__ __forceinline__ void near_load_tables(unsigned char* smem_raw) {
     double* ktab = reinterpret_cast<double*>(smem_raw);
     double* etab = ktab + kKtab;
-    for (int i = threadIdx.x; i < kKtab; i += kNearThreads) ktab[i] = (&fte_k_coef[0][0])[i];
+    float* ktab32 = reinterpret_cast<float*>(etab + 64);
+    for (int i = threadIdx.x; i < kKtab; i += kNearThreads) {
+        ktab[i] = (&fte_k_coef[0][0])[i];
+        ktab32[i] = (float)(&fte_k_coef[0][0])[i];
+    }
     for (int i = threadIdx.x; i < 64; i += kNearThreads) etab[i] = fte_exp_tab[i];
 }
 
@@ -445,7 +565,26 @@ int near_cap(const fte_context* ctx) {
 
 }  // namespace
 
-void fte_near_fill_params(int kind, const CellList& cl, double xi, double Lx, double Ly, NearParamsHost* hp) {
+double fte_near_fp32_threshold(double tol) {
+    // FP32 terms carry relative rounding ~1e-7 and a pair's terms scale with
+    // e^-x (1 + x); pairs with e^-x (1 + x) <= 1e5 tol keep that rounding
+    // about 1e-2 tol below the sum's own scale, which the FP64 pairs with
+    // x < 1 set.  Never below x = 1 (the Stokeslet's log branch stays FP64).
+    const double target = 1e5 * tol;
+    if (!(target > 0) || target >= 2.0 / std::exp(1.0)) return 1.0;
+    double lo = 1.0, hi = 800.0;
+    for (int it = 0; it < 100; it++) {
+        double mid = 0.5 * (lo + hi);
+        if (std::exp(-mid) * (1 + mid) > target)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return hi;
+}
+
+void fte_near_fill_params(int kind, const CellList& cl, double xi, double Lx, double Ly, NearParamsHost* hp,
+                          double x32) {
     NearParams& p = *reinterpret_cast<NearParams*>(hp->raw);
     p.nsx = cl.nsx;
     p.nsy = cl.nsy;
@@ -470,6 +609,7 @@ void fte_near_fill_params(int kind, const CellList& cl, double xi, double Lx, do
     double bsx = Lx / cl.nsx, bsy = Ly / cl.nsy;
     double bmax = bsx > bsy ? bsx : bsy;
     p.cut32 = (float)(p.cutoffsq + 1e-4 * bmax * bmax);
+    p.x32 = x32 >= 1e30 ? INFINITY : (float)(x32 > 1.0 ? x32 : 1.0);
     p.cap = 0;
     p.ur = nullptr;
     p.ustride = 0;
@@ -560,9 +700,10 @@ int fte_near_launch_batch(fte_context* ctx, int kind, int nv, const void* plist_
     }
 }
 
-int fte_near_launch(fte_context* ctx, int kind, const CellList& cl, double xi, double Lx, double Ly, double2* ur) {
+int fte_near_launch(fte_context* ctx, int kind, const CellList& cl, double xi, double Lx, double Ly, double2* ur,
+                    double x32) {
     NearParamsHost hp;
-    fte_near_fill_params(kind, cl, xi, Lx, Ly, &hp);
+    fte_near_fill_params(kind, cl, xi, Lx, Ly, &hp, x32);
     return fte_near_launch_nv(ctx, kind, 1, hp, ur, 0);
 }
 

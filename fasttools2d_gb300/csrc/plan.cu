@@ -400,7 +400,8 @@ extern "C" int fte_plan_create(fte_context* c, int kind, const double* xsrc, con
     cl.q1 = p->q1;
     cl.q2 = p->q2;
     cl.qstride = nsrc;
-    fte_near_fill_params(kind, cl, prm.xi, Lx, Ly, &p->near);
+    fte_near_fill_params(kind, cl, prm.xi, Lx, Ly, &p->near,
+                         opt->form == FTE_FORM_MIXED ? fte_near_fp32_threshold(prm.tol) : HUGE_VAL);
     fte_near_set_output(&p->near, p->ur, ntar, fte_near_cap(c, kind, nv));
     // warm the FFT tables so that executions (and graph capture) allocate nothing
     FTE_TRY(fte_fft_prepare(c, prm.Mx));

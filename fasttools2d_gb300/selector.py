@@ -1,0 +1,568 @@
+"""Learned parameter selector for the spectral Ewald sums.
+
+No counterpart in the reference: its drivers take xi, the grid M, the window
+support P and the real-space cutoff from analytic error estimates
+(StokesSLP_ewald_2p.m:27-35,85-104; StokesDLP_ewald_2p.m:27-38,307-327).  This
+module learns corrections to the tuned analytic choice of the mixed form
+(``choose_params(..., form=FORM_MIXED)``) from measured GPU times and errors:
+
+* features (8): log10 N_src, log10 N_trg, box aspect ratio, cluster fraction,
+  three quantiles (10/50/90 %) of the nearest-neighbour distance in units of
+  the mean spacing (log10), log10 tolerance;
+* network: FP32 MLP 8 -> 64 -> 64 -> 4 (tanh), one per kernel (SLP, DLP),
+  trained and evaluated with the library's own CUDA kernels
+  (``fte_mlp_loss_grad``, ``fte_mlp_adam``, ``fte_mlp_forward``);
+* outputs: log(nside / nside_T), log(xi / xi_T), log(Mx / Mx_T) and
+  (P - P_T) / 2 relative to the tuned choice T -- i.e. cutoff, xi, M and P;
+* labels: for each generated configuration, the fastest of a set of parameter
+  candidates around T whose error against a converged FP64 evaluation meets
+  the tolerance (times and errors measured on the GPU);
+* safety: ``Selector.evaluate`` checks the learned result on a random sample
+  of targets against an FP64 evaluation at 1/100 of the tolerance and falls
+  back to the tuned analytic choice when the check misses the tolerance.
+
+Run ``python -m fasttools2d_gb300.selector train --out DIR`` on a GPU to
+generate data, train both networks, evaluate on held-out configurations and
+write ``selector_model.npz`` plus a JSON report.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+import os
+import time
+
+import numpy as np
+
+from . import (FORM_MIXED, FORM_PLAIN, KIND_DLP, KIND_SLP, FteError, StokesDLP_ewald_2p, StokesSLP_ewald_2p, _check,
+               choose_params, default_context, lib)
+from . import workloads as wl
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+MODEL_PATH = os.path.join(HERE, "selector_model.npz")
+FEATURES = ["log10_nsrc", "log10_ntar", "aspect", "cluster_fraction", "log10_nn_q10", "log10_nn_q50",
+            "log10_nn_q90", "log10_tol"]
+N_IN, N_HID, N_OUT = 8, 64, 4
+
+
+# ---- features -------------------------------------------------------------------
+def features(xsrc, ysrc, ntar, Lx, Ly, tol, sample=2048, seed=0):
+    """The 8 selector inputs of a configuration (host computation)."""
+    from scipy.spatial import cKDTree
+
+    x = np.asarray(xsrc, dtype=np.float64)
+    y = np.asarray(ysrc, dtype=np.float64)
+    n = len(x)
+    px = np.minimum(np.mod(x + Lx / 2, Lx), np.nextafter(Lx, 0))
+    py = np.minimum(np.mod(y + Ly / 2, Ly), np.nextafter(Ly, 0))
+    pts = np.stack([px, py], 1)
+    tree = cKDTree(pts, boxsize=[Lx, Ly])
+    rng = np.random.default_rng(seed)
+    idx = rng.choice(n, size=min(n, sample), replace=False) if n > sample else np.arange(n)
+    d, _ = tree.query(pts[idx], k=2)
+    h = np.sqrt(Lx * Ly / max(n, 1))
+    r = np.maximum(d[:, 1] / h, 1e-6)
+    q10, q50, q90 = np.log10(np.quantile(r, [0.1, 0.5, 0.9]))
+    return np.array([np.log10(max(n, 1)), np.log10(max(ntar, 1)), max(Lx, Ly) / min(Lx, Ly), float(np.mean(r < 0.25)),
+                     q10, q50, q90, np.log10(tol)], dtype=np.float64)
+
+
+# ---- the network on the GPU -------------------------------------------------------
+def _ptr(t):
+    return C.c_void_p(t.data_ptr())
+
+
+def init_params(seed=0):
+    """Glorot-uniform weights, zero biases, packed as the kernels expect."""
+    rng = np.random.default_rng(seed)
+    parts = []
+    for fan_out, fan_in in ((N_HID, N_IN), (N_HID, N_HID), (N_OUT, N_HID)):
+        lim = np.sqrt(6.0 / (fan_in + fan_out))
+        parts += [rng.uniform(-lim, lim, size=fan_out * fan_in), np.zeros(fan_out)]
+    p = np.concatenate(parts).astype(np.float32)
+    assert p.size == lib().fte_mlp_param_count()
+    return p
+
+
+def mlp_forward(params, X, stream=None):
+    """Network outputs for X [n x 8] (numpy); params FP32 (numpy or CUDA tensor)."""
+    import torch
+
+    dev = torch.device("cuda")
+    p = params if hasattr(params, "is_cuda") else torch.tensor(np.asarray(params, np.float32), device=dev)
+    x = torch.tensor(np.asarray(X, np.float32).reshape(-1, N_IN), device=dev)
+    y = torch.empty((x.shape[0], N_OUT), dtype=torch.float32, device=dev)
+    st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+    _check(lib().fte_mlp_forward(_ptr(p), _ptr(x), x.shape[0], _ptr(y), C.c_void_p(st)))
+    return y.cpu().numpy().astype(np.float64)
+
+
+def mlp_loss_grad(params, X, T, weights=None):
+    """(loss, gradient) of the weighted mean squared error, by the CUDA kernels."""
+    import torch
+
+    dev = torch.device("cuda")
+    p = torch.tensor(np.asarray(params, np.float32), device=dev)
+    x = torch.tensor(np.asarray(X, np.float32), device=dev)
+    t = torch.tensor(np.asarray(T, np.float32), device=dev)
+    w = torch.tensor(np.asarray(weights, np.float32), device=dev) if weights is not None else None
+    n = x.shape[0]
+    scratch = torch.empty(int(lib().fte_mlp_scratch_floats(n)), dtype=torch.float32, device=dev)
+    g = torch.empty_like(p)
+    loss = torch.empty(1, dtype=torch.float32, device=dev)
+    st = torch.cuda.current_stream().cuda_stream
+    _check(lib().fte_mlp_loss_grad(_ptr(p), _ptr(x), _ptr(t), _ptr(w) if w is not None else None, n, _ptr(scratch),
+                                   _ptr(g), _ptr(loss), C.c_void_p(st)))
+    return float(loss.item()), g.cpu().numpy().astype(np.float64)
+
+
+def train(X, Y, weights=None, steps=4000, lr=2e-3, seed=0, val_frac=0.1, log=None):
+    """Fit one network (inputs and outputs standardised) with full-batch Adam
+    on the GPU; keeps the parameters of the best validation loss."""
+    import torch
+
+    dev = torch.device("cuda")
+    X = np.asarray(X, np.float64)
+    Y = np.asarray(Y, np.float64)
+    rng = np.random.default_rng(seed)
+    perm = rng.permutation(len(X))
+    nval = max(1, int(len(X) * val_frac))
+    va, tr = perm[:nval], perm[nval:]
+    xm, xs = X[tr].mean(0), X[tr].std(0) + 1e-6
+    ys = Y[tr].std(0) + 1e-3
+    Xn = (X - xm) / xs
+    Yn = Y / ys
+    f32 = lambda a: torch.tensor(np.asarray(a, np.float32), device=dev)  # noqa: E731
+    xt, yt = f32(Xn[tr]), f32(Yn[tr])
+    xv, yv = f32(Xn[va]), f32(Yn[va])
+    wt = f32(np.asarray(weights)[tr]) if weights is not None else None
+    p = f32(init_params(seed))
+    m = torch.zeros_like(p)
+    v = torch.zeros_like(p)
+    g = torch.empty_like(p)
+    loss = torch.empty(1, dtype=torch.float32, device=dev)
+    ntr, nva = xt.shape[0], xv.shape[0]
+    s_tr = torch.empty(int(lib().fte_mlp_scratch_floats(ntr)), dtype=torch.float32, device=dev)
+    s_va = torch.empty(int(lib().fte_mlp_scratch_floats(nva)), dtype=torch.float32, device=dev)
+    gv = torch.empty_like(p)
+    lv = torch.empty(1, dtype=torch.float32, device=dev)
+    st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    L = lib()
+    best, best_p, hist = np.inf, p.clone(), []
+    for k in range(1, steps + 1):
+        _check(L.fte_mlp_loss_grad(_ptr(p), _ptr(xt), _ptr(yt), _ptr(wt) if wt is not None else None, ntr,
+                                   _ptr(s_tr), _ptr(g), _ptr(loss), st))
+        _check(L.fte_mlp_adam(_ptr(p), _ptr(g), _ptr(m), _ptr(v), k, lr, 0.9, 0.999, 1e-8, st))
+        if k % 50 == 0 or k == steps:
+            _check(L.fte_mlp_loss_grad(_ptr(p), _ptr(xv), _ptr(yv), None, nva, _ptr(s_va), _ptr(gv), _ptr(lv), st))
+            lval, ltr = float(lv.item()), float(loss.item())
+            hist.append((k, ltr, lval))
+            if lval < best:
+                best, best_p = lval, p.clone()
+            if log:
+                log(f"step {k} train {ltr:.4f} val {lval:.4f}")
+    return {"params": best_p.cpu().numpy(), "xmean": xm, "xstd": xs, "yscale": ys, "history": np.array(hist),
+            "val_loss": best}
+
+
+# ---- parameter sets -------------------------------------------------------------
+def _run(kind, cfg, tol, ctx, **kw):
+    """One mixed/plain driver evaluation on device arrays; returns (u (n,2) numpy, info)."""
+    fn = StokesSLP_ewald_2p if kind == KIND_SLP else StokesDLP_ewald_2p
+    args = [cfg["xs"], cfg["ys"], cfg["xt"], cfg["yt"]]
+    if kind == KIND_DLP:
+        args += [cfg["n1"], cfg["n2"]]
+    args += [cfg["f1"], cfg["f2"], cfg["Lx"], cfg["Ly"]]
+    out, info = fn(*args, tol=tol, ctx=ctx, return_info=True, parts=False, **kw)
+    return out, info
+
+
+def _u(out):
+    import torch
+
+    return torch.stack([out[0], out[1]], 1)
+
+
+def _rel_err(u, ref):
+    return float((u - ref).abs().max() / ref.abs().max())
+
+
+def overrides_from(prm):
+    """Driver options that reproduce a parameter set."""
+    return dict(P=int(prm.P), nside_x=int(prm.nside_x), nside_y=int(prm.nside_y), xi=float(prm.xi), Mx=int(prm.Mx),
+                My=int(prm.My))
+
+
+def targets_of(prm, T):
+    """Network targets of a parameter set relative to the tuned choice T."""
+    return np.array([np.log(prm.nside_x / T.nside_x), np.log(prm.xi / T.xi), np.log(prm.Mx / T.Mx),
+                     (prm.P - T.P) / 2.0])
+
+
+def params_from(y, T):
+    """Valid driver options from network outputs y relative to T."""
+    A, B = int(T.A), int(T.B)
+    a = max(1, int(round(T.nside_x / A * np.exp(y[0]))))
+    t = max(2, int(round(T.Mx / A * np.exp(y[2]))))
+    while (A * t) % 2 or (B * t) % 2:
+        t += 1
+    P = int(np.clip(T.P + 2 * round(float(y[3])), 4, 24))
+    while P + 1 > min(A * t, B * t):
+        t += 2
+    return dict(P=P, nside_x=A * a, nside_y=B * a, xi=float(T.xi * np.exp(y[1])), Mx=A * t, My=B * t)
+
+
+# candidates around the tuned choice, the same for every configuration so that
+# labels are comparable: cell-list scale (xi and the grid follow from the
+# estimates) x window support change
+CANDIDATES = [(sa, dp) for sa in (0.7, 1.0, 1.4, 2.0) for dp in (-2, 0, 2)]
+# a label must meet the tolerance with this margin
+LABEL_MARGIN = 0.5
+
+
+# ---- the selector ------------------------------------------------------------------
+class Selector:
+    """Learned choice of (cutoff, xi, M, P) with a sampled FP64 check."""
+
+    def __init__(self, path: str = MODEL_PATH, ctx=None):
+        import torch
+
+        z = np.load(path)
+        self.ctx = ctx or default_context()
+        self.nets = {}
+        for kind, name in ((KIND_SLP, "slp"), (KIND_DLP, "dlp")):
+            self.nets[kind] = {
+                "params": torch.tensor(z[f"{name}_params"].astype(np.float32), device="cuda"),
+                "xmean": z[f"{name}_xmean"], "xstd": z[f"{name}_xstd"], "yscale": z[f"{name}_yscale"]}
+
+    def predict(self, kind, feats):
+        net = self.nets[kind]
+        xn = (np.asarray(feats, np.float64) - net["xmean"]) / net["xstd"]
+        return mlp_forward(net["params"], xn[None, :])[0] * net["yscale"]
+
+    def choose(self, kind, cfg, tol, feats=None):
+        """Options for the driver (mixed form) and the tuned choice T."""
+        f1 = cfg["f1"].cpu().numpy() if hasattr(cfg["f1"], "cpu") else cfg["f1"]
+        f2 = cfg["f2"].cpu().numpy() if hasattr(cfg["f2"], "cpu") else cfg["f2"]
+        T = choose_params(kind, f1, f2, len(cfg["xt"]), cfg["Lx"], cfg["Ly"], tol=tol, form=FORM_MIXED)
+        if feats is None:
+            xs = cfg["xs"].cpu().numpy() if hasattr(cfg["xs"], "cpu") else cfg["xs"]
+            ys = cfg["ys"].cpu().numpy() if hasattr(cfg["ys"], "cpu") else cfg["ys"]
+            feats = features(xs, ys, len(cfg["xt"]), cfg["Lx"], cfg["Ly"], tol)
+        return params_from(self.predict(kind, feats), T), T
+
+    def evaluate(self, kind, cfg, tol, check=True, sample=64, seed=0, feats=None):
+        """Evaluate with the learned parameters; if the sampled FP64 check
+        misses the tolerance, evaluate again with the tuned analytic choice.
+        Returns (u1, u2, report)."""
+        import torch
+
+        opts, T = self.choose(kind, cfg, tol, feats)
+        t0 = time.perf_counter()
+        out, info = _run(kind, cfg, tol, self.ctx, form=FORM_MIXED, **opts)
+        torch.cuda.synchronize()
+        t_learned = time.perf_counter() - t0
+        rep = {"used": "learned", "params": opts, "t_learned_s": t_learned, "check_err": None, "t_check_s": 0.0}
+        if check:
+            t1 = time.perf_counter()
+            err = sampled_check(kind, cfg, tol, _u(out), self.ctx, sample=sample, seed=seed)
+            rep["t_check_s"] = time.perf_counter() - t1
+            rep["check_err"] = err
+            if not err <= tol:
+                t2 = time.perf_counter()
+                out, info = _run(kind, cfg, tol, self.ctx, form=FORM_MIXED)
+                torch.cuda.synchronize()
+                rep["t_fallback_s"] = time.perf_counter() - t2
+                rep["used"] = "fallback"
+        return out[0], out[1], rep
+
+
+def sampled_check(kind, cfg, tol, u, ctx, sample=64, seed=0):
+    """max |u - u_ref| / max |u_ref| on a random sample of targets, u_ref from
+    an FP64 evaluation (tuned parameters, FP64 k-space) at 1/100 of the
+    tolerance."""
+    import torch
+
+    n = len(cfg["xt"])
+    g = np.random.default_rng(seed)
+    idx = torch.tensor(np.sort(g.choice(n, size=min(n, sample), replace=False)), device=u.device)
+    sub = dict(cfg)
+    sub["xt"], sub["yt"] = cfg["xt"][idx], cfg["yt"][idx]
+    ref, _ = _run(kind, sub, min(max(tol * 1e-2, 1e-14), 1e-8), ctx, form=FORM_MIXED)
+    return _rel_err(u[idx], _u(ref))
+
+
+def reference(kind, cfg, ctx):
+    """Converged FP64 velocities (tuned parameters at tolerance 1e-14)."""
+    out, _ = _run(kind, cfg, 1e-14, ctx, form=FORM_MIXED)
+    return _u(out)
+
+
+# ---- data generation, training and evaluation (GPU) ------------------------------
+def random_config(rng, nmin=1e3, nmax=3e5):
+    """A configuration of the training distribution: N log-uniform, box aspect
+    p/4 (p = 4..16), uniform points or half uniform / half on ellipses,
+    targets = sources, zero-mean N(0,1) densities, tolerance log-uniform in
+    [1e-12, 1e-4]."""
+    N = int(round(np.exp(rng.uniform(np.log(nmin), np.log(nmax)))))
+    p = int(rng.integers(4, 17))
+    Lx, Ly = (p / 4.0, 1.0) if rng.random() < 0.5 else (1.0, p / 4.0)
+    clustered = rng.random() < 0.5
+    if clustered:
+        nu = N // 2
+        cap = max(1, int(30 * Lx * Ly))
+        n_ell = max(1, min((N - nu) // 256, cap))
+        X, Y, N1, N2, _ = wl.ellipse_field(rng, n_ell, max(16, (N - nu) // n_ell), Lx, Ly, 0.02, 0.06)
+        th = rng.random(nu) * 2 * np.pi
+        xs = np.concatenate([(rng.random(nu) - 0.5) * Lx, X])
+        ys = np.concatenate([(rng.random(nu) - 0.5) * Ly, Y])
+        n1 = np.concatenate([np.cos(th), N1])
+        n2 = np.concatenate([np.sin(th), N2])
+    else:
+        xs, ys = (rng.random(N) - 0.5) * Lx, (rng.random(N) - 0.5) * Ly
+        th = rng.random(N) * 2 * np.pi
+        n1, n2 = np.cos(th), np.sin(th)
+    n = len(xs)
+    f1, f2 = rng.standard_normal(n), rng.standard_normal(n)
+    tol = float(10 ** rng.uniform(-12, -4))
+    kind = int(rng.integers(0, 2))
+    return dict(xs=xs, ys=ys, xt=xs.copy(), yt=ys.copy(), n1=n1, n2=n2, f1=f1 - f1.mean(), f2=f2 - f2.mean(), Lx=Lx,
+                Ly=Ly, tol=tol, kind=kind, clustered=clustered)
+
+
+def _to_dev(cfg):
+    import torch
+
+    d = dict(cfg)
+    for k in ("xs", "ys", "xt", "yt", "n1", "n2", "f1", "f2"):
+        d[k] = torch.tensor(cfg[k], dtype=torch.float64, device="cuda")
+    return d
+
+
+def _timed(kind, cfg, tol, ctx, reps=2, **kw):
+    """Best GPU time (ms, library events) of `reps` evaluations."""
+    best, out, info = np.inf, None, None
+    for _ in range(reps):
+        out, info = _run(kind, cfg, tol, ctx, **kw)
+        best = min(best, info.ms_total)
+    return best, out, info
+
+
+CAND_FIELDS = ["P", "nside_x", "nside_y", "Mx", "My", "xi", "form", "t_ms", "err"]
+
+
+def _cand_row(prm, t, err):
+    return [prm.P, prm.nside_x, prm.nside_y, prm.Mx, prm.My, prm.xi, prm.form, t, err]
+
+
+def label_config(cfg, ctx, rng):
+    """Time and check the tuned choice and the candidates around it on one
+    configuration.  Returns a record with every candidate's absolute
+    parameters, GPU time (ms) and error against the converged evaluation."""
+    kind, tol = cfg["kind"], cfg["tol"]
+    d = _to_dev(cfg)
+    ref = reference(kind, d, ctx)
+    T = choose_params(kind, cfg["f1"], cfg["f2"], len(cfg["xt"]), cfg["Lx"], cfg["Ly"], tol=tol, form=FORM_MIXED)
+    t_T, out, info = _timed(kind, d, tol, ctx, form=FORM_MIXED)
+    rows = [_cand_row(info.params, t_T, _rel_err(_u(out), ref))]
+    for sa, dp in CANDIDATES:
+        a = max(1, int(round(T.nside_x / T.A * sa)))
+        P = int(np.clip(T.P + dp, 4, 24))
+        if sa == 1.0 and dp == 0:
+            continue  # T itself
+        try:
+            t, out, info = _timed(kind, d, tol, ctx, form=FORM_MIXED, P=P, nside_x=T.A * a, nside_y=T.B * a)
+        except FteError:
+            continue
+        rows.append(_cand_row(info.params, t, _rel_err(_u(out), ref)))
+    feats = features(cfg["xs"], cfg["ys"], len(cfg["xt"]), cfg["Lx"], cfg["Ly"], tol)
+    qsum = float(np.sum(cfg["f1"] ** 2 + cfg["f2"] ** 2))
+    return {"kind": kind, "tol": tol, "n": len(cfg["xs"]), "ntar": len(cfg["xt"]), "Lx": cfg["Lx"], "Ly": cfg["Ly"],
+            "qsum": qsum, "feats": feats, "cands": np.array(rows, dtype=np.float64)}
+
+
+def tuned_of(rec, **kw):
+    """The tuned choice T of a recorded configuration (host only)."""
+    n = int(rec["n"])
+    f1 = np.zeros(n)
+    f1[0] = np.sqrt(rec["qsum"])
+    return choose_params(int(rec["kind"]), f1, np.zeros(n), int(rec["ntar"]), float(rec["Lx"]), float(rec["Ly"]),
+                         tol=float(rec["tol"]), form=FORM_MIXED, **kw)
+
+
+def label_targets(rec):
+    """(targets, t_best, t_T) of a record: the fastest candidate meeting the
+    tolerance, relative to the current tuned choice; None if none met it."""
+    c = rec["cands"]
+    ok = c[:, 8] <= LABEL_MARGIN * rec["tol"]
+    if not ok.any():
+        return None
+    j = int(np.argmin(np.where(ok, c[:, 7], np.inf)))
+    T = tuned_of(rec)
+    y = np.array([np.log(c[j, 1] / T.nside_x), np.log(c[j, 5] / T.xi), np.log(c[j, 3] / T.Mx), (c[j, 0] - T.P) / 2])
+    return y, float(c[j, 7]), float(c[0, 7])
+
+
+def save_records(path, recs):
+    np.savez(path, feats=np.array([r["feats"] for r in recs]), kind=np.array([r["kind"] for r in recs]),
+             tol=np.array([r["tol"] for r in recs]), n=np.array([r["n"] for r in recs]),
+             ntar=np.array([r["ntar"] for r in recs]), Lx=np.array([r["Lx"] for r in recs]),
+             Ly=np.array([r["Ly"] for r in recs]), qsum=np.array([r["qsum"] for r in recs]),
+             ncand=np.array([len(r["cands"]) for r in recs]), cands=np.concatenate([r["cands"] for r in recs]))
+
+
+def load_records(path):
+    z = np.load(path)
+    recs, o = [], 0
+    for i in range(len(z["kind"])):
+        k = int(z["ncand"][i])
+        recs.append({"feats": z["feats"][i], "kind": int(z["kind"][i]), "tol": float(z["tol"][i]), "n": int(z["n"][i]),
+                     "ntar": int(z["ntar"][i]), "Lx": float(z["Lx"][i]), "Ly": float(z["Ly"][i]),
+                     "qsum": float(z["qsum"][i]), "cands": z["cands"][o:o + k]})
+        o += k
+    return recs
+
+
+def fit_models(recs, steps=4000, seed=5, log=None):
+    """Train both networks on recorded configurations."""
+    model = {}
+    for kind, name in ((KIND_SLP, "slp"), (KIND_DLP, "dlp")):
+        X, Y, W = [], [], []
+        for r in recs:
+            if r["kind"] != kind:
+                continue
+            lab = label_targets(r)
+            if lab is None:
+                continue
+            y, tb, tT = lab
+            X.append(r["feats"])
+            Y.append(y)
+            # weight each configuration by the share of time it can save
+            W.append(max(tT - tb, 0.0) / max(tT, 1e-9) + 0.25)
+        W = np.array(W) / np.mean(W)
+        res = train(np.array(X), np.array(Y), weights=W, steps=steps, seed=seed, log=log)
+        for k in ("params", "xmean", "xstd", "yscale"):
+            model[f"{name}_{k}"] = res[k]
+        model[f"{name}_val_loss"] = np.array(res["val_loss"])
+        model[f"{name}_samples"] = np.array(len(X))
+    return model
+
+
+def evaluate_heldout(sel, cfgs, ctx, log=None):
+    """Learned (with check and fallback) vs the tuned analytic choice vs the
+    drivers' analytic choice (FP64, P = 24) on held-out configurations."""
+    import torch
+
+    rows = []
+    for i, cfg in enumerate(cfgs):
+        kind, tol = cfg["kind"], cfg["tol"]
+        d = _to_dev(cfg)
+        ref = reference(kind, d, ctx)
+        t_an, out_an, _ = _timed(kind, d, tol, ctx, form=FORM_PLAIN)
+        t_T, out_T, _ = _timed(kind, d, tol, ctx, form=FORM_MIXED)
+        err_T = _rel_err(_u(out_T), ref)
+        ts = time.perf_counter()
+        feats = features(cfg["xs"], cfg["ys"], len(cfg["xt"]), cfg["Lx"], cfg["Ly"], tol)
+        opts, T = sel.choose(kind, d, tol, feats)
+        t_select = (time.perf_counter() - ts) * 1e3
+        try:
+            t_L, out_L, _ = _timed(kind, d, tol, ctx, form=FORM_MIXED, **opts)
+            err_L = _rel_err(_u(out_L), ref)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            chk = sampled_check(kind, d, tol, _u(out_L), ctx, seed=i)
+            t_chk = (time.perf_counter() - t0) * 1e3
+        except FteError:
+            t_L, err_L, chk, t_chk = np.inf, np.inf, np.inf, 0.0
+        fallback = not chk <= tol
+        t_sel = (t_L if np.isfinite(t_L) else 0.0) + (t_T if fallback else 0.0)
+        err_sel = err_T if fallback else err_L
+        rows.append({"kind": kind, "tol": tol, "n": len(cfg["xs"]), "t_analytic_ms": t_an,
+                     "err_analytic": _rel_err(_u(out_an), ref), "t_tuned_ms": t_T, "err_tuned": err_T,
+                     "t_learned_ms": t_L, "err_learned": err_L, "check_err": chk, "t_check_ms": t_chk,
+                     "t_select_ms": t_select,
+                     "fallback": fallback, "t_selected_ms": t_sel, "err_selected": err_sel})
+        if log and i % 50 == 0:
+            log(f"heldout {i}: {rows[-1]}")
+    return rows
+
+
+def summarize(rows):
+    r = {k: np.array([x[k] for x in rows], dtype=np.float64) for k in rows[0] if k not in ("fallback",)}
+    fb = np.array([x["fallback"] for x in rows])
+    tol = r["tol"]
+    return {
+        "configs": len(rows),
+        "total_ms": {"analytic_fp64": float(r["t_analytic_ms"].sum()), "tuned": float(r["t_tuned_ms"].sum()),
+                     "learned_with_fallback": float(r["t_selected_ms"].sum()),
+                     "learned_with_fallback_and_check": float(r["t_selected_ms"].sum() + r["t_check_ms"].sum())},
+        "meets_tol": {"analytic_fp64": float(np.mean(r["err_analytic"] <= tol)),
+                      "tuned": float(np.mean(r["err_tuned"] <= tol)),
+                      "learned_raw": float(np.mean(r["err_learned"] <= tol)),
+                      "learned_with_fallback": float(np.mean(r["err_selected"] <= tol))},
+        "host_select_ms": float(r["t_select_ms"].sum()),
+        "fallbacks": int(fb.sum()),
+        "median_speedup_vs_tuned": float(np.median(r["t_tuned_ms"] / np.maximum(r["t_selected_ms"], 1e-9))),
+        "median_speedup_vs_analytic": float(np.median(r["t_analytic_ms"] / np.maximum(r["t_selected_ms"], 1e-9))),
+    }
+
+
+def main(argv=None):
+    import argparse
+
+    import torch
+
+    ap = argparse.ArgumentParser(description="generate data, train and evaluate the parameter selector")
+    ap.add_argument("cmd", choices=["train"])
+    ap.add_argument("--configs", type=int, default=2000)
+    ap.add_argument("--heldout", type=int, default=500)
+    ap.add_argument("--nmax", type=float, default=3e5)
+    ap.add_argument("--steps", type=int, default=4000)
+    ap.add_argument("--out", default=".")
+    ap.add_argument("--seed", type=int, default=5)
+    ap.add_argument("--data", default=None, help="recorded configurations to train on (skips labelling)")
+    a = ap.parse_args(argv)
+    os.makedirs(a.out, exist_ok=True)
+    logf = open(os.path.join(a.out, "selector_log.txt"), "w")
+
+    def log(s):
+        logf.write(s + "\n")
+        logf.flush()
+
+    ctx = default_context()
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+    ctx.set_timing(True)
+    rng = np.random.default_rng(a.seed)
+    t0 = time.time()
+    if a.data:
+        recs = load_records(a.data)
+    else:
+        recs = []
+        for i in range(a.configs):
+            cfg = random_config(rng, nmax=a.nmax)
+            recs.append(label_config(cfg, ctx, rng))
+            if i % 100 == 0:
+                c = recs[-1]["cands"]
+                log(f"label {i} {time.time() - t0:.1f}s kind={recs[-1]['kind']} n={recs[-1]['n']} "
+                    f"tol={recs[-1]['tol']:.1e} tT={c[0, 7]:.2f} tmin={c[:, 7].min():.2f}")
+        save_records(os.path.join(a.out, "selector_data.npz"), recs)
+    t_label = time.time() - t0
+    model = fit_models(recs, steps=a.steps, seed=a.seed, log=log)
+    path = os.path.join(a.out, "selector_model.npz")
+    np.savez(path, **model)
+    sel = Selector(path, ctx)
+    hrng = np.random.default_rng(a.seed + 1000)
+    rows = evaluate_heldout(sel, [random_config(hrng, nmax=a.nmax) for _ in range(a.heldout)], ctx, log=log)
+    rep = {"train_configs": len(recs), "label_seconds": t_label, "n_range": [1e3, a.nmax],
+           "samples": {k: int(model[f"{k}_samples"]) for k in ("slp", "dlp")},
+           "val_loss": {k: float(model[f"{k}_val_loss"]) for k in ("slp", "dlp")},
+           "heldout": summarize(rows)}
+    json.dump(rep, open(os.path.join(a.out, "selector_report.json"), "w"), indent=1)
+    json.dump(rows, open(os.path.join(a.out, "selector_heldout.json"), "w"))
+    print(json.dumps(rep), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -95,6 +95,7 @@ typedef struct {
     const double* weights; /* optional quadrature weights, multiplied into f (length nsrc) */
     int form;              /* FTE_FORM_PLAIN or FTE_FORM_MIXED */
     int tune;              /* plans: 1 = time the k-space tile sizes on the plan's points at creation */
+    double slack;          /* FTE_FORM_MIXED: error-estimate slack of the tuned choice (0: 3) */
 } fte_options;
 
 /* Per-call diagnostics (optional output of the driver entries). */
@@ -195,6 +196,31 @@ int fte_batch_destroy(fte_batch* batch);
  * FTE_DEVICE_POINTERS, device arrays; host copies synchronise) */
 int fte_batch_set_density(fte_batch* batch, int i, const double* f1s, const double* f2s, unsigned flags);
 int fte_batch_get_velocity(fte_batch* batch, int i, double* u1s, double* u2s, unsigned flags);
+
+/* ---- learned parameter selector: the network ------------------------------ */
+/* No counterpart in the reference.  An FP32 multilayer perceptron
+ * 8 -> 64 -> 64 -> 4 (tanh hidden units) that maps features of a
+ * configuration to corrections of the tuned parameter choice (cell list,
+ * xi, grid, window support).  Parameters are one FP32 vector of
+ * FTE_MLP_PARAMS values: W1[64x8], b1[64], W2[64x64], b2[64], W3[4x64], b3[4]
+ * (row-major, y = W x + b).  All pointers are device pointers; `stream` is a
+ * cudaStream_t (NULL: default stream); calls are asynchronous. */
+#define FTE_MLP_IN 8
+#define FTE_MLP_HIDDEN 64
+#define FTE_MLP_OUT 4
+#define FTE_MLP_PARAMS (FTE_MLP_HIDDEN * FTE_MLP_IN + FTE_MLP_HIDDEN + FTE_MLP_HIDDEN * FTE_MLP_HIDDEN + \
+                        FTE_MLP_HIDDEN + FTE_MLP_OUT * FTE_MLP_HIDDEN + FTE_MLP_OUT)
+int fte_mlp_param_count(void);
+/* scratch (floats) of fte_mlp_loss_grad for n samples */
+size_t fte_mlp_scratch_floats(int n);
+/* Y[n x 4] = network(X[n x 8]) */
+int fte_mlp_forward(const float* params, const float* X, int n, float* Y, void* stream);
+/* loss = (1/n) sum_i w_i |y_i - t_i|^2 (w null: 1) and its gradient (FTE_MLP_PARAMS floats) */
+int fte_mlp_loss_grad(const float* params, const float* X, const float* T, const float* weights, int n,
+                      float* scratch, float* grad, float* loss, void* stream);
+/* one Adam step (step = 1, 2, ...; m, v: moment vectors, zero at step 1) */
+int fte_mlp_adam(float* params, const float* grad, float* m, float* v, int step, float lr, float beta1,
+                 float beta2, float eps, void* stream);
 
 /* ---- allocation-free variant --------------------------------------------- */
 /* No counterpart in the reference.  The Stokeslet k-space sum of
