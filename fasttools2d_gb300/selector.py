@@ -19,7 +19,8 @@ module learns corrections to the tuned analytic choice of the mixed form
   the tolerance (times and errors measured on the GPU);
 * safety: ``Selector.evaluate`` checks the learned result on a random sample
   of targets against an FP64 evaluation at 1/100 of the tolerance and falls
-  back to the tuned analytic choice when the check misses the tolerance.
+  back to the drivers' analytic choice (FP64) when the sampled error exceeds
+  half the tolerance.
 
 Run ``python -m fasttools2d_gb300.selector train --out DIR`` on a GPU to
 generate data, train both networks, evaluate on held-out configurations and
@@ -218,6 +219,9 @@ def params_from(y, T):
 CANDIDATES = [(sa, dp) for sa in (0.7, 1.0, 1.4, 2.0) for dp in (-2, 0, 2)]
 # a label must meet the tolerance with this margin
 LABEL_MARGIN = 0.5
+# the sampled check sees 64 targets, whose largest error is below the largest
+# over all targets: it passes only below this fraction of the tolerance
+CHECK_MARGIN = 0.7
 
 
 # ---- the selector ------------------------------------------------------------------
@@ -253,8 +257,8 @@ class Selector:
 
     def evaluate(self, kind, cfg, tol, check=True, sample=64, seed=0, feats=None):
         """Evaluate with the learned parameters; if the sampled FP64 check
-        misses the tolerance, evaluate again with the tuned analytic choice.
-        Returns (u1, u2, report)."""
+        misses half the tolerance, evaluate again with the drivers' analytic
+        choice in FP64.  Returns (u1, u2, report)."""
         import torch
 
         opts, T = self.choose(kind, cfg, tol, feats)
@@ -268,9 +272,9 @@ class Selector:
             err = sampled_check(kind, cfg, tol, _u(out), self.ctx, sample=sample, seed=seed)
             rep["t_check_s"] = time.perf_counter() - t1
             rep["check_err"] = err
-            if not err <= tol:
+            if not err <= CHECK_MARGIN * tol:
                 t2 = time.perf_counter()
-                out, info = _run(kind, cfg, tol, self.ctx, form=FORM_MIXED)
+                out, info = _run(kind, cfg, tol, self.ctx, form=FORM_PLAIN)
                 torch.cuda.synchronize()
                 rep["t_fallback_s"] = time.perf_counter() - t2
                 rep["used"] = "fallback"
@@ -278,9 +282,9 @@ class Selector:
 
 
 def sampled_check(kind, cfg, tol, u, ctx, sample=64, seed=0):
-    """max |u - u_ref| / max |u_ref| on a random sample of targets, u_ref from
-    an FP64 evaluation (tuned parameters, FP64 k-space) at 1/100 of the
-    tolerance."""
+    """max over a random sample of targets of |u - u_ref|, relative to max |u|
+    over all targets (the scale the tolerance refers to); u_ref from an FP64
+    evaluation (tuned parameters, FP64 k-space) at 1/100 of the tolerance."""
     import torch
 
     n = len(cfg["xt"])
@@ -289,7 +293,7 @@ def sampled_check(kind, cfg, tol, u, ctx, sample=64, seed=0):
     sub = dict(cfg)
     sub["xt"], sub["yt"] = cfg["xt"][idx], cfg["yt"][idx]
     ref, _ = _run(kind, sub, min(max(tol * 1e-2, 1e-14), 1e-8), ctx, form=FORM_MIXED)
-    return _rel_err(u[idx], _u(ref))
+    return float((u[idx] - _u(ref)).abs().max() / u.abs().max())
 
 
 def reference(kind, cfg, ctx):
@@ -438,7 +442,9 @@ def fit_models(recs, steps=4000, seed=5, log=None):
             X.append(r["feats"])
             Y.append(y)
             # weight each configuration by the share of time it can save
-            W.append(max(tT - tb, 0.0) / max(tT, 1e-9) + 0.25)
+            # weight by the absolute time at stake, so that large problems,
+            # which dominate a workload's total, are fitted best
+            W.append(tT * (max(tT - tb, 0.0) / max(tT, 1e-9) + 0.1))
         W = np.array(W) / np.mean(W)
         res = train(np.array(X), np.array(Y), weights=W, steps=steps, seed=seed, log=log)
         for k in ("params", "xmean", "xstd", "yscale"):
@@ -449,8 +455,9 @@ def fit_models(recs, steps=4000, seed=5, log=None):
 
 
 def evaluate_heldout(sel, cfgs, ctx, log=None):
-    """Learned (with check and fallback) vs the tuned analytic choice vs the
-    drivers' analytic choice (FP64, P = 24) on held-out configurations."""
+    """Learned (with check and fallback to the drivers' analytic choice) vs
+    the tuned analytic choice vs the drivers' analytic choice (FP64, P = 24)
+    on held-out configurations."""
     import torch
 
     rows = []
@@ -459,6 +466,7 @@ def evaluate_heldout(sel, cfgs, ctx, log=None):
         d = _to_dev(cfg)
         ref = reference(kind, d, ctx)
         t_an, out_an, _ = _timed(kind, d, tol, ctx, form=FORM_PLAIN)
+        err_an = _rel_err(_u(out_an), ref)
         t_T, out_T, _ = _timed(kind, d, tol, ctx, form=FORM_MIXED)
         err_T = _rel_err(_u(out_T), ref)
         ts = time.perf_counter()
@@ -474,11 +482,11 @@ def evaluate_heldout(sel, cfgs, ctx, log=None):
             t_chk = (time.perf_counter() - t0) * 1e3
         except FteError:
             t_L, err_L, chk, t_chk = np.inf, np.inf, np.inf, 0.0
-        fallback = not chk <= tol
-        t_sel = (t_L if np.isfinite(t_L) else 0.0) + (t_T if fallback else 0.0)
-        err_sel = err_T if fallback else err_L
+        fallback = not chk <= CHECK_MARGIN * tol
+        t_sel = (t_L if np.isfinite(t_L) else 0.0) + (t_an if fallback else 0.0)
+        err_sel = err_an if fallback else err_L
         rows.append({"kind": kind, "tol": tol, "n": len(cfg["xs"]), "t_analytic_ms": t_an,
-                     "err_analytic": _rel_err(_u(out_an), ref), "t_tuned_ms": t_T, "err_tuned": err_T,
+                     "err_analytic": err_an, "t_tuned_ms": t_T, "err_tuned": err_T,
                      "t_learned_ms": t_L, "err_learned": err_L, "check_err": chk, "t_check_ms": t_chk,
                      "t_select_ms": t_select,
                      "fallback": fallback, "t_selected_ms": t_sel, "err_selected": err_sel})

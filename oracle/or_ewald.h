@@ -110,6 +110,23 @@ void or_dlp_kspace_ds(const double* xsrc, const double* ysrc, int Nsrc, const do
                       int Ntar, const double* n1, const double* n2, const double* f1, const double* f2, double Lx,
                       double Ly, double xi, int kinf, double* u);
 
+/* Other quantities (or_quant.c): pressure, pressure gradient, velocity
+ * gradient, stress, vorticity.  Outputs have or_q_ncomp(q) components per
+ * target (interleaved, caller's target order): pressure 1; pressure gradient
+ * 2; velocity gradient and stress 4, in the gateways' order; vorticity 1.
+ * n is required for the DLP and ignored for the SLP. */
+#define OR_Q_PRESSURE 1
+#define OR_Q_PRESSURE_GRAD 2
+#define OR_Q_GRADIENT 3
+#define OR_Q_STRESS 4
+#define OR_Q_VORTICITY 5
+int or_q_ncomp(int q);
+int or_q_real(int kind, int q, const double* psrc, int Nsrc, const double* ptar, int Ntar, const double* f,
+              const double* n, double xi, int nside_x, int nside_y, double Lx, double Ly, double* out);
+int or_q_kspace(int kind, int q, const double* psrc, int Nsrc, const double* ptar, int Ntar, const double* f,
+                const double* n, double xi, double eta, int Mx, int My, double Lx, double Ly, double w, int P,
+                double* out);
+
 /* Truth oracle: a converged Ewald sum with its own xi_o, real-space cutoff
  * rcut (periodic images, cell binned) and Fourier box |jk| <= kinf.  Includes
  * the SLP self term and, for the DLP, the zero mode.  Points must already be
