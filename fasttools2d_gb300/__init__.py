@@ -39,6 +39,13 @@ FORM_PLAIN = 0
 FORM_MIXED = 1
 KIND_SLP = 0
 KIND_DLP = 1
+Q_VELOCITY = 0
+Q_PRESSURE = 1
+Q_PRESSURE_GRAD = 2
+Q_GRADIENT = 3
+Q_STRESS = 4
+Q_VORTICITY = 5
+Q_NCOMP = {Q_VELOCITY: 2, Q_PRESSURE: 1, Q_PRESSURE_GRAD: 2, Q_GRADIENT: 4, Q_STRESS: 4, Q_VORTICITY: 1}
 
 
 class FteError(RuntimeError):
@@ -115,6 +122,9 @@ SIGNATURES = {
     "fte_batch_destroy": (_i, [_vp]),
     "fte_batch_set_density": (_i, [_vp, _i, _vp, _vp, _u]),
     "fte_batch_get_velocity": (_i, [_vp, _i, _vp, _vp, _u]),
+    "fte_q_ncomp": (_i, [_i]),
+    "fte_q_real": (_i, [_vp, _i, _i, _vp, _i64, _vp, _i64, _vp, _vp, _d, _i, _i, _d, _d, _vp, _u]),
+    "fte_q_kspace": (_i, [_vp, _i, _i, _vp, _i64, _vp, _i64, _vp, _vp, _d, _d, _i, _i, _d, _d, _d, _i, _vp, _u]),
     "fte_mlp_param_count": (_i, []),
     "fte_mlp_scratch_floats": (C.c_size_t, [_i]),
     "fte_mlp_forward": (_i, [_vp, _vp, _i, _vp, _vp]),
@@ -523,3 +533,78 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+# ---- other quantities: gateway level ------------------------------------------------
+
+def q_real(kind, q, psrc, ptar, f, n, xi, nside_x, nside_y, Lx, Ly, ctx: Context | None = None):
+    """Real-space sum of quantity q (``Q_PRESSURE`` .. ``Q_VORTICITY``): (Ntar, ncomp)."""
+    ctx = ctx or default_context()
+    A = _Args()
+    ps, ns = A.arr(psrc, 2)
+    pt, nt = A.arr(ptar, 2)
+    pf, nf = A.arr(f, 2)
+    pn, nn = A.arr(n, 2) if kind == KIND_DLP else (None, ns)
+    if nf != ns or nn != ns:
+        raise ValueError("psrc, f (and n) must be the same size.")
+    out, po = A.out((nt, Q_NCOMP.get(q, 1)))  # an unknown q is rejected by the library
+    _check(lib().fte_q_real(ctx.h, int(kind), int(q), ps, ns, pt, nt, pf, pn, float(xi), int(nside_x), int(nside_y),
+                            float(Lx), float(Ly), po, A.flags))
+    return out
+
+
+def q_kspace(kind, q, psrc, ptar, f, n, xi, eta, Mx, My, Lx, Ly, w, P, ctx: Context | None = None):
+    """k-space sum of quantity q: (Ntar, ncomp)."""
+    ctx = ctx or default_context()
+    A = _Args()
+    ps, ns = A.arr(psrc, 2)
+    pt, nt = A.arr(ptar, 2)
+    pf, nf = A.arr(f, 2)
+    pn, nn = A.arr(n, 2) if kind == KIND_DLP else (None, ns)
+    if nf != ns or nn != ns:
+        raise ValueError("psrc, f (and n) must be the same size.")
+    out, po = A.out((nt, Q_NCOMP.get(q, 1)))  # an unknown q is rejected by the library
+    _check(lib().fte_q_kspace(ctx.h, int(kind), int(q), ps, ns, pt, nt, pf, pn, float(xi), float(eta), int(Mx),
+                              int(My), float(Lx), float(Ly), float(w), int(P), po, A.flags))
+    return out
+
+
+def _make_q_gateways():
+    """mex_stokes_{slp,dlp}_<q>_{real,kspace} with each gateway's own argument
+    order (PeriodicEwald/src/mex/Stokes{SLP,DLP}/mex_stokes_*_{real,kspace}.cpp):
+    real (psrc, ptar, f, [n,] xi, nside_x, nside_y, Lx, Ly); k-space either
+    (psrc, ptar, xi, eta, f, [n,] Mx, My, Lx, Ly, w, P) or, for the pressure, the
+    pressure gradient and the stresslet vorticity, (psrc, ptar, f, [n,] xi, eta,
+    Mx, My, Lx, Ly, w, P)."""
+    names = {Q_PRESSURE: "pressure", Q_PRESSURE_GRAD: "pressure_grad", Q_GRADIENT: "gradient", Q_STRESS: "stress",
+             Q_VORTICITY: "vorticity"}
+    f_first = {(KIND_SLP, Q_PRESSURE), (KIND_SLP, Q_PRESSURE_GRAD), (KIND_DLP, Q_PRESSURE),
+               (KIND_DLP, Q_PRESSURE_GRAD), (KIND_DLP, Q_VORTICITY)}
+    g = globals()
+    for kind, kn in ((KIND_SLP, "slp"), (KIND_DLP, "dlp")):
+        for q, qn in names.items():
+            if kind == KIND_SLP:
+                def real(psrc, ptar, f, xi, nside_x, nside_y, Lx, Ly, ctx=None, _q=q):
+                    return q_real(KIND_SLP, _q, psrc, ptar, f, None, xi, nside_x, nside_y, Lx, Ly, ctx)
+                if (kind, q) in f_first:
+                    def ksp(psrc, ptar, f, xi, eta, Mx, My, Lx, Ly, w, P, ctx=None, _q=q):
+                        return q_kspace(KIND_SLP, _q, psrc, ptar, f, None, xi, eta, Mx, My, Lx, Ly, w, P, ctx)
+                else:
+                    def ksp(psrc, ptar, xi, eta, f, Mx, My, Lx, Ly, w, P, ctx=None, _q=q):
+                        return q_kspace(KIND_SLP, _q, psrc, ptar, f, None, xi, eta, Mx, My, Lx, Ly, w, P, ctx)
+            else:
+                def real(psrc, ptar, f, n, xi, nside_x, nside_y, Lx, Ly, ctx=None, _q=q):
+                    return q_real(KIND_DLP, _q, psrc, ptar, f, n, xi, nside_x, nside_y, Lx, Ly, ctx)
+                if (kind, q) in f_first:
+                    def ksp(psrc, ptar, f, n, xi, eta, Mx, My, Lx, Ly, w, P, ctx=None, _q=q):
+                        return q_kspace(KIND_DLP, _q, psrc, ptar, f, n, xi, eta, Mx, My, Lx, Ly, w, P, ctx)
+                else:
+                    def ksp(psrc, ptar, xi, eta, f, n, Mx, My, Lx, Ly, w, P, ctx=None, _q=q):
+                        return q_kspace(KIND_DLP, _q, psrc, ptar, f, n, xi, eta, Mx, My, Lx, Ly, w, P, ctx)
+            real.__name__ = f"mex_stokes_{kn}_{qn}_real"
+            ksp.__name__ = f"mex_stokes_{kn}_{qn}_kspace"
+            g[real.__name__] = real
+            g[ksp.__name__] = ksp
+
+
+_make_q_gateways()

@@ -1104,6 +1104,128 @@ static int kspace_entry(fte_context* c, int kind, const double* psrc, int64_t ns
     return FTE_OK;
 }
 
+// ---------------------------------------------------------------------------
+// other quantities, gateway level
+// ---------------------------------------------------------------------------
+extern "C" int fte_q_ncomp(int q) {
+    switch (q) {
+        case FTE_Q_VELOCITY: return 2;
+        case FTE_Q_PRESSURE: return 1;
+        case FTE_Q_PRESSURE_GRAD: return 2;
+        case FTE_Q_GRADIENT: return 4;
+        case FTE_Q_STRESS: return 4;
+        case FTE_Q_VORTICITY: return 1;
+        default: return 0;
+    }
+}
+
+static int check_q(int kind, int q) {
+    if (kind != FTE_KIND_SLP && kind != FTE_KIND_DLP) {
+        fte_set_error("unknown kind %d", kind);
+        return FTE_ERR_INVALID;
+    }
+    if (q < FTE_Q_PRESSURE || q > FTE_Q_VORTICITY) {
+        fte_set_error("quantity %d is not one of FTE_Q_PRESSURE .. FTE_Q_VORTICITY", q);
+        return FTE_ERR_INVALID;
+    }
+    return FTE_OK;
+}
+
+extern "C" int fte_q_real(fte_context* c, int kind, int q, const double* psrc, int64_t nsrc, const double* ptar,
+                          int64_t ntar, const double* f, const double* n, double xi, int nsx, int nsy, double Lx,
+                          double Ly, double* out, unsigned flags) {
+    if (!c) {
+        fte_set_error("null context");
+        return FTE_ERR_INVALID;
+    }
+    FTE_TRY(check_q(kind, q));
+    FTE_TRY(check_counts(nsrc, ntar));
+    FTE_TRY(check_box(Lx, Ly));
+    FTE_TRY(check_real_params(xi, nsx, nsy));
+    if ((nsrc > 0 && (!psrc || !f || (kind == FTE_KIND_DLP && !n))) || (ntar > 0 && (!ptar || !out))) {
+        fte_set_error("null array argument");
+        return FTE_ERR_INVALID;
+    }
+    FTE_CUDA_TRY(cudaSetDevice(c->device));
+    const bool host = !(flags & FTE_DEVICE_POINTERS);
+    const int nc = fte_q_ncomp(q);
+    size_t need = fte_cells_ws(nsrc, ntar, nsx * nsy) + ws_bytes((size_t)nc * (ntar + 1), 8);
+    if (host) need += ws_bytes(2 * (nsrc + 1), 8) * 3 + ws_bytes(2 * (ntar + 1), 8);
+    FTE_TRY(fte_ws_reserve(c, need));
+    WsCarver wc{c->ws, 0, c->ws_size};
+    Stager st{c, &wc, host};
+    const double *dps, *dpt, *df, *dn;
+    FTE_TRY(st.put(psrc, 2 * (size_t)nsrc, &dps));
+    FTE_TRY(st.put(ptar, 2 * (size_t)ntar, &dpt));
+    FTE_TRY(st.put(f, 2 * (size_t)nsrc, &df));
+    FTE_TRY(st.put(kind == FTE_KIND_DLP ? n : nullptr, 2 * (size_t)nsrc, &dn));
+    double* dout = host ? wc.take<double>((size_t)nc * (ntar + 1)) : out;
+    FTE_WS_CHECK(wc);
+    if (ntar > 0) {
+        CellList cl;
+        FTE_TRY(fte_cells_build(c, wc, kind, dps, nsrc, dpt, ntar, df, dn, nullptr, nsx, nsy, Lx, Ly, &cl));
+        FTE_TRY(fte_q_near_launch(c, kind, q, cl, df, dn, xi, Lx, Ly, dout));
+        FTE_TRY(finish_output(c, host, out, dout, (size_t)nc * ntar));
+    }
+    FTE_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return FTE_OK;
+}
+
+extern "C" int fte_q_kspace(fte_context* c, int kind, int q, const double* psrc, int64_t nsrc, const double* ptar,
+                            int64_t ntar, const double* f, const double* n, double xi, double eta, int Mx, int My,
+                            double Lx, double Ly, double w, int P, double* out, unsigned flags) {
+    if (!c) {
+        fte_set_error("null context");
+        return FTE_ERR_INVALID;
+    }
+    FTE_TRY(check_q(kind, q));
+    FTE_TRY(check_counts(nsrc, ntar));
+    FTE_TRY(check_box(Lx, Ly));
+    FTE_TRY(check_kspace_params(xi, eta, Mx, My, Lx, Ly, w, P));
+    if ((nsrc > 0 && (!psrc || !f || (kind == FTE_KIND_DLP && !n))) || (ntar > 0 && (!ptar || !out))) {
+        fte_set_error("null array argument");
+        return FTE_ERR_INVALID;
+    }
+    FTE_CUDA_TRY(cudaSetDevice(c->device));
+    const bool host = !(flags & FTE_DEVICE_POINTERS);
+    const int nc = fte_q_ncomp(q);
+    size_t need = fte_q_kspace_ws(Mx, My, nsrc, ntar) + ws_bytes((size_t)nc * (ntar + 1), 8);
+    if (host) need += ws_bytes(2 * (nsrc + 1), 8) * 3 + ws_bytes(2 * (ntar + 1), 8);
+    FTE_TRY(fte_ws_reserve(c, need));
+    WsCarver wc{c->ws, 0, c->ws_size};
+    Stager st{c, &wc, host};
+    const double *dps, *dpt, *df, *dn;
+    FTE_TRY(st.put(psrc, 2 * (size_t)nsrc, &dps));
+    FTE_TRY(st.put(ptar, 2 * (size_t)ntar, &dpt));
+    FTE_TRY(st.put(f, 2 * (size_t)nsrc, &df));
+    FTE_TRY(st.put(kind == FTE_KIND_DLP ? n : nullptr, 2 * (size_t)nsrc, &dn));
+    double* dout = host ? wc.take<double>((size_t)nc * (ntar + 1)) : out;
+    FTE_WS_CHECK(wc);
+    KspaceArgs a;
+    a.kind = kind;
+    a.form = FTE_FORM_PLAIN;
+    a.nsrc = nsrc;
+    a.ntar = ntar;
+    a.psrc = dps;
+    a.ptar = dpt;
+    a.f = df;
+    a.nrm = dn;
+    a.wts = nullptr;
+    a.xi = xi;
+    a.eta = eta;
+    a.w = w;
+    a.Lx = Lx;
+    a.Ly = Ly;
+    a.Mx = Mx;
+    a.My = My;
+    a.P = P;
+    a.uk = nullptr;
+    FTE_TRY(fte_q_kspace_run(c, wc, q, a, dout));
+    FTE_TRY(finish_output(c, host, out, dout, (size_t)nc * ntar));
+    FTE_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return FTE_OK;
+}
+
 extern "C" int fte_slp_kspace(fte_context* c, const double* psrc, int64_t nsrc, const double* ptar, int64_t ntar,
                               double xi, double eta, const double* f, int Mx, int My, double Lx, double Ly, double w,
                               int P, double* uk, unsigned flags) {

@@ -294,3 +294,11 @@ int fte_kspace_run(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, fte_info
 // scratch for one candidate's tile bins, fte_tiles_ws(max(nsrc, ntar), tiles
 // of 8 nodes))
 int fte_kspace_tune(fte_context* ctx, void* grid, WsCarver bins, KspaceArgs& a, float* ms_spread, float* ms_gather);
+
+// other quantities (quant.cu, kspace.cu): real-space sums from a cell list
+// (f, nrm: input order, interleaved) and k-space sums; out holds
+// fte_q_ncomp(q) values per target
+int fte_q_near_launch(fte_context* ctx, int kind, int q, const CellList& cl, const double* f, const double* nrm,
+                      double xi, double Lx, double Ly, double* out);
+size_t fte_q_kspace_ws(int Mx, int My, int64_t nsrc, int64_t ntar);
+int fte_q_kspace_run(fte_context* ctx, WsCarver& wc, int q, const KspaceArgs& a, double* out);

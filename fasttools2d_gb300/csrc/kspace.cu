@@ -29,6 +29,7 @@
 
 #include "fft.cuh"
 #include "fte_internal.cuh"
+#include "quant_filters.cuh"
 
 namespace {
 
@@ -1531,6 +1532,212 @@ int fte_kspace_run(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, fte_info
     }
     FTE_TRY(fte_record(ctx, 5));
     (void)info;
+    return FTE_OK;
+}
+
+// ===========================================================================
+// k-space sums of the other quantities (FP64): the velocity pipeline's spread,
+// transforms and gather around the quantity's filter.  The filter stores the
+// Hermitian part of the reference's filtered spectrum, (G(k) + conj G(-k)) / 2
+// with G(-k) evaluated at the wave numbers the reference assigns to the index
+// of -k (Nyquist rows and columns keep +k), which is what real(ifft2) of the
+// reference's full spectrum equals.
+// ===========================================================================
+namespace {
+template <int KIND, int Q>
+__global__ void k_filter_q(double2* __restrict__ Hh, int Mx, int My, double Lx, double Ly, double xi, double eta) {
+    constexpr int NG = KIND == FTE_KIND_SLP ? 2 : 4;
+    constexpr int NO = fte_q_nout(Q);
+    const int Kh = My / 2 + 1;
+    const size_t GS = (size_t)Mx * Kh;
+    const double tpx = 2.0 * FTE_PI / Lx, tpy = 2.0 * FTE_PI / Ly;
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < GS; idx += (size_t)gridDim.x * blockDim.x) {
+        const int j = (int)(idx / Kh), k = (int)(idx % Kh);
+        double2 in[NG], out[NO], out2[NO];
+#pragma unroll
+        for (int g = 0; g < NG; g++) in[g] = Hh[g * GS + idx];
+        if (j == 0 && k == 0) {
+#pragma unroll
+            for (int o = 0; o < NO; o++) out[o] = make_double2(0.0, 0.0);
+        } else {
+            const double k1 = j <= Mx / 2 ? tpx * j : tpx * (j - Mx);
+            const double k2 = tpy * k;
+            fte_q_apply<KIND, Q>(k1, k2, xi, eta, in, out);
+            const bool nyq_x = 2 * j == Mx, nyq_y = 2 * k == My;
+            double2 cin[NG];
+#pragma unroll
+            for (int g = 0; g < NG; g++) cin[g] = make_double2(in[g].x, -in[g].y);
+            fte_q_apply<KIND, Q>(nyq_x ? k1 : -k1, nyq_y ? k2 : -k2, xi, eta, cin, out2);
+#pragma unroll
+            for (int o = 0; o < NO; o++)
+                out[o] = make_double2(0.5 * (out[o].x + out2[o].x), 0.5 * (out[o].y - out2[o].y));
+        }
+#pragma unroll
+        for (int o = 0; o < NO; o++) Hh[o * GS + idx] = out[o];
+    }
+}
+
+// out[t * no + c] from gathered component pairs
+__global__ void k_q_pack(const double2* __restrict__ a, const double2* __restrict__ b, int64_t n, int no,
+                         double* __restrict__ out) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+        const double2 u = a[t];
+        if (no == 1) {
+            out[t] = u.x;
+        } else {
+            const double2 v = b[t];
+            out[4 * t] = u.x;
+            out[4 * t + 1] = u.y;
+            out[4 * t + 2] = v.x;
+            out[4 * t + 3] = v.y;
+        }
+    }
+}
+
+template <int KIND>
+int q_filter_launch(fte_context* ctx, int q, double2* Hh, const KspaceArgs& a) {
+    int fb = (int)(((size_t)a.Mx * (a.My / 2 + 1) + 255) / 256);
+    if (fb > ctx->num_sms * 32) fb = ctx->num_sms * 32;
+    switch (q) {
+        case FTE_Q_PRESSURE:
+            FTE_LAUNCH(ctx, (k_filter_q<KIND, FTE_Q_PRESSURE>), fb, 256, 0, Hh, a.Mx, a.My, a.Lx, a.Ly, a.xi, a.eta);
+            return FTE_OK;
+        case FTE_Q_PRESSURE_GRAD:
+            FTE_LAUNCH(ctx, (k_filter_q<KIND, FTE_Q_PRESSURE_GRAD>), fb, 256, 0, Hh, a.Mx, a.My, a.Lx, a.Ly, a.xi,
+                       a.eta);
+            return FTE_OK;
+        case FTE_Q_GRADIENT:
+            FTE_LAUNCH(ctx, (k_filter_q<KIND, FTE_Q_GRADIENT>), fb, 256, 0, Hh, a.Mx, a.My, a.Lx, a.Ly, a.xi, a.eta);
+            return FTE_OK;
+        case FTE_Q_STRESS:
+            FTE_LAUNCH(ctx, (k_filter_q<KIND, FTE_Q_STRESS>), fb, 256, 0, Hh, a.Mx, a.My, a.Lx, a.Ly, a.xi, a.eta);
+            return FTE_OK;
+        case FTE_Q_VORTICITY:
+            FTE_LAUNCH(ctx, (k_filter_q<KIND, FTE_Q_VORTICITY>), fb, 256, 0, Hh, a.Mx, a.My, a.Lx, a.Ly, a.xi, a.eta);
+            return FTE_OK;
+        default: break;
+    }
+    fte_set_error("unknown quantity %d", q);
+    return FTE_ERR_INVALID;
+}
+}  // namespace
+
+size_t fte_q_kspace_ws(int Mx, int My, int64_t nsrc, int64_t ntar) {
+    // four grids cover every kind's inputs and every quantity's outputs
+    return fte_kspace_ws(FTE_KIND_DLP, FTE_FORM_PLAIN, Mx, My, nsrc, ntar) + 2 * ws_bytes((size_t)ntar + 1, 16) + 4096;
+}
+
+int fte_q_kspace_run(fte_context* ctx, WsCarver& wc, int q, const KspaceArgs& a, double* out) {
+    const int ng = a.kind == FTE_KIND_SLP ? 2 : 4;
+    const int no = fte_q_nout(q);
+    const int nh = ng > no ? ng : no;  // grids held at once
+    const int Mx = a.Mx, My = a.My;
+    const size_t G = (size_t)Mx * My;
+    const int Kh = My / 2 + 1;
+    double* H = wc.take<double>(4 * G);
+    double2* Hh = wc.take<double2>(4 * (size_t)Mx * Kh);
+    double2* ga = wc.take<double2>((size_t)a.ntar + 1);
+    double2* gb = wc.take<double2>((size_t)a.ntar + 1);
+    FTE_WS_CHECK(wc);
+    const WinParams wp = win_params(a);
+    const bool long_y = !fte_fft_fits_block(My, sizeof(double2));
+    const bool long_x = !fte_fft_fits_block(Mx, sizeof(double2));
+    FftDev py{}, px{};
+    LongFft ly, lx;
+    if (long_y)
+        FTE_TRY(fte_get_long_plan(ctx, My, &ly));
+    else
+        FTE_TRY(fte_get_plan(ctx, My, &py));
+    if (long_x)
+        FTE_TRY(fte_get_long_plan(ctx, Mx, &lx));
+    else
+        FTE_TRY(fte_get_plan(ctx, Mx, &px));
+    const size_t sm_y = 2 * (size_t)py.m * sizeof(double2), sm_x = 2 * (size_t)px.m * sizeof(double2);
+    if (sm_y > (size_t)ctx->max_smem_optin || sm_x > (size_t)ctx->max_smem_optin) {
+        fte_set_error("grid %d x %d beyond this device's shared memory", Mx, My);
+        return FTE_ERR_UNSUPPORTED;
+    }
+    double2* S = long_y ? wc.take<double2>((size_t)nh * (Mx / 2) * My) : nullptr;
+    const size_t lsy = long_y ? fte_long_scratch(My, (long long)nh * (Mx / 2)) : 0;
+    const size_t lsx = long_x ? fte_long_scratch(Mx, (long long)nh * Kh) : 0;
+    double2* LS = (lsy || lsx) ? wc.take<double2>(lsy > lsx ? lsy : lsx) : nullptr;
+    FTE_WS_CHECK(wc);
+    const LineMap rows{(long long)My, 0, 1, 1};
+    const LineMap cols{(long long)Mx * Kh, 1, (long long)Kh, Kh};
+
+    int ts_s = 0, ts_g = 0;
+    FTE_TRY(resolve_tiles(ctx, a, &ts_s, &ts_g));
+    if (!ts_s || !ts_g) {
+        fte_set_error("window support P=%d too wide for the spread/gather tiles", a.P);
+        return FTE_ERR_UNSUPPORTED;
+    }
+    FTE_CUDA_TRY(cudaMemsetAsync(H, 0, sizeof(double) * ng * G, ctx->stream));
+    if (a.nsrc > 0) {
+        TileBins tb;
+        WsCarver w2 = wc;
+        FTE_TRY(fte_tiles_build(ctx, w2, a.psrc, a.nsrc, a.Lx, a.Ly, wp.h, ts_s, (Mx + ts_s - 1) / ts_s,
+                                (My + ts_s - 1) / ts_s, &tb));
+        FTE_WS_CHECK(w2);
+        FTE_TRY(launch_spread_tiled(ctx, a, tb, wp, H));
+    }
+    // forward: ng grids
+    if (!long_y) {
+        FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_y_r2c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_y));
+        FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_y_c2r, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_y));
+        FTE_LAUNCH(ctx, k_fft_y_r2c, dim3(Mx / 2, ng), fft_threads(py.m), sm_y, (const double*)H, Hh, Mx, My, py);
+    } else {
+        FTE_LAUNCH(ctx, k_ly_pack_r2c, ew_grid(ctx, (long long)ng * (Mx / 2) * My), 256, 0, (const double*)H, S, Mx,
+                   My, ng);
+        FTE_TRY(fte_long_fft(ctx, ly, S, rows, (long long)ng * (Mx / 2), false, LS));
+        FTE_LAUNCH(ctx, k_ly_unpack_r2c, ew_grid(ctx, (long long)ng * (Mx / 2) * Kh), 256, 0, (const double2*)S, Hh,
+                   Mx, My, ng);
+    }
+    if (!long_x) {
+        FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_x));
+        FTE_LAUNCH(ctx, k_fft_x, dim3(Kh, ng), fft_threads(px.m), sm_x, Hh, Mx, Kh, px, 0);
+    } else {
+        FTE_TRY(fte_long_fft(ctx, lx, Hh, cols, (long long)ng * Kh, false, LS));
+    }
+    if (a.kind == FTE_KIND_SLP)
+        FTE_TRY(q_filter_launch<FTE_KIND_SLP>(ctx, q, Hh, a));
+    else
+        FTE_TRY(q_filter_launch<FTE_KIND_DLP>(ctx, q, Hh, a));
+    // inverse: no grids
+    if (!long_x)
+        FTE_LAUNCH(ctx, k_fft_x, dim3(Kh, no), fft_threads(px.m), sm_x, Hh, Mx, Kh, px, 1);
+    else
+        FTE_TRY(fte_long_fft(ctx, lx, Hh, cols, (long long)no * Kh, true, LS));
+    if (!long_y) {
+        FTE_LAUNCH(ctx, k_fft_y_c2r, dim3(Mx / 2, no), fft_threads(py.m), sm_y, (const double2*)Hh, H, Mx, My, py);
+    } else {
+        FTE_LAUNCH(ctx, k_ly_pack_c2r, ew_grid(ctx, (long long)no * (Mx / 2) * Kh), 256, 0, (const double2*)Hh, S, Mx,
+                   My, no);
+        FTE_TRY(fte_long_fft(ctx, ly, S, rows, (long long)no * (Mx / 2), true, LS));
+        FTE_LAUNCH(ctx, k_ly_unpack_c2r, ew_grid(ctx, (long long)no * (Mx / 2) * My), 256, 0, (const double2*)S, H,
+                   Mx, My, no);
+    }
+    if (a.ntar == 0) return FTE_OK;
+    // gather pairs of grids
+    TileBins tb;
+    FTE_TRY(fte_tiles_build(ctx, wc, a.ptar, a.ntar, a.Lx, a.Ly, wp.h, ts_g, (Mx + ts_g - 1) / ts_g,
+                            (My + ts_g - 1) / ts_g, &tb));
+    FTE_WS_CHECK(wc);
+    const double scale = gather_scale(a);
+    KspaceArgs ag = a;
+    ag.form = FTE_FORM_PLAIN;
+    if (no == 2) {
+        ag.uk = reinterpret_cast<double2*>(out);
+        FTE_TRY(launch_gather_tiled(ctx, ag, tb, wp, H, scale));
+        return FTE_OK;
+    }
+    ag.uk = ga;
+    FTE_TRY(launch_gather_tiled(ctx, ag, tb, wp, H, scale));  // grids 0 (and 1)
+    if (no == 4) {
+        ag.uk = gb;
+        FTE_TRY(launch_gather_tiled(ctx, ag, tb, wp, H + 2 * G, scale));  // grids 2, 3
+    }
+    FTE_LAUNCH(ctx, k_q_pack, ew_grid(ctx, a.ntar), 256, 0, (const double2*)ga, (const double2*)gb, (int64_t)a.ntar,
+               no, out);
     return FTE_OK;
 }
 

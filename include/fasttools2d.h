@@ -197,6 +197,30 @@ int fte_batch_destroy(fte_batch* batch);
 int fte_batch_set_density(fte_batch* batch, int i, const double* f1s, const double* f2s, unsigned flags);
 int fte_batch_get_velocity(fte_batch* batch, int i, double* u1s, double* u2s, unsigned flags);
 
+/* ---- other quantities: gateway level ------------------------------------- */
+/* Replace the reference's quantity gateways (PeriodicEwald/src/mex/):
+ *   StokesSLP/mex_stokes_slp_<q>_real.cpp, StokesSLP/mex_stokes_slp_<q>_kspace.cpp,
+ *   StokesDLP/mex_stokes_dlp_<q>_real.cpp, StokesDLP/mex_stokes_dlp_<q>_kspace.cpp
+ * for q = pressure, pressure_grad, gradient, stress, vorticity.  Arguments
+ * carry the same meaning as there (the gateways differ only in argument
+ * order); n (normals) is used by the stresslet (FTE_KIND_DLP) only.  out
+ * receives fte_q_ncomp(q) values per target (interleaved, the caller's target
+ * order): pressure and vorticity 1, pressure gradient 2, velocity gradient
+ * and stress 4, each in the gateway's component order and scaling.  FP64. */
+#define FTE_Q_VELOCITY 0
+#define FTE_Q_PRESSURE 1
+#define FTE_Q_PRESSURE_GRAD 2
+#define FTE_Q_GRADIENT 3
+#define FTE_Q_STRESS 4
+#define FTE_Q_VORTICITY 5
+int fte_q_ncomp(int quantity);
+int fte_q_real(fte_context* ctx, int kind, int quantity, const double* psrc, int64_t nsrc, const double* ptar,
+               int64_t ntar, const double* f, const double* n, double xi, int nside_x, int nside_y, double Lx,
+               double Ly, double* out, unsigned flags);
+int fte_q_kspace(fte_context* ctx, int kind, int quantity, const double* psrc, int64_t nsrc, const double* ptar,
+                 int64_t ntar, const double* f, const double* n, double xi, double eta, int Mx, int My, double Lx,
+                 double Ly, double w, int P, double* out, unsigned flags);
+
 /* ---- learned parameter selector: the network ------------------------------ */
 /* No counterpart in the reference.  An FP32 multilayer perceptron
  * 8 -> 64 -> 64 -> 4 (tanh hidden units) that maps features of a

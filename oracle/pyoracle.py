@@ -301,9 +301,9 @@ def _ref_lib(gateway: str, flavour: str):
     return _ref[key]
 
 
-def ref_call(gateway: str, args, n_out: int, flavour: str = "O3"):
+def ref_call(gateway: str, args, n_out: int, flavour: str = "O3", ncomp: int = 2):
     """Call a reference gateway.  Matrix args are (N, 2) arrays (passed as
-    2 x N); scalars are passed as 1 x 1.  Returns the (n_out, 2) output."""
+    2 x N); scalars are passed as 1 x 1.  Returns the (n_out, ncomp) output."""
     L = _ref_lib(gateway, flavour)
     mats = []
     ms, ns = [], []
@@ -318,10 +318,10 @@ def ref_call(gateway: str, args, n_out: int, flavour: str = "O3"):
             ns.append(arr.shape[0])
         mats.append(arr)
     ptrs = (_dp * len(mats))(*[_p(m) for m in mats])
-    out = np.zeros((n_out, 2))
+    out = np.zeros((n_out, ncomp))
     err = C.create_string_buffer(512)
     rc = L.ref_call(len(mats), ptrs, (C.c_long * len(ms))(*ms), (C.c_long * len(ns))(*ns), _p(out),
-                    C.c_long(2 * n_out), err, 512)
+                    C.c_long(ncomp * n_out), err, 512)
     if rc != 0:
         raise RuntimeError(err.value.decode())
     return out
@@ -357,3 +357,59 @@ def ref_stokes_dlp_ewald_2p(xsrc, ysrc, xtar, ytar, n1, n2, f1, f2, Lx, Ly, P=24
     uk[:, 1] += np.sum(fn * ys) / (Lx * Ly)
     u = ur + uk
     return u[:, 0], u[:, 1], ur, uk, prm
+
+
+# ---- other SE quantities (or_quant.c) ------------------------------------------
+Q_PRESSURE, Q_PRESSURE_GRAD, Q_GRADIENT, Q_STRESS, Q_VORTICITY = 1, 2, 3, 4, 5
+Q_NAMES = {Q_PRESSURE: "pressure", Q_PRESSURE_GRAD: "pressure_grad", Q_GRADIENT: "gradient", Q_STRESS: "stress",
+           Q_VORTICITY: "vorticity"}
+Q_NCOMP = {Q_PRESSURE: 1, Q_PRESSURE_GRAD: 2, Q_GRADIENT: 4, Q_STRESS: 4, Q_VORTICITY: 1}
+
+
+def q_real(kind, q, psrc, ptar, f, n, xi, nside_x, nside_y, Lx, Ly):
+    """Real-space sum of quantity q: (Ntar, ncomp)."""
+    psrc, ptar, f = _c(psrc), _c(ptar), _c(f)
+    nn = _c(n) if n is not None else None
+    out = np.zeros((ptar.shape[0], Q_NCOMP[q]))
+    L = lib()
+    L.or_q_real.restype = C.c_int
+    rc = L.or_q_real(C.c_int(kind), C.c_int(q), _p(psrc), C.c_int(psrc.shape[0]), _p(ptar), C.c_int(ptar.shape[0]),
+                     _p(f), _p(nn) if nn is not None else None, C.c_double(xi), C.c_int(nside_x), C.c_int(nside_y),
+                     C.c_double(Lx), C.c_double(Ly), _p(out))
+    assert rc == 0
+    return out
+
+
+def q_kspace(kind, q, psrc, ptar, f, n, xi, eta, Mx, My, Lx, Ly, w, P):
+    """k-space sum of quantity q: (Ntar, ncomp)."""
+    psrc, ptar, f = _c(psrc), _c(ptar), _c(f)
+    nn = _c(n) if n is not None else None
+    out = np.zeros((ptar.shape[0], Q_NCOMP[q]))
+    L = lib()
+    L.or_q_kspace.restype = C.c_int
+    rc = L.or_q_kspace(C.c_int(kind), C.c_int(q), _p(psrc), C.c_int(psrc.shape[0]), _p(ptar), C.c_int(ptar.shape[0]),
+                       _p(f), _p(nn) if nn is not None else None, C.c_double(xi), C.c_double(eta), C.c_int(Mx),
+                       C.c_int(My), C.c_double(Lx), C.c_double(Ly), C.c_double(w), C.c_int(P), _p(out))
+    assert rc == 0
+    return out
+
+
+# argument order of each reference quantity gateway (PeriodicEwald/src/mex/Stokes*/mex_stokes_*_{real,kspace}.cpp)
+_KSPACE_F_FIRST = {("slp", Q_PRESSURE), ("slp", Q_PRESSURE_GRAD), ("dlp", Q_PRESSURE), ("dlp", Q_PRESSURE_GRAD),
+                   ("dlp", Q_VORTICITY)}
+
+
+def ref_q_real(kind, q, psrc, ptar, f, n, xi, nside_x, nside_y, Lx, Ly, flavour="O3"):
+    k = "slp" if kind == KIND_SLP else "dlp"
+    args = [psrc, ptar, f] + ([n] if kind == KIND_DLP else []) + [xi, nside_x, nside_y, Lx, Ly]
+    return ref_call(f"{k}_{Q_NAMES[q]}_real", args, len(ptar), flavour, Q_NCOMP[q])
+
+
+def ref_q_kspace(kind, q, psrc, ptar, f, n, xi, eta, Mx, My, Lx, Ly, w, P, flavour="O3"):
+    k = "slp" if kind == KIND_SLP else "dlp"
+    dens = [f] + ([n] if kind == KIND_DLP else [])
+    if (k, q) in _KSPACE_F_FIRST:
+        args = [psrc, ptar] + dens + [xi, eta, Mx, My, Lx, Ly, w, P]
+    else:
+        args = [psrc, ptar, xi, eta] + dens + [Mx, My, Lx, Ly, w, P]
+    return ref_call(f"{k}_{Q_NAMES[q]}_kspace", args, len(ptar), flavour, Q_NCOMP[q])
