@@ -125,6 +125,8 @@ SIGNATURES = {
     "fte_q_ncomp": (_i, [_i]),
     "fte_q_real": (_i, [_vp, _i, _i, _vp, _i64, _vp, _i64, _vp, _vp, _d, _i, _i, _d, _d, _vp, _u]),
     "fte_q_kspace": (_i, [_vp, _i, _i, _vp, _i64, _vp, _i64, _vp, _vp, _d, _d, _i, _i, _d, _d, _d, _i, _vp, _u]),
+    "fte_stokes_q_ewald_2p": (_i, [_vp, _i, _i, _vp, _vp, _i64, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _d, _d,
+                                   C.POINTER(Options), _vp, _vp, _vp, C.POINTER(Info), _u]),
     "fte_mlp_param_count": (_i, []),
     "fte_mlp_scratch_floats": (C.c_size_t, [_i]),
     "fte_mlp_forward": (_i, [_vp, _vp, _i, _vp, _vp]),
@@ -608,3 +610,72 @@ def _make_q_gateways():
 
 
 _make_q_gateways()
+
+
+# ---- other quantities: driver level -------------------------------------------------
+
+def q_ewald_2p(kind, q, xsrc, ysrc, xtar, ytar, f1, f2, Lx, Ly, n1=None, n2=None, b1=None, b2=None, P=None, Nb=None,
+               tol=1e-16, xi=None, Mx=None, My=None, nside_x=None, nside_y=None, ctx: Context | None = None,
+               return_info=False):
+    """The quantity drivers (StokesSLP/DLP_<q>_ewald_2p): returns (out, out_real, out_k, xi) with out of
+    shape (Ntar,) for the pressure and the vorticity and (Ntar, 2) otherwise."""
+    ctx = ctx or default_context()
+    A = _Args()
+    pxs, ns = A.arr(xsrc, 1)
+    pys, _ = A.arr(ysrc, 1)
+    pxt, nt = A.arr(xtar, 1)
+    pyt, _ = A.arr(ytar, 1)
+    pn1, _ = A.arr(n1, 1)
+    pn2, _ = A.arr(n2, 1)
+    pf1, _ = A.arr(f1, 1)
+    pf2, _ = A.arr(f2, 1)
+    pb1, _ = A.arr(b1, 1)
+    pb2, _ = A.arr(b2, 1)
+    shape = (nt,) if q in (Q_PRESSURE, Q_VORTICITY) else (nt, 2)
+    out, po = A.out(shape)
+    outr, por = A.out(shape)
+    outk, pok = A.out(shape)
+    opt = _options(P, Nb, tol, xi, Mx, My, nside_x, nside_y)
+    info = Info()
+    _check(lib().fte_stokes_q_ewald_2p(ctx.h, int(kind), int(q), pxs, pys, ns, pxt, pyt, nt, pn1, pn2, pf1, pf2, pb1,
+                                       pb2, float(Lx), float(Ly), C.byref(opt), po, por, pok, C.byref(info),
+                                       A.flags))
+    res = (out, outr, outk, info.params.xi)
+    return (res, info) if return_info else res
+
+
+def _make_q_drivers():
+    """StokesSLP_<q>_ewald_2p / StokesDLP_<q>_ewald_2p with the MATLAB drivers'
+    positional arguments and outputs (PeriodicEwald/src/matlab/):
+      pressure, pressure_grad, vorticity: (..., [n1, n2,] f1, f2, Lx, Ly) -> (p, pr, pk, xi)
+      gradient, stress: (..., [n1, n2,] f1, f2, b1, b2, Lx, Ly) -> (out1, out2, out_r, out_k, xi)"""
+    names = {Q_PRESSURE: "pressure", Q_PRESSURE_GRAD: "pressure_grad", Q_GRADIENT: "gradient", Q_STRESS: "stress",
+             Q_VORTICITY: "vorticity"}
+    g = globals()
+    for kind, kn in ((KIND_SLP, "SLP"), (KIND_DLP, "DLP")):
+        for q, qn in names.items():
+            with_b = q in (Q_GRADIENT, Q_STRESS)
+
+            def drv(*args, _k=kind, _q=q, _b=with_b, **kw):
+                a = list(args)
+                xs, ys, xt, yt = a[:4]
+                rest = a[4:]
+                n1 = n2 = None
+                if _k == KIND_DLP:
+                    n1, n2, rest = rest[0], rest[1], rest[2:]
+                f1, f2, rest = rest[0], rest[1], rest[2:]
+                b1 = b2 = None
+                if _b:
+                    b1, b2, rest = rest[0], rest[1], rest[2:]
+                Lx, Ly = rest[0], rest[1]
+                out, outr, outk, xi = q_ewald_2p(_k, _q, xs, ys, xt, yt, f1, f2, Lx, Ly, n1=n1, n2=n2, b1=b1, b2=b2,
+                                                 **kw)
+                if _b:
+                    return out[:, 0], out[:, 1], outr, outk, xi
+                return out, outr, outk, xi
+
+            drv.__name__ = f"Stokes{kn}_{qn}_ewald_2p"
+            g[drv.__name__] = drv
+
+
+_make_q_drivers()

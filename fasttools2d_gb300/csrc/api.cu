@@ -6,6 +6,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <complex>
+#include <algorithm>
 #include <vector>
 
 #include "fte_internal.cuh"
@@ -1388,6 +1389,339 @@ static int ewald_entry(fte_context* c, int kind, const double* xsrc, const doubl
             info->ms_spread = fte_elapsed(c, 2, 3);
             info->ms_fft = fte_elapsed(c, 3, 4);
             info->ms_gather = fte_elapsed(c, 4, 5);
+        }
+    }
+    return FTE_OK;
+}
+
+// ---------------------------------------------------------------------------
+// other quantities, driver level: StokesSLP_<q>_ewald_2p / StokesDLP_<q>_ewald_2p
+// (PeriodicEwald/src/matlab/), q = pressure, pressure_grad, gradient, stress,
+// vorticity.  As the MATLAB drivers: wrap the points, choose the parameters
+// (the velocity drivers' estimates; the stresslet vorticity driver uses the
+// Stokeslet's), call the gateways, then per quantity
+//   SLP pressure:  p  = pr + pk,  pk = k-space - sum(f1 x + f2 y) / (2 Lx Ly)
+//   DLP pressure:  p  = pr + pk + pself,  pk = k-space - sum(n.f) / (2 Lx Ly),
+//                  pself = xi^2 (f.n) / (2 pi) of a source at the target
+//   SLP pressure gradient:  p = -(pr + pk + pself),  pself = xi^2 f / (2 pi)
+//   DLP pressure gradient:  p = -2 (pr + pk)
+//   velocity gradient (b):  u_1 = T1 b1 + T3 b2,  u_2 = T2 b1 + T4 b2 for the
+//                  real and k parts; DLP adds uself = xi^2 (q Re(b n*) +
+//                  n Re(q b*) + b Re(q n*)) / (2 pi) (complex q = f1 + i f2 ...)
+//   SLP stress (b): as the gradient, plus sum(f1 x + f2 y) / (2 Lx Ly) on both
+//                  components
+//   DLP stress (b): real part contracted (T1 b1 + T2 b2, T3 b1 + T4 b2), k part
+//                  as the gradient plus sum(n.f) / (2 Lx Ly); self term
+//                  -pself on the first component (pself = xi^2 b Re(q n*) /
+//                  (2 pi), complex in the driver: its real part is kept) and
+//                  2 uself
+//   SLP vorticity:  omega = omegar + omegak - sum(f1 y - f2 x) / (2 Lx Ly)
+//   DLP vorticity:  omega = omegar + omegak
+// Self terms: the drivers take the sources that coincide with some target
+// (before wrapping, exact equality) and add their terms elementwise to the
+// targets (k-th such source to the k-th target), or to every target when
+// there is exactly one; other counts do not fit the drivers' vector sums and
+// are rejected.
+// ---------------------------------------------------------------------------
+namespace {
+// acc[0] = sum f1^2 + f2^2, acc[1] = sum f1 x + f2 y, acc[2] = sum n.f, acc[3] = sum f1 y - f2 x
+__global__ void k_q_sums(const double* __restrict__ p, const double* __restrict__ f, const double* __restrict__ nrm,
+                         int64_t n, double* __restrict__ acc) {
+    double a[4] = {0, 0, 0, 0};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double f1 = f[2 * i], f2 = f[2 * i + 1], x = p[2 * i], y = p[2 * i + 1];
+        a[0] += f1 * f1 + f2 * f2;
+        a[1] += f1 * x + f2 * y;
+        if (nrm) a[2] += nrm[2 * i] * f1 + nrm[2 * i + 1] * f2;
+        a[3] += f1 * y - f2 * x;
+    }
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        double v = a[c];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if ((threadIdx.x & 31) == 0) atomicAdd(&acc[c], v);
+    }
+}
+
+__global__ void k_q_combine(int kind, int q, int64_t nt, const double* __restrict__ R, const double* __restrict__ K,
+                            const double* __restrict__ b1, const double* __restrict__ b2, const int* __restrict__ eqs,
+                            const double* __restrict__ f, const double* __restrict__ nrm, double xi,
+                            const double* __restrict__ sums, double area2, double* __restrict__ out,
+                            double* __restrict__ outr, double* __restrict__ outk) {
+    const double inv2pi = 1.0 / (2 * FTE_PI);
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt; t += (int64_t)gridDim.x * blockDim.x) {
+        const int s = eqs ? eqs[t] : -1;
+        double q1 = 0, q2 = 0, m1 = 0, m2 = 0;
+        if (s >= 0) {
+            q1 = f[2 * s];
+            q2 = f[2 * s + 1];
+            if (nrm) {
+                m1 = nrm[2 * s];
+                m2 = nrm[2 * s + 1];
+            }
+        }
+        if (q == FTE_Q_PRESSURE) {
+            const double r = R[t];
+            double k = K[t];
+            double self = 0;
+            if (kind == FTE_KIND_SLP) {
+                k = k + -sums[1] / area2;
+            } else {
+                k = k + -(sums[2] / area2);
+                if (s >= 0) self = xi * xi * (q1 * m1 + q2 * m2) * inv2pi;
+            }
+            out[t] = r + k + self;
+            if (outr) outr[t] = r;
+            if (outk) outk[t] = k;
+        } else if (q == FTE_Q_PRESSURE_GRAD) {
+            for (int c = 0; c < 2; c++) {
+                const double r = R[2 * t + c], k = K[2 * t + c];
+                double v;
+                if (kind == FTE_KIND_SLP) {
+                    const double self = s >= 0 ? xi * xi * (c ? q2 : q1) * inv2pi : 0.0;
+                    v = -(r + k + self);
+                } else {
+                    v = -2 * (r + k);
+                }
+                out[2 * t + c] = v;
+                if (outr) outr[2 * t + c] = r;
+                if (outk) outk[2 * t + c] = k;
+            }
+        } else if (q == FTE_Q_GRADIENT || q == FTE_Q_STRESS) {
+            const double B1 = b1[t], B2 = b2[t];
+            const double* r4 = R + 4 * t;
+            const double* k4 = K + 4 * t;
+            double r_1, r_2;
+            if (kind == FTE_KIND_DLP && q == FTE_Q_STRESS) {
+                r_1 = r4[0] * B1 + r4[1] * B2;
+                r_2 = r4[2] * B1 + r4[3] * B2;
+            } else {
+                r_1 = r4[0] * B1 + r4[2] * B2;
+                r_2 = r4[1] * B1 + r4[3] * B2;
+            }
+            double k_1 = k4[0] * B1 + k4[2] * B2, k_2 = k4[1] * B1 + k4[3] * B2;
+            double u_1 = r_1 + k_1, u_2 = r_2 + k_2;
+            if (q == FTE_Q_STRESS) {
+                if (kind == FTE_KIND_SLP) {
+                    const double z = sums[1] / area2;
+                    u_1 += z;
+                    u_2 += z;
+                } else {
+                    const double z = sums[2] / area2;
+                    k_1 += z;
+                    k_2 += z;
+                    u_1 = r_1 + k_1;
+                    u_2 = r_2 + k_2;
+                }
+            }
+            if (kind == FTE_KIND_DLP && s >= 0) {
+                // complex q = f1 + i f2, n = n1 + i n2, b = b1 + i b2
+                const double bn = B1 * m1 + B2 * m2;  // Re(b conj n)
+                const double qb = q1 * B1 + q2 * B2;  // Re(q conj b)
+                const double qn = q1 * m1 + q2 * m2;  // Re(q conj n)
+                const double s1 = xi * xi * (q1 * bn + m1 * qb + B1 * qn) * inv2pi;
+                const double s2 = xi * xi * (q2 * bn + m2 * qb + B2 * qn) * inv2pi;
+                if (q == FTE_Q_GRADIENT) {
+                    u_1 += s1;
+                    u_2 += s2;
+                } else {
+                    const double pself_re = xi * xi * B1 * qn * inv2pi;
+                    u_1 += -pself_re + 2 * s1;
+                    u_2 += 2 * s2;
+                }
+            }
+            out[2 * t] = u_1;
+            out[2 * t + 1] = u_2;
+            if (outr) {
+                outr[2 * t] = r_1;
+                outr[2 * t + 1] = r_2;
+            }
+            if (outk) {
+                outk[2 * t] = k_1;
+                outk[2 * t + 1] = k_2;
+            }
+        } else {  // vorticity
+            const double r = R[t], k = K[t];
+            double v = r + k;
+            if (kind == FTE_KIND_SLP) v = v - sums[3] / area2;
+            out[t] = v;
+            if (outr) outr[t] = r;
+            if (outk) outk[t] = k;
+        }
+    }
+}
+}  // namespace
+
+extern "C" int fte_stokes_q_ewald_2p(fte_context* c, int kind, int q, const double* xsrc, const double* ysrc,
+                                     int64_t nsrc, const double* xtar, const double* ytar, int64_t ntar,
+                                     const double* n1, const double* n2, const double* f1, const double* f2,
+                                     const double* b1, const double* b2, double Lx, double Ly,
+                                     const fte_options* opt, double* out, double* out_real, double* out_k,
+                                     fte_info* info, unsigned flags) {
+    if (!c) {
+        fte_set_error("null context");
+        return FTE_ERR_INVALID;
+    }
+    FTE_TRY(check_q(kind, q));
+    FTE_TRY(check_counts(nsrc, ntar));
+    FTE_TRY(check_box(Lx, Ly));
+    const bool with_b = q == FTE_Q_GRADIENT || q == FTE_Q_STRESS;
+    if ((nsrc > 0 && (!xsrc || !ysrc || !f1 || !f2 || (kind == FTE_KIND_DLP && (!n1 || !n2)))) ||
+        (ntar > 0 && (!xtar || !ytar || !out || (with_b && (!b1 || !b2))))) {
+        fte_set_error("null array argument");
+        return FTE_ERR_INVALID;
+    }
+    fte_options defaults;
+    std::memset(&defaults, 0, sizeof(defaults));
+    if (!opt) opt = &defaults;
+    if (opt->P != 0 && (opt->P < 2 || opt->P % 2 || opt->P > 64)) {
+        fte_set_error("window support P must be even and in [2, 64] (P=%d)", opt->P);
+        return FTE_ERR_INVALID;
+    }
+    FTE_CUDA_TRY(cudaSetDevice(c->device));
+    const bool host = !(flags & FTE_DEVICE_POINTERS);
+    const long long k0 = c->kernels;
+    const int nc = fte_q_ncomp(q);
+    const int nd = (q == FTE_Q_PRESSURE || q == FTE_Q_VORTICITY) ? 1 : 2;  // driver outputs per target
+    FTE_TRY(fte_record(c, 0));
+
+    // sources coinciding with targets (before wrapping): the drivers' self terms
+    const bool self_terms = (kind == FTE_KIND_DLP && (q == FTE_Q_PRESSURE || q == FTE_Q_GRADIENT ||
+                                                      q == FTE_Q_STRESS)) ||
+                            (kind == FTE_KIND_SLP && q == FTE_Q_PRESSURE_GRAD);
+    std::vector<int> eqs;
+    if (self_terms && nsrc > 0 && ntar > 0) {
+        std::vector<double> hx(nsrc), hy(nsrc), tx(ntar), ty(ntar);
+        const cudaMemcpyKind kd = host ? cudaMemcpyHostToHost : cudaMemcpyDeviceToHost;
+        FTE_CUDA_TRY(cudaMemcpy(hx.data(), xsrc, nsrc * 8, kd));
+        FTE_CUDA_TRY(cudaMemcpy(hy.data(), ysrc, nsrc * 8, kd));
+        FTE_CUDA_TRY(cudaMemcpy(tx.data(), xtar, ntar * 8, kd));
+        FTE_CUDA_TRY(cudaMemcpy(ty.data(), ytar, ntar * 8, kd));
+        std::vector<std::pair<double, double>> tk(ntar);
+        for (int64_t t = 0; t < ntar; t++) tk[t] = {tx[t], ty[t]};
+        std::sort(tk.begin(), tk.end());
+        std::vector<int> eq;
+        for (int64_t s2 = 0; s2 < nsrc; s2++)
+            if (std::binary_search(tk.begin(), tk.end(), std::make_pair(hx[s2], hy[s2]))) eq.push_back((int)s2);
+        if (!eq.empty()) {
+            if ((int64_t)eq.size() == ntar) {
+                eqs = eq;
+            } else if (eq.size() == 1) {
+                eqs.assign(ntar, eq[0]);
+            } else {
+                fte_set_error("%zu sources coincide with targets but there are %lld targets: the driver's self "
+                              "terms pair the k-th such source with the k-th target",
+                              eq.size(), (long long)ntar);
+                return FTE_ERR_UNSUPPORTED;
+            }
+        }
+    }
+
+    size_t base = ws_bytes(2 * (nsrc + 1), 8) * 3 + ws_bytes(2 * (ntar + 1), 8) +
+                  2 * ws_bytes((size_t)nc * (ntar + 1), 8) + 3 * ws_bytes((size_t)nd * (ntar + 1), 8) +
+                  ws_bytes(ntar + 1, 4) + 4096;
+    if (host) base += ws_bytes(nsrc + 1, 8) * 6 + ws_bytes(ntar + 1, 8) * 4;
+    FTE_TRY(fte_ws_reserve(c, base));
+    WsCarver wc{c->ws, 0, c->ws_size};
+    Stager st{c, &wc, host};
+    const double *dxs, *dys, *dxt, *dyt, *df1, *df2, *dn1 = nullptr, *dn2 = nullptr, *db1 = nullptr, *db2 = nullptr;
+    FTE_TRY(st.put(xsrc, nsrc, &dxs));
+    FTE_TRY(st.put(ysrc, nsrc, &dys));
+    FTE_TRY(st.put(xtar, ntar, &dxt));
+    FTE_TRY(st.put(ytar, ntar, &dyt));
+    FTE_TRY(st.put(f1, nsrc, &df1));
+    FTE_TRY(st.put(f2, nsrc, &df2));
+    if (kind == FTE_KIND_DLP) {
+        FTE_TRY(st.put(n1, nsrc, &dn1));
+        FTE_TRY(st.put(n2, nsrc, &dn2));
+    }
+    if (with_b) {
+        FTE_TRY(st.put(b1, ntar, &db1));
+        FTE_TRY(st.put(b2, ntar, &db2));
+    }
+    double* ps = wc.take<double>(2 * (nsrc + 1));
+    double* pt = wc.take<double>(2 * (ntar + 1));
+    double* pf = wc.take<double>(2 * (nsrc + 1));
+    double* pn = kind == FTE_KIND_DLP ? wc.take<double>(2 * (nsrc + 1)) : nullptr;
+    double* dR = wc.take<double>((size_t)nc * (ntar + 1));
+    double* dK = wc.take<double>((size_t)nc * (ntar + 1));
+    double* dout = host ? wc.take<double>((size_t)nd * (ntar + 1)) : out;
+    double* dor = out_real ? (host ? wc.take<double>((size_t)nd * (ntar + 1)) : out_real) : nullptr;
+    double* dok = out_k ? (host ? wc.take<double>((size_t)nd * (ntar + 1)) : out_k) : nullptr;
+    int* deq = eqs.empty() ? nullptr : wc.take<int>(ntar + 1);
+    double* acc = wc.take<double>(8);
+    FTE_WS_CHECK(wc);
+    FTE_CUDA_TRY(cudaMemsetAsync(acc, 0, 8 * sizeof(double), c->stream));
+    if (nsrc > 0) {
+        FTE_LAUNCH(c, k_wrap_pack, grid1d(c, nsrc), 256, 0, dxs, dys, nsrc, Lx, Ly, ps);
+        FTE_LAUNCH(c, k_pack, grid1d(c, nsrc), 256, 0, df1, df2, nsrc, pf);
+        if (pn) FTE_LAUNCH(c, k_pack, grid1d(c, nsrc), 256, 0, dn1, dn2, nsrc, pn);
+        FTE_LAUNCH(c, k_q_sums, grid1d(c, nsrc), 256, 0, (const double*)ps, (const double*)pf, (const double*)pn,
+                   nsrc, acc);
+    }
+    if (ntar > 0) FTE_LAUNCH(c, k_wrap_pack, grid1d(c, ntar), 256, 0, dxt, dyt, ntar, Lx, Ly, pt);
+    if (deq) FTE_CUDA_TRY(cudaMemcpyAsync(deq, eqs.data(), ntar * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    FTE_CUDA_TRY(cudaMemcpyAsync(c->host_scalars, acc, 4 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    FTE_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    const double Q = c->host_scalars[0] + 1.0;
+    // the stresslet vorticity driver uses the Stokeslet's estimates and point count
+    const int est_kind = (kind == FTE_KIND_DLP && q == FTE_Q_VORTICITY) ? FTE_KIND_SLP : kind;
+    fte_params prm;
+    FTE_TRY(choose_params_q(est_kind, nsrc, ntar, Q, Lx, Ly, opt, &prm));
+    FTE_TRY(check_real_params(prm.xi, prm.nside_x, prm.nside_y));
+    FTE_TRY(check_kspace_params(prm.xi, prm.eta, prm.Mx, prm.My, Lx, Ly, prm.w, prm.P));
+    size_t need = fte_cells_ws(nsrc, ntar, prm.nside_x * prm.nside_y) + fte_q_kspace_ws(prm.Mx, prm.My, nsrc, ntar) +
+                  8192;
+    FTE_TRY(fte_ws2_reserve(c, need));
+    if (ntar > 0) {
+        WsCarver wc2{c->ws2, 0, c->ws2_size};
+        CellList cl;
+        FTE_TRY(fte_record(c, 1));
+        FTE_TRY(fte_cells_build(c, wc2, kind, ps, nsrc, pt, ntar, pf, pn, nullptr, prm.nside_x, prm.nside_y, Lx, Ly,
+                                &cl));
+        FTE_TRY(fte_record(c, 6));
+        FTE_TRY(fte_q_near_launch(c, kind, q, cl, pf, pn, prm.xi, Lx, Ly, dR));
+        FTE_TRY(fte_record(c, 7));
+        WsCarver wck{c->ws2, 0, c->ws2_size};
+        KspaceArgs a;
+        a.kind = kind;
+        a.form = FTE_FORM_PLAIN;
+        a.nsrc = nsrc;
+        a.ntar = ntar;
+        a.psrc = ps;
+        a.ptar = pt;
+        a.f = pf;
+        a.nrm = pn;
+        a.wts = nullptr;
+        a.xi = prm.xi;
+        a.eta = prm.eta;
+        a.w = prm.w;
+        a.Lx = Lx;
+        a.Ly = Ly;
+        a.Mx = prm.Mx;
+        a.My = prm.My;
+        a.P = prm.P;
+        a.uk = nullptr;
+        FTE_TRY(fte_q_kspace_run(c, wck, q, a, dK));
+        FTE_TRY(fte_record(c, 5));
+        // device copy of the sums for the combination
+        double* dsums = acc;
+        FTE_LAUNCH(c, k_q_combine, grid1d(c, ntar), 256, 0, kind, q, ntar, (const double*)dR, (const double*)dK, db1,
+                   db2, (const int*)deq, (const double*)pf, (const double*)pn, prm.xi, (const double*)dsums,
+                   2 * Lx * Ly, dout, dor, dok);
+        FTE_TRY(finish_output(c, host, out, dout, (size_t)nd * ntar));
+        if (out_real) FTE_TRY(finish_output(c, host, out_real, dor, (size_t)nd * ntar));
+        if (out_k) FTE_TRY(finish_output(c, host, out_k, dok, (size_t)nd * ntar));
+    }
+    FTE_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    if (info) {
+        std::memset(info, 0, sizeof(*info));
+        info->params = prm;
+        info->kernels_launched = (int)(c->kernels - k0);
+        if (c->timing && ntar > 0) {
+            info->ms_total = fte_elapsed(c, 0, 5);
+            info->ms_cells = fte_elapsed(c, 1, 6);
+            info->ms_near = fte_elapsed(c, 6, 7);
         }
     }
     return FTE_OK;

@@ -221,6 +221,22 @@ int fte_q_kspace(fte_context* ctx, int kind, int quantity, const double* psrc, i
                  int64_t ntar, const double* f, const double* n, double xi, double eta, int Mx, int My, double Lx,
                  double Ly, double w, int P, double* out, unsigned flags);
 
+/* Driver level: replace PeriodicEwald/src/matlab/StokesSLP_<q>_ewald_2p.m and
+ * StokesDLP_<q>_ewald_2p.m (wrapping, the analytic parameter choice, the two
+ * gateways, zero modes, the self terms of sources that coincide with
+ * targets, and for the gradient and the stress the contraction with the
+ * vector b = (b1, b2) at each target).  out receives the driver's result: 1
+ * value per target for the pressure and the vorticity, 2 (interleaved) for
+ * the pressure gradient, gradient.b and stress.b; out_real / out_k (may be
+ * NULL) the driver's real and k parts, same layout.  n1/n2: stresslet only;
+ * b1/b2: gradient and stress only.  opt as for the velocity drivers (FP64
+ * plain form; opt->form is ignored).  info->params.xi is the driver's xi. */
+int fte_stokes_q_ewald_2p(fte_context* ctx, int kind, int quantity, const double* xsrc, const double* ysrc,
+                          int64_t nsrc, const double* xtar, const double* ytar, int64_t ntar, const double* n1,
+                          const double* n2, const double* f1, const double* f2, const double* b1, const double* b2,
+                          double Lx, double Ly, const fte_options* opt, double* out, double* out_real,
+                          double* out_k, fte_info* info, unsigned flags);
+
 /* ---- learned parameter selector: the network ------------------------------ */
 /* No counterpart in the reference.  An FP32 multilayer perceptron
  * 8 -> 64 -> 64 -> 4 (tanh hidden units) that maps features of a

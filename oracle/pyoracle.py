@@ -413,3 +413,92 @@ def ref_q_kspace(kind, q, psrc, ptar, f, n, xi, eta, Mx, My, Lx, Ly, w, P, flavo
     else:
         args = [psrc, ptar, xi, eta] + dens + [Mx, My, Lx, Ly, w, P]
     return ref_call(f"{k}_{Q_NAMES[q]}_kspace", args, len(ptar), flavour, Q_NCOMP[q])
+
+
+def ref_q_ewald_2p(kind, q, xsrc, ysrc, xtar, ytar, f1, f2, Lx, Ly, n1=None, n2=None, b1=None, b2=None, P=24, Nb=0.0,
+                   tol=1e-16, gateways="ref", flavour="O3"):
+    """The MATLAB drivers StokesSLP_<q>_ewald_2p / StokesDLP_<q>_ewald_2p
+    (PeriodicEwald/src/matlab/) restated around the gateways: the reference's
+    own compiled gateways (gateways="ref") or the oracle's (gateways="oracle").
+    Returns (out, out_real, out_k, params) with out of shape (Ntar,) for the
+    pressure and the vorticity and (Ntar, 2) otherwise."""
+    xsrc, ysrc, xtar, ytar = (np.asarray(a, dtype=np.float64) for a in (xsrc, ysrc, xtar, ytar))
+    f1, f2 = np.asarray(f1, dtype=np.float64), np.asarray(f2, dtype=np.float64)
+    nt = len(xtar)
+    # sources that coincide with a target, before wrapping (ismember(zsrc, ztar))
+    equal = np.nonzero(np.isin(xsrc + 1j * ysrc, xtar + 1j * ytar))[0]
+    est_kind = KIND_SLP if (kind == KIND_DLP and q == Q_VORTICITY) else kind
+    prm = choose_params(est_kind, f1, f2, len(xsrc), nt, Lx, Ly, P, Nb, tol)
+    xs, ys = matlab_wrap(xsrc, Lx), matlab_wrap(ysrc, Ly)
+    ps = np.stack([xs, ys], 1)
+    pt = np.stack([matlab_wrap(xtar, Lx), matlab_wrap(ytar, Ly)], 1)
+    f = np.stack([f1, f2], 1)
+    n = np.stack([np.asarray(n1, dtype=np.float64), np.asarray(n2, dtype=np.float64)], 1) if kind == KIND_DLP else None
+    if gateways == "ref":
+        R = ref_q_real(kind, q, ps, pt, f, n, prm.xi, prm.nside_x, prm.nside_y, Lx, Ly, flavour)
+        K = ref_q_kspace(kind, q, ps, pt, f, n, prm.xi, prm.eta, prm.Mx, prm.My, Lx, Ly, prm.w, prm.P, flavour)
+    else:
+        R = q_real(kind, q, ps, pt, f, n, prm.xi, prm.nside_x, prm.nside_y, Lx, Ly)
+        K = q_kspace(kind, q, ps, pt, f, n, prm.xi, prm.eta, prm.Mx, prm.My, Lx, Ly, prm.w, prm.P)
+    xi = prm.xi
+    area2 = 2 * Lx * Ly
+
+    def per_target(v):
+        """the drivers' elementwise (or scalar-broadcast) addition of self terms"""
+        if len(equal) == nt or len(equal) == 1:
+            return v if len(equal) == nt else np.broadcast_to(v, (nt,) + np.shape(v)[1:])
+        raise ValueError("self terms need one coincident source per target")
+
+    has_eq = len(equal) > 0
+    if q == Q_PRESSURE:
+        r, k = R[:, 0], K[:, 0]
+        if kind == KIND_SLP:
+            k = k + -np.sum(f1 * xs + f2 * ys) / area2
+            return r + k, r, k, prm
+        k = k + -(np.sum(n[:, 0] * f1 + n[:, 1] * f2) / area2)
+        pself = 0.0
+        if has_eq:
+            q_ = f1[equal] + 1j * f2[equal]
+            m_ = n[equal, 0] + 1j * n[equal, 1]
+            pself = per_target(xi ** 2 * np.real(q_ * np.conj(m_)) / (2 * np.pi))
+        return r + k + pself, r, k, prm
+    if q == Q_PRESSURE_GRAD:
+        if kind == KIND_SLP:
+            pself = 0.0
+            if has_eq:
+                pself = per_target(xi ** 2 * f[equal] / (2 * np.pi))
+            return -(R + K + pself), R, K, prm
+        return -2 * (R + K), R, K, prm
+    if q in (Q_GRADIENT, Q_STRESS):
+        b1, b2 = np.asarray(b1, dtype=np.float64), np.asarray(b2, dtype=np.float64)
+        if kind == KIND_DLP and q == Q_STRESS:
+            rr = np.stack([R[:, 0] * b1 + R[:, 1] * b2, R[:, 2] * b1 + R[:, 3] * b2], 1)
+        else:
+            rr = np.stack([R[:, 0] * b1 + R[:, 2] * b2, R[:, 1] * b1 + R[:, 3] * b2], 1)
+        kk = np.stack([K[:, 0] * b1 + K[:, 2] * b2, K[:, 1] * b1 + K[:, 3] * b2], 1)
+        if q == Q_STRESS and kind == KIND_SLP:
+            u = rr + kk + np.sum(f1 * xs + f2 * ys) / area2
+            return u, rr, kk, prm
+        if q == Q_STRESS:
+            kk = kk + np.sum(n[:, 0] * f1 + n[:, 1] * f2) / area2
+        u = rr + kk
+        if kind == KIND_DLP and has_eq:
+            q_ = f1[equal] + 1j * f2[equal]
+            m_ = n[equal, 0] + 1j * n[equal, 1]
+            b_ = b1 + 1j * b2
+            us = xi ** 2 * (q_ * np.real(b_ * np.conj(m_)) + m_ * np.real(q_ * np.conj(b_)) +
+                            b_ * np.real(q_ * np.conj(m_))) / (2 * np.pi)
+            us = per_target(us)
+            if q == Q_GRADIENT:
+                u = u + np.stack([np.real(us), np.imag(us)], 1)
+            else:
+                pself = xi ** 2 * b_ * np.real(q_ * np.conj(m_)) / (2 * np.pi)
+                pself = per_target(pself)
+                # the driver's first component is complex there; its real part
+                u = u + np.stack([-np.real(pself) + 2 * np.real(us), 2 * np.imag(us)], 1)
+        return u, rr, kk, prm
+    r, k = R[:, 0], K[:, 0]
+    v = r + k
+    if kind == KIND_SLP:
+        v = v - np.sum(f1 * ys - f2 * xs) / area2
+    return v, r, k, prm

@@ -11,7 +11,7 @@ from oracle import pyoracle as po
 pytestmark = pytest.mark.gpu
 
 TOL = 1e-12
-NAMES = golden_names("quant_")
+NAMES = [n for n in golden_names("quant_") if not n.startswith("quant_drv_")]
 
 
 def _ft():
@@ -99,3 +99,39 @@ def test_unknown_quantity_is_rejected(gpu_ctx):
     ps = np.zeros((4, 2))
     with pytest.raises(ft.FteError):
         ft.q_real(0, 9, ps, ps, ps, None, 10.0, 2, 2, 1.0, 1.0, ctx=gpu_ctx)
+
+
+DRV = golden_names("quant_drv_")
+
+
+@pytest.mark.parametrize("name", DRV)
+def test_quantity_drivers_match_reference(gpu_ctx, name):
+    """StokesSLP/DLP_<q>_ewald_2p on the GPU against the drivers built on the
+    reference's gateways: targets equal to the sources (self terms) and
+    separate targets."""
+    ft = _ft()
+    g = load_golden(name)
+    kind, q = int(g["kind"]), int(g["quantity"])
+    for i in (0, 1):
+        d = {k[3:]: g[k] for k in g if k.startswith(f"c{i}_")}
+        (o, r, k, xi), info = ft.q_ewald_2p(kind, q, d["xsrc"], d["ysrc"], d["xtar"], d["ytar"], d["f1"], d["f2"],
+                                            float(d["Lx"]), float(d["Ly"]), n1=d["n1"], n2=d["n2"], b1=d["b1"],
+                                            b2=d["b2"], tol=float(d["tol"]), ctx=gpu_ctx, return_info=True)
+        assert xi == pytest.approx(float(d["xi"]), rel=1e-14) and info.params.Mx == int(d["Mx"])
+        assert rel_max(o, d["out"]) <= TOL, (name, i)
+        assert rel_max(r, d["out_real"]) <= TOL and rel_max(k, d["out_k"]) <= TOL, (name, i)
+
+
+def test_named_quantity_drivers(gpu_ctx):
+    ft = _ft()
+    g = load_golden("quant_drv_dlp_stress")
+    d = {k[3:]: g[k] for k in g if k.startswith("c0_")}
+    s1, s2, sr, sk, xi = ft.StokesDLP_stress_ewald_2p(d["xsrc"], d["ysrc"], d["xtar"], d["ytar"], d["n1"], d["n2"],
+                                                      d["f1"], d["f2"], d["b1"], d["b2"], float(d["Lx"]),
+                                                      float(d["Ly"]), tol=float(d["tol"]), ctx=gpu_ctx)
+    assert rel_max(np.stack([s1, s2], 1), d["out"]) <= TOL
+    g = load_golden("quant_drv_slp_pressure")
+    d = {k[3:]: g[k] for k in g if k.startswith("c1_")}
+    p, pr, pk, xi = ft.StokesSLP_pressure_ewald_2p(d["xsrc"], d["ysrc"], d["xtar"], d["ytar"], d["f1"], d["f2"],
+                                                   float(d["Lx"]), float(d["Ly"]), tol=float(d["tol"]), ctx=gpu_ctx)
+    assert rel_max(p, d["out"]) <= TOL

@@ -7,7 +7,7 @@ import pytest
 from conftest import golden_names, load_golden, rel_max
 from oracle import pyoracle as po
 
-NAMES = golden_names("quant_")
+NAMES = [n for n in golden_names("quant_") if not n.startswith("quant_drv_")]
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -31,3 +31,22 @@ def test_oracle_matches_reference_gateways(name):
     assert ur.shape == g["real"].shape and uk.shape == g["kspace"].shape
     assert rel_max(ur, g["real"]) <= 1e-13, name
     assert rel_max(uk, g["kspace"]) <= 1e-13, name
+
+
+DRV = golden_names("quant_drv_")
+
+
+@pytest.mark.parametrize("name", DRV)
+def test_driver_restatement_on_oracle_gateways(name):
+    """The drivers' glue around the oracle's gateways reproduces the golden
+    drivers built around the reference's own gateways."""
+    g = load_golden(name)
+    kind, q = int(g["kind"]), int(g["quantity"])
+    for i in (0, 1):
+        d = {k[3:]: g[k] for k in g if k.startswith(f"c{i}_")}
+        o, r, k, prm = po.ref_q_ewald_2p(kind, q, d["xsrc"], d["ysrc"], d["xtar"], d["ytar"], d["f1"], d["f2"],
+                                         float(d["Lx"]), float(d["Ly"]), d["n1"], d["n2"], d["b1"], d["b2"],
+                                         tol=float(d["tol"]), gateways="oracle")
+        assert prm.xi == pytest.approx(float(d["xi"])) and prm.Mx == int(d["Mx"])
+        assert rel_max(o, d["out"]) <= 1e-13, (name, i)
+        assert rel_max(r, d["out_real"]) <= 1e-13 and rel_max(k, d["out_k"]) <= 1e-13, (name, i)
