@@ -658,7 +658,36 @@ int next_smooth_even(int n) {
 
 // transform work of a length-n line relative to a 7-smooth line of n points:
 // Bluestein runs two transforms of a smooth length m >= 2n - 1 (about 2.2 n)
-double fft_weight(int n) { return smooth7(n, nullptr) ? (double)n : 5.5 * (double)n; }
+// Transform work per point of a length-n line: the sum over the Stockham
+// passes of each radix's arithmetic per point (twiddles included; radix 8
+// does three levels for 9 FP64 operations per point, the paired odd-radix
+// DFTs cost more per level); Bluestein runs two transforms of a smooth
+// length m >= 2n - 1 plus the chirp products.
+// per-point cost of the Stockham passes of a 7-smooth n (radix-8 passes
+// first, then one 4 or 2, then 3, 5, 7 as the plans order them); -1 when n
+// is not 7-smooth.  Allocation-free: the chooser calls it thousands of times.
+double smooth_line_cost(int n) {
+    if (n < 1) return -1;
+    int c2 = 0, c3 = 0, c5 = 0, c7 = 0;
+    while (n % 2 == 0) n /= 2, c2++;
+    while (n % 3 == 0) n /= 3, c3++;
+    while (n % 5 == 0) n /= 5, c5++;
+    while (n % 7 == 0) n /= 7, c7++;
+    if (n != 1) return -1;
+    const int c8 = c2 / 3, r2 = c2 - 3 * c8;
+    return 9.0 * c8 + (r2 == 2 ? 7.0 : (r2 == 1 ? 5.0 : 0.0)) + 8.0 * c3 + 11.0 * c5 + 13.0 * c7;
+}
+double line_cost(int n) {
+    const double c = smooth_line_cost(n);
+    if (c >= 0) return c;
+    // Bluestein: two transforms of a smooth length near 2n plus the chirp
+    // products, per point of n (estimated without searching the length)
+    const double m = 2.2 * n;
+    return (2 * 3.4 * std::log2(m) + 12) * m / n;
+}
+// 2-D transform work of an Mx x My grid in units that equal points x log2(points)
+// for power-of-two sides (about 3.1 operations per point and level)
+double fft_work(int Mx, int My) { return (double)Mx * My * (line_cost(Mx) + line_cost(My)) / 3.1; }
 
 // Grid resolving kinf modes along Lx with square cells (hx = hy):
 // Mx = A t, My = B t (Lx / Ly = A / B), t >= 2 kinf / A, both even; among
@@ -674,7 +703,7 @@ void pick_grid(int A, int B, int kinf, int* Mx, int* My) {
     for (int t = t0; t <= t0 + span; t++) {
         int mx = A * t, my = B * t;
         if (mx % 2 || my % 2) continue;
-        double w = fft_weight(mx) * my * std::log2((double)mx) + fft_weight(my) * mx * std::log2((double)my);
+        double w = fft_work(mx, my);
         if (w < best) {
             best = w;
             bt = t;
@@ -749,7 +778,7 @@ static int choose_params_tuned(int kind, int64_t nsrc, int64_t ntar, double Q, d
         double pairs = (double)nsrc * (double)ntar * FTE_PI * rc * rc / area * 1.03;
         double win = (double)(P + 1) * (P + 1) * ((double)nsrc * ng + (double)ntar * 2);
         double pts = (double)Mx * My;
-        double fftw = (fft_weight(Mx) * My + fft_weight(My) * Mx) / 2 * std::log2(pts);
+        double fftw = fft_work(Mx, My);
         double cost = kCostPair * pairs + (f32 ? kCostWin32 : kCostWin64) * win +
                       (f32 ? kCostFft32 : kCostFft64) * (long64 ? 2.5 : 1.0) * nfft * fftw;
         if (cost < best) {

@@ -115,23 +115,41 @@ __device__ __forceinline__ void dft_small(typename Cx<T>::V* v, bool inv) {
         v[3] = cadd(e[3], o3);
         v[7] = csub(e[3], o3);
     } else {
+        // odd R: pair the inputs r and R - r.  With t_r = v_r + v_{R-r},
+        // u_r = v_r - v_{R-r} (r = 1..H, H = (R-1)/2):
+        //   out_0     = v_0 + sum_r t_r
+        //   out_s     = A_s - i B_s,  out_{R-s} = A_s + i B_s   (forward; inverse swaps)
+        //   A_s = v_0 + sum_r cos(2 pi r s / R) t_r,  B_s = sum_r sin(2 pi r s / R) u_r
+        // about a third of the arithmetic of the direct sum over all r, s.
+        constexpr int H = (R - 1) / 2;
         const double* rc = R == 3 ? fte_root3[0] : (R == 5 ? fte_root5[0] : fte_root7[0]);
         const double* rs = R == 3 ? fte_root3[1] : (R == 5 ? fte_root5[1] : fte_root7[1]);
-        V out[R];
+        V t[H], u[H];
+        V out0 = v[0];
 #pragma unroll
-        for (int s = 0; s < R; s++) {
-            T ax = 0, ay = 0;
-#pragma unroll
-            for (int r = 0; r < R; r++) {
-                int m = (r * s) % R;
-                T c = (T)rc[m], sn = inv ? (T)rs[m] : -(T)rs[m];
-                ax += v[r].x * c - v[r].y * sn;
-                ay += v[r].x * sn + v[r].y * c;
-            }
-            out[s] = Cx<T>::mk(ax, ay);
+        for (int r = 1; r <= H; r++) {
+            t[r - 1] = cadd(v[r], v[R - r]);
+            u[r - 1] = csub(v[r], v[R - r]);
+            out0 = cadd(out0, t[r - 1]);
         }
 #pragma unroll
-        for (int s = 0; s < R; s++) v[s] = out[s];
+        for (int s = 1; s <= H; s++) {
+            T ax = v[0].x, ay = v[0].y, bx = 0, by = 0;
+#pragma unroll
+            for (int r = 1; r <= H; r++) {
+                const int m = (r * s) % R;
+                const T c = (T)rc[m], sn = (T)rs[m];
+                ax += c * t[r - 1].x;
+                ay += c * t[r - 1].y;
+                bx += sn * u[r - 1].x;
+                by += sn * u[r - 1].y;
+            }
+            // -i B = (by, -bx); forward: out_s = A - iB, out_{R-s} = A + iB
+            const V am = Cx<T>::mk(ax + by, ay - bx), ap = Cx<T>::mk(ax - by, ay + bx);
+            v[s] = inv ? ap : am;
+            v[R - s] = inv ? am : ap;
+        }
+        v[0] = out0;
     }
 }
 

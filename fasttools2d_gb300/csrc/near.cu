@@ -567,11 +567,12 @@ int near_cap(const fte_context* ctx) {
 
 double fte_near_fp32_threshold(double tol) {
     // FP32 terms carry relative rounding ~1e-7 and a pair's terms scale with
-    // e^-x (1 + x); pairs with e^-x (1 + x) <= 1e6 tol keep that rounding
-    // near 1e-1 tol of the sum's own scale, which the FP64 pairs with x < 1
-    // set, and the per-pair rounding errors add incoherently.  Never below
-    // x = 1 (the Stokeslet's log branch stays FP64).
-    const double target = 1e6 * tol;
+    // e^-x (1 + x); pairs with e^-x (1 + x) <= 1e7 tol keep that rounding
+    // at about tol of a single near term (the sum's scale is set by the FP64
+    // pairs with x < 1, tens of them per target), and the per-pair rounding
+    // errors add incoherently.  Never below x = 1 (the Stokeslet's log
+    // branch stays FP64).
+    const double target = 1e7 * tol;
     if (!(target > 0) || target >= 2.0 / std::exp(1.0)) return 1.0;
     double lo = 1.0, hi = 800.0;
     for (int it = 0; it < 100; it++) {
