@@ -11,13 +11,16 @@
 // GPU design: one CTA per target box stages the 3x3 neighbourhood's sources
 // (image shift applied, FP64 positions and densities, FP32 box-relative
 // positions) in shared memory, in chunks when the neighbourhood is large.  A
-// warp owns one target at a time: its lanes sweep the staged sources 32 at a
-// time with a conservative FP32 distance test, compact the survivors into a
-// per-warp ring queue (ballot + popc), and every full queue of 32 candidate
-// pairs is evaluated with all lanes busy in FP64 (exact cutoff test, exp, E1).
-// GB300's FP64 pipe issues a warp instruction every ~16 cycles per SM, so the
-// compaction is what keeps the FP64 work proportional to pairs inside the
-// cutoff instead of to candidate pairs.
+// warp sweeps its targets one after another: its lanes test the staged
+// sources 32 at a time with a conservative FP32 distance test, compact the
+// survivors into per-warp ring queues (ballot + popc), and every full queue
+// of 32 candidate pairs is evaluated with all lanes busy in FP64 (exact
+// cutoff test, exp, E1).  Queue entries carry the slot of their target, so
+// up to four targets are in flight and a target's last, partial batch is
+// filled by the next targets' pairs.  GB300's FP64 pipe issues a warp
+// instruction every ~16 cycles per SM whatever the number of active lanes,
+// so full batches are what keeps the FP64 work proportional to the pairs
+// inside the cutoff.
 #include "fte_internal.cuh"
 
 #define FTE_E1_STORAGE_R static __constant__
@@ -79,12 +82,6 @@ __device__ __forceinline__ double fte_e1(double x, double emx, double inv_x, con
 #pragma unroll
     for (int j = FTE_E1_DEG_G - 1; j >= 0; j--) g = fma(g, t, c[j]);
     return emx * g * inv_x;
-}
-
-__device__ __forceinline__ double warp_sum(double v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    return v;
 }
 
 // exp(-x) for x >= 0 (0 beyond 700): 2^(-n/64) exp(-r) with n = round(64 x / ln 2),
@@ -176,6 +173,9 @@ __device__ __forceinline__ float fte_kfun32(float x, const float* __restrict__ k
 template <int KIND, int NV>
 struct NearSmem {
     static constexpr int kDen = KIND == FTE_KIND_SLP ? 2 : 4;
+    // targets a warp keeps in flight (ring entries carry the slot): the
+    // accumulators cost NSLOT * NV * 2 doubles per lane
+    static constexpr int kSlots = NV == 1 ? 4 : (NV == 2 ? 2 : 1);
     __host__ __device__ static size_t bytes(int cap) {
         return (kKtab + 64) * sizeof(double) + kKtab * sizeof(float) +
                (size_t)cap * ((2 + kDen * NV) * sizeof(double) + sizeof(float2) + kDen * NV * sizeof(float)) +
@@ -190,6 +190,7 @@ template <int KIND, int NV>
 __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned char* smem_raw, int* nb_box,
                                          int* nb_start, double* nb_shx, double* nb_shy) {
     constexpr int kDen = NearSmem<KIND, NV>::kDen;
+    constexpr int NSLOT = NearSmem<KIND, NV>::kSlots;
     const int cap = prm.cap;
     const double* ktab = reinterpret_cast<const double*>(smem_raw);
     const double* etab = ktab + kKtab;
@@ -207,6 +208,11 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
     int* qf = qbuf + warp * 3 * kQueue;
     int* qn = qf + kQueue;
     int* qs = qn + kQueue;
+    // per warp and target slot: the target's position and its FP32-class sums
+    __shared__ double2 tslot[kNearWarps * 4];
+    __shared__ float fsum_all[kNearWarps * 8];
+    double2* tsl = tslot + warp * 4;
+    float* fsw = fsum_all + warp * 8;
     const float x32 = prm.x32;
     const float cutf = (float)prm.cutoffsq;
     const float pf32 = (float)prm.pf;
@@ -292,123 +298,226 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
         __syncthreads();
         const int own_lim = n_own - chunk;  // local index < own_lim: own box
 
-        for (int t = warp; t < nt; t += kNearWarps) {
-            const double2 tp = prm.tpos[t0 + t];
-            const float tx32 = (float)(tp.x - cx), ty32 = (float)(tp.y - cy);
-            double acc[NV][2];
-            float acc32[NV][2];
+        // A warp keeps up to NSLOT of its targets in flight.  FP64 ring
+        // entries are (staged source << 2 | slot), the lanes accumulate per
+        // slot, and a target is reduced once the rings have passed every
+        // entry it pushed: the batch that would end one target's sweep half
+        // empty fills up with the next targets' pairs instead.  The FP32 class
+        // is cheap and is finished per target.
+        const int ntw = warp < nt ? (nt - warp + kNearWarps - 1) / kNearWarps : 0;
+        int Pf = 0, Ef = 0, Pn = 0, En = 0;  // pushed / evaluated counts of rings qf, qn
+        int tailF[NSLOT], tailN[NSLOT];      // Pf, Pn after each slot's sweep
+        double acc[NSLOT][NV][2];
+        float acc32[NV][2];
 #pragma unroll
-            for (int v = 0; v < NV; v++) acc[v][0] = acc[v][1] = 0.0, acc32[v][0] = acc32[v][1] = 0.0f;
-            int hf = 0, cf = 0, hn = 0, cn = 0, hs = 0, cs = 0;  // ring heads and counts
+        for (int j = 0; j < NSLOT; j++) {
+            tailF[j] = tailN[j] = 0;
+#pragma unroll
+            for (int v = 0; v < NV; v++) acc[j][v][0] = acc[j][v][1] = 0.0;
+        }
+#pragma unroll
+        for (int v = 0; v < NV; v++) acc32[v][0] = acc32[v][1] = 0.0f;
+        float tx32 = 0.0f, ty32 = 0.0f;  // box-relative position of the target being swept
 
-            // FP32 class: the same pair terms in FP32 from box-relative
-            // positions, accumulated per lane in FP32 and added to the FP64
-            // sum once per target
-            auto eval_slp32 = [&](int s) {
-                const float2 q = s32[s];
-                const float dx = tx32 - q.x, dy = ty32 - q.y;
-                const float r2 = fmaf(dx, dx, dy * dy);
-                if (!(s < own_lim) && !(r2 < cutf)) return;
-                const float x = r2 * xi2f;
-                const float e = expf(-x);
-                const float A = e * fte_kfun32(x, ktab32);
-                const float gr = __fdividef(e, r2);
+        // slot `tag`'s accumulators of vector v, selected into (a0, a1) and
+        // back: register moves only, no FP64 work per slot
+        auto acc_get = [&](int tag, int v, double& a0, double& a1) {
+            a0 = acc[0][v][0];
+            a1 = acc[0][v][1];
 #pragma unroll
-                for (int v = 0; v < NV; v++) {
-                    const float* d = den32 + (size_t)v * 2 * cap + s;
-                    const float fx = d[0], fy = d[cap];
-                    const float c = gr * fmaf(dx, fx, dy * fy);
-                    acc32[v][0] = fmaf(A, fx, fmaf(c, dx, acc32[v][0]));
-                    acc32[v][1] = fmaf(A, fy, fmaf(c, dy, acc32[v][1]));
-                }
-            };
-            auto eval_dlp32 = [&](int s) {
-                const float2 q = s32[s];
-                const float dx = tx32 - q.x, dy = ty32 - q.y;
-                const float r2 = fmaf(dx, dx, dy * dy);
-                if (!(s < own_lim) && !(r2 < cutf)) return;
-                const float x = r2 * xi2f;
-                const float e2 = expf(-x);
-                const float ir2 = __frcp_rn(r2);
-                const float facb = -4.0f * (1.0f + x) * ir2 * ir2;
+            for (int j = 1; j < NSLOT; j++)
+                if (tag == j) a0 = acc[j][v][0], a1 = acc[j][v][1];
+        };
+        auto acc_put = [&](int tag, int v, double a0, double a1) {
 #pragma unroll
-                for (int v = 0; v < NV; v++) {
-                    const float* d = den32 + (size_t)v * 4 * cap + s;
-                    const float s11 = d[0], h = d[cap], s22 = d[2 * cap], tr = d[3 * cap];
-                    const float u = fmaf(dx, s11, dy * h);
-                    const float w = fmaf(dy, s22, dx * h);
-                    const float fQ = facb * fmaf(dx, u, dy * w);
-                    const float w1 = fmaf(dx, tr, u + u);
-                    const float w2 = fmaf(dy, tr, w + w);
-                    acc32[v][0] = fmaf(e2, fmaf(fQ, dx, pf32 * w1), acc32[v][0]);
-                    acc32[v][1] = fmaf(e2, fmaf(fQ, dy, pf32 * w2), acc32[v][1]);
-                }
-            };
+            for (int j = 0; j < NSLOT; j++)
+                if (tag == j) acc[j][v][0] = a0, acc[j][v][1] = a1;
+        };
 
-            // Stokeslet pair (mex_stokes_slp_real.cpp:161-225 / 264-323):
-            //   u += (0.5 E1(x) - e^-x) f + e^-x (r.f) r / r^2,   x = xi^2 r^2
-            auto eval_slp = [&](int s, bool small_x) {
-                double dx = tp.x - sx[s], dy = tp.y - sy[s];
-                double r2 = fma(dx, dx, dy * dy);
-                bool own = s < own_lim;
-                if (own && fabs(r2) < 1e-15) {
+        // FP32 class: the same pair terms in FP32 from box-relative
+        // positions, accumulated per lane in FP32 for the target being swept
+        auto eval_slp32 = [&](int s) {
+            const float2 q = s32[s];
+            const float dx = tx32 - q.x, dy = ty32 - q.y;
+            const float r2 = fmaf(dx, dx, dy * dy);
+            if (!(s < own_lim) && !(r2 < cutf)) return;
+            const float x = r2 * xi2f;
+            const float e = expf(-x);
+            const float A = e * fte_kfun32(x, ktab32);
+            const float gr = __fdividef(e, r2);
 #pragma unroll
-                    for (int v = 0; v < NV; v++) {
-                        const double* d = den + (size_t)v * 2 * cap + s;
-                        acc[v][0] = fma(prm.selfc, d[0], acc[v][0]);
-                        acc[v][1] = fma(prm.selfc, d[cap], acc[v][1]);
-                    }
-                    return;
-                }
-                if (!own && !(r2 < prm.cutoffsq)) return;
-                double x = r2 * prm.xi2;
-                double emx = fte_expm(x, etab);
-                double A;
-                if (small_x) {
-                    double tt = fma(2.0, x, -1.0);
-                    double R = fte_e1_coef_r[FTE_E1_DEG_R];
+            for (int v = 0; v < NV; v++) {
+                const float* d = den32 + (size_t)v * 2 * cap + s;
+                const float fx = d[0], fy = d[cap];
+                const float c = gr * fmaf(dx, fx, dy * fy);
+                acc32[v][0] = fmaf(A, fx, fmaf(c, dx, acc32[v][0]));
+                acc32[v][1] = fmaf(A, fy, fmaf(c, dy, acc32[v][1]));
+            }
+        };
+        auto eval_dlp32 = [&](int s) {
+            const float2 q = s32[s];
+            const float dx = tx32 - q.x, dy = ty32 - q.y;
+            const float r2 = fmaf(dx, dx, dy * dy);
+            if (!(s < own_lim) && !(r2 < cutf)) return;
+            const float x = r2 * xi2f;
+            const float e2 = expf(-x);
+            const float ir2 = __frcp_rn(r2);
+            const float facb = -4.0f * (1.0f + x) * ir2 * ir2;
 #pragma unroll
-                    for (int k = FTE_E1_DEG_R - 1; k >= 0; k--) R = fma(R, tt, fte_e1_coef_r[k]);
-                    double E = fma(x, R, -FTE_EULER - log(x));
-                    A = fma(0.5, E, -emx);
-                } else {
-                    A = emx * fte_kfun(x, ktab);
-                }
-                double gr = emx * fte_rcp(r2);
+            for (int v = 0; v < NV; v++) {
+                const float* d = den32 + (size_t)v * 4 * cap + s;
+                const float s11 = d[0], h = d[cap], s22 = d[2 * cap], tr = d[3 * cap];
+                const float u = fmaf(dx, s11, dy * h);
+                const float w = fmaf(dy, s22, dx * h);
+                const float fQ = facb * fmaf(dx, u, dy * w);
+                const float w1 = fmaf(dx, tr, u + u);
+                const float w2 = fmaf(dy, tr, w + w);
+                acc32[v][0] = fmaf(e2, fmaf(fQ, dx, pf32 * w1), acc32[v][0]);
+                acc32[v][1] = fmaf(e2, fmaf(fQ, dy, pf32 * w2), acc32[v][1]);
+            }
+        };
+
+        // Stokeslet pair (mex_stokes_slp_real.cpp:161-225 / 264-323):
+        //   u += (0.5 E1(x) - e^-x) f + e^-x (r.f) r / r^2,   x = xi^2 r^2
+        auto eval_slp = [&](int ent, bool small_x) {
+            const int s = ent >> 2, tag = ent & 3;
+            const double2 tp = tsl[tag];
+            double dx = tp.x - sx[s], dy = tp.y - sy[s];
+            double r2 = fma(dx, dx, dy * dy);
+            bool own = s < own_lim;
+            if (own && fabs(r2) < 1e-15) {
 #pragma unroll
                 for (int v = 0; v < NV; v++) {
                     const double* d = den + (size_t)v * 2 * cap + s;
-                    double fx = d[0], fy = d[cap];
-                    double c = gr * fma(dx, fx, dy * fy);
-                    acc[v][0] = fma(A, fx, fma(c, dx, acc[v][0]));
-                    acc[v][1] = fma(A, fy, fma(c, dy, acc[v][1]));
+                    double a0, a1;
+                    acc_get(tag, v, a0, a1);
+                    a0 = fma(prm.selfc, d[0], a0);
+                    a1 = fma(prm.selfc, d[cap], a1);
+                    acc_put(tag, v, a0, a1);
                 }
-            };
-            // stresslet pair (mex_stokes_dlp_real.cpp:117-138 / 162-181):
-            //   u_i += e^-x [ -4 (1+x) r_i (r.S.r)/r^4 + 2 xi^2 (f_i (r.n) + n_i (r.f) + (f.n) r_i) ]
-            auto eval_dlp = [&](int s) {
-                double dx = tp.x - sx[s], dy = tp.y - sy[s];
-                double r2 = fma(dx, dx, dy * dy);
-                bool own = s < own_lim;
-                if (own ? (r2 == 0.0) : !(r2 < prm.cutoffsq)) return;
-                double x = r2 * prm.xi2;
-                double e2 = fte_expm(x, etab);
-                double ir2 = fte_rcp(r2);
-                double facb = -4.0 * (1.0 + x) * ir2 * ir2;
+                return;
+            }
+            if (!own && !(r2 < prm.cutoffsq)) return;
+            double x = r2 * prm.xi2;
+            double emx = fte_expm(x, etab);
+            double A;
+            if (small_x) {
+                double tt = fma(2.0, x, -1.0);
+                double R = fte_e1_coef_r[FTE_E1_DEG_R];
 #pragma unroll
-                for (int v = 0; v < NV; v++) {
-                    const double* d = den + (size_t)v * 4 * cap + s;
-                    double s11 = d[0], h = d[cap], s22 = d[2 * cap], tr = d[3 * cap];
-                    double u = fma(dx, s11, dy * h);  // (S r)_1 with S symmetrised
-                    double w = fma(dy, s22, dx * h);  // (S r)_2
-                    double Q = fma(dx, u, dy * w);    // r.S.r
-                    double fQ = facb * Q;
-                    double w1 = fma(dx, tr, u + u);   // f_1 (r.n) + n_1 (r.f) + (f.n) r_1
-                    double w2 = fma(dy, tr, w + w);
-                    acc[v][0] = fma(e2, fma(fQ, dx, prm.pf * w1), acc[v][0]);
-                    acc[v][1] = fma(e2, fma(fQ, dy, prm.pf * w2), acc[v][1]);
+                for (int k = FTE_E1_DEG_R - 1; k >= 0; k--) R = fma(R, tt, fte_e1_coef_r[k]);
+                double E = fma(x, R, -FTE_EULER - log(x));
+                A = fma(0.5, E, -emx);
+            } else {
+                A = emx * fte_kfun(x, ktab);
+            }
+            double gr = emx * fte_rcp(r2);
+#pragma unroll
+            for (int v = 0; v < NV; v++) {
+                const double* d = den + (size_t)v * 2 * cap + s;
+                double fx = d[0], fy = d[cap];
+                double c = gr * fma(dx, fx, dy * fy);
+                double a0, a1;
+                acc_get(tag, v, a0, a1);
+                a0 = fma(A, fx, fma(c, dx, a0));
+                a1 = fma(A, fy, fma(c, dy, a1));
+                acc_put(tag, v, a0, a1);
+            }
+        };
+        // stresslet pair (mex_stokes_dlp_real.cpp:117-138 / 162-181):
+        //   u_i += e^-x [ -4 (1+x) r_i (r.S.r)/r^4 + 2 xi^2 (f_i (r.n) + n_i (r.f) + (f.n) r_i) ]
+        auto eval_dlp = [&](int ent) {
+            const int s = ent >> 2, tag = ent & 3;
+            const double2 tp = tsl[tag];
+            double dx = tp.x - sx[s], dy = tp.y - sy[s];
+            double r2 = fma(dx, dx, dy * dy);
+            bool own = s < own_lim;
+            if (own ? (r2 == 0.0) : !(r2 < prm.cutoffsq)) return;
+            double x = r2 * prm.xi2;
+            double e2 = fte_expm(x, etab);
+            double ir2 = fte_rcp(r2);
+            double facb = -4.0 * (1.0 + x) * ir2 * ir2;
+#pragma unroll
+            for (int v = 0; v < NV; v++) {
+                const double* d = den + (size_t)v * 4 * cap + s;
+                double s11 = d[0], h = d[cap], s22 = d[2 * cap], tr = d[3 * cap];
+                double u = fma(dx, s11, dy * h);  // (S r)_1 with S symmetrised
+                double w = fma(dy, s22, dx * h);  // (S r)_2
+                double Q = fma(dx, u, dy * w);    // r.S.r
+                double fQ = facb * Q;
+                double w1 = fma(dx, tr, u + u);   // f_1 (r.n) + n_1 (r.f) + (f.n) r_1
+                double w2 = fma(dy, tr, w + w);
+                double a0, a1;
+                acc_get(tag, v, a0, a1);
+                a0 = fma(e2, fma(fQ, dx, prm.pf * w1), a0);
+                a1 = fma(e2, fma(fQ, dy, prm.pf * w2), a1);
+                acc_put(tag, v, a0, a1);
+            }
+        };
+
+        // evaluate everything pending in ring qf (if df) and qn (if dn);
+        // both hold fewer than 32 entries here
+        auto drain = [&](bool df, bool dn) {
+            const int cf = df ? Pf - Ef : 0, cn = dn ? Pn - En : 0;
+            if (KIND == FTE_KIND_SLP) {
+                // the two rings share one pass when they fit in a warp
+                if (cf + cn <= 32) {
+                    if (lane < cf)
+                        eval_slp(qf[(Ef + lane) & (kQueue - 1)], false);
+                    else if (lane < cf + cn)
+                        eval_slp(qn[(En + lane - cf) & (kQueue - 1)], true);
+                } else {
+                    if (lane < cf) eval_slp(qf[(Ef + lane) & (kQueue - 1)], false);
+                    if (lane < cn) eval_slp(qn[(En + lane) & (kQueue - 1)], true);
                 }
-            };
+            } else {
+                if (lane < cf) eval_dlp(qf[(Ef + lane) & (kQueue - 1)]);
+            }
+            Ef += cf;
+            En += cn;
+            __syncwarp();
+        };
+
+        // target kk of this warp: finish its pairs, reduce its slot, store
+        auto finalize = [&](int kk) {
+            const int sl = kk & (NSLOT - 1);
+            int tf = tailF[0], tn = tailN[0];
+#pragma unroll
+            for (int j = 1; j < NSLOT; j++)
+                if (sl == j) tf = tailF[j], tn = tailN[j];
+            const bool df = Ef < tf, dn = En < tn;
+            if (df || dn) drain(df, dn);
+            const int oi = prm.tidx[t0 + warp + kk * kNearWarps];
+            const bool hi = (lane & 16) != 0;
+#pragma unroll
+            for (int v = 0; v < NV; v++) {
+                double a0, a1;
+                acc_get(sl, v, a0, a1);
+                // lanes 0-15 reduce component 0, lanes 16-31 component 1
+                double keep = hi ? a1 : a0;
+                keep += __shfl_xor_sync(0xffffffffu, hi ? a0 : a1, 16);
+#pragma unroll
+                for (int o = 8; o > 0; o >>= 1) keep += __shfl_xor_sync(0xffffffffu, keep, o);
+                if ((lane & 15) == 0) {
+                    const double val = (keep + (double)fsw[(sl * NV + v) * 2 + (hi ? 1 : 0)]) * inv4pi;
+                    double* o = reinterpret_cast<double*>(prm.ur + v * prm.ustride + oi) + (hi ? 1 : 0);
+                    if (chunk == 0)
+                        *o = val;
+                    else
+                        *o += val;
+                }
+                acc_put(sl, v, 0.0, 0.0);
+            }
+        };
+
+        for (int k = 0; k < ntw; k++) {
+            const int slot = k & (NSLOT - 1);
+            const double2 tp = prm.tpos[t0 + warp + k * kNearWarps];
+            if (lane == 0) tsl[slot] = tp;
+            __syncwarp();
+            tx32 = (float)(tp.x - cx);
+            ty32 = (float)(tp.y - cy);
+            int hs = 0, cs = 0;  // FP32-class ring head and count
 
             for (int base = 0; base < clen; base += 32) {
                 int s = base + lane;
@@ -439,78 +548,68 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
                         __syncwarp();
                     }
                 }
+                const int ent = (s << 2) | slot;
                 if (KIND == FTE_KIND_SLP) {
                     bool pf_ = pass && !small_x, pn_ = pass && small_x;
                     unsigned mf = __ballot_sync(0xffffffffu, pf_);
                     unsigned mn = __ballot_sync(0xffffffffu, pn_);
-                    if (pf_) qf[(hf + cf + __popc(mf & lt_mask)) & (kQueue - 1)] = s;
-                    if (pn_) qn[(hn + cn + __popc(mn & lt_mask)) & (kQueue - 1)] = s;
-                    cf += __popc(mf);
-                    cn += __popc(mn);
+                    if (pf_) qf[(Pf + __popc(mf & lt_mask)) & (kQueue - 1)] = ent;
+                    if (pn_) qn[(Pn + __popc(mn & lt_mask)) & (kQueue - 1)] = ent;
+                    Pf += __popc(mf);
+                    Pn += __popc(mn);
                     __syncwarp();
-                    if (cf >= 32) {
-                        eval_slp(qf[(hf + lane) & (kQueue - 1)], false);
-                        hf = (hf + 32) & (kQueue - 1);
-                        cf -= 32;
+                    if (Pf - Ef >= 32) {
+                        eval_slp(qf[(Ef + lane) & (kQueue - 1)], false);
+                        Ef += 32;
                         __syncwarp();
                     }
-                    if (cn >= 32) {
-                        eval_slp(qn[(hn + lane) & (kQueue - 1)], true);
-                        hn = (hn + 32) & (kQueue - 1);
-                        cn -= 32;
+                    if (Pn - En >= 32) {
+                        eval_slp(qn[(En + lane) & (kQueue - 1)], true);
+                        En += 32;
                         __syncwarp();
                     }
                 } else {
                     unsigned mf = __ballot_sync(0xffffffffu, pass);
-                    if (pass) qf[(hf + cf + __popc(mf & lt_mask)) & (kQueue - 1)] = s;
-                    cf += __popc(mf);
+                    if (pass) qf[(Pf + __popc(mf & lt_mask)) & (kQueue - 1)] = ent;
+                    Pf += __popc(mf);
                     __syncwarp();
-                    if (cf >= 32) {
-                        eval_dlp(qf[(hf + lane) & (kQueue - 1)]);
-                        hf = (hf + 32) & (kQueue - 1);
-                        cf -= 32;
+                    if (Pf - Ef >= 32) {
+                        eval_dlp(qf[(Ef + lane) & (kQueue - 1)]);
+                        Ef += 32;
                         __syncwarp();
                     }
                 }
             }
-            if (KIND == FTE_KIND_SLP) {
-                // the two partial rings share one pass when they fit in a warp
-                if (cf + cn <= 32) {
-                    if (lane < cf)
-                        eval_slp(qf[(hf + lane) & (kQueue - 1)], false);
-                    else if (lane < cf + cn)
-                        eval_slp(qn[(hn + lane - cf) & (kQueue - 1)], true);
-                } else {
-                    if (lane < cf) eval_slp(qf[(hf + lane) & (kQueue - 1)], false);
-                    if (lane < cn) eval_slp(qn[(hn + lane) & (kQueue - 1)], true);
-                }
-            } else {
-                if (lane < cf) eval_dlp(qf[(hf + lane) & (kQueue - 1)]);
-            }
+            // the target's FP32 class: last partial batch, then its sums
+            // (lanes 0-15 reduce component 0, lanes 16-31 component 1)
             if (lane < cs) {
                 if (KIND == FTE_KIND_SLP)
                     eval_slp32(qs[(hs + lane) & (kQueue - 1)]);
                 else
                     eval_dlp32(qs[(hs + lane) & (kQueue - 1)]);
             }
-            __syncwarp();
+            {
+                const bool hi = (lane & 16) != 0;
 #pragma unroll
-            for (int v = 0; v < NV; v++) {
-                acc[v][0] += (double)acc32[v][0];
-                acc[v][1] += (double)acc32[v][1];
-                double a0 = warp_sum(acc[v][0]), a1 = warp_sum(acc[v][1]);
-                if (lane == 0) {
-                    double2* o = prm.ur + v * prm.ustride + prm.tidx[t0 + t];
-                    double2 val = make_double2(a0 * inv4pi, a1 * inv4pi);
-                    if (chunk == 0) {
-                        *o = val;
-                    } else {
-                        double2 old = *o;
-                        *o = make_double2(old.x + val.x, old.y + val.y);
-                    }
+                for (int v = 0; v < NV; v++) {
+                    float keep = hi ? acc32[v][1] : acc32[v][0];
+                    keep += __shfl_xor_sync(0xffffffffu, hi ? acc32[v][0] : acc32[v][1], 16);
+#pragma unroll
+                    for (int o = 8; o > 0; o >>= 1) keep += __shfl_xor_sync(0xffffffffu, keep, o);
+                    if ((lane & 15) == 0) fsw[(slot * NV + v) * 2 + (hi ? 1 : 0)] = keep;
+                    acc32[v][0] = acc32[v][1] = 0.0f;
                 }
             }
+#pragma unroll
+            for (int j = 0; j < NSLOT; j++)
+                if (slot == j) tailF[j] = Pf, tailN[j] = Pn;
+            // the oldest target in flight gives up its slot to target k + 1
+            if (k >= NSLOT - 1) finalize(k - (NSLOT - 1));
         }
+        // end of the chunk: evaluate what the rings hold, store the rest
+        if (Pf > Ef || Pn > En) drain(true, true);
+        for (int kk = ntw - (NSLOT - 1) > 0 ? ntw - (NSLOT - 1) : 0; kk < ntw; kk++) finalize(kk);
+        __syncwarp();
     }
 }
 
