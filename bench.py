@@ -339,8 +339,9 @@ def batched_section(ft, wl, ctx, stream, steps, warmup, flush):
         "speedup_vs_plain_loop": loop_ms / graph_ms,
         "setup_s": setup_s, "gpu_launches_per_step": launches,
         "max_rel_diff_vs_plain_loop": worst,
-        "tiles_spread_gather": tiles, "kspace_forms": {("fp32" if k == ft.FORM_MIXED else "fp64"): v
-                                                       for k, v in forms.items()},
+        "tiles_spread_gather": tiles,
+        "kspace_forms": {{ft.FORM_MIXED: "fp32", ft.FORM_FF: "float-float"}.get(k, "fp64"): v
+                         for k, v in forms.items()},
         "e2e": {"targets_per_s": targets_per_step / (e2e_ms / 1e3), "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "l2": "flushed before every step",

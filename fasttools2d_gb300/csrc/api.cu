@@ -720,6 +720,7 @@ void pick_grid(int A, int B, int kinf, int* Mx, int* My) {
 static const double kCostPair = 0.094e-9;      // one FP64 near pair
 static const double kCostWin64 = 3.2e-12;      // one window node x grid, FP64 spread/gather
 static const double kCostWin32 = 1.2e-12;      // same in FP32 with compensation
+static const double kCostWinFF = 1.0e-12;      // same in float-float (FP32 pipe), window records included
 static const double kCostFft64 = 3.5e-11;      // per complex grid point x log2(points), 7-smooth FP64
 static const double kCostFft32 = 1.2e-11;      // same in FP32
 // Calibration of the tuned choice against converged FP64 sums on 2000
@@ -731,6 +732,9 @@ static const double kCostFft32 = 1.2e-11;      // same in FP32
 static const double kTolSlack[2] = {1.0, 3.0};
 static const double kWinRatio[2] = {3000.0, 300.0};
 static const double kFp32Floor[2] = {1e-6, 2e-7};
+// float-float spread and gather (~48-bit values) hold their ~1e-13 relative
+// error well below tolerances from 1e-11 up
+static const double kFfFloor[2] = {1e-11, 1e-11};
 
 static int choose_params_tuned(int kind, int64_t nsrc, int64_t ntar, double Q, double Lx, double Ly,
                                const fte_options* opt, fte_params* o) {
@@ -738,7 +742,13 @@ static int choose_params_tuned(int kind, int64_t nsrc, int64_t ntar, double Q, d
     FTE_TRY(choose_params_q(kind, nsrc, ntar, Q, Lx, Ly, opt, o));
     const double tol = o->tol;
     const double tol_e = tol * (opt && opt->slack > 0 ? opt->slack : kTolSlack[kind]);
+    const int force = opt ? opt->kspace : FTE_KSPACE_AUTO;
+    if (force < FTE_KSPACE_AUTO || force > FTE_KSPACE_FF) {
+        fte_set_error("unknown k-space arithmetic %d", force);
+        return FTE_ERR_INVALID;
+    }
     const bool fp32 = tol >= kFp32Floor[kind];
+    const bool ffok = tol >= kFfFloor[kind];
     int P = opt && opt->P > 0 ? opt->P : 0;
     if (P == 0) {
         for (P = 4; P < 24; P += 2) {
@@ -772,14 +782,28 @@ static int choose_params_tuned(int kind, int64_t nsrc, int64_t ntar, double Q, d
         if ((double)Mx * My > 4.0e8) continue;  // 4 grids of 4e8 nodes: 13 GB
         if (P + 1 > Mx || P + 1 > My) continue;
         // FP32 k-space where the tolerance allows it and lines fit a block
-        // transform; FP64 lines longer than a block take the long transform
-        const bool f32 = fp32 && fte_fft_fits_block(Mx, 8) && fte_fft_fits_block(My, 8);
+        // transform, else float-float spread and gather where the tolerance
+        // allows, else FP64; FP64 lines longer than a block take the long
+        // transform
+        const bool fits32 = fte_fft_fits_block(Mx, 8) && fte_fft_fits_block(My, 8);
+        int kf;
+        if (force == FTE_KSPACE_FP32) {
+            if (!fits32) continue;
+            kf = FTE_FORM_MIXED;
+        } else if (force == FTE_KSPACE_FF) {
+            kf = FTE_FORM_FF;
+        } else if (force == FTE_KSPACE_FP64) {
+            kf = FTE_FORM_PLAIN;
+        } else {
+            kf = fp32 && fits32 ? FTE_FORM_MIXED : (ffok ? FTE_FORM_FF : FTE_FORM_PLAIN);
+        }
+        const bool f32 = kf == FTE_FORM_MIXED;
         const bool long64 = !f32 && (!fte_fft_fits_block(Mx, 16) || !fte_fft_fits_block(My, 16));
         double pairs = (double)nsrc * (double)ntar * FTE_PI * rc * rc / area * 1.03;
         double win = (double)(P + 1) * (P + 1) * ((double)nsrc * ng + (double)ntar * 2);
         double pts = (double)Mx * My;
         double fftw = fft_work(Mx, My);
-        double cost = kCostPair * pairs + (f32 ? kCostWin32 : kCostWin64) * win +
+        double cost = kCostPair * pairs + (f32 ? kCostWin32 : (kf == FTE_FORM_FF ? kCostWinFF : kCostWin64)) * win +
                       (f32 ? kCostFft32 : kCostFft64) * (long64 ? 2.5 : 1.0) * nfft * fftw;
         if (cost < best) {
             best = cost;
@@ -795,7 +819,7 @@ static int choose_params_tuned(int kind, int64_t nsrc, int64_t ntar, double Q, d
             double m = 0.95 * std::sqrt(FTE_PI * P);
             bestp.w = P * Lx / Mx / 2;
             bestp.eta = (2 * xi * bestp.w / m) * (2 * xi * bestp.w / m);
-            best_form = f32 ? FTE_FORM_MIXED : FTE_FORM_PLAIN;
+            best_form = kf;
         }
         if (opt && opt->nside_x > 0) break;
     }
@@ -1358,7 +1382,7 @@ static int ewald_entry(fte_context* c, int kind, const double* xsrc, const doubl
     FTE_TRY(check_kspace_params(prm.xi, prm.eta, prm.Mx, prm.My, Lx, Ly, prm.w, prm.P));
     // second workspace: cell list, grids and outputs (the staged point data stays in the first)
     size_t need = fte_cells_ws(nsrc, ntar, prm.nside_x * prm.nside_y) +
-                  fte_kspace_ws(kind, FTE_FORM_PLAIN, prm.Mx, prm.My, nsrc, ntar) + ws_bytes(2 * (ntar + 1), 8) * 3 + 8192;
+                  fte_kspace_ws(kind, prm.form, prm.Mx, prm.My, nsrc, ntar) + ws_bytes(2 * (ntar + 1), 8) * 3 + 8192;
     FTE_TRY(fte_ws2_reserve(c, need));
     WsCarver wc2{c->ws2, 0, c->ws2_size};
     FTE_TRY(fte_record(c, 1));

@@ -286,6 +286,8 @@ struct KspaceArgs {
     int ts_spread = 0, ts_gather = 0;
 };
 size_t fte_kspace_ws(int kind, int form, int Mx, int My, int64_t nsrc, int64_t ntar);
+// float-float form: bytes of the sources' window records (0 for the other forms)
+size_t fte_kspace_rec_ws(int form, int64_t nsrc);
 // build the spread/gather tile bins that fte_kspace_run would build for `a`
 int fte_kspace_tiles(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, TileBins* src, TileBins* tar);
 int fte_kspace_run(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, fte_info* info);

@@ -1111,6 +1111,285 @@ __global__ void k_filter32(float2* __restrict__ Hh, int Mx, int My, double Lx, d
     }
 }
 
+// ===========================================================================
+// Float-float k-space (FTE_FORM_FF): the spread and the gather carry every
+// window weight, density and grid value as an unevaluated sum hi + lo of two
+// FP32 numbers (about 48 significant bits) and do their arithmetic on the
+// FP32 pipe, which GB300 runs at 64 times its FP64 rate: products by the
+// FMA-based exact product (Dekker 1971, "A floating-point technique for
+// extending the available precision"), sums by Knuth's two-sum.  The
+// transforms and the filter stay FP64.  Per-point window factors are formed
+// once in FP64 (the reference's closest node and four exponentials,
+// ewald_tools.cpp:86-114, 182-190), rounded to float-float, and the window
+// rows by float-float recurrences; relative error ~1e-13 against FP64.
+// ===========================================================================
+__device__ __forceinline__ float2 ff_split(double v) {
+    const float hi = __double2float_rn(v);
+    return make_float2(hi, __double2float_rn(v - (double)hi));
+}
+__device__ __forceinline__ double ff_join(float s, float c) { return (double)s + (double)c; }
+// a b rounded to a normalised pair (error below ~2^-46 |a b|)
+__device__ __forceinline__ float2 ff_mul(float2 a, float2 b) {
+    const float p = __fmul_rn(a.x, b.x);
+    float e = __fmaf_rn(a.x, b.x, -p);
+    e = __fmaf_rn(a.x, b.y, e);
+    e = __fmaf_rn(a.y, b.x, e);
+    const float s = __fadd_rn(p, e);
+    return make_float2(s, __fsub_rn(e, __fsub_rn(s, p)));
+}
+// (s, c) += a b; s holds the running sum, c the collected low-order parts
+__device__ __forceinline__ void ff_mac(float2 a, float2 b, float& s, float& c) {
+    const float p = __fmul_rn(a.x, b.x);
+    float e = __fmaf_rn(a.x, b.x, -p);
+    e = __fmaf_rn(a.x, b.y, e);
+    e = __fmaf_rn(a.y, b.x, e);
+    const float t = __fadd_rn(s, p);
+    const float bp = __fsub_rn(t, s);
+    const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+    s = t;
+    c = __fadd_rn(c, __fadd_rn(err, e));
+}
+__device__ __forceinline__ float2 ff_norm(float s, float c) {
+    const float h = __fadd_rn(s, c);
+    return make_float2(h, __fsub_rn(c, __fsub_rn(h, s)));
+}
+
+// per-source window record in tile order (64 bytes)
+struct FfWin {
+    int mx, my;            // first window node
+    float2 e0, ex3, ey3;   // ex e4y, e3x, e3y (float-float)
+    float2 q[4];           // densities of the grids (SLP: f1, f2; DLP: f1 n1, f2 n1, f1 n2, f2 n2), weights folded in
+};
+static_assert(sizeof(FfWin) == 64, "FfWin layout");
+
+__device__ __forceinline__ void load_e1_ff(float2* e1, const WinParams& wp) {
+    double t0 = -2 * wp.xi * wp.xi / wp.eta * wp.h * wp.h;
+    for (int j = threadIdx.x; j <= wp.P; j += blockDim.x) {
+        int jj = j - wp.P / 2;
+        e1[j] = ff_split(exp(t0 * jj * jj));
+    }
+}
+
+// window records of the sources in tile order (k indexes perm)
+__global__ void k_ff_win(int kind, const double* __restrict__ p, const double* __restrict__ f,
+                         const double* __restrict__ nrm, const double* __restrict__ wts, const int* __restrict__ perm,
+                         int64_t n, WinParams wp, FfWin* __restrict__ out) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        const int i = perm[k];
+        Win wn = window_of(p[2 * i], p[2 * i + 1], wp);
+        FfWin r;
+        r.mx = wn.mx;
+        r.my = wn.my;
+        r.e0 = ff_split(wn.ex * wn.e4y);
+        r.ex3 = ff_split(wn.e3x);
+        r.ey3 = ff_split(wn.e3y);
+        double f1 = f[2 * i], f2 = f[2 * i + 1];
+        if (wts) {
+            f1 *= wts[i];
+            f2 *= wts[i];
+        }
+        if (kind == FTE_KIND_SLP) {
+            r.q[0] = ff_split(f1);
+            r.q[1] = ff_split(f2);
+            r.q[2] = r.q[3] = make_float2(0.f, 0.f);
+        } else {
+            const double n1 = nrm[2 * i], n2 = nrm[2 * i + 1];
+            r.q[0] = ff_split(f1 * n1);
+            r.q[1] = ff_split(f2 * n1);
+            r.q[2] = ff_split(f1 * n2);
+            r.q[3] = ff_split(f2 * n2);
+        }
+        out[k] = r;
+    }
+}
+
+// Column-owned spread of grids (2 pass, 2 pass + 1) in float-float: the
+// scheme of k_spread_cols (warp w adds every region column c = w mod warps,
+// lane j window row j) with pairs in shared memory; the region is flushed
+// to the FP64 grids.
+__global__ void __launch_bounds__(kColThreads) k_spread_ff(int pass, const FfWin* __restrict__ recs,
+                                                          const int* __restrict__ toff, int ts, int ntx, int nty,
+                                                          WinParams wp, double* __restrict__ H0,
+                                                          double* __restrict__ H1) {
+    extern __shared__ __align__(16) unsigned char shraw[];
+    float2* shf = reinterpret_cast<float2*>(shraw);
+    const int P1 = wp.P + 1, W = tile_region(ts, wp.P), WW = W * W;
+    const int P1e = (P1 + 1) & ~1;
+    float2* buf = shf;                      // 2 * WW
+    float2* e1 = buf + 2 * WW;              // P1e
+    float2* fw = e1 + P1e;                  // kColChunk * 2 * P1
+    float2* wy = fw + kColChunk * 2 * P1;   // kColChunk * P1
+    int* org = reinterpret_cast<int*>(wy + kColChunk * P1);  // kColChunk * 2 (lx, ly)
+    load_e1_ff(e1, wp);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int tile = blockIdx.x; tile < ntx * nty; tile += gridDim.x) {
+        const int k0 = toff[tile], k1 = toff[tile + 1];
+        if (k0 == k1) continue;
+        const int ox = (tile % ntx) * ts - wp.P / 2 - 2, oy = (tile / ntx) * ts - wp.P / 2 - 2;
+        __syncthreads();
+        for (int i = threadIdx.x; i < 2 * WW; i += blockDim.x) buf[i] = make_float2(0.f, 0.f);
+        for (int c0 = k0; c0 < k1; c0 += kColChunk) {
+            const int cn = min(kColChunk, k1 - c0);
+            __syncthreads();
+            // window rows (warp 0) and density-weighted columns (warp 1) of
+            // the chunk's sources
+            if (warp == 0 && lane < cn) {
+                const FfWin& r = recs[c0 + lane];
+                const float2 e3 = r.ey3;
+                float2 ey = make_float2(1.f, 0.f);
+                for (int j = 0; j < P1; j++) {
+                    wy[lane * P1 + j] = ff_mul(e1[j], ey);
+                    ey = ff_mul(ey, e3);
+                }
+                org[2 * lane] = r.mx - ox;
+                org[2 * lane + 1] = r.my - oy;
+            } else if (warp == 1 && lane < cn) {
+                const FfWin& r = recs[c0 + lane];
+                const float2 e3 = r.ex3, q0 = r.q[2 * pass], q1 = r.q[2 * pass + 1];
+                float2 ex = r.e0;
+                float2* fa = fw + (lane * 2) * P1;
+                for (int a = 0; a < P1; a++) {
+                    const float2 wxa = ff_mul(ex, e1[a]);
+                    fa[a] = ff_mul(q0, wxa);
+                    fa[P1 + a] = ff_mul(q1, wxa);
+                    ex = ff_mul(ex, e3);
+                }
+            }
+            __syncthreads();
+            for (int s = 0; s < cn; s++) {
+                const int lx = org[2 * s], ly = org[2 * s + 1];
+                const bool inside = lx >= 0 && ly >= 0 && lx + wp.P < W && ly + wp.P < W;
+                // first column >= lx owned by this warp
+                int c = lx + ((warp - lx) % nw + nw) % nw;
+                if (lane < P1) {
+                    const float2 wyj = wy[s * P1 + lane];
+                    const float2* fa = fw + (s * 2) * P1;
+                    const float2* fb = fa + P1;
+                    if (inside) {
+                        for (; c <= lx + wp.P; c += nw) {
+                            float2* b0 = buf + c * W + ly + lane;
+                            float2 v0 = b0[0], v1 = b0[WW];
+                            ff_mac(fa[c - lx], wyj, v0.x, v0.y);
+                            ff_mac(fb[c - lx], wyj, v1.x, v1.y);
+                            b0[0] = v0;
+                            b0[WW] = v1;
+                        }
+                    } else {
+                        // window outside the region: straight into the global grids
+                        const size_t row = fte_wrap_index(oy + ly + lane, wp.My);
+                        for (; c <= lx + wp.P; c += nw) {
+                            const size_t at = (size_t)fte_wrap_index(ox + c, wp.Mx) * wp.My + row;
+                            const float2 p0 = ff_mul(fa[c - lx], wyj), p1 = ff_mul(fb[c - lx], wyj);
+                            atomicAdd(&H0[at], ff_join(p0.x, p0.y));
+                            atomicAdd(&H1[at], ff_join(p1.x, p1.y));
+                        }
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < 2 * WW; idx += blockDim.x) {
+            const float2 v = buf[idx];
+            if (v.x == 0.f && v.y == 0.f) continue;
+            int g = idx >= WW, r = idx - g * WW;
+            int xx = r / W, yy = r - xx * W;
+            size_t at = (size_t)fte_wrap_index(ox + xx, wp.Mx) * wp.My + fte_wrap_index(oy + yy, wp.My);
+            atomicAdd(g ? &H1[at] : &H0[at], ff_join(v.x, v.y));
+        }
+    }
+}
+
+size_t spread_ff_smem(int ts, int P) {
+    const int P1 = P + 1, W = tile_region(ts, P);
+    return (size_t)(2 * W * W + ((P1 + 1) & ~1) + kColChunk * 3 * P1) * sizeof(float2) + kColChunk * 2 * sizeof(int);
+}
+
+// FP64 grid values -> float-float pairs, in place
+__global__ void k_ff_split(double* __restrict__ H, int64_t n) {
+    float2* o = reinterpret_cast<float2*>(H);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double v = H[i];
+        o[i] = ff_split(v);
+    }
+}
+
+// Tiled gather in float-float from grids of pairs: a thread per target, the
+// tile's region of both grids staged once in shared memory.
+__global__ void __launch_bounds__(kTileThreads) k_gather_ff(const double* __restrict__ p, const int* __restrict__ toff,
+                                                           const int* __restrict__ perm, int ts, int ntx, int nty,
+                                                           WinParams wp, const float2* __restrict__ G0,
+                                                           const float2* __restrict__ G1, double scale,
+                                                           double2* __restrict__ out) {
+    extern __shared__ __align__(16) unsigned char shraw[];
+    float2* shf = reinterpret_cast<float2*>(shraw);
+    const int P1 = wp.P + 1, W = tile_region(ts, wp.P), WW = W * W;
+    float2* r0 = shf;
+    float2* r1 = r0 + WW;
+    float2* e1 = r1 + WW;
+    float2* wyb = e1 + ((P1 + 1) & ~1) + threadIdx.x * P1;
+    load_e1_ff(e1, wp);
+    for (int tile = blockIdx.x; tile < ntx * nty; tile += gridDim.x) {
+        const int k0 = toff[tile], k1 = toff[tile + 1];
+        if (k0 == k1) continue;
+        const int ox = (tile % ntx) * ts - wp.P / 2 - 2, oy = (tile / ntx) * ts - wp.P / 2 - 2;
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < WW; idx += blockDim.x) {
+            int xx = idx / W, yy = idx - xx * W;
+            size_t at = (size_t)fte_wrap_index(ox + xx, wp.Mx) * wp.My + fte_wrap_index(oy + yy, wp.My);
+            r0[idx] = G0[at];
+            r1[idx] = G1[at];
+        }
+        __syncthreads();
+        for (int k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
+            const int i = perm[k];
+            Win wn = window_of(p[2 * i], p[2 * i + 1], wp);
+            {
+                const float2 e3 = ff_split(wn.e3y);
+                float2 ey = make_float2(1.f, 0.f);
+                for (int j = 0; j < P1; j++) {
+                    wyb[j] = ff_mul(e1[j], ey);
+                    ey = ff_mul(ey, e3);
+                }
+            }
+            const float2 e3x = ff_split(wn.e3x);
+            float2 ex = ff_split(wn.ex * wn.e4y);
+            const int lx = wn.mx - ox, ly = wn.my - oy;
+            float a0 = 0.f, c0 = 0.f, a1 = 0.f, c1 = 0.f;
+            const bool inside = lx >= 0 && ly >= 0 && lx + wp.P < W && ly + wp.P < W;
+            for (int a = 0; a < P1; a++) {
+                const float2 wxa = ff_mul(ex, e1[a]);
+                ex = ff_mul(ex, e3x);
+                float s0 = 0.f, t0 = 0.f, s1 = 0.f, t1 = 0.f;
+                if (inside) {
+                    const float2* g0 = r0 + (lx + a) * W + ly;
+                    const float2* g1 = r1 + (lx + a) * W + ly;
+                    for (int j = 0; j < P1; j++) {
+                        const float2 w = wyb[j];
+                        ff_mac(w, g0[j], s0, t0);
+                        ff_mac(w, g1[j], s1, t1);
+                    }
+                } else {
+                    const size_t base = (size_t)fte_wrap_index(wn.mx + a, wp.Mx) * wp.My;
+                    for (int j = 0; j < P1; j++) {
+                        const size_t at = base + fte_wrap_index(wn.my + j, wp.My);
+                        const float2 w = wyb[j];
+                        ff_mac(w, G0[at], s0, t0);
+                        ff_mac(w, G1[at], s1, t1);
+                    }
+                }
+                ff_mac(wxa, ff_norm(s0, t0), a0, c0);
+                ff_mac(wxa, ff_norm(s1, t1), a1, c1);
+            }
+            out[i] = make_double2(ff_join(a0, c0) * scale, ff_join(a1, c1) * scale);
+        }
+    }
+}
+
+size_t gather_ff_smem(int ts, int P) {
+    const int P1 = P + 1, W = tile_region(ts, P);
+    return 2 * (size_t)W * W * sizeof(float2) + (size_t)(((P1 + 1) & ~1) + kTileThreads * P1) * sizeof(float2);
+}
+
 // ---- tile sizes -------------------------------------------------------------
 // Spread and gather tiles are ts x ts grid nodes (ts >= 8); a tile's shared-
 // memory region (ts + P + 4 nodes a side) must fit the two-CTAs-per-SM budget.
@@ -1122,12 +1401,14 @@ size_t gather64_smem(int ts, int P) {
 }
 bool spread_fits(const fte_context* ctx, int form, int ts, int P) {
     if (ts < 8 || ts > 256) return false;
-    size_t sm = form == FTE_FORM_MIXED ? spread_cols32_smem(ts, P) : spread_cols_smem(ts, P);
+    size_t sm = form == FTE_FORM_MIXED ? spread_cols32_smem(ts, P)
+                : (form == FTE_FORM_FF ? spread_ff_smem(ts, P) : spread_cols_smem(ts, P));
     return sm <= tile_budget(ctx);
 }
 bool gather_fits(const fte_context* ctx, int form, int ts, int P) {
     if (ts < 8 || ts > 256) return false;
-    size_t sm = form == FTE_FORM_MIXED ? gather32_smem(ts, P) : gather64_smem(ts, P);
+    size_t sm = form == FTE_FORM_MIXED ? gather32_smem(ts, P)
+                : (form == FTE_FORM_FF ? gather_ff_smem(ts, P) : gather64_smem(ts, P));
     return sm <= tile_budget(ctx);
 }
 int resolve_tiles(const fte_context* ctx, const KspaceArgs& a, int* ts_s, int* ts_g) {
@@ -1170,15 +1451,31 @@ WinParams win_params(const KspaceArgs& a) {
     return wp;
 }
 
-// tiled spread of all source grids (H holds ng grids of G nodes, FP64 or FP32)
-int launch_spread_tiled(fte_context* ctx, const KspaceArgs& a, const TileBins& tb, const WinParams& wp, void* H) {
+// tiled spread of all source grids (H holds ng grids of G nodes, FP64 or
+// FP32); the float-float form first writes the sources' window records to
+// recs (nsrc entries)
+int launch_spread_tiled(fte_context* ctx, const KspaceArgs& a, const TileBins& tb, const WinParams& wp, void* H,
+                        FfWin* recs) {
     const int ng = a.kind == FTE_KIND_SLP ? 2 : 4;
     const size_t G = (size_t)a.Mx * a.My;
     const bool f32 = a.form == FTE_FORM_MIXED;
     const size_t sm = f32 ? spread_cols32_smem(tb.ts, a.P) : spread_cols_smem(tb.ts, a.P);
     const int nt = tb.ntx * tb.nty;
     const int grid = nt < ctx->num_sms * 8 ? nt : ctx->num_sms * 8;
-    if (f32) {
+    if (a.form == FTE_FORM_FF) {
+        if (!recs) {
+            fte_set_error("internal: float-float spread without window records");
+            return FTE_ERR_INVALID;
+        }
+        double* Hd = static_cast<double*>(H);
+        const size_t smf = spread_ff_smem(tb.ts, a.P);
+        FTE_LAUNCH(ctx, k_ff_win, ew_grid(ctx, a.nsrc), 256, 0, a.kind, a.psrc, a.f, a.nrm, a.wts, (const int*)tb.perm,
+                   a.nsrc, wp, recs);
+        FTE_CUDA_TRY(cudaFuncSetAttribute(k_spread_ff, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smf));
+        for (int pass = 0; pass < ng / 2; pass++)
+            FTE_LAUNCH(ctx, k_spread_ff, grid, kColThreads, smf, pass, (const FfWin*)recs, (const int*)tb.off, tb.ts,
+                       tb.ntx, tb.nty, wp, Hd + 2 * pass * G, Hd + (2 * pass + 1) * G);
+    } else if (f32) {
         float* Hf = static_cast<float*>(H);
         FTE_CUDA_TRY(cudaFuncSetAttribute(k_spread_cols32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
         for (int pass = 0; pass < ng / 2; pass++) {
@@ -1200,13 +1497,20 @@ int launch_spread_tiled(fte_context* ctx, const KspaceArgs& a, const TileBins& t
     return FTE_OK;
 }
 
-// tiled gather of the two velocity grids at the targets
+// tiled gather of the two velocity grids at the targets (the float-float
+// form reads grids already split into pairs)
 int launch_gather_tiled(fte_context* ctx, const KspaceArgs& a, const TileBins& tb, const WinParams& wp,
                         const void* H, double scale) {
     const size_t G = (size_t)a.Mx * a.My;
     const int nt = tb.ntx * tb.nty;
     const int grid = nt < ctx->num_sms * 8 ? nt : ctx->num_sms * 8;
-    if (a.form == FTE_FORM_MIXED) {
+    if (a.form == FTE_FORM_FF) {
+        const float2* Hf = static_cast<const float2*>(H);
+        size_t sm = gather_ff_smem(tb.ts, a.P);
+        FTE_CUDA_TRY(cudaFuncSetAttribute(k_gather_ff, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        FTE_LAUNCH(ctx, k_gather_ff, grid, kTileThreads, sm, a.ptar, (const int*)tb.off, (const int*)tb.perm, tb.ts,
+                   tb.ntx, tb.nty, wp, Hf, Hf + G, scale, a.uk);
+    } else if (a.form == FTE_FORM_MIXED) {
         const float* Hf = static_cast<const float*>(H);
         size_t sm = gather32_smem(tb.ts, a.P);
         FTE_CUDA_TRY(cudaFuncSetAttribute(k_gather_tiled32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
@@ -1269,7 +1573,7 @@ int kspace_run_mixed(fte_context* ctx, WsCarver& wc, const KspaceArgs& a) {
     }
     FTE_TRY(fte_record(ctx, 2));
     FTE_CUDA_TRY(cudaMemsetAsync(H, 0, sizeof(float) * ng * G, ctx->stream));
-    if (a.nsrc > 0) FTE_TRY(launch_spread_tiled(ctx, a, tb_s, wp, H));
+    if (a.nsrc > 0) FTE_TRY(launch_spread_tiled(ctx, a, tb_s, wp, H, nullptr));
     FTE_TRY(fte_record(ctx, 3));
     FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_y_r2c32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_y));
     FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_y_c2r32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_y));
@@ -1346,6 +1650,7 @@ int fte_kspace_tune(fte_context* ctx, void* grid, WsCarver bins, KspaceArgs& a, 
         TileBins tb;
         rc = fte_tiles_build(ctx, w, a.psrc, a.nsrc, a.Lx, a.Ly, wp.h, ts, (a.Mx + ts - 1) / ts,
                              (a.My + ts - 1) / ts, &tb);
+        FfWin* recs = a.form == FTE_FORM_FF ? w.take<FfWin>(a.nsrc) : nullptr;
         if (!rc && !w.ok()) {
             fte_set_error("internal: tuner bin scratch too small");
             rc = FTE_ERR_ALLOC;
@@ -1355,7 +1660,7 @@ int fte_kspace_tune(fte_context* ctx, void* grid, WsCarver bins, KspaceArgs& a, 
             rc = time3(
                 [&]() -> int {
                     FTE_CUDA_TRY(cudaMemsetAsync(grid, 0, gbytes, ctx->stream));
-                    return launch_spread_tiled(ctx, a, tb, wp, grid);
+                    return launch_spread_tiled(ctx, a, tb, wp, grid, recs);
                 },
                 &ms);
         if (!rc && ms < best_s) {
@@ -1390,6 +1695,10 @@ int fte_kspace_tune(fte_context* ctx, void* grid, WsCarver bins, KspaceArgs& a, 
     return FTE_OK;
 }
 
+size_t fte_kspace_rec_ws(int form, int64_t nsrc) {
+    return form == FTE_FORM_FF ? ws_bytes((size_t)nsrc + 1, sizeof(FfWin)) : 0;
+}
+
 size_t fte_kspace_ws(int kind, int form, int Mx, int My, int64_t nsrc, int64_t ntar) {
     int ng = kind == FTE_KIND_SLP ? 2 : 4;
     size_t G = (size_t)Mx * My;
@@ -1397,7 +1706,7 @@ size_t fte_kspace_ws(int kind, int form, int Mx, int My, int64_t nsrc, int64_t n
     // tiles no smaller than 8 nodes
     int ntiles = ((Mx + 7) / 8) * ((My + 7) / 8);
     size_t s = ws_bytes(ng * G, sizeof(double)) + ws_bytes(ng * Gh, sizeof(double2)) + fte_tiles_ws(nsrc, ntiles) +
-               fte_tiles_ws(ntar, ntiles) + 4096;
+               fte_tiles_ws(ntar, ntiles) + fte_kspace_rec_ws(form, nsrc) + 4096;
     if (form != FTE_FORM_MIXED) {
         // long FP64 transforms: staging lines along y and the four-step scratch
         const bool ly = !fte_fft_fits_block(My, sizeof(double2)), lx = !fte_fft_fits_block(Mx, sizeof(double2));
@@ -1470,11 +1779,15 @@ int fte_kspace_run(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, fte_info
         fte_set_error("internal: prebuilt tiles do not match the FP64 tile sizes");
         return FTE_ERR_INVALID;
     }
+    // float-float form: window records of the sources (tiled spread only)
+    const bool ff = a.form == FTE_FORM_FF;
+    FfWin* recs = ff && a.nsrc > 0 && ts_s > 0 ? wc.take<FfWin>(a.nsrc) : nullptr;
+    FTE_WS_CHECK(wc);
 
     FTE_TRY(fte_record(ctx, 2));
     FTE_CUDA_TRY(cudaMemsetAsync(H, 0, sizeof(double) * ng * G, ctx->stream));
     if (a.nsrc > 0 && ts_s > 0) {
-        FTE_TRY(launch_spread_tiled(ctx, a, tb_s, wp, H));
+        FTE_TRY(launch_spread_tiled(ctx, a, tb_s, wp, H, recs));
     } else if (a.nsrc > 0) {
         if (ng == 2) {
             FTE_CUDA_TRY(cudaFuncSetAttribute(k_spread<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_pt));
@@ -1524,6 +1837,7 @@ int fte_kspace_run(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, fte_info
     FTE_TRY(fte_record(ctx, 4));
     const double scale = gather_scale(a);
     if (a.ntar > 0 && ts_g > 0) {
+        if (ff) FTE_LAUNCH(ctx, k_ff_split, ew_grid(ctx, 2LL * (long long)G), 256, 0, H, 2LL * (long long)G);
         FTE_TRY(launch_gather_tiled(ctx, a, tb_g, wp, H, scale));
     } else if (a.ntar > 0) {
         FTE_CUDA_TRY(cudaFuncSetAttribute(k_gather, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_pt));
@@ -1678,7 +1992,7 @@ int fte_q_kspace_run(fte_context* ctx, WsCarver& wc, int q, const KspaceArgs& a,
         FTE_TRY(fte_tiles_build(ctx, w2, a.psrc, a.nsrc, a.Lx, a.Ly, wp.h, ts_s, (Mx + ts_s - 1) / ts_s,
                                 (My + ts_s - 1) / ts_s, &tb));
         FTE_WS_CHECK(w2);
-        FTE_TRY(launch_spread_tiled(ctx, a, tb, wp, H));
+        FTE_TRY(launch_spread_tiled(ctx, a, tb, wp, H, nullptr));
     }
     // forward: ng grids
     if (!long_y) {

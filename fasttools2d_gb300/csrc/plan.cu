@@ -323,7 +323,7 @@ extern "C" int fte_plan_create(fte_context* c, int kind, const double* xsrc, con
     ka.Mx = prm.Mx;
     ka.My = prm.My;
     ka.P = prm.P;
-    p->kscratch_size = fte_kspace_ws(kind, prm.form, prm.Mx, prm.My, 0, 0) + (1 << 16);
+    p->kscratch_size = fte_kspace_ws(kind, prm.form, prm.Mx, prm.My, 0, 0) + fte_kspace_rec_ws(prm.form, nsrc) + (1 << 16);
     size_t need = 3 * ws_bytes(2 * (nsrc + 1), 8) + ws_bytes(2 * (ntar + 1), 8) + ws_bytes(nsrc + 1, 8) +
                   fte_cells_ws(nsrc, ntar, prm.nside_x * prm.nside_y) +
                   fte_kspace_ws(kind, prm.form, prm.Mx, prm.My, nsrc, ntar) + 3 * ws_bytes(nv * (nsrc + 1), 8) +
@@ -385,7 +385,7 @@ extern "C" int fte_plan_create(fte_context* c, int kind, const double* xsrc, con
         // the staged inputs are no longer needed: the context workspace holds
         // one candidate's tile bins at a time
         const int ntiles8 = ((prm.Mx + 7) / 8) * ((prm.My + 7) / 8);
-        const size_t bins = fte_tiles_ws(nsrc > ntar ? nsrc : ntar, ntiles8) + 4096;
+        const size_t bins = fte_tiles_ws(nsrc > ntar ? nsrc : ntar, ntiles8) + fte_kspace_rec_ws(prm.form, nsrc) + 4096;
         FTE_CUDA_TRY(cudaStreamSynchronize(c->stream));
         FTE_TRY(fte_ws_reserve(c, bins));
         WsCarver bw{c->ws, 0, c->ws_size};

@@ -57,6 +57,16 @@ extern "C" {
 /* arithmetic forms */
 #define FTE_FORM_PLAIN 0  /* FP64 everywhere (the drop-in) */
 #define FTE_FORM_MIXED 1  /* FP32 spread/FFT/filter/gather (compensated), FP64 near sums */
+/* fte_params.form only: spread and gather in float-float (pairs of FP32
+ * numbers, ~48 bits), FP64 transforms and filter, FP64 near sums */
+#define FTE_FORM_FF 2
+
+/* fte_options.kspace (FTE_FORM_MIXED): the k-space arithmetic of the tuned
+ * choice; AUTO lets the chooser pick by tolerance and cost */
+#define FTE_KSPACE_AUTO 0
+#define FTE_KSPACE_FP64 1
+#define FTE_KSPACE_FP32 2
+#define FTE_KSPACE_FF 3
 
 /* kinds */
 #define FTE_KIND_SLP 0
@@ -78,7 +88,8 @@ typedef struct {
     int Mx, My;     /* grid size */
     double w;       /* window half-width P*h/2 */
     double eta;     /* window shape (2 xi w / m)^2, m = 0.95 sqrt(pi P) */
-    int form;       /* arithmetic of the k-space part: FTE_FORM_PLAIN (FP64) or FTE_FORM_MIXED (FP32) */
+    int form;       /* arithmetic of the k-space part: FTE_FORM_PLAIN (FP64), FTE_FORM_MIXED (FP32) or
+                       FTE_FORM_FF (float-float spread and gather) */
     int ts_spread;  /* k-space spread / gather tile sizes in grid nodes (plans; 0: the default rule) */
     int ts_gather;
 } fte_params;
@@ -95,7 +106,8 @@ typedef struct {
     const double* weights; /* optional quadrature weights, multiplied into f (length nsrc) */
     int form;              /* FTE_FORM_PLAIN or FTE_FORM_MIXED */
     int tune;              /* plans: 1 = time the k-space tile sizes on the plan's points at creation */
-    double slack;          /* FTE_FORM_MIXED: error-estimate slack of the tuned choice (0: 3) */
+    double slack;          /* FTE_FORM_MIXED: error-estimate slack of the tuned choice (0: calibrated) */
+    int kspace;            /* FTE_FORM_MIXED: FTE_KSPACE_* (0: the chooser's pick) */
 } fte_options;
 
 /* Per-call diagnostics (optional output of the driver entries). */

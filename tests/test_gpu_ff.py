@@ -1,0 +1,126 @@
+"""Float-float k-space (FTE_FORM_FF): spread and gather in pairs of FP32
+numbers, FP64 transforms and filter.
+
+* against the FP64 k-space on the same parameters: the k-space parts agree to
+  ~1e-13 of their maximum (the pairs carry ~48 bits);
+* the tuned choice picks it between the FP32 floor and 1e-11 and meets the
+  tolerance against converged FP64 Ewald sums;
+* plans (tile bins and window records built once, tuned tiles) give the
+  driver's result.
+"""
+import numpy as np
+import pytest
+
+from conftest import load_golden
+from oracle import pyoracle as po
+
+pytestmark = pytest.mark.gpu
+
+
+def _ft():
+    import fasttools2d_gb300 as ft
+
+    return ft
+
+
+def _case(seed, n, Lx, Ly):
+    rng = np.random.default_rng(seed)
+    xs, ys = (rng.random(n) - 0.5) * Lx, (rng.random(n) - 0.5) * Ly
+    xt, yt = (rng.random(n) - 0.5) * Lx, (rng.random(n) - 0.5) * Ly
+    f1, f2 = rng.standard_normal(n), rng.standard_normal(n)
+    f1 -= f1.mean()
+    f2 -= f2.mean()
+    th = rng.random(n) * 2 * np.pi
+    return xs, ys, xt, yt, f1, f2, np.cos(th), np.sin(th)
+
+
+def _run(ft, ctx, kind, d, Lx, Ly, **kw):
+    xs, ys, xt, yt, f1, f2, n1, n2 = d
+    if kind == "slp":
+        return ft.StokesSLP_ewald_2p(xs, ys, xt, yt, f1, f2, Lx, Ly, form=ft.FORM_MIXED, ctx=ctx, return_info=True,
+                                     **kw)
+    return ft.StokesDLP_ewald_2p(xs, ys, xt, yt, n1, n2, f1, f2, Lx, Ly, form=ft.FORM_MIXED, ctx=ctx,
+                                 return_info=True, **kw)
+
+
+@pytest.mark.parametrize("kind", ["slp", "dlp"])
+@pytest.mark.parametrize("geom", [(20000, 1.0, 1.0, 41), (12000, 2.0, 1.0, 42), (9000, 1.0, 2.75, 43)])
+def test_ff_kspace_matches_fp64(gpu_ctx, kind, geom):
+    ft = _ft()
+    n, Lx, Ly, seed = geom
+    d = _case(seed, n, Lx, Ly)
+    out_f, info_f = _run(ft, gpu_ctx, kind, d, Lx, Ly, tol=1e-10, kspace=ft.KSPACE_FF)
+    p = info_f.params
+    assert p.form == ft.FORM_FF
+    same = dict(P=p.P, xi=p.xi, Mx=p.Mx, My=p.My, nside_x=p.nside_x, nside_y=p.nside_y)
+    out_d, info_d = _run(ft, gpu_ctx, kind, d, Lx, Ly, tol=1e-10, kspace=ft.KSPACE_FP64, **same)
+    q = info_d.params
+    assert q.form == ft.FORM_PLAIN
+    assert (q.P, q.Mx, q.My, q.nside_x, q.xi) == (p.P, p.Mx, p.My, p.nside_x, p.xi)
+    uk_f, uk_d = out_f[3], out_d[3]
+    rel = np.max(np.abs(uk_f - uk_d)) / np.max(np.abs(uk_d))
+    assert rel <= 2e-12, rel
+    # the real-space parts are the same kernel on the same parameters; the
+    # cell lists' order within a box may differ between calls, which moves
+    # the FP32 pair class's rounding (well below the tolerance)
+    assert np.max(np.abs(out_f[2] - out_d[2])) <= 1e-10 * np.max(np.abs(out_d[2]))
+
+
+@pytest.mark.parametrize("tol", [1e-9, 1e-11])
+@pytest.mark.parametrize("geom", [(20000, 1.0, 1.0, 51), (12000, 3.75, 1.0, 52)])
+def test_ff_chosen_and_meets_tolerance(gpu_ctx, tol, geom):
+    ft = _ft()
+    n, Lx, Ly, seed = geom
+    d = _case(seed, n, Lx, Ly)
+    xs, ys, xt, yt, f1, f2, n1, n2 = d
+    idx = np.arange(0, n, 40)
+    for kind in ("slp", "dlp"):
+        out, info = _run(ft, gpu_ctx, kind, d, Lx, Ly, tol=tol)
+        assert info.params.form == ft.FORM_FF, info.params.as_dict()
+        if kind == "slp":
+            truth = po.ewald_truth(po.KIND_SLP, xs, ys, xt[idx], yt[idx], f1, f2, Lx, Ly)
+        else:
+            truth = po.ewald_truth(po.KIND_DLP, xs, ys, xt[idx], yt[idx], f1, f2, Lx, Ly, n1=n1, n2=n2)
+        u = np.stack([out[0][idx], out[1][idx]], 1)
+        err = np.max(np.abs(u - truth)) / np.max(np.abs(truth))
+        assert err <= tol, (kind, err, info.params.as_dict())
+
+
+def test_ff_on_ellipses(gpu_ctx):
+    """Clustered boundary points with self-coincident targets, FF forced at
+    tol 1e-10, against the reference's own SE output (absolute criterion, as
+    for the other forms)."""
+    ft = _ft()
+    g = load_golden("config2_mini")
+    for kind in ("slp", "dlp"):
+        d = (g["xsrc"], g["ysrc"], g["xtar"], g["ytar"], g["f1"], g["f2"], g["n1"], g["n2"])
+        out, info = _run(ft, gpu_ctx, kind, d, 2.0, 1.0, tol=1e-10, kspace=ft.KSPACE_FF)
+        assert info.params.form == ft.FORM_FF
+        ref = g[kind + "_u"]
+        u = np.stack([out[0], out[1]], 1)
+        assert np.max(np.abs(u - ref)) <= 1e-10 * max(1.0, np.max(np.abs(ref))), kind
+
+
+@pytest.mark.parametrize("tune", [False, True])
+def test_ff_plan_matches_driver(gpu_ctx, tune):
+    ft = _ft()
+    n, Lx, Ly = 15000, 2.0, 1.0
+    xs, ys, xt, yt, f1, f2, n1, n2 = _case(61, n, Lx, Ly)
+    rng = np.random.default_rng(62)
+    fs1, fs2 = rng.standard_normal((3, n)), rng.standard_normal((3, n))
+    for kind in (ft.KIND_SLP, ft.KIND_DLP):
+        plan = ft.Plan(kind, xs, ys, xt, yt, f1, f2, Lx, Ly, n1=n1, n2=n2, tol=1e-10, form=ft.FORM_MIXED,
+                       kspace=ft.KSPACE_FF, nvmax=3, tune=tune, ctx=gpu_ctx)
+        p = plan.params
+        assert p.form == ft.FORM_FF
+        u1s, u2s = plan.execute(fs1, fs2)
+        for v in range(3):
+            kw = dict(tol=1e-10, form=ft.FORM_MIXED, kspace=ft.KSPACE_FF, P=p.P, xi=p.xi, Mx=p.Mx, My=p.My,
+                      nside_x=p.nside_x, nside_y=p.nside_y, ctx=gpu_ctx)
+            if kind == ft.KIND_SLP:
+                o = ft.StokesSLP_ewald_2p(xs, ys, xt, yt, fs1[v], fs2[v], Lx, Ly, **kw)
+            else:
+                o = ft.StokesDLP_ewald_2p(xs, ys, xt, yt, n1, n2, fs1[v], fs2[v], Lx, Ly, **kw)
+            ref = np.stack([o[0], o[1]], 1)
+            got = np.stack([np.asarray(u1s[v]), np.asarray(u2s[v])], 1)
+            assert np.max(np.abs(got - ref)) <= 1e-12 * np.max(np.abs(ref)), (kind, v)

@@ -52,7 +52,7 @@ def test_mixed_form_meets_tolerance(gpu_ctx, tol, geom):
         assert err <= tol, (kind, err, info.params.as_dict())
         # the FP32 k-space is used only where it can meet the tolerance
         if tol < 1e-7:
-            assert info.params.form == ft.FORM_PLAIN
+            assert info.params.form != ft.FORM_MIXED
 
 
 def test_mixed_form_on_ellipses(gpu_ctx):
