@@ -39,6 +39,7 @@ FORM_PLAIN = 0
 FORM_MIXED = 1
 FORM_FF = 2  # fte_params.form only: float-float spread and gather
 KSPACE_AUTO, KSPACE_FP64, KSPACE_FP32, KSPACE_FF = 0, 1, 2, 3
+NEAR_AUTO, NEAR_FP64, NEAR_FF = 0, 1, 2
 KIND_SLP = 0
 KIND_DLP = 1
 Q_VELOCITY = 0
@@ -73,7 +74,7 @@ class Options(C.Structure):
     _fields_ = [("P", C.c_int), ("Nb", C.c_double), ("tol", C.c_double), ("xi", C.c_double),
                 ("Mx", C.c_int), ("My", C.c_int), ("nside_x", C.c_int), ("nside_y", C.c_int),
                 ("weights", C.c_void_p), ("form", C.c_int), ("tune", C.c_int), ("slack", C.c_double),
-                ("kspace", C.c_int)]
+                ("kspace", C.c_int), ("near", C.c_int)]
 
 
 class Info(C.Structure):
@@ -338,7 +339,7 @@ def mex_stokes_dlp_kspace(psrc, ptar, xi, eta, f, n, Mx, My, Lx, Ly, w, P, ctx: 
 # ---- driver-shaped entries -----------------------------------------------------
 
 def _options(P=None, Nb=None, tol=1e-16, xi=None, Mx=None, My=None, nside_x=None, nside_y=None, weights_ptr=None,
-             form=FORM_PLAIN, tune=False, slack=None, kspace=KSPACE_AUTO) -> Options:
+             form=FORM_PLAIN, tune=False, slack=None, kspace=KSPACE_AUTO, near=NEAR_AUTO) -> Options:
     o = Options()
     o.P = int(P or 0)
     o.Nb = float(Nb) if Nb else 0.0
@@ -353,6 +354,7 @@ def _options(P=None, Nb=None, tol=1e-16, xi=None, Mx=None, My=None, nside_x=None
     o.tune = 1 if tune else 0
     o.slack = float(slack) if slack else 0.0
     o.kspace = int(kspace or 0)
+    o.near = int(near or 0)
     return o
 
 
@@ -370,7 +372,7 @@ def _print_verbose(kind: str, ns: int, nt: int, info: Info):
 
 
 def _ewald(kind, xsrc, ysrc, xtar, ytar, n1, n2, f1, f2, Lx, Ly, P, Nb, tol, verbose, weights, xi, Mx, My,
-           nside_x, nside_y, form, ctx, return_info, out, parts, slack=None, kspace=KSPACE_AUTO):
+           nside_x, nside_y, form, ctx, return_info, out, parts, slack=None, kspace=KSPACE_AUTO, near=NEAR_AUTO):
     ctx = ctx or default_context()
     A = _Args()
     pxs, ns = A.arr(xsrc, 1)
@@ -389,7 +391,7 @@ def _ewald(kind, xsrc, ysrc, xtar, ytar, n1, n2, f1, f2, Lx, Ly, P, Nb, tol, ver
     if parts:
         ur, pur = A.out((nt, 2))
         uk, puk = A.out((nt, 2))
-    opt = _options(P, Nb, tol, xi, Mx, My, nside_x, nside_y, pw, form, slack=slack, kspace=kspace)
+    opt = _options(P, Nb, tol, xi, Mx, My, nside_x, nside_y, pw, form, slack=slack, kspace=kspace, near=near)
     info = Info()
     if verbose:
         ctx.set_timing(True)
@@ -409,30 +411,31 @@ def _ewald(kind, xsrc, ysrc, xtar, ytar, n1, n2, f1, f2, Lx, Ly, P, Nb, tol, ver
 def StokesSLP_ewald_2p(xsrc, ysrc, xtar, ytar, f1, f2, Lx, Ly, P=None, Nb=None, tol=1e-16, verbose=0,
                        weights=None, xi=None, Mx=None, My=None, nside_x=None, nside_y=None, form=FORM_PLAIN,
                        ctx: Context | None = None, return_info: bool = False, out=None, parts: bool = True,
-                       slack=None, kspace=KSPACE_AUTO):
+                       slack=None, kspace=KSPACE_AUTO, near=NEAR_AUTO):
     """Spectral Ewald evaluation of the doubly-periodic Stokeslet.
 
     Returns (u1, u2, ur, uk, xi) like the MATLAB driver; ur and uk are
     (Ntar, 2) (None when parts=False).  ``out=(u1, u2)`` supplies the output
     buffers (same side as the inputs).  ``form=FORM_MIXED`` takes the tuned
     parameter choice with FP32 pairs where the tolerance allows; ``kspace``
-    (KSPACE_*) then forces its k-space arithmetic.
+    (KSPACE_*) then forces its k-space arithmetic and ``near`` (NEAR_*) the
+    arithmetic of the real-space pairs.
     """
     return _ewald(KIND_SLP, xsrc, ysrc, xtar, ytar, None, None, f1, f2, Lx, Ly, P, Nb, tol, verbose, weights, xi, Mx,
-                  My, nside_x, nside_y, form, ctx, return_info, out, parts, slack, kspace)
+                  My, nside_x, nside_y, form, ctx, return_info, out, parts, slack, kspace, near)
 
 
 def StokesDLP_ewald_2p(xsrc, ysrc, xtar, ytar, n1, n2, f1, f2, Lx, Ly, P=None, Nb=None, tol=1e-16, verbose=0,
                        weights=None, xi=None, Mx=None, My=None, nside_x=None, nside_y=None, form=FORM_PLAIN,
                        ctx: Context | None = None, return_info: bool = False, out=None, parts: bool = True,
-                       slack=None, kspace=KSPACE_AUTO):
+                       slack=None, kspace=KSPACE_AUTO, near=NEAR_AUTO):
     """Spectral Ewald evaluation of the doubly-periodic stresslet (double layer).
 
     Returns (u1, u2, ur, uk, xi); uk includes the k = 0 mode like the MATLAB
     driver.  Options as for StokesSLP_ewald_2p.
     """
     return _ewald(KIND_DLP, xsrc, ysrc, xtar, ytar, n1, n2, f1, f2, Lx, Ly, P, Nb, tol, verbose, weights, xi, Mx,
-                  My, nside_x, nside_y, form, ctx, return_info, out, parts, slack, kspace)
+                  My, nside_x, nside_y, form, ctx, return_info, out, parts, slack, kspace, near)
 
 
 def choose_params(kind, f1, f2, ntar, Lx, Ly, P=None, Nb=None, tol=1e-16, **kw) -> Params:

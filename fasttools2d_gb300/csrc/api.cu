@@ -1391,9 +1391,11 @@ static int ewald_entry(fte_context* c, int kind, const double* xsrc, const doubl
         FTE_TRY(fte_cells_build(c, wc2, kind, ps, nsrc, pt, ntar, pf, pn, dw, prm.nside_x, prm.nside_y, Lx, Ly, &cl));
         FTE_TRY(fte_record(c, 6));
         // the mixed form evaluates the pairs whose terms are far below the
-        // tolerance in FP32
-        const double x32 = opt->form == FTE_FORM_MIXED ? fte_near_fp32_threshold(prm.tol) : HUGE_VAL;
-        FTE_TRY(fte_near_launch(c, kind, cl, prm.xi, Lx, Ly, dur, x32));
+        // tolerance in FP32 and the other pairs with x >= 1 in float-float
+        double x32;
+        bool ffn;
+        FTE_TRY(fte_near_classes(opt, prm.tol, &x32, &ffn));
+        FTE_TRY(fte_near_launch(c, kind, cl, prm.xi, Lx, Ly, dur, x32, ffn));
         FTE_TRY(fte_record(c, 7));
         KspaceArgs a;
         a.kind = kind;

@@ -248,18 +248,25 @@ int fte_tiles_build(fte_context* ctx, WsCarver& wc, const double* p, int64_t n, 
                     int ts, int ntx, int nty, TileBins* out);
 
 int fte_near_launch(fte_context* ctx, int kind, const CellList& cl, double xi, double Lx, double Ly, double2* ur,
-                    double x32 = HUGE_VAL);
+                    double x32 = HUGE_VAL, bool ff = false);
 // xi^2 r^2 above which a pair's terms are small enough for FP32 at tolerance
 // tol (mixed form); HUGE_VAL: every pair in FP64
 double fte_near_fp32_threshold(double tol);
+// mixed form: may the FP64 pairs with xi^2 r^2 >= 1 be evaluated in
+// float-float at tolerance tol
+bool fte_near_ff_ok(double tol);
+// the near-pair classes of the options (x32 = HUGE_VAL: no FP32 class)
+int fte_near_classes(const fte_options* opt, double tol, double* x32, bool* ff);
 // Near-field launch description, opaque outside near.cu.
 struct NearParamsHost {
     alignas(16) unsigned char raw[256];
 };
 void fte_near_fill_params(int kind, const CellList& cl, double xi, double Lx, double Ly, NearParamsHost* hp,
-                          double x32 = HUGE_VAL);
+                          double x32 = HUGE_VAL, bool ff = false);
 size_t fte_near_params_size();
-int fte_near_cap(const fte_context* ctx, int kind, int nv);
+bool fte_near_uses_ff(const NearParamsHost& hp);
+// sources staged per chunk (ff: the description uses the float-float class)
+int fte_near_cap(const fte_context* ctx, int kind, int nv, bool ff);
 // nv (1..4) density vectors at q* + v*cl.qstride; outputs at ur + v*ustride
 int fte_near_launch_nv(fte_context* ctx, int kind, int nv, const NearParamsHost& hp, double2* ur, long long ustride);
 // many problems in one launch: plist_dev = device array of the filled

@@ -27,6 +27,7 @@
 #include <cmath>
 #include <mutex>
 
+#include "ff.cuh"
 #include "fft.cuh"
 #include "fte_internal.cuh"
 #include "quant_filters.cuh"
@@ -282,6 +283,8 @@ __global__ void __launch_bounds__(kTileThreads) k_spread_tiled(const double* __r
 // so every update is one FMA on an address no other thread touches.
 // mode 0: (f1, f2) [Stokeslet]; 1: (f1 n1, f2 n1); 2: (f1 n2, f2 n2) [stresslet].
 constexpr int kColThreads = 256;
+constexpr int kColWarps = kColThreads / 32;  // a power of two (column owner = column mod warps)
+static_assert((kColWarps & (kColWarps - 1)) == 0, "column ownership needs a power-of-two warp count");
 constexpr int kColChunk = 32;
 
 __global__ void __launch_bounds__(kColThreads) k_spread_cols(int mode, const double* __restrict__ p,
@@ -301,7 +304,8 @@ __global__ void __launch_bounds__(kColThreads) k_spread_cols(int mode, const dou
     double* wy = fw + kColChunk * 2 * P1; // kColChunk * P1
     int* org = reinterpret_cast<int*>(wy + kColChunk * P1);  // kColChunk * 2 (lx, ly; lx < 0: global path)
     load_e1(e1, wp);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    constexpr int nw = kColWarps;
     for (int tile = blockIdx.x; tile < ntx * nty; tile += gridDim.x) {
         const int k0 = toff[tile], k1 = toff[tile + 1];
         if (k0 == k1) continue;
@@ -363,7 +367,7 @@ __global__ void __launch_bounds__(kColThreads) k_spread_cols(int mode, const dou
                 if (lx < 0) continue;
                 const int ly = org[2 * s + 1];
                 // first column >= lx owned by this warp
-                int c = lx + ((warp - lx) % nw + nw) % nw;
+                int c = lx + ((warp - lx) & (nw - 1));
                 if (lane < P1) {
                     const double wyj = wy[s * P1 + lane];
                     const double* fa = fw + (s * 2) * P1;
@@ -851,7 +855,8 @@ __global__ void __launch_bounds__(kColThreads) k_spread_cols32(int mode, const d
     float* fw = car + 2 * WW;               // kColChunk32 * 2 * P1
     float* wy = fw + kColChunk32 * 2 * P1;  // kColChunk32 * P1
     int* org = reinterpret_cast<int*>(wy + kColChunk32 * P1);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    constexpr int nw = kColWarps;
     for (int tile = blockIdx.x; tile < ntx * nty; tile += gridDim.x) {
         const int k0 = toff[tile], k1 = toff[tile + 1];
         if (k0 == k1) continue;
@@ -911,7 +916,7 @@ __global__ void __launch_bounds__(kColThreads) k_spread_cols32(int mode, const d
                 const int lx = org[2 * s];
                 if (lx < 0) continue;
                 const int ly = org[2 * s + 1];
-                int c = lx + ((warp - lx) % nw + nw) % nw;
+                int c = lx + ((warp - lx) & (nw - 1));
                 if (lane < P1) {
                     const float wyj = wy[s * P1 + lane];
                     const float* fa = fw + (s * 2) * P1;
@@ -1123,37 +1128,6 @@ __global__ void k_filter32(float2* __restrict__ Hh, int Mx, int My, double Lx, d
 // ewald_tools.cpp:86-114, 182-190), rounded to float-float, and the window
 // rows by float-float recurrences; relative error ~1e-13 against FP64.
 // ===========================================================================
-__device__ __forceinline__ float2 ff_split(double v) {
-    const float hi = __double2float_rn(v);
-    return make_float2(hi, __double2float_rn(v - (double)hi));
-}
-__device__ __forceinline__ double ff_join(float s, float c) { return (double)s + (double)c; }
-// a b rounded to a normalised pair (error below ~2^-46 |a b|)
-__device__ __forceinline__ float2 ff_mul(float2 a, float2 b) {
-    const float p = __fmul_rn(a.x, b.x);
-    float e = __fmaf_rn(a.x, b.x, -p);
-    e = __fmaf_rn(a.x, b.y, e);
-    e = __fmaf_rn(a.y, b.x, e);
-    const float s = __fadd_rn(p, e);
-    return make_float2(s, __fsub_rn(e, __fsub_rn(s, p)));
-}
-// (s, c) += a b; s holds the running sum, c the collected low-order parts
-__device__ __forceinline__ void ff_mac(float2 a, float2 b, float& s, float& c) {
-    const float p = __fmul_rn(a.x, b.x);
-    float e = __fmaf_rn(a.x, b.x, -p);
-    e = __fmaf_rn(a.x, b.y, e);
-    e = __fmaf_rn(a.y, b.x, e);
-    const float t = __fadd_rn(s, p);
-    const float bp = __fsub_rn(t, s);
-    const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(p, bp));
-    s = t;
-    c = __fadd_rn(c, __fadd_rn(err, e));
-}
-__device__ __forceinline__ float2 ff_norm(float s, float c) {
-    const float h = __fadd_rn(s, c);
-    return make_float2(h, __fsub_rn(c, __fsub_rn(h, s)));
-}
-
 // per-source window record in tile order (64 bytes)
 struct FfWin {
     int mx, my;            // first window node
@@ -1221,7 +1195,8 @@ __global__ void __launch_bounds__(kColThreads) k_spread_ff(int pass, const FfWin
     float2* wy = fw + kColChunk * 2 * P1;   // kColChunk * P1
     int* org = reinterpret_cast<int*>(wy + kColChunk * P1);  // kColChunk * 2 (lx, ly)
     load_e1_ff(e1, wp);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    constexpr int nw = kColWarps;
     for (int tile = blockIdx.x; tile < ntx * nty; tile += gridDim.x) {
         const int k0 = toff[tile], k1 = toff[tile + 1];
         if (k0 == k1) continue;
@@ -1260,7 +1235,7 @@ __global__ void __launch_bounds__(kColThreads) k_spread_ff(int pass, const FfWin
                 const int lx = org[2 * s], ly = org[2 * s + 1];
                 const bool inside = lx >= 0 && ly >= 0 && lx + wp.P < W && ly + wp.P < W;
                 // first column >= lx owned by this warp
-                int c = lx + ((warp - lx) % nw + nw) % nw;
+                int c = lx + ((warp - lx) & (nw - 1));
                 if (lane < P1) {
                     const float2 wyj = wy[s * P1 + lane];
                     const float2* fa = fw + (s * 2) * P1;

@@ -22,6 +22,7 @@
 // so full batches are what keeps the FP64 work proportional to the pairs
 // inside the cutoff.
 #include "fte_internal.cuh"
+#include "ff.cuh"
 
 #define FTE_E1_STORAGE_R static __constant__
 #define FTE_E1_STORAGE_G static __device__ const
@@ -52,6 +53,11 @@ struct NearParams {
     // pairs with xi^2 r^2 >= x32 are evaluated in FP32 (their terms are
     // below the tolerance's reach of FP32 rounding); +inf: all FP64
     float x32;
+    // mixed form at tolerances the float-float class meets: the FP64 pairs
+    // with x >= 1 are evaluated in float-float (ffnear = 1); constants as
+    // float-float
+    int ffnear;
+    float2 xi2ff, pfff, cutff, selcff;
     int cap;
     double2* __restrict__ ur;  // vector v at ur + v * ustride
     long long ustride;
@@ -165,20 +171,125 @@ __device__ __forceinline__ float fte_kfun32(float x, const float* __restrict__ k
     return k;
 }
 
+// exp(-x) in float-float for 0 <= x < 80 (0 beyond): the reduction of
+// fte_expm with n = round(64 x / ln 2) and ln2/64 split in three FP32 parts
+// (the first with 13 trailing zero bits, so n C1 is exact for n < 8192);
+// exp(-r), |r| <= ln2/128, as 1 - r + r^2/2 in float-float plus the cubic and
+// higher Taylor terms in FP32 (they are below 3e-8); 2^(-j/64) from a
+// float-float table.  Relative error ~4e-14.
+__device__ __forceinline__ float2 fte_expm_ff(float2 x, const float2* __restrict__ tab) {
+    const float C1 = 1.082611084e-02f, C2 = 4.313856607e-06f, C3 = -2.016456257e-13f;
+    const int n = __float2int_rn(x.x * 9.233248138e+01f);
+    const float nf = (float)n;
+    const float rh = __fsub_rn(x.x, __fmul_rn(nf, C1));
+    const float p2 = __fmul_rn(nf, C2);
+    const float e2 = __fmaf_rn(nf, C2, -p2);
+    // r = rh - p2 + (x.lo - e2 - n C3)
+    const float s = __fsub_rn(rh, p2);
+    const float bb = __fsub_rn(s, rh);
+    float e = __fadd_rn(__fsub_rn(rh, __fsub_rn(s, bb)), __fsub_rn(-p2, bb));
+    e = __fsub_rn(__fsub_rn(__fadd_rn(e, x.y), e2), __fmul_rn(nf, C3));
+    const float2 r = ff_norm(s, e);
+    const float r1 = r.x;
+    float q = __fmaf_rn(r1, -1.0f / 120.0f, 1.0f / 24.0f);
+    q = __fmaf_rn(r1, q, -1.0f / 6.0f);
+    q = __fmul_rn(q, __fmul_rn(r1, __fmul_rn(r1, r1)));
+    // r^2 / 2 in float-float
+    const float p = __fmul_rn(r1, r1);
+    float pe = __fmaf_rn(r1, r1, -p);
+    pe = __fmaf_rn(__fadd_rn(r1, r1), r.y, pe);
+    float2 h = ff_norm(__fmul_rn(p, 0.5f), __fmul_rn(pe, 0.5f));
+    h = ff_add(h, make_float2(q, 0.0f));
+    h = ff_add(h, ff_neg(r));
+    h = ff_add(make_float2(1.0f, 0.0f), h);
+    const float2 m = ff_mul(h, tab[n & 63]);
+    const float sc = __int_as_float((127 - (n >> 6)) << 23);  // 2^-(n >> 6)
+    return x.x < 80.0f ? make_float2(__fmul_rn(m.x, sc), __fmul_rn(m.y, sc)) : make_float2(0.0f, 0.0f);
+}
+
+// K(x) in float-float from the float-float table (x >= 1 less a rounding
+// margin): the piece and t from x.hi, t's low part from x.lo; Horner with
+// the degree-10..5 terms in FP32 (relative size below 1e-7 of K) and the
+// rest in float-float.  Relative error ~5e-15.
+__device__ __forceinline__ float2 fte_kfun_ff(float2 x, const float2* __restrict__ ktab) {
+    const int bits = __float_as_int(x.x);
+    int e = (bits >> 23) - 127;
+    int q = (bits >> 20) & 7;
+    float mant = __int_as_float((bits & 0x007FFFFF) | 0x3F800000);
+    float sc = __int_as_float((127 - e) << 23);  // 2^-e
+    if (e < 0) {
+        e = 0;
+        q = 0;
+        mant = x.x;
+        sc = 1.0f;
+    } else if (e > 9) {
+        e = 9;
+        q = 7;
+        mant = 2.0f;
+        sc = 0.0f;
+    }
+    const float mid = __int_as_float(0x3F800000 | (q << 20) | (1 << 19));
+    const float2 t = ff_norm(__fmul_rn(__fsub_rn(mant, mid), 16.0f), __fmul_rn(__fmul_rn(x.y, sc), 16.0f));
+    const float2* c = ktab + (8 * e + q) * (FTE_K_DEG + 1);
+    float k = c[FTE_K_DEG].x;
+#pragma unroll
+    for (int j = FTE_K_DEG - 1; j >= 5; j--) k = __fmaf_rn(k, t.x, c[j].x);
+    float2 kk = make_float2(k, 0.0f);
+#pragma unroll
+    for (int j = 4; j >= 0; j--) kk = ff_add(ff_mul(kk, t), c[j]);
+    return kk;
+}
+
+// ln x in float-float for a normal x.hi > 0: x = m 2^e with m in [1, 2),
+// y0 = logf(m) (about an ulp) and one Newton step y0 + m e^-y0 - 1, plus
+// e ln 2.  Absolute error ~1e-13.
+__device__ __forceinline__ float2 fte_log_ff(float2 x, const float2* __restrict__ etab) {
+    const int e = (__float_as_int(x.x) >> 23) - 127;
+    const float sc = __int_as_float((127 - e) << 23);  // 2^-e
+    const float2 m = make_float2(__fmul_rn(x.x, sc), __fmul_rn(x.y, sc));
+    const float y0 = logf(m.x);
+    const float2 t = ff_add(ff_mul(m, fte_expm_ff(make_float2(y0, 0.0f), etab)), make_float2(-1.0f, 0.0f));
+    const float2 y = ff_add(make_float2(y0, 0.0f), t);
+    const float2 ln2 = make_float2(6.931471825e-01f, -1.904654212e-09f);
+    return ff_add(y, ff_mulf(ln2, (float)e));
+}
+
+// 0.5 E1(x) - e^-x for 0 < x < 1 in float-float: E1 = -gamma - ln x +
+// x R(2x - 1) with the degree-11..6 terms of R in FP32 (below 4e-7 of R) and
+// the rest in float-float (R's coefficients as float-float in rtab).
+// Absolute error ~1e-13.
+__device__ __forceinline__ float2 fte_slp_small_ff(float2 x, float2 emx, const float2* __restrict__ rtab,
+                                                   const float2* __restrict__ etab) {
+    const float2 t = ff_add(make_float2(__fadd_rn(x.x, x.x), __fadd_rn(x.y, x.y)), make_float2(-1.0f, 0.0f));
+    float k = rtab[FTE_E1_DEG_R].x;
+#pragma unroll
+    for (int j = FTE_E1_DEG_R - 1; j >= 6; j--) k = __fmaf_rn(k, t.x, rtab[j].x);
+    float2 kk = make_float2(k, 0.0f);
+#pragma unroll
+    for (int j = 5; j >= 0; j--) kk = ff_add(ff_mul(kk, t), rtab[j]);
+    const float2 g = make_float2(5.772156715e-01f, -6.637773886e-09f);  // Euler's gamma
+    float2 E = ff_add(ff_mul(x, kk), ff_neg(g));
+    E = ff_add(E, ff_neg(fte_log_ff(x, etab)));
+    return ff_add(make_float2(__fmul_rn(E.x, 0.5f), __fmul_rn(E.y, 0.5f)), ff_neg(emx));
+}
+
 // Shared-memory layout of the near-field kernels (per CTA):
-//   K(x) table, exp table, FP32 K(x) table, then per staged source: x, y
-//   (FP64), NV density sets (SLP: f1, f2; DLP: S11, (S12+S21)/2, S22,
-//   S11+S22) in FP64 and in FP32, FP32 box-relative position; then three
-//   64-entry rings per warp.
+//   K(x) table, exp table, their float-float copies, FP32 K(x) table, then
+//   per staged source: x, y (FP64), NV density sets (SLP: f1, f2; DLP: S11,
+//   (S12+S21)/2, S22, S11+S22) in FP64 and in FP32, FP32 box-relative
+//   position, and with the float-float class the low parts of the position
+//   and the densities; then three 64-entry rings per warp.
 template <int KIND, int NV>
 struct NearSmem {
     static constexpr int kDen = KIND == FTE_KIND_SLP ? 2 : 4;
     // targets a warp keeps in flight (ring entries carry the slot): the
     // accumulators cost NSLOT * NV * 2 doubles per lane
     static constexpr int kSlots = NV == 1 ? 4 : (NV == 2 ? 2 : 1);
-    __host__ __device__ static size_t bytes(int cap) {
-        return (kKtab + 64) * sizeof(double) + kKtab * sizeof(float) +
+    static constexpr int kHead = 2 * kKtab + 128 + 12 + kKtab / 2 + 1;  // doubles before the staged sources
+    __host__ __device__ static size_t bytes(int cap, bool ff) {
+        return kHead * sizeof(double) +
                (size_t)cap * ((2 + kDen * NV) * sizeof(double) + sizeof(float2) + kDen * NV * sizeof(float)) +
+               (ff ? (size_t)cap * (sizeof(float2) + kDen * NV * sizeof(float)) : 0) +
                kNearWarps * 3 * kQueue * sizeof(int) + 64;
     }
 };
@@ -192,26 +303,38 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
     constexpr int kDen = NearSmem<KIND, NV>::kDen;
     constexpr int NSLOT = NearSmem<KIND, NV>::kSlots;
     const int cap = prm.cap;
+    // float-float class (density vectors beyond two keep the FP64 path: the
+    // float-float accumulators would not fit the register budget)
+    const bool ffn = NV <= 2 && prm.ffnear != 0;
     const double* ktab = reinterpret_cast<const double*>(smem_raw);
     const double* etab = ktab + kKtab;
-    const float* ktab32 = reinterpret_cast<const float*>(etab + 64);
-    double* sx = reinterpret_cast<double*>(smem_raw) + kKtab + 64 + kKtab / 2 + 1;
+    const float2* ktabff = reinterpret_cast<const float2*>(etab + 64);
+    const float2* etabff = ktabff + kKtab;
+    const float2* rtabff = etabff + 64;
+    const float* ktab32 = reinterpret_cast<const float*>(rtabff + 12);
+    double* sx = reinterpret_cast<double*>(smem_raw) + NearSmem<KIND, NV>::kHead;
     double* sy = sx + cap;
     double* den = sy + cap;  // den[(v * kDen + c) * cap + i]
     float2* s32 = reinterpret_cast<float2*>(den + (size_t)kDen * NV * cap);
     float* den32 = reinterpret_cast<float*>(s32 + cap);  // den32[(v * kDen + c) * cap + i]
-    int* qbuf = reinterpret_cast<int*>(den32 + (size_t)kDen * NV * cap);
+    // float-float class: low parts of the box-relative position and densities
+    float2* slo = reinterpret_cast<float2*>(den32 + (size_t)kDen * NV * cap);
+    float* dlo = reinterpret_cast<float*>(slo + (ffn ? cap : 0));
+    int* qbuf = reinterpret_cast<int*>(dlo + (ffn ? (size_t)kDen * NV * cap : 0));
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    // per warp: ring 0 = FP64 pairs with x >= 1 (all FP64 stresslet pairs),
-    // ring 1 = x < 1 (Stokeslet), ring 2 = the FP32 class (x >= x32)
+    // per warp: ring 0 = pairs with x >= 1 (FP64, or float-float when ffn),
+    // ring 1 = x < 1 (FP64; the stresslet's only with ffn, else its FP64
+    // pairs all take ring 0), ring 2 = the FP32 class (x >= x32)
     int* qf = qbuf + warp * 3 * kQueue;
     int* qn = qf + kQueue;
     int* qs = qn + kQueue;
     // per warp and target slot: the target's position and its FP32-class sums
     __shared__ double2 tslot[kNearWarps * 4];
+    __shared__ float4 tslot_ff[kNearWarps * 4];  // box-relative (x hi, x lo, y hi, y lo)
     __shared__ float fsum_all[kNearWarps * 8];
     double2* tsl = tslot + warp * 4;
+    float4* tsf = tslot_ff + warp * 4;
     float* fsw = fsum_all + warp * 8;
     const float x32 = prm.x32;
     const float cutf = (float)prm.cutoffsq;
@@ -280,6 +403,11 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
                     d[cap] = prm.q1[o];
                     d32[0] = (float)d[0];
                     d32[cap] = (float)d[cap];
+                    if (ffn) {
+                        float* dl = dlo + (size_t)v * kDen * cap + i;
+                        dl[0] = (float)(d[0] - (double)d32[0]);
+                        dl[cap] = (float)(d[cap] - (double)d32[cap]);
+                    }
                 } else {
                     // S11, (S12 + S21)/2, S22, S11 + S22
                     double s11 = prm.q0[o], ssym = prm.q1[o], s22 = prm.q2[o];
@@ -291,9 +419,17 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
                     d32[cap] = (float)(0.5 * ssym);
                     d32[2 * cap] = (float)s22;
                     d32[3 * cap] = (float)(s11 + s22);
+                    if (ffn) {
+                        float* dl = dlo + (size_t)v * kDen * cap + i;
+#pragma unroll
+                        for (int c = 0; c < 4; c++) dl[c * cap] = (float)(d[c * cap] - (double)d32[c * cap]);
+                    }
                 }
             }
-            s32[i] = make_float2((float)(xs - cx), (float)(ys - cy));
+            const double rx = xs - cx, ry = ys - cy;
+            const float2 h32 = make_float2((float)rx, (float)ry);
+            s32[i] = h32;
+            if (ffn) slo[i] = make_float2((float)(rx - (double)h32.x), (float)(ry - (double)h32.y));
         }
         __syncthreads();
         const int own_lim = n_own - chunk;  // local index < own_lim: own box
@@ -305,19 +441,28 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
         // empty fills up with the next targets' pairs instead.  The FP32 class
         // is cheap and is finished per target.
         const int ntw = warp < nt ? (nt - warp + kNearWarps - 1) / kNearWarps : 0;
+        // x below which a pair takes ring qn
+        const float xsplit = (KIND == FTE_KIND_DLP && ffn) ? 1e-8f : 1.0f;
         int Pf = 0, Ef = 0, Pn = 0, En = 0;  // pushed / evaluated counts of rings qf, qn
         int tailF[NSLOT], tailN[NSLOT];      // Pf, Pn after each slot's sweep
         double acc[NSLOT][NV][2];
+        float accf[NSLOT][NV][4];  // float-float class: (sum, low parts) per component
         float acc32[NV][2];
 #pragma unroll
         for (int j = 0; j < NSLOT; j++) {
             tailF[j] = tailN[j] = 0;
 #pragma unroll
-            for (int v = 0; v < NV; v++) acc[j][v][0] = acc[j][v][1] = 0.0;
+            for (int v = 0; v < NV; v++) {
+                acc[j][v][0] = acc[j][v][1] = 0.0;
+                accf[j][v][0] = accf[j][v][1] = accf[j][v][2] = accf[j][v][3] = 0.0f;
+            }
         }
 #pragma unroll
         for (int v = 0; v < NV; v++) acc32[v][0] = acc32[v][1] = 0.0f;
         float tx32 = 0.0f, ty32 = 0.0f;  // box-relative position of the target being swept
+        // FP64 accumulators in use in this chunk (always without ffn; with
+        // ffn only after a pass over the stresslet's qn ring)
+        bool any64 = !ffn;
 
         // slot `tag`'s accumulators of vector v, selected into (a0, a1) and
         // back: register moves only, no FP64 work per slot
@@ -332,6 +477,24 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
 #pragma unroll
             for (int j = 0; j < NSLOT; j++)
                 if (tag == j) acc[j][v][0] = a0, acc[j][v][1] = a1;
+        };
+        auto accf_get = [&](int tag, int v, float* a) {
+#pragma unroll
+            for (int i = 0; i < 4; i++) a[i] = accf[0][v][i];
+#pragma unroll
+            for (int j = 1; j < NSLOT; j++)
+                if (tag == j) {
+#pragma unroll
+                    for (int i = 0; i < 4; i++) a[i] = accf[j][v][i];
+                }
+        };
+        auto accf_put = [&](int tag, int v, const float* a) {
+#pragma unroll
+            for (int j = 0; j < NSLOT; j++)
+                if (tag == j) {
+#pragma unroll
+                    for (int i = 0; i < 4; i++) accf[j][v][i] = a[i];
+                }
         };
 
         // FP32 class: the same pair terms in FP32 from box-relative
@@ -455,26 +618,145 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
             }
         };
 
+        // The same pair terms in float-float (pairs with x >= 1 at mixed-form
+        // tolerances from 1e-11): box-relative positions and densities as
+        // (FP32, low part), relative error ~1e-13 per term.
+        auto ff_geom = [&](int s, int tag, float2& dx, float2& dy, float2& r2) {
+            const float4 tq = tsf[tag];
+            const float2 sh = s32[s], sl = slo[s];
+            dx = ff_add(make_float2(tq.x, tq.y), make_float2(-sh.x, -sl.x));
+            dy = ff_add(make_float2(tq.z, tq.w), make_float2(-sh.y, -sl.y));
+            r2 = ff_add(ff_sqr(dx), ff_sqr(dy));
+        };
+        // u += A f + gr (r.f) r for every vector (Stokeslet, float-float)
+        auto slp_ff_add = [&](int s, int tag, float2 dx, float2 dy, float2 A, float2 gr) {
+#pragma unroll
+            for (int v = 0; v < NV; v++) {
+                const float* d = den32 + (size_t)v * 2 * cap + s;
+                const float* dl = dlo + (size_t)v * 2 * cap + s;
+                const float2 fx = make_float2(d[0], dl[0]), fy = make_float2(d[cap], dl[cap]);
+                const float2 c = ff_mul(gr, ff_add(ff_mul(dx, fx), ff_mul(dy, fy)));
+                float a[4];
+                accf_get(tag, v, a);
+                ff_acc(ff_add(ff_mul(A, fx), ff_mul(c, dx)), a[0], a[1]);
+                ff_acc(ff_add(ff_mul(A, fy), ff_mul(c, dy)), a[2], a[3]);
+                accf_put(tag, v, a);
+            }
+        };
+        // x >= 1: A = e^-x K(x)
+        auto eval_slp_ff = [&](int ent) {
+            if constexpr (NV <= 2) {
+                const int s = ent >> 2, tag = ent & 3;
+                float2 dx, dy, r2;
+                ff_geom(s, tag, dx, dy, r2);
+                if (!(s < own_lim) && !ff_lt(r2, prm.cutff)) return;
+                const float2 x = ff_mul(r2, prm.xi2ff);
+                const float2 emx = fte_expm_ff(x, etabff);
+                slp_ff_add(s, tag, dx, dy, ff_mul(emx, fte_kfun_ff(x, ktabff)), ff_mul(emx, ff_rcp(r2)));
+            }
+        };
+        // x < 1: A = 0.5 E1(x) - e^-x by its series; the self term
+        // (-1 - gamma/2 - log xi) f for a coincident source of the own box
+        auto eval_slp_ff_small = [&](int ent) {
+            if constexpr (NV <= 2) {
+                const int s = ent >> 2, tag = ent & 3;
+                float2 dx, dy, r2;
+                ff_geom(s, tag, dx, dy, r2);
+                const bool own = s < own_lim;
+                if (own && r2.x < 1e-15f) {
+#pragma unroll
+                    for (int v = 0; v < NV; v++) {
+                        const float* d = den32 + (size_t)v * 2 * cap + s;
+                        const float* dl = dlo + (size_t)v * 2 * cap + s;
+                        float a[4];
+                        accf_get(tag, v, a);
+                        ff_acc(ff_mul(prm.selcff, make_float2(d[0], dl[0])), a[0], a[1]);
+                        ff_acc(ff_mul(prm.selcff, make_float2(d[cap], dl[cap])), a[2], a[3]);
+                        accf_put(tag, v, a);
+                    }
+                    return;
+                }
+                if (!own && !ff_lt(r2, prm.cutff)) return;
+                const float2 x = ff_mul(r2, prm.xi2ff);
+                const float2 emx = fte_expm_ff(x, etabff);
+                slp_ff_add(s, tag, dx, dy, fte_slp_small_ff(x, emx, rtabff, etabff), ff_mul(emx, ff_rcp(r2)));
+            }
+        };
+        auto eval_dlp_ff = [&](int ent) {
+            if constexpr (NV <= 2) {
+                const int s = ent >> 2, tag = ent & 3;
+                float2 dx, dy, r2;
+                ff_geom(s, tag, dx, dy, r2);
+                if (!(s < own_lim) && !ff_lt(r2, prm.cutff)) return;
+                const float2 x = ff_mul(r2, prm.xi2ff);
+                const float2 e2 = fte_expm_ff(x, etabff);
+                const float2 ir2 = ff_rcp(r2);
+                const float2 facb = ff_mulf(ff_mul(ff_add(make_float2(1.0f, 0.0f), x), ff_sqr(ir2)), -4.0f);
+#pragma unroll
+                for (int v = 0; v < NV; v++) {
+                    const float* d = den32 + (size_t)v * 4 * cap + s;
+                    const float* dl = dlo + (size_t)v * 4 * cap + s;
+                    const float2 s11 = make_float2(d[0], dl[0]), h = make_float2(d[cap], dl[cap]);
+                    const float2 s22 = make_float2(d[2 * cap], dl[2 * cap]), tr = make_float2(d[3 * cap], dl[3 * cap]);
+                    const float2 u = ff_add(ff_mul(dx, s11), ff_mul(dy, h));
+                    const float2 w = ff_add(ff_mul(dy, s22), ff_mul(dx, h));
+                    const float2 fQ = ff_mul(facb, ff_add(ff_mul(dx, u), ff_mul(dy, w)));
+                    const float2 w1 = ff_add(ff_mul(dx, tr), make_float2(2.0f * u.x, 2.0f * u.y));
+                    const float2 w2 = ff_add(ff_mul(dy, tr), make_float2(2.0f * w.x, 2.0f * w.y));
+                    const float2 t0 = ff_add(ff_mul(fQ, dx), ff_mul(prm.pfff, w1));
+                    const float2 t1 = ff_add(ff_mul(fQ, dy), ff_mul(prm.pfff, w2));
+                    float a[4];
+                    accf_get(tag, v, a);
+                    ff_acc(ff_mul(e2, t0), a[0], a[1]);
+                    ff_acc(ff_mul(e2, t1), a[2], a[3]);
+                    accf_put(tag, v, a);
+                }
+            }
+        };
+        // ring qf: x >= 1 (float-float when ffn; the stresslet's x >= 1e-8);
+        // ring qn: x < 1 (the stresslet's x < 1e-8, FP64; the Stokeslet's in
+        // float-float when ffn)
+        auto evalF = [&](int ent) {
+            if (KIND == FTE_KIND_SLP) {
+                if (ffn)
+                    eval_slp_ff(ent);
+                else
+                    eval_slp(ent, false);
+            } else {
+                if (ffn)
+                    eval_dlp_ff(ent);
+                else
+                    eval_dlp(ent);
+            }
+        };
+        auto evalN = [&](int ent) {
+            if (KIND == FTE_KIND_SLP) {
+                if (ffn)
+                    eval_slp_ff_small(ent);
+                else
+                    eval_slp(ent, true);
+            } else {
+                eval_dlp(ent);
+            }
+        };
+
         // evaluate everything pending in ring qf (if df) and qn (if dn);
         // both hold fewer than 32 entries here
         auto drain = [&](bool df, bool dn) {
             const int cf = df ? Pf - Ef : 0, cn = dn ? Pn - En : 0;
-            if (KIND == FTE_KIND_SLP) {
-                // the two rings share one pass when they fit in a warp
-                if (cf + cn <= 32) {
-                    if (lane < cf)
-                        eval_slp(qf[(Ef + lane) & (kQueue - 1)], false);
-                    else if (lane < cf + cn)
-                        eval_slp(qn[(En + lane - cf) & (kQueue - 1)], true);
-                } else {
-                    if (lane < cf) eval_slp(qf[(Ef + lane) & (kQueue - 1)], false);
-                    if (lane < cn) eval_slp(qn[(En + lane) & (kQueue - 1)], true);
-                }
+            // the two rings share one pass when they fit in a warp
+            if (cf + cn <= 32) {
+                if (lane < cf)
+                    evalF(qf[(Ef + lane) & (kQueue - 1)]);
+                else if (lane < cf + cn)
+                    evalN(qn[(En + lane - cf) & (kQueue - 1)]);
             } else {
-                if (lane < cf) eval_dlp(qf[(Ef + lane) & (kQueue - 1)]);
+                if (lane < cf) evalF(qf[(Ef + lane) & (kQueue - 1)]);
+                if (lane < cn) evalN(qn[(En + lane) & (kQueue - 1)]);
             }
             Ef += cf;
             En += cn;
+            if (KIND == FTE_KIND_DLP && cn > 0) any64 = true;
             __syncwarp();
         };
 
@@ -491,13 +773,43 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
             const bool hi = (lane & 16) != 0;
 #pragma unroll
             for (int v = 0; v < NV; v++) {
-                double a0, a1;
-                acc_get(sl, v, a0, a1);
                 // lanes 0-15 reduce component 0, lanes 16-31 component 1
-                double keep = hi ? a1 : a0;
-                keep += __shfl_xor_sync(0xffffffffu, hi ? a0 : a1, 16);
+                double keep = 0.0;
+                if (any64) {
+                    double a0, a1;
+                    acc_get(sl, v, a0, a1);
+                    keep = hi ? a1 : a0;
+                    keep += __shfl_xor_sync(0xffffffffu, hi ? a0 : a1, 16);
 #pragma unroll
-                for (int o = 8; o > 0; o >>= 1) keep += __shfl_xor_sync(0xffffffffu, keep, o);
+                    for (int o = 8; o > 0; o >>= 1) keep += __shfl_xor_sync(0xffffffffu, keep, o);
+                    acc_put(sl, v, 0.0, 0.0);
+                }
+                if (ffn) {
+                    // the float-float and FP32 sums, reduced in float-float
+                    float a[4];
+                    accf_get(sl, v, a);
+                    float2 kf = hi ? make_float2(a[2], a[3]) : make_float2(a[0], a[1]);
+                    const float2 sf = hi ? make_float2(a[0], a[1]) : make_float2(a[2], a[3]);
+                    kf = ff_add(kf, make_float2(__shfl_xor_sync(0xffffffffu, sf.x, 16),
+                                                __shfl_xor_sync(0xffffffffu, sf.y, 16)));
+#pragma unroll
+                    for (int o = 8; o > 0; o >>= 1)
+                        kf = ff_add(kf, make_float2(__shfl_xor_sync(0xffffffffu, kf.x, o),
+                                                    __shfl_xor_sync(0xffffffffu, kf.y, o)));
+                    a[0] = a[1] = a[2] = a[3] = 0.0f;
+                    accf_put(sl, v, a);
+                    if ((lane & 15) == 0) {
+                        kf = ff_add(kf, make_float2(fsw[(sl * NV + v) * 2 + (hi ? 1 : 0)], 0.0f));
+                        const float2 i4p = make_float2(7.957746834e-02f, 3.210319122e-09f);  // 1 / (4 pi)
+                        const double val = fma(keep, inv4pi, ff_join(ff_mul(kf, i4p)));
+                        double* o = reinterpret_cast<double*>(prm.ur + v * prm.ustride + oi) + (hi ? 1 : 0);
+                        if (chunk == 0)
+                            *o = val;
+                        else
+                            *o += val;
+                    }
+                    continue;
+                }
                 if ((lane & 15) == 0) {
                     const double val = (keep + (double)fsw[(sl * NV + v) * 2 + (hi ? 1 : 0)]) * inv4pi;
                     double* o = reinterpret_cast<double*>(prm.ur + v * prm.ustride + oi) + (hi ? 1 : 0);
@@ -506,17 +818,33 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
                     else
                         *o += val;
                 }
-                acc_put(sl, v, 0.0, 0.0);
             }
         };
 
+        // the warp's next 32 targets are read and converted by its lanes at
+        // once (lane l: target k0 + l); the one being swept is taken from
+        // its lane
+        double2 tpl = make_double2(0.0, 0.0);
+        float4 tfl = make_float4(0.f, 0.f, 0.f, 0.f);
         for (int k = 0; k < ntw; k++) {
             const int slot = k & (NSLOT - 1);
-            const double2 tp = prm.tpos[t0 + warp + k * kNearWarps];
-            if (lane == 0) tsl[slot] = tp;
+            if ((k & 31) == 0 && k + lane < ntw) {
+                tpl = prm.tpos[t0 + warp + (k + lane) * kNearWarps];
+                const double rx = tpl.x - cx, ry = tpl.y - cy;
+                if (ffn) {
+                    const float2 fx = ff_split(rx), fy = ff_split(ry);
+                    tfl = make_float4(fx.x, fx.y, fy.x, fy.y);
+                } else {
+                    tfl = make_float4((float)rx, 0.f, (float)ry, 0.f);
+                }
+            }
+            if (lane == (k & 31)) {
+                tsl[slot] = tpl;
+                tsf[slot] = tfl;
+            }
+            tx32 = __shfl_sync(0xffffffffu, tfl.x, k & 31);
+            ty32 = __shfl_sync(0xffffffffu, tfl.z, k & 31);
             __syncwarp();
-            tx32 = (float)(tp.x - cx);
-            ty32 = (float)(tp.y - cy);
             int hs = 0, cs = 0;  // FP32-class ring head and count
 
             for (int base = 0; base < clen; base += 32) {
@@ -528,7 +856,7 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
                     float r2f = dx * dx + dy * dy;
                     pass = (s < own_lim) || (r2f < prm.cut32);
                     const float xf = r2f * xi2f;
-                    small_x = xf < 1.0f;
+                    small_x = xf < xsplit;
                     single = xf >= x32;
                 }
                 {
@@ -549,35 +877,27 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
                     }
                 }
                 const int ent = (s << 2) | slot;
-                if (KIND == FTE_KIND_SLP) {
-                    bool pf_ = pass && !small_x, pn_ = pass && small_x;
-                    unsigned mf = __ballot_sync(0xffffffffu, pf_);
-                    unsigned mn = __ballot_sync(0xffffffffu, pn_);
-                    if (pf_) qf[(Pf + __popc(mf & lt_mask)) & (kQueue - 1)] = ent;
-                    if (pn_) qn[(Pn + __popc(mn & lt_mask)) & (kQueue - 1)] = ent;
-                    Pf += __popc(mf);
-                    Pn += __popc(mn);
+                // the stresslet splits its FP64 pairs at x = 1 only for the
+                // float-float class
+                const bool split = KIND == FTE_KIND_SLP || ffn;
+                const bool pf_ = pass && !(split && small_x), pn_ = pass && split && small_x;
+                const unsigned mf = __ballot_sync(0xffffffffu, pf_);
+                const unsigned mn = __ballot_sync(0xffffffffu, pn_);
+                if (pf_) qf[(Pf + __popc(mf & lt_mask)) & (kQueue - 1)] = ent;
+                if (pn_) qn[(Pn + __popc(mn & lt_mask)) & (kQueue - 1)] = ent;
+                Pf += __popc(mf);
+                Pn += __popc(mn);
+                __syncwarp();
+                if (Pf - Ef >= 32) {
+                    evalF(qf[(Ef + lane) & (kQueue - 1)]);
+                    Ef += 32;
                     __syncwarp();
-                    if (Pf - Ef >= 32) {
-                        eval_slp(qf[(Ef + lane) & (kQueue - 1)], false);
-                        Ef += 32;
-                        __syncwarp();
-                    }
-                    if (Pn - En >= 32) {
-                        eval_slp(qn[(En + lane) & (kQueue - 1)], true);
-                        En += 32;
-                        __syncwarp();
-                    }
-                } else {
-                    unsigned mf = __ballot_sync(0xffffffffu, pass);
-                    if (pass) qf[(Pf + __popc(mf & lt_mask)) & (kQueue - 1)] = ent;
-                    Pf += __popc(mf);
+                }
+                if (Pn - En >= 32) {
+                    evalN(qn[(En + lane) & (kQueue - 1)]);
+                    En += 32;
+                    if (KIND == FTE_KIND_DLP) any64 = true;
                     __syncwarp();
-                    if (Pf - Ef >= 32) {
-                        eval_dlp(qf[(Ef + lane) & (kQueue - 1)]);
-                        Ef += 32;
-                        __syncwarp();
-                    }
                 }
             }
             // the target's FP32 class: last partial batch, then its sums
@@ -617,12 +937,22 @@ template <int KIND, int NV>
 __device__ __forceinline__ void near_load_tables(unsigned char* smem_raw) {
     double* ktab = reinterpret_cast<double*>(smem_raw);
     double* etab = ktab + kKtab;
-    float* ktab32 = reinterpret_cast<float*>(etab + 64);
+    float2* ktabff = reinterpret_cast<float2*>(etab + 64);
+    float2* etabff = ktabff + kKtab;
+    float2* rtabff = etabff + 64;
+    float* ktab32 = reinterpret_cast<float*>(rtabff + 12);
     for (int i = threadIdx.x; i < kKtab; i += kNearThreads) {
-        ktab[i] = (&fte_k_coef[0][0])[i];
-        ktab32[i] = (float)(&fte_k_coef[0][0])[i];
+        const double c = (&fte_k_coef[0][0])[i];
+        ktab[i] = c;
+        ktabff[i] = ff_split(c);
+        ktab32[i] = (float)c;
     }
-    for (int i = threadIdx.x; i < 64; i += kNearThreads) etab[i] = fte_exp_tab[i];
+    for (int i = threadIdx.x; i < 64; i += kNearThreads) {
+        etab[i] = fte_exp_tab[i];
+        etabff[i] = ff_split(fte_exp_tab[i]);
+    }
+    static_assert(FTE_E1_DEG_R + 1 <= 12, "small-x E1 table");
+    for (int i = threadIdx.x; i <= FTE_E1_DEG_R; i += kNearThreads) rtabff[i] = ff_split(fte_e1_coef_r[i]);
 }
 
 // one problem: grid-stride over its boxes
@@ -649,20 +979,49 @@ __global__ void __launch_bounds__(kNearThreads, 2) k_near_batch(const unsigned c
     near_load_tables<KIND, NV>(smem_raw);
     for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
         const int2 w = items[it];
-        const NearParams prm = *reinterpret_cast<const NearParams*>(plist + (size_t)w.x * kParamStride);
+        // read in place (a register copy of the description would spill)
+        const NearParams& prm = *reinterpret_cast<const NearParams*>(plist + (size_t)w.x * kParamStride);
         near_box<KIND, NV>(prm, w.y, smem_raw, nb_box, nb_start, nb_shx, nb_shy);
     }
 }
 
 template <int KIND, int NV>
-int near_cap(const fte_context* ctx) {
+int near_cap(const fte_context* ctx, bool ff) {
     int cap = 2048;
     const size_t budget = 110 * 1024 < (size_t)ctx->max_smem_optin ? 110 * 1024 : (size_t)ctx->max_smem_optin;
-    while (cap > 128 && NearSmem<KIND, NV>::bytes(cap) > budget) cap -= 64;
+    while (cap > 128 && NearSmem<KIND, NV>::bytes(cap, ff) > budget) cap -= 64;
     return cap;
+}
+// shared memory of a launch whose problems may use either layout
+template <int KIND, int NV>
+size_t near_smem_any(const fte_context* ctx) {
+    const size_t a = NearSmem<KIND, NV>::bytes(near_cap<KIND, NV>(ctx, false), false);
+    const size_t b = NearSmem<KIND, NV>::bytes(near_cap<KIND, NV>(ctx, true), true);
+    return a > b ? a : b;
 }
 
 }  // namespace
+
+int fte_near_classes(const fte_options* opt, double tol, double* x32, bool* ff) {
+    *x32 = HUGE_VAL;
+    *ff = false;
+    if (!opt || opt->form != FTE_FORM_MIXED) return FTE_OK;
+    switch (opt->near) {
+        case FTE_NEAR_AUTO:
+            *x32 = fte_near_fp32_threshold(tol);
+            *ff = fte_near_ff_ok(tol);
+            return FTE_OK;
+        case FTE_NEAR_FP64: return FTE_OK;
+        case FTE_NEAR_FF: *ff = true; return FTE_OK;
+        default: fte_set_error("unknown near-pair arithmetic %d", opt->near); return FTE_ERR_INVALID;
+    }
+}
+
+bool fte_near_ff_ok(double tol) {
+    // float-float terms carry ~1e-13 relative error (exp, K(x) and the
+    // reciprocal ~4e-14 each); from tol 1e-11 up that stays two orders below
+    return tol >= 1e-11;
+}
 
 double fte_near_fp32_threshold(double tol) {
     // FP32 terms carry relative rounding ~1e-7 and a pair's terms scale with
@@ -685,7 +1044,7 @@ double fte_near_fp32_threshold(double tol) {
 }
 
 void fte_near_fill_params(int kind, const CellList& cl, double xi, double Lx, double Ly, NearParamsHost* hp,
-                          double x32) {
+                          double x32, bool ff) {
     NearParams& p = *reinterpret_cast<NearParams*>(hp->raw);
     p.nsx = cl.nsx;
     p.nsy = cl.nsy;
@@ -711,6 +1070,17 @@ void fte_near_fill_params(int kind, const CellList& cl, double xi, double Lx, do
     double bmax = bsx > bsy ? bsx : bsy;
     p.cut32 = (float)(p.cutoffsq + 1e-4 * bmax * bmax);
     p.x32 = x32 >= 1e30 ? INFINITY : (float)(x32 > 1.0 ? x32 : 1.0);
+    p.ffnear = ff ? 1 : 0;
+    {
+        const float h = (float)p.xi2;
+        p.xi2ff = make_float2(h, (float)(p.xi2 - (double)h));
+        const float g = (float)p.pf;
+        p.pfff = make_float2(g, (float)(p.pf - (double)g));
+        const float c = (float)p.cutoffsq;
+        p.cutff = make_float2(c, (float)(p.cutoffsq - (double)c));
+        const float q = (float)p.selfc;
+        p.selcff = make_float2(q, (float)(p.selfc - (double)q));
+    }
     p.cap = 0;
     p.ur = nullptr;
     p.ustride = 0;
@@ -722,8 +1092,9 @@ size_t fte_near_params_size() { return sizeof(NearParams); }
 namespace {
 template <int KIND, int NV>
 int near_launch_one(fte_context* ctx, NearParams p) {
-    p.cap = near_cap<KIND, NV>(ctx);
-    size_t smem = NearSmem<KIND, NV>::bytes(p.cap);
+    const bool ff = NV <= 2 && p.ffnear;
+    p.cap = near_cap<KIND, NV>(ctx, ff);
+    size_t smem = NearSmem<KIND, NV>::bytes(p.cap, ff);
     int grid = p.nb < ctx->num_sms * 16 ? p.nb : ctx->num_sms * 16;
     if (grid < 1) grid = 1;
     FTE_CUDA_TRY(cudaFuncSetAttribute(k_near<KIND, NV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -733,7 +1104,7 @@ int near_launch_one(fte_context* ctx, NearParams p) {
 
 template <int KIND, int NV>
 int near_launch_batch(fte_context* ctx, const unsigned char* plist_dev, const int2* items, int nitems) {
-    size_t smem = NearSmem<KIND, NV>::bytes(near_cap<KIND, NV>(ctx));
+    size_t smem = near_smem_any<KIND, NV>(ctx);
     int grid = nitems < ctx->num_sms * 16 ? nitems : ctx->num_sms * 16;
     if (grid < 1) return FTE_OK;
     FTE_CUDA_TRY(cudaFuncSetAttribute(k_near_batch<KIND, NV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -742,20 +1113,23 @@ int near_launch_batch(fte_context* ctx, const unsigned char* plist_dev, const in
 }
 }  // namespace
 
-int fte_near_cap(const fte_context* ctx, int kind, int nv) {
+bool fte_near_uses_ff(const NearParamsHost& hp) { return reinterpret_cast<const NearParams*>(hp.raw)->ffnear != 0; }
+
+int fte_near_cap(const fte_context* ctx, int kind, int nv, bool ff) {
+    ff = ff && nv <= 2;
     if (kind == FTE_KIND_SLP) {
         switch (nv) {
-            case 1: return near_cap<FTE_KIND_SLP, 1>(ctx);
-            case 2: return near_cap<FTE_KIND_SLP, 2>(ctx);
-            case 3: return near_cap<FTE_KIND_SLP, 3>(ctx);
-            default: return near_cap<FTE_KIND_SLP, 4>(ctx);
+            case 1: return near_cap<FTE_KIND_SLP, 1>(ctx, ff);
+            case 2: return near_cap<FTE_KIND_SLP, 2>(ctx, ff);
+            case 3: return near_cap<FTE_KIND_SLP, 3>(ctx, ff);
+            default: return near_cap<FTE_KIND_SLP, 4>(ctx, ff);
         }
     }
     switch (nv) {
-        case 1: return near_cap<FTE_KIND_DLP, 1>(ctx);
-        case 2: return near_cap<FTE_KIND_DLP, 2>(ctx);
-        case 3: return near_cap<FTE_KIND_DLP, 3>(ctx);
-        default: return near_cap<FTE_KIND_DLP, 4>(ctx);
+        case 1: return near_cap<FTE_KIND_DLP, 1>(ctx, ff);
+        case 2: return near_cap<FTE_KIND_DLP, 2>(ctx, ff);
+        case 3: return near_cap<FTE_KIND_DLP, 3>(ctx, ff);
+        default: return near_cap<FTE_KIND_DLP, 4>(ctx, ff);
     }
 }
 
@@ -802,9 +1176,9 @@ int fte_near_launch_batch(fte_context* ctx, int kind, int nv, const void* plist_
 }
 
 int fte_near_launch(fte_context* ctx, int kind, const CellList& cl, double xi, double Lx, double Ly, double2* ur,
-                    double x32) {
+                    double x32, bool ff) {
     NearParamsHost hp;
-    fte_near_fill_params(kind, cl, xi, Lx, Ly, &hp, x32);
+    fte_near_fill_params(kind, cl, xi, Lx, Ly, &hp, x32, ff);
     return fte_near_launch_nv(ctx, kind, 1, hp, ur, 0);
 }
 

@@ -400,9 +400,11 @@ extern "C" int fte_plan_create(fte_context* c, int kind, const double* xsrc, con
     cl.q1 = p->q1;
     cl.q2 = p->q2;
     cl.qstride = nsrc;
-    fte_near_fill_params(kind, cl, prm.xi, Lx, Ly, &p->near,
-                         opt->form == FTE_FORM_MIXED ? fte_near_fp32_threshold(prm.tol) : HUGE_VAL);
-    fte_near_set_output(&p->near, p->ur, ntar, fte_near_cap(c, kind, nv));
+    double x32;
+    bool ffn;
+    FTE_TRY(fte_near_classes(opt, prm.tol, &x32, &ffn));
+    fte_near_fill_params(kind, cl, prm.xi, Lx, Ly, &p->near, x32, ffn);
+    fte_near_set_output(&p->near, p->ur, ntar, fte_near_cap(c, kind, nv, fte_near_uses_ff(p->near)));
     // warm the FFT tables so that executions (and graph capture) allocate nothing
     FTE_TRY(fte_fft_prepare(c, prm.Mx));
     FTE_TRY(fte_fft_prepare(c, prm.My));
@@ -589,7 +591,7 @@ extern "C" int fte_batch_create(fte_context* c, fte_plan* const* plans, int npla
         if (p->ntar > 0) {
             int k = p->kind;
             NearParamsHost h = p->near;
-            fte_near_set_output(&h, p->ur, p->ntar, fte_near_cap(c, k, nv));
+            fte_near_set_output(&h, p->ur, p->ntar, fte_near_cap(c, k, nv, fte_near_uses_ff(h)));
             int idx = (int)pls[k].size();
             pls[k].push_back(h);
             int nb = p->prm.nside_x * p->prm.nside_y;

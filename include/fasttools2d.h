@@ -68,6 +68,14 @@ extern "C" {
 #define FTE_KSPACE_FP32 2
 #define FTE_KSPACE_FF 3
 
+/* fte_options.near (FTE_FORM_MIXED): the arithmetic of the real-space pairs;
+ * AUTO: FP32 for pairs whose terms are below the tolerance's reach of FP32
+ * rounding, float-float for the others where the tolerance allows (>= 1e-11),
+ * else FP64 */
+#define FTE_NEAR_AUTO 0
+#define FTE_NEAR_FP64 1 /* every pair in FP64 */
+#define FTE_NEAR_FF 2   /* float-float pairs (stresslet pairs with xi^2 r^2 < 1e-8 in FP64), no FP32 class */
+
 /* kinds */
 #define FTE_KIND_SLP 0
 #define FTE_KIND_DLP 1
@@ -108,6 +116,7 @@ typedef struct {
     int tune;              /* plans: 1 = time the k-space tile sizes on the plan's points at creation */
     double slack;          /* FTE_FORM_MIXED: error-estimate slack of the tuned choice (0: calibrated) */
     int kspace;            /* FTE_FORM_MIXED: FTE_KSPACE_* (0: the chooser's pick) */
+    int near;              /* FTE_FORM_MIXED: FTE_NEAR_* (0: by tolerance) */
 } fte_options;
 
 /* Per-call diagnostics (optional output of the driver entries). */

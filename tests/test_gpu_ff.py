@@ -124,3 +124,39 @@ def test_ff_plan_matches_driver(gpu_ctx, tune):
             ref = np.stack([o[0], o[1]], 1)
             got = np.stack([np.asarray(u1s[v]), np.asarray(u2s[v])], 1)
             assert np.max(np.abs(got - ref)) <= 1e-12 * np.max(np.abs(ref)), (kind, v)
+
+
+@pytest.mark.parametrize("kind", ["slp", "dlp"])
+@pytest.mark.parametrize("geom", [(20000, 1.0, 1.0, 71), (12000, 2.0, 1.0, 72), (9000, 1.0, 2.75, 73)])
+def test_ff_near_matches_fp64(gpu_ctx, kind, geom):
+    """Float-float pairs against FP64 pairs on the same parameters, without
+    the FP32 class: real-space parts within 1e-12 of their maximum."""
+    ft = _ft()
+    n, Lx, Ly, seed = geom
+    d = _case(seed, n, Lx, Ly)
+    out_f, info = _run(ft, gpu_ctx, kind, d, Lx, Ly, tol=1e-10, kspace=ft.KSPACE_FP64, near=ft.NEAR_FF)
+    p = info.params
+    same = dict(P=p.P, xi=p.xi, Mx=p.Mx, My=p.My, nside_x=p.nside_x, nside_y=p.nside_y)
+    out_d, _ = _run(ft, gpu_ctx, kind, d, Lx, Ly, tol=1e-10, kspace=ft.KSPACE_FP64, near=ft.NEAR_FP64, **same)
+    ur_f, ur_d = out_f[2], out_d[2]
+    rel = np.max(np.abs(ur_f - ur_d)) / np.max(np.abs(ur_d))
+    assert rel <= 1e-12, rel
+
+
+def test_ff_near_two_vectors(gpu_ctx):
+    """Plans with two density vectors (two targets in flight per warp) take
+    the float-float class too; compared with FP64 pairs."""
+    ft = _ft()
+    n, Lx, Ly = 15000, 1.0, 1.0
+    xs, ys, xt, yt, f1, f2, n1, n2 = _case(81, n, Lx, Ly)
+    rng = np.random.default_rng(82)
+    fs1, fs2 = rng.standard_normal((2, n)), rng.standard_normal((2, n))
+    for kind in (ft.KIND_SLP, ft.KIND_DLP):
+        res = []
+        for near in (ft.NEAR_FF, ft.NEAR_FP64):
+            plan = ft.Plan(kind, xs, ys, xt, yt, f1, f2, Lx, Ly, n1=n1, n2=n2, tol=1e-10, form=ft.FORM_MIXED,
+                           kspace=ft.KSPACE_FP64, near=near, nvmax=2, ctx=gpu_ctx, nside_x=60, nside_y=60)
+            u1s, u2s = plan.execute(fs1, fs2)
+            res.append(np.stack([np.asarray(u1s), np.asarray(u2s)], -1))
+        rel = np.max(np.abs(res[0] - res[1])) / np.max(np.abs(res[1]))
+        assert rel <= 1e-12, (kind, rel)
