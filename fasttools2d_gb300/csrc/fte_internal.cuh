@@ -271,7 +271,8 @@ int fte_near_cap(const fte_context* ctx, int kind, int nv, bool ff);
 int fte_near_launch_nv(fte_context* ctx, int kind, int nv, const NearParamsHost& hp, double2* ur, long long ustride);
 // many problems in one launch: plist_dev = device array of the filled
 // descriptions (ur/ustride/cap set), items = (problem, box) pairs
-int fte_near_launch_batch(fte_context* ctx, int kind, int nv, const void* plist_dev, const int2* items, int nitems);
+int fte_near_launch_batch(fte_context* ctx, int kind, int nv, bool ff, const void* plist_dev, const int2* items,
+                          int nitems);
 void fte_near_set_output(NearParamsHost* hp, double2* ur, long long ustride, int cap);
 
 struct KspaceArgs {

@@ -297,15 +297,18 @@ struct NearSmem {
 // All targets of box b against the 3x3 neighbourhood of sources, for NV
 // density vectors at once: the pair geometry and the special functions are
 // evaluated once per pair and shared by the vectors.
-template <int KIND, int NV>
+template <int KIND, int NV, bool FF>
 __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned char* smem_raw, int* nb_box,
                                          int* nb_start, double* nb_shx, double* nb_shy) {
     constexpr int kDen = NearSmem<KIND, NV>::kDen;
-    constexpr int NSLOT = NearSmem<KIND, NV>::kSlots;
+    // float-float class (FF; density vectors beyond two keep the FP64 path:
+    // the float-float accumulators would not fit the register budget)
+    constexpr bool ffn = FF && NV <= 2;
+    // targets in flight: the FP64 classes gain from four (partial FP64
+    // batches are what costs), the float-float ones from two (the slot
+    // selects are what costs)
+    constexpr int NSLOT = ffn ? 2 : NearSmem<KIND, NV>::kSlots;
     const int cap = prm.cap;
-    // float-float class (density vectors beyond two keep the FP64 path: the
-    // float-float accumulators would not fit the register budget)
-    const bool ffn = NV <= 2 && prm.ffnear != 0;
     const double* ktab = reinterpret_cast<const double*>(smem_raw);
     const double* etab = ktab + kKtab;
     const float2* ktabff = reinterpret_cast<const float2*>(etab + 64);
@@ -465,35 +468,46 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
         bool any64 = !ffn;
 
         // slot `tag`'s accumulators of vector v, selected into (a0, a1) and
-        // back: register moves only, no FP64 work per slot
+        // back: selects only (written as conditional expressions, which
+        // compile to selects rather than branches), no FP64 work per slot
         auto acc_get = [&](int tag, int v, double& a0, double& a1) {
             a0 = acc[0][v][0];
             a1 = acc[0][v][1];
 #pragma unroll
             for (int j = 1; j < NSLOT; j++)
-                if (tag == j) a0 = acc[j][v][0], a1 = acc[j][v][1];
+                {
+                    const bool m = tag == j;
+                    a0 = m ? acc[j][v][0] : a0;
+                    a1 = m ? acc[j][v][1] : a1;
+                }
         };
         auto acc_put = [&](int tag, int v, double a0, double a1) {
 #pragma unroll
             for (int j = 0; j < NSLOT; j++)
-                if (tag == j) acc[j][v][0] = a0, acc[j][v][1] = a1;
+                {
+                    const bool m = tag == j;
+                    acc[j][v][0] = m ? a0 : acc[j][v][0];
+                    acc[j][v][1] = m ? a1 : acc[j][v][1];
+                }
         };
         auto accf_get = [&](int tag, int v, float* a) {
 #pragma unroll
             for (int i = 0; i < 4; i++) a[i] = accf[0][v][i];
 #pragma unroll
             for (int j = 1; j < NSLOT; j++)
-                if (tag == j) {
+                {
+                    const bool m = tag == j;
 #pragma unroll
-                    for (int i = 0; i < 4; i++) a[i] = accf[j][v][i];
+                    for (int i = 0; i < 4; i++) a[i] = m ? accf[j][v][i] : a[i];
                 }
         };
         auto accf_put = [&](int tag, int v, const float* a) {
 #pragma unroll
             for (int j = 0; j < NSLOT; j++)
-                if (tag == j) {
+                {
+                    const bool m = tag == j;
 #pragma unroll
-                    for (int i = 0; i < 4; i++) accf[j][v][i] = a[i];
+                    for (int i = 0; i < 4; i++) accf[j][v][i] = m ? a[i] : accf[j][v][i];
                 }
         };
 
@@ -956,21 +970,21 @@ __device__ __forceinline__ void near_load_tables(unsigned char* smem_raw) {
 }
 
 // one problem: grid-stride over its boxes
-template <int KIND, int NV>
+template <int KIND, int NV, bool FF>
 __global__ void __launch_bounds__(kNearThreads, 2) k_near(const NearParams prm) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int nb_box[9], nb_start[10];
     __shared__ double nb_shx[9], nb_shy[9];
     near_load_tables<KIND, NV>(smem_raw);
     for (int b = blockIdx.x; b < prm.nb; b += gridDim.x)
-        near_box<KIND, NV>(prm, b, smem_raw, nb_box, nb_start, nb_shx, nb_shy);
+        near_box<KIND, NV, FF>(prm, b, smem_raw, nb_box, nb_start, nb_shx, nb_shy);
 }
 
 // many problems: grid-stride over a (problem, box) work list; descriptions
 // are stored in NearParamsHost slots (kParamStride bytes apart)
 constexpr int kParamStride = sizeof(NearParamsHost);
 
-template <int KIND, int NV>
+template <int KIND, int NV, bool FF>
 __global__ void __launch_bounds__(kNearThreads, 2) k_near_batch(const unsigned char* __restrict__ plist,
                                                                 const int2* __restrict__ items, int nitems) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -981,7 +995,7 @@ __global__ void __launch_bounds__(kNearThreads, 2) k_near_batch(const unsigned c
         const int2 w = items[it];
         // read in place (a register copy of the description would spill)
         const NearParams& prm = *reinterpret_cast<const NearParams*>(plist + (size_t)w.x * kParamStride);
-        near_box<KIND, NV>(prm, w.y, smem_raw, nb_box, nb_start, nb_shx, nb_shy);
+        near_box<KIND, NV, FF>(prm, w.y, smem_raw, nb_box, nb_start, nb_shx, nb_shy);
     }
 }
 
@@ -992,14 +1006,6 @@ int near_cap(const fte_context* ctx, bool ff) {
     while (cap > 128 && NearSmem<KIND, NV>::bytes(cap, ff) > budget) cap -= 64;
     return cap;
 }
-// shared memory of a launch whose problems may use either layout
-template <int KIND, int NV>
-size_t near_smem_any(const fte_context* ctx) {
-    const size_t a = NearSmem<KIND, NV>::bytes(near_cap<KIND, NV>(ctx, false), false);
-    const size_t b = NearSmem<KIND, NV>::bytes(near_cap<KIND, NV>(ctx, true), true);
-    return a > b ? a : b;
-}
-
 }  // namespace
 
 int fte_near_classes(const fte_options* opt, double tol, double* x32, bool* ff) {
@@ -1097,18 +1103,41 @@ int near_launch_one(fte_context* ctx, NearParams p) {
     size_t smem = NearSmem<KIND, NV>::bytes(p.cap, ff);
     int grid = p.nb < ctx->num_sms * 16 ? p.nb : ctx->num_sms * 16;
     if (grid < 1) grid = 1;
-    FTE_CUDA_TRY(cudaFuncSetAttribute(k_near<KIND, NV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    FTE_LAUNCH(ctx, (k_near<KIND, NV>), grid, kNearThreads, smem, p);
+    if constexpr (NV <= 2) {
+        if (ff) {
+            FTE_CUDA_TRY(
+                cudaFuncSetAttribute(k_near<KIND, NV, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            FTE_LAUNCH(ctx, (k_near<KIND, NV, true>), grid, kNearThreads, smem, p);
+            return FTE_OK;
+        }
+    }
+    {
+        FTE_CUDA_TRY(
+            cudaFuncSetAttribute(k_near<KIND, NV, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        FTE_LAUNCH(ctx, (k_near<KIND, NV, false>), grid, kNearThreads, smem, p);
+    }
     return FTE_OK;
 }
 
 template <int KIND, int NV>
-int near_launch_batch(fte_context* ctx, const unsigned char* plist_dev, const int2* items, int nitems) {
-    size_t smem = near_smem_any<KIND, NV>(ctx);
+int near_launch_batch(fte_context* ctx, bool ff, const unsigned char* plist_dev, const int2* items, int nitems) {
+    ff = ff && NV <= 2;
+    const size_t smem = NearSmem<KIND, NV>::bytes(near_cap<KIND, NV>(ctx, ff), ff);
     int grid = nitems < ctx->num_sms * 16 ? nitems : ctx->num_sms * 16;
     if (grid < 1) return FTE_OK;
-    FTE_CUDA_TRY(cudaFuncSetAttribute(k_near_batch<KIND, NV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    FTE_LAUNCH(ctx, (k_near_batch<KIND, NV>), grid, kNearThreads, smem, plist_dev, items, nitems);
+    if constexpr (NV <= 2) {
+        if (ff) {
+            FTE_CUDA_TRY(cudaFuncSetAttribute(k_near_batch<KIND, NV, true>,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            FTE_LAUNCH(ctx, (k_near_batch<KIND, NV, true>), grid, kNearThreads, smem, plist_dev, items, nitems);
+            return FTE_OK;
+        }
+    }
+    {
+        FTE_CUDA_TRY(cudaFuncSetAttribute(k_near_batch<KIND, NV, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smem));
+        FTE_LAUNCH(ctx, (k_near_batch<KIND, NV, false>), grid, kNearThreads, smem, plist_dev, items, nitems);
+    }
     return FTE_OK;
 }
 }  // namespace
@@ -1157,21 +1186,22 @@ int fte_near_launch_nv(fte_context* ctx, int kind, int nv, const NearParamsHost&
     }
 }
 
-int fte_near_launch_batch(fte_context* ctx, int kind, int nv, const void* plist_dev, const int2* items, int nitems) {
+int fte_near_launch_batch(fte_context* ctx, int kind, int nv, bool ff, const void* plist_dev, const int2* items,
+                          int nitems) {
     const unsigned char* pl = static_cast<const unsigned char*>(plist_dev);
     if (kind == FTE_KIND_SLP) {
         switch (nv) {
-            case 1: return near_launch_batch<FTE_KIND_SLP, 1>(ctx, pl, items, nitems);
-            case 2: return near_launch_batch<FTE_KIND_SLP, 2>(ctx, pl, items, nitems);
-            case 3: return near_launch_batch<FTE_KIND_SLP, 3>(ctx, pl, items, nitems);
-            default: return near_launch_batch<FTE_KIND_SLP, 4>(ctx, pl, items, nitems);
+            case 1: return near_launch_batch<FTE_KIND_SLP, 1>(ctx, ff, pl, items, nitems);
+            case 2: return near_launch_batch<FTE_KIND_SLP, 2>(ctx, ff, pl, items, nitems);
+            case 3: return near_launch_batch<FTE_KIND_SLP, 3>(ctx, ff, pl, items, nitems);
+            default: return near_launch_batch<FTE_KIND_SLP, 4>(ctx, ff, pl, items, nitems);
         }
     }
     switch (nv) {
-        case 1: return near_launch_batch<FTE_KIND_DLP, 1>(ctx, pl, items, nitems);
-        case 2: return near_launch_batch<FTE_KIND_DLP, 2>(ctx, pl, items, nitems);
-        case 3: return near_launch_batch<FTE_KIND_DLP, 3>(ctx, pl, items, nitems);
-        default: return near_launch_batch<FTE_KIND_DLP, 4>(ctx, pl, items, nitems);
+        case 1: return near_launch_batch<FTE_KIND_DLP, 1>(ctx, ff, pl, items, nitems);
+        case 2: return near_launch_batch<FTE_KIND_DLP, 2>(ctx, ff, pl, items, nitems);
+        case 3: return near_launch_batch<FTE_KIND_DLP, 3>(ctx, ff, pl, items, nitems);
+        default: return near_launch_batch<FTE_KIND_DLP, 4>(ctx, ff, pl, items, nitems);
     }
 }
 

@@ -169,10 +169,11 @@ struct fte_batch {
     int nv = 1;
     char* mem = nullptr;
     std::vector<double*> f1, f2, u1, u2;
-    // batched near-field work lists (device): per kind, plist + items
-    void* plist[2] = {nullptr, nullptr};
-    int2* items[2] = {nullptr, nullptr};
-    int nitems[2] = {0, 0};
+    // batched near-field work lists (device): per kind and near-pair form
+    // (list kind * 2 + ff), plist + items
+    void* plist[4] = {nullptr, nullptr, nullptr, nullptr};
+    int2* items[4] = {nullptr, nullptr, nullptr, nullptr};
+    int nitems[4] = {0, 0, 0, 0};
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     std::vector<cudaStream_t> streams;
@@ -494,9 +495,9 @@ static int batch_run(fte_batch* b) {
                        (const int*)p->cl.sidx, p->q0, p->q1, p->q2, p->fv);
     }
     // one persistent near-field launch per kind over all (plan, box) items
-    for (int kind = 0; kind < 2; kind++)
-        if (b->nitems[kind] > 0)
-            FTE_TRY(fte_near_launch_batch(c, kind, b->nv, b->plist[kind], b->items[kind], b->nitems[kind]));
+    for (int l = 0; l < 4; l++)
+        if (b->nitems[l] > 0)
+            FTE_TRY(fte_near_launch_batch(c, l / 2, b->nv, l % 2 == 1, b->plist[l], b->items[l], b->nitems[l]));
     // k-space and combination of every plan on forked streams
     const int S = (int)b->streams.size();
     FTE_CUDA_TRY(cudaEventRecord(b->events[0], main));
@@ -583,22 +584,23 @@ extern "C" int fte_batch_create(fte_context* c, fte_plan* const* plans, int npla
     b->plans.assign(plans, plans + nplans);
     // device buffers of densities and velocities, and the near-field work lists
     size_t need = 0;
-    std::vector<int2> its[2];
-    std::vector<NearParamsHost> pls[2];
+    std::vector<int2> its[4];
+    std::vector<NearParamsHost> pls[4];
     for (int i = 0; i < nplans; i++) {
         fte_plan* p = plans[i];
         need += 2 * ws_bytes(nv * (p->nsrc + 1), 8) + 2 * ws_bytes(nv * (p->ntar + 1), 8);
         if (p->ntar > 0) {
-            int k = p->kind;
             NearParamsHost h = p->near;
-            fte_near_set_output(&h, p->ur, p->ntar, fte_near_cap(c, k, nv, fte_near_uses_ff(h)));
+            const bool ff = fte_near_uses_ff(h) && nv <= 2;
+            const int k = p->kind * 2 + (ff ? 1 : 0);
+            fte_near_set_output(&h, p->ur, p->ntar, fte_near_cap(c, p->kind, nv, ff));
             int idx = (int)pls[k].size();
             pls[k].push_back(h);
             int nb = p->prm.nside_x * p->prm.nside_y;
             for (int box = 0; box < nb; box++) its[k].push_back(make_int2(idx, box));
         }
     }
-    for (int k = 0; k < 2; k++)
+    for (int k = 0; k < 4; k++)
         need += ws_bytes(pls[k].size() * sizeof(NearParamsHost), 1) + ws_bytes(its[k].size() * sizeof(int2), 1);
     need += 4096;
     if (cudaMalloc(&b->mem, need) != cudaSuccess) {
@@ -615,7 +617,7 @@ extern "C" int fte_batch_create(fte_context* c, fte_plan* const* plans, int npla
         b->u1.push_back(bm.take<double>(nv * (p->ntar + 1)));
         b->u2.push_back(bm.take<double>(nv * (p->ntar + 1)));
     }
-    for (int k = 0; k < 2; k++) {
+    for (int k = 0; k < 4; k++) {
         b->nitems[k] = (int)its[k].size();
         if (b->nitems[k] == 0) continue;
         b->plist[k] = bm.take<NearParamsHost>(pls[k].size());
@@ -629,7 +631,7 @@ extern "C" int fte_batch_create(fte_context* c, fte_plan* const* plans, int npla
     // zero the density/velocity buffers, then upload the work lists (in that
     // order, on the context's stream, finished before the host vectors go)
     FTE_CUDA_TRY(cudaMemsetAsync(b->mem, 0, bm.off, c->stream));
-    for (int k = 0; k < 2; k++) {
+    for (int k = 0; k < 4; k++) {
         if (b->nitems[k] == 0) continue;
         FTE_CUDA_TRY(cudaMemcpyAsync(b->plist[k], pls[k].data(), pls[k].size() * sizeof(NearParamsHost),
                                      cudaMemcpyHostToDevice, c->stream));
