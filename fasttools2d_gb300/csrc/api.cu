@@ -68,6 +68,9 @@ static void plan_free(FftPlan* p) {
     cudaFree(p->tw32);
     cudaFree(p->chirp32);
     cudaFree(p->bhat32);
+    cudaFree(p->twff);
+    cudaFree(p->chirpff);
+    cudaFree(p->bhatff);
     delete p;
 }
 
@@ -247,6 +250,12 @@ static void host_dft(std::vector<std::complex<double>>& a) {
     }
 }
 
+// float-float copy of a complex FP64 value
+static float4 ff4(std::complex<double> z) {
+    const float rh = (float)z.real(), ih = (float)z.imag();
+    return make_float4(rh, (float)(z.real() - (double)rh), ih, (float)(z.imag() - (double)ih));
+}
+
 template <typename T>
 static int upload(T** dst, const std::vector<T>& v) {
     FTE_CUDA_TRY(cudaMalloc(dst, v.size() * sizeof(T)));
@@ -282,37 +291,46 @@ int fte_get_plan(fte_context* c, int n, FftDev* out) {
         const int m = p->m;
         std::vector<double2> tw(m);
         std::vector<float2> tw32(m);
+        std::vector<float4> twf(m);
         for (int t = 0; t < m; t++) {
             auto z = unit_root(t, m);
             tw[t] = make_double2(z.real(), z.imag());
             tw32[t] = make_float2((float)z.real(), (float)z.imag());
+            twf[t] = ff4(z);
         }
         int st = upload(&p->tw, tw);
         if (!st) st = upload(&p->tw32, tw32);
+        if (!st) st = upload(&p->twff, twf);
         if (!st && p->bluestein) {
             std::vector<double2> ch(n);
             std::vector<float2> ch32(n);
+            std::vector<float4> chf(n);
             std::vector<std::complex<double>> b(m, 0.0);
             for (int k = 0; k < n; k++) {
                 long long k2 = ((long long)k * k) % (2LL * n);
                 auto z = unit_root(k2, 2LL * n);  // exp(-i pi k^2 / n)
                 ch[k] = make_double2(z.real(), z.imag());
                 ch32[k] = make_float2((float)z.real(), (float)z.imag());
+                chf[k] = ff4(z);
                 b[k] = std::conj(z);
                 if (k > 0) b[m - k] = std::conj(z);
             }
             host_dft(b);
             std::vector<double2> bh(m);
             std::vector<float2> bh32(m);
+            std::vector<float4> bhf(m);
             for (int k = 0; k < m; k++) {
                 auto z = b[k] / (double)m;
                 bh[k] = make_double2(z.real(), z.imag());
                 bh32[k] = make_float2((float)z.real(), (float)z.imag());
+                bhf[k] = ff4(z);
             }
             st = upload(&p->chirp, ch);
             if (!st) st = upload(&p->chirp32, ch32);
             if (!st) st = upload(&p->bhat, bh);
             if (!st) st = upload(&p->bhat32, bh32);
+            if (!st) st = upload(&p->chirpff, chf);
+            if (!st) st = upload(&p->bhatff, bhf);
         }
         if (st) {
             plan_free(p);
@@ -331,6 +349,9 @@ int fte_get_plan(fte_context* c, int n, FftDev* out) {
     out->tw32 = p->tw32;
     out->chirp32 = p->chirp32;
     out->bhat32 = p->bhat32;
+    out->twff = p->twff;
+    out->chirpff = p->chirpff;
+    out->bhatff = p->bhatff;
     return FTE_OK;
 }
 

@@ -62,6 +62,9 @@ struct FftPlan {
     float2* tw32 = nullptr;    // FP32 copies for the mixed form
     float2* chirp32 = nullptr;
     float2* bhat32 = nullptr;
+    float4* twff = nullptr;    // float-float copies (re hi, re lo, im hi, im lo)
+    float4* chirpff = nullptr;
+    float4* bhatff = nullptr;
 };
 
 // Device view of a plan passed by value to kernels.
@@ -74,6 +77,9 @@ struct FftDev {
     const float2* tw32;
     const float2* chirp32;
     const float2* bhat32;
+    const float4* twff;
+    const float4* chirpff;
+    const float4* bhatff;
 };
 
 // Long 1-D transforms: lines whose block transform does not fit one block's

@@ -530,6 +530,68 @@ __global__ void k_fft_y_c2r(const double2* __restrict__ Hh, double* __restrict__
     }
 }
 
+// ---- the same three transforms in float-float (FFT lines of FfCx) --------------
+__global__ void k_fft_y_r2c_ff(const double* __restrict__ H, float4* __restrict__ Hh, int Mx, int My, FftDev plan) {
+    extern __shared__ __align__(16) unsigned char shff[];
+    float4* A = reinterpret_cast<float4*>(shff);
+    float4* B = A + plan.m;
+    const int c = blockIdx.x, g = blockIdx.y;
+    const int Kh = My / 2 + 1;
+    const double* h0 = H + ((size_t)g * Mx + 2 * c) * My;
+    const double* h1 = h0 + My;
+    for (int y = threadIdx.x; y < My; y += blockDim.x) A[y] = ffc_mk(ff_split(h0[y]), ff_split(h1[y]));
+    float4* R = fft_block<FfCx>(A, B, plan, false);
+    float4* o0 = Hh + ((size_t)g * Mx + 2 * c) * Kh;
+    float4* o1 = o0 + Kh;
+    const float2 half = make_float2(0.5f, 0.0f);
+    for (int k = threadIdx.x; k < Kh; k += blockDim.x) {
+        const float4 zk = R[k], zm = R[(My - k) % My];
+        // A_k = (Z_k + conj Z_{-k})/2,  B_k = (Z_k - conj Z_{-k})/(2i)
+        o0[k] = cscale(ffc_mk(ff_add(ffc_re(zk), ffc_re(zm)), ff_add(ffc_im(zk), ff_neg(ffc_im(zm)))), half);
+        o1[k] = cscale(ffc_mk(ff_add(ffc_im(zk), ffc_im(zm)), ff_add(ffc_re(zm), ff_neg(ffc_re(zk)))), half);
+    }
+}
+
+__global__ void k_fft_x_ff(float4* __restrict__ Hh, int Mx, int Kh, FftDev plan, int inv) {
+    extern __shared__ __align__(16) unsigned char shff[];
+    float4* A = reinterpret_cast<float4*>(shff);
+    float4* B = A + plan.m;
+    const int k = blockIdx.x, g = blockIdx.y;
+    float4* base = Hh + (size_t)g * Mx * Kh + k;
+    for (int x = threadIdx.x; x < Mx; x += blockDim.x) A[x] = base[(size_t)x * Kh];
+    float4* R = fft_block<FfCx>(A, B, plan, inv != 0);
+    for (int x = threadIdx.x; x < Mx; x += blockDim.x) base[(size_t)x * Kh] = R[x];
+}
+
+// half spectra -> real grids as float-float pairs (the gather's input)
+__global__ void k_fft_y_c2r_ff(const float4* __restrict__ Hh, float2* __restrict__ H, int Mx, int My, FftDev plan) {
+    extern __shared__ __align__(16) unsigned char shff[];
+    float4* A = reinterpret_cast<float4*>(shff);
+    float4* B = A + plan.m;
+    const int c = blockIdx.x, g = blockIdx.y;
+    const int Kh = My / 2 + 1;
+    const float4* i0 = Hh + ((size_t)g * Mx + 2 * c) * Kh;
+    const float4* i1 = i0 + Kh;
+    for (int k = threadIdx.x; k < Kh; k += blockDim.x) {
+        float4 a = i0[k], b = i1[k];
+        if (k == 0 || 2 * k == My) {
+            a.z = a.w = 0.f;
+            b.z = b.w = 0.f;
+        }
+        // Z_k = a + i b ; Z_{My-k} = conj(a) + i conj(b)
+        A[k] = ffc_mk(ff_add(ffc_re(a), ff_neg(ffc_im(b))), ff_add(ffc_im(a), ffc_re(b)));
+        if (k > 0 && 2 * k < My) A[My - k] = ffc_mk(ff_add(ffc_re(a), ffc_im(b)), ff_add(ffc_re(b), ff_neg(ffc_im(a))));
+    }
+    float4* R = fft_block<FfCx>(A, B, plan, true);
+    float2* o0 = H + ((size_t)g * Mx + 2 * c) * My;
+    float2* o1 = o0 + My;
+    for (int y = threadIdx.x; y < My; y += blockDim.x) {
+        const float4 z = R[y];
+        o0[y] = ffc_re(z);
+        o1[y] = ffc_im(z);
+    }
+}
+
 // ---- k-space multipliers ------------------------------------------------------
 // SLP (mex_stokes_slp_kspace.cpp:128-139): G = (K^2 H - k (k.H)) (1/K^4 + 1/(4 xi^2 K^2)) e^{-(1-eta)K^2/(4xi^2)}
 __device__ __forceinline__ void slp_mult(double k1, double k2, double xi, double eta, double2 q1, double2 q2,
@@ -557,17 +619,29 @@ __device__ __forceinline__ void dlp_mult(double k1, double k2, double xi, double
     g2 = make_double2(-x2i * e, x2r * e);
 }
 
-template <int KIND>
-__global__ void k_filter(double2* __restrict__ Hh, int Mx, int My, double Lx, double Ly, double xi, double eta) {
+// spectra in FP64 (double2) or float-float (float4), read and written in FP64
+__device__ __forceinline__ double2 spec_ld(const double2* p) { return *p; }
+__device__ __forceinline__ double2 spec_ld(const float4* p) {
+    const float4 v = *p;
+    return make_double2(ff_join(v.x, v.y), ff_join(v.z, v.w));
+}
+__device__ __forceinline__ void spec_st(double2* p, double2 v) { *p = v; }
+__device__ __forceinline__ void spec_st(float4* p, double2 v) {
+    const float2 r = ff_split(v.x), i = ff_split(v.y);
+    *p = make_float4(r.x, r.y, i.x, i.y);
+}
+
+template <int KIND, typename S>
+__global__ void k_filter(S* __restrict__ Hh, int Mx, int My, double Lx, double Ly, double xi, double eta) {
     const int Kh = My / 2 + 1;
     const size_t GS = (size_t)Mx * Kh;
     const size_t tot = GS;
     for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < tot; idx += (size_t)gridDim.x * blockDim.x) {
         int j = (int)(idx / Kh), k = (int)(idx % Kh);
-        double2* p0 = Hh + idx;
+        S* p0 = Hh + idx;
         if (j == 0 && k == 0) {
-            p0[0] = make_double2(0, 0);
-            p0[GS] = make_double2(0, 0);
+            spec_st(p0, make_double2(0, 0));
+            spec_st(p0 + GS, make_double2(0, 0));
             continue;
         }
         double k1 = (j <= Mx / 2) ? 2.0 * FTE_PI / Lx * j : 2.0 * FTE_PI / Lx * (j - Mx);
@@ -575,7 +649,7 @@ __global__ void k_filter(double2* __restrict__ Hh, int Mx, int My, double Lx, do
         bool nyq_x = (2 * j == Mx), nyq_y = (2 * k == My);
         double2 g1, g2;
         if (KIND == FTE_KIND_SLP) {
-            double2 q1 = p0[0], q2 = p0[GS];
+            double2 q1 = spec_ld(p0), q2 = spec_ld(p0 + GS);
             slp_mult(k1, k2, xi, eta, q1, q2, g1, g2);
             if (nyq_x || nyq_y) {
                 double2 h1, h2;
@@ -584,7 +658,7 @@ __global__ void k_filter(double2* __restrict__ Hh, int Mx, int My, double Lx, do
                 g2 = make_double2(0.5 * (g2.x + h2.x), 0.5 * (g2.y + h2.y));
             }
         } else {
-            double2 a = p0[0], s21 = p0[GS], s12 = p0[2 * GS], d = p0[3 * GS];
+            double2 a = spec_ld(p0), s21 = spec_ld(p0 + GS), s12 = spec_ld(p0 + 2 * GS), d = spec_ld(p0 + 3 * GS);
             dlp_mult(k1, k2, xi, eta, a, s21, s12, d, g1, g2);
             if (nyq_x || nyq_y) {
                 double2 h1, h2;
@@ -593,8 +667,8 @@ __global__ void k_filter(double2* __restrict__ Hh, int Mx, int My, double Lx, do
                 g2 = make_double2(0.5 * (g2.x + h2.x), 0.5 * (g2.y + h2.y));
             }
         }
-        p0[0] = g1;
-        p0[GS] = g2;
+        spec_st(p0, g1);
+        spec_st(p0 + GS, g2);
     }
 }
 
@@ -1288,6 +1362,15 @@ __global__ void k_ff_split(double* __restrict__ H, int64_t n) {
     }
 }
 
+// float-float pairs -> FP64 grid values, in place
+__global__ void k_ff_join(double* __restrict__ H, int64_t n) {
+    const float2* o = reinterpret_cast<const float2*>(H);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float2 v = o[i];
+        H[i] = ff_join(v);
+    }
+}
+
 // Tiled gather in float-float from grids of pairs: a thread per target, the
 // tile's region of both grids staged once in shared memory.
 __global__ void __launch_bounds__(kTileThreads) k_gather_ff(const double* __restrict__ p, const int* __restrict__ toff,
@@ -1775,6 +1858,40 @@ int fte_kspace_run(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, fte_info
         }
     }
     FTE_TRY(fte_record(ctx, 3));
+    // float-float form with block transforms: the transforms in float-float
+    // too, the last one writing the float-float grids the gather reads
+    const bool fft_ff = ff && !long_x && !long_y;
+    if (fft_ff) {
+        float4* Hf = reinterpret_cast<float4*>(Hh);
+        FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_y_r2c_ff, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_y));
+        FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_y_c2r_ff, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_y));
+        FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_x_ff, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_x));
+        FTE_LAUNCH(ctx, k_fft_y_r2c_ff, dim3(Mx / 2, ng), fft_threads(py.m), sm_y, (const double*)H, Hf, Mx, My, py);
+        FTE_LAUNCH(ctx, k_fft_x_ff, dim3(Kh, ng), fft_threads(px.m), sm_x, Hf, Mx, Kh, px, 0);
+        int fb = (int)(((size_t)Mx * Kh + 255) / 256);
+        if (fb > ctx->num_sms * 32) fb = ctx->num_sms * 32;
+        if (a.kind == FTE_KIND_SLP)
+            FTE_LAUNCH(ctx, (k_filter<FTE_KIND_SLP, float4>), fb, 256, 0, Hf, Mx, My, a.Lx, a.Ly, a.xi, a.eta);
+        else
+            FTE_LAUNCH(ctx, (k_filter<FTE_KIND_DLP, float4>), fb, 256, 0, Hf, Mx, My, a.Lx, a.Ly, a.xi, a.eta);
+        FTE_LAUNCH(ctx, k_fft_x_ff, dim3(Kh, 2), fft_threads(px.m), sm_x, Hf, Mx, Kh, px, 1);
+        FTE_LAUNCH(ctx, k_fft_y_c2r_ff, dim3(Mx / 2, 2), fft_threads(py.m), sm_y, (const float4*)Hf,
+                   reinterpret_cast<float2*>(H), Mx, My, py);
+        FTE_TRY(fte_record(ctx, 4));
+        const double scale = gather_scale(a);
+        if (a.ntar > 0 && ts_g > 0) {
+            FTE_TRY(launch_gather_tiled(ctx, a, tb_g, wp, H, scale));
+        } else if (a.ntar > 0) {
+            // the per-point gather reads FP64 grids
+            FTE_LAUNCH(ctx, k_ff_join, ew_grid(ctx, 2LL * (long long)G), 256, 0, H, 2LL * (long long)G);
+            FTE_CUDA_TRY(cudaFuncSetAttribute(k_gather, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_pt));
+            FTE_LAUNCH(ctx, k_gather, pt_grid(ctx, a.ntar), kPtThreads, sm_pt, a.ptar, a.ntar, wp, (const double*)H,
+                       (const double*)(H + G), scale, a.uk);
+        }
+        FTE_TRY(fte_record(ctx, 5));
+        (void)info;
+        return FTE_OK;
+    }
     if (!long_y) {
         FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_y_r2c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_y));
         FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_y_c2r, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_y));
@@ -1795,9 +1912,9 @@ int fte_kspace_run(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, fte_info
     int fb = (int)(((size_t)Mx * Kh + 255) / 256);
     if (fb > ctx->num_sms * 32) fb = ctx->num_sms * 32;
     if (a.kind == FTE_KIND_SLP)
-        FTE_LAUNCH(ctx, k_filter<FTE_KIND_SLP>, fb, 256, 0, Hh, Mx, My, a.Lx, a.Ly, a.xi, a.eta);
+        FTE_LAUNCH(ctx, (k_filter<FTE_KIND_SLP, double2>), fb, 256, 0, Hh, Mx, My, a.Lx, a.Ly, a.xi, a.eta);
     else
-        FTE_LAUNCH(ctx, k_filter<FTE_KIND_DLP>, fb, 256, 0, Hh, Mx, My, a.Lx, a.Ly, a.xi, a.eta);
+        FTE_LAUNCH(ctx, (k_filter<FTE_KIND_DLP, double2>), fb, 256, 0, Hh, Mx, My, a.Lx, a.Ly, a.xi, a.eta);
     if (!long_x)
         FTE_LAUNCH(ctx, k_fft_x, dim3(Kh, 2), fft_threads(px.m), sm_x, Hh, Mx, Kh, px, 1);
     else
@@ -2274,7 +2391,7 @@ extern "C" int fte_slp_kspace_noalloc(const double* psrc, int64_t nsrc, const do
     NA_LAUNCH(k_fft_y_r2c, dim3(Mx / 2, 2), fft_threads(py.m), sm_y, stream, (const double*)H, Hh, Mx, My, py);
     NA_LAUNCH(k_fft_x, dim3(Kh, 2), fft_threads(px.m), sm_x, stream, Hh, Mx, Kh, px, 0);
     int fb = (int)(((size_t)Mx * Kh + 255) / 256);
-    NA_LAUNCH(k_filter<FTE_KIND_SLP>, fb, 256, 0, stream, Hh, Mx, My, Lx, Ly, xi, eta);
+    NA_LAUNCH((k_filter<FTE_KIND_SLP, double2>), fb, 256, 0, stream, Hh, Mx, My, Lx, Ly, xi, eta);
     NA_LAUNCH(k_fft_x, dim3(Kh, 2), fft_threads(px.m), sm_x, stream, Hh, Mx, Kh, px, 1);
     NA_LAUNCH(k_fft_y_c2r, dim3(Mx / 2, 2), fft_threads(py.m), sm_y, stream, (const double2*)Hh, H, Mx, My, py);
     double s = 4 * xi * xi / eta;

@@ -160,3 +160,33 @@ def test_ff_near_two_vectors(gpu_ctx):
             res.append(np.stack([np.asarray(u1s), np.asarray(u2s)], -1))
         rel = np.max(np.abs(res[0] - res[1])) / np.max(np.abs(res[1]))
         assert rel <= 1e-12, (kind, rel)
+
+
+@pytest.mark.parametrize("kind", ["slp", "dlp"])
+@pytest.mark.parametrize("grid", [(218, 218, 1.0, 1.0), (436, 218, 2.0, 1.0)])
+def test_ff_transforms_bluestein_and_odd_radices(gpu_ctx, kind, grid):
+    """Grids whose lines need Bluestein (218 = 2 * 109, 436 = 4 * 109) in the
+    float-float transforms: k-space parts against the FP64 transforms on the
+    same parameters."""
+    ft = _ft()
+    Mx, My, Lx, Ly = grid
+    d = _case(91, 6000, Lx, Ly)
+    kw = dict(tol=1e-10, Mx=Mx, My=My, nside_x=int(12 * Lx), nside_y=int(12 * Ly), P=16)
+    out_f, info = _run(ft, gpu_ctx, kind, d, Lx, Ly, kspace=ft.KSPACE_FF, **kw)
+    assert info.params.form == ft.FORM_FF and info.params.Mx == Mx
+    out_d, _ = _run(ft, gpu_ctx, kind, d, Lx, Ly, kspace=ft.KSPACE_FP64, xi=info.params.xi, **kw)
+    rel = np.max(np.abs(out_f[3] - out_d[3])) / np.max(np.abs(out_d[3]))
+    assert rel <= 2e-12, rel
+
+
+@pytest.mark.parametrize("kind", ["slp", "dlp"])
+def test_ff_transforms_smooth_radices(gpu_ctx, kind):
+    """7-smooth grids with radices 3, 5 and 7 (210 = 2 3 5 7, 252 = 4 9 7)."""
+    ft = _ft()
+    d = _case(92, 6000, 1.0, 1.2)
+    kw = dict(tol=1e-10, Mx=210, My=252, nside_x=12, nside_y=14, P=16)
+    out_f, info = _run(ft, gpu_ctx, kind, d, 1.0, 1.2, kspace=ft.KSPACE_FF, **kw)
+    assert info.params.form == ft.FORM_FF
+    out_d, _ = _run(ft, gpu_ctx, kind, d, 1.0, 1.2, kspace=ft.KSPACE_FP64, xi=info.params.xi, **kw)
+    rel = np.max(np.abs(out_f[3] - out_d[3])) / np.max(np.abs(out_d[3]))
+    assert rel <= 2e-12, rel
