@@ -737,13 +737,22 @@ void pick_grid(int A, int B, int kinf, int* Mx, int* My) {
 
 }  // namespace
 
-// unit costs (seconds) measured on GB300 for the cost model
-static const double kCostPair = 0.094e-9;      // one FP64 near pair
+// Unit costs (seconds) of the cost model, fitted on GB300 to stage times of
+// the mixed form at 1e6 uniform points, tolerances 1e-10, 1e-8 and 1e-6,
+// cell lists of 100^2 to 225^2 boxes: the near field as per-target +
+// per-pair + per-box terms (the box term is the staging of each 3x3
+// neighbourhood and the drain of the pair queues at each box's end), spread
+// + gather per window node and grid, transforms per unit of fft_work.
+static const double kCostTarget = 0.6e-9;      // near field, per target
+static const double kCostPair = 14e-12;        // per pair within the cutoff (float-float / FP32 classes)
+static const double kCostPair64 = 40e-12;      // same with FP64 pairs (tolerances below 1e-11)
+static const double kCostBox = 40e-9;          // per box of the cell list
 static const double kCostWin64 = 3.2e-12;      // one window node x grid, FP64 spread/gather
-static const double kCostWin32 = 1.2e-12;      // same in FP32 with compensation
-static const double kCostWinFF = 1.0e-12;      // same in float-float (FP32 pipe), window records included
-static const double kCostFft64 = 3.5e-11;      // per complex grid point x log2(points), 7-smooth FP64
-static const double kCostFft32 = 1.2e-11;      // same in FP32
+static const double kCostWin32 = 2.5e-12;      // same in FP32 (an exponential per node)
+static const double kCostWinFF = 1.7e-12;      // same in float-float (FP32 pipe), window records included
+static const double kCostFft64 = 9e-12;        // per unit of fft_work, 7-smooth FP64 block transforms
+static const double kCostFftFF = 4.5e-12;      // same in float-float
+static const double kCostFft32 = 3e-12;        // same in FP32
 // Calibration of the tuned choice against converged FP64 sums on 2000
 // generated configurations (uniform and clustered points, aspect 1..4,
 // tolerances 1e-12..1e-4): the stresslet's estimates meet the tolerance with
@@ -802,30 +811,39 @@ static int choose_params_tuned(int kind, int64_t nsrc, int64_t ntar, double Q, d
         if (std::fabs(Lx / Mx - Ly / My) > 1e-12 * (Lx / Mx)) continue;
         if ((double)Mx * My > 4.0e8) continue;  // 4 grids of 4e8 nodes: 13 GB
         if (P + 1 > Mx || P + 1 > My) continue;
-        // FP32 k-space where the tolerance allows it and lines fit a block
-        // transform, else float-float spread and gather where the tolerance
-        // allows, else FP64; FP64 lines longer than a block take the long
-        // transform
+        // k-space arithmetic: the cheapest the tolerance allows (FP32 only
+        // with block transforms) unless forced; FP64 lines longer than a
+        // block take the long transform, and so do the float-float form's
         const bool fits32 = fte_fft_fits_block(Mx, 8) && fte_fft_fits_block(My, 8);
-        int kf;
-        if (force == FTE_KSPACE_FP32) {
-            if (!fits32) continue;
-            kf = FTE_FORM_MIXED;
-        } else if (force == FTE_KSPACE_FF) {
-            kf = FTE_FORM_FF;
-        } else if (force == FTE_KSPACE_FP64) {
-            kf = FTE_FORM_PLAIN;
-        } else {
-            kf = fp32 && fits32 ? FTE_FORM_MIXED : (ffok ? FTE_FORM_FF : FTE_FORM_PLAIN);
+        const bool long64 = !fte_fft_fits_block(Mx, 16) || !fte_fft_fits_block(My, 16);
+        const double pairs = (double)nsrc * (double)ntar * FTE_PI * rc * rc / area * 1.03;
+        const double win = (double)(P + 1) * (P + 1) * ((double)nsrc * ng + (double)ntar * 2);
+        const double fftw = fft_work(Mx, My) * nfft;
+        const double near = kCostTarget * (double)ntar + (ffok ? kCostPair : kCostPair64) * pairs +
+                            kCostBox * (double)nsx * (double)nsy;
+        int kf = -1;
+        double cost = 1e300;
+        for (int f : {FTE_FORM_MIXED, FTE_FORM_FF, FTE_FORM_PLAIN}) {
+            const bool allowed = force == FTE_KSPACE_AUTO
+                                     ? (f == FTE_FORM_MIXED ? fp32 && fits32 : (f == FTE_FORM_FF ? ffok : true))
+                                     : (force == FTE_KSPACE_FP32 ? f == FTE_FORM_MIXED && fits32
+                                                                 : f == (force == FTE_KSPACE_FF ? FTE_FORM_FF
+                                                                                                : FTE_FORM_PLAIN));
+            if (!allowed) continue;
+            double c;
+            if (f == FTE_FORM_MIXED)
+                c = kCostWin32 * win + kCostFft32 * fftw;
+            else if (f == FTE_FORM_FF)
+                c = kCostWinFF * win + (long64 ? 2.5 * kCostFft64 : kCostFftFF) * fftw;
+            else
+                c = kCostWin64 * win + (long64 ? 2.5 : 1.0) * kCostFft64 * fftw;
+            if (c < cost) {
+                cost = c;
+                kf = f;
+            }
         }
-        const bool f32 = kf == FTE_FORM_MIXED;
-        const bool long64 = !f32 && (!fte_fft_fits_block(Mx, 16) || !fte_fft_fits_block(My, 16));
-        double pairs = (double)nsrc * (double)ntar * FTE_PI * rc * rc / area * 1.03;
-        double win = (double)(P + 1) * (P + 1) * ((double)nsrc * ng + (double)ntar * 2);
-        double pts = (double)Mx * My;
-        double fftw = fft_work(Mx, My);
-        double cost = kCostPair * pairs + (f32 ? kCostWin32 : (kf == FTE_FORM_FF ? kCostWinFF : kCostWin64)) * win +
-                      (f32 ? kCostFft32 : kCostFft64) * (long64 ? 2.5 : 1.0) * nfft * fftw;
+        if (kf < 0) continue;
+        cost += near;
         if (cost < best) {
             best = cost;
             bestp = *o;
