@@ -1421,7 +1421,8 @@ static int ewald_entry(fte_context* c, int kind, const double* xsrc, const doubl
     FTE_TRY(check_kspace_params(prm.xi, prm.eta, prm.Mx, prm.My, Lx, Ly, prm.w, prm.P));
     // second workspace: cell list, grids and outputs (the staged point data stays in the first)
     size_t need = fte_cells_ws(nsrc, ntar, prm.nside_x * prm.nside_y) +
-                  fte_kspace_ws(kind, prm.form, prm.Mx, prm.My, nsrc, ntar) + ws_bytes(2 * (ntar + 1), 8) * 3 + 8192;
+                  fte_kspace_ws(kind, prm.form, prm.Mx, prm.My, nsrc, ntar) + ws_bytes(2 * (ntar + 1), 8) * 3 +
+                  fte_near_ff_ws(kind, 1, nsrc) + 8192;
     FTE_TRY(fte_ws2_reserve(c, need));
     WsCarver wc2{c->ws2, 0, c->ws2_size};
     FTE_TRY(fte_record(c, 1));
@@ -1434,7 +1435,12 @@ static int ewald_entry(fte_context* c, int kind, const double* xsrc, const doubl
         double x32;
         bool ffn;
         FTE_TRY(fte_near_classes(opt, prm.tol, &x32, &ffn));
-        FTE_TRY(fte_near_launch(c, kind, cl, prm.xi, Lx, Ly, dur, x32, ffn));
+        void* ffmem = nullptr;
+        if (ffn) {
+            ffmem = wc2.take<char>(fte_near_ff_ws(kind, 1, nsrc));
+            FTE_WS_CHECK(wc2);
+        }
+        FTE_TRY(fte_near_launch(c, kind, cl, prm.xi, Lx, Ly, dur, x32, ffn, ffmem));
         FTE_TRY(fte_record(c, 7));
         KspaceArgs a;
         a.kind = kind;

@@ -179,6 +179,7 @@ int fte_cells_build(fte_context* ctx, WsCarver& wc, int kind, const double* psrc
     cl->nsx = nsx;
     cl->nsy = nsy;
     cl->nb = nb;
+    cl->nsrc = nsrc;
     int* scnt = wc.take<int>(nb + 1);
     int* tcnt = wc.take<int>(nb + 1);
     cl->src_off = wc.take<int>(nb + 1);

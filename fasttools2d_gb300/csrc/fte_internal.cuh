@@ -235,6 +235,7 @@ struct CellList {
     int max_neigh;  // upper bound of sources in a 3x3 neighbourhood (0 = unknown)
     long long qstride;  // distance between density vectors in q0..q2 (0: one vector)
     int* sidx;          // original index of each sorted source (plans only; may be null)
+    int64_t nsrc = 0;   // sources
 };
 
 size_t fte_cells_ws(int64_t nsrc, int64_t ntar, int nb);
@@ -253,8 +254,9 @@ size_t fte_tiles_ws(int64_t n, int ntiles);
 int fte_tiles_build(fte_context* ctx, WsCarver& wc, const double* p, int64_t n, double Lx, double Ly, double h,
                     int ts, int ntx, int nty, TileBins* out);
 
+// ff: float-float pairs, with ffmem scratch of fte_near_ff_ws(kind, 1, nsrc)
 int fte_near_launch(fte_context* ctx, int kind, const CellList& cl, double xi, double Lx, double Ly, double2* ur,
-                    double x32 = HUGE_VAL, bool ff = false);
+                    double x32 = HUGE_VAL, bool ff = false, void* ffmem = nullptr);
 // xi^2 r^2 above which a pair's terms are small enough for FP32 at tolerance
 // tol (mixed form); HUGE_VAL: every pair in FP64
 double fte_near_fp32_threshold(double tol);
@@ -265,12 +267,19 @@ bool fte_near_ff_ok(double tol);
 int fte_near_classes(const fte_options* opt, double tol, double* x32, bool* ff);
 // Near-field launch description, opaque outside near.cu.
 struct NearParamsHost {
-    alignas(16) unsigned char raw[256];
+    alignas(16) unsigned char raw[320];
 };
 void fte_near_fill_params(int kind, const CellList& cl, double xi, double Lx, double Ly, NearParamsHost* hp,
                           double x32 = HUGE_VAL, bool ff = false);
 size_t fte_near_params_size();
 bool fte_near_uses_ff(const NearParamsHost& hp);
+// float-float pairs read per-source float-float data (own-box-relative
+// positions, densities of nv vectors) prepared once per evaluation:
+// scratch bytes, attaching the scratch to a description, and the preparation
+// (after the densities are in place)
+size_t fte_near_ff_ws(int kind, int nv, int64_t nsrc);
+void fte_near_ff_attach(NearParamsHost* hp, int kind, int nv, int64_t nsrc, void* mem);
+int fte_near_ff_prep(fte_context* ctx, int kind, int nv, const NearParamsHost& hp);
 // sources staged per chunk (ff: the description uses the float-float class)
 int fte_near_cap(const fte_context* ctx, int kind, int nv, bool ff);
 // nv (1..4) density vectors at q* + v*cl.qstride; outputs at ur + v*ustride

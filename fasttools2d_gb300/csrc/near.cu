@@ -58,6 +58,14 @@ struct NearParams {
     // float-float
     int ffnear;
     float2 xi2ff, pfff, cutff, selcff;
+    // float-float class: per sorted source, its position relative to the
+    // centre of its own box (x hi, x lo, y hi, y lo) and its staged density
+    // values as float-float, value c of vector v at qff[(v * kDen + c) *
+    // qffstride + i]; box sides as float-float (written by fte_near_ff_prep)
+    const float4* __restrict__ sff;
+    const float2* __restrict__ qff;
+    long long qffstride;
+    float2 bsxff, bsyff;
     int cap;
     double2* __restrict__ ur;  // vector v at ur + v * ustride
     long long ustride;
@@ -286,11 +294,15 @@ struct NearSmem {
     // accumulators cost NSLOT * NV * 2 doubles per lane
     static constexpr int kSlots = NV == 1 ? 4 : (NV == 2 ? 2 : 1);
     static constexpr int kHead = 2 * kKtab + 128 + 12 + kKtab / 2 + 1;  // doubles before the staged sources
+    // per staged source: FP64 layout (x, y, densities; FP32 copies) or, with
+    // the float-float class, float-float only (position and densities as
+    // FP32 + low part)
+    __host__ __device__ static size_t per_source(bool ff) {
+        return ff ? 2 * sizeof(float2) + 2 * kDen * NV * sizeof(float)
+                  : (2 + kDen * NV) * sizeof(double) + sizeof(float2) + kDen * NV * sizeof(float);
+    }
     __host__ __device__ static size_t bytes(int cap, bool ff) {
-        return kHead * sizeof(double) +
-               (size_t)cap * ((2 + kDen * NV) * sizeof(double) + sizeof(float2) + kDen * NV * sizeof(float)) +
-               (ff ? (size_t)cap * (sizeof(float2) + kDen * NV * sizeof(float)) : 0) +
-               kNearWarps * 3 * kQueue * sizeof(int) + 64;
+        return kHead * sizeof(double) + (size_t)cap * per_source(ff) + kNearWarps * 3 * kQueue * sizeof(int) + 64;
     }
 };
 
@@ -315,12 +327,14 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
     const float2* etabff = ktabff + kKtab;
     const float2* rtabff = etabff + 64;
     const float* ktab32 = reinterpret_cast<const float*>(rtabff + 12);
-    double* sx = reinterpret_cast<double*>(smem_raw) + NearSmem<KIND, NV>::kHead;
-    double* sy = sx + cap;
-    double* den = sy + cap;  // den[(v * kDen + c) * cap + i]
-    float2* s32 = reinterpret_cast<float2*>(den + (size_t)kDen * NV * cap);
+    // FP64 layout: x, y, densities (FP64), FP32 position, FP32 densities;
+    // float-float layout: FP32 position, FP32 densities, their low parts
+    double* const s0 = reinterpret_cast<double*>(smem_raw) + NearSmem<KIND, NV>::kHead;
+    double* sx = ffn ? nullptr : s0;
+    double* sy = ffn ? nullptr : s0 + cap;
+    double* den = ffn ? nullptr : s0 + 2 * cap;  // den[(v * kDen + c) * cap + i]
+    float2* s32 = ffn ? reinterpret_cast<float2*>(s0) : reinterpret_cast<float2*>(s0 + (size_t)(2 + kDen * NV) * cap);
     float* den32 = reinterpret_cast<float*>(s32 + cap);  // den32[(v * kDen + c) * cap + i]
-    // float-float class: low parts of the box-relative position and densities
     float2* slo = reinterpret_cast<float2*>(den32 + (size_t)kDen * NV * cap);
     float* dlo = reinterpret_cast<float*>(slo + (ffn ? cap : 0));
     int* qbuf = reinterpret_cast<int*>(dlo + (ffn ? (size_t)kDen * NV * cap : 0));
@@ -392,6 +406,26 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
 #pragma unroll
             for (int k = 1; k < 9; k++) e += (g >= nb_start[k]);
             int si = prm.src_off[nb_box[e]] + (g - nb_start[e]);
+            if constexpr (ffn) {
+                // own-box-relative position + the neighbour's offset (a whole
+                // number of box sides), densities as prepared
+                const int oxe = e == 0 ? 0 : (e <= 3 ? -1 : (e <= 5 ? 0 : 1));
+                const int oye = e == 0 ? 0 : ((e == 1 || e == 4 || e == 6) ? -1 : ((e == 2 || e == 7) ? 0 : 1));
+                const float4 r = prm.sff[si];
+                const float2 px = ff_add(make_float2(r.x, r.y), make_float2(oxe * prm.bsxff.x, oxe * prm.bsxff.y));
+                const float2 py = ff_add(make_float2(r.z, r.w), make_float2(oye * prm.bsyff.x, oye * prm.bsyff.y));
+                s32[i] = make_float2(px.x, py.x);
+                slo[i] = make_float2(px.y, py.y);
+#pragma unroll
+                for (int v = 0; v < NV; v++)
+#pragma unroll
+                    for (int c = 0; c < kDen; c++) {
+                        const float2 q = prm.qff[(size_t)(v * kDen + c) * prm.qffstride + si];
+                        den32[(size_t)(v * kDen + c) * cap + i] = q.x;
+                        dlo[(size_t)(v * kDen + c) * cap + i] = q.y;
+                    }
+                continue;
+            }
             double2 p = prm.spos[si];
             double xs = p.x + nb_shx[e], ys = p.y + nb_shy[e];
             sx[i] = xs;
@@ -406,11 +440,6 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
                     d[cap] = prm.q1[o];
                     d32[0] = (float)d[0];
                     d32[cap] = (float)d[cap];
-                    if (ffn) {
-                        float* dl = dlo + (size_t)v * kDen * cap + i;
-                        dl[0] = (float)(d[0] - (double)d32[0]);
-                        dl[cap] = (float)(d[cap] - (double)d32[cap]);
-                    }
                 } else {
                     // S11, (S12 + S21)/2, S22, S11 + S22
                     double s11 = prm.q0[o], ssym = prm.q1[o], s22 = prm.q2[o];
@@ -422,17 +451,9 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
                     d32[cap] = (float)(0.5 * ssym);
                     d32[2 * cap] = (float)s22;
                     d32[3 * cap] = (float)(s11 + s22);
-                    if (ffn) {
-                        float* dl = dlo + (size_t)v * kDen * cap + i;
-#pragma unroll
-                        for (int c = 0; c < 4; c++) dl[c * cap] = (float)(d[c * cap] - (double)d32[c * cap]);
-                    }
                 }
             }
-            const double rx = xs - cx, ry = ys - cy;
-            const float2 h32 = make_float2((float)rx, (float)ry);
-            s32[i] = h32;
-            if (ffn) slo[i] = make_float2((float)(rx - (double)h32.x), (float)(ry - (double)h32.y));
+            s32[i] = make_float2((float)(xs - cx), (float)(ys - cy));
         }
         __syncthreads();
         const int own_lim = n_own - chunk;  // local index < own_lim: own box
@@ -444,8 +465,8 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
         // empty fills up with the next targets' pairs instead.  The FP32 class
         // is cheap and is finished per target.
         const int ntw = warp < nt ? (nt - warp + kNearWarps - 1) / kNearWarps : 0;
-        // x below which a pair takes ring qn
-        const float xsplit = (KIND == FTE_KIND_DLP && ffn) ? 1e-8f : 1.0f;
+        // x below which a Stokeslet pair takes ring qn
+        const float xsplit = 1.0f;
         int Pf = 0, Ef = 0, Pn = 0, En = 0;  // pushed / evaluated counts of rings qf, qn
         int tailF[NSLOT], tailN[NSLOT];      // Pf, Pn after each slot's sweep
         double acc[NSLOT][NV][2];
@@ -463,9 +484,8 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
 #pragma unroll
         for (int v = 0; v < NV; v++) acc32[v][0] = acc32[v][1] = 0.0f;
         float tx32 = 0.0f, ty32 = 0.0f;  // box-relative position of the target being swept
-        // FP64 accumulators in use in this chunk (always without ffn; with
-        // ffn only after a pass over the stresslet's qn ring)
-        bool any64 = !ffn;
+        // FP64 accumulators in use (the float-float form has no FP64 pairs)
+        constexpr bool any64 = !ffn;
 
         // slot `tag`'s accumulators of vector v, selected into (a0, a1) and
         // back: selects only (written as conditional expressions, which
@@ -701,7 +721,7 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
                 const int s = ent >> 2, tag = ent & 3;
                 float2 dx, dy, r2;
                 ff_geom(s, tag, dx, dy, r2);
-                if (!(s < own_lim) && !ff_lt(r2, prm.cutff)) return;
+                if (s < own_lim ? (r2.x == 0.0f && r2.y == 0.0f) : !ff_lt(r2, prm.cutff)) return;
                 const float2 x = ff_mul(r2, prm.xi2ff);
                 const float2 e2 = fte_expm_ff(x, etabff);
                 const float2 ir2 = ff_rcp(r2);
@@ -727,9 +747,8 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
                 }
             }
         };
-        // ring qf: x >= 1 (float-float when ffn; the stresslet's x >= 1e-8);
-        // ring qn: x < 1 (the stresslet's x < 1e-8, FP64; the Stokeslet's in
-        // float-float when ffn)
+        // ring qf: the Stokeslet's x >= 1 and every stresslet pair; ring qn:
+        // the Stokeslet's x < 1 (float-float when ffn, else FP64)
         auto evalF = [&](int ent) {
             if (KIND == FTE_KIND_SLP) {
                 if (ffn)
@@ -770,7 +789,6 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
             }
             Ef += cf;
             En += cn;
-            if (KIND == FTE_KIND_DLP && cn > 0) any64 = true;
             __syncwarp();
         };
 
@@ -789,7 +807,7 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
             for (int v = 0; v < NV; v++) {
                 // lanes 0-15 reduce component 0, lanes 16-31 component 1
                 double keep = 0.0;
-                if (any64) {
+                if constexpr (any64) {
                     double a0, a1;
                     acc_get(sl, v, a0, a1);
                     keep = hi ? a1 : a0;
@@ -891,9 +909,9 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
                     }
                 }
                 const int ent = (s << 2) | slot;
-                // the stresslet splits its FP64 pairs at x = 1 only for the
-                // float-float class
-                const bool split = KIND == FTE_KIND_SLP || ffn;
+                // the Stokeslet's pairs with x < 1 take ring qn (the series of
+                // E1); the stresslet has one pair formula
+                const bool split = KIND == FTE_KIND_SLP;
                 const bool pf_ = pass && !(split && small_x), pn_ = pass && split && small_x;
                 const unsigned mf = __ballot_sync(0xffffffffu, pf_);
                 const unsigned mn = __ballot_sync(0xffffffffu, pn_);
@@ -910,7 +928,6 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
                 if (Pn - En >= 32) {
                     evalN(qn[(En + lane) & (kQueue - 1)]);
                     En += 32;
-                    if (KIND == FTE_KIND_DLP) any64 = true;
                     __syncwarp();
                 }
             }
@@ -996,6 +1013,42 @@ __global__ void __launch_bounds__(kNearThreads, 2) k_near_batch(const unsigned c
         // read in place (a register copy of the description would spill)
         const NearParams& prm = *reinterpret_cast<const NearParams*>(plist + (size_t)w.x * kParamStride);
         near_box<KIND, NV, FF>(prm, w.y, smem_raw, nb_box, nb_start, nb_shx, nb_shy);
+    }
+}
+
+// Float-float data of the sorted sources for nv density vectors: position
+// relative to the centre of the source's own box, and the staged density
+// values (SLP: f1, f2; DLP: S11, (S12 + S21)/2, S22, S11 + S22) as
+// float-float.  A warp per box.
+template <int KIND>
+__global__ void k_near_ff_prep(const NearParams prm, int nv, float4* __restrict__ sff, float2* __restrict__ qff) {
+    constexpr int kDen = KIND == FTE_KIND_SLP ? 2 : 4;
+    const int lane = threadIdx.x & 31;
+    const int wpb = blockDim.x >> 5;
+    for (int b = blockIdx.x * wpb + (threadIdx.x >> 5); b < prm.nb; b += gridDim.x * wpb) {
+        const int bx = b % prm.nsx, by = b / prm.nsx;
+        const double cx = -prm.Lx / 2 + (bx + 0.5) * prm.Lx / prm.nsx;
+        const double cy = -prm.Ly / 2 + (by + 0.5) * prm.Ly / prm.nsy;
+        const int i1 = prm.src_off[b + 1];
+        for (int i = prm.src_off[b] + lane; i < i1; i += 32) {
+            const double2 p = prm.spos[i];
+            const float2 fx = ff_split(p.x - cx), fy = ff_split(p.y - cy);
+            sff[i] = make_float4(fx.x, fx.y, fy.x, fy.y);
+            for (int v = 0; v < nv; v++) {
+                const long long o = v * prm.qstride + i;
+                float2* q = qff + (size_t)v * kDen * prm.qffstride + i;
+                if (KIND == FTE_KIND_SLP) {
+                    q[0] = ff_split(prm.q0[o]);
+                    q[prm.qffstride] = ff_split(prm.q1[o]);
+                } else {
+                    const double s11 = prm.q0[o], s22 = prm.q2[o];
+                    q[0] = ff_split(s11);
+                    q[prm.qffstride] = ff_split(0.5 * prm.q1[o]);
+                    q[2 * prm.qffstride] = ff_split(s22);
+                    q[3 * prm.qffstride] = ff_split(s11 + s22);
+                }
+            }
+        }
     }
 }
 
@@ -1087,6 +1140,9 @@ void fte_near_fill_params(int kind, const CellList& cl, double xi, double Lx, do
         const float q = (float)p.selfc;
         p.selcff = make_float2(q, (float)(p.selfc - (double)q));
     }
+    p.sff = nullptr;
+    p.qff = nullptr;
+    p.qffstride = 0;
     p.cap = 0;
     p.ur = nullptr;
     p.ustride = 0;
@@ -1206,9 +1262,17 @@ int fte_near_launch_batch(fte_context* ctx, int kind, int nv, bool ff, const voi
 }
 
 int fte_near_launch(fte_context* ctx, int kind, const CellList& cl, double xi, double Lx, double Ly, double2* ur,
-                    double x32, bool ff) {
+                    double x32, bool ff, void* ffmem) {
     NearParamsHost hp;
     fte_near_fill_params(kind, cl, xi, Lx, Ly, &hp, x32, ff);
+    if (ff) {
+        if (!ffmem) {
+            fte_set_error("internal: float-float near pairs without scratch");
+            return FTE_ERR_INVALID;
+        }
+        fte_near_ff_attach(&hp, kind, 1, cl.nsrc, ffmem);
+        FTE_TRY(fte_near_ff_prep(ctx, kind, 1, hp));
+    }
     return fte_near_launch_nv(ctx, kind, 1, hp, ur, 0);
 }
 
@@ -1275,4 +1339,40 @@ void fte_near_set_output(NearParamsHost* hp, double2* ur, long long ustride, int
     p.ur = ur;
     p.ustride = ustride;
     p.cap = cap;
+}
+
+size_t fte_near_ff_ws(int kind, int nv, int64_t nsrc) {
+    const int kden = kind == FTE_KIND_SLP ? 2 : 4;
+    return ws_bytes((size_t)nsrc + 1, sizeof(float4)) + ws_bytes((size_t)kden * nv * (nsrc + 1), sizeof(float2));
+}
+
+void fte_near_ff_attach(NearParamsHost* hp, int kind, int nv, int64_t nsrc, void* mem) {
+    NearParams& p = *reinterpret_cast<NearParams*>(hp->raw);
+    const int kden = kind == FTE_KIND_SLP ? 2 : 4;
+    WsCarver w{static_cast<char*>(mem), 0, fte_near_ff_ws(kind, nv, nsrc)};
+    p.sff = w.take<float4>((size_t)nsrc + 1);
+    p.qff = w.take<float2>((size_t)kden * nv * (nsrc + 1));
+    p.qffstride = nsrc;
+    const double bx = p.Lx / p.nsx, by = p.Ly / p.nsy;
+    const float hx = (float)bx, hy = (float)by;
+    p.bsxff = make_float2(hx, (float)(bx - (double)hx));
+    p.bsyff = make_float2(hy, (float)(by - (double)hy));
+}
+
+int fte_near_ff_prep(fte_context* ctx, int kind, int nv, const NearParamsHost& hp) {
+    const NearParams& p = *reinterpret_cast<const NearParams*>(hp.raw);
+    if (!p.ffnear || p.nb == 0) return FTE_OK;
+    if (!p.sff || !p.qff) {
+        fte_set_error("internal: float-float near data not attached");
+        return FTE_ERR_INVALID;
+    }
+    int grid = (p.nb + 7) / 8;
+    if (grid > ctx->num_sms * 16) grid = ctx->num_sms * 16;
+    float4* sff = const_cast<float4*>(p.sff);
+    float2* qff = const_cast<float2*>(p.qff);
+    if (kind == FTE_KIND_SLP)
+        FTE_LAUNCH(ctx, k_near_ff_prep<FTE_KIND_SLP>, grid, 256, 0, p, nv, sff, qff);
+    else
+        FTE_LAUNCH(ctx, k_near_ff_prep<FTE_KIND_DLP>, grid, 256, 0, p, nv, sff, qff);
+    return FTE_OK;
 }

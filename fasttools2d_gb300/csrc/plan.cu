@@ -161,6 +161,8 @@ struct fte_plan {
     double2 *ur = nullptr, *uk = nullptr;
     char* kscratch = nullptr;  // grids and spectra of one vector
     size_t kscratch_size = 0;
+    bool ffnear = false;       // float-float near pairs (per-source data in ffmem)
+    char* ffmem = nullptr;
 };
 
 struct fte_batch {
@@ -194,7 +196,10 @@ static int plan_exec_body(fte_plan* p, int nv, const double* f1s, const double* 
                        (const double*)p->wts, (const int*)p->cl.sidx, p->q0, p->q1, p->q2, p->fv);
     }
     if (nt == 0) return FTE_OK;
-    if (!skip_near) FTE_TRY(fte_near_launch_nv(c, p->kind, nv, p->near, p->ur, nt));
+    if (!skip_near) {
+        if (p->ffnear && ns > 0) FTE_TRY(fte_near_ff_prep(c, p->kind, nv, p->near));
+        FTE_TRY(fte_near_launch_nv(c, p->kind, nv, p->near, p->ur, nt));
+    }
     for (int v = 0; v < nv; v++) {
         WsCarver wc{p->kscratch, 0, p->kscratch_size};
         KspaceArgs a;
@@ -325,11 +330,15 @@ extern "C" int fte_plan_create(fte_context* c, int kind, const double* xsrc, con
     ka.My = prm.My;
     ka.P = prm.P;
     p->kscratch_size = fte_kspace_ws(kind, prm.form, prm.Mx, prm.My, 0, 0) + fte_kspace_rec_ws(prm.form, nsrc) + (1 << 16);
+    double x32;
+    bool ffn;
+    FTE_TRY(fte_near_classes(opt, prm.tol, &x32, &ffn));
+    const size_t ffws = ffn ? fte_near_ff_ws(kind, nv, nsrc) : 0;
     size_t need = 3 * ws_bytes(2 * (nsrc + 1), 8) + ws_bytes(2 * (ntar + 1), 8) + ws_bytes(nsrc + 1, 8) +
                   fte_cells_ws(nsrc, ntar, prm.nside_x * prm.nside_y) +
                   fte_kspace_ws(kind, prm.form, prm.Mx, prm.My, nsrc, ntar) + 3 * ws_bytes(nv * (nsrc + 1), 8) +
                   ws_bytes(2 * nv * (nsrc + 1), 8) + ws_bytes(16 * nv, 8) + 2 * ws_bytes(nv * (ntar + 1), 16) +
-                  p->kscratch_size + (1 << 16);
+                  p->kscratch_size + ffws + (1 << 16);
     if (cudaMalloc(&p->mem, need) != cudaSuccess) {
         cudaGetLastError();
         delete p;
@@ -362,6 +371,7 @@ extern "C" int fte_plan_create(fte_context* c, int kind, const double* xsrc, con
     p->ur = pm.take<double2>(nv * (ntar + 1));
     p->uk = pm.take<double2>(nv * (ntar + 1));
     p->kscratch = pm.take<char>(p->kscratch_size);
+    p->ffmem = ffn ? pm.take<char>(ffws) : nullptr;
     FTE_WS_CHECK(pm);
     if (nsrc > 0) {
         FTE_LAUNCH(c, k_plan_wrap, grid_of(c, nsrc), 256, 0, dxs, dys, nsrc, Lx, Ly, p->ps);
@@ -401,10 +411,9 @@ extern "C" int fte_plan_create(fte_context* c, int kind, const double* xsrc, con
     cl.q1 = p->q1;
     cl.q2 = p->q2;
     cl.qstride = nsrc;
-    double x32;
-    bool ffn;
-    FTE_TRY(fte_near_classes(opt, prm.tol, &x32, &ffn));
     fte_near_fill_params(kind, cl, prm.xi, Lx, Ly, &p->near, x32, ffn);
+    p->ffnear = ffn;
+    if (ffn) fte_near_ff_attach(&p->near, kind, nv, nsrc, p->ffmem);
     fte_near_set_output(&p->near, p->ur, ntar, fte_near_cap(c, kind, nv, fte_near_uses_ff(p->near)));
     // warm the FFT tables so that executions (and graph capture) allocate nothing
     FTE_TRY(fte_fft_prepare(c, prm.Mx));
@@ -493,6 +502,7 @@ static int batch_run(fte_batch* b) {
             FTE_LAUNCH(c, k_plan_dens<FTE_KIND_DLP>, grid_of(c, p->nsrc), 256, 0, (const double*)b->f1[i],
                        (const double*)b->f2[i], b->nv, p->nsrc, (const double*)p->nrm, (const double*)p->wts,
                        (const int*)p->cl.sidx, p->q0, p->q1, p->q2, p->fv);
+        if (p->ffnear && p->ntar > 0) FTE_TRY(fte_near_ff_prep(c, p->kind, b->nv, p->near));
     }
     // one persistent near-field launch per kind over all (plan, box) items
     for (int l = 0; l < 4; l++)
