@@ -49,6 +49,7 @@ struct NearParams {
     const double2* __restrict__ tpos;
     const int* __restrict__ tidx;
     double Lx, Ly, xi, xi2, inv_xi2, selfc, cutoffsq, pf;
+    double bsx, bsy;  // box sides Lx / nsx, Ly / nsy
     float cut32;
     // pairs with xi^2 r^2 >= x32 are evaluated in FP32 (their terms are
     // below the tolerance's reach of FP32 rounding); +inf: all FP64
@@ -70,6 +71,12 @@ struct NearParams {
     double2* __restrict__ ur;  // vector v at ur + v * ustride
     long long ustride;
 };
+
+// centre of box (bx, by): the reference frame of the box-relative FP32 and
+// float-float coordinates (the same expression wherever they are formed)
+__device__ __forceinline__ double2 box_centre(const NearParams& prm, int bx, int by) {
+    return make_double2(fma(bx + 0.5, prm.bsx, -0.5 * prm.Lx), fma(by + 0.5, prm.bsy, -0.5 * prm.Ly));
+}
 
 // E1(x) for x > 0 from the piecewise polynomials of gen_e1_coeffs.py:
 //   x < 1:     -gamma - ln x + x R(2x - 1)
@@ -373,8 +380,10 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
         int tx = (psx + prm.nsx) % prm.nsx, ty = (psy + prm.nsy) % prm.nsy;
         int sb = ty * prm.nsx + tx;
         nb_box[tid] = sb;
-        nb_shx[tid] = (prm.Lx * (psx - tx)) / prm.nsx;
-        nb_shy[tid] = (prm.Ly * (psy - ty)) / prm.nsy;
+        if (!ffn) {  // image shifts (the float-float staging adds whole box sides instead)
+            nb_shx[tid] = (prm.Lx * (psx - tx)) / prm.nsx;
+            nb_shy[tid] = (prm.Ly * (psy - ty)) / prm.nsy;
+        }
     }
     __syncthreads();
     if (tid == 0) {
@@ -388,8 +397,8 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
     __syncthreads();
     const int S = nb_start[9];
     const int n_own = nb_start[1];
-    const double cx = -prm.Lx / 2 + (bx + 0.5) * prm.Lx / prm.nsx;
-    const double cy = -prm.Ly / 2 + (by + 0.5) * prm.Ly / prm.nsy;
+    const double2 bc = box_centre(prm, bx, by);
+    const double cx = bc.x, cy = bc.y;
 
     if (S == 0) {
         for (int t = tid; t < nt; t += kNearThreads)
@@ -833,7 +842,8 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
                     if ((lane & 15) == 0) {
                         kf = ff_add(kf, make_float2(fsw[(sl * NV + v) * 2 + (hi ? 1 : 0)], 0.0f));
                         const float2 i4p = make_float2(7.957746834e-02f, 3.210319122e-09f);  // 1 / (4 pi)
-                        const double val = fma(keep, inv4pi, ff_join(ff_mul(kf, i4p)));
+                        double val = ff_join(ff_mul(kf, i4p));
+                        if constexpr (any64) val = fma(keep, inv4pi, val);
                         double* o = reinterpret_cast<double*>(prm.ur + v * prm.ustride + oi) + (hi ? 1 : 0);
                         if (chunk == 0)
                             *o = val;
@@ -1027,8 +1037,8 @@ __global__ void k_near_ff_prep(const NearParams prm, int nv, float4* __restrict_
     const int wpb = blockDim.x >> 5;
     for (int b = blockIdx.x * wpb + (threadIdx.x >> 5); b < prm.nb; b += gridDim.x * wpb) {
         const int bx = b % prm.nsx, by = b / prm.nsx;
-        const double cx = -prm.Lx / 2 + (bx + 0.5) * prm.Lx / prm.nsx;
-        const double cy = -prm.Ly / 2 + (by + 0.5) * prm.Ly / prm.nsy;
+        const double2 bc = box_centre(prm, bx, by);
+        const double cx = bc.x, cy = bc.y;
         const int i1 = prm.src_off[b + 1];
         for (int i = prm.src_off[b] + lane; i < i1; i += 32) {
             const double2 p = prm.spos[i];
@@ -1125,6 +1135,8 @@ void fte_near_fill_params(int kind, const CellList& cl, double xi, double Lx, do
     p.selfc = -(1.0 + 0.5 * FTE_EULER) - log(xi);
     p.cutoffsq = Lx * Ly / cl.nsx / cl.nsy;
     p.pf = 2.0 * xi * xi;
+    p.bsx = Lx / cl.nsx;
+    p.bsy = Ly / cl.nsy;
     double bsx = Lx / cl.nsx, bsy = Ly / cl.nsy;
     double bmax = bsx > bsy ? bsx : bsy;
     p.cut32 = (float)(p.cutoffsq + 1e-4 * bmax * bmax);
