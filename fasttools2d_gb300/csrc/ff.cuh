@@ -80,3 +80,39 @@ __device__ __forceinline__ float2 ff_rcp(float2 a) {
 }
 // a < b
 __device__ __forceinline__ bool ff_lt(float2 a, float2 b) { return a.x < b.x || (a.x == b.x && a.y < b.y); }
+
+// exp(-x) in float-float for -80 < x < 80 (0 beyond 80): n = round(64 x /
+// ln 2), r = x - n ln2/64 with ln2/64 split in three FP32 parts
+// (the first with 13 trailing zero bits, so n C1 is exact for n < 8192);
+// exp(-r), |r| <= ln2/128, as 1 - r + r^2/2 in float-float plus the cubic and
+// higher Taylor terms in FP32 (they are below 3e-8); 2^(-j/64) from a
+// float-float table.  Relative error ~4e-14.
+__device__ __forceinline__ float2 fte_expm_ff(float2 x, const float2* __restrict__ tab) {
+    const float C1 = 1.082611084e-02f, C2 = 4.313856607e-06f, C3 = -2.016456257e-13f;
+    const int n = __float2int_rn(x.x * 9.233248138e+01f);
+    const float nf = (float)n;
+    const float rh = __fsub_rn(x.x, __fmul_rn(nf, C1));
+    const float p2 = __fmul_rn(nf, C2);
+    const float e2 = __fmaf_rn(nf, C2, -p2);
+    // r = rh - p2 + (x.lo - e2 - n C3)
+    const float s = __fsub_rn(rh, p2);
+    const float bb = __fsub_rn(s, rh);
+    float e = __fadd_rn(__fsub_rn(rh, __fsub_rn(s, bb)), __fsub_rn(-p2, bb));
+    e = __fsub_rn(__fsub_rn(__fadd_rn(e, x.y), e2), __fmul_rn(nf, C3));
+    const float2 r = ff_norm(s, e);
+    const float r1 = r.x;
+    float q = __fmaf_rn(r1, -1.0f / 120.0f, 1.0f / 24.0f);
+    q = __fmaf_rn(r1, q, -1.0f / 6.0f);
+    q = __fmul_rn(q, __fmul_rn(r1, __fmul_rn(r1, r1)));
+    // r^2 / 2 in float-float
+    const float p = __fmul_rn(r1, r1);
+    float pe = __fmaf_rn(r1, r1, -p);
+    pe = __fmaf_rn(__fadd_rn(r1, r1), r.y, pe);
+    float2 h = ff_norm(__fmul_rn(p, 0.5f), __fmul_rn(pe, 0.5f));
+    h = ff_add(h, make_float2(q, 0.0f));
+    h = ff_add(h, ff_neg(r));
+    h = ff_add(make_float2(1.0f, 0.0f), h);
+    const float2 m = ff_mul(h, tab[n & 63]);
+    const float sc = __int_as_float((127 - (n >> 6)) << 23);  // 2^-(n >> 6) (n >> 6 floors)
+    return x.x < 80.0f ? make_float2(__fmul_rn(m.x, sc), __fmul_rn(m.y, sc)) : make_float2(0.0f, 0.0f);
+}

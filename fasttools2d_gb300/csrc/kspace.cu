@@ -672,6 +672,118 @@ __global__ void k_filter(S* __restrict__ Hh, int Mx, int My, double Lx, double L
     }
 }
 
+// ---- the multipliers in float-float (float-float spectra) ---------------------
+// The same formulas as slp_mult / dlp_mult and k_filter, on the FP32 pipe:
+// wave numbers k = (2 pi / L) index from a float-float 2 pi / L, the Gaussian
+// factor by fte_expm_ff, 1/K by ff_rcp.  Relative error ~1e-13.
+struct FfFilt {
+    float2 c1, c2;  // 2 pi / Lx, 2 pi / Ly
+    float2 c4, cq;  // 1 / (4 xi^2), (1 - eta) / (4 xi^2)
+};
+
+__device__ __forceinline__ float2 ff_scale2(float2 a, float c) { return make_float2(a.x * c, a.y * c); }
+
+// SLP: G = (K q - k (k.q)) (1/K^2 + 1/(4 xi^2 K)) e^{-(1-eta) K/(4 xi^2)}
+__device__ __forceinline__ void slp_mult_ff(float2 k1, float2 k2, const FfFilt& f, const float2* etab, float4 q1,
+                                            float4 q2, float4& g1, float4& g2) {
+    const float2 K = ff_add(ff_sqr(k1), ff_sqr(k2));
+    const float2 iK = ff_rcp(K);
+    const float2 e = ff_mul(ff_add(ff_sqr(iK), ff_mul(iK, f.c4)), fte_expm_ff(ff_mul(K, f.cq), etab));
+    const float2 kqr = ff_add(ff_mul(k1, ffc_re(q1)), ff_mul(k2, ffc_re(q2)));
+    const float2 kqi = ff_add(ff_mul(k1, ffc_im(q1)), ff_mul(k2, ffc_im(q2)));
+    g1 = ffc_mk(ff_mul(ff_add(ff_mul(K, ffc_re(q1)), ff_neg(ff_mul(k1, kqr))), e),
+                ff_mul(ff_add(ff_mul(K, ffc_im(q1)), ff_neg(ff_mul(k1, kqi))), e));
+    g2 = ffc_mk(ff_mul(ff_add(ff_mul(K, ffc_re(q2)), ff_neg(ff_mul(k2, kqr))), e),
+                ff_mul(ff_add(ff_mul(K, ffc_im(q2)), ff_neg(ff_mul(k2, kqi))), e));
+}
+
+// DLP on the spectra of S11, S21, S12, S22 (as dlp_mult)
+__device__ __forceinline__ void dlp_mult_ff(float2 k1, float2 k2, const FfFilt& f, const float2* etab, float4 a,
+                                            float4 s21, float4 s12, float4 d, float4& g1, float4& g2) {
+    const float2 K = ff_add(ff_sqr(k1), ff_sqr(k2));
+    const float2 iK = ff_rcp(K);
+    const float2 e = ff_mul(ff_mul(fte_expm_ff(ff_mul(K, f.cq), etab), ff_add(make_float2(1.0f, 0.0f), ff_mul(K, f.c4))),
+                            iK);
+    const float2 k11 = ff_sqr(k1), k12 = ff_mul(k1, k2), k22 = ff_sqr(k2);
+    float2 x1[2], x2[2];
+#pragma unroll
+    for (int c = 0; c < 2; c++) {  // real, imaginary parts (real multipliers)
+        const float2 av = c ? ffc_im(a) : ffc_re(a), dv = c ? ffc_im(d) : ffc_re(d);
+        const float2 sv = ff_add(c ? ffc_im(s21) : ffc_re(s21), c ? ffc_im(s12) : ffc_re(s12));
+        const float2 q = ff_mul(ff_add(ff_add(ff_mul(k11, av), ff_mul(k12, sv)), ff_mul(k22, dv)), iK);
+        const float2 ad = ff_add(av, dv);
+        x1[c] = ff_add(ff_add(ff_add(ff_scale2(ff_mul(av, k1), 2.0f), ff_mul(k2, sv)), ff_mul(k1, ad)),
+                       ff_neg(ff_scale2(ff_mul(k1, q), 2.0f)));
+        x2[c] = ff_add(ff_add(ff_add(ff_scale2(ff_mul(dv, k2), 2.0f), ff_mul(k1, sv)), ff_mul(k2, ad)),
+                       ff_neg(ff_scale2(ff_mul(k2, q), 2.0f)));
+    }
+    // g = i x e
+    g1 = ffc_mk(ff_neg(ff_mul(x1[1], e)), ff_mul(x1[0], e));
+    g2 = ffc_mk(ff_neg(ff_mul(x2[1], e)), ff_mul(x2[0], e));
+}
+
+__device__ __forceinline__ float4 ffc_avg(float4 a, float4 b) {
+    return ffc_mk(ff_scale2(ff_add(ffc_re(a), ffc_re(b)), 0.5f), ff_scale2(ff_add(ffc_im(a), ffc_im(b)), 0.5f));
+}
+
+template <int KIND>
+__global__ void k_filter_ff(float4* __restrict__ Hh, int Mx, int My, FfFilt f) {
+    __shared__ float2 etab[64];
+    for (int i = threadIdx.x; i < 64; i += blockDim.x) etab[i] = ff_split(exp2(-i / 64.0));
+    __syncthreads();
+    const int Kh = My / 2 + 1;
+    const size_t GS = (size_t)Mx * Kh;
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < GS; idx += (size_t)gridDim.x * blockDim.x) {
+        const int j = (int)(idx / Kh), k = (int)(idx % Kh);
+        float4* p0 = Hh + idx;
+        if (j == 0 && k == 0) {
+            const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+            p0[0] = z;
+            p0[GS] = z;
+            continue;
+        }
+        const float2 k1 = ff_mulf(f.c1, (float)((j <= Mx / 2) ? j : j - Mx));
+        const float2 k2 = ff_mulf(f.c2, (float)k);
+        const bool nyq_x = (2 * j == Mx), nyq_y = (2 * k == My);
+        const float2 k1m = nyq_x ? ff_neg(k1) : k1, k2m = nyq_y ? ff_neg(k2) : k2;
+        float4 g1, g2;
+        if (KIND == FTE_KIND_SLP) {
+            const float4 q1 = p0[0], q2 = p0[GS];
+            slp_mult_ff(k1, k2, f, etab, q1, q2, g1, g2);
+            if (nyq_x || nyq_y) {
+                float4 h1, h2;
+                slp_mult_ff(k1m, k2m, f, etab, q1, q2, h1, h2);
+                g1 = ffc_avg(g1, h1);
+                g2 = ffc_avg(g2, h2);
+            }
+        } else {
+            const float4 a = p0[0], s21 = p0[GS], s12 = p0[2 * GS], d = p0[3 * GS];
+            dlp_mult_ff(k1, k2, f, etab, a, s21, s12, d, g1, g2);
+            if (nyq_x || nyq_y) {
+                float4 h1, h2;
+                dlp_mult_ff(k1m, k2m, f, etab, a, s21, s12, d, h1, h2);
+                g1 = ffc_avg(g1, h1);
+                g2 = ffc_avg(g2, h2);
+            }
+        }
+        p0[0] = g1;
+        p0[GS] = g2;
+    }
+}
+
+FfFilt ff_filter_consts(double Lx, double Ly, double xi, double eta) {
+    auto sp = [](double v) {
+        const float h = (float)v;
+        return make_float2(h, (float)(v - (double)h));
+    };
+    FfFilt f;
+    f.c1 = sp(2.0 * FTE_PI / Lx);
+    f.c2 = sp(2.0 * FTE_PI / Ly);
+    f.c4 = sp(0.25 / (xi * xi));
+    f.cq = sp((1.0 - eta) / (4.0 * xi * xi));
+    return f;
+}
+
 inline int pt_grid(fte_context* ctx, int64_t n) {
     int64_t b = (n + kPtThreads - 1) / kPtThreads;
     int64_t maxb = (int64_t)ctx->num_sms * 16;
@@ -1870,10 +1982,21 @@ int fte_kspace_run(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, fte_info
         FTE_LAUNCH(ctx, k_fft_x_ff, dim3(Kh, ng), fft_threads(px.m), sm_x, Hf, Mx, Kh, px, 0);
         int fb = (int)(((size_t)Mx * Kh + 255) / 256);
         if (fb > ctx->num_sms * 32) fb = ctx->num_sms * 32;
-        if (a.kind == FTE_KIND_SLP)
+        // the multipliers in float-float while (1 - eta) K / (4 xi^2) stays
+        // inside the float-float exponential's range (it reaches K ~ (pi M / L)^2)
+        const double kmax = FTE_PI * (Mx / a.Lx > My / a.Ly ? Mx / a.Lx : My / a.Ly);
+        const double xext = fabs(1.0 - a.eta) * 2.0 * kmax * kmax / (4.0 * a.xi * a.xi);
+        if (xext < 75.0) {
+            const FfFilt ffc = ff_filter_consts(a.Lx, a.Ly, a.xi, a.eta);
+            if (a.kind == FTE_KIND_SLP)
+                FTE_LAUNCH(ctx, k_filter_ff<FTE_KIND_SLP>, fb, 256, 0, Hf, Mx, My, ffc);
+            else
+                FTE_LAUNCH(ctx, k_filter_ff<FTE_KIND_DLP>, fb, 256, 0, Hf, Mx, My, ffc);
+        } else if (a.kind == FTE_KIND_SLP) {
             FTE_LAUNCH(ctx, (k_filter<FTE_KIND_SLP, float4>), fb, 256, 0, Hf, Mx, My, a.Lx, a.Ly, a.xi, a.eta);
-        else
+        } else {
             FTE_LAUNCH(ctx, (k_filter<FTE_KIND_DLP, float4>), fb, 256, 0, Hf, Mx, My, a.Lx, a.Ly, a.xi, a.eta);
+        }
         FTE_LAUNCH(ctx, k_fft_x_ff, dim3(Kh, 2), fft_threads(px.m), sm_x, Hf, Mx, Kh, px, 1);
         FTE_LAUNCH(ctx, k_fft_y_c2r_ff, dim3(Mx / 2, 2), fft_threads(py.m), sm_y, (const float4*)Hf,
                    reinterpret_cast<float2*>(H), Mx, My, py);
