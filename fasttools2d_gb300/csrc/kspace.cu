@@ -1365,21 +1365,20 @@ __global__ void k_ff_win(int kind, const double* __restrict__ p, const double* _
 
 // Column-owned spread of grids (2 pass, 2 pass + 1) in float-float: the
 // scheme of k_spread_cols (warp w adds every region column c = w mod warps,
-// lane j window row j) with pairs in shared memory; the region is flushed
-// to the FP64 grids.
+// lane j window row j) with the two grids' (sum, low parts) interleaved in one
+// float4 per region node; the region is flushed to the FP64 grids.
 __global__ void __launch_bounds__(kColThreads) k_spread_ff(int pass, const FfWin* __restrict__ recs,
                                                           const int* __restrict__ toff, int ts, int ntx, int nty,
                                                           WinParams wp, double* __restrict__ H0,
                                                           double* __restrict__ H1) {
     extern __shared__ __align__(16) unsigned char shraw[];
-    float2* shf = reinterpret_cast<float2*>(shraw);
     const int P1 = wp.P + 1, W = tile_region(ts, wp.P), WW = W * W;
     const int P1e = (P1 + 1) & ~1;
-    float2* buf = shf;                      // 2 * WW
-    float2* e1 = buf + 2 * WW;              // P1e
-    float2* fw = e1 + P1e;                  // kColChunk * 2 * P1
-    float2* wy = fw + kColChunk * 2 * P1;   // kColChunk * P1
-    int* org = reinterpret_cast<int*>(wy + kColChunk * P1);  // kColChunk * 2 (lx, ly)
+    float4* buf = reinterpret_cast<float4*>(shraw);  // WW: (grid 0 sum, low, grid 1 sum, low)
+    float4* fw = buf + WW;                            // kColChunk * P1: q0 wx, q1 wx (float-float each)
+    float2* e1 = reinterpret_cast<float2*>(fw + kColChunk * P1);  // P1e
+    float2* wy = e1 + P1e;                                         // kColChunk * P1
+    int* org = reinterpret_cast<int*>(wy + kColChunk * P1);        // kColChunk * 2 (lx, ly)
     load_e1_ff(e1, wp);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     constexpr int nw = kColWarps;
@@ -1388,7 +1387,7 @@ __global__ void __launch_bounds__(kColThreads) k_spread_ff(int pass, const FfWin
         if (k0 == k1) continue;
         const int ox = (tile % ntx) * ts - wp.P / 2 - 2, oy = (tile / ntx) * ts - wp.P / 2 - 2;
         __syncthreads();
-        for (int i = threadIdx.x; i < 2 * WW; i += blockDim.x) buf[i] = make_float2(0.f, 0.f);
+        for (int i = threadIdx.x; i < WW; i += blockDim.x) buf[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         for (int c0 = k0; c0 < k1; c0 += kColChunk) {
             const int cn = min(kColChunk, k1 - c0);
             __syncthreads();
@@ -1408,39 +1407,39 @@ __global__ void __launch_bounds__(kColThreads) k_spread_ff(int pass, const FfWin
                 const FfWin& r = recs[c0 + lane];
                 const float2 e3 = r.ex3, q0 = r.q[2 * pass], q1 = r.q[2 * pass + 1];
                 float2 ex = r.e0;
-                float2* fa = fw + (lane * 2) * P1;
+                float4* fa = fw + lane * P1;
                 for (int a = 0; a < P1; a++) {
                     const float2 wxa = ff_mul(ex, e1[a]);
-                    fa[a] = ff_mul(q0, wxa);
-                    fa[P1 + a] = ff_mul(q1, wxa);
+                    const float2 u = ff_mul(q0, wxa), v = ff_mul(q1, wxa);
+                    fa[a] = make_float4(u.x, u.y, v.x, v.y);
                     ex = ff_mul(ex, e3);
                 }
             }
             __syncthreads();
-            for (int s = 0; s < cn; s++) {
-                const int lx = org[2 * s], ly = org[2 * s + 1];
-                const bool inside = lx >= 0 && ly >= 0 && lx + wp.P < W && ly + wp.P < W;
-                // first column >= lx owned by this warp
-                int c = lx + ((warp - lx) & (nw - 1));
-                if (lane < P1) {
+            if (lane < P1) {
+                for (int s = 0; s < cn; s++) {
+                    const int2 o = *reinterpret_cast<const int2*>(org + 2 * s);
+                    const int lx = o.x, ly = o.y;
                     const float2 wyj = wy[s * P1 + lane];
-                    const float2* fa = fw + (s * 2) * P1;
-                    const float2* fb = fa + P1;
-                    if (inside) {
+                    const float4* fa = fw + s * P1;
+                    // first column >= lx owned by this warp
+                    int c = lx + ((warp - lx) & (nw - 1));
+                    if (lx >= 0 && ly >= 0 && lx + wp.P < W && ly + wp.P < W) {
+                        float4* b = buf + ly + lane;
                         for (; c <= lx + wp.P; c += nw) {
-                            float2* b0 = buf + c * W + ly + lane;
-                            float2 v0 = b0[0], v1 = b0[WW];
-                            ff_mac(fa[c - lx], wyj, v0.x, v0.y);
-                            ff_mac(fb[c - lx], wyj, v1.x, v1.y);
-                            b0[0] = v0;
-                            b0[WW] = v1;
+                            const float4 f = fa[c - lx];
+                            float4 v = b[c * W];
+                            ff_mac(make_float2(f.x, f.y), wyj, v.x, v.y);
+                            ff_mac(make_float2(f.z, f.w), wyj, v.z, v.w);
+                            b[c * W] = v;
                         }
                     } else {
                         // window outside the region: straight into the global grids
                         const size_t row = fte_wrap_index(oy + ly + lane, wp.My);
                         for (; c <= lx + wp.P; c += nw) {
                             const size_t at = (size_t)fte_wrap_index(ox + c, wp.Mx) * wp.My + row;
-                            const float2 p0 = ff_mul(fa[c - lx], wyj), p1 = ff_mul(fb[c - lx], wyj);
+                            const float4 f = fa[c - lx];
+                            const float2 p0 = ff_mul(make_float2(f.x, f.y), wyj), p1 = ff_mul(make_float2(f.z, f.w), wyj);
                             atomicAdd(&H0[at], ff_join(p0.x, p0.y));
                             atomicAdd(&H1[at], ff_join(p1.x, p1.y));
                         }
@@ -1449,20 +1448,26 @@ __global__ void __launch_bounds__(kColThreads) k_spread_ff(int pass, const FfWin
             }
         }
         __syncthreads();
-        for (int idx = threadIdx.x; idx < 2 * WW; idx += blockDim.x) {
-            const float2 v = buf[idx];
-            if (v.x == 0.f && v.y == 0.f) continue;
-            int g = idx >= WW, r = idx - g * WW;
-            int xx = r / W, yy = r - xx * W;
-            size_t at = (size_t)fte_wrap_index(ox + xx, wp.Mx) * wp.My + fte_wrap_index(oy + yy, wp.My);
-            atomicAdd(g ? &H1[at] : &H0[at], ff_join(v.x, v.y));
+        // flush: warp per region column, lanes along it (wrapped indices formed
+        // incrementally)
+        for (int xx = warp; xx < W; xx += nw) {
+            const size_t col = (size_t)fte_wrap_index(ox + xx, wp.Mx) * wp.My;
+            int gy = fte_wrap_index(oy + lane, wp.My);
+            for (int yy = lane; yy < W; yy += 32) {
+                const float4 v = buf[xx * W + yy];
+                if (v.x != 0.f || v.y != 0.f) atomicAdd(&H0[col + gy], ff_join(v.x, v.y));
+                if (v.z != 0.f || v.w != 0.f) atomicAdd(&H1[col + gy], ff_join(v.z, v.w));
+                gy += 32;
+                while (gy >= wp.My) gy -= wp.My;
+            }
         }
     }
 }
 
 size_t spread_ff_smem(int ts, int P) {
     const int P1 = P + 1, W = tile_region(ts, P);
-    return (size_t)(2 * W * W + ((P1 + 1) & ~1) + kColChunk * 3 * P1) * sizeof(float2) + kColChunk * 2 * sizeof(int);
+    return (size_t)W * W * sizeof(float4) + (size_t)kColChunk * P1 * sizeof(float4) +
+           (size_t)(((P1 + 1) & ~1) + kColChunk * P1) * sizeof(float2) + kColChunk * 2 * sizeof(int);
 }
 
 // FP64 grid values -> float-float pairs, in place
