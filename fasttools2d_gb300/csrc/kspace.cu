@@ -1334,15 +1334,24 @@ __device__ __forceinline__ void load_e1_ff(float2* e1, const WinParams& wp) {
 __global__ void k_ff_win(int kind, const double* __restrict__ p, const double* __restrict__ f,
                          const double* __restrict__ nrm, const double* __restrict__ wts, const int* __restrict__ perm,
                          int64_t n, WinParams wp, FfWin* __restrict__ out) {
+    // the three window factors as float-float exponentials of FP64 arguments:
+    // e0 = ex e4y = exp(t (px^2 + py^2 + 2 w (px + py))), e3x = exp(-2 t h px),
+    // e3y = exp(-2 t h py), t = -2 xi^2 / eta (the factors of window_of)
+    __shared__ float2 etab[64];
+    for (int j = threadIdx.x; j < 64; j += blockDim.x) etab[j] = ff_split(exp2(-j / 64.0));
+    __syncthreads();
+    const double t = -2 * wp.xi * wp.xi / wp.eta;
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
         const int i = perm[k];
-        Win wn = window_of(p[2 * i], p[2 * i + 1], wp);
+        int mx, my;
+        double px, py;
+        fte_closest_node(p[2 * i], p[2 * i + 1], wp.Lx, wp.Ly, wp.h, wp.P, &mx, &my, &px, &py);
         FfWin r;
-        r.mx = wn.mx;
-        r.my = wn.my;
-        r.e0 = ff_split(wn.ex * wn.e4y);
-        r.ex3 = ff_split(wn.e3x);
-        r.ey3 = ff_split(wn.e3y);
+        r.mx = mx;
+        r.my = my;
+        r.e0 = fte_expm_ff(ff_split(-t * (px * px + py * py + 2 * wp.w * (px + py))), etab);
+        r.ex3 = fte_expm_ff(ff_split(2 * t * wp.h * px), etab);
+        r.ey3 = fte_expm_ff(ff_split(2 * t * wp.h * py), etab);
         double f1 = f[2 * i], f2 = f[2 * i + 1];
         if (wts) {
             f1 *= wts[i];
@@ -1502,7 +1511,10 @@ __global__ void __launch_bounds__(kTileThreads) k_gather_ff(const double* __rest
     float2* r1 = r0 + WW;
     float2* e1 = r1 + WW;
     float2* wyb = e1 + ((P1 + 1) & ~1) + threadIdx.x * P1;
+    __shared__ float2 etab[64];  // 2^(-j/64) for the window factors (as in k_ff_win)
+    for (int j = threadIdx.x; j < 64; j += blockDim.x) etab[j] = ff_split(exp2(-j / 64.0));
     load_e1_ff(e1, wp);
+    const double tw = -2 * wp.xi * wp.xi / wp.eta;
     for (int tile = blockIdx.x; tile < ntx * nty; tile += gridDim.x) {
         const int k0 = toff[tile], k1 = toff[tile + 1];
         if (k0 == k1) continue;
@@ -1517,18 +1529,20 @@ __global__ void __launch_bounds__(kTileThreads) k_gather_ff(const double* __rest
         __syncthreads();
         for (int k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
             const int i = perm[k];
-            Win wn = window_of(p[2 * i], p[2 * i + 1], wp);
+            int mx, my;
+            double px, py;
+            fte_closest_node(p[2 * i], p[2 * i + 1], wp.Lx, wp.Ly, wp.h, wp.P, &mx, &my, &px, &py);
             {
-                const float2 e3 = ff_split(wn.e3y);
+                const float2 e3 = fte_expm_ff(ff_split(2 * tw * wp.h * py), etab);
                 float2 ey = make_float2(1.f, 0.f);
                 for (int j = 0; j < P1; j++) {
                     wyb[j] = ff_mul(e1[j], ey);
                     ey = ff_mul(ey, e3);
                 }
             }
-            const float2 e3x = ff_split(wn.e3x);
-            float2 ex = ff_split(wn.ex * wn.e4y);
-            const int lx = wn.mx - ox, ly = wn.my - oy;
+            const float2 e3x = fte_expm_ff(ff_split(2 * tw * wp.h * px), etab);
+            float2 ex = fte_expm_ff(ff_split(-tw * (px * px + py * py + 2 * wp.w * (px + py))), etab);
+            const int lx = mx - ox, ly = my - oy;
             float a0 = 0.f, c0 = 0.f, a1 = 0.f, c1 = 0.f;
             const bool inside = lx >= 0 && ly >= 0 && lx + wp.P < W && ly + wp.P < W;
             for (int a = 0; a < P1; a++) {
@@ -1544,9 +1558,9 @@ __global__ void __launch_bounds__(kTileThreads) k_gather_ff(const double* __rest
                         ff_mac(w, g1[j], s1, t1);
                     }
                 } else {
-                    const size_t base = (size_t)fte_wrap_index(wn.mx + a, wp.Mx) * wp.My;
+                    const size_t base = (size_t)fte_wrap_index(mx + a, wp.Mx) * wp.My;
                     for (int j = 0; j < P1; j++) {
-                        const size_t at = base + fte_wrap_index(wn.my + j, wp.My);
+                        const size_t at = base + fte_wrap_index(my + j, wp.My);
                         const float2 w = wyb[j];
                         ff_mac(w, G0[at], s0, t0);
                         ff_mac(w, G1[at], s1, t1);
