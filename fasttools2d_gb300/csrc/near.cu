@@ -30,8 +30,19 @@
 
 namespace {
 
-constexpr int kNearThreads = 256;
-constexpr int kNearWarps = kNearThreads / 32;
+// CTA shape per layout.  The float-float kernel runs 4 warps per CTA and 4
+// CTAs per SM: a box's targets are shared by fewer warps (longer runs of
+// targets per warp, fewer queue drains per box) and boxes overlap across
+// more CTAs.  The FP64 kernel keeps 8 warps and 2 CTAs (its larger staged
+// sources want the bigger shared-memory share).
+template <bool L>
+struct NearCfg {
+    static constexpr int threads = L ? 128 : 256;
+    static constexpr int warps = threads / 32;
+    static constexpr int ctas = L ? 4 : 2;          // per SM
+    static constexpr int grid_per_sm = L ? 32 : 16;  // grid-stride launch size
+    static constexpr size_t budget = L ? 54 * 1024 : 110 * 1024;
+};
 constexpr int kQueue = 64;
 constexpr int kGtab = FTE_E1_NPIECE_G * (FTE_E1_DEG_G + 1);
 constexpr int kKtab = FTE_K_NPIECE * (FTE_K_DEG + 1);
@@ -264,7 +275,12 @@ struct NearSmem {
     // targets a warp keeps in flight (ring entries carry the slot): the
     // accumulators cost NSLOT * NV * 2 doubles per lane
     static constexpr int kSlots = NV == 1 ? 4 : (NV == 2 ? 2 : 1);
-    static constexpr int kHead = 2 * kKtab + 128 + 12 + kKtab / 2 + 1;  // doubles before the staged sources
+    // doubles before the staged sources: the FP64 kernel's K(x) and exp
+    // tables, or the float-float kernel's K(x), exp and small-x E1 tables,
+    // then the FP32 K(x) table
+    __host__ __device__ static constexpr int head(bool ff) {
+        return (ff ? kKtab + 64 + 12 : kKtab + 64) + kKtab / 2 + 1;
+    }
     // per staged source: FP64 layout (x, y, densities; FP32 copies) or, with
     // the float-float class, float-float only (position and densities as
     // FP32 + low part)
@@ -273,7 +289,8 @@ struct NearSmem {
                   : (2 + kDen * NV) * sizeof(double) + sizeof(float2) + kDen * NV * sizeof(float);
     }
     __host__ __device__ static size_t bytes(int cap, bool ff) {
-        return kHead * sizeof(double) + (size_t)cap * per_source(ff) + kNearWarps * 3 * kQueue * sizeof(int) + 64;
+        return head(ff) * sizeof(double) + (size_t)cap * per_source(ff) +
+               (ff ? NearCfg<true>::warps : NearCfg<false>::warps) * 3 * kQueue * sizeof(int) + 64;
     }
 };
 
@@ -284,23 +301,26 @@ template <int KIND, int NV, bool FF>
 __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned char* smem_raw, int* nb_box,
                                          int* nb_start, double* nb_shx, double* nb_shy) {
     constexpr int kDen = NearSmem<KIND, NV>::kDen;
-    // float-float class (FF; density vectors beyond two keep the FP64 path:
-    // the float-float accumulators would not fit the register budget)
-    constexpr bool ffn = FF && NV <= 2;
+    // float-float class (FF)
+    constexpr bool ffn = FF;
+    constexpr int kNearThreads = NearCfg<ffn>::threads;
+    constexpr int kNearWarps = NearCfg<ffn>::warps;
     // targets in flight: the FP64 classes gain from four (partial FP64
     // batches are what costs), the float-float ones from two (the slot
-    // selects are what costs)
-    constexpr int NSLOT = ffn ? 2 : NearSmem<KIND, NV>::kSlots;
+    // selects are what costs); one beyond two density vectors (registers)
+    constexpr int NSLOT = ffn ? (NV <= 2 ? 2 : 1) : NearSmem<KIND, NV>::kSlots;
     const int cap = prm.cap;
+    // tables: FP64 kernel: ktab, etab, ktab32; float-float kernel: ktabff,
+    // etabff, rtabff, ktab32
     const double* ktab = reinterpret_cast<const double*>(smem_raw);
     const double* etab = ktab + kKtab;
-    const float2* ktabff = reinterpret_cast<const float2*>(etab + 64);
+    const float2* ktabff = reinterpret_cast<const float2*>(smem_raw);
     const float2* etabff = ktabff + kKtab;
     const float2* rtabff = etabff + 64;
-    const float* ktab32 = reinterpret_cast<const float*>(rtabff + 12);
+    const float* ktab32 = ffn ? reinterpret_cast<const float*>(rtabff + 12) : reinterpret_cast<const float*>(etab + 64);
     // FP64 layout: x, y, densities (FP64), FP32 position, FP32 densities;
     // float-float layout: FP32 position, FP32 densities, their low parts
-    double* const s0 = reinterpret_cast<double*>(smem_raw) + NearSmem<KIND, NV>::kHead;
+    double* const s0 = reinterpret_cast<double*>(smem_raw) + NearSmem<KIND, NV>::head(ffn);
     double* sx = ffn ? nullptr : s0;
     double* sy = ffn ? nullptr : s0 + cap;
     double* den = ffn ? nullptr : s0 + 2 * cap;  // den[(v * kDen + c) * cap + i]
@@ -652,7 +672,7 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
         };
         // x >= 1: A = e^-x K(x)
         auto eval_slp_ff = [&](int ent) {
-            if constexpr (NV <= 2) {
+            {
                 const int s = ent >> 2, tag = ent & 3;
                 float2 dx, dy, r2;
                 ff_geom(s, tag, dx, dy, r2);
@@ -665,7 +685,7 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
         // x < 1: A = 0.5 E1(x) - e^-x by its series; the self term
         // (-1 - gamma/2 - log xi) f for a coincident source of the own box
         auto eval_slp_ff_small = [&](int ent) {
-            if constexpr (NV <= 2) {
+            {
                 const int s = ent >> 2, tag = ent & 3;
                 float2 dx, dy, r2;
                 ff_geom(s, tag, dx, dy, r2);
@@ -690,7 +710,7 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
             }
         };
         auto eval_dlp_ff = [&](int ent) {
-            if constexpr (NV <= 2) {
+            {
                 const int s = ent >> 2, tag = ent & 3;
                 float2 dx, dy, r2;
                 ff_geom(s, tag, dx, dy, r2);
@@ -938,35 +958,43 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
     }
 }
 
-template <int KIND, int NV>
+template <int KIND, int NV, bool FF>
 __device__ __forceinline__ void near_load_tables(unsigned char* smem_raw) {
-    double* ktab = reinterpret_cast<double*>(smem_raw);
-    double* etab = ktab + kKtab;
-    float2* ktabff = reinterpret_cast<float2*>(etab + 64);
-    float2* etabff = ktabff + kKtab;
-    float2* rtabff = etabff + 64;
-    float* ktab32 = reinterpret_cast<float*>(rtabff + 12);
-    for (int i = threadIdx.x; i < kKtab; i += kNearThreads) {
-        const double c = (&fte_k_coef[0][0])[i];
-        ktab[i] = c;
-        ktabff[i] = ff_split(c);
-        ktab32[i] = (float)c;
+    constexpr bool ffn = FF;
+    constexpr int kNearThreads = NearCfg<FF>::threads;
+    if constexpr (ffn) {
+        float2* ktabff = reinterpret_cast<float2*>(smem_raw);
+        float2* etabff = ktabff + kKtab;
+        float2* rtabff = etabff + 64;
+        float* ktab32 = reinterpret_cast<float*>(rtabff + 12);
+        for (int i = threadIdx.x; i < kKtab; i += kNearThreads) {
+            const double c = (&fte_k_coef[0][0])[i];
+            ktabff[i] = ff_split(c);
+            ktab32[i] = (float)c;
+        }
+        for (int i = threadIdx.x; i < 64; i += kNearThreads) etabff[i] = ff_split(fte_exp_tab[i]);
+        static_assert(FTE_E1_DEG_R + 1 <= 12, "small-x E1 table");
+        for (int i = threadIdx.x; i <= FTE_E1_DEG_R; i += kNearThreads) rtabff[i] = ff_split(fte_e1_coef_r[i]);
+    } else {
+        double* ktab = reinterpret_cast<double*>(smem_raw);
+        double* etab = ktab + kKtab;
+        float* ktab32 = reinterpret_cast<float*>(etab + 64);
+        for (int i = threadIdx.x; i < kKtab; i += kNearThreads) {
+            const double c = (&fte_k_coef[0][0])[i];
+            ktab[i] = c;
+            ktab32[i] = (float)c;
+        }
+        for (int i = threadIdx.x; i < 64; i += kNearThreads) etab[i] = fte_exp_tab[i];
     }
-    for (int i = threadIdx.x; i < 64; i += kNearThreads) {
-        etab[i] = fte_exp_tab[i];
-        etabff[i] = ff_split(fte_exp_tab[i]);
-    }
-    static_assert(FTE_E1_DEG_R + 1 <= 12, "small-x E1 table");
-    for (int i = threadIdx.x; i <= FTE_E1_DEG_R; i += kNearThreads) rtabff[i] = ff_split(fte_e1_coef_r[i]);
 }
 
 // one problem: grid-stride over its boxes
 template <int KIND, int NV, bool FF>
-__global__ void __launch_bounds__(kNearThreads, 2) k_near(const NearParams prm) {
+__global__ void __launch_bounds__(NearCfg<FF>::threads, NearCfg<FF>::ctas) k_near(const NearParams prm) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int nb_box[9], nb_start[10];
     __shared__ double nb_shx[9], nb_shy[9];
-    near_load_tables<KIND, NV>(smem_raw);
+    near_load_tables<KIND, NV, FF>(smem_raw);
     for (int b = blockIdx.x; b < prm.nb; b += gridDim.x)
         near_box<KIND, NV, FF>(prm, b, smem_raw, nb_box, nb_start, nb_shx, nb_shy);
 }
@@ -976,12 +1004,12 @@ __global__ void __launch_bounds__(kNearThreads, 2) k_near(const NearParams prm) 
 constexpr int kParamStride = sizeof(NearParamsHost);
 
 template <int KIND, int NV, bool FF>
-__global__ void __launch_bounds__(kNearThreads, 2) k_near_batch(const unsigned char* __restrict__ plist,
+__global__ void __launch_bounds__(NearCfg<FF>::threads, NearCfg<FF>::ctas) k_near_batch(const unsigned char* __restrict__ plist,
                                                                 const int2* __restrict__ items, int nitems) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int nb_box[9], nb_start[10];
     __shared__ double nb_shx[9], nb_shy[9];
-    near_load_tables<KIND, NV>(smem_raw);
+    near_load_tables<KIND, NV, FF>(smem_raw);
     for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
         const int2 w = items[it];
         // read in place (a register copy of the description would spill)
@@ -1029,8 +1057,10 @@ __global__ void k_near_ff_prep(const NearParams prm, int nv, float4* __restrict_
 template <int KIND, int NV>
 int near_cap(const fte_context* ctx, bool ff) {
     int cap = 2048;
-    const size_t budget = 110 * 1024 < (size_t)ctx->max_smem_optin ? 110 * 1024 : (size_t)ctx->max_smem_optin;
-    while (cap > 128 && NearSmem<KIND, NV>::bytes(cap, ff) > budget) cap -= 64;
+    // shared memory of one of the CTAs an SM holds (227 KB per SM)
+    const size_t b0 = ff ? NearCfg<true>::budget : NearCfg<false>::budget;
+    const size_t budget = b0 < (size_t)ctx->max_smem_optin ? b0 : (size_t)ctx->max_smem_optin;
+    while (cap > 64 && NearSmem<KIND, NV>::bytes(cap, ff) > budget) cap -= 32;
     return cap;
 }
 }  // namespace
@@ -1130,45 +1160,41 @@ size_t fte_near_params_size() { return sizeof(NearParams); }
 namespace {
 template <int KIND, int NV>
 int near_launch_one(fte_context* ctx, NearParams p) {
-    const bool ff = NV <= 2 && p.ffnear;
+    const bool ff = p.ffnear != 0;
     p.cap = near_cap<KIND, NV>(ctx, ff);
     size_t smem = NearSmem<KIND, NV>::bytes(p.cap, ff);
-    int grid = p.nb < ctx->num_sms * 16 ? p.nb : ctx->num_sms * 16;
-    if (grid < 1) grid = 1;
-    if constexpr (NV <= 2) {
-        if (ff) {
-            FTE_CUDA_TRY(
-                cudaFuncSetAttribute(k_near<KIND, NV, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            FTE_LAUNCH(ctx, (k_near<KIND, NV, true>), grid, kNearThreads, smem, p);
-            return FTE_OK;
-        }
-    }
-    {
+    if (ff) {
+        using C = NearCfg<true>;
+        const int grid = p.nb < ctx->num_sms * C::grid_per_sm ? (p.nb > 0 ? p.nb : 1) : ctx->num_sms * C::grid_per_sm;
+        FTE_CUDA_TRY(
+            cudaFuncSetAttribute(k_near<KIND, NV, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        FTE_LAUNCH(ctx, (k_near<KIND, NV, true>), grid, C::threads, smem, p);
+    } else {
+        using C = NearCfg<false>;
+        const int grid = p.nb < ctx->num_sms * C::grid_per_sm ? (p.nb > 0 ? p.nb : 1) : ctx->num_sms * C::grid_per_sm;
         FTE_CUDA_TRY(
             cudaFuncSetAttribute(k_near<KIND, NV, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        FTE_LAUNCH(ctx, (k_near<KIND, NV, false>), grid, kNearThreads, smem, p);
+        FTE_LAUNCH(ctx, (k_near<KIND, NV, false>), grid, C::threads, smem, p);
     }
     return FTE_OK;
 }
 
 template <int KIND, int NV>
 int near_launch_batch(fte_context* ctx, bool ff, const unsigned char* plist_dev, const int2* items, int nitems) {
-    ff = ff && NV <= 2;
     const size_t smem = NearSmem<KIND, NV>::bytes(near_cap<KIND, NV>(ctx, ff), ff);
-    int grid = nitems < ctx->num_sms * 16 ? nitems : ctx->num_sms * 16;
-    if (grid < 1) return FTE_OK;
-    if constexpr (NV <= 2) {
-        if (ff) {
-            FTE_CUDA_TRY(cudaFuncSetAttribute(k_near_batch<KIND, NV, true>,
-                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            FTE_LAUNCH(ctx, (k_near_batch<KIND, NV, true>), grid, kNearThreads, smem, plist_dev, items, nitems);
-            return FTE_OK;
-        }
-    }
-    {
+    if (nitems < 1) return FTE_OK;
+    if (ff) {
+        using C = NearCfg<true>;
+        const int grid = nitems < ctx->num_sms * C::grid_per_sm ? nitems : ctx->num_sms * C::grid_per_sm;
+        FTE_CUDA_TRY(cudaFuncSetAttribute(k_near_batch<KIND, NV, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smem));
+        FTE_LAUNCH(ctx, (k_near_batch<KIND, NV, true>), grid, C::threads, smem, plist_dev, items, nitems);
+    } else {
+        using C = NearCfg<false>;
+        const int grid = nitems < ctx->num_sms * C::grid_per_sm ? nitems : ctx->num_sms * C::grid_per_sm;
         FTE_CUDA_TRY(cudaFuncSetAttribute(k_near_batch<KIND, NV, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)smem));
-        FTE_LAUNCH(ctx, (k_near_batch<KIND, NV, false>), grid, kNearThreads, smem, plist_dev, items, nitems);
+        FTE_LAUNCH(ctx, (k_near_batch<KIND, NV, false>), grid, C::threads, smem, plist_dev, items, nitems);
     }
     return FTE_OK;
 }
@@ -1177,7 +1203,6 @@ int near_launch_batch(fte_context* ctx, bool ff, const unsigned char* plist_dev,
 bool fte_near_uses_ff(const NearParamsHost& hp) { return reinterpret_cast<const NearParams*>(hp.raw)->ffnear != 0; }
 
 int fte_near_cap(const fte_context* ctx, int kind, int nv, bool ff) {
-    ff = ff && nv <= 2;
     if (kind == FTE_KIND_SLP) {
         switch (nv) {
             case 1: return near_cap<FTE_KIND_SLP, 1>(ctx, ff);

@@ -601,7 +601,7 @@ extern "C" int fte_batch_create(fte_context* c, fte_plan* const* plans, int npla
         need += 2 * ws_bytes(nv * (p->nsrc + 1), 8) + 2 * ws_bytes(nv * (p->ntar + 1), 8);
         if (p->ntar > 0) {
             NearParamsHost h = p->near;
-            const bool ff = fte_near_uses_ff(h) && nv <= 2;
+            const bool ff = fte_near_uses_ff(h);
             const int k = p->kind * 2 + (ff ? 1 : 0);
             fte_near_set_output(&h, p->ur, p->ntar, fte_near_cap(c, p->kind, nv, ff));
             int idx = (int)pls[k].size();
