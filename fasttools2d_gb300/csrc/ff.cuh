@@ -78,6 +78,16 @@ __device__ __forceinline__ float2 ff_rcp(float2 a) {
     e = __fmaf_rn(-a.y, y, e);
     return ff_norm(y, __fmul_rn(y, e));
 }
+// x^n, n >= 0, by binary powering
+__device__ __forceinline__ float2 ff_powi(float2 x, int n) {
+    float2 r = make_float2(1.f, 0.f);
+    while (n) {
+        if (n & 1) r = ff_mul(r, x);
+        n >>= 1;
+        if (n) x = ff_mul(x, x);
+    }
+    return r;
+}
 // a < b
 __device__ __forceinline__ bool ff_lt(float2 a, float2 b) { return a.x < b.x || (a.x == b.x && a.y < b.y); }
 

@@ -631,8 +631,9 @@ __device__ __forceinline__ void spec_st(float4* p, double2 v) {
     *p = make_float4(r.x, r.y, i.x, i.y);
 }
 
+// DLP spectra: ng = 4 (S11, S21, S12, S22) or 3 (S11, S12 + S21, S22)
 template <int KIND, typename S>
-__global__ void k_filter(S* __restrict__ Hh, int Mx, int My, double Lx, double Ly, double xi, double eta) {
+__global__ void k_filter(S* __restrict__ Hh, int Mx, int My, double Lx, double Ly, double xi, double eta, int ng) {
     const int Kh = My / 2 + 1;
     const size_t GS = (size_t)Mx * Kh;
     const size_t tot = GS;
@@ -658,7 +659,8 @@ __global__ void k_filter(S* __restrict__ Hh, int Mx, int My, double Lx, double L
                 g2 = make_double2(0.5 * (g2.x + h2.x), 0.5 * (g2.y + h2.y));
             }
         } else {
-            double2 a = spec_ld(p0), s21 = spec_ld(p0 + GS), s12 = spec_ld(p0 + 2 * GS), d = spec_ld(p0 + 3 * GS);
+            const double2 a = spec_ld(p0), s21 = spec_ld(p0 + GS), d = spec_ld(p0 + (ng - 1) * GS);
+            const double2 s12 = ng == 4 ? spec_ld(p0 + 2 * GS) : make_double2(0, 0);
             dlp_mult(k1, k2, xi, eta, a, s21, s12, d, g1, g2);
             if (nyq_x || nyq_y) {
                 double2 h1, h2;
@@ -727,7 +729,7 @@ __device__ __forceinline__ float4 ffc_avg(float4 a, float4 b) {
 }
 
 template <int KIND>
-__global__ void k_filter_ff(float4* __restrict__ Hh, int Mx, int My, FfFilt f) {
+__global__ void k_filter_ff(float4* __restrict__ Hh, int Mx, int My, FfFilt f, int ng) {
     __shared__ float2 etab[64];
     for (int i = threadIdx.x; i < 64; i += blockDim.x) etab[i] = ff_split(exp2(-i / 64.0));
     __syncthreads();
@@ -757,7 +759,8 @@ __global__ void k_filter_ff(float4* __restrict__ Hh, int Mx, int My, FfFilt f) {
                 g2 = ffc_avg(g2, h2);
             }
         } else {
-            const float4 a = p0[0], s21 = p0[GS], s12 = p0[2 * GS], d = p0[3 * GS];
+            const float4 a = p0[0], s21 = p0[GS], d = p0[(ng - 1) * GS];
+            const float4 s12 = ng == 4 ? p0[2 * GS] : make_float4(0.f, 0.f, 0.f, 0.f);
             dlp_mult_ff(k1, k2, f, etab, a, s21, s12, d, g1, g2);
             if (nyq_x || nyq_y) {
                 float4 h1, h2;
@@ -1318,7 +1321,7 @@ __global__ void k_filter32(float2* __restrict__ Hh, int Mx, int My, double Lx, d
 struct FfWin {
     int mx, my;            // first window node
     float2 e0, ex3, ey3;   // ex e4y, e3x, e3y (float-float)
-    float2 q[4];           // densities of the grids (SLP: f1, f2; DLP: f1 n1, f2 n1, f1 n2, f2 n2), weights folded in
+    float2 q[4];           // densities of the grids (SLP: f1, f2; DLP: f1 n1, f2 n1 + f1 n2, f2 n2), weights folded in
 };
 static_assert(sizeof(FfWin) == 64, "FfWin layout");
 
@@ -1362,11 +1365,13 @@ __global__ void k_ff_win(int kind, const double* __restrict__ p, const double* _
             r.q[1] = ff_split(f2);
             r.q[2] = r.q[3] = make_float2(0.f, 0.f);
         } else {
+            // the stresslet's three symmetric products (the multiplier takes
+            // f2 n1 and f1 n2 only through their sum)
             const double n1 = nrm[2 * i], n2 = nrm[2 * i + 1];
             r.q[0] = ff_split(f1 * n1);
-            r.q[1] = ff_split(f2 * n1);
-            r.q[2] = ff_split(f1 * n2);
-            r.q[3] = ff_split(f2 * n2);
+            r.q[1] = ff_split(f2 * n1 + f1 * n2);
+            r.q[2] = ff_split(f2 * n2);
+            r.q[3] = make_float2(0.f, 0.f);
         }
         out[k] = r;
     }
@@ -1374,12 +1379,16 @@ __global__ void k_ff_win(int kind, const double* __restrict__ p, const double* _
 
 // Column-owned spread of grids (2 pass, 2 pass + 1) in float-float: the
 // scheme of k_spread_cols (warp w adds every region column c = w mod warps,
-// lane j window row j) with the two grids' (sum, low parts) interleaved in one
-// float4 per region node; the region is flushed to the FP64 grids.
-__global__ void __launch_bounds__(kColThreads) k_spread_ff(int pass, const FfWin* __restrict__ recs,
+// lane j window row j) with the first two grids' (sum, low parts) interleaved
+// in one float4 per region node (a third grid's pair in a float2 array); the
+// region is flushed to the FP64 grids.  NG = 2 (Stokeslet: f1, f2) or 3
+// (stresslet: the symmetric products f1 n1, f1 n2 + f2 n1, f2 n2 -- the
+// stresslet multiplier sees the two mixed products only through their sum).
+template <int NG>
+__global__ void __launch_bounds__(kColThreads) k_spread_ff(const FfWin* __restrict__ recs,
                                                           const int* __restrict__ toff, int ts, int ntx, int nty,
                                                           WinParams wp, double* __restrict__ H0,
-                                                          double* __restrict__ H1) {
+                                                          double* __restrict__ H1, double* __restrict__ H2) {
     extern __shared__ __align__(16) unsigned char shraw[];
     const int P1 = wp.P + 1, W = tile_region(ts, wp.P), WW = W * W;
     const int P1e = (P1 + 1) & ~1;
@@ -1387,7 +1396,9 @@ __global__ void __launch_bounds__(kColThreads) k_spread_ff(int pass, const FfWin
     float4* fw = buf + WW;                            // kColChunk * P1: q0 wx, q1 wx (float-float each)
     float2* e1 = reinterpret_cast<float2*>(fw + kColChunk * P1);  // P1e
     float2* wy = e1 + P1e;                                         // kColChunk * P1
-    int* org = reinterpret_cast<int*>(wy + kColChunk * P1);        // kColChunk * 2 (lx, ly)
+    float2* buf2 = wy + kColChunk * P1;                            // NG == 3: WW (grid 2 sum, low)
+    float2* fw2 = buf2 + (NG == 3 ? WW : 0);                       // NG == 3: kColChunk * P1 (q2 wx)
+    int* org = reinterpret_cast<int*>(fw2 + (NG == 3 ? kColChunk * P1 : 0));  // kColChunk * 2 (lx, ly)
     load_e1_ff(e1, wp);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     constexpr int nw = kColWarps;
@@ -1396,32 +1407,44 @@ __global__ void __launch_bounds__(kColThreads) k_spread_ff(int pass, const FfWin
         if (k0 == k1) continue;
         const int ox = (tile % ntx) * ts - wp.P / 2 - 2, oy = (tile / ntx) * ts - wp.P / 2 - 2;
         __syncthreads();
-        for (int i = threadIdx.x; i < WW; i += blockDim.x) buf[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int i = threadIdx.x; i < WW; i += blockDim.x) {
+            buf[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+            if constexpr (NG == 3) buf2[i] = make_float2(0.f, 0.f);
+        }
         for (int c0 = k0; c0 < k1; c0 += kColChunk) {
             const int cn = min(kColChunk, k1 - c0);
             __syncthreads();
-            // window rows (warp 0) and density-weighted columns (warp 1) of
-            // the chunk's sources
-            if (warp == 0 && lane < cn) {
-                const FfWin& r = recs[c0 + lane];
-                const float2 e3 = r.ey3;
-                float2 ey = make_float2(1.f, 0.f);
-                for (int j = 0; j < P1; j++) {
-                    wy[lane * P1 + j] = ff_mul(e1[j], ey);
-                    ey = ff_mul(ey, e3);
-                }
-                org[2 * lane] = r.mx - ox;
-                org[2 * lane + 1] = r.my - oy;
-            } else if (warp == 1 && lane < cn) {
-                const FfWin& r = recs[c0 + lane];
-                const float2 e3 = r.ex3, q0 = r.q[2 * pass], q1 = r.q[2 * pass + 1];
-                float2 ex = r.e0;
-                float4* fa = fw + lane * P1;
-                for (int a = 0; a < P1; a++) {
-                    const float2 wxa = ff_mul(ex, e1[a]);
-                    const float2 u = ff_mul(q0, wxa), v = ff_mul(q1, wxa);
-                    fa[a] = make_float4(u.x, u.y, v.x, v.y);
-                    ex = ff_mul(ex, e3);
+            // window rows (warps 0-3) and density-weighted columns (warps
+            // 4-7) of the chunk's sources, a quarter of the support per warp
+            // (each quarter's recurrence starts from a power of the ratio)
+            {
+                const int seg = warp & 3, L = (P1 + 3) >> 2;
+                const int j0 = seg * L, j1 = min(P1, j0 + L);
+                if (lane < cn && j0 < j1) {
+                    const FfWin& r = recs[c0 + lane];
+                    if (warp < 4) {
+                        const float2 e3 = r.ey3;
+                        float2 ey = ff_powi(e3, j0);
+                        for (int j = j0; j < j1; j++) {
+                            wy[lane * P1 + j] = ff_mul(e1[j], ey);
+                            ey = ff_mul(ey, e3);
+                        }
+                        if (seg == 0) {
+                            org[2 * lane] = r.mx - ox;
+                            org[2 * lane + 1] = r.my - oy;
+                        }
+                    } else {
+                        const float2 e3 = r.ex3, q0 = r.q[0], q1 = r.q[1], q2 = r.q[2];
+                        float2 ex = j0 ? ff_mul(r.e0, ff_powi(e3, j0)) : r.e0;
+                        float4* fa = fw + lane * P1;
+                        for (int a = j0; a < j1; a++) {
+                            const float2 wxa = ff_mul(ex, e1[a]);
+                            const float2 u = ff_mul(q0, wxa), v = ff_mul(q1, wxa);
+                            fa[a] = make_float4(u.x, u.y, v.x, v.y);
+                            if constexpr (NG == 3) fw2[lane * P1 + a] = ff_mul(q2, wxa);
+                            ex = ff_mul(ex, e3);
+                        }
+                    }
                 }
             }
             __syncthreads();
@@ -1431,16 +1454,23 @@ __global__ void __launch_bounds__(kColThreads) k_spread_ff(int pass, const FfWin
                     const int lx = o.x, ly = o.y;
                     const float2 wyj = wy[s * P1 + lane];
                     const float4* fa = fw + s * P1;
+                    const float2* fa2 = fw2 + s * P1;
                     // first column >= lx owned by this warp
                     int c = lx + ((warp - lx) & (nw - 1));
                     if (lx >= 0 && ly >= 0 && lx + wp.P < W && ly + wp.P < W) {
                         float4* b = buf + ly + lane;
+                        float2* b2 = buf2 + ly + lane;
                         for (; c <= lx + wp.P; c += nw) {
                             const float4 f = fa[c - lx];
                             float4 v = b[c * W];
                             ff_mac(make_float2(f.x, f.y), wyj, v.x, v.y);
                             ff_mac(make_float2(f.z, f.w), wyj, v.z, v.w);
                             b[c * W] = v;
+                            if constexpr (NG == 3) {
+                                float2 v2 = b2[c * W];
+                                ff_mac(fa2[c - lx], wyj, v2.x, v2.y);
+                                b2[c * W] = v2;
+                            }
                         }
                     } else {
                         // window outside the region: straight into the global grids
@@ -1451,6 +1481,10 @@ __global__ void __launch_bounds__(kColThreads) k_spread_ff(int pass, const FfWin
                             const float2 p0 = ff_mul(make_float2(f.x, f.y), wyj), p1 = ff_mul(make_float2(f.z, f.w), wyj);
                             atomicAdd(&H0[at], ff_join(p0.x, p0.y));
                             atomicAdd(&H1[at], ff_join(p1.x, p1.y));
+                            if constexpr (NG == 3) {
+                                const float2 p2 = ff_mul(fa2[c - lx], wyj);
+                                atomicAdd(&H2[at], ff_join(p2.x, p2.y));
+                            }
                         }
                     }
                 }
@@ -1466,6 +1500,10 @@ __global__ void __launch_bounds__(kColThreads) k_spread_ff(int pass, const FfWin
                 const float4 v = buf[xx * W + yy];
                 if (v.x != 0.f || v.y != 0.f) atomicAdd(&H0[col + gy], ff_join(v.x, v.y));
                 if (v.z != 0.f || v.w != 0.f) atomicAdd(&H1[col + gy], ff_join(v.z, v.w));
+                if constexpr (NG == 3) {
+                    const float2 v2 = buf2[xx * W + yy];
+                    if (v2.x != 0.f || v2.y != 0.f) atomicAdd(&H2[col + gy], ff_join(v2.x, v2.y));
+                }
                 gy += 32;
                 while (gy >= wp.My) gy -= wp.My;
             }
@@ -1473,10 +1511,11 @@ __global__ void __launch_bounds__(kColThreads) k_spread_ff(int pass, const FfWin
     }
 }
 
-size_t spread_ff_smem(int ts, int P) {
+size_t spread_ff_smem(int ts, int P, int ng) {
     const int P1 = P + 1, W = tile_region(ts, P);
+    const size_t third = ng == 3 ? ((size_t)W * W + (size_t)kColChunk * P1) * sizeof(float2) : 0;
     return (size_t)W * W * sizeof(float4) + (size_t)kColChunk * P1 * sizeof(float4) +
-           (size_t)(((P1 + 1) & ~1) + kColChunk * P1) * sizeof(float2) + kColChunk * 2 * sizeof(int);
+           (size_t)(((P1 + 1) & ~1) + kColChunk * P1) * sizeof(float2) + third + kColChunk * 2 * sizeof(int);
 }
 
 // FP64 grid values -> float-float pairs, in place
@@ -1498,7 +1537,12 @@ __global__ void k_ff_join(double* __restrict__ H, int64_t n) {
 }
 
 // Tiled gather in float-float from grids of pairs: a thread per target, the
-// tile's region of both grids staged once in shared memory.
+// tile's region of both grids staged once in shared memory.  PM > 0: window
+// supports of at most PM nodes, the target's window column held in registers
+// and the node loops unrolled to PM (independent products in flight, no
+// shared-memory traffic for the weights); PM == 0: any support, the window
+// column in a per-thread shared-memory row.
+template <int PM>
 __global__ void __launch_bounds__(kTileThreads) k_gather_ff(const double* __restrict__ p, const int* __restrict__ toff,
                                                            const int* __restrict__ perm, int ts, int ntx, int nty,
                                                            WinParams wp, const float2* __restrict__ G0,
@@ -1510,7 +1554,7 @@ __global__ void __launch_bounds__(kTileThreads) k_gather_ff(const double* __rest
     float2* r0 = shf;
     float2* r1 = r0 + WW;
     float2* e1 = r1 + WW;
-    float2* wyb = e1 + ((P1 + 1) & ~1) + threadIdx.x * P1;
+    float2* wyb = e1 + ((P1 + 1) & ~1) + threadIdx.x * P1;  // PM == 0 only
     __shared__ float2 etab[64];  // 2^(-j/64) for the window factors (as in k_ff_win)
     for (int j = threadIdx.x; j < 64; j += blockDim.x) etab[j] = ff_split(exp2(-j / 64.0));
     load_e1_ff(e1, wp);
@@ -1532,12 +1576,21 @@ __global__ void __launch_bounds__(kTileThreads) k_gather_ff(const double* __rest
             int mx, my;
             double px, py;
             fte_closest_node(p[2 * i], p[2 * i + 1], wp.Lx, wp.Ly, wp.h, wp.P, &mx, &my, &px, &py);
+            float2 wy[PM > 0 ? PM : 1];
             {
                 const float2 e3 = fte_expm_ff(ff_split(2 * tw * wp.h * py), etab);
                 float2 ey = make_float2(1.f, 0.f);
-                for (int j = 0; j < P1; j++) {
-                    wyb[j] = ff_mul(e1[j], ey);
-                    ey = ff_mul(ey, e3);
+                if constexpr (PM > 0) {
+#pragma unroll
+                    for (int j = 0; j < PM; j++) {
+                        wy[j] = j < P1 ? ff_mul(e1[j], ey) : make_float2(0.f, 0.f);
+                        ey = ff_mul(ey, e3);
+                    }
+                } else {
+                    for (int j = 0; j < P1; j++) {
+                        wyb[j] = ff_mul(e1[j], ey);
+                        ey = ff_mul(ey, e3);
+                    }
                 }
             }
             const float2 e3x = fte_expm_ff(ff_split(2 * tw * wp.h * px), etab);
@@ -1552,18 +1605,39 @@ __global__ void __launch_bounds__(kTileThreads) k_gather_ff(const double* __rest
                 if (inside) {
                     const float2* g0 = r0 + (lx + a) * W + ly;
                     const float2* g1 = r1 + (lx + a) * W + ly;
-                    for (int j = 0; j < P1; j++) {
-                        const float2 w = wyb[j];
-                        ff_mac(w, g0[j], s0, t0);
-                        ff_mac(w, g1[j], s1, t1);
+                    if constexpr (PM > 0) {
+#pragma unroll
+                        for (int j = 0; j < PM; j++) {
+                            if (j < P1) {
+                                ff_mac(wy[j], g0[j], s0, t0);
+                                ff_mac(wy[j], g1[j], s1, t1);
+                            }
+                        }
+                    } else {
+                        for (int j = 0; j < P1; j++) {
+                            const float2 w = wyb[j];
+                            ff_mac(w, g0[j], s0, t0);
+                            ff_mac(w, g1[j], s1, t1);
+                        }
                     }
                 } else {
                     const size_t base = (size_t)fte_wrap_index(mx + a, wp.Mx) * wp.My;
-                    for (int j = 0; j < P1; j++) {
-                        const size_t at = base + fte_wrap_index(my + j, wp.My);
-                        const float2 w = wyb[j];
-                        ff_mac(w, G0[at], s0, t0);
-                        ff_mac(w, G1[at], s1, t1);
+                    if constexpr (PM > 0) {
+#pragma unroll
+                        for (int j = 0; j < PM; j++) {
+                            if (j < P1) {
+                                const size_t at = base + fte_wrap_index(my + j, wp.My);
+                                ff_mac(wy[j], G0[at], s0, t0);
+                                ff_mac(wy[j], G1[at], s1, t1);
+                            }
+                        }
+                    } else {
+                        for (int j = 0; j < P1; j++) {
+                            const size_t at = base + fte_wrap_index(my + j, wp.My);
+                            const float2 w = wyb[j];
+                            ff_mac(w, G0[at], s0, t0);
+                            ff_mac(w, G1[at], s1, t1);
+                        }
                     }
                 }
                 ff_mac(wxa, ff_norm(s0, t0), a0, c0);
@@ -1574,9 +1648,13 @@ __global__ void __launch_bounds__(kTileThreads) k_gather_ff(const double* __rest
     }
 }
 
+// the register form's support bound for window support P1 (0: none fits)
+__host__ __device__ inline int gather_ff_pm(int P1) { return P1 <= 16 ? 16 : (P1 <= 24 ? 24 : (P1 <= 32 ? 32 : 0)); }
+
 size_t gather_ff_smem(int ts, int P) {
     const int P1 = P + 1, W = tile_region(ts, P);
-    return 2 * (size_t)W * W * sizeof(float2) + (size_t)(((P1 + 1) & ~1) + kTileThreads * P1) * sizeof(float2);
+    const size_t rows = gather_ff_pm(P1) ? 0 : (size_t)kTileThreads * P1;  // per-thread window columns
+    return 2 * (size_t)W * W * sizeof(float2) + (size_t)(((P1 + 1) & ~1) + rows) * sizeof(float2);
 }
 
 // ---- tile sizes -------------------------------------------------------------
@@ -1588,10 +1666,10 @@ size_t gather64_smem(int ts, int P) {
     const int P1 = P + 1, W = tile_region(ts, P);
     return 2 * (size_t)W * W * sizeof(double) + (size_t)(((P1 + 1) & ~1) + kPtThreads * P1) * sizeof(double);
 }
-bool spread_fits(const fte_context* ctx, int form, int ts, int P) {
+bool spread_fits(const fte_context* ctx, int form, int kind, int ts, int P) {
     if (ts < 8 || ts > 256) return false;
     size_t sm = form == FTE_FORM_MIXED ? spread_cols32_smem(ts, P)
-                : (form == FTE_FORM_FF ? spread_ff_smem(ts, P) : spread_cols_smem(ts, P));
+                : (form == FTE_FORM_FF ? spread_ff_smem(ts, P, kind == FTE_KIND_SLP ? 2 : 3) : spread_cols_smem(ts, P));
     return sm <= tile_budget(ctx);
 }
 bool gather_fits(const fte_context* ctx, int form, int ts, int P) {
@@ -1604,14 +1682,14 @@ int resolve_tiles(const fte_context* ctx, const KspaceArgs& a, int* ts_s, int* t
     *ts_s = 0;
     *ts_g = 0;
     if (a.ts_spread > 0) {
-        if (!spread_fits(ctx, a.form, a.ts_spread, a.P)) {
+        if (!spread_fits(ctx, a.form, a.kind, a.ts_spread, a.P)) {
             fte_set_error("spread tile %d does not fit shared memory at P=%d", a.ts_spread, a.P);
             return FTE_ERR_INVALID;
         }
         *ts_s = a.ts_spread;
     } else {
         for (int ts = 64; ts >= 8 && !*ts_s; ts -= 4)
-            if (spread_fits(ctx, a.form, ts, a.P)) *ts_s = ts;
+            if (spread_fits(ctx, a.form, a.kind, ts, a.P)) *ts_s = ts;
     }
     if (a.ts_gather > 0) {
         if (!gather_fits(ctx, a.form, a.ts_gather, a.P)) {
@@ -1619,6 +1697,14 @@ int resolve_tiles(const fte_context* ctx, const KspaceArgs& a, int* ts_s, int* t
             return FTE_ERR_INVALID;
         }
         *ts_g = a.ts_gather;
+    } else if (a.form == FTE_FORM_FF && gather_ff_pm(a.P + 1)) {
+        // register form: tiles small enough for four CTAs per SM (more warps
+        // to hide the products' latency; the region re-reads cost little),
+        // at most 28 nodes a side (fewer idle threads in a tile's last round
+        // of targets; 28 was the fastest of 24..48 at 1e6 points)
+        for (int ts = 28; ts >= 8 && !*ts_g; ts -= 4)
+            if (gather_ff_smem(ts, a.P) <= tile_budget(ctx) / 2) *ts_g = ts;
+        if (!*ts_g) *ts_g = 8;
     } else {
         for (int ts = 64; ts >= 8 && !*ts_g; ts -= 4)
             if (gather_fits(ctx, a.form, ts, a.P)) *ts_g = ts;
@@ -1656,14 +1742,22 @@ int launch_spread_tiled(fte_context* ctx, const KspaceArgs& a, const TileBins& t
             fte_set_error("internal: float-float spread without window records");
             return FTE_ERR_INVALID;
         }
+        // one pass over the sources: the Stokeslet's two grids or the
+        // stresslet's three symmetric ones
         double* Hd = static_cast<double*>(H);
-        const size_t smf = spread_ff_smem(tb.ts, a.P);
+        const int ngf = a.kind == FTE_KIND_SLP ? 2 : 3;
+        const size_t smf = spread_ff_smem(tb.ts, a.P, ngf);
         FTE_LAUNCH(ctx, k_ff_win, ew_grid(ctx, a.nsrc), 256, 0, a.kind, a.psrc, a.f, a.nrm, a.wts, (const int*)tb.perm,
                    a.nsrc, wp, recs);
-        FTE_CUDA_TRY(cudaFuncSetAttribute(k_spread_ff, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smf));
-        for (int pass = 0; pass < ng / 2; pass++)
-            FTE_LAUNCH(ctx, k_spread_ff, grid, kColThreads, smf, pass, (const FfWin*)recs, (const int*)tb.off, tb.ts,
-                       tb.ntx, tb.nty, wp, Hd + 2 * pass * G, Hd + (2 * pass + 1) * G);
+        if (ngf == 2) {
+            FTE_CUDA_TRY(cudaFuncSetAttribute(k_spread_ff<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smf));
+            FTE_LAUNCH(ctx, k_spread_ff<2>, grid, kColThreads, smf, (const FfWin*)recs, (const int*)tb.off, tb.ts,
+                       tb.ntx, tb.nty, wp, Hd, Hd + G, nullptr);
+        } else {
+            FTE_CUDA_TRY(cudaFuncSetAttribute(k_spread_ff<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smf));
+            FTE_LAUNCH(ctx, k_spread_ff<3>, grid, kColThreads, smf, (const FfWin*)recs, (const int*)tb.off, tb.ts,
+                       tb.ntx, tb.nty, wp, Hd, Hd + G, Hd + 2 * G);
+        }
     } else if (f32) {
         float* Hf = static_cast<float*>(H);
         FTE_CUDA_TRY(cudaFuncSetAttribute(k_spread_cols32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
@@ -1696,9 +1790,18 @@ int launch_gather_tiled(fte_context* ctx, const KspaceArgs& a, const TileBins& t
     if (a.form == FTE_FORM_FF) {
         const float2* Hf = static_cast<const float2*>(H);
         size_t sm = gather_ff_smem(tb.ts, a.P);
-        FTE_CUDA_TRY(cudaFuncSetAttribute(k_gather_ff, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        FTE_LAUNCH(ctx, k_gather_ff, grid, kTileThreads, sm, a.ptar, (const int*)tb.off, (const int*)tb.perm, tb.ts,
-                   tb.ntx, tb.nty, wp, Hf, Hf + G, scale, a.uk);
+        auto go = [&](auto kern) -> int {
+            FTE_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+            FTE_LAUNCH(ctx, kern, grid, kTileThreads, sm, a.ptar, (const int*)tb.off, (const int*)tb.perm, tb.ts,
+                       tb.ntx, tb.nty, wp, Hf, Hf + G, scale, a.uk);
+            return FTE_OK;
+        };
+        switch (gather_ff_pm(a.P + 1)) {
+            case 16: FTE_TRY(go(k_gather_ff<16>)); break;
+            case 24: FTE_TRY(go(k_gather_ff<24>)); break;
+            case 32: FTE_TRY(go(k_gather_ff<32>)); break;
+            default: FTE_TRY(go(k_gather_ff<0>)); break;
+        }
     } else if (a.form == FTE_FORM_MIXED) {
         const float* Hf = static_cast<const float*>(H);
         size_t sm = gather32_smem(tb.ts, a.P);
@@ -1834,7 +1937,7 @@ int fte_kspace_tune(fte_context* ctx, void* grid, WsCarver bins, KspaceArgs& a, 
     float best_s = 1e30f, best_g = 1e30f;
     int ts_s = 0, ts_g = 0;
     for (int ts : cand) {
-        if (rc || a.nsrc == 0 || !spread_fits(ctx, a.form, ts, a.P)) continue;
+        if (rc || a.nsrc == 0 || !spread_fits(ctx, a.form, a.kind, ts, a.P)) continue;
         WsCarver w = bins;
         TileBins tb;
         rc = fte_tiles_build(ctx, w, a.psrc, a.nsrc, a.Lx, a.Ly, wp.h, ts, (a.Mx + ts - 1) / ts,
@@ -1973,8 +2076,11 @@ int fte_kspace_run(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, fte_info
     FfWin* recs = ff && a.nsrc > 0 && ts_s > 0 ? wc.take<FfWin>(a.nsrc) : nullptr;
     FTE_WS_CHECK(wc);
 
+    // grids spread: the stresslet's tiled float-float spread writes its
+    // three symmetric products (S12 + S21 as one grid)
+    const int ngs = ff && a.kind == FTE_KIND_DLP && ts_s > 0 ? 3 : ng;
     FTE_TRY(fte_record(ctx, 2));
-    FTE_CUDA_TRY(cudaMemsetAsync(H, 0, sizeof(double) * ng * G, ctx->stream));
+    FTE_CUDA_TRY(cudaMemsetAsync(H, 0, sizeof(double) * ngs * G, ctx->stream));
     if (a.nsrc > 0 && ts_s > 0) {
         FTE_TRY(launch_spread_tiled(ctx, a, tb_s, wp, H, recs));
     } else if (a.nsrc > 0) {
@@ -1997,8 +2103,8 @@ int fte_kspace_run(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, fte_info
         FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_y_r2c_ff, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_y));
         FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_y_c2r_ff, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_y));
         FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_x_ff, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_x));
-        FTE_LAUNCH(ctx, k_fft_y_r2c_ff, dim3(Mx / 2, ng), fft_threads(py.m), sm_y, (const double*)H, Hf, Mx, My, py);
-        FTE_LAUNCH(ctx, k_fft_x_ff, dim3(Kh, ng), fft_threads(px.m), sm_x, Hf, Mx, Kh, px, 0);
+        FTE_LAUNCH(ctx, k_fft_y_r2c_ff, dim3(Mx / 2, ngs), fft_threads(py.m), sm_y, (const double*)H, Hf, Mx, My, py);
+        FTE_LAUNCH(ctx, k_fft_x_ff, dim3(Kh, ngs), fft_threads(px.m), sm_x, Hf, Mx, Kh, px, 0);
         int fb = (int)(((size_t)Mx * Kh + 255) / 256);
         if (fb > ctx->num_sms * 32) fb = ctx->num_sms * 32;
         // the multipliers in float-float while (1 - eta) K / (4 xi^2) stays
@@ -2008,13 +2114,13 @@ int fte_kspace_run(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, fte_info
         if (xext < 75.0) {
             const FfFilt ffc = ff_filter_consts(a.Lx, a.Ly, a.xi, a.eta);
             if (a.kind == FTE_KIND_SLP)
-                FTE_LAUNCH(ctx, k_filter_ff<FTE_KIND_SLP>, fb, 256, 0, Hf, Mx, My, ffc);
+                FTE_LAUNCH(ctx, k_filter_ff<FTE_KIND_SLP>, fb, 256, 0, Hf, Mx, My, ffc, ngs);
             else
-                FTE_LAUNCH(ctx, k_filter_ff<FTE_KIND_DLP>, fb, 256, 0, Hf, Mx, My, ffc);
+                FTE_LAUNCH(ctx, k_filter_ff<FTE_KIND_DLP>, fb, 256, 0, Hf, Mx, My, ffc, ngs);
         } else if (a.kind == FTE_KIND_SLP) {
-            FTE_LAUNCH(ctx, (k_filter<FTE_KIND_SLP, float4>), fb, 256, 0, Hf, Mx, My, a.Lx, a.Ly, a.xi, a.eta);
+            FTE_LAUNCH(ctx, (k_filter<FTE_KIND_SLP, float4>), fb, 256, 0, Hf, Mx, My, a.Lx, a.Ly, a.xi, a.eta, ngs);
         } else {
-            FTE_LAUNCH(ctx, (k_filter<FTE_KIND_DLP, float4>), fb, 256, 0, Hf, Mx, My, a.Lx, a.Ly, a.xi, a.eta);
+            FTE_LAUNCH(ctx, (k_filter<FTE_KIND_DLP, float4>), fb, 256, 0, Hf, Mx, My, a.Lx, a.Ly, a.xi, a.eta, ngs);
         }
         FTE_LAUNCH(ctx, k_fft_x_ff, dim3(Kh, 2), fft_threads(px.m), sm_x, Hf, Mx, Kh, px, 1);
         FTE_LAUNCH(ctx, k_fft_y_c2r_ff, dim3(Mx / 2, 2), fft_threads(py.m), sm_y, (const float4*)Hf,
@@ -2037,26 +2143,26 @@ int fte_kspace_run(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, fte_info
     if (!long_y) {
         FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_y_r2c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_y));
         FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_y_c2r, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_y));
-        FTE_LAUNCH(ctx, k_fft_y_r2c, dim3(Mx / 2, ng), fft_threads(py.m), sm_y, (const double*)H, Hh, Mx, My, py);
+        FTE_LAUNCH(ctx, k_fft_y_r2c, dim3(Mx / 2, ngs), fft_threads(py.m), sm_y, (const double*)H, Hh, Mx, My, py);
     } else {
-        const long long tot = (long long)ng * (Mx / 2) * My;
-        FTE_LAUNCH(ctx, k_ly_pack_r2c, ew_grid(ctx, tot), 256, 0, (const double*)H, S, Mx, My, ng);
-        FTE_TRY(fte_long_fft(ctx, ly, S, rows, (long long)ng * (Mx / 2), false, LS));
-        FTE_LAUNCH(ctx, k_ly_unpack_r2c, ew_grid(ctx, (long long)ng * (Mx / 2) * Kh), 256, 0, (const double2*)S, Hh,
-                   Mx, My, ng);
+        const long long tot = (long long)ngs * (Mx / 2) * My;
+        FTE_LAUNCH(ctx, k_ly_pack_r2c, ew_grid(ctx, tot), 256, 0, (const double*)H, S, Mx, My, ngs);
+        FTE_TRY(fte_long_fft(ctx, ly, S, rows, (long long)ngs * (Mx / 2), false, LS));
+        FTE_LAUNCH(ctx, k_ly_unpack_r2c, ew_grid(ctx, (long long)ngs * (Mx / 2) * Kh), 256, 0, (const double2*)S, Hh,
+                   Mx, My, ngs);
     }
     if (!long_x) {
         FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_x));
-        FTE_LAUNCH(ctx, k_fft_x, dim3(Kh, ng), fft_threads(px.m), sm_x, Hh, Mx, Kh, px, 0);
+        FTE_LAUNCH(ctx, k_fft_x, dim3(Kh, ngs), fft_threads(px.m), sm_x, Hh, Mx, Kh, px, 0);
     } else {
-        FTE_TRY(fte_long_fft(ctx, lx, Hh, cols, (long long)ng * Kh, false, LS));
+        FTE_TRY(fte_long_fft(ctx, lx, Hh, cols, (long long)ngs * Kh, false, LS));
     }
     int fb = (int)(((size_t)Mx * Kh + 255) / 256);
     if (fb > ctx->num_sms * 32) fb = ctx->num_sms * 32;
     if (a.kind == FTE_KIND_SLP)
-        FTE_LAUNCH(ctx, (k_filter<FTE_KIND_SLP, double2>), fb, 256, 0, Hh, Mx, My, a.Lx, a.Ly, a.xi, a.eta);
+        FTE_LAUNCH(ctx, (k_filter<FTE_KIND_SLP, double2>), fb, 256, 0, Hh, Mx, My, a.Lx, a.Ly, a.xi, a.eta, ngs);
     else
-        FTE_LAUNCH(ctx, (k_filter<FTE_KIND_DLP, double2>), fb, 256, 0, Hh, Mx, My, a.Lx, a.Ly, a.xi, a.eta);
+        FTE_LAUNCH(ctx, (k_filter<FTE_KIND_DLP, double2>), fb, 256, 0, Hh, Mx, My, a.Lx, a.Ly, a.xi, a.eta, ngs);
     if (!long_x)
         FTE_LAUNCH(ctx, k_fft_x, dim3(Kh, 2), fft_threads(px.m), sm_x, Hh, Mx, Kh, px, 1);
     else
@@ -2533,7 +2639,7 @@ extern "C" int fte_slp_kspace_noalloc(const double* psrc, int64_t nsrc, const do
     NA_LAUNCH(k_fft_y_r2c, dim3(Mx / 2, 2), fft_threads(py.m), sm_y, stream, (const double*)H, Hh, Mx, My, py);
     NA_LAUNCH(k_fft_x, dim3(Kh, 2), fft_threads(px.m), sm_x, stream, Hh, Mx, Kh, px, 0);
     int fb = (int)(((size_t)Mx * Kh + 255) / 256);
-    NA_LAUNCH((k_filter<FTE_KIND_SLP, double2>), fb, 256, 0, stream, Hh, Mx, My, Lx, Ly, xi, eta);
+    NA_LAUNCH((k_filter<FTE_KIND_SLP, double2>), fb, 256, 0, stream, Hh, Mx, My, Lx, Ly, xi, eta, 2);
     NA_LAUNCH(k_fft_x, dim3(Kh, 2), fft_threads(px.m), sm_x, stream, Hh, Mx, Kh, px, 1);
     NA_LAUNCH(k_fft_y_c2r, dim3(Mx / 2, 2), fft_threads(py.m), sm_y, stream, (const double2*)Hh, H, Mx, My, py);
     double s = 4 * xi * xi / eta;

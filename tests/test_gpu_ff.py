@@ -66,6 +66,23 @@ def test_ff_kspace_matches_fp64(gpu_ctx, kind, geom):
     assert np.max(np.abs(out_f[2] - out_d[2])) <= 1e-10 * np.max(np.abs(out_d[2]))
 
 
+@pytest.mark.parametrize("kind", ["slp", "dlp"])
+@pytest.mark.parametrize("P", [12, 16, 24, 32])
+def test_ff_gather_supports(gpu_ctx, kind, P):
+    """Window supports on either side of the gather's register bounds (16, 24
+    and 32 nodes) and beyond them (the shared-memory form)."""
+    ft = _ft()
+    Lx, Ly = 1.0, 1.5
+    d = _case(60 + P, 6000, Lx, Ly)
+    out_f, info_f = _run(ft, gpu_ctx, kind, d, Lx, Ly, tol=1e-10, kspace=ft.KSPACE_FF, P=P)
+    p = info_f.params
+    assert p.form == ft.FORM_FF and p.P == P
+    same = dict(P=p.P, xi=p.xi, Mx=p.Mx, My=p.My, nside_x=p.nside_x, nside_y=p.nside_y)
+    out_d, _ = _run(ft, gpu_ctx, kind, d, Lx, Ly, tol=1e-10, kspace=ft.KSPACE_FP64, **same)
+    rel = np.max(np.abs(out_f[3] - out_d[3])) / np.max(np.abs(out_d[3]))
+    assert rel <= 2e-12, rel
+
+
 @pytest.mark.parametrize("tol", [1e-9, 1e-11])
 @pytest.mark.parametrize("geom", [(20000, 1.0, 1.0, 51), (12000, 3.75, 1.0, 52)])
 def test_ff_chosen_and_meets_tolerance(gpu_ctx, tol, geom):
