@@ -743,15 +743,16 @@ void pick_grid(int A, int B, int kinf, int* Mx, int* My) {
 // per-pair + per-box terms (the box term is the staging of each 3x3
 // neighbourhood and the drain of the pair queues at each box's end), spread
 // + gather per window node and grid, transforms per unit of fft_work.
-static const double kCostTarget = 0.6e-9;      // near field, per target
-static const double kCostPair = 14e-12;        // per pair within the cutoff (float-float / FP32 classes)
+static const double kCostTarget = 0.3e-9;      // near field, per target
+static const double kCostPair = 15e-12;        // per pair within the cutoff (float-float / FP32 classes)
 static const double kCostPair64 = 40e-12;      // same with FP64 pairs (tolerances below 1e-11)
-static const double kCostBox = 40e-9;          // per box of the cell list
+static const double kCostBox = 30e-9;          // per box of the cell list
 static const double kCostWin64 = 3.2e-12;      // one window node x grid, FP64 spread/gather
 static const double kCostWin32 = 2.5e-12;      // same in FP32 (an exponential per node)
-static const double kCostWinFF = 1.7e-12;      // same in float-float (FP32 pipe), window records included
+static const double kCostWinFF = 1.31e-12;     // same in float-float (FP32 pipe), window records included
+static const double kCostGridFF = 16e-12;      // float-float: per grid node x grid (tile staging, flushes)
 static const double kCostFft64 = 9e-12;        // per unit of fft_work, 7-smooth FP64 block transforms
-static const double kCostFftFF = 4.5e-12;      // same in float-float
+static const double kCostFftFF = 2.95e-12;     // same in float-float (filter included)
 static const double kCostFft32 = 3e-12;        // same in FP32
 // Calibration of the tuned choice against converged FP64 sums on 2000
 // generated configurations (uniform and clustered points, aspect 1..4,
@@ -819,6 +820,10 @@ static int choose_params_tuned(int kind, int64_t nsrc, int64_t ntar, double Q, d
         const double pairs = (double)nsrc * (double)ntar * FTE_PI * rc * rc / area * 1.03;
         const double win = (double)(P + 1) * (P + 1) * ((double)nsrc * ng + (double)ntar * 2);
         const double fftw = fft_work(Mx, My) * nfft;
+        // the float-float stresslet spreads and transforms three grids
+        // (the symmetric products), not four
+        const double winff = kind == FTE_KIND_SLP ? win : (double)(P + 1) * (P + 1) * ((double)nsrc * 3 + (double)ntar * 2);
+        const double fftwff = kind == FTE_KIND_SLP ? fftw : fft_work(Mx, My) * 2.5;
         const double near = kCostTarget * (double)ntar + (ffok ? kCostPair : kCostPair64) * pairs +
                             kCostBox * (double)nsx * (double)nsy;
         int kf = -1;
@@ -834,7 +839,8 @@ static int choose_params_tuned(int kind, int64_t nsrc, int64_t ntar, double Q, d
             if (f == FTE_FORM_MIXED)
                 c = kCostWin32 * win + kCostFft32 * fftw;
             else if (f == FTE_FORM_FF)
-                c = kCostWinFF * win + (long64 ? 2.5 * kCostFft64 : kCostFftFF) * fftw;
+                c = kCostWinFF * winff + kCostGridFF * (double)Mx * My * (kind == FTE_KIND_SLP ? 4 : 5) +
+                    (long64 ? 2.5 * kCostFft64 : kCostFftFF) * fftwff;
             else
                 c = kCostWin64 * win + (long64 ? 2.5 : 1.0) * kCostFft64 * fftw;
             if (c < cost) {
