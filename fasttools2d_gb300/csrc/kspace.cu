@@ -531,7 +531,9 @@ __global__ void k_fft_y_c2r(const double2* __restrict__ Hh, double* __restrict__
 }
 
 // ---- the same three transforms in float-float (FFT lines of FfCx) --------------
-__global__ void k_fft_y_r2c_ff(const double* __restrict__ H, float4* __restrict__ Hh, int Mx, int My, FftDev plan) {
+// (two CTAs of up to 512 threads per SM: registers capped at 64 so that a
+// second line's transform hides the first's barrier and load latency)
+__global__ void __launch_bounds__(512, 2) k_fft_y_r2c_ff(const double* __restrict__ H, float4* __restrict__ Hh, int Mx, int My, FftDev plan) {
     extern __shared__ __align__(16) unsigned char shff[];
     float4* A = reinterpret_cast<float4*>(shff);
     float4* B = A + plan.m;
@@ -552,7 +554,7 @@ __global__ void k_fft_y_r2c_ff(const double* __restrict__ H, float4* __restrict_
     }
 }
 
-__global__ void k_fft_x_ff(float4* __restrict__ Hh, int Mx, int Kh, FftDev plan, int inv) {
+__global__ void __launch_bounds__(512, 2) k_fft_x_ff(float4* __restrict__ Hh, int Mx, int Kh, FftDev plan, int inv) {
     extern __shared__ __align__(16) unsigned char shff[];
     float4* A = reinterpret_cast<float4*>(shff);
     float4* B = A + plan.m;
@@ -564,7 +566,7 @@ __global__ void k_fft_x_ff(float4* __restrict__ Hh, int Mx, int Kh, FftDev plan,
 }
 
 // half spectra -> real grids as float-float pairs (the gather's input)
-__global__ void k_fft_y_c2r_ff(const float4* __restrict__ Hh, float2* __restrict__ H, int Mx, int My, FftDev plan) {
+__global__ void __launch_bounds__(512, 2) k_fft_y_c2r_ff(const float4* __restrict__ Hh, float2* __restrict__ H, int Mx, int My, FftDev plan) {
     extern __shared__ __align__(16) unsigned char shff[];
     float4* A = reinterpret_cast<float4*>(shff);
     float4* B = A + plan.m;
@@ -1543,7 +1545,7 @@ __global__ void k_ff_join(double* __restrict__ H, int64_t n) {
 // shared-memory traffic for the weights); PM == 0: any support, the window
 // column in a per-thread shared-memory row.
 template <int PM>
-__global__ void __launch_bounds__(kTileThreads) k_gather_ff(const double* __restrict__ p, const int* __restrict__ toff,
+__global__ void __launch_bounds__(kTileThreads, 5) k_gather_ff(const double* __restrict__ p, const int* __restrict__ toff,
                                                            const int* __restrict__ perm, int ts, int ntx, int nty,
                                                            WinParams wp, const float2* __restrict__ G0,
                                                            const float2* __restrict__ G1, double scale,

@@ -39,9 +39,9 @@ template <bool L>
 struct NearCfg {
     static constexpr int threads = L ? 128 : 256;
     static constexpr int warps = threads / 32;
-    static constexpr int ctas = L ? 4 : 2;          // per SM
+    static constexpr int ctas = L ? 5 : 2;          // per SM
     static constexpr int grid_per_sm = L ? 32 : 16;  // grid-stride launch size
-    static constexpr size_t budget = L ? 54 * 1024 : 110 * 1024;
+    static constexpr size_t budget = L ? 44 * 1024 : 110 * 1024;
 };
 constexpr int kQueue = 64;
 constexpr int kGtab = FTE_E1_NPIECE_G * (FTE_E1_DEG_G + 1);
