@@ -744,15 +744,15 @@ void pick_grid(int A, int B, int kinf, int* Mx, int* My) {
 // neighbourhood and the drain of the pair queues at each box's end), spread
 // + gather per window node and grid, transforms per unit of fft_work.
 static const double kCostTarget = 0.3e-9;      // near field, per target
-static const double kCostPair = 15e-12;        // per pair within the cutoff (float-float / FP32 classes)
+static const double kCostPair = 14e-12;        // per pair within the cutoff (float-float / FP32 classes)
 static const double kCostPair64 = 40e-12;      // same with FP64 pairs (tolerances below 1e-11)
-static const double kCostBox = 30e-9;          // per box of the cell list
+static const double kCostBox = 28e-9;          // per box of the cell list
 static const double kCostWin64 = 3.2e-12;      // one window node x grid, FP64 spread/gather
 static const double kCostWin32 = 2.5e-12;      // same in FP32 (an exponential per node)
 static const double kCostWinFF = 1.31e-12;     // same in float-float (FP32 pipe), window records included
 static const double kCostGridFF = 16e-12;      // float-float: per grid node x grid (tile staging, flushes)
 static const double kCostFft64 = 9e-12;        // per unit of fft_work, 7-smooth FP64 block transforms
-static const double kCostFftFF = 2.95e-12;     // same in float-float (filter included)
+static const double kCostFftFF = 2.3e-12;      // same in float-float (filter included)
 static const double kCostFft32 = 3e-12;        // same in FP32
 // Calibration of the tuned choice against converged FP64 sums on 2000
 // generated configurations (uniform and clustered points, aspect 1..4,

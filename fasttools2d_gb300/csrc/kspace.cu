@@ -1690,6 +1690,14 @@ int resolve_tiles(const fte_context* ctx, const KspaceArgs& a, int* ts_s, int* t
         }
         *ts_s = a.ts_spread;
     } else {
+        // float-float: three CTAs per SM where that still leaves tiles of at
+        // least 28 nodes a side (else the halo flushes cost more than the
+        // occupancy gains: measured at 1e6 points, P 14..22)
+        if (a.form == FTE_FORM_FF) {
+            const int ngf = a.kind == FTE_KIND_SLP ? 2 : 3;
+            for (int ts = 64; ts >= 28 && !*ts_s; ts -= 4)
+                if (spread_ff_smem(ts, a.P, ngf) <= tile_budget(ctx) * 2 / 3) *ts_s = ts;
+        }
         for (int ts = 64; ts >= 8 && !*ts_s; ts -= 4)
             if (spread_fits(ctx, a.form, a.kind, ts, a.P)) *ts_s = ts;
     }
