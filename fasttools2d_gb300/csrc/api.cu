@@ -629,29 +629,31 @@ static int choose_params_q(int kind, int64_t nsrc, int64_t ntar, double Q, doubl
 // ---------------------------------------------------------------------------
 namespace {
 
-double xi_estimate(int kind, double Q, double Lx, double Ly, double rc, double tol) {
+// x0, k0 > 0: start the Newton iteration there instead of the drivers' start
+// (the tuned chooser starts each candidate from the previous one's root)
+double xi_estimate(int kind, double Q, double Lx, double Ly, double rc, double tol, double x0 = 0) {
     if (kind == FTE_KIND_SLP)
         return newton(
-            4 / rc, tol,
+            x0 > 0 ? x0 : 4 / rc, tol,
             [&](double x) { return std::sqrt(Q * FTE_PI / (4 * Lx * Ly * x)) * std::exp(-x * x * rc * rc) - tol; },
             [&](double x) {
                 return -std::sqrt(Q * FTE_PI / (4 * Lx * Ly)) * std::exp(-x * x * rc * rc) *
                        (0.5 * std::pow(x, -1.5) + 2 * rc * rc * x * std::sqrt(1 / x));
             });
     return newton(
-        1 / rc, tol,
+        x0 > 0 ? x0 : 1 / rc, tol,
         [&](double x) { return std::exp(-x * x * rc * rc) * x * rc * std::sqrt(2 * FTE_PI * Q / (Lx * Ly)) - tol; },
         [&](double x) {
             return (1 - 2 * x * x * rc * rc) * std::exp(-x * x * rc * rc) * std::sqrt(2 * FTE_PI * Q / (Lx * Ly)) * rc;
         });
 }
 
-int kinf_estimate(int kind, double Q, double Lx, double xi, double tol) {
+double kinf_root(int kind, double Q, double Lx, double xi, double tol, double k0 = 0) {
     const double L1 = Lx;
     double k;
     if (kind == FTE_KIND_SLP)
         k = newton(
-            std::round(5 * xi), tol,
+            k0 > 0 ? k0 : std::round(5 * xi), tol,
             [&](double k) {
                 return std::sqrt(4 * Q * FTE_PI * L1 / (std::pow(L1, 6) * k)) * std::exp(-k * k / (4 * xi * xi)) - tol;
             },
@@ -661,13 +663,16 @@ int kinf_estimate(int kind, double Q, double Lx, double xi, double tol) {
             });
     else
         k = newton(
-            std::round(5 * xi), tol,
+            k0 > 0 ? k0 : std::round(5 * xi), tol,
             [&](double k) { return std::sqrt(k * 8 * FTE_PI * Q * L1) * std::exp(-k * k / (4 * xi * xi)) - tol; },
             [&](double k) {
                 return std::sqrt(8 * FTE_PI * Q * L1) * std::exp(-k * k / (4 * xi * xi)) *
                        (0.5 * std::pow(k, -0.5) - 2 * std::pow(k, 1.5) / (4 * xi * xi));
             });
-    return (int)std::round(Lx * k / (2 * FTE_PI));
+    return k;
+}
+int kinf_estimate(int kind, double Q, double Lx, double xi, double tol) {
+    return (int)std::round(Lx * kinf_root(kind, Q, Lx, xi, tol) / (2 * FTE_PI));
 }
 
 int next_smooth_even(int n) {
@@ -698,13 +703,24 @@ double smooth_line_cost(int n) {
     const int c8 = c2 / 3, r2 = c2 - 3 * c8;
     return 9.0 * c8 + (r2 == 2 ? 7.0 : (r2 == 1 ? 5.0 : 0.0)) + 8.0 * c3 + 11.0 * c5 + 13.0 * c7;
 }
-double line_cost(int n) {
+double line_cost_direct(int n) {
     const double c = smooth_line_cost(n);
     if (c >= 0) return c;
     // Bluestein: two transforms of a smooth length near 2n plus the chirp
     // products, per point of n (estimated without searching the length)
     const double m = 2.2 * n;
     return (2 * 3.4 * std::log2(m) + 12) * m / n;
+}
+// line_cost for lengths below 32768 from a table built once per process (the
+// tuned chooser evaluates it ~10^4 times per call while the GPU waits)
+double line_cost(int n) {
+    constexpr int kMax = 32768;
+    static const std::vector<double> tab = [] {
+        std::vector<double> t(kMax);
+        for (int i = 1; i < kMax; i++) t[i] = line_cost_direct(i);
+        return t;
+    }();
+    return n > 0 && n < kMax ? tab[n] : line_cost_direct(n);
 }
 // 2-D transform work of an Mx x My grid in units that equal points x log2(points)
 // for power-of-two sides (about 3.1 operations per point and level)
@@ -796,6 +812,10 @@ static int choose_params_tuned(int kind, int64_t nsrc, int64_t ntar, double Q, d
     fte_params bestp = *o;
     int best_form = FTE_FORM_PLAIN;
     int last_a = -1;
+    // Newton roots of the previous candidate (warm starts: the estimates'
+    // roots scale about as 1 / rc and xi, and a cold start from the drivers'
+    // guess takes tens of iterations per candidate)
+    double prev_xr = 0, prev_k = 0, prev_xi = 0;
     for (int step = -12; step <= 40; step++) {
         int a = (int)std::lround(a0 * std::pow(1.1, step));
         if (opt && opt->nside_x > 0) a = opt->nside_x / A;
@@ -803,8 +823,14 @@ static int choose_params_tuned(int kind, int64_t nsrc, int64_t ntar, double Q, d
         last_a = a;
         int nsx = a * A, nsy = a * B;
         double rc = Lx / nsx;
-        double xi = (opt && opt->xi > 0) ? opt->xi : xi_estimate(kind, Q, Lx, Ly, rc, tol_e);
-        int kinf = kinf_estimate(kind, Q, Lx, xi, tol_e);
+        // (10 % below the scaled root: the iteration then enters the
+        // convergence band from the same side as from the drivers' start)
+        double xi = (opt && opt->xi > 0) ? opt->xi : xi_estimate(kind, Q, Lx, Ly, rc, tol_e, 0.9 * prev_xr / rc);
+        const double kr = kinf_root(kind, Q, Lx, xi, tol_e, prev_xi > 0 ? 0.9 * prev_k * xi / prev_xi : 0);
+        prev_xr = xi * rc;
+        prev_k = kr;
+        prev_xi = xi;
+        int kinf = (int)std::round(Lx * kr / (2 * FTE_PI));
         int Mx, My;
         pick_grid(A, B, kinf, &Mx, &My);
         if (opt && opt->Mx > 0) Mx = opt->Mx;
