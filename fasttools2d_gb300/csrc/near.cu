@@ -873,11 +873,23 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
             __syncwarp();
             int hs = 0, cs = 0;  // FP32-class ring head and count
 
+            // stresslet: the next batch's staged position is loaded one batch
+            // ahead (the ring stores in between would otherwise keep the load
+            // behind them; measured 3 % faster for the stresslet, 1 % slower
+            // for the Stokeslet, whose larger loop body hides the load)
+            constexpr bool ahead = KIND == FTE_KIND_DLP;
+            float2 qnext = ahead && lane < clen ? s32[lane] : make_float2(0.f, 0.f);
             for (int base = 0; base < clen; base += 32) {
                 int s = base + lane;
                 bool pass = false, small_x = false, single = false;
+                float2 q;
+                if constexpr (ahead) {
+                    q = qnext;
+                    if (s + 32 < clen) qnext = s32[s + 32];
+                } else {
+                    q = s < clen ? s32[s] : make_float2(0.f, 0.f);
+                }
                 if (s < clen) {
-                    float2 q = s32[s];
                     float dx = q.x - tx32, dy = q.y - ty32;
                     float r2f = dx * dx + dy * dy;
                     pass = (s < own_lim) || (r2f < prm.cut32);
@@ -905,24 +917,31 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
                 const int ent = (s << 2) | slot;
                 // the Stokeslet's pairs with x < 1 take ring qn (the series of
                 // E1); the stresslet has one pair formula
-                const bool split = KIND == FTE_KIND_SLP;
-                const bool pf_ = pass && !(split && small_x), pn_ = pass && split && small_x;
-                const unsigned mf = __ballot_sync(0xffffffffu, pf_);
-                const unsigned mn = __ballot_sync(0xffffffffu, pn_);
-                if (pf_) qf[(Pf + __popc(mf & lt_mask)) & (kQueue - 1)] = ent;
-                if (pn_) qn[(Pn + __popc(mn & lt_mask)) & (kQueue - 1)] = ent;
-                Pf += __popc(mf);
-                Pn += __popc(mn);
+                if constexpr (KIND == FTE_KIND_SLP) {
+                    const bool pf_ = pass && !small_x, pn_ = pass && small_x;
+                    const unsigned mf = __ballot_sync(0xffffffffu, pf_);
+                    const unsigned mn = __ballot_sync(0xffffffffu, pn_);
+                    if (pf_) qf[(Pf + __popc(mf & lt_mask)) & (kQueue - 1)] = ent;
+                    if (pn_) qn[(Pn + __popc(mn & lt_mask)) & (kQueue - 1)] = ent;
+                    Pf += __popc(mf);
+                    Pn += __popc(mn);
+                } else {
+                    const unsigned mf = __ballot_sync(0xffffffffu, pass);
+                    if (pass) qf[(Pf + __popc(mf & lt_mask)) & (kQueue - 1)] = ent;
+                    Pf += __popc(mf);
+                }
                 __syncwarp();
                 if (Pf - Ef >= 32) {
                     evalF(qf[(Ef + lane) & (kQueue - 1)]);
                     Ef += 32;
                     __syncwarp();
                 }
-                if (Pn - En >= 32) {
-                    evalN(qn[(En + lane) & (kQueue - 1)]);
-                    En += 32;
-                    __syncwarp();
+                if constexpr (KIND == FTE_KIND_SLP) {
+                    if (Pn - En >= 32) {
+                        evalN(qn[(En + lane) & (kQueue - 1)]);
+                        En += 32;
+                        __syncwarp();
+                    }
                 }
             }
             // the target's FP32 class: last partial batch, then its sums
