@@ -777,6 +777,12 @@ static const double kCostFft32 = 3e-12;        // same in FP32
 // needs no slack and one more window step (tol / 3000), and FP32 grids bottom
 // out near 2.5e-7 (Stokeslet) and 4e-8 (stresslet) relative.
 static const double kTolSlack[2] = {1.0, 3.0};
+// The k-space truncation of the Stokeslet estimate is an RMS figure for
+// spread-out sources: at targets on densely sampled boundaries (sources
+// 1e-3 apart on curves, config 2's ellipses in a 2 x 1 box) the max-norm
+// error reached 3x the tolerance at the estimate's kinf.  kinf is therefore
+// taken at the tolerance times this factor (the grid grows ~4 % per side).
+static const double kKinfSlack[2] = {0.1, 1.0};
 static const double kWinRatio[2] = {3000.0, 300.0};
 static const double kFp32Floor[2] = {1e-6, 2e-7};
 // float-float spread and gather (~48-bit values) hold their ~1e-13 relative
@@ -826,7 +832,8 @@ static int choose_params_tuned(int kind, int64_t nsrc, int64_t ntar, double Q, d
         // (10 % below the scaled root: the iteration then enters the
         // convergence band from the same side as from the drivers' start)
         double xi = (opt && opt->xi > 0) ? opt->xi : xi_estimate(kind, Q, Lx, Ly, rc, tol_e, 0.9 * prev_xr / rc);
-        const double kr = kinf_root(kind, Q, Lx, xi, tol_e, prev_xi > 0 ? 0.9 * prev_k * xi / prev_xi : 0);
+        const double kr =
+            kinf_root(kind, Q, Lx, xi, tol_e * kKinfSlack[kind], prev_xi > 0 ? 0.9 * prev_k * xi / prev_xi : 0);
         prev_xr = xi * rc;
         prev_k = kr;
         prev_xi = xi;
