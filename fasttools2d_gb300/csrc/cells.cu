@@ -19,9 +19,10 @@ constexpr int kScanTile = kScanThreads * kScanItems;
 
 __global__ void k_assign(const double* __restrict__ p, int64_t n, int nsx, int nsy, double Lx, double Ly,
                          int* __restrict__ box, int* __restrict__ rank, int* __restrict__ counts) {
+    const double rLx = __drcp_rn(Lx), rLy = __drcp_rn(Ly);
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         double x = p[2 * i], y = p[2 * i + 1];
-        int b = fte_cell_1d(y, Ly, nsy) * nsx + fte_cell_1d(x, Lx, nsx);
+        int b = fte_cell_1d(y, Ly, rLy, nsy) * nsx + fte_cell_1d(x, Lx, rLx, nsx);
         box[i] = b;
         rank[i] = atomicAdd(&counts[b], 1);
     }
@@ -113,10 +114,10 @@ __global__ void k_scatter_tar(const double* __restrict__ p, int64_t n, const int
 __global__ void k_tile_assign(const double* __restrict__ p, int64_t n, double Lx, double Ly, double h, int ts,
                               int ntx, int nty, int* __restrict__ tile, int* __restrict__ rank,
                               int* __restrict__ counts) {
-    const double lhx = __ddiv_rn(Lx, 2.0), lhy = __ddiv_rn(Ly, 2.0);
+    const double lhx = __dmul_rn(Lx, 0.5), lhy = __dmul_rn(Ly, 0.5), rh = __drcp_rn(h);
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        double ax = floor(__ddiv_rn(__dadd_rn(p[2 * i], lhx), h));
-        double ay = floor(__ddiv_rn(__dadd_rn(p[2 * i + 1], lhy), h));
+        double ax = floor(fte_div_rcp(__dadd_rn(p[2 * i], lhx), h, rh));
+        double ay = floor(fte_div_rcp(__dadd_rn(p[2 * i + 1], lhy), h, rh));
         ax = fmin(fmax(ax, 0.0), (double)(ntx * ts - 1));
         ay = fmin(fmax(ay, 0.0), (double)(nty * ts - 1));
         int tx = min((int)ax / ts, ntx - 1), ty = min((int)ay / ts, nty - 1);

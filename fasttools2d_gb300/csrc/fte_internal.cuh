@@ -180,18 +180,33 @@ double fte_elapsed(fte_context* ctx, int a, int b);
 // Device helpers shared by the kernels.
 // ---------------------------------------------------------------------------
 
+// x / d rounded to nearest from rd = RN(1/d): q = RN(x rd), the remainder
+// x - q d exactly by one FMA, and RN(q + (x - q d) rd), which is the IEEE
+// quotient for normal operands (P. Markstein, "Computation of elementary
+// functions on the IBM RISC System/6000 processor", IBM J. Res. Develop. 34,
+// 1990).  One multiply and two FMAs instead of a division: the per-point
+// kernels divide by a grid step, a cell side or a box length that is fixed
+// for the launch, and GB300 issues FP64 at 1/64 of its FP32 rate.
+__device__ __forceinline__ double fte_div_rcp(double x, double d, double rd) {
+    const double q = __dmul_rn(x, rd);
+    const double r = __fma_rn(-q, d, x);
+    return __fma_rn(r, rd, q);
+}
+
 // First window node (mx, my) and in-cell offsets (px, py) of a point: the
 // reference's FindClosestNode (PeriodicEwald/src/mex/common/ewald_tools.cpp:116-144).
 // Written with explicitly rounded operations so that no multiply-add is fused:
-// the tie-break below depends on the exact rounding of each step.
-__device__ __forceinline__ void fte_closest_node(double x, double y, double Lx, double Ly, double h, int P, int* mx,
-                                                 int* my, double* px, double* py) {
+// the tie-break below depends on the exact rounding of each step (the
+// quotients by h are the IEEE quotients, formed from rh = RN(1/h); halving
+// is exact).
+__device__ __forceinline__ void fte_closest_node(double x, double y, double Lx, double Ly, double h, double rh, int P,
+                                                 int* mx, int* my, double* px, double* py) {
     const double TOL = 1e-13;
-    double qx = __ddiv_rn(x, h), qy = __ddiv_rn(y, h);
+    double qx = fte_div_rcp(x, h, rh), qy = fte_div_rcp(y, h, rh);
     double ppx = __dsub_rn(x, __dmul_rn(h, floor(qx)));
     double ppy = __dsub_rn(y, __dmul_rn(h, floor(qy)));
-    double lhx = __ddiv_rn(Lx, 2.0), lhy = __ddiv_rn(Ly, 2.0);
-    double ax = __ddiv_rn(__dadd_rn(x, lhx), h), ay = __ddiv_rn(__dadd_rn(y, lhy), h);
+    double lhx = __dmul_rn(Lx, 0.5), lhy = __dmul_rn(Ly, 0.5);
+    double ax = fte_div_rcp(__dadd_rn(x, lhx), h, rh), ay = fte_div_rcp(__dadd_rn(y, lhy), h, rh);
     int half = P / 2;
     int ix = (int)__dsub_rn(floor(ax), (double)half);
     int iy = (int)__dsub_rn(floor(ay), (double)half);
@@ -205,6 +220,21 @@ __device__ __forceinline__ void fte_closest_node(double x, double y, double Lx, 
     *py = ppy;
 }
 
+// MATLAB mod(v + L/2, L) - L/2 with mod's round-off compensation
+// (StokesSLP_ewald_2p.m:75-78): exactly 0 when a/L is an integer to within
+// eps; rL = RN(1/L).
+__device__ __forceinline__ double fte_wrap_coord(double v, double L, double rL) {
+    const double hl = __dmul_rn(L, 0.5);
+    const double a = __dadd_rn(v, hl);
+    const double q = fte_div_rcp(a, L, rL);
+    double r;
+    if (fabs(__dsub_rn(q, round(q))) <= 2.220446049250313e-16 * fabs(q))
+        r = 0.0;
+    else
+        r = __dsub_rn(a, __dmul_rn(floor(q), L));
+    return __dsub_rn(r, hl);
+}
+
 __device__ __forceinline__ int fte_wrap_index(int i, int M) {
     int r = i % M;
     return r < 0 ? r + M : r;
@@ -212,8 +242,9 @@ __device__ __forceinline__ int fte_wrap_index(int i, int M) {
 
 // Cell of a point: floor(nside (x/L + 0.5)) clamped to [0, nside-1]
 // (PeriodicEwald/src/mex/common/ewald_tools.cpp:57-64).
-__device__ __forceinline__ int fte_cell_1d(double x, double L, int nside) {
-    int b = (int)floor(__dmul_rn((double)nside, __dadd_rn(__ddiv_rn(x, L), 0.5)));
+// rL = RN(1/L).
+__device__ __forceinline__ int fte_cell_1d(double x, double L, double rL, int nside) {
+    int b = (int)floor(__dmul_rn((double)nside, __dadd_rn(fte_div_rcp(x, L, rL), 0.5)));
     if (b < 0) b = 0;
     if (b >= nside) b = nside - 1;
     return b;

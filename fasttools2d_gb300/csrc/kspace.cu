@@ -38,6 +38,7 @@ constexpr int kPtThreads = 128;
 
 struct WinParams {
     double Lx, Ly, h, xi, eta, w;
+    double rh;  // RN(1 / h)
     int P, Mx, My;
 };
 
@@ -50,7 +51,7 @@ struct Win {
 __device__ __forceinline__ Win window_of(double x, double y, const WinParams& wp) {
     Win o;
     double px, py;
-    fte_closest_node(x, y, wp.Lx, wp.Ly, wp.h, wp.P, &o.mx, &o.my, &px, &py);
+    fte_closest_node(x, y, wp.Lx, wp.Ly, wp.h, wp.rh, wp.P, &o.mx, &o.my, &px, &py);
     double t = -2 * wp.xi * wp.xi / wp.eta;
     o.ex = exp(t * (px * px + py * py + 2 * wp.w * px));
     o.e4y = exp(2 * t * wp.w * py);
@@ -1026,7 +1027,7 @@ __device__ __forceinline__ void win32(double pp, const WinParams& wp, float* out
 
 __device__ __forceinline__ void closest32(double x, double y, const WinParams& wp, int* mx, int* my, double* px,
                                           double* py) {
-    fte_closest_node(x, y, wp.Lx, wp.Ly, wp.h, wp.P, mx, my, px, py);
+    fte_closest_node(x, y, wp.Lx, wp.Ly, wp.h, wp.rh, wp.P, mx, my, px, py);
 }
 
 constexpr int kColChunk32 = 64;
@@ -1350,7 +1351,7 @@ __global__ void k_ff_win(int kind, const double* __restrict__ p, const double* _
         const int i = perm[k];
         int mx, my;
         double px, py;
-        fte_closest_node(p[2 * i], p[2 * i + 1], wp.Lx, wp.Ly, wp.h, wp.P, &mx, &my, &px, &py);
+        fte_closest_node(p[2 * i], p[2 * i + 1], wp.Lx, wp.Ly, wp.h, wp.rh, wp.P, &mx, &my, &px, &py);
         FfWin r;
         r.mx = mx;
         r.my = my;
@@ -1577,7 +1578,7 @@ __global__ void __launch_bounds__(kTileThreads, 5) k_gather_ff(const double* __r
             const int i = perm[k];
             int mx, my;
             double px, py;
-            fte_closest_node(p[2 * i], p[2 * i + 1], wp.Lx, wp.Ly, wp.h, wp.P, &mx, &my, &px, &py);
+            fte_closest_node(p[2 * i], p[2 * i + 1], wp.Lx, wp.Ly, wp.h, wp.rh, wp.P, &mx, &my, &px, &py);
             float2 wy[PM > 0 ? PM : 1];
             {
                 const float2 e3 = fte_expm_ff(ff_split(2 * tw * wp.h * py), etab);
@@ -1727,6 +1728,7 @@ WinParams win_params(const KspaceArgs& a) {
     wp.Lx = a.Lx;
     wp.Ly = a.Ly;
     wp.h = a.Lx / a.Mx;
+    wp.rh = 1.0 / wp.h;
     wp.xi = a.xi;
     wp.eta = a.eta;
     wp.w = a.w;
@@ -2623,6 +2625,7 @@ extern "C" int fte_slp_kspace_noalloc(const double* psrc, int64_t nsrc, const do
     wp.Lx = Lx;
     wp.Ly = Ly;
     wp.h = Lx / Mx;
+    wp.rh = 1.0 / wp.h;
     wp.xi = xi;
     wp.eta = eta;
     wp.w = w;

@@ -94,22 +94,12 @@ __global__ void k_plan_combine(const double2* __restrict__ ur, const double2* __
         }
 }
 
-__device__ __forceinline__ double plan_wrap(double v, double L) {
-    double a = __dadd_rn(v, __ddiv_rn(L, 2.0));
-    double q = __ddiv_rn(a, L);
-    double r;
-    if (fabs(__dsub_rn(q, round(q))) <= 2.220446049250313e-16 * fabs(q))
-        r = 0.0;
-    else
-        r = __dsub_rn(a, __dmul_rn(floor(q), L));
-    return __dsub_rn(r, __ddiv_rn(L, 2.0));
-}
-
 __global__ void k_plan_wrap(const double* __restrict__ x, const double* __restrict__ y, int64_t n, double Lx,
                             double Ly, double* __restrict__ p) {
+    const double rLx = __drcp_rn(Lx), rLy = __drcp_rn(Ly);
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        p[2 * i] = plan_wrap(x[i], Lx);
-        p[2 * i + 1] = plan_wrap(y[i], Ly);
+        p[2 * i] = fte_wrap_coord(x[i], Lx, rLx);
+        p[2 * i + 1] = fte_wrap_coord(y[i], Ly, rLy);
     }
 }
 
