@@ -207,3 +207,21 @@ def test_ff_transforms_smooth_radices(gpu_ctx, kind):
     out_d, _ = _run(ft, gpu_ctx, kind, d, 1.0, 1.2, kspace=ft.KSPACE_FP64, xi=info.params.xi, **kw)
     rel = np.max(np.abs(out_f[3] - out_d[3])) / np.max(np.abs(out_d[3]))
     assert rel <= 2e-12, rel
+
+
+@pytest.mark.parametrize("kind", ["slp", "dlp"])
+def test_ff_spread_gather_around_long_transforms(gpu_ctx, kind):
+    """Lines beyond one block (8000 x 32 grid of a 250 x 1 box): the
+    float-float spread and gather run around the FP64 long transforms and the
+    FP64 multiplier, the stresslet on its three symmetric grids; k-space parts
+    against the FP64 k-space on the same parameters."""
+    ft = _ft()
+    Lx, Ly = 250.0, 1.0
+    d = _case(77, 3000, Lx, Ly)
+    same = dict(P=16, xi=10.0, Mx=8000, My=32, nside_x=500, nside_y=2)
+    out_f, info_f = _run(ft, gpu_ctx, kind, d, Lx, Ly, tol=1e-10, kspace=ft.KSPACE_FF, **same)
+    assert info_f.params.form == ft.FORM_FF
+    out_d, info_d = _run(ft, gpu_ctx, kind, d, Lx, Ly, tol=1e-10, kspace=ft.KSPACE_FP64, **same)
+    assert info_d.params.form == ft.FORM_PLAIN
+    rel = np.max(np.abs(out_f[3] - out_d[3])) / np.max(np.abs(out_d[3]))
+    assert rel <= 2e-12, rel
