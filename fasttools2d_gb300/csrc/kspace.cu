@@ -544,14 +544,15 @@ __global__ void __launch_bounds__(512, 2) k_fft_y_r2c_ff(const double* __restric
     const double* h1 = h0 + My;
     for (int y = threadIdx.x; y < My; y += blockDim.x) A[y] = ffc_mk(ff_split(h0[y]), ff_split(h1[y]));
     float4* R = fft_block<FfCx>(A, B, plan, false);
-    float4* o0 = Hh + ((size_t)g * Mx + 2 * c) * Kh;
-    float4* o1 = o0 + Kh;
+    // half spectra stored ky-major ([g][ky][x]): the x transforms then read
+    // and write contiguous lines; columns 2c and 2c + 1 are adjacent
+    float4* o0 = Hh + (size_t)g * Mx * Kh + 2 * c;
     const float2 half = make_float2(0.5f, 0.0f);
     for (int k = threadIdx.x; k < Kh; k += blockDim.x) {
         const float4 zk = R[k], zm = R[(My - k) % My];
         // A_k = (Z_k + conj Z_{-k})/2,  B_k = (Z_k - conj Z_{-k})/(2i)
-        o0[k] = cscale(ffc_mk(ff_add(ffc_re(zk), ffc_re(zm)), ff_add(ffc_im(zk), ff_neg(ffc_im(zm)))), half);
-        o1[k] = cscale(ffc_mk(ff_add(ffc_im(zk), ffc_im(zm)), ff_add(ffc_re(zm), ff_neg(ffc_re(zk)))), half);
+        o0[(size_t)k * Mx] = cscale(ffc_mk(ff_add(ffc_re(zk), ffc_re(zm)), ff_add(ffc_im(zk), ff_neg(ffc_im(zm)))), half);
+        o0[(size_t)k * Mx + 1] = cscale(ffc_mk(ff_add(ffc_im(zk), ffc_im(zm)), ff_add(ffc_re(zm), ff_neg(ffc_re(zk)))), half);
     }
 }
 
@@ -560,10 +561,10 @@ __global__ void __launch_bounds__(512, 2) k_fft_x_ff(float4* __restrict__ Hh, in
     float4* A = reinterpret_cast<float4*>(shff);
     float4* B = A + plan.m;
     const int k = blockIdx.x, g = blockIdx.y;
-    float4* base = Hh + (size_t)g * Mx * Kh + k;
-    for (int x = threadIdx.x; x < Mx; x += blockDim.x) A[x] = base[(size_t)x * Kh];
+    float4* base = Hh + ((size_t)g * Kh + k) * Mx;  // ky-major half spectra: line k is contiguous
+    for (int x = threadIdx.x; x < Mx; x += blockDim.x) A[x] = base[x];
     float4* R = fft_block<FfCx>(A, B, plan, inv != 0);
-    for (int x = threadIdx.x; x < Mx; x += blockDim.x) base[(size_t)x * Kh] = R[x];
+    for (int x = threadIdx.x; x < Mx; x += blockDim.x) base[x] = R[x];
 }
 
 // half spectra -> real grids as float-float pairs (the gather's input)
@@ -573,10 +574,9 @@ __global__ void __launch_bounds__(512, 2) k_fft_y_c2r_ff(const float4* __restric
     float4* B = A + plan.m;
     const int c = blockIdx.x, g = blockIdx.y;
     const int Kh = My / 2 + 1;
-    const float4* i0 = Hh + ((size_t)g * Mx + 2 * c) * Kh;
-    const float4* i1 = i0 + Kh;
+    const float4* i0 = Hh + (size_t)g * Mx * Kh + 2 * c;  // ky-major: columns 2c, 2c + 1 adjacent
     for (int k = threadIdx.x; k < Kh; k += blockDim.x) {
-        float4 a = i0[k], b = i1[k];
+        float4 a = i0[(size_t)k * Mx], b = i0[(size_t)k * Mx + 1];
         if (k == 0 || 2 * k == My) {
             a.z = a.w = 0.f;
             b.z = b.w = 0.f;
@@ -634,14 +634,16 @@ __device__ __forceinline__ void spec_st(float4* p, double2 v) {
     *p = make_float4(r.x, r.y, i.x, i.y);
 }
 
-// DLP spectra: ng = 4 (S11, S21, S12, S22) or 3 (S11, S12 + S21, S22)
-template <int KIND, typename S>
+// DLP spectra: ng = 4 (S11, S21, S12, S22) or 3 (S11, S12 + S21, S22).
+// KYMAJOR: half spectra stored [g][ky][x] (the float-float block transforms)
+// instead of [g][x][ky].
+template <int KIND, typename S, bool KYMAJOR = false>
 __global__ void k_filter(S* __restrict__ Hh, int Mx, int My, double Lx, double Ly, double xi, double eta, int ng) {
     const int Kh = My / 2 + 1;
     const size_t GS = (size_t)Mx * Kh;
     const size_t tot = GS;
     for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < tot; idx += (size_t)gridDim.x * blockDim.x) {
-        int j = (int)(idx / Kh), k = (int)(idx % Kh);
+        const int j = KYMAJOR ? (int)(idx % Mx) : (int)(idx / Kh), k = KYMAJOR ? (int)(idx / Mx) : (int)(idx % Kh);
         S* p0 = Hh + idx;
         if (j == 0 && k == 0) {
             spec_st(p0, make_double2(0, 0));
@@ -739,7 +741,7 @@ __global__ void k_filter_ff(float4* __restrict__ Hh, int Mx, int My, FfFilt f, i
     const int Kh = My / 2 + 1;
     const size_t GS = (size_t)Mx * Kh;
     for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < GS; idx += (size_t)gridDim.x * blockDim.x) {
-        const int j = (int)(idx / Kh), k = (int)(idx % Kh);
+        const int k = (int)(idx / Mx), j = (int)(idx % Mx);  // ky-major half spectra
         float4* p0 = Hh + idx;
         if (j == 0 && k == 0) {
             const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -2130,9 +2132,9 @@ int fte_kspace_run(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, fte_info
             else
                 FTE_LAUNCH(ctx, k_filter_ff<FTE_KIND_DLP>, fb, 256, 0, Hf, Mx, My, ffc, ngs);
         } else if (a.kind == FTE_KIND_SLP) {
-            FTE_LAUNCH(ctx, (k_filter<FTE_KIND_SLP, float4>), fb, 256, 0, Hf, Mx, My, a.Lx, a.Ly, a.xi, a.eta, ngs);
+            FTE_LAUNCH(ctx, (k_filter<FTE_KIND_SLP, float4, true>), fb, 256, 0, Hf, Mx, My, a.Lx, a.Ly, a.xi, a.eta, ngs);
         } else {
-            FTE_LAUNCH(ctx, (k_filter<FTE_KIND_DLP, float4>), fb, 256, 0, Hf, Mx, My, a.Lx, a.Ly, a.xi, a.eta, ngs);
+            FTE_LAUNCH(ctx, (k_filter<FTE_KIND_DLP, float4, true>), fb, 256, 0, Hf, Mx, My, a.Lx, a.Ly, a.xi, a.eta, ngs);
         }
         FTE_LAUNCH(ctx, k_fft_x_ff, dim3(Kh, 2), fft_threads(px.m), sm_x, Hf, Mx, Kh, px, 1);
         FTE_LAUNCH(ctx, k_fft_y_c2r_ff, dim3(Mx / 2, 2), fft_threads(py.m), sm_y, (const float4*)Hf,
