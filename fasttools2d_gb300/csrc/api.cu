@@ -671,17 +671,6 @@ double kinf_root(int kind, double Q, double Lx, double xi, double tol, double k0
             });
     return k;
 }
-int kinf_estimate(int kind, double Q, double Lx, double xi, double tol) {
-    return (int)std::round(Lx * kinf_root(kind, Q, Lx, xi, tol) / (2 * FTE_PI));
-}
-
-int next_smooth_even(int n) {
-    if (n < 2) n = 2;
-    if (n % 2) n++;
-    while (!smooth7(n, nullptr)) n += 2;
-    return n;
-}
-
 // transform work of a length-n line relative to a 7-smooth line of n points:
 // Bluestein runs two transforms of a smooth length m >= 2n - 1 (about 2.2 n)
 // Transform work per point of a length-n line: the sum over the Stockham
