@@ -38,7 +38,7 @@ def _worker(rank, world, port, out):
 
 def test_two_gloo_ranks_reduce_with_max():
     port = _free_port()
-    manager = mp.Manager()
+    manager = mp.get_context("spawn").Manager()
     out = manager.dict()
     mp.spawn(_worker, args=(2, port, out), nprocs=2, join=True)
     for rank in (0, 1):
