@@ -111,9 +111,16 @@ __global__ void k_scatter_tar(const double* __restrict__ p, int64_t n, const int
 
 // Grid tile of a point for the k-space kernels: floor((x + L/2)/h), the node
 // index FindClosestNode starts from, divided by the tile size, clamped.
+// With W > 0 (target bins of the tiled gathers, W = the staged region's row
+// length) a point also gets the residue mod 16 of its window's first row in
+// the staged region, counted per (tile, residue): k_tile_scatter then orders
+// each tile's points round-robin over the residues, so that the 16 threads
+// of a half-warp, which read the region at those rows' offsets, mostly hit
+// distinct shared-memory banks (8-byte values).  The order is a heuristic:
+// the node it assumes ignores the tie-break of FindClosestNode.
 __global__ void k_tile_assign(const double* __restrict__ p, int64_t n, double Lx, double Ly, double h, int ts,
                               int ntx, int nty, int* __restrict__ tile, int* __restrict__ rank,
-                              int* __restrict__ counts) {
+                              int* __restrict__ counts, int W, int* __restrict__ counts16) {
     const double lhx = __dmul_rn(Lx, 0.5), lhy = __dmul_rn(Ly, 0.5), rh = __drcp_rn(h);
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         double ax = floor(fte_div_rcp(__dadd_rn(p[2 * i], lhx), h, rh));
@@ -123,14 +130,37 @@ __global__ void k_tile_assign(const double* __restrict__ p, int64_t n, double Lx
         int tx = min((int)ax / ts, ntx - 1), ty = min((int)ay / ts, nty - 1);
         int t = ty * ntx + tx;
         tile[i] = t;
-        rank[i] = atomicAdd(&counts[t], 1);
+        const int rk = atomicAdd(&counts[t], 1);
+        if (W > 0) {
+            const int r = (((int)ax - tx * ts + 2) * W + ((int)ay - ty * ts + 2)) & 15;
+            rank[i] = (r << 26) | atomicAdd(&counts16[16 * t + r], 1);
+        } else {
+            rank[i] = rk;
+        }
     }
 }
 
+// W > 0: position in the tile = the points of earlier rounds (sum over
+// residues of min(count, round)) + the earlier residues present in this
+// round; a bijection onto the tile's slots
 __global__ void k_tile_scatter(int64_t n, const int* __restrict__ tile, const int* __restrict__ rank,
-                               const int* __restrict__ off, int* __restrict__ perm) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        perm[off[tile[i]] + rank[i]] = (int)i;
+                               const int* __restrict__ off, int* __restrict__ perm, int W,
+                               const int* __restrict__ counts16) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int t = tile[i];
+        int pos = rank[i];
+        if (W > 0) {
+            const int r = pos >> 26, q = pos & ((1 << 26) - 1);
+            const int* c = counts16 + 16 * t;
+            pos = 0;
+#pragma unroll
+            for (int b = 0; b < 16; b++) {
+                const int cb = c[b];
+                pos += min(cb, q) + ((b < r && cb > q) ? 1 : 0);
+            }
+        }
+        perm[off[t] + pos] = (int)i;
+    }
 }
 
 inline int grid_for(int64_t n, int threads, int max_blocks) {
@@ -226,12 +256,13 @@ int fte_cells_build(fte_context* ctx, WsCarver& wc, int kind, const double* psrc
 }
 
 size_t fte_tiles_ws(int64_t n, int ntiles) {
-    return 4 * ws_bytes(ntiles + 1, sizeof(int)) + 3 * ws_bytes((size_t)(n + 1), sizeof(int)) +
+    return 4 * ws_bytes(ntiles + 1, sizeof(int)) + ws_bytes(16 * (size_t)ntiles + 1, sizeof(int)) +
+           3 * ws_bytes((size_t)(n + 1), sizeof(int)) +
            4 * ws_bytes((size_t)(ntiles + 1) / 4096 + 8, sizeof(int)) + 4096;
 }
 
 int fte_tiles_build(fte_context* ctx, WsCarver& wc, const double* p, int64_t n, double Lx, double Ly, double h,
-                    int ts, int ntx, int nty, TileBins* out) {
+                    int ts, int ntx, int nty, TileBins* out, int region_w) {
     int nt = ntx * nty;
     out->ntx = ntx;
     out->nty = nty;
@@ -241,15 +272,17 @@ int fte_tiles_build(fte_context* ctx, WsCarver& wc, const double* p, int64_t n, 
     int* tile = wc.take<int>(n + 1);
     int* rank = wc.take<int>(n + 1);
     out->perm = wc.take<int>(n + 1);
+    int* cnt16 = region_w > 0 ? wc.take<int>(16 * (size_t)nt + 1) : nullptr;
     FTE_WS_CHECK(wc);
     FTE_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(int) * (nt + 1), ctx->stream));
+    if (cnt16) FTE_CUDA_TRY(cudaMemsetAsync(cnt16, 0, sizeof(int) * 16 * (size_t)nt, ctx->stream));
     int maxb = ctx->num_sms * 8;
     if (n > 0)
         FTE_LAUNCH(ctx, k_tile_assign, grid_for(n, 256, maxb), 256, 0, p, n, Lx, Ly, h, ts, ntx, nty, tile, rank,
-                   cnt);
+                   cnt, region_w, cnt16);
     FTE_TRY(fte_scan_exclusive(ctx, wc, cnt, out->off, nt + 1));
     if (n > 0)
         FTE_LAUNCH(ctx, k_tile_scatter, grid_for(n, 256, maxb), 256, 0, n, (const int*)tile, (const int*)rank,
-                   (const int*)out->off, out->perm);
+                   (const int*)out->off, out->perm, region_w, (const int*)cnt16);
     return FTE_OK;
 }

@@ -282,8 +282,10 @@ struct TileBins {
     int* perm;  // original index of the k-th point in tile order
 };
 size_t fte_tiles_ws(int64_t n, int ntiles);
+// region_w > 0: order each tile's points for the tiled gathers (staged
+// region rows of region_w nodes; see k_tile_assign)
 int fte_tiles_build(fte_context* ctx, WsCarver& wc, const double* p, int64_t n, double Lx, double Ly, double h,
-                    int ts, int ntx, int nty, TileBins* out);
+                    int ts, int ntx, int nty, TileBins* out, int region_w = 0);
 
 // ff: float-float pairs, with ffmem scratch of fte_near_ff_ws(kind, 1, nsrc)
 int fte_near_launch(fte_context* ctx, int kind, const CellList& cl, double xi, double Lx, double Ly, double2* ur,

@@ -1872,7 +1872,7 @@ int kspace_run_mixed(fte_context* ctx, WsCarver& wc, const KspaceArgs& a) {
         tb_g = *a.pre_tar;
     else if (a.ntar > 0)
         FTE_TRY(fte_tiles_build(ctx, wc, a.ptar, a.ntar, a.Lx, a.Ly, wp.h, ts_g, (Mx + ts_g - 1) / ts_g,
-                                (My + ts_g - 1) / ts_g, &tb_g));
+                                (My + ts_g - 1) / ts_g, &tb_g, tile_region(ts_g, a.P)));
     if ((a.nsrc > 0 && tb_s.ts != ts_s) || (a.ntar > 0 && tb_g.ts != ts_g)) {
         fte_set_error("internal: prebuilt tiles do not match the mixed-form tile sizes");
         return FTE_ERR_INVALID;
@@ -1912,7 +1912,7 @@ int fte_kspace_tiles(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, TileBi
                                 (a.My + ts_s - 1) / ts_s, src));
     if (ts_g > 0 && a.ntar > 0)
         FTE_TRY(fte_tiles_build(ctx, wc, a.ptar, a.ntar, a.Lx, a.Ly, h, ts_g, (a.Mx + ts_g - 1) / ts_g,
-                                (a.My + ts_g - 1) / ts_g, tar));
+                                (a.My + ts_g - 1) / ts_g, tar, tile_region(ts_g, a.P)));
     return FTE_OK;
 }
 
@@ -1980,7 +1980,7 @@ int fte_kspace_tune(fte_context* ctx, void* grid, WsCarver bins, KspaceArgs& a, 
         WsCarver w = bins;
         TileBins tb;
         rc = fte_tiles_build(ctx, w, a.ptar, a.ntar, a.Lx, a.Ly, wp.h, ts, (a.Mx + ts - 1) / ts,
-                             (a.My + ts - 1) / ts, &tb);
+                             (a.My + ts - 1) / ts, &tb, tile_region(ts, a.P));
         if (!rc && !w.ok()) {
             fte_set_error("internal: tuner bin scratch too small");
             rc = FTE_ERR_ALLOC;
@@ -2080,7 +2080,7 @@ int fte_kspace_run(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, fte_info
         tb_g = *a.pre_tar;
     else if (ts_g > 0 && a.ntar > 0)
         FTE_TRY(fte_tiles_build(ctx, wc, a.ptar, a.ntar, a.Lx, a.Ly, wp.h, ts_g, (Mx + ts_g - 1) / ts_g,
-                                (My + ts_g - 1) / ts_g, &tb_g));
+                                (My + ts_g - 1) / ts_g, &tb_g, tile_region(ts_g, a.P)));
     if ((a.nsrc > 0 && tb_s.ts != ts_s) || (a.ntar > 0 && tb_g.ts != ts_g)) {
         fte_set_error("internal: prebuilt tiles do not match the FP64 tile sizes");
         return FTE_ERR_INVALID;
@@ -2388,7 +2388,7 @@ int fte_q_kspace_run(fte_context* ctx, WsCarver& wc, int q, const KspaceArgs& a,
     // gather pairs of grids
     TileBins tb;
     FTE_TRY(fte_tiles_build(ctx, wc, a.ptar, a.ntar, a.Lx, a.Ly, wp.h, ts_g, (Mx + ts_g - 1) / ts_g,
-                            (My + ts_g - 1) / ts_g, &tb));
+                            (My + ts_g - 1) / ts_g, &tb, tile_region(ts_g, a.P)));
     FTE_WS_CHECK(wc);
     const double scale = gather_scale(a);
     KspaceArgs ag = a;
