@@ -272,6 +272,7 @@ int fte_tiles_build(fte_context* ctx, WsCarver& wc, const double* p, int64_t n, 
     int* tile = wc.take<int>(n + 1);
     int* rank = wc.take<int>(n + 1);
     out->perm = wc.take<int>(n + 1);
+    if (n >= (int64_t(1) << 26)) region_w = 0;  // ranks within a residue class are packed in 26 bits
     int* cnt16 = region_w > 0 ? wc.take<int>(16 * (size_t)nt + 1) : nullptr;
     FTE_WS_CHECK(wc);
     FTE_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(int) * (nt + 1), ctx->stream));
