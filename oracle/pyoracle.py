@@ -10,8 +10,10 @@ never imports it.
 * ``ref_call`` -- the reference's own MEX gateways
   (PeriodicEwald/src/mex/{StokesSLP,StokesDLP}/mex_stokes_*.cpp), compiled
   unmodified under ``oracle/_ref`` against the MEX stand-in in ``mexshim/``.
-  They exist only where the reference checkout and an x86-64 compiler were
-  available at build time.
+  They are built where the reference checkout is available and, on hosts
+  without it (the aarch64 GPU hosts), from the verbatim copies of the
+  velocity path's sources that the build with the checkout staged under
+  ``oracle/_ref/src`` (checked against ``oracle/ref_sources.sha256``).
 
 Point/density arrays are numpy float64 arrays of shape (N, 2) in C order, i.e.
 the reference's 2 x N column-major layout with x/y interleaved.
@@ -62,9 +64,24 @@ def build(quiet: bool = True) -> str:
     return LIB_PATH
 
 
-def build_reference() -> bool:
-    """Compile the reference gateways into oracle/_ref (x86-64 with the checkout only)."""
-    out = subprocess.run(["make", "-C", HERE, "ref"], capture_output=True, text=True)
+def staged_reference() -> bool:
+    """True where the verbatim copies of the reference's velocity sources
+    (staged under oracle/_ref/src by ``make ref`` on a host with the checkout)
+    are present."""
+    return os.path.exists(os.path.join(REF_DIR, "src", "common", "ewald_tools.cpp"))
+
+
+def build_reference(ref_root: str | None = None, portable: bool = False) -> bool:
+    """Compile the reference gateways into oracle/_ref with oracle/Makefile.
+
+    ref_root: the reference checkout (all gateways; also stages the velocity
+    path's sources); None: the staged copy (the four velocity gateways).
+    portable: also the x86 flavour built on the portable SSE header (P3)."""
+    cmd = ["make", "-C", HERE, f"-j{min(16, os.cpu_count() or 1)}", "ref"]
+    if portable:
+        cmd.append("ref-portable")
+    cmd.append(f"REF_ROOT={ref_root or ''}")
+    out = subprocess.run(cmd, capture_output=True, text=True)
     return out.returncode == 0
 
 

@@ -104,8 +104,8 @@ def run_mex_case(name, gateway, args, n_out, **meta):
 
 def main():
     if not po.ref_available("O3"):
-        if not po.build_reference():
-            raise SystemExit("reference gateways unavailable: run `make -C oracle ref` on x86-64 with the checkout")
+        if not po.build_reference(os.environ.get("FTE_REF_ROOT", "/root/reference")):
+            raise SystemExit("reference gateways unavailable: run `make -C oracle ref REF_ROOT=<checkout>`")
 
     # 1. The reference's direct-sum test setup
     #    (PeriodicEwald/tests/direct_sums/direct_sums_velocity_test.m:13-44):
