@@ -9,7 +9,12 @@
 #include <algorithm>
 #include <vector>
 
+#include <atomic>
+#include <mutex>
+#include <utility>
+
 #include "fte_internal.cuh"
+#include "../../include/fasttools2d_debug.h"
 
 // ---------------------------------------------------------------------------
 // errors
@@ -21,6 +26,94 @@ void fte_set_error(const char* fmt, ...) {
     va_start(ap, fmt);
     vsnprintf(g_err, sizeof(g_err), fmt, ap);
     va_end(ap);
+}
+
+cudaError_t fte_smem_ceiling_raw(const void* kernel, size_t bytes) {
+    static std::mutex mu;
+    static std::map<std::pair<int, const void*>, size_t> ceiling;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(mu);
+    auto key = std::make_pair(dev, kernel);
+    auto it = ceiling.find(key);
+    if (it == ceiling.end()) {
+        int optin = 0;
+        e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        if (e != cudaSuccess) return e;
+        cudaFuncAttributes fa;
+        e = cudaFuncGetAttributes(&fa, kernel);
+        if (e != cudaSuccess) return e;
+        const size_t cap = (size_t)optin > fa.sharedSizeBytes ? (size_t)optin - fa.sharedSizeBytes : 0;
+        e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap);
+        if (e != cudaSuccess) return e;
+        it = ceiling.emplace(key, cap).first;
+    }
+    return bytes <= it->second ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+// ---------------------------------------------------------------------------
+// host-side allocation fault injection (tests)
+// ---------------------------------------------------------------------------
+static std::atomic<int> g_fail_alloc_countdown{0};
+
+extern "C" int fte_debug_fail_alloc(int after) {
+    g_fail_alloc_countdown.store(after > 0 ? after : 0);
+    return FTE_OK;
+}
+
+bool fte_alloc_should_fail() {
+    int v = g_fail_alloc_countdown.load();
+    while (v > 0) {
+        if (g_fail_alloc_countdown.compare_exchange_weak(v, v - 1)) return v == 1;
+    }
+    return false;
+}
+
+// ---------------------------------------------------------------------------
+// input checks
+// ---------------------------------------------------------------------------
+__global__ void k_count_nonfinite(FiniteSet s, unsigned int* __restrict__ bad) {
+    unsigned int cnt = 0;
+    for (int a = 0; a < s.k; a++) {
+        const double* __restrict__ v = s.p[a];
+        for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < s.n[a];
+             i += (int64_t)gridDim.x * blockDim.x)
+            cnt += isfinite(v[i]) ? 0u : 1u;
+    }
+    if (cnt) atomicAdd(bad, cnt);
+}
+
+int fte_finite_launch(fte_context* c, const FiniteSet& s) {
+    unsigned int* host_count = reinterpret_cast<unsigned int*>(c->host_scalars + 48);
+    *host_count = 0;
+    if (s.k == 0) return FTE_OK;
+    int64_t most = 0;
+    for (int a = 0; a < s.k; a++) most = s.n[a] > most ? s.n[a] : most;
+    int64_t blocks = (most + 255) / 256;
+    const int cap = 4 * (c->num_sms > 0 ? c->num_sms : 152);
+    const int grid = (int)(blocks < cap ? (blocks < 1 ? 1 : blocks) : cap);
+    FTE_CUDA_TRY(cudaMemsetAsync(c->dev_flags, 0, sizeof(unsigned int), c->stream));
+    FTE_LAUNCH(c, k_count_nonfinite, grid, 256, 0, s, c->dev_flags);
+    FTE_CUDA_TRY(cudaMemcpyAsync(host_count, c->dev_flags, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->stream));
+    return FTE_OK;
+}
+
+int fte_finite_result(fte_context* c, const char* entry) {
+    const unsigned int bad = *reinterpret_cast<const unsigned int*>(c->host_scalars + 48);
+    if (bad) {
+        fte_set_error("%s: %u non-finite values (NaN or Inf) in the point, density, normal or weight arrays", entry,
+                      bad);
+        return FTE_ERR_INVALID;
+    }
+    return FTE_OK;
+}
+
+int fte_check_finite(fte_context* c, const FiniteSet& s, const char* entry) {
+    if (s.k == 0) return FTE_OK;
+    FTE_TRY(fte_finite_launch(c, s));
+    FTE_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return fte_finite_result(c, entry);
 }
 
 extern "C" const char* fte_last_error(void) { return g_err; }
@@ -56,6 +149,7 @@ extern "C" int fte_create(fte_context** out, int device) {
     c->stream = c->own_stream;
     for (int i = 0; i < 8; i++) FTE_CUDA_TRY(cudaEventCreate(&c->ev[i]));
     FTE_CUDA_TRY(cudaMallocHost(&c->host_scalars, 64 * sizeof(double)));
+    FTE_CUDA_TRY(cudaMalloc(&c->dev_flags, 64));
     *out = c;
     return FTE_OK;
 }
@@ -88,6 +182,7 @@ extern "C" int fte_destroy(fte_context* c) {
     if (c->ws) cudaFree(c->ws);
     if (c->ws2) cudaFree(c->ws2);
     if (c->host_scalars) cudaFreeHost(c->host_scalars);
+    if (c->dev_flags) cudaFree(c->dev_flags);
     for (int i = 0; i < 8; i++)
         if (c->ev[i]) cudaEventDestroy(c->ev[i]);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
@@ -124,7 +219,7 @@ int fte_ws_reserve(fte_context* c, size_t bytes) {
         c->ws_size = 0;
     }
     size_t want = bytes + bytes / 8 + (1 << 20);
-    cudaError_t e = cudaMalloc(&c->ws, want);
+    cudaError_t e = fte_alloc_should_fail() ? cudaErrorMemoryAllocation : cudaMalloc(&c->ws, want);
     if (e != cudaSuccess) {
         cudaGetLastError();
         fte_set_error("device workspace of %zu bytes could not be allocated: %s", want, cudaGetErrorString(e));
@@ -143,7 +238,7 @@ int fte_ws2_reserve(fte_context* c, size_t bytes) {
         c->ws2_size = 0;
     }
     size_t want = bytes + bytes / 8 + (1 << 20);
-    cudaError_t e = cudaMalloc(&c->ws2, want);
+    cudaError_t e = fte_alloc_should_fail() ? cudaErrorMemoryAllocation : cudaMalloc(&c->ws2, want);
     if (e != cudaSuccess) {
         cudaGetLastError();
         fte_set_error("device workspace of %zu bytes could not be allocated: %s", want, cudaGetErrorString(e));
@@ -485,7 +580,7 @@ int fte_fft_prepare(fte_context* c, int n) {
 // ---------------------------------------------------------------------------
 // parameter selection: the MATLAB drivers' analytic choice
 // (StokesSLP_ewald_2p.m:27-35,85-104 and find_kinfb :147-173, find_xi :178-202;
-//  StokesDLP_ewald_2p.m:27-38,307-327 and find_kinfb :373-399, find_xi :404-427).
+//  StokesDLP_ewald_2p.m:27-38,105-125 and find_kinfb :171-197, find_xi :202-224).
 // Estimates of Palsson & Tornberg 2019; Newton iterations with the step in
 // the negative direction limited to 0.9 of the iterate, at most 101 steps.
 // find_kinfb is called with Lx in place of Ly, as the drivers do.
@@ -1137,6 +1232,12 @@ static int real_entry(fte_context* c, int kind, const double* psrc, int64_t nsrc
     FTE_TRY(st.put(kind == FTE_KIND_DLP ? nrm : nullptr, 2 * (size_t)nsrc, &dn));
     double2* dur = host ? wc.take<double2>(ntar + 1) : reinterpret_cast<double2*>(ur);
     FTE_WS_CHECK(wc);
+    FiniteSet fin;
+    fin.add(dps, 2 * nsrc);
+    fin.add(dpt, 2 * ntar);
+    fin.add(df, 2 * nsrc);
+    fin.add(dn, 2 * nsrc);
+    FTE_TRY(fte_check_finite(c, fin, kind == FTE_KIND_SLP ? "fte_slp_real" : "fte_dlp_real"));
     if (ntar > 0) {
         CellList cl;
         FTE_TRY(fte_cells_build(c, wc, kind, dps, nsrc, dpt, ntar, df, dn, nullptr, nsx, nsy, Lx, Ly, &cl));
@@ -1187,6 +1288,12 @@ static int kspace_entry(fte_context* c, int kind, const double* psrc, int64_t ns
     FTE_TRY(st.put(kind == FTE_KIND_DLP ? nrm : nullptr, 2 * (size_t)nsrc, &dn));
     double2* duk = host ? wc.take<double2>(ntar + 1) : reinterpret_cast<double2*>(uk);
     FTE_WS_CHECK(wc);
+    FiniteSet fin;
+    fin.add(dps, 2 * nsrc);
+    fin.add(dpt, 2 * ntar);
+    fin.add(df, 2 * nsrc);
+    fin.add(dn, 2 * nsrc);
+    FTE_TRY(fte_check_finite(c, fin, kind == FTE_KIND_SLP ? "fte_slp_kspace" : "fte_dlp_kspace"));
     KspaceArgs a;
     a.kind = kind;
     a.form = FTE_FORM_PLAIN;
@@ -1269,6 +1376,12 @@ extern "C" int fte_q_real(fte_context* c, int kind, int q, const double* psrc, i
     FTE_TRY(st.put(kind == FTE_KIND_DLP ? n : nullptr, 2 * (size_t)nsrc, &dn));
     double* dout = host ? wc.take<double>((size_t)nc * (ntar + 1)) : out;
     FTE_WS_CHECK(wc);
+    FiniteSet fin;
+    fin.add(dps, 2 * nsrc);
+    fin.add(dpt, 2 * ntar);
+    fin.add(df, 2 * nsrc);
+    fin.add(dn, 2 * nsrc);
+    FTE_TRY(fte_check_finite(c, fin, "fte_q_real"));
     if (ntar > 0) {
         CellList cl;
         FTE_TRY(fte_cells_build(c, wc, kind, dps, nsrc, dpt, ntar, df, dn, nullptr, nsx, nsy, Lx, Ly, &cl));
@@ -1309,6 +1422,12 @@ extern "C" int fte_q_kspace(fte_context* c, int kind, int q, const double* psrc,
     FTE_TRY(st.put(kind == FTE_KIND_DLP ? n : nullptr, 2 * (size_t)nsrc, &dn));
     double* dout = host ? wc.take<double>((size_t)nc * (ntar + 1)) : out;
     FTE_WS_CHECK(wc);
+    FiniteSet fin;
+    fin.add(dps, 2 * nsrc);
+    fin.add(dpt, 2 * ntar);
+    fin.add(df, 2 * nsrc);
+    fin.add(dn, 2 * nsrc);
+    FTE_TRY(fte_check_finite(c, fin, "fte_q_kspace"));
     KspaceArgs a;
     a.kind = kind;
     a.form = FTE_FORM_PLAIN;
@@ -1409,6 +1528,11 @@ static int ewald_entry(fte_context* c, int kind, const double* xsrc, const doubl
     double2* duk = wc.take<double2>(ntar + 1);
     double* acc = wc.take<double>(8);
     FTE_WS_CHECK(wc);
+    FiniteSet fin;
+    for (const double* a : {dxs, dys, df1, df2, dn1, dn2, dw}) fin.add(a, nsrc);
+    fin.add(dxt, ntar);
+    fin.add(dyt, ntar);
+    FTE_TRY(fte_finite_launch(c, fin));
     if (nsrc > 0) {
         FTE_LAUNCH(c, k_wrap_pack, grid1d(c, nsrc), 256, 0, dxs, dys, nsrc, Lx, Ly, ps);
         FTE_LAUNCH(c, k_pack, grid1d(c, nsrc), 256, 0, df1, df2, nsrc, pf);
@@ -1426,6 +1550,7 @@ static int ewald_entry(fte_context* c, int kind, const double* xsrc, const doubl
     }
     FTE_CUDA_TRY(cudaMemcpyAsync(c->host_scalars, acc, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     FTE_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    FTE_TRY(fte_finite_result(c, kind == FTE_KIND_SLP ? "fte_stokes_slp_ewald_2p" : "fte_stokes_dlp_ewald_2p"));
     double Q = c->host_scalars[0] + 1.0;
     fte_params prm;
     if (opt->form == FTE_FORM_MIXED)
@@ -1766,6 +1891,10 @@ extern "C" int fte_stokes_q_ewald_2p(fte_context* c, int kind, int q, const doub
     int* deq = eqs.empty() ? nullptr : wc.take<int>(ntar + 1);
     double* acc = wc.take<double>(8);
     FTE_WS_CHECK(wc);
+    FiniteSet fin;
+    for (const double* a : {dxs, dys, df1, df2, dn1, dn2}) fin.add(a, nsrc);
+    for (const double* a : {dxt, dyt, db1, db2}) fin.add(a, ntar);
+    FTE_TRY(fte_finite_launch(c, fin));
     FTE_CUDA_TRY(cudaMemsetAsync(acc, 0, 8 * sizeof(double), c->stream));
     if (nsrc > 0) {
         FTE_LAUNCH(c, k_wrap_pack, grid1d(c, nsrc), 256, 0, dxs, dys, nsrc, Lx, Ly, ps);
@@ -1778,6 +1907,7 @@ extern "C" int fte_stokes_q_ewald_2p(fte_context* c, int kind, int q, const doub
     if (deq) FTE_CUDA_TRY(cudaMemcpyAsync(deq, eqs.data(), ntar * sizeof(int), cudaMemcpyHostToDevice, c->stream));
     FTE_CUDA_TRY(cudaMemcpyAsync(c->host_scalars, acc, 4 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     FTE_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    FTE_TRY(fte_finite_result(c, "fte_stokes_q_ewald_2p"));
     const double Q = c->host_scalars[0] + 1.0;
     // the stresslet vorticity driver uses the Stokeslet's estimates and point count
     const int est_kind = (kind == FTE_KIND_DLP && q == FTE_Q_VORTICITY) ? FTE_KIND_SLP : kind;

@@ -1,6 +1,6 @@
 // cells.cu -- device cell list for the real-space sums.
 //
-// Restates the reference's Assign (PeriodicEwald/src/mex/common/ewald_tools.cpp:37-110):
+// Restates the reference's Assign (PeriodicEwald/src/mex/common/ewald_tools.cpp:7-80):
 // boxes are nside_x x nside_y, numbered box_y*nside_x + box_x, points are
 // binned with floor(nside (x/L + 0.5)) clamped to the box range.  On the GPU
 // the counting sort is a histogram with atomics (which also hands each point

@@ -28,6 +28,21 @@ void fte_set_error(const char* fmt, ...);
         }                                                                                          \
     } while (0)
 
+// Dynamic shared-memory ceiling of a kernel.  The ceiling
+// (cudaFuncAttributeMaxDynamicSharedMemorySize) belongs to the kernel -- one
+// value per device for the whole process -- not to a context or a stream, so
+// setting it per call to that call's own need would let a concurrent call on
+// another thread lower it between a raise and the matching launch.  Instead it
+// is raised once per (device, kernel), under a lock, to the most the device
+// allows that kernel (the opt-in maximum minus the kernel's static shared
+// memory), and never lowered.  Returns cudaErrorInvalidValue when `bytes`
+// exceeds that ceiling (the launch would fail).
+cudaError_t fte_smem_ceiling_raw(const void* kernel, size_t bytes);
+template <typename K>
+inline cudaError_t fte_smem_ceiling(K* kernel, size_t bytes) {
+    return fte_smem_ceiling_raw(reinterpret_cast<const void*>(kernel), bytes);
+}
+
 #define FTE_TRY(expr)          \
     do {                       \
         int s_ = (expr);       \
@@ -129,7 +144,40 @@ struct fte_context {
     cudaEvent_t ev[8] = {nullptr};
     int max_smem_optin = 0;
     int num_sms = 0;
+    unsigned int* dev_flags = nullptr;  // device counters of the input checks
 };
+
+// ---------------------------------------------------------------------------
+// Input checks.  Every array value of an entry's points, densities, normals
+// and weights must be finite: a NaN or infinite coordinate has no cell, grid
+// node or periodic image.  The check is one launch over the staged device
+// arrays; its count is read back with the entry's first synchronisation, and
+// the entry then fails with FTE_ERR_INVALID before any other kernel runs.
+// ---------------------------------------------------------------------------
+struct FiniteSet {
+    enum { kMax = 12 };
+    const double* p[kMax] = {nullptr};
+    int64_t n[kMax] = {0};
+    int k = 0;
+    void add(const double* a, int64_t count) {
+        if (a && count > 0 && k < kMax) {
+            p[k] = a;
+            n[k] = count;
+            k++;
+        }
+    }
+};
+// queue the check and the read-back of its count (no synchronisation)
+int fte_finite_launch(fte_context* c, const FiniteSet& s);
+// after a synchronisation of c->stream: FTE_ERR_INVALID if a value was not finite
+int fte_finite_result(fte_context* c, const char* entry);
+// both, with a synchronisation between them
+int fte_check_finite(fte_context* c, const FiniteSet& s, const char* entry);
+
+// Host-side fault injection for tests (fasttools2d_debug.h): true when the
+// device allocation about to be made must fail as if the device were out of
+// memory.
+bool fte_alloc_should_fail();
 
 // Bump allocator over the context workspace.  Sizes are rounded to 256 B.
 struct WsCarver {
@@ -194,7 +242,7 @@ __device__ __forceinline__ double fte_div_rcp(double x, double d, double rd) {
 }
 
 // First window node (mx, my) and in-cell offsets (px, py) of a point: the
-// reference's FindClosestNode (PeriodicEwald/src/mex/common/ewald_tools.cpp:116-144).
+// reference's FindClosestNode (PeriodicEwald/src/mex/common/ewald_tools.cpp:86-114).
 // Written with explicitly rounded operations so that no multiply-add is fused:
 // the tie-break below depends on the exact rounding of each step (the
 // quotients by h are the IEEE quotients, formed from rh = RN(1/h); halving
@@ -241,7 +289,7 @@ __device__ __forceinline__ int fte_wrap_index(int i, int M) {
 }
 
 // Cell of a point: floor(nside (x/L + 0.5)) clamped to [0, nside-1]
-// (PeriodicEwald/src/mex/common/ewald_tools.cpp:57-64).
+// (PeriodicEwald/src/mex/common/ewald_tools.cpp:27-34).
 // rL = RN(1/L).
 __device__ __forceinline__ int fte_cell_1d(double x, double L, double rL, int nside) {
     int b = (int)floor(__dmul_rn((double)nside, __dadd_rn(fte_div_rcp(x, L, rL), 0.5)));

@@ -3,7 +3,7 @@
 // Restates the reference's k-space gateways
 //   SLP: PeriodicEwald/src/mex/StokesSLP/mex_stokes_slp_kspace.cpp:47-209
 //   DLP: PeriodicEwald/src/mex/StokesDLP/mex_stokes_dlp_kspace.cpp:266-487
-// and the shared Spread/Gather (PeriodicEwald/src/mex/common/ewald_tools.cpp:150-301):
+// and the shared Spread/Gather (PeriodicEwald/src/mex/common/ewald_tools.cpp:120-271):
 //
 //   1. spread: every source adds omega(node) q_c to (P+1)^2 nodes of each
 //      grid, omega the fast-Gaussian-gridding window of the reference
@@ -42,7 +42,7 @@ struct WinParams {
     int P, Mx, My;
 };
 
-// per-point window factors, as in ewald_tools.cpp:182-190 / 256-262
+// per-point window factors, as in ewald_tools.cpp:152-160 / 226-232
 struct Win {
     int mx, my;
     double ex, e4y, e3x, e3y;
@@ -60,7 +60,7 @@ __device__ __forceinline__ Win window_of(double x, double y, const WinParams& wp
     return o;
 }
 
-// e1[j] = exp(-2 xi^2/eta h^2 (j - P/2)^2)   (ewald_tools.cpp:155-157)
+// e1[j] = exp(-2 xi^2/eta h^2 (j - P/2)^2)   (ewald_tools.cpp:125-127)
 __device__ __forceinline__ void load_e1(double* e1, const WinParams& wp) {
     double t0 = -2 * wp.xi * wp.xi / wp.eta * wp.h * wp.h;
     for (int j = threadIdx.x; j <= wp.P; j += blockDim.x) {
@@ -976,8 +976,8 @@ int fte_long_fft(fte_context* c, const LongFft& f, double2* X, LineMap mx, long 
         fte_set_error("long FFT: block transforms of %d / %d exceed shared memory", f.n2, f.n1);
         return FTE_ERR_UNSUPPORTED;
     }
-    FTE_CUDA_TRY(cudaFuncSetAttribute(k_lf_pass1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1));
-    FTE_CUDA_TRY(cudaFuncSetAttribute(k_lf_pass2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2));
+    FTE_CUDA_TRY(fte_smem_ceiling(k_lf_pass1, (int)sm1));
+    FTE_CUDA_TRY(fte_smem_ceiling(k_lf_pass2, (int)sm2));
     const LineMap flat{(long long)f.L, 0, 1, 1};
     auto four_step = [&](double2* data, LineMap m, double2* Y, bool iv) -> int {
         FTE_LAUNCH(c, k_lf_pass1, dim3((unsigned)nl, f.n1), fft_threads(f.d2.m), sm1, (const double2*)data, m, f.L,
@@ -1319,7 +1319,7 @@ __global__ void k_filter32(float2* __restrict__ Hh, int Mx, int My, double Lx, d
 // extending the available precision"), sums by Knuth's two-sum.  The
 // transforms and the filter stay FP64.  Per-point window factors are formed
 // once in FP64 (the reference's closest node and four exponentials,
-// ewald_tools.cpp:86-114, 182-190), rounded to float-float, and the window
+// ewald_tools.cpp:86-114, 152-160), rounded to float-float, and the window
 // rows by float-float recurrences; relative error ~1e-13 against FP64.
 // ===========================================================================
 // per-source window record in tile order (64 bytes)
@@ -1764,17 +1764,17 @@ int launch_spread_tiled(fte_context* ctx, const KspaceArgs& a, const TileBins& t
         FTE_LAUNCH(ctx, k_ff_win, ew_grid(ctx, a.nsrc), 256, 0, a.kind, a.psrc, a.f, a.nrm, a.wts, (const int*)tb.perm,
                    a.nsrc, wp, recs);
         if (ngf == 2) {
-            FTE_CUDA_TRY(cudaFuncSetAttribute(k_spread_ff<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smf));
+            FTE_CUDA_TRY(fte_smem_ceiling(k_spread_ff<2>, (int)smf));
             FTE_LAUNCH(ctx, k_spread_ff<2>, grid, kColThreads, smf, (const FfWin*)recs, (const int*)tb.off, tb.ts,
                        tb.ntx, tb.nty, wp, Hd, Hd + G, nullptr);
         } else {
-            FTE_CUDA_TRY(cudaFuncSetAttribute(k_spread_ff<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smf));
+            FTE_CUDA_TRY(fte_smem_ceiling(k_spread_ff<3>, (int)smf));
             FTE_LAUNCH(ctx, k_spread_ff<3>, grid, kColThreads, smf, (const FfWin*)recs, (const int*)tb.off, tb.ts,
                        tb.ntx, tb.nty, wp, Hd, Hd + G, Hd + 2 * G);
         }
     } else if (f32) {
         float* Hf = static_cast<float*>(H);
-        FTE_CUDA_TRY(cudaFuncSetAttribute(k_spread_cols32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        FTE_CUDA_TRY(fte_smem_ceiling(k_spread_cols32, (int)sm));
         for (int pass = 0; pass < ng / 2; pass++) {
             int mode = ng == 2 ? 0 : 1 + pass;
             FTE_LAUNCH(ctx, k_spread_cols32, grid, kColThreads, sm, mode, a.psrc, a.f, a.nrm, a.wts,
@@ -1783,7 +1783,7 @@ int launch_spread_tiled(fte_context* ctx, const KspaceArgs& a, const TileBins& t
         }
     } else {
         double* Hd = static_cast<double*>(H);
-        FTE_CUDA_TRY(cudaFuncSetAttribute(k_spread_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        FTE_CUDA_TRY(fte_smem_ceiling(k_spread_cols, (int)sm));
         for (int pass = 0; pass < ng / 2; pass++) {
             int mode = ng == 2 ? 0 : 1 + pass;
             FTE_LAUNCH(ctx, k_spread_cols, grid, kColThreads, sm, mode, a.psrc, a.f, a.nrm, a.wts,
@@ -1805,7 +1805,7 @@ int launch_gather_tiled(fte_context* ctx, const KspaceArgs& a, const TileBins& t
         const float2* Hf = static_cast<const float2*>(H);
         size_t sm = gather_ff_smem(tb.ts, a.P);
         auto go = [&](auto kern) -> int {
-            FTE_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+            FTE_CUDA_TRY(fte_smem_ceiling(kern, (int)sm));
             FTE_LAUNCH(ctx, kern, grid, kTileThreads, sm, a.ptar, (const int*)tb.off, (const int*)tb.perm, tb.ts,
                        tb.ntx, tb.nty, wp, Hf, Hf + G, scale, a.uk);
             return FTE_OK;
@@ -1819,13 +1819,13 @@ int launch_gather_tiled(fte_context* ctx, const KspaceArgs& a, const TileBins& t
     } else if (a.form == FTE_FORM_MIXED) {
         const float* Hf = static_cast<const float*>(H);
         size_t sm = gather32_smem(tb.ts, a.P);
-        FTE_CUDA_TRY(cudaFuncSetAttribute(k_gather_tiled32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        FTE_CUDA_TRY(fte_smem_ceiling(k_gather_tiled32, (int)sm));
         FTE_LAUNCH(ctx, k_gather_tiled32, grid, kTileThreads, sm, a.ptar, (const int*)tb.off, (const int*)tb.perm,
                    tb.ts, tb.ntx, tb.nty, wp, Hf, Hf + G, scale, a.uk);
     } else {
         const double* Hd = static_cast<const double*>(H);
         size_t sm = gather64_smem(tb.ts, a.P);
-        FTE_CUDA_TRY(cudaFuncSetAttribute(k_gather_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        FTE_CUDA_TRY(fte_smem_ceiling(k_gather_tiled, (int)sm));
         FTE_LAUNCH(ctx, k_gather_tiled, grid, kTileThreads, sm, a.ptar, (const int*)tb.off, (const int*)tb.perm,
                    tb.ts, tb.ntx, tb.nty, wp, Hd, Hd + G, scale, a.uk);
     }
@@ -1881,9 +1881,9 @@ int kspace_run_mixed(fte_context* ctx, WsCarver& wc, const KspaceArgs& a) {
     FTE_CUDA_TRY(cudaMemsetAsync(H, 0, sizeof(float) * ng * G, ctx->stream));
     if (a.nsrc > 0) FTE_TRY(launch_spread_tiled(ctx, a, tb_s, wp, H, nullptr));
     FTE_TRY(fte_record(ctx, 3));
-    FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_y_r2c32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_y));
-    FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_y_c2r32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_y));
-    FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_x32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_x));
+    FTE_CUDA_TRY(fte_smem_ceiling(k_fft_y_r2c32, (int)sm_y));
+    FTE_CUDA_TRY(fte_smem_ceiling(k_fft_y_c2r32, (int)sm_y));
+    FTE_CUDA_TRY(fte_smem_ceiling(k_fft_x32, (int)sm_x));
     FTE_LAUNCH(ctx, k_fft_y_r2c32, dim3(Mx / 2, ng), fft_threads(py.m), sm_y, (const float*)H, Hh, Mx, My, py);
     FTE_LAUNCH(ctx, k_fft_x32, dim3(Kh, ng), fft_threads(px.m), sm_x, Hh, Mx, Kh, px, 0);
     int fb = (int)(((size_t)Mx * Kh + 255) / 256);
@@ -2099,11 +2099,11 @@ int fte_kspace_run(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, fte_info
         FTE_TRY(launch_spread_tiled(ctx, a, tb_s, wp, H, recs));
     } else if (a.nsrc > 0) {
         if (ng == 2) {
-            FTE_CUDA_TRY(cudaFuncSetAttribute(k_spread<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_pt));
+            FTE_CUDA_TRY(fte_smem_ceiling(k_spread<2>, (int)sm_pt));
             FTE_LAUNCH(ctx, k_spread<2>, pt_grid(ctx, a.nsrc), kPtThreads, sm_pt, a.psrc, a.f, a.nrm, a.wts, a.nsrc,
                        wp, H);
         } else {
-            FTE_CUDA_TRY(cudaFuncSetAttribute(k_spread<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_pt));
+            FTE_CUDA_TRY(fte_smem_ceiling(k_spread<4>, (int)sm_pt));
             FTE_LAUNCH(ctx, k_spread<4>, pt_grid(ctx, a.nsrc), kPtThreads, sm_pt, a.psrc, a.f, a.nrm, a.wts, a.nsrc,
                        wp, H);
         }
@@ -2114,9 +2114,9 @@ int fte_kspace_run(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, fte_info
     const bool fft_ff = ff && !long_x && !long_y;
     if (fft_ff) {
         float4* Hf = reinterpret_cast<float4*>(Hh);
-        FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_y_r2c_ff, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_y));
-        FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_y_c2r_ff, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_y));
-        FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_x_ff, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_x));
+        FTE_CUDA_TRY(fte_smem_ceiling(k_fft_y_r2c_ff, (int)sm_y));
+        FTE_CUDA_TRY(fte_smem_ceiling(k_fft_y_c2r_ff, (int)sm_y));
+        FTE_CUDA_TRY(fte_smem_ceiling(k_fft_x_ff, (int)sm_x));
         FTE_LAUNCH(ctx, k_fft_y_r2c_ff, dim3(Mx / 2, ngs), fft_threads(py.m), sm_y, (const double*)H, Hf, Mx, My, py);
         FTE_LAUNCH(ctx, k_fft_x_ff, dim3(Kh, ngs), fft_threads(px.m), sm_x, Hf, Mx, Kh, px, 0);
         int fb = (int)(((size_t)Mx * Kh + 255) / 256);
@@ -2146,7 +2146,7 @@ int fte_kspace_run(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, fte_info
         } else if (a.ntar > 0) {
             // the per-point gather reads FP64 grids
             FTE_LAUNCH(ctx, k_ff_join, ew_grid(ctx, 2LL * (long long)G), 256, 0, H, 2LL * (long long)G);
-            FTE_CUDA_TRY(cudaFuncSetAttribute(k_gather, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_pt));
+            FTE_CUDA_TRY(fte_smem_ceiling(k_gather, (int)sm_pt));
             FTE_LAUNCH(ctx, k_gather, pt_grid(ctx, a.ntar), kPtThreads, sm_pt, a.ptar, a.ntar, wp, (const double*)H,
                        (const double*)(H + G), scale, a.uk);
         }
@@ -2155,8 +2155,8 @@ int fte_kspace_run(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, fte_info
         return FTE_OK;
     }
     if (!long_y) {
-        FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_y_r2c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_y));
-        FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_y_c2r, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_y));
+        FTE_CUDA_TRY(fte_smem_ceiling(k_fft_y_r2c, (int)sm_y));
+        FTE_CUDA_TRY(fte_smem_ceiling(k_fft_y_c2r, (int)sm_y));
         FTE_LAUNCH(ctx, k_fft_y_r2c, dim3(Mx / 2, ngs), fft_threads(py.m), sm_y, (const double*)H, Hh, Mx, My, py);
     } else {
         const long long tot = (long long)ngs * (Mx / 2) * My;
@@ -2166,7 +2166,7 @@ int fte_kspace_run(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, fte_info
                    Mx, My, ngs);
     }
     if (!long_x) {
-        FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_x));
+        FTE_CUDA_TRY(fte_smem_ceiling(k_fft_x, (int)sm_x));
         FTE_LAUNCH(ctx, k_fft_x, dim3(Kh, ngs), fft_threads(px.m), sm_x, Hh, Mx, Kh, px, 0);
     } else {
         FTE_TRY(fte_long_fft(ctx, lx, Hh, cols, (long long)ngs * Kh, false, LS));
@@ -2194,7 +2194,7 @@ int fte_kspace_run(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, fte_info
         if (ff) FTE_LAUNCH(ctx, k_ff_split, ew_grid(ctx, 2LL * (long long)G), 256, 0, H, 2LL * (long long)G);
         FTE_TRY(launch_gather_tiled(ctx, a, tb_g, wp, H, scale));
     } else if (a.ntar > 0) {
-        FTE_CUDA_TRY(cudaFuncSetAttribute(k_gather, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_pt));
+        FTE_CUDA_TRY(fte_smem_ceiling(k_gather, (int)sm_pt));
         FTE_LAUNCH(ctx, k_gather, pt_grid(ctx, a.ntar), kPtThreads, sm_pt, a.ptar, a.ntar, wp, (const double*)H,
                    (const double*)(H + G), scale, a.uk);
     }
@@ -2350,8 +2350,8 @@ int fte_q_kspace_run(fte_context* ctx, WsCarver& wc, int q, const KspaceArgs& a,
     }
     // forward: ng grids
     if (!long_y) {
-        FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_y_r2c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_y));
-        FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_y_c2r, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_y));
+        FTE_CUDA_TRY(fte_smem_ceiling(k_fft_y_r2c, (int)sm_y));
+        FTE_CUDA_TRY(fte_smem_ceiling(k_fft_y_c2r, (int)sm_y));
         FTE_LAUNCH(ctx, k_fft_y_r2c, dim3(Mx / 2, ng), fft_threads(py.m), sm_y, (const double*)H, Hh, Mx, My, py);
     } else {
         FTE_LAUNCH(ctx, k_ly_pack_r2c, ew_grid(ctx, (long long)ng * (Mx / 2) * My), 256, 0, (const double*)H, S, Mx,
@@ -2361,7 +2361,7 @@ int fte_q_kspace_run(fte_context* ctx, WsCarver& wc, int q, const KspaceArgs& a,
                    Mx, My, ng);
     }
     if (!long_x) {
-        FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_x));
+        FTE_CUDA_TRY(fte_smem_ceiling(k_fft_x, (int)sm_x));
         FTE_LAUNCH(ctx, k_fft_x, dim3(Kh, ng), fft_threads(px.m), sm_x, Hh, Mx, Kh, px, 0);
     } else {
         FTE_TRY(fte_long_fft(ctx, lx, Hh, cols, (long long)ng * Kh, false, LS));
@@ -2605,7 +2605,7 @@ extern "C" int fte_slp_kspace_noalloc(const double* psrc, int64_t nsrc, const do
     double* H = base;                                           // 2 real grids
     double2* Hh = reinterpret_cast<double2*>(base + kNaGrid);   // 2 half spectra
     double2* tab = reinterpret_cast<double2*>(base + kNaGrid + kNaSpec);
-    FftDev py, px;
+    FftDev py{}, px{};
     if (!na_plan(My, tab, &py) || !na_plan(Mx, tab + 3 * kNaMaxFft, &px)) {
         fte_set_error("fte_slp_kspace_noalloc: FFT length beyond the fixed tables");
         return FTE_ERR_UNSUPPORTED;
@@ -2641,13 +2641,13 @@ extern "C" int fte_slp_kspace_noalloc(const double* psrc, int64_t nsrc, const do
         int64_t b = (n + kPtThreads - 1) / kPtThreads;
         return (int)(b < 1 ? 1 : (b > 4096 ? 4096 : b));
     };
-    // The dynamic shared-memory ceiling is a per-kernel attribute that other
-    // entries set to their own sizes; raise it to what these launches need.
-    FTE_CUDA_TRY(cudaFuncSetAttribute(k_spread<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_pt));
-    FTE_CUDA_TRY(cudaFuncSetAttribute(k_gather, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_pt));
-    FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_y_r2c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_y));
-    FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_y_c2r, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_y));
-    FTE_CUDA_TRY(cudaFuncSetAttribute(k_fft_x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_x));
+    // dynamic shared-memory ceilings: raised once per kernel and device and
+    // never lowered (shared with the other entries), checked against these sizes
+    FTE_CUDA_TRY(fte_smem_ceiling(k_spread<2>, (int)sm_pt));
+    FTE_CUDA_TRY(fte_smem_ceiling(k_gather, (int)sm_pt));
+    FTE_CUDA_TRY(fte_smem_ceiling(k_fft_y_r2c, (int)sm_y));
+    FTE_CUDA_TRY(fte_smem_ceiling(k_fft_y_c2r, (int)sm_y));
+    FTE_CUDA_TRY(fte_smem_ceiling(k_fft_x, (int)sm_x));
     if (nsrc > 0)
         NA_LAUNCH(k_spread<2>, blocks(nsrc), kPtThreads, sm_pt, stream, psrc, f, (const double*)nullptr,
                   (const double*)nullptr, nsrc, wp, H);

@@ -1195,13 +1195,13 @@ int near_launch_one(fte_context* ctx, NearParams p) {
         using C = NearCfg<true>;
         const int grid = p.nb < ctx->num_sms * C::grid_per_sm ? (p.nb > 0 ? p.nb : 1) : ctx->num_sms * C::grid_per_sm;
         FTE_CUDA_TRY(
-            cudaFuncSetAttribute(k_near<KIND, NV, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            fte_smem_ceiling(k_near<KIND, NV, true>, (int)smem));
         FTE_LAUNCH(ctx, (k_near<KIND, NV, true>), grid, C::threads, smem, p);
     } else {
         using C = NearCfg<false>;
         const int grid = p.nb < ctx->num_sms * C::grid_per_sm ? (p.nb > 0 ? p.nb : 1) : ctx->num_sms * C::grid_per_sm;
         FTE_CUDA_TRY(
-            cudaFuncSetAttribute(k_near<KIND, NV, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            fte_smem_ceiling(k_near<KIND, NV, false>, (int)smem));
         FTE_LAUNCH(ctx, (k_near<KIND, NV, false>), grid, C::threads, smem, p);
     }
     return FTE_OK;
@@ -1214,14 +1214,12 @@ int near_launch_batch(fte_context* ctx, bool ff, const unsigned char* plist_dev,
     if (ff) {
         using C = NearCfg<true>;
         const int grid = nitems < ctx->num_sms * C::grid_per_sm ? nitems : ctx->num_sms * C::grid_per_sm;
-        FTE_CUDA_TRY(cudaFuncSetAttribute(k_near_batch<KIND, NV, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)smem));
+        FTE_CUDA_TRY(fte_smem_ceiling(k_near_batch<KIND, NV, true>, (int)smem));
         FTE_LAUNCH(ctx, (k_near_batch<KIND, NV, true>), grid, C::threads, smem, plist_dev, items, nitems);
     } else {
         using C = NearCfg<false>;
         const int grid = nitems < ctx->num_sms * C::grid_per_sm ? nitems : ctx->num_sms * C::grid_per_sm;
-        FTE_CUDA_TRY(cudaFuncSetAttribute(k_near_batch<KIND, NV, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)smem));
+        FTE_CUDA_TRY(fte_smem_ceiling(k_near_batch<KIND, NV, false>, (int)smem));
         FTE_LAUNCH(ctx, (k_near_batch<KIND, NV, false>), grid, C::threads, smem, plist_dev, items, nitems);
     }
     return FTE_OK;

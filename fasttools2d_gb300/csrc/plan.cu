@@ -2,7 +2,7 @@
 // plans replayed as one CUDA graph.
 //
 // The reference recomputes everything on every call (cell list,
-// ewald_tools.cpp:37-110; windows, ewald_tools.cpp:150-229), which in an
+// ewald_tools.cpp:7-80; windows, ewald_tools.cpp:120-199), which in an
 // iterative solver (GMRES on a boundary integral equation) repeats all the
 // geometry work for every new density.  A plan does the density-independent
 // work once: wrapping, the parameter choice, the real-space cell list and the
@@ -292,6 +292,15 @@ extern "C" int fte_plan_create(fte_context* c, int kind, const double* xsrc, con
         fte_set_error("fte_plan_create: staging workspace too small");
         return FTE_ERR_ALLOC;
     }
+    FiniteSet fin;
+    for (const double* a : {dxs, dys, df1, df2, dn1, dn2, dw}) fin.add(a, nsrc);
+    fin.add(dxt, ntar);
+    fin.add(dyt, ntar);
+    st = fte_finite_launch(c, fin);
+    if (st) {
+        delete p;
+        return st;
+    }
     cudaMemsetAsync(acc, 0, 8 * sizeof(double), c->stream);
     if (nsrc > 0) k_plan_sumsq<<<grid_of(c, nsrc), 256, 0, c->stream>>>(df1, df2, dw, nsrc, acc);
     cudaMemcpyAsync(c->host_scalars, acc, sizeof(double), cudaMemcpyDeviceToHost, c->stream);
@@ -299,6 +308,11 @@ extern "C" int fte_plan_create(fte_context* c, int kind, const double* xsrc, con
         delete p;
         fte_set_error("fte_plan_create: %s", cudaGetErrorString(cudaGetLastError()));
         return FTE_ERR_CUDA;
+    }
+    st = fte_finite_result(c, "fte_plan_create");
+    if (st) {
+        delete p;
+        return st;
     }
     double Q = c->host_scalars[0] + 1.0;
     st = fte_choose_params_ex(kind, nsrc, ntar, Q, Lx, Ly, opt, &p->prm);
@@ -329,7 +343,7 @@ extern "C" int fte_plan_create(fte_context* c, int kind, const double* xsrc, con
                   fte_kspace_ws(kind, prm.form, prm.Mx, prm.My, nsrc, ntar) + 3 * ws_bytes(nv * (nsrc + 1), 8) +
                   ws_bytes(2 * nv * (nsrc + 1), 8) + ws_bytes(16 * nv, 8) + 2 * ws_bytes(nv * (ntar + 1), 16) +
                   p->kscratch_size + ffws + (1 << 16);
-    if (cudaMalloc(&p->mem, need) != cudaSuccess) {
+    if (fte_alloc_should_fail() || cudaMalloc(&p->mem, need) != cudaSuccess) {
         cudaGetLastError();
         delete p;
         fte_set_error("fte_plan_create: %zu bytes of device memory not available", need);

@@ -308,7 +308,7 @@ int q_near_launch(fte_context* ctx, QNearParams p) {
     const size_t smem = q_smem<KIND>(cap);
     int grid = p.nb < ctx->num_sms * 16 ? p.nb : ctx->num_sms * 16;
     if (grid < 1) grid = 1;
-    FTE_CUDA_TRY(cudaFuncSetAttribute(k_near_q<KIND, Q>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    FTE_CUDA_TRY(fte_smem_ceiling(k_near_q<KIND, Q>, (int)smem));
     FTE_LAUNCH(ctx, (k_near_q<KIND, Q>), grid, kQThreads, smem, p);
     return FTE_OK;
 }

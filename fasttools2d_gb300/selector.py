@@ -2,7 +2,7 @@
 
 No counterpart in the reference: its drivers take xi, the grid M, the window
 support P and the real-space cutoff from analytic error estimates
-(StokesSLP_ewald_2p.m:27-35,85-104; StokesDLP_ewald_2p.m:27-38,307-327).  This
+(StokesSLP_ewald_2p.m:27-35,85-104; StokesDLP_ewald_2p.m:27-38,105-125).  This
 module learns corrections to the tuned analytic choice of the mixed form
 (``choose_params(..., form=FORM_MIXED)``) from measured GPU times and errors:
 

@@ -14,7 +14,7 @@
  *   fte_stokes_dlp_ewald_2p <- StokesDLP_ewald_2p PeriodicEwald/src/matlab/StokesDLP_ewald_2p.m:1-163
  *   fte_choose_params       <- the drivers' parameter selection and find_xi/find_kinfb
  *                              (StokesSLP_ewald_2p.m:27-35,85-104,147-202;
- *                               StokesDLP_ewald_2p.m:27-38,307-327,373-427)
+ *                               StokesDLP_ewald_2p.m:27-38,105-125,171-224)
  *
  * Conventions (as the MEX gateways): point, density and normal arrays given
  * as one pointer are 2 x N column-major doubles, i.e. x/y interleaved
@@ -55,10 +55,20 @@ extern "C" {
 #define FTE_DEVICE_POINTERS 1u /* all array arguments are device pointers */
 
 /* arithmetic forms */
-#define FTE_FORM_PLAIN 0  /* FP64 everywhere (the drop-in) */
-#define FTE_FORM_MIXED 1  /* FP32 spread/FFT/filter/gather (compensated), FP64 near sums */
-/* fte_params.form only: spread and gather in float-float (pairs of FP32
- * numbers, ~48 bits), FP64 transforms and filter, FP64 near sums */
+/* fte_options.form: FTE_FORM_PLAIN = the drivers' parameters, FP64
+ * everywhere (the drop-in); FTE_FORM_MIXED = the tuned parameter choice with
+ * the cheapest arithmetic per stage that meets the tolerance (the precision
+ * form).  fte_params.form reports the k-space arithmetic of an evaluation:
+ *   FTE_FORM_PLAIN  FP64 spread, transforms, multiplier and gather;
+ *   FTE_FORM_MIXED  FP32 spread (Kahan-compensated), transforms and gather,
+ *                   the multiplier in FP64 (tol >= 1e-6 SLP, 2e-7 DLP);
+ *   FTE_FORM_FF     float-float (pairs of FP32 numbers, ~48 bits) spread,
+ *                   transforms, multiplier and gather (tol >= 1e-11).
+ * The real-space pairs of the mixed form are FP32 for pairs whose terms lie
+ * far below the tolerance, float-float for the others from tol 1e-11, and
+ * FP64 below (fte_options.near). */
+#define FTE_FORM_PLAIN 0
+#define FTE_FORM_MIXED 1
 #define FTE_FORM_FF 2
 
 /* fte_options.kspace (FTE_FORM_MIXED): the k-space arithmetic of the tuned
@@ -97,7 +107,7 @@ typedef struct {
     double w;       /* window half-width P*h/2 */
     double eta;     /* window shape (2 xi w / m)^2, m = 0.95 sqrt(pi P) */
     int form;       /* arithmetic of the k-space part: FTE_FORM_PLAIN (FP64), FTE_FORM_MIXED (FP32) or
-                       FTE_FORM_FF (float-float spread and gather) */
+                       FTE_FORM_FF (float-float spread, transforms, multiplier and gather) */
     int ts_spread;  /* k-space spread / gather tile sizes in grid nodes (plans; 0: the default rule) */
     int ts_gather;
 } fte_params;
@@ -178,7 +188,7 @@ int fte_choose_params(int kind, int64_t nsrc, int64_t ntar, const double* f1, co
 
 /* ---- plans: geometry reused across density vectors ------------------------ */
 /* No single counterpart in the reference, which recomputes the cell list
- * (PeriodicEwald/src/mex/common/ewald_tools.cpp:37-110) and the parameters
+ * (PeriodicEwald/src/mex/common/ewald_tools.cpp:7-80) and the parameters
  * (PeriodicEwald/src/matlab/StokesSLP_ewald_2p.m:85-104) on every call.  A
  * plan does the density-independent work of a driver call once: wrapping,
  * the parameter choice (from f1, f2, a representative density, and opt; the

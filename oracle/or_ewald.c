@@ -73,7 +73,7 @@ double or_expint_e1(double x) {
 /* ------------------------------------------------------------------------
  * MATLAB rat(x) with its default tolerance 1e-6*|x|: nearest-integer
  * continued-fraction expansion (the algorithm documented for rat).
- * Used by the drivers at StokesSLP_ewald_2p.m:85 / StokesDLP_ewald_2p.m:307.
+ * Used by the drivers at StokesSLP_ewald_2p.m:85 / StokesDLP_ewald_2p.m:105.
  * ---------------------------------------------------------------------- */
 static double or_matlab_round(double v) { return round(v); } /* half away from zero, as MATLAB */
 
@@ -111,7 +111,7 @@ static double or_matlab_mod(double a, double m) {
 }
 
 /* ------------------------------------------------------------------------
- * Cell list: ewald_tools.cpp:37-110.  Boxes are nside_x x nside_y, numbered
+ * Cell list: ewald_tools.cpp:7-80.  Boxes are nside_x x nside_y, numbered
  * box_y*nside_x + box_x; a counting sort keeps each box's points in input
  * order.
  * ---------------------------------------------------------------------- */
@@ -164,7 +164,7 @@ int or_assign(const double* psrc, const double* ptar, double Lx, double Ly, int 
 }
 
 /* ------------------------------------------------------------------------
- * First window node and in-cell offset: ewald_tools.cpp:116-144.
+ * First window node and in-cell offset: ewald_tools.cpp:86-114.
  * ---------------------------------------------------------------------- */
 void or_find_closest_node(double x, double y, double Lx, double Ly, double h, int P, int* mx, int* my, double* px,
                           double* py) {
@@ -181,7 +181,7 @@ void or_find_closest_node(double x, double y, double Lx, double Ly, double h, in
 }
 
 /* ------------------------------------------------------------------------
- * Gaussian spreading with fast Gaussian gridding: ewald_tools.cpp:150-229.
+ * Gaussian spreading with fast Gaussian gridding: ewald_tools.cpp:120-199.
  * Grid storage is column-major My x Mx: H[x*My + y].  As in the reference,
  * OpenMP threads take sources and serialise on one lock per grid column.
  * ---------------------------------------------------------------------- */
@@ -223,7 +223,7 @@ void or_spread(double* H1, double* H2, double* e1, const double* psrc, const dou
 }
 
 /* ------------------------------------------------------------------------
- * Gather with quadrature: ewald_tools.cpp:236-301.  Adds into
+ * Gather with quadrature: ewald_tools.cpp:206-271.  Adds into
  * output[total_components*k + component_number-1].
  * ---------------------------------------------------------------------- */
 void or_gather(const double* H, int total_components, int component_number, const double* e1, const double* ptar,
@@ -581,8 +581,8 @@ int or_dlp_kspace(const double* psrc, int Nsrc, const double* ptar, int Ntar, do
  * Parameter selection (Palsson & Tornberg 2019 estimates, Newton solves):
  *   SLP: StokesSLP_ewald_2p.m:27-35,85-104 with find_kinfb :147-173 and
  *        find_xi :178-202.  find_kinfb receives Lx twice (:96).
- *   DLP: StokesDLP_ewald_2p.m:27-38,307-327 with find_kinfb :373-399 and
- *        find_xi :404-427.  Its find_kinfb keeps MATLAB's left-to-right
+ *   DLP: StokesDLP_ewald_2p.m:27-38,105-125 with find_kinfb :171-197 and
+ *        find_xi :202-224.  Its find_kinfb keeps MATLAB's left-to-right
  *        evaluation of k*8*pi*Q*max(Lx,Ly)/Lx^3*Ly^3 (:379-381).
  * ---------------------------------------------------------------------- */
 static double or_slp_kf(double k, double Q, double Lx, double Ly, double xi, double tol) {
@@ -690,7 +690,7 @@ int or_choose_params(int kind, int nsrc, int ntar, const double* f1, const doubl
 }
 
 /* ------------------------------------------------------------------------
- * Drivers: StokesSLP_ewald_2p.m:74-136 and StokesDLP_ewald_2p.m:295-363.
+ * Drivers: StokesSLP_ewald_2p.m:74-136 and StokesDLP_ewald_2p.m:93-163.
  * The DLP driver's perturbation of n and f by 1e-60 on MATLAB releases
  * other than R2017a (:69-81) works around MATLAB returning real-valued FFT
  * arrays; it is not restated (the R2017a branch is followed).
@@ -753,7 +753,7 @@ int or_stokes_dlp_ewald_2p(const double* xsrc, const double* ysrc, int Nsrc, con
     int rc = or_dlp_real(ps, Nsrc, pt, Ntar, f, nn, o.xi, o.nside_x, o.nside_y, Lx, Ly, ur);
     if (!rc) rc = or_dlp_kspace(ps, Nsrc, pt, Ntar, o.xi, o.eta, f, nn, o.Mx, o.My, Lx, Ly, o.w, o.P, uk);
     if (!rc) {
-        /* zero mode, StokesDLP_ewald_2p.m:351-353, with the wrapped source coordinates */
+        /* zero mode, StokesDLP_ewald_2p.m:149-151, with the wrapped source coordinates */
         double zx = 0, zy = 0;
         for (int j = 0; j < Nsrc; j++) {
             double fn = f1[j] * n1[j] + f2[j] * n2[j];

@@ -9,10 +9,10 @@
  *
  * Every function restates a piece of annabroms/FastTools2D (paths relative
  * to that project):
- *   or_assign               PeriodicEwald/src/mex/common/ewald_tools.cpp:37-110
- *   or_find_closest_node    PeriodicEwald/src/mex/common/ewald_tools.cpp:116-144
- *   or_spread               PeriodicEwald/src/mex/common/ewald_tools.cpp:150-229
- *   or_gather               PeriodicEwald/src/mex/common/ewald_tools.cpp:236-301
+ *   or_assign               PeriodicEwald/src/mex/common/ewald_tools.cpp:7-80
+ *   or_find_closest_node    PeriodicEwald/src/mex/common/ewald_tools.cpp:86-114
+ *   or_spread               PeriodicEwald/src/mex/common/ewald_tools.cpp:120-199
+ *   or_gather               PeriodicEwald/src/mex/common/ewald_tools.cpp:206-271
  *   or_slp_real             PeriodicEwald/src/mex/StokesSLP/mex_stokes_slp_real.cpp:58-357
  *   or_slp_kspace           PeriodicEwald/src/mex/StokesSLP/mex_stokes_slp_kspace.cpp:7-215
  *   or_dlp_real             PeriodicEwald/src/mex/StokesDLP/mex_stokes_dlp_real.cpp:15-211

@@ -66,7 +66,7 @@ def test_config2_full_parts_match_oracle(gpu_ctx, cfg2, kind):
     else:
         our = po.dlp_real(ps, pt, f, n, p.xi, p.nside_x, p.nside_y, c["Lx"], c["Ly"])
         ouk = po.dlp_kspace(ps, pt, p.xi, p.eta, f, n, p.Mx, p.My, c["Lx"], c["Ly"], p.w, p.P)
-        # the drivers' zero mode (StokesDLP_ewald_2p.m:351-353) is part of uk:
+        # the drivers' zero mode (StokesDLP_ewald_2p.m:149-151) is part of uk:
         # sum over sources of (f . n) times the wrapped position, over Lx Ly
         fn = f[:, 0] * n[:, 0] + f[:, 1] * n[:, 1]
         ouk = ouk + (fn[:, None] * ps).sum(0) / (c["Lx"] * c["Ly"])

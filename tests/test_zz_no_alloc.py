@@ -53,11 +53,12 @@ def _call_noalloc(fn, case, stream):
     import torch
 
     ps, pt, xi, eta, f, Mx, My, Lx, Ly, w, P = case
-    dps = torch.tensor(ps, dtype=torch.float64, device="cuda")
+    dps = torch.tensor(ps, dtype=torch.float64, device="cuda").reshape(-1, 2)
     dpt = torch.tensor(pt, dtype=torch.float64, device="cuda")
-    df = torch.tensor(f, dtype=torch.float64, device="cuda")
+    df = torch.tensor(f, dtype=torch.float64, device="cuda").reshape(-1, 2)
     out = torch.full((len(pt), 2), float("nan"), dtype=torch.float64, device="cuda")
-    st = fn(dps.data_ptr(), len(ps), dpt.data_ptr(), len(pt), xi, eta, df.data_ptr(), Mx, My, Lx, Ly, w, P,
+    torch.cuda.synchronize()
+    st = fn(dps.data_ptr(), len(dps), dpt.data_ptr(), len(pt), xi, eta, df.data_ptr(), Mx, My, Lx, Ly, w, P,
             out.data_ptr(), stream)
     torch.cuda.synchronize()
     return st, out.cpu().numpy()
@@ -77,6 +78,39 @@ def test_noalloc_matches_allocating_entry(gpu_ctx):
         ref = ft.mex_stokes_slp_kspace(ps, pt, xi, eta, f, Mx, My, Lx, Ly, w, P, ctx=gpu_ctx)
         assert np.all(np.isfinite(out))
         assert rel_max(out, ref) <= TOL_FP64
+
+
+def test_noalloc_matches_reference_fixture(gpu_ctx):
+    """The p16 case (P = 16, a window half-width the drivers would not pick)
+    against the reference gateway's own output stored in the fixture."""
+    import torch
+
+    ft, fn = _entry()
+    case = _cases()[1]
+    st, out = _call_noalloc(fn, case, torch.cuda.current_stream().cuda_stream)
+    assert st == ft.FTE_OK, ft.lib().fte_last_error()
+    assert rel_max(out, load_golden("mex_slp_kspace_p16")["out"]) <= TOL_FP64
+
+
+def test_noalloc_on_a_new_stream_and_without_sources(gpu_ctx):
+    """A call on a freshly created stream (the grid clear, the transforms and
+    the gather are ordered on that stream), then a call with no sources after
+    it: the shared array still holds the previous grids, which the entry must
+    clear, so the result is exactly zero."""
+    import torch
+
+    ft, fn = _entry()
+    first = _cases()[0]
+    s = torch.cuda.Stream()
+    st, out = _call_noalloc(fn, first, s.cuda_stream)
+    assert st == ft.FTE_OK, ft.lib().fte_last_error()
+    ps, pt, xi, eta, f, Mx, My, Lx, Ly, w, P = first
+    ref = ft.mex_stokes_slp_kspace(ps, pt, xi, eta, f, Mx, My, Lx, Ly, w, P, ctx=gpu_ctx)
+    assert rel_max(out, ref) <= TOL_FP64
+    empty = (np.zeros((0, 2)), pt, xi, eta, np.zeros((0, 2)), Mx, My, Lx, Ly, w, P)
+    st, out = _call_noalloc(fn, empty, s.cuda_stream)
+    assert st == ft.FTE_OK, ft.lib().fte_last_error()
+    assert np.array_equal(out, np.zeros_like(out))
 
 
 def test_noalloc_rejects_grids_beyond_its_scratch(gpu_ctx):
