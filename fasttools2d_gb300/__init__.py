@@ -131,6 +131,7 @@ SIGNATURES = {
     "fte_q_kspace": (_i, [_vp, _i, _i, _vp, _i64, _vp, _i64, _vp, _vp, _d, _d, _i, _i, _d, _d, _d, _i, _vp, _u]),
     "fte_stokes_q_ewald_2p": (_i, [_vp, _i, _i, _vp, _vp, _i64, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _d, _d,
                                    C.POINTER(Options), _vp, _vp, _vp, C.POINTER(Info), _u]),
+    "fte_nn_sample": (_i, [_vp, _vp, _vp, _i64, _d, _d, _i, _vp, _u]),
     "fte_mlp_param_count": (_i, []),
     "fte_mlp_scratch_floats": (C.c_size_t, [_i]),
     "fte_mlp_forward": (_i, [_vp, _vp, _i, _vp, _vp]),
@@ -447,6 +448,22 @@ def choose_params(kind, f1, f2, ntar, Lx, Ly, P=None, Nb=None, tol=1e-16, **kw) 
     _check(lib().fte_choose_params(int(kind), len(f1), int(ntar), f1.ctypes.data, f2.ctypes.data, float(Lx),
                                    float(Ly), C.byref(opt), C.byref(prm)))
     return prm
+
+
+def nn_sample(xsrc, ysrc, Lx, Ly, nsample=2048, ctx: Context | None = None):
+    """Distances from a deterministic sample of the sources (every stride-th,
+    stride = max(1, N // nsample)) to their nearest other source in the
+    periodic box, computed on the GPU from a device cell list
+    (``fte_nn_sample``).  Host or CUDA arrays; returns a numpy array."""
+    ctx = ctx or default_context()
+    A = _Args()
+    px, n = A.arr(xsrc, 1)
+    py, _ = A.arr(ysrc, 1)
+    stride = max(1, n // nsample)
+    ns = min(nsample, (n + stride - 1) // stride)
+    out, po = A.out((ns,))
+    _check(lib().fte_nn_sample(ctx.h, px, py, n, float(Lx), float(Ly), int(nsample), po, A.flags))
+    return out.cpu().numpy() if hasattr(out, "cpu") else out
 
 
 # ---- plans and batches -----------------------------------------------------------

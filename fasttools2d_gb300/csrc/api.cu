@@ -835,6 +835,38 @@ void pick_grid(int A, int B, int kinf, int* Mx, int* My) {
     *My = B * bt;
 }
 
+// Grid with its own step per axis (boxes whose aspect ratio is no small
+// rational): each side resolves the same wave number, Mx >= 2 kx, My >= 2 ky
+// (kx = Lx k / 2 pi, ky = Ly k / 2 pi), both even; among the even sizes up to
+// a short span above those bounds, the pair with the least transform work.
+void pick_grid_axes(double kx, double ky, int* Mx, int* My) {
+    auto lo = [](double k) {
+        int m = (int)std::ceil(2.0 * k - 1e-9);
+        if (m < 2) m = 2;
+        return m + (m & 1);
+    };
+    const int x0 = lo(kx), y0 = lo(ky);
+    auto span = [](int m) {
+        int s = m / 8 > 16 ? m / 8 : 16;
+        return s > 128 ? 128 : s;
+    };
+    double best = 1e300;
+    int bx = x0, by = y0;
+    for (int mx = x0; mx <= x0 + span(x0); mx += 2) {
+        const double cx = line_cost(mx);
+        for (int my = y0; my <= y0 + span(y0); my += 2) {
+            const double w = (double)mx * my * (cx + line_cost(my));
+            if (w < best) {
+                best = w;
+                bx = mx;
+                by = my;
+            }
+        }
+    }
+    *Mx = bx;
+    *My = by;
+}
+
 }  // namespace
 
 // Unit costs (seconds) of the cost model, fitted on GB300 to stage times of
@@ -894,7 +926,17 @@ static int choose_params_tuned(int kind, int64_t nsrc, int64_t ntar, double Q, d
         }
     }
     const int A = o->A, B = o->B;
+    // A box whose aspect ratio is a small rational A / B keeps the drivers'
+    // geometry: square cells (nside = a (A, B)) and equal grid steps
+    // (M = t (A, B)).  Any other box -- Lx / Ly irrational, or a ratio whose
+    // rat() terms are large, for which the drivers' cell list and A-fold grid
+    // explode -- gets cells of nearly equal sides (Lx / rc0 and Ly / rc0
+    // rounded; the cutoff is the shorter side) and a grid step per axis.
+    const bool rational = A <= 16 && B <= 16 && std::fabs(Lx * B - Ly * A) <= 1e-12 * Lx * B;
     const int a0 = o->nside_x / A;
+    // cells holding the drivers' Nb points on average
+    const double rc_ref = std::sqrt(Lx * Ly * o->Nb / std::fmax(1.0, (double)nsrc + (double)ntar));
+    int last_nsx = -1, last_nsy = -1;
     const double area = Lx * Ly;
     const int ng = kind == FTE_KIND_SLP ? 2 : 4;
     const double nfft = kind == FTE_KIND_SLP ? 2.0 : 3.0;
@@ -907,12 +949,29 @@ static int choose_params_tuned(int kind, int64_t nsrc, int64_t ntar, double Q, d
     // guess takes tens of iterations per candidate)
     double prev_xr = 0, prev_k = 0, prev_xi = 0;
     for (int step = -12; step <= 40; step++) {
-        int a = (int)std::lround(a0 * std::pow(1.1, step));
-        if (opt && opt->nside_x > 0) a = opt->nside_x / A;
-        if (a < 1 || a == last_a) continue;
-        last_a = a;
-        int nsx = a * A, nsy = a * B;
-        double rc = Lx / nsx;
+        int nsx, nsy;
+        if (rational) {
+            int a = (int)std::lround(a0 * std::pow(1.1, step));
+            if (opt && opt->nside_x > 0) a = opt->nside_x / A;
+            if (a < 1 || a == last_a) continue;
+            last_a = a;
+            nsx = a * A;
+            nsy = a * B;
+        } else {
+            const double rc0 = rc_ref * std::pow(1.1, -step);
+            nsx = (int)std::lround(Lx / rc0);
+            nsy = (int)std::lround(Ly / rc0);
+            if (opt && opt->nside_x > 0) {
+                nsx = opt->nside_x;
+                nsy = opt->nside_y > 0 ? opt->nside_y : (int)std::lround(Ly * nsx / Lx);
+            }
+            if (nsx < 1) nsx = 1;
+            if (nsy < 1) nsy = 1;
+            if ((nsx == last_nsx && nsy == last_nsy) || (double)nsx * nsy > 1e8) continue;
+            last_nsx = nsx;
+            last_nsy = nsy;
+        }
+        double rc = rational ? Lx / nsx : std::fmin(Lx / nsx, Ly / nsy);
         // (10 % below the scaled root: the iteration then enters the
         // convergence band from the same side as from the drivers' start)
         double xi = (opt && opt->xi > 0) ? opt->xi : xi_estimate(kind, Q, Lx, Ly, rc, tol_e, 0.9 * prev_xr / rc);
@@ -923,10 +982,13 @@ static int choose_params_tuned(int kind, int64_t nsrc, int64_t ntar, double Q, d
         prev_xi = xi;
         int kinf = (int)std::round(Lx * kr / (2 * FTE_PI));
         int Mx, My;
-        pick_grid(A, B, kinf, &Mx, &My);
+        if (rational)
+            pick_grid(A, B, kinf, &Mx, &My);
+        else
+            pick_grid_axes(Lx * kr / (2 * FTE_PI), Ly * kr / (2 * FTE_PI), &Mx, &My);
         if (opt && opt->Mx > 0) Mx = opt->Mx;
         if (opt && opt->My > 0) My = opt->My;
-        if (std::fabs(Lx / Mx - Ly / My) > 1e-12 * (Lx / Mx)) continue;
+        if (rational && std::fabs(Lx / Mx - Ly / My) > 1e-12 * (Lx / Mx)) continue;
         if ((double)Mx * My > 4.0e8) continue;  // 4 grids of 4e8 nodes: 13 GB
         if (P + 1 > Mx || P + 1 > My) continue;
         // k-space arithmetic: the cheapest the tolerance allows (FP32 only
@@ -980,11 +1042,14 @@ static int choose_params_tuned(int kind, int64_t nsrc, int64_t ntar, double Q, d
             bestp.My = My;
             double m = 0.95 * std::sqrt(FTE_PI * P);
             bestp.w = P * Lx / Mx / 2;
-            bestp.eta = (2 * xi * bestp.w / m) * (2 * xi * bestp.w / m);
+            // one Gaussian shape for both axes, set by the narrower support
+            const double wmin = rational ? bestp.w : P * std::fmin(Lx / Mx, Ly / My) / 2;
+            bestp.eta = (2 * xi * wmin / m) * (2 * xi * wmin / m);
             best_form = kf;
         }
         if (opt && opt->nside_x > 0) break;
     }
+    (void)last_a;
     if (best >= 1e300) {
         fte_set_error("no tuned parameters within the grid limits (%d x %d boxes)", o->nside_x, o->nside_y);
         return FTE_ERR_UNSUPPORTED;
@@ -1152,7 +1217,11 @@ int check_real_params(double xi, int nsx, int nsy) {
     return FTE_OK;
 }
 
-int check_kspace_params(double xi, double eta, int Mx, int My, double Lx, double Ly, double w, int P) {
+// equal_steps: the reference's requirement Lx / Mx = Ly / My (gateways and
+// the drivers' form); the mixed form's tuned choice may give each axis its own
+// step
+int check_kspace_params(double xi, double eta, int Mx, int My, double Lx, double Ly, double w, int P,
+                        bool equal_steps = true) {
     if (!(xi > 0) || !std::isfinite(xi) || !(eta > 0) || !std::isfinite(eta) || !std::isfinite(w)) {
         fte_set_error("xi, eta must be positive and w finite (xi=%g, eta=%g, w=%g)", xi, eta, w);
         return FTE_ERR_INVALID;
@@ -1167,8 +1236,15 @@ int check_kspace_params(double xi, double eta, int Mx, int My, double Lx, double
     }
     // P + 1 > M is allowed: the window then wraps around the periodic grid
     // more than once, as it does in the reference.
+    if ((double)Mx * (double)My > 2147483648.0) {
+        // e.g. the drivers' grid (A M, B M) of a box whose aspect ratio has
+        // large rat() terms: the reference cannot hold it either
+        fte_set_error("grid of %d x %d nodes exceeds 2^31 nodes (a box whose aspect ratio Lx/Ly is no small "
+                      "rational needs the mixed form's tuned choice)", Mx, My);
+        return FTE_ERR_UNSUPPORTED;
+    }
     double hx = Lx / Mx, hy = Ly / My;
-    if (std::fabs(hx - hy) > 1e-12 * std::fmax(hx, hy)) {
+    if (equal_steps && std::fabs(hx - hy) > 1e-12 * std::fmax(hx, hy)) {
         fte_set_error("grid spacing must be equal in x and y (Lx/Mx=%.17g, Ly/My=%.17g)", hx, hy);
         return FTE_ERR_INVALID;
     }
@@ -1558,7 +1634,7 @@ static int ewald_entry(fte_context* c, int kind, const double* xsrc, const doubl
     else
         FTE_TRY(choose_params_q(kind, nsrc, ntar, Q, Lx, Ly, opt, &prm));
     FTE_TRY(check_real_params(prm.xi, prm.nside_x, prm.nside_y));
-    FTE_TRY(check_kspace_params(prm.xi, prm.eta, prm.Mx, prm.My, Lx, Ly, prm.w, prm.P));
+    FTE_TRY(check_kspace_params(prm.xi, prm.eta, prm.Mx, prm.My, Lx, Ly, prm.w, prm.P, opt->form != FTE_FORM_MIXED));
     // second workspace: cell list, grids and outputs (the staged point data stays in the first)
     size_t need = fte_cells_ws(nsrc, ntar, prm.nside_x * prm.nside_y) +
                   fte_kspace_ws(kind, prm.form, prm.Mx, prm.My, nsrc, ntar) + ws_bytes(2 * (ntar + 1), 8) * 3 +
@@ -1569,6 +1645,7 @@ static int ewald_entry(fte_context* c, int kind, const double* xsrc, const doubl
     if (ntar > 0) {
         CellList cl;
         FTE_TRY(fte_cells_build(c, wc2, kind, ps, nsrc, pt, ntar, pf, pn, dw, prm.nside_x, prm.nside_y, Lx, Ly, &cl));
+        if (opt->form == FTE_FORM_MIXED) cl.cutoffsq = fte_tuned_cutoffsq(prm, Lx, Ly);
         FTE_TRY(fte_record(c, 6));
         // the mixed form evaluates the pairs whose terms are far below the
         // tolerance in FP32 and the other pairs with x >= 1 in float-float

@@ -118,13 +118,13 @@ __global__ void k_scatter_tar(const double* __restrict__ p, int64_t n, const int
 // of a half-warp, which read the region at those rows' offsets, mostly hit
 // distinct shared-memory banks (8-byte values).  The order is a heuristic:
 // the node it assumes ignores the tie-break of FindClosestNode.
-__global__ void k_tile_assign(const double* __restrict__ p, int64_t n, double Lx, double Ly, double h, int ts,
-                              int ntx, int nty, int* __restrict__ tile, int* __restrict__ rank,
+__global__ void k_tile_assign(const double* __restrict__ p, int64_t n, double Lx, double Ly, double hx, double hy,
+                              int ts, int ntx, int nty, int* __restrict__ tile, int* __restrict__ rank,
                               int* __restrict__ counts, int W, int* __restrict__ counts16) {
-    const double lhx = __dmul_rn(Lx, 0.5), lhy = __dmul_rn(Ly, 0.5), rh = __drcp_rn(h);
+    const double lhx = __dmul_rn(Lx, 0.5), lhy = __dmul_rn(Ly, 0.5), rhx = __drcp_rn(hx), rhy = __drcp_rn(hy);
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        double ax = floor(fte_div_rcp(__dadd_rn(p[2 * i], lhx), h, rh));
-        double ay = floor(fte_div_rcp(__dadd_rn(p[2 * i + 1], lhy), h, rh));
+        double ax = floor(fte_div_rcp(__dadd_rn(p[2 * i], lhx), hx, rhx));
+        double ay = floor(fte_div_rcp(__dadd_rn(p[2 * i + 1], lhy), hy, rhy));
         ax = fmin(fmax(ax, 0.0), (double)(ntx * ts - 1));
         ay = fmin(fmax(ay, 0.0), (double)(nty * ts - 1));
         int tx = min((int)ax / ts, ntx - 1), ty = min((int)ay / ts, nty - 1);
@@ -261,8 +261,8 @@ size_t fte_tiles_ws(int64_t n, int ntiles) {
            4 * ws_bytes((size_t)(ntiles + 1) / 4096 + 8, sizeof(int)) + 4096;
 }
 
-int fte_tiles_build(fte_context* ctx, WsCarver& wc, const double* p, int64_t n, double Lx, double Ly, double h,
-                    int ts, int ntx, int nty, TileBins* out, int region_w) {
+int fte_tiles_build(fte_context* ctx, WsCarver& wc, const double* p, int64_t n, double Lx, double Ly, double hx,
+                    double hy, int ts, int ntx, int nty, TileBins* out, int region_w) {
     int nt = ntx * nty;
     out->ntx = ntx;
     out->nty = nty;
@@ -279,8 +279,8 @@ int fte_tiles_build(fte_context* ctx, WsCarver& wc, const double* p, int64_t n, 
     if (cnt16) FTE_CUDA_TRY(cudaMemsetAsync(cnt16, 0, sizeof(int) * 16 * (size_t)nt, ctx->stream));
     int maxb = ctx->num_sms * 8;
     if (n > 0)
-        FTE_LAUNCH(ctx, k_tile_assign, grid_for(n, 256, maxb), 256, 0, p, n, Lx, Ly, h, ts, ntx, nty, tile, rank,
-                   cnt, region_w, cnt16);
+        FTE_LAUNCH(ctx, k_tile_assign, grid_for(n, 256, maxb), 256, 0, p, n, Lx, Ly, hx, hy, ts, ntx, nty, tile,
+                   rank, cnt, region_w, cnt16);
     FTE_TRY(fte_scan_exclusive(ctx, wc, cnt, out->off, nt + 1));
     if (n > 0)
         FTE_LAUNCH(ctx, k_tile_scatter, grid_for(n, 256, maxb), 256, 0, n, (const int*)tile, (const int*)rank,

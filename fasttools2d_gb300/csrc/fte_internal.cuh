@@ -242,24 +242,26 @@ __device__ __forceinline__ double fte_div_rcp(double x, double d, double rd) {
 }
 
 // First window node (mx, my) and in-cell offsets (px, py) of a point: the
-// reference's FindClosestNode (PeriodicEwald/src/mex/common/ewald_tools.cpp:86-114).
-// Written with explicitly rounded operations so that no multiply-add is fused:
-// the tie-break below depends on the exact rounding of each step (the
-// quotients by h are the IEEE quotients, formed from rh = RN(1/h); halving
-// is exact).
-__device__ __forceinline__ void fte_closest_node(double x, double y, double Lx, double Ly, double h, double rh, int P,
-                                                 int* mx, int* my, double* px, double* py) {
+// reference's FindClosestNode (PeriodicEwald/src/mex/common/ewald_tools.cpp:86-114),
+// with a grid step per axis (hx = Lx/Mx, hy = Ly/My; the reference has one h,
+// and hx = hy reproduces it exactly).  Written with explicitly rounded
+// operations so that no multiply-add is fused: the tie-break below depends on
+// the exact rounding of each step (the quotients by h are the IEEE quotients,
+// formed from rh = RN(1/h); halving is exact).
+__device__ __forceinline__ void fte_closest_node(double x, double y, double Lx, double Ly, double hx, double rhx,
+                                                 double hy, double rhy, int P, int* mx, int* my, double* px,
+                                                 double* py) {
     const double TOL = 1e-13;
-    double qx = fte_div_rcp(x, h, rh), qy = fte_div_rcp(y, h, rh);
-    double ppx = __dsub_rn(x, __dmul_rn(h, floor(qx)));
-    double ppy = __dsub_rn(y, __dmul_rn(h, floor(qy)));
+    double qx = fte_div_rcp(x, hx, rhx), qy = fte_div_rcp(y, hy, rhy);
+    double ppx = __dsub_rn(x, __dmul_rn(hx, floor(qx)));
+    double ppy = __dsub_rn(y, __dmul_rn(hy, floor(qy)));
     double lhx = __dmul_rn(Lx, 0.5), lhy = __dmul_rn(Ly, 0.5);
-    double ax = fte_div_rcp(__dadd_rn(x, lhx), h, rh), ay = fte_div_rcp(__dadd_rn(y, lhy), h, rh);
+    double ax = fte_div_rcp(__dadd_rn(x, lhx), hx, rhx), ay = fte_div_rcp(__dadd_rn(y, lhy), hy, rhy);
     int half = P / 2;
     int ix = (int)__dsub_rn(floor(ax), (double)half);
     int iy = (int)__dsub_rn(floor(ay), (double)half);
-    if (fabs(ppx) < TOL || fabs(__dsub_rn(ppx, h)) < TOL) ppx = 0;
-    if (fabs(ppy) < TOL || fabs(__dsub_rn(ppy, h)) < TOL) ppy = 0;
+    if (fabs(ppx) < TOL || fabs(__dsub_rn(ppx, hx)) < TOL) ppx = 0;
+    if (fabs(ppy) < TOL || fabs(__dsub_rn(ppy, hy)) < TOL) ppy = 0;
     if (ppx == 0 && remainder(__dsub_rn(ax, (double)half), 1.0) < 0) ix++;
     if (ppy == 0 && remainder(__dsub_rn(ay, (double)half), 1.0) < 0) iy++;
     *mx = ix;
@@ -315,7 +317,22 @@ struct CellList {
     long long qstride;  // distance between density vectors in q0..q2 (0: one vector)
     int* sidx;          // original index of each sorted source (plans only; may be null)
     int64_t nsrc = 0;   // sources
+    // real-space cutoff squared; 0: the reference's Lx Ly / (nsx nsy) (the
+    // square of the side of square cells).  The tuned choice of a box with an
+    // irrational aspect ratio has nearly square cells and sets the square of
+    // the shorter side, so that the 3 x 3 neighbourhood covers the cutoff disc.
+    double cutoffsq = 0.0;
 };
+
+// Cutoff squared of a tuned parameter choice whose cells have unequal sides
+// (boxes with an irrational aspect ratio): the square of the shorter side; 0
+// (the reference's Lx Ly / (nsx nsy)) for square cells.
+inline double fte_tuned_cutoffsq(const fte_params& p, double Lx, double Ly) {
+    const double bx = Lx / p.nside_x, by = Ly / p.nside_y;
+    if (std::fabs(bx - by) <= 1e-12 * std::fmax(bx, by)) return 0.0;
+    const double r = std::fmin(bx, by);
+    return r * r;
+}
 
 size_t fte_cells_ws(int64_t nsrc, int64_t ntar, int nb);
 int fte_cells_build(fte_context* ctx, WsCarver& wc, int kind, const double* psrc, int64_t nsrc, const double* ptar,
@@ -332,7 +349,8 @@ struct TileBins {
 size_t fte_tiles_ws(int64_t n, int ntiles);
 // region_w > 0: order each tile's points for the tiled gathers (staged
 // region rows of region_w nodes; see k_tile_assign)
-int fte_tiles_build(fte_context* ctx, WsCarver& wc, const double* p, int64_t n, double Lx, double Ly, double h,
+int fte_tiles_build(fte_context* ctx, WsCarver& wc, const double* p, int64_t n, double Lx, double Ly, double hx,
+                    double hy,
                     int ts, int ntx, int nty, TileBins* out, int region_w = 0);
 
 // ff: float-float pairs, with ffmem scratch of fte_near_ff_ws(kind, 1, nsrc)

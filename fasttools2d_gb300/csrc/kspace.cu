@@ -36,11 +36,24 @@ namespace {
 
 constexpr int kPtThreads = 128;
 
+// Window geometry.  h, rh, w belong to the x axis (h = Lx / Mx, w = P h / 2
+// as the drivers choose it), hy, rhy, wy to the y axis.  The reference has
+// one step (hx = hy, checked by its drivers); the tuned choice for boxes whose
+// aspect ratio is not a small rational gives each axis its own step, and then
+// aniso = 1: the window keeps one Gaussian shape eta (isotropic in physical
+// space, the filter deconvolves it) and each axis its own table e1 of
+// exp(-2 xi^2/eta h^2 j^2) and its support half-width P h / 2.
 struct WinParams {
     double Lx, Ly, h, xi, eta, w;
     double rh;  // RN(1 / h)
     int P, Mx, My;
+    double hy, rhy, wy;
+    int aniso;
 };
+
+// doubles (or float2) of the e1 table(s) in shared memory: one table padded
+// to an even length, two when the axes' steps differ
+__host__ __device__ inline int e1_len(int P, int aniso) { return (aniso ? 2 : 1) * ((P + 2) & ~1); }
 
 // per-point window factors, as in ewald_tools.cpp:152-160 / 226-232
 struct Win {
@@ -51,22 +64,30 @@ struct Win {
 __device__ __forceinline__ Win window_of(double x, double y, const WinParams& wp) {
     Win o;
     double px, py;
-    fte_closest_node(x, y, wp.Lx, wp.Ly, wp.h, wp.rh, wp.P, &o.mx, &o.my, &px, &py);
+    fte_closest_node(x, y, wp.Lx, wp.Ly, wp.h, wp.rh, wp.hy, wp.rhy, wp.P, &o.mx, &o.my, &px, &py);
     double t = -2 * wp.xi * wp.xi / wp.eta;
     o.ex = exp(t * (px * px + py * py + 2 * wp.w * px));
-    o.e4y = exp(2 * t * wp.w * py);
+    o.e4y = exp(2 * t * wp.wy * py);
     o.e3x = exp(-2 * t * wp.h * px);
-    o.e3y = exp(-2 * t * wp.h * py);
+    o.e3y = exp(-2 * t * wp.hy * py);
     return o;
 }
 
-// e1[j] = exp(-2 xi^2/eta h^2 (j - P/2)^2)   (ewald_tools.cpp:125-127)
+// e1[j] = exp(-2 xi^2/eta h^2 (j - P/2)^2)   (ewald_tools.cpp:125-127); with
+// aniso the y axis's table follows at e1 + (P + 2 & ~1)
 __device__ __forceinline__ void load_e1(double* e1, const WinParams& wp) {
     double t0 = -2 * wp.xi * wp.xi / wp.eta * wp.h * wp.h;
+    double t0y = -2 * wp.xi * wp.xi / wp.eta * wp.hy * wp.hy;
+    const int P1e = (wp.P + 2) & ~1;
     for (int j = threadIdx.x; j <= wp.P; j += blockDim.x) {
         int jj = j - wp.P / 2;
         e1[j] = exp(t0 * jj * jj);
+        if (wp.aniso) e1[P1e + j] = exp(t0y * jj * jj);
     }
+}
+template <typename T>
+__device__ __forceinline__ const T* e1y_of(const T* e1, const WinParams& wp) {
+    return wp.aniso ? e1 + ((wp.P + 2) & ~1) : e1;
 }
 
 // ---- spread: one thread per source, FP64 atomics into the global grids ------
@@ -77,8 +98,9 @@ __global__ void __launch_bounds__(kPtThreads) k_spread(const double* __restrict_
     extern __shared__ double sh[];
     double* e1 = sh;
     const int P1 = wp.P + 1;
-    double* wyb = e1 + ((P1 + 1) & ~1) + threadIdx.x * P1;
+    double* wyb = e1 + e1_len(wp.P, wp.aniso) + threadIdx.x * P1;
     load_e1(e1, wp);
+    const double* e1y = e1y_of(e1, wp);
     __syncthreads();
     const size_t G = (size_t)wp.Mx * wp.My;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -104,7 +126,7 @@ __global__ void __launch_bounds__(kPtThreads) k_spread(const double* __restrict_
         // y factors e1[y] e3y^y
         double ey = 1.0;
         for (int j = 0; j < P1; j++) {
-            wyb[j] = ey * e1[j];
+            wyb[j] = ey * e1y[j];
             ey *= wn.e3y;
         }
         bool ywrap = !(wn.my >= 0 && wn.my + wp.P < wp.My);
@@ -134,15 +156,16 @@ __global__ void __launch_bounds__(kPtThreads) k_gather(const double* __restrict_
     extern __shared__ double sh[];
     double* e1 = sh;
     const int P1 = wp.P + 1;
-    double* wyb = e1 + ((P1 + 1) & ~1) + threadIdx.x * P1;
+    double* wyb = e1 + e1_len(wp.P, wp.aniso) + threadIdx.x * P1;
     load_e1(e1, wp);
+    const double* e1y = e1y_of(e1, wp);
     __syncthreads();
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         double x = p[2 * i], y = p[2 * i + 1];
         Win wn = window_of(x, y, wp);
         double ey = 1.0;
         for (int j = 0; j < P1; j++) {
-            wyb[j] = ey * e1[j];
+            wyb[j] = ey * e1y[j];
             ey *= wn.e3y;
         }
         bool ywrap = !(wn.my >= 0 && wn.my + wp.P < wp.My);
@@ -201,8 +224,9 @@ __global__ void __launch_bounds__(kTileThreads) k_spread_tiled(const double* __r
     const int P1 = wp.P + 1, W = tile_region(ts, wp.P), WW = W * W;
     double* buf = sh;
     double* e1 = buf + NG * WW;
-    double* wyb = e1 + ((P1 + 1) & ~1) + threadIdx.x * P1;
+    double* wyb = e1 + e1_len(wp.P, wp.aniso) + threadIdx.x * P1;
     load_e1(e1, wp);
+    const double* e1y = e1y_of(e1, wp);
     const size_t G = (size_t)wp.Mx * wp.My;
     for (int tile = blockIdx.x; tile < ntx * nty; tile += gridDim.x) {
         const int k0 = toff[tile], k1 = toff[tile + 1];
@@ -232,7 +256,7 @@ __global__ void __launch_bounds__(kTileThreads) k_spread_tiled(const double* __r
             }
             double ey = 1.0;
             for (int j = 0; j < P1; j++) {
-                wyb[j] = ey * e1[j];
+                wyb[j] = ey * e1y[j];
                 ey *= wn.e3y;
             }
             const int lx = wn.mx - ox, ly = wn.my - oy;
@@ -300,11 +324,12 @@ __global__ void __launch_bounds__(kColThreads) k_spread_cols(int mode, const dou
     const int P1 = wp.P + 1, W = tile_region(ts, wp.P), WW = W * W;
     const int P1e = (P1 + 1) & ~1;
     double* buf = sh;                     // 2 * WW
-    double* e1 = buf + 2 * WW;            // P1e
-    double* fw = e1 + P1e;                // kColChunk * 2 * P1
+    double* e1 = buf + 2 * WW;            // e1_len (P1e, or 2 P1e with aniso)
+    double* fw = e1 + e1_len(wp.P, wp.aniso);  // kColChunk * 2 * P1
     double* wy = fw + kColChunk * 2 * P1; // kColChunk * P1
     int* org = reinterpret_cast<int*>(wy + kColChunk * P1);  // kColChunk * 2 (lx, ly; lx < 0: global path)
     load_e1(e1, wp);
+    const double* e1y = e1y_of(e1, wp);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     constexpr int nw = kColWarps;
     for (int tile = blockIdx.x; tile < ntx * nty; tile += gridDim.x) {
@@ -335,7 +360,7 @@ __global__ void __launch_bounds__(kColThreads) k_spread_cols(int mode, const dou
                 }
                 double ey = 1.0;
                 for (int j = 0; j < P1; j++) {
-                    wy[s * P1 + j] = ey * e1[j];
+                    wy[s * P1 + j] = ey * e1y[j];
                     ey *= wn.e3y;
                 }
                 double ex = wn.ex * wn.e4y;
@@ -393,9 +418,9 @@ __global__ void __launch_bounds__(kColThreads) k_spread_cols(int mode, const dou
     }
 }
 
-size_t spread_cols_smem(int ts, int P) {
+size_t spread_cols_smem(int ts, int P, int aniso = 0) {
     const int P1 = P + 1, W = tile_region(ts, P);
-    return (size_t)(2 * W * W + ((P1 + 1) & ~1) + kColChunk * 3 * P1) * sizeof(double) + kColChunk * 2 * sizeof(int);
+    return (size_t)(2 * W * W + e1_len(P, aniso) + kColChunk * 3 * P1) * sizeof(double) + kColChunk * 2 * sizeof(int);
 }
 
 __global__ void __launch_bounds__(kTileThreads) k_gather_tiled(const double* __restrict__ p,
@@ -409,8 +434,9 @@ __global__ void __launch_bounds__(kTileThreads) k_gather_tiled(const double* __r
     double* r0 = sh;
     double* r1 = r0 + WW;
     double* e1 = r1 + WW;
-    double* wyb = e1 + ((P1 + 1) & ~1) + threadIdx.x * P1;
+    double* wyb = e1 + e1_len(wp.P, wp.aniso) + threadIdx.x * P1;
     load_e1(e1, wp);
+    const double* e1y = e1y_of(e1, wp);
     for (int tile = blockIdx.x; tile < ntx * nty; tile += gridDim.x) {
         const int k0 = toff[tile], k1 = toff[tile + 1];
         if (k0 == k1) continue;
@@ -428,7 +454,7 @@ __global__ void __launch_bounds__(kTileThreads) k_gather_tiled(const double* __r
             Win wn = window_of(p[2 * i], p[2 * i + 1], wp);
             double ey = 1.0;
             for (int j = 0; j < P1; j++) {
-                wyb[j] = ey * e1[j];
+                wyb[j] = ey * e1y[j];
                 ey *= wn.e3y;
             }
             const int lx = wn.mx - ox, ly = wn.my - oy;
@@ -1018,18 +1044,19 @@ size_t tile_budget(const fte_context* ctx) {
 // FP32 and the columns in FP64.  Filter multipliers are evaluated in FP64 and
 // applied to the FP32 spectra.
 // ===========================================================================
-__device__ __forceinline__ void win32(double pp, const WinParams& wp, float* out) {
+// h: the axis's grid step (wp.h along x, wp.hy along y)
+__device__ __forceinline__ void win32(double pp, double h, const WinParams& wp, float* out) {
     const double t = -2 * wp.xi * wp.xi / wp.eta;
     const int P1 = wp.P + 1;
     for (int a = 0; a < P1; a++) {
-        double d = fma((double)(a - wp.P / 2), wp.h, -pp);
+        double d = fma((double)(a - wp.P / 2), h, -pp);
         out[a] = expf((float)(t * d * d));
     }
 }
 
 __device__ __forceinline__ void closest32(double x, double y, const WinParams& wp, int* mx, int* my, double* px,
                                           double* py) {
-    fte_closest_node(x, y, wp.Lx, wp.Ly, wp.h, wp.rh, wp.P, mx, my, px, py);
+    fte_closest_node(x, y, wp.Lx, wp.Ly, wp.h, wp.rh, wp.hy, wp.rhy, wp.P, mx, my, px, py);
 }
 
 constexpr int kColChunk32 = 64;
@@ -1080,9 +1107,9 @@ __global__ void __launch_bounds__(kColThreads) k_spread_cols32(int mode, const d
                     q1 = f2 * nrm[2 * i + 1];
                 }
                 float* wyx = wy + s * P1;
-                win32(py, wp, wyx);
+                win32(py, wp.hy, wp, wyx);
                 float* fa = fw + (s * 2) * P1;
-                win32(px, wp, fa);
+                win32(px, wp.h, wp, fa);
                 const float q0f = (float)q0, q1f = (float)q1;
                 for (int a = 0; a < P1; a++) {
                     float wxa = fa[a];
@@ -1175,8 +1202,8 @@ __global__ void __launch_bounds__(kTileThreads) k_gather_tiled32(const double* _
             int mx, my;
             double px, py;
             closest32(p[2 * i], p[2 * i + 1], wp, &mx, &my, &px, &py);
-            win32(px, wp, wxb);
-            win32(py, wp, wyb);
+            win32(px, wp.h, wp, wxb);
+            win32(py, wp.hy, wp, wyb);
             const int lx = mx - ox, ly = my - oy;
             const bool inside = lx >= 0 && ly >= 0 && lx + wp.P < W && ly + wp.P < W;
             double acc0 = 0.0, acc1 = 0.0;
@@ -1332,10 +1359,19 @@ static_assert(sizeof(FfWin) == 64, "FfWin layout");
 
 __device__ __forceinline__ void load_e1_ff(float2* e1, const WinParams& wp) {
     double t0 = -2 * wp.xi * wp.xi / wp.eta * wp.h * wp.h;
+    double t0y = -2 * wp.xi * wp.xi / wp.eta * wp.hy * wp.hy;
+    const int P1e = (wp.P + 2) & ~1;
     for (int j = threadIdx.x; j <= wp.P; j += blockDim.x) {
         int jj = j - wp.P / 2;
         e1[j] = ff_split(exp(t0 * jj * jj));
+        if (wp.aniso) e1[P1e + j] = ff_split(exp(t0y * jj * jj));
     }
+}
+
+// exponent of e0 = ex e4y: px^2 + py^2 + 2 (w px + wy py), formed as the
+// reference forms it (2 w (px + py)) when the axes share their step
+__device__ __forceinline__ double e0_arg(double px, double py, const WinParams& wp) {
+    return wp.aniso ? px * px + py * py + 2 * (wp.w * px + wp.wy * py) : px * px + py * py + 2 * wp.w * (px + py);
 }
 
 // window records of the sources in tile order (k indexes perm)
@@ -1353,13 +1389,13 @@ __global__ void k_ff_win(int kind, const double* __restrict__ p, const double* _
         const int i = perm[k];
         int mx, my;
         double px, py;
-        fte_closest_node(p[2 * i], p[2 * i + 1], wp.Lx, wp.Ly, wp.h, wp.rh, wp.P, &mx, &my, &px, &py);
+        fte_closest_node(p[2 * i], p[2 * i + 1], wp.Lx, wp.Ly, wp.h, wp.rh, wp.hy, wp.rhy, wp.P, &mx, &my, &px, &py);
         FfWin r;
         r.mx = mx;
         r.my = my;
-        r.e0 = fte_expm_ff(ff_split(-t * (px * px + py * py + 2 * wp.w * (px + py))), etab);
+        r.e0 = fte_expm_ff(ff_split(-t * e0_arg(px, py, wp)), etab);
         r.ex3 = fte_expm_ff(ff_split(2 * t * wp.h * px), etab);
-        r.ey3 = fte_expm_ff(ff_split(2 * t * wp.h * py), etab);
+        r.ey3 = fte_expm_ff(ff_split(2 * t * wp.hy * py), etab);
         double f1 = f[2 * i], f2 = f[2 * i + 1];
         if (wts) {
             f1 *= wts[i];
@@ -1399,12 +1435,13 @@ __global__ void __launch_bounds__(kColThreads) k_spread_ff(const FfWin* __restri
     const int P1e = (P1 + 1) & ~1;
     float4* buf = reinterpret_cast<float4*>(shraw);  // WW: (grid 0 sum, low, grid 1 sum, low)
     float4* fw = buf + WW;                            // kColChunk * P1: q0 wx, q1 wx (float-float each)
-    float2* e1 = reinterpret_cast<float2*>(fw + kColChunk * P1);  // P1e
-    float2* wy = e1 + P1e;                                         // kColChunk * P1
+    float2* e1 = reinterpret_cast<float2*>(fw + kColChunk * P1);  // e1_len (P1e, 2 P1e with aniso)
+    float2* wy = e1 + e1_len(wp.P, wp.aniso);                      // kColChunk * P1
     float2* buf2 = wy + kColChunk * P1;                            // NG == 3: WW (grid 2 sum, low)
     float2* fw2 = buf2 + (NG == 3 ? WW : 0);                       // NG == 3: kColChunk * P1 (q2 wx)
     int* org = reinterpret_cast<int*>(fw2 + (NG == 3 ? kColChunk * P1 : 0));  // kColChunk * 2 (lx, ly)
     load_e1_ff(e1, wp);
+    const float2* e1y = e1y_of(e1, wp);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     constexpr int nw = kColWarps;
     for (int tile = blockIdx.x; tile < ntx * nty; tile += gridDim.x) {
@@ -1431,7 +1468,7 @@ __global__ void __launch_bounds__(kColThreads) k_spread_ff(const FfWin* __restri
                         const float2 e3 = r.ey3;
                         float2 ey = ff_powi(e3, j0);
                         for (int j = j0; j < j1; j++) {
-                            wy[lane * P1 + j] = ff_mul(e1[j], ey);
+                            wy[lane * P1 + j] = ff_mul(e1y[j], ey);
                             ey = ff_mul(ey, e3);
                         }
                         if (seg == 0) {
@@ -1516,11 +1553,11 @@ __global__ void __launch_bounds__(kColThreads) k_spread_ff(const FfWin* __restri
     }
 }
 
-size_t spread_ff_smem(int ts, int P, int ng) {
+size_t spread_ff_smem(int ts, int P, int ng, int aniso = 0) {
     const int P1 = P + 1, W = tile_region(ts, P);
     const size_t third = ng == 3 ? ((size_t)W * W + (size_t)kColChunk * P1) * sizeof(float2) : 0;
     return (size_t)W * W * sizeof(float4) + (size_t)kColChunk * P1 * sizeof(float4) +
-           (size_t)(((P1 + 1) & ~1) + kColChunk * P1) * sizeof(float2) + third + kColChunk * 2 * sizeof(int);
+           (size_t)(e1_len(P, aniso) + kColChunk * P1) * sizeof(float2) + third + kColChunk * 2 * sizeof(int);
 }
 
 // FP64 grid values -> float-float pairs, in place
@@ -1559,10 +1596,11 @@ __global__ void __launch_bounds__(kTileThreads, 5) k_gather_ff(const double* __r
     float2* r0 = shf;
     float2* r1 = r0 + WW;
     float2* e1 = r1 + WW;
-    float2* wyb = e1 + ((P1 + 1) & ~1) + threadIdx.x * P1;  // PM == 0 only
+    float2* wyb = e1 + e1_len(wp.P, wp.aniso) + threadIdx.x * P1;  // PM == 0 only
     __shared__ float2 etab[64];  // 2^(-j/64) for the window factors (as in k_ff_win)
     for (int j = threadIdx.x; j < 64; j += blockDim.x) etab[j] = ff_split(exp2(-j / 64.0));
     load_e1_ff(e1, wp);
+    const float2* e1y = e1y_of(e1, wp);
     const double tw = -2 * wp.xi * wp.xi / wp.eta;
     for (int tile = blockIdx.x; tile < ntx * nty; tile += gridDim.x) {
         const int k0 = toff[tile], k1 = toff[tile + 1];
@@ -1580,26 +1618,27 @@ __global__ void __launch_bounds__(kTileThreads, 5) k_gather_ff(const double* __r
             const int i = perm[k];
             int mx, my;
             double px, py;
-            fte_closest_node(p[2 * i], p[2 * i + 1], wp.Lx, wp.Ly, wp.h, wp.rh, wp.P, &mx, &my, &px, &py);
+            fte_closest_node(p[2 * i], p[2 * i + 1], wp.Lx, wp.Ly, wp.h, wp.rh, wp.hy, wp.rhy, wp.P, &mx, &my, &px,
+                             &py);
             float2 wy[PM > 0 ? PM : 1];
             {
-                const float2 e3 = fte_expm_ff(ff_split(2 * tw * wp.h * py), etab);
+                const float2 e3 = fte_expm_ff(ff_split(2 * tw * wp.hy * py), etab);
                 float2 ey = make_float2(1.f, 0.f);
                 if constexpr (PM > 0) {
 #pragma unroll
                     for (int j = 0; j < PM; j++) {
-                        wy[j] = j < P1 ? ff_mul(e1[j], ey) : make_float2(0.f, 0.f);
+                        wy[j] = j < P1 ? ff_mul(e1y[j], ey) : make_float2(0.f, 0.f);
                         ey = ff_mul(ey, e3);
                     }
                 } else {
                     for (int j = 0; j < P1; j++) {
-                        wyb[j] = ff_mul(e1[j], ey);
+                        wyb[j] = ff_mul(e1y[j], ey);
                         ey = ff_mul(ey, e3);
                     }
                 }
             }
             const float2 e3x = fte_expm_ff(ff_split(2 * tw * wp.h * px), etab);
-            float2 ex = fte_expm_ff(ff_split(-tw * (px * px + py * py + 2 * wp.w * (px + py))), etab);
+            float2 ex = fte_expm_ff(ff_split(-tw * e0_arg(px, py, wp)), etab);
             const int lx = mx - ox, ly = my - oy;
             float a0 = 0.f, c0 = 0.f, a1 = 0.f, c1 = 0.f;
             const bool inside = lx >= 0 && ly >= 0 && lx + wp.P < W && ly + wp.P < W;
@@ -1656,10 +1695,10 @@ __global__ void __launch_bounds__(kTileThreads, 5) k_gather_ff(const double* __r
 // the register form's support bound for window support P1 (0: none fits)
 __host__ __device__ inline int gather_ff_pm(int P1) { return P1 <= 16 ? 16 : (P1 <= 24 ? 24 : (P1 <= 32 ? 32 : 0)); }
 
-size_t gather_ff_smem(int ts, int P) {
+size_t gather_ff_smem(int ts, int P, int aniso = 0) {
     const int P1 = P + 1, W = tile_region(ts, P);
     const size_t rows = gather_ff_pm(P1) ? 0 : (size_t)kTileThreads * P1;  // per-thread window columns
-    return 2 * (size_t)W * W * sizeof(float2) + (size_t)(((P1 + 1) & ~1) + rows) * sizeof(float2);
+    return 2 * (size_t)W * W * sizeof(float2) + (size_t)(e1_len(P, aniso) + rows) * sizeof(float2);
 }
 
 // ---- tile sizes -------------------------------------------------------------
@@ -1667,27 +1706,35 @@ size_t gather_ff_smem(int ts, int P) {
 // memory region (ts + P + 4 nodes a side) must fit the two-CTAs-per-SM budget.
 // The default is the largest fitting multiple of 4 up to 64; a plan may carry
 // a tuned size instead (fte_kspace_tune).
-size_t gather64_smem(int ts, int P) {
+size_t gather64_smem(int ts, int P, int aniso = 0) {
     const int P1 = P + 1, W = tile_region(ts, P);
-    return 2 * (size_t)W * W * sizeof(double) + (size_t)(((P1 + 1) & ~1) + kPtThreads * P1) * sizeof(double);
+    return 2 * (size_t)W * W * sizeof(double) + (size_t)(e1_len(P, aniso) + kPtThreads * P1) * sizeof(double);
 }
-bool spread_fits(const fte_context* ctx, int form, int kind, int ts, int P) {
+// do the axes' grid steps differ (beyond rounding)?
+int kspace_aniso(double Lx, int Mx, double Ly, int My) {
+    const double hx = Lx / Mx, hy = Ly / My;
+    return std::fabs(hx - hy) > 1e-12 * std::fmax(hx, hy) ? 1 : 0;
+}
+int kspace_aniso(const KspaceArgs& a) { return kspace_aniso(a.Lx, a.Mx, a.Ly, a.My); }
+bool spread_fits(const fte_context* ctx, int form, int kind, int ts, int P, int aniso = 0) {
     if (ts < 8 || ts > 256) return false;
     size_t sm = form == FTE_FORM_MIXED ? spread_cols32_smem(ts, P)
-                : (form == FTE_FORM_FF ? spread_ff_smem(ts, P, kind == FTE_KIND_SLP ? 2 : 3) : spread_cols_smem(ts, P));
+                : (form == FTE_FORM_FF ? spread_ff_smem(ts, P, kind == FTE_KIND_SLP ? 2 : 3, aniso)
+                                       : spread_cols_smem(ts, P, aniso));
     return sm <= tile_budget(ctx);
 }
-bool gather_fits(const fte_context* ctx, int form, int ts, int P) {
+bool gather_fits(const fte_context* ctx, int form, int ts, int P, int aniso = 0) {
     if (ts < 8 || ts > 256) return false;
     size_t sm = form == FTE_FORM_MIXED ? gather32_smem(ts, P)
-                : (form == FTE_FORM_FF ? gather_ff_smem(ts, P) : gather64_smem(ts, P));
+                : (form == FTE_FORM_FF ? gather_ff_smem(ts, P, aniso) : gather64_smem(ts, P, aniso));
     return sm <= tile_budget(ctx);
 }
 int resolve_tiles(const fte_context* ctx, const KspaceArgs& a, int* ts_s, int* ts_g) {
     *ts_s = 0;
     *ts_g = 0;
+    const int an = kspace_aniso(a);
     if (a.ts_spread > 0) {
-        if (!spread_fits(ctx, a.form, a.kind, a.ts_spread, a.P)) {
+        if (!spread_fits(ctx, a.form, a.kind, a.ts_spread, a.P, an)) {
             fte_set_error("spread tile %d does not fit shared memory at P=%d", a.ts_spread, a.P);
             return FTE_ERR_INVALID;
         }
@@ -1699,13 +1746,13 @@ int resolve_tiles(const fte_context* ctx, const KspaceArgs& a, int* ts_s, int* t
         if (a.form == FTE_FORM_FF) {
             const int ngf = a.kind == FTE_KIND_SLP ? 2 : 3;
             for (int ts = 64; ts >= 28 && !*ts_s; ts -= 4)
-                if (spread_ff_smem(ts, a.P, ngf) <= tile_budget(ctx) * 2 / 3) *ts_s = ts;
+                if (spread_ff_smem(ts, a.P, ngf, an) <= tile_budget(ctx) * 2 / 3) *ts_s = ts;
         }
         for (int ts = 64; ts >= 8 && !*ts_s; ts -= 4)
-            if (spread_fits(ctx, a.form, a.kind, ts, a.P)) *ts_s = ts;
+            if (spread_fits(ctx, a.form, a.kind, ts, a.P, an)) *ts_s = ts;
     }
     if (a.ts_gather > 0) {
-        if (!gather_fits(ctx, a.form, a.ts_gather, a.P)) {
+        if (!gather_fits(ctx, a.form, a.ts_gather, a.P, an)) {
             fte_set_error("gather tile %d does not fit shared memory at P=%d", a.ts_gather, a.P);
             return FTE_ERR_INVALID;
         }
@@ -1716,15 +1763,19 @@ int resolve_tiles(const fte_context* ctx, const KspaceArgs& a, int* ts_s, int* t
         // at most 28 nodes a side (fewer idle threads in a tile's last round
         // of targets; 28 was the fastest of 24..48 at 1e6 points)
         for (int ts = 28; ts >= 8 && !*ts_g; ts -= 4)
-            if (gather_ff_smem(ts, a.P) <= tile_budget(ctx) / 2) *ts_g = ts;
+            if (gather_ff_smem(ts, a.P, an) <= tile_budget(ctx) / 2) *ts_g = ts;
         if (!*ts_g) *ts_g = 8;
     } else {
         for (int ts = 64; ts >= 8 && !*ts_g; ts -= 4)
-            if (gather_fits(ctx, a.form, ts, a.P)) *ts_g = ts;
+            if (gather_fits(ctx, a.form, ts, a.P, an)) *ts_g = ts;
     }
     return FTE_OK;
 }
 
+// Window parameters of an evaluation.  With equal steps (the reference's
+// case) the y axis takes the x axis's values, so that every result is the
+// reference's; otherwise hy = Ly / My and the y support keeps the x axis's
+// ratio w / h (w = P h / 2 when the chooser set it).
 WinParams win_params(const KspaceArgs& a) {
     WinParams wp;
     wp.Lx = a.Lx;
@@ -1737,6 +1788,16 @@ WinParams win_params(const KspaceArgs& a) {
     wp.P = a.P;
     wp.Mx = a.Mx;
     wp.My = a.My;
+    wp.aniso = kspace_aniso(a);
+    if (wp.aniso) {
+        wp.hy = a.Ly / a.My;
+        wp.rhy = 1.0 / wp.hy;
+        wp.wy = a.w * (wp.hy / wp.h);
+    } else {
+        wp.hy = wp.h;
+        wp.rhy = wp.rh;
+        wp.wy = wp.w;
+    }
     return wp;
 }
 
@@ -1748,7 +1809,7 @@ int launch_spread_tiled(fte_context* ctx, const KspaceArgs& a, const TileBins& t
     const int ng = a.kind == FTE_KIND_SLP ? 2 : 4;
     const size_t G = (size_t)a.Mx * a.My;
     const bool f32 = a.form == FTE_FORM_MIXED;
-    const size_t sm = f32 ? spread_cols32_smem(tb.ts, a.P) : spread_cols_smem(tb.ts, a.P);
+    const size_t sm = f32 ? spread_cols32_smem(tb.ts, a.P) : spread_cols_smem(tb.ts, a.P, wp.aniso);
     const int nt = tb.ntx * tb.nty;
     const int grid = nt < ctx->num_sms * 8 ? nt : ctx->num_sms * 8;
     if (a.form == FTE_FORM_FF) {
@@ -1760,7 +1821,7 @@ int launch_spread_tiled(fte_context* ctx, const KspaceArgs& a, const TileBins& t
         // stresslet's three symmetric ones
         double* Hd = static_cast<double*>(H);
         const int ngf = a.kind == FTE_KIND_SLP ? 2 : 3;
-        const size_t smf = spread_ff_smem(tb.ts, a.P, ngf);
+        const size_t smf = spread_ff_smem(tb.ts, a.P, ngf, wp.aniso);
         FTE_LAUNCH(ctx, k_ff_win, ew_grid(ctx, a.nsrc), 256, 0, a.kind, a.psrc, a.f, a.nrm, a.wts, (const int*)tb.perm,
                    a.nsrc, wp, recs);
         if (ngf == 2) {
@@ -1803,7 +1864,7 @@ int launch_gather_tiled(fte_context* ctx, const KspaceArgs& a, const TileBins& t
     const int grid = nt < ctx->num_sms * 8 ? nt : ctx->num_sms * 8;
     if (a.form == FTE_FORM_FF) {
         const float2* Hf = static_cast<const float2*>(H);
-        size_t sm = gather_ff_smem(tb.ts, a.P);
+        size_t sm = gather_ff_smem(tb.ts, a.P, wp.aniso);
         auto go = [&](auto kern) -> int {
             FTE_CUDA_TRY(fte_smem_ceiling(kern, (int)sm));
             FTE_LAUNCH(ctx, kern, grid, kTileThreads, sm, a.ptar, (const int*)tb.off, (const int*)tb.perm, tb.ts,
@@ -1824,7 +1885,7 @@ int launch_gather_tiled(fte_context* ctx, const KspaceArgs& a, const TileBins& t
                    tb.ts, tb.ntx, tb.nty, wp, Hf, Hf + G, scale, a.uk);
     } else {
         const double* Hd = static_cast<const double*>(H);
-        size_t sm = gather64_smem(tb.ts, a.P);
+        size_t sm = gather64_smem(tb.ts, a.P, wp.aniso);
         FTE_CUDA_TRY(fte_smem_ceiling(k_gather_tiled, (int)sm));
         FTE_LAUNCH(ctx, k_gather_tiled, grid, kTileThreads, sm, a.ptar, (const int*)tb.off, (const int*)tb.perm,
                    tb.ts, tb.ntx, tb.nty, wp, Hd, Hd + G, scale, a.uk);
@@ -1832,10 +1893,13 @@ int launch_gather_tiled(fte_context* ctx, const KspaceArgs& a, const TileBins& t
     return FTE_OK;
 }
 
+// (4 xi^2/eta)^2 hx hy / pi / (4 pi) / (Mx My): the reference's
+// (4 xi^2/eta)^2 h^2 / pi scale (ewald_tools.cpp:267-269) with the cell area
+// hx hy of the grid, and the inverse transform's normalisation
 double gather_scale(const KspaceArgs& a) {
-    const double h = a.Lx / a.Mx;
+    const WinParams wp = win_params(a);
     double s = 4 * a.xi * a.xi / a.eta;
-    s = s * s * h * h / FTE_PI;
+    s = s * s * wp.h * wp.hy / FTE_PI;
     return s / (4 * FTE_PI) / ((double)a.Mx * (double)a.My);
 }
 
@@ -1866,12 +1930,12 @@ int kspace_run_mixed(fte_context* ctx, WsCarver& wc, const KspaceArgs& a) {
     if (a.pre_src && a.nsrc > 0)
         tb_s = *a.pre_src;
     else if (a.nsrc > 0)
-        FTE_TRY(fte_tiles_build(ctx, wc, a.psrc, a.nsrc, a.Lx, a.Ly, wp.h, ts_s, (Mx + ts_s - 1) / ts_s,
+        FTE_TRY(fte_tiles_build(ctx, wc, a.psrc, a.nsrc, a.Lx, a.Ly, wp.h, wp.hy, ts_s, (Mx + ts_s - 1) / ts_s,
                                 (My + ts_s - 1) / ts_s, &tb_s));
     if (a.pre_tar && a.ntar > 0)
         tb_g = *a.pre_tar;
     else if (a.ntar > 0)
-        FTE_TRY(fte_tiles_build(ctx, wc, a.ptar, a.ntar, a.Lx, a.Ly, wp.h, ts_g, (Mx + ts_g - 1) / ts_g,
+        FTE_TRY(fte_tiles_build(ctx, wc, a.ptar, a.ntar, a.Lx, a.Ly, wp.h, wp.hy, ts_g, (Mx + ts_g - 1) / ts_g,
                                 (My + ts_g - 1) / ts_g, &tb_g, tile_region(ts_g, a.P)));
     if ((a.nsrc > 0 && tb_s.ts != ts_s) || (a.ntar > 0 && tb_g.ts != ts_g)) {
         fte_set_error("internal: prebuilt tiles do not match the mixed-form tile sizes");
@@ -1906,12 +1970,12 @@ int fte_kspace_tiles(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, TileBi
     FTE_TRY(resolve_tiles(ctx, a, &ts_s, &ts_g));
     src->ts = tar->ts = 0;
     src->ntx = tar->ntx = 0;
-    const double h = a.Lx / a.Mx;
+    const WinParams wp = win_params(a);
     if (ts_s > 0 && a.nsrc > 0)
-        FTE_TRY(fte_tiles_build(ctx, wc, a.psrc, a.nsrc, a.Lx, a.Ly, h, ts_s, (a.Mx + ts_s - 1) / ts_s,
+        FTE_TRY(fte_tiles_build(ctx, wc, a.psrc, a.nsrc, a.Lx, a.Ly, wp.h, wp.hy, ts_s, (a.Mx + ts_s - 1) / ts_s,
                                 (a.My + ts_s - 1) / ts_s, src));
     if (ts_g > 0 && a.ntar > 0)
-        FTE_TRY(fte_tiles_build(ctx, wc, a.ptar, a.ntar, a.Lx, a.Ly, h, ts_g, (a.Mx + ts_g - 1) / ts_g,
+        FTE_TRY(fte_tiles_build(ctx, wc, a.ptar, a.ntar, a.Lx, a.Ly, wp.h, wp.hy, ts_g, (a.Mx + ts_g - 1) / ts_g,
                                 (a.My + ts_g - 1) / ts_g, tar, tile_region(ts_g, a.P)));
     return FTE_OK;
 }
@@ -1951,10 +2015,10 @@ int fte_kspace_tune(fte_context* ctx, void* grid, WsCarver bins, KspaceArgs& a, 
     float best_s = 1e30f, best_g = 1e30f;
     int ts_s = 0, ts_g = 0;
     for (int ts : cand) {
-        if (rc || a.nsrc == 0 || !spread_fits(ctx, a.form, a.kind, ts, a.P)) continue;
+        if (rc || a.nsrc == 0 || !spread_fits(ctx, a.form, a.kind, ts, a.P, kspace_aniso(a))) continue;
         WsCarver w = bins;
         TileBins tb;
-        rc = fte_tiles_build(ctx, w, a.psrc, a.nsrc, a.Lx, a.Ly, wp.h, ts, (a.Mx + ts - 1) / ts,
+        rc = fte_tiles_build(ctx, w, a.psrc, a.nsrc, a.Lx, a.Ly, wp.h, wp.hy, ts, (a.Mx + ts - 1) / ts,
                              (a.My + ts - 1) / ts, &tb);
         FfWin* recs = a.form == FTE_FORM_FF ? w.take<FfWin>(a.nsrc) : nullptr;
         if (!rc && !w.ok()) {
@@ -1976,10 +2040,10 @@ int fte_kspace_tune(fte_context* ctx, void* grid, WsCarver bins, KspaceArgs& a, 
     }
     const double scale = gather_scale(a);
     for (int ts : cand) {
-        if (rc || a.ntar == 0 || !gather_fits(ctx, a.form, ts, a.P)) continue;
+        if (rc || a.ntar == 0 || !gather_fits(ctx, a.form, ts, a.P, kspace_aniso(a))) continue;
         WsCarver w = bins;
         TileBins tb;
-        rc = fte_tiles_build(ctx, w, a.ptar, a.ntar, a.Lx, a.Ly, wp.h, ts, (a.Mx + ts - 1) / ts,
+        rc = fte_tiles_build(ctx, w, a.ptar, a.ntar, a.Lx, a.Ly, wp.h, wp.hy, ts, (a.Mx + ts - 1) / ts,
                              (a.My + ts - 1) / ts, &tb, tile_region(ts, a.P));
         if (!rc && !w.ok()) {
             fte_set_error("internal: tuner bin scratch too small");
@@ -2062,7 +2126,7 @@ int fte_kspace_run(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, fte_info
     const LineMap rows{(long long)My, 0, 1, 1};
     const LineMap cols{(long long)Mx * Kh, 1, (long long)Kh, Kh};
     const int P1 = a.P + 1;
-    size_t sm_pt = (size_t)(((P1 + 1) & ~1) + kPtThreads * P1) * sizeof(double);
+    size_t sm_pt = (size_t)(e1_len(a.P, wp.aniso) + kPtThreads * P1) * sizeof(double);
 
     // tile the grid for the shared-memory spread and gather (0: window too
     // wide for any tile; the per-point kernels with global atomics are used)
@@ -2074,12 +2138,12 @@ int fte_kspace_run(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, fte_info
     if (a.pre_src && ts_s > 0 && a.nsrc > 0)
         tb_s = *a.pre_src;
     else if (ts_s > 0 && a.nsrc > 0)
-        FTE_TRY(fte_tiles_build(ctx, wc, a.psrc, a.nsrc, a.Lx, a.Ly, wp.h, ts_s, (Mx + ts_s - 1) / ts_s,
+        FTE_TRY(fte_tiles_build(ctx, wc, a.psrc, a.nsrc, a.Lx, a.Ly, wp.h, wp.hy, ts_s, (Mx + ts_s - 1) / ts_s,
                                 (My + ts_s - 1) / ts_s, &tb_s));
     if (a.pre_tar && ts_g > 0 && a.ntar > 0)
         tb_g = *a.pre_tar;
     else if (ts_g > 0 && a.ntar > 0)
-        FTE_TRY(fte_tiles_build(ctx, wc, a.ptar, a.ntar, a.Lx, a.Ly, wp.h, ts_g, (Mx + ts_g - 1) / ts_g,
+        FTE_TRY(fte_tiles_build(ctx, wc, a.ptar, a.ntar, a.Lx, a.Ly, wp.h, wp.hy, ts_g, (Mx + ts_g - 1) / ts_g,
                                 (My + ts_g - 1) / ts_g, &tb_g, tile_region(ts_g, a.P)));
     if ((a.nsrc > 0 && tb_s.ts != ts_s) || (a.ntar > 0 && tb_g.ts != ts_g)) {
         fte_set_error("internal: prebuilt tiles do not match the FP64 tile sizes");
@@ -2343,7 +2407,7 @@ int fte_q_kspace_run(fte_context* ctx, WsCarver& wc, int q, const KspaceArgs& a,
     if (a.nsrc > 0) {
         TileBins tb;
         WsCarver w2 = wc;
-        FTE_TRY(fte_tiles_build(ctx, w2, a.psrc, a.nsrc, a.Lx, a.Ly, wp.h, ts_s, (Mx + ts_s - 1) / ts_s,
+        FTE_TRY(fte_tiles_build(ctx, w2, a.psrc, a.nsrc, a.Lx, a.Ly, wp.h, wp.hy, ts_s, (Mx + ts_s - 1) / ts_s,
                                 (My + ts_s - 1) / ts_s, &tb));
         FTE_WS_CHECK(w2);
         FTE_TRY(launch_spread_tiled(ctx, a, tb, wp, H, nullptr));
@@ -2387,7 +2451,7 @@ int fte_q_kspace_run(fte_context* ctx, WsCarver& wc, int q, const KspaceArgs& a,
     if (a.ntar == 0) return FTE_OK;
     // gather pairs of grids
     TileBins tb;
-    FTE_TRY(fte_tiles_build(ctx, wc, a.ptar, a.ntar, a.Lx, a.Ly, wp.h, ts_g, (Mx + ts_g - 1) / ts_g,
+    FTE_TRY(fte_tiles_build(ctx, wc, a.ptar, a.ntar, a.Lx, a.Ly, wp.h, wp.hy, ts_g, (Mx + ts_g - 1) / ts_g,
                             (My + ts_g - 1) / ts_g, &tb, tile_region(ts_g, a.P)));
     FTE_WS_CHECK(wc);
     const double scale = gather_scale(a);
@@ -2634,6 +2698,10 @@ extern "C" int fte_slp_kspace_noalloc(const double* psrc, int64_t nsrc, const do
     wp.P = P;
     wp.Mx = Mx;
     wp.My = My;
+    wp.hy = wp.h;  // equal steps (checked above)
+    wp.rhy = wp.rh;
+    wp.wy = wp.w;
+    wp.aniso = 0;
     const int P1 = P + 1;
     const size_t sm_pt = (size_t)(((P1 + 1) & ~1) + kPtThreads * P1) * sizeof(double);
     const size_t sm_y = 2 * (size_t)py.m * sizeof(double2), sm_x = 2 * (size_t)px.m * sizeof(double2);

@@ -1155,7 +1155,7 @@ void fte_near_fill_params(int kind, const CellList& cl, double xi, double Lx, do
     p.xi2 = xi * xi;
     p.inv_xi2 = 1.0 / (xi * xi);
     p.selfc = -(1.0 + 0.5 * FTE_EULER) - log(xi);
-    p.cutoffsq = Lx * Ly / cl.nsx / cl.nsy;
+    p.cutoffsq = cl.cutoffsq > 0.0 ? cl.cutoffsq : Lx * Ly / cl.nsx / cl.nsy;
     p.pf = 2.0 * xi * xi;
     p.bsx = Lx / cl.nsx;
     p.bsy = Ly / cl.nsy;

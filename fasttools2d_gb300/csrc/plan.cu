@@ -386,6 +386,7 @@ extern "C" int fte_plan_create(fte_context* c, int kind, const double* xsrc, con
     if (ntar > 0) FTE_LAUNCH(c, k_plan_wrap, grid_of(c, ntar), 256, 0, dxt, dyt, ntar, Lx, Ly, p->pt);
     FTE_TRY(fte_cells_build(c, pm, kind, p->ps, nsrc, p->pt, ntar, pf, p->nrm, p->wts, prm.nside_x, prm.nside_y, Lx,
                             Ly, &p->cl));
+    if (opt->form == FTE_FORM_MIXED) p->cl.cutoffsq = fte_tuned_cutoffsq(prm, Lx, Ly);
     FTE_WS_CHECK(pm);
     ka.psrc = p->ps;
     ka.ptar = p->pt;

@@ -47,25 +47,31 @@ N_IN, N_HID, N_OUT = 8, 64, 4
 
 
 # ---- features -------------------------------------------------------------------
-def features(xsrc, ysrc, ntar, Lx, Ly, tol, sample=2048, seed=0):
-    """The 8 selector inputs of a configuration (host computation)."""
-    from scipy.spatial import cKDTree
-
-    x = np.asarray(xsrc, dtype=np.float64)
-    y = np.asarray(ysrc, dtype=np.float64)
-    n = len(x)
-    px = np.minimum(np.mod(x + Lx / 2, Lx), np.nextafter(Lx, 0))
-    py = np.minimum(np.mod(y + Ly / 2, Ly), np.nextafter(Ly, 0))
-    pts = np.stack([px, py], 1)
-    tree = cKDTree(pts, boxsize=[Lx, Ly])
-    rng = np.random.default_rng(seed)
-    idx = rng.choice(n, size=min(n, sample), replace=False) if n > sample else np.arange(n)
-    d, _ = tree.query(pts[idx], k=2)
-    h = np.sqrt(Lx * Ly / max(n, 1))
-    r = np.maximum(d[:, 1] / h, 1e-6)
+def features_from_nn(dist, nsrc, ntar, Lx, Ly, tol):
+    """The 8 selector inputs from the nearest-neighbour distances of a sample
+    of the sources: log10 N_src, log10 N_trg, aspect ratio, the fraction of
+    sampled sources closer than a quarter of the mean spacing h = sqrt(Lx Ly /
+    N) to another source (the cluster fraction), the 10/50/90 % quantiles of
+    log10(distance / h), log10 tol."""
+    h = np.sqrt(Lx * Ly / max(nsrc, 1))
+    r = np.maximum(np.asarray(dist, dtype=np.float64) / h, 1e-6)
+    r = np.where(np.isfinite(r), r, 1e6)
     q10, q50, q90 = np.log10(np.quantile(r, [0.1, 0.5, 0.9]))
-    return np.array([np.log10(max(n, 1)), np.log10(max(ntar, 1)), max(Lx, Ly) / min(Lx, Ly), float(np.mean(r < 0.25)),
-                     q10, q50, q90, np.log10(tol)], dtype=np.float64)
+    return np.array([np.log10(max(nsrc, 1)), np.log10(max(ntar, 1)), max(Lx, Ly) / min(Lx, Ly),
+                     float(np.mean(r < 0.25)), q10, q50, q90, np.log10(tol)], dtype=np.float64)
+
+
+def features(xsrc, ysrc, ntar, Lx, Ly, tol, sample=2048, ctx=None):
+    """The 8 selector inputs of a configuration.  The nearest-neighbour
+    distances of a sample of the sources come from the GPU
+    (``fte_nn_sample``: a device cell list and a ring search per sampled
+    source); host or CUDA arrays."""
+    from . import nn_sample
+
+    n = len(xsrc)
+    if n < 2:
+        return features_from_nn(np.full(1, np.sqrt(Lx * Ly)), n, ntar, Lx, Ly, tol)
+    return features_from_nn(nn_sample(xsrc, ysrc, Lx, Ly, nsample=sample, ctx=ctx), n, ntar, Lx, Ly, tol)
 
 
 # ---- the network on the GPU -------------------------------------------------------
@@ -200,28 +206,59 @@ def targets_of(prm, T):
                      (prm.P - T.P) / 2.0])
 
 
+def _rational(T):
+    """Does the tuned choice T use the drivers' geometry (square cells,
+    nside = a (A, B), equal grid steps M = t (A, B))?"""
+    A, B = int(T.A), int(T.B)
+    return A <= 16 and B <= 16 and T.nside_x % A == 0 and T.nside_y % B == 0 and T.Mx % A == 0 and T.My % B == 0 \
+        and T.nside_x // A == T.nside_y // B and T.Mx // A == T.My // B
+
+
 def params_from(y, T):
     """Valid driver options from network outputs y relative to T."""
-    A, B = int(T.A), int(T.B)
-    a = max(1, int(round(T.nside_x / A * np.exp(y[0]))))
-    t = max(2, int(round(T.Mx / A * np.exp(y[2]))))
-    while (A * t) % 2 or (B * t) % 2:
-        t += 1
     P = int(np.clip(T.P + 2 * round(float(y[3])), 4, 24))
-    while P + 1 > min(A * t, B * t):
-        t += 2
-    return dict(P=P, nside_x=A * a, nside_y=B * a, xi=float(T.xi * np.exp(y[1])), Mx=A * t, My=B * t)
+    xi = float(T.xi * np.exp(y[1]))
+    if _rational(T):
+        A, B = int(T.A), int(T.B)
+        a = max(1, int(round(T.nside_x / A * np.exp(y[0]))))
+        t = max(2, int(round(T.Mx / A * np.exp(y[2]))))
+        while (A * t) % 2 or (B * t) % 2:
+            t += 1
+        while P + 1 > min(A * t, B * t):
+            t += 2
+        return dict(P=P, nside_x=A * a, nside_y=B * a, xi=xi, Mx=A * t, My=B * t)
+    # a box with its own step per axis: each count scaled on its own
+    s = np.exp(y[0])
+    nx, ny = max(1, int(round(T.nside_x * s))), max(1, int(round(T.nside_y * s)))
+    g = np.exp(y[2])
+    mx, my = max(2, int(round(T.Mx * g / 2)) * 2), max(2, int(round(T.My * g / 2)) * 2)
+    while P + 1 > min(mx, my):
+        mx, my = mx + 2, my + 2
+    return dict(P=P, nside_x=nx, nside_y=ny, xi=xi, Mx=mx, My=my)
 
 
 # candidates around the tuned choice, the same for every configuration so that
 # labels are comparable: cell-list scale (xi and the grid follow from the
 # estimates) x window support change
-CANDIDATES = [(sa, dp) for sa in (0.7, 1.0, 1.4, 2.0) for dp in (-2, 0, 2)]
+CANDIDATES = [(sa, dp) for sa in (0.7, 1.0, 1.4, 2.0) for dp in (-4, -2, 0, 2)]
 # a label must meet the tolerance with this margin
 LABEL_MARGIN = 0.5
 # the sampled check sees 64 targets, whose largest error is below the largest
 # over all targets: it passes only below this fraction of the tolerance
 CHECK_MARGIN = 0.7
+# the fallback: the analytic error-estimate choice (the mixed form's tuned
+# parameters, estimates solved for this fraction of the tolerance)
+FALLBACK_TOL = 0.1
+
+
+def _host(a):
+    return a.cpu().numpy() if hasattr(a, "cpu") else np.asarray(a)
+
+
+def tuned_choice(kind, cfg, tol, **kw):
+    """The mixed form's tuned analytic choice T for a configuration."""
+    return choose_params(kind, _host(cfg["f1"]), _host(cfg["f2"]), len(cfg["xt"]), cfg["Lx"], cfg["Ly"], tol=tol,
+                         form=FORM_MIXED, **kw)
 
 
 # ---- the selector ------------------------------------------------------------------
@@ -246,19 +283,16 @@ class Selector:
 
     def choose(self, kind, cfg, tol, feats=None):
         """Options for the driver (mixed form) and the tuned choice T."""
-        f1 = cfg["f1"].cpu().numpy() if hasattr(cfg["f1"], "cpu") else cfg["f1"]
-        f2 = cfg["f2"].cpu().numpy() if hasattr(cfg["f2"], "cpu") else cfg["f2"]
-        T = choose_params(kind, f1, f2, len(cfg["xt"]), cfg["Lx"], cfg["Ly"], tol=tol, form=FORM_MIXED)
+        T = tuned_choice(kind, cfg, tol)
         if feats is None:
-            xs = cfg["xs"].cpu().numpy() if hasattr(cfg["xs"], "cpu") else cfg["xs"]
-            ys = cfg["ys"].cpu().numpy() if hasattr(cfg["ys"], "cpu") else cfg["ys"]
-            feats = features(xs, ys, len(cfg["xt"]), cfg["Lx"], cfg["Ly"], tol)
+            feats = features(cfg["xs"], cfg["ys"], len(cfg["xt"]), cfg["Lx"], cfg["Ly"], tol, ctx=self.ctx)
         return params_from(self.predict(kind, feats), T), T
 
     def evaluate(self, kind, cfg, tol, check=True, sample=64, seed=0, feats=None):
         """Evaluate with the learned parameters; if the sampled FP64 check
-        misses half the tolerance, evaluate again with the drivers' analytic
-        choice in FP64.  Returns (u1, u2, report)."""
+        misses CHECK_MARGIN of the tolerance, evaluate again with the analytic
+        error-estimate choice (the tuned choice at a tenth of the tolerance).
+        Returns (u1, u2, report)."""
         import torch
 
         opts, T = self.choose(kind, cfg, tol, feats)
@@ -274,7 +308,7 @@ class Selector:
             rep["check_err"] = err
             if not err <= CHECK_MARGIN * tol:
                 t2 = time.perf_counter()
-                out, info = _run(kind, cfg, tol, self.ctx, form=FORM_PLAIN)
+                out, info = _run(kind, cfg, tol * FALLBACK_TOL, self.ctx, form=FORM_MIXED)
                 torch.cuda.synchronize()
                 rep["t_fallback_s"] = time.perf_counter() - t2
                 rep["used"] = "fallback"
@@ -303,7 +337,7 @@ def reference(kind, cfg, ctx):
 
 
 # ---- data generation, training and evaluation (GPU) ------------------------------
-def random_config(rng, nmin=1e3, nmax=3e5):
+def random_config(rng, nmin=1e3, nmax=1e6):
     """A configuration of the training distribution: N log-uniform, box aspect
     p/4 (p = 4..16), uniform points or half uniform / half on ellipses,
     targets = sources, zero-mean N(0,1) densities, tolerance log-uniform in
@@ -369,17 +403,22 @@ def label_config(cfg, ctx, rng):
     T = choose_params(kind, cfg["f1"], cfg["f2"], len(cfg["xt"]), cfg["Lx"], cfg["Ly"], tol=tol, form=FORM_MIXED)
     t_T, out, info = _timed(kind, d, tol, ctx, form=FORM_MIXED)
     rows = [_cand_row(info.params, t_T, _rel_err(_u(out), ref))]
+    rational = _rational(T)
     for sa, dp in CANDIDATES:
-        a = max(1, int(round(T.nside_x / T.A * sa)))
         P = int(np.clip(T.P + dp, 4, 24))
         if sa == 1.0 and dp == 0:
             continue  # T itself
+        if rational:
+            a = max(1, int(round(T.nside_x / T.A * sa)))
+            cells = dict(nside_x=T.A * a, nside_y=T.B * a)
+        else:
+            cells = dict(nside_x=max(1, int(round(T.nside_x * sa))), nside_y=max(1, int(round(T.nside_y * sa))))
         try:
-            t, out, info = _timed(kind, d, tol, ctx, form=FORM_MIXED, P=P, nside_x=T.A * a, nside_y=T.B * a)
+            t, out, info = _timed(kind, d, tol, ctx, form=FORM_MIXED, P=P, **cells)
         except FteError:
             continue
         rows.append(_cand_row(info.params, t, _rel_err(_u(out), ref)))
-    feats = features(cfg["xs"], cfg["ys"], len(cfg["xt"]), cfg["Lx"], cfg["Ly"], tol)
+    feats = features(d["xs"], d["ys"], len(cfg["xt"]), cfg["Lx"], cfg["Ly"], tol, ctx=ctx)
     qsum = float(np.sum(cfg["f1"] ** 2 + cfg["f2"] ** 2))
     return {"kind": kind, "tol": tol, "n": len(cfg["xs"]), "ntar": len(cfg["xt"]), "Lx": cfg["Lx"], "Ly": cfg["Ly"],
             "qsum": qsum, "feats": feats, "cands": np.array(rows, dtype=np.float64)}
@@ -455,9 +494,10 @@ def fit_models(recs, steps=4000, seed=5, log=None):
 
 
 def evaluate_heldout(sel, cfgs, ctx, log=None):
-    """Learned (with check and fallback to the drivers' analytic choice) vs
-    the tuned analytic choice vs the drivers' analytic choice (FP64, P = 24)
-    on held-out configurations."""
+    """Learned (with check and fallback to the tuned choice at a tenth of the
+    tolerance) vs the tuned analytic choice vs the drivers' analytic choice
+    (FP64, P = 24) on held-out configurations.  The features (GPU
+    nearest-neighbour sample) and the sampled FP64 check are timed apart."""
     import torch
 
     rows = []
@@ -469,10 +509,11 @@ def evaluate_heldout(sel, cfgs, ctx, log=None):
         err_an = _rel_err(_u(out_an), ref)
         t_T, out_T, _ = _timed(kind, d, tol, ctx, form=FORM_MIXED)
         err_T = _rel_err(_u(out_T), ref)
+        torch.cuda.synchronize()
         ts = time.perf_counter()
-        feats = features(cfg["xs"], cfg["ys"], len(cfg["xt"]), cfg["Lx"], cfg["Ly"], tol)
+        feats = features(d["xs"], d["ys"], len(cfg["xt"]), cfg["Lx"], cfg["Ly"], tol, ctx=ctx)
+        t_feat = (time.perf_counter() - ts) * 1e3
         opts, T = sel.choose(kind, d, tol, feats)
-        t_select = (time.perf_counter() - ts) * 1e3
         try:
             t_L, out_L, _ = _timed(kind, d, tol, ctx, form=FORM_MIXED, **opts)
             err_L = _rel_err(_u(out_L), ref)
@@ -483,12 +524,16 @@ def evaluate_heldout(sel, cfgs, ctx, log=None):
         except FteError:
             t_L, err_L, chk, t_chk = np.inf, np.inf, np.inf, 0.0
         fallback = not chk <= CHECK_MARGIN * tol
-        t_sel = (t_L if np.isfinite(t_L) else 0.0) + (t_an if fallback else 0.0)
-        err_sel = err_an if fallback else err_L
+        t_fb, err_fb = 0.0, err_L
+        if fallback:
+            t_fb, out_fb, _ = _timed(kind, d, tol * FALLBACK_TOL, ctx, form=FORM_MIXED)
+            err_fb = _rel_err(_u(out_fb), ref)
+        t_sel = (t_L if np.isfinite(t_L) else 0.0) + t_fb
+        err_sel = err_fb if fallback else err_L
         rows.append({"kind": kind, "tol": tol, "n": len(cfg["xs"]), "t_analytic_ms": t_an,
                      "err_analytic": err_an, "t_tuned_ms": t_T, "err_tuned": err_T,
                      "t_learned_ms": t_L, "err_learned": err_L, "check_err": chk, "t_check_ms": t_chk,
-                     "t_select_ms": t_select,
+                     "t_features_ms": t_feat,
                      "fallback": fallback, "t_selected_ms": t_sel, "err_selected": err_sel})
         if log and i % 50 == 0:
             log(f"heldout {i}: {rows[-1]}")
@@ -503,12 +548,14 @@ def summarize(rows):
         "configs": len(rows),
         "total_ms": {"analytic_fp64": float(r["t_analytic_ms"].sum()), "tuned": float(r["t_tuned_ms"].sum()),
                      "learned_with_fallback": float(r["t_selected_ms"].sum()),
+                     "learned_with_fallback_and_features": float(r["t_selected_ms"].sum() + r["t_features_ms"].sum()),
                      "learned_with_fallback_and_check": float(r["t_selected_ms"].sum() + r["t_check_ms"].sum())},
         "meets_tol": {"analytic_fp64": float(np.mean(r["err_analytic"] <= tol)),
                       "tuned": float(np.mean(r["err_tuned"] <= tol)),
                       "learned_raw": float(np.mean(r["err_learned"] <= tol)),
                       "learned_with_fallback": float(np.mean(r["err_selected"] <= tol))},
-        "host_select_ms": float(r["t_select_ms"].sum()),
+        "features_ms": float(r["t_features_ms"].sum()),
+        "check_ms": float(r["t_check_ms"].sum()),
         "fallbacks": int(fb.sum()),
         "median_speedup_vs_tuned": float(np.median(r["t_tuned_ms"] / np.maximum(r["t_selected_ms"], 1e-9))),
         "median_speedup_vs_analytic": float(np.median(r["t_analytic_ms"] / np.maximum(r["t_selected_ms"], 1e-9))),
@@ -524,7 +571,9 @@ def main(argv=None):
     ap.add_argument("cmd", choices=["train"])
     ap.add_argument("--configs", type=int, default=2000)
     ap.add_argument("--heldout", type=int, default=500)
-    ap.add_argument("--nmax", type=float, default=3e5)
+    ap.add_argument("--nmax", type=float, default=1e6)
+    ap.add_argument("--max-label-seconds", type=float, default=0.0,
+                    help="stop labelling after this long (0: label every configuration)")
     ap.add_argument("--steps", type=int, default=4000)
     ap.add_argument("--out", default=".")
     ap.add_argument("--seed", type=int, default=5)
@@ -549,8 +598,13 @@ def main(argv=None):
     else:
         recs = []
         for i in range(a.configs):
+            if a.max_label_seconds > 0 and time.time() - t0 > a.max_label_seconds:
+                log(f"labelling stopped after {i} configurations ({time.time() - t0:.0f} s)")
+                break
             cfg = random_config(rng, nmax=a.nmax)
             recs.append(label_config(cfg, ctx, rng))
+            if i % 500 == 499:
+                save_records(os.path.join(a.out, "selector_data.npz"), recs)
             if i % 100 == 0:
                 c = recs[-1]["cands"]
                 log(f"label {i} {time.time() - t0:.1f}s kind={recs[-1]['kind']} n={recs[-1]['n']} "

@@ -293,6 +293,15 @@ int fte_mlp_loss_grad(const float* params, const float* X, const float* T, const
 int fte_mlp_adam(float* params, const float* grad, float* m, float* v, int step, float lr, float beta1,
                  float beta2, float eps, void* stream);
 
+/* Layout statistics for the selector's features (no counterpart in the
+ * reference): for a sample of the sources -- every stride-th one, stride =
+ * max(1, nsrc / nsample) -- the distance to the nearest other source in the
+ * periodic Lx x Ly box, from a device cell list.  out receives
+ * min(nsample, ceil(nsrc / stride)) distances in sample order (host array, or
+ * device with FTE_DEVICE_POINTERS, like xsrc and ysrc).  Synchronises. */
+int fte_nn_sample(fte_context* ctx, const double* xsrc, const double* ysrc, int64_t nsrc, double Lx, double Ly,
+                  int nsample, double* out, unsigned flags);
+
 /* ---- allocation-free variant --------------------------------------------- */
 /* No counterpart in the reference.  The Stokeslet k-space sum of
  * fte_slp_kspace (same arguments and results) for callers that may not

@@ -78,6 +78,39 @@ def test_adam_step_matches_oracle(gpu_ctx):
     assert np.max(np.abs(t[3].cpu().numpy() - rv)) <= 1e-6
 
 
+@pytest.mark.parametrize("layout", ["uniform", "clustered", "narrow"])
+def test_nn_sample_matches_brute_force(gpu_ctx, layout):
+    """fte_nn_sample (device cell list, ring search) against a brute-force
+    minimum-image search of the same sampled sources."""
+    import fasttools2d_gb300 as ft
+
+    rng = np.random.default_rng(7)
+    n, Lx, Ly = 30000, 1.0, 1.0
+    if layout == "uniform":
+        x, y = rng.random(n) - 0.5, rng.random(n) - 0.5
+    elif layout == "clustered":
+        c = rng.integers(0, 5, n)
+        x = (rng.random(5) - 0.5)[c] + 0.01 * rng.standard_normal(n)
+        y = (rng.random(5) - 0.5)[c] + 0.01 * rng.standard_normal(n)
+    else:
+        n, Lx, Ly = 4000, 7.3, 0.05
+        x, y = (rng.random(n) - 0.5) * Lx, (rng.random(n) - 0.5) * Ly
+    d = ft.nn_sample(x, y, Lx, Ly, nsample=500, ctx=gpu_ctx)
+    stride = max(1, n // 500)
+    idx = np.arange(0, n, stride)[:len(d)]
+    wx = np.mod(x + Lx / 2, Lx) - Lx / 2
+    wy = np.mod(y + Ly / 2, Ly) - Ly / 2
+    dx = wx[idx, None] - wx[None, :]
+    dy = wy[idx, None] - wy[None, :]
+    dx -= Lx * np.round(dx / Lx)
+    dy -= Ly * np.round(dy / Ly)
+    dd = np.hypot(dx, dy)
+    dd[np.arange(len(idx)), idx] = np.inf
+    ref = dd.min(1)
+    assert len(d) == len(idx) == 500
+    assert np.allclose(d, ref, rtol=1e-12, atol=1e-15)
+
+
 def test_training_fits_a_smooth_map(gpu_ctx):
     sel = _sel()
     rng = np.random.default_rng(11)

@@ -40,24 +40,35 @@ def test_oracle_adam_first_step_is_sign_descent():
     assert np.allclose(q[g != 0], -0.1 * np.sign(g[g != 0]))
 
 
+def _nn_periodic(x, y, Lx, Ly):
+    """Nearest-neighbour distance of every point (minimum image), brute force."""
+    dx = x[:, None] - x[None, :]
+    dy = y[:, None] - y[None, :]
+    dx -= Lx * np.round(dx / Lx)
+    dy -= Ly * np.round(dy / Ly)
+    d = np.hypot(dx, dy)
+    np.fill_diagonal(d, np.inf)
+    return d.min(1)
+
+
 def test_features_on_known_layouts():
     ft = pytest.importorskip("fasttools2d_gb300")
     from fasttools2d_gb300 import selector
 
-    pytest.importorskip("scipy")
     # a square lattice: every nearest neighbour at the mean spacing
     k = 40
     g = (np.arange(k) + 0.5) / k - 0.5
     X, Y = np.meshgrid(g, g)
-    f = selector.features(X.ravel(), Y.ravel(), 1234, 1.0, 1.0, 1e-8)
+    d = _nn_periodic(X.ravel(), Y.ravel(), 1.0, 1.0)
+    f = selector.features_from_nn(d, k * k, 1234, 1.0, 1.0, 1e-8)
     assert f.shape == (8,)
     assert f[0] == pytest.approx(np.log10(k * k)) and f[1] == pytest.approx(np.log10(1234))
     assert f[2] == pytest.approx(1.0) and f[3] == 0.0
     assert np.allclose(f[4:7], 0.0, atol=1e-9) and f[7] == pytest.approx(-8.0)
     # all points in one tight cluster: small neighbour distances
     rng = np.random.default_rng(1)
-    f2 = selector.features(0.001 * rng.standard_normal(2000), 0.001 * rng.standard_normal(2000), 2000, 2.0, 1.0,
-                           1e-6)
+    x, y = 0.001 * rng.standard_normal(2000), 0.001 * rng.standard_normal(2000)
+    f2 = selector.features_from_nn(_nn_periodic(x, y, 2.0, 1.0), 2000, 2000, 2.0, 1.0, 1e-6)
     assert f2[2] == pytest.approx(2.0) and f2[3] > 0.9 and f2[5] < -1.0
     del ft
 
@@ -77,10 +88,29 @@ def test_targets_and_params_round_trip():
         assert opts["xi"] == pytest.approx(T.xi)
         y = np.array([0.2, -0.1, 0.15, 1.0])
         o = selector.params_from(y, T)
+        assert selector._rational(T)
         assert o["nside_x"] % T.A == 0 and o["nside_y"] % T.B == 0
         assert o["Mx"] * T.B == o["My"] * T.A and o["Mx"] % 2 == 0 and o["My"] % 2 == 0
         assert o["P"] == min(T.P + 2, 24)
         assert np.log(o["xi"] / T.xi) == pytest.approx(-0.1)
+
+
+def test_params_round_trip_on_irrational_box():
+    """Boxes with a step per axis: zero corrections give the tuned choice
+    back, and corrections scale each axis on its own (even grid sizes)."""
+    ft = pytest.importorskip("fasttools2d_gb300")
+    from fasttools2d_gb300 import selector
+
+    rng = np.random.default_rng(4)
+    n = 20000
+    f1, f2 = rng.standard_normal(n), rng.standard_normal(n)
+    T = ft.choose_params(1, f1, f2, n, 1.0, np.sqrt(2.0), tol=1e-8, form=ft.FORM_MIXED)
+    assert not selector._rational(T)
+    o = selector.params_from(np.zeros(4), T)
+    assert (o["P"], o["nside_x"], o["nside_y"], o["Mx"], o["My"]) == (T.P, T.nside_x, T.nside_y, T.Mx, T.My)
+    o = selector.params_from(np.array([0.3, 0.0, 0.2, -1.0]), T)
+    assert o["Mx"] % 2 == 0 and o["My"] % 2 == 0 and o["P"] == T.P - 2
+    assert o["nside_x"] == round(T.nside_x * np.exp(0.3)) and o["nside_y"] == round(T.nside_y * np.exp(0.3))
 
 
 def test_committed_model_layout():
