@@ -241,7 +241,14 @@ def batched_section(ft, wl, ctx, stream, steps, warmup, flush):
               batch; a step is one replay of its CUDA graph.
     baseline: the untuned plain per-instance loop -- one FP64 driver call per
               (configuration, kernel, vector) with the analytic parameters.
-    Both with inputs resident on the GPU; L2 flushed before every step."""
+    ablations, to separate what each part adds:
+      mixed_loop     the mixed form's driver called per (configuration,
+                     kernel, vector) with the batch's parameters (same
+                     arithmetic and parameters; no plans, batch or graph)
+      plans_loop     the batch's plans executed one after another (geometry
+                     reused, all vectors per call; no batch or graph)
+      batch_untuned  the same batch with the default tile sizes (no autotuner)
+    All with inputs resident on the GPU; L2 flushed before every step."""
     import numpy as np
     import torch
 
@@ -318,6 +325,69 @@ def batched_section(ft, wl, ctx, stream, steps, warmup, flush):
     torch.cuda.synchronize()
     graph_ms = sum(a.elapsed_time(b) for a, b in ev) / bsteps
 
+    def device_ms(fn, reps):
+        ev = events(reps)
+        torch.cuda.synchronize()
+        for i in range(reps):
+            flush.fill_(float(i))
+            ev[i][0].record(stream)
+            fn()
+            ev[i][1].record(stream)
+        torch.cuda.synchronize()
+        return sum(a.elapsed_time(b) for a, b in ev) / reps
+
+    # ablation 1: the mixed form's driver per instance with the batch's parameters
+    ov = []
+    for p in plans:
+        q = p.params
+        ov.append(dict(P=q.P, xi=q.xi, Mx=q.Mx, My=q.My, nside_x=q.nside_x, nside_y=q.nside_y))
+    mix_out = [(torch.empty_like(dev[i // len(kinds)]["f1"][0]), torch.empty_like(dev[i // len(kinds)]["f1"][0]))
+               for i in range(len(plans))]
+
+    def mixed_loop():
+        for i, p in enumerate(plans):
+            d = dev[i // len(kinds)]
+            u1, u2 = mix_out[i]
+            for v in range(nv):
+                if p.kind == ft.KIND_SLP:
+                    ft.StokesSLP_ewald_2p(d["xsrc"], d["ysrc"], d["xsrc"], d["ysrc"], d["f1"][v], d["f2"][v],
+                                          d["Lx"], d["Ly"], tol=tol, form=ft.FORM_MIXED, ctx=ctx, out=(u1, u2),
+                                          parts=False, **ov[i])
+                else:
+                    ft.StokesDLP_ewald_2p(d["xsrc"], d["ysrc"], d["xsrc"], d["ysrc"], d["n1"], d["n2"], d["f1"][v],
+                                          d["f2"][v], d["Lx"], d["Ly"], tol=tol, form=ft.FORM_MIXED, ctx=ctx,
+                                          out=(u1, u2), parts=False, **ov[i])
+
+    mixed_loop()
+    mixed_loop_ms = device_ms(mixed_loop, 2)
+
+    # ablation 2: the plans one after another (no batch, no graph)
+    def plans_loop():
+        for i, p in enumerate(plans):
+            d = dev[i // len(kinds)]
+            p.execute(d["f1"], d["f2"])
+
+    plans_loop()
+    plans_loop_ms = device_ms(plans_loop, 2)
+
+    # ablation 3: the same batch with the default tiles (no autotuner)
+    plans_u = []
+    for d in dev:
+        for kind in kinds:
+            plans_u.append(ft.Plan(kind, d["xsrc"], d["ysrc"], d["xsrc"], d["ysrc"], d["f1"][0], d["f2"][0], d["Lx"],
+                                   d["Ly"], n1=d["n1"], n2=d["n2"], tol=tol, form=ft.FORM_MIXED, nvmax=nv, tune=False,
+                                   ctx=ctx))
+    batch_u = ft.Batch(plans_u, nv, ctx=ctx)
+    for i in range(len(plans_u)):
+        d = dev[i // len(kinds)]
+        batch_u.set_density(i, d["f1"], d["f2"])
+    for _ in range(warmup):
+        batch_u.launch(True)
+    untuned_ms = device_ms(lambda: batch_u.launch(True), bsteps)
+    batch_u.close()
+    for p in plans_u:
+        p.close()
+
     # agreement with the FP64 plain loop (both at tolerance 1e-8)
     worst = 0.0
     for i, p in enumerate(plans):
@@ -372,6 +442,8 @@ def batched_section(ft, wl, ctx, stream, steps, warmup, flush):
         "plain_loop": {"targets_per_s": targets_per_step / (loop_ms / 1e3), "ms_per_step": loop_ms,
                        "calls_per_step": len(cfgs) * len(kinds) * nv},
         "speedup_vs_plain_loop": loop_ms / graph_ms,
+        "ablation_ms_per_step": {"mixed_loop": mixed_loop_ms, "plans_loop": plans_loop_ms,
+                                 "batch_untuned": untuned_ms, "batch_tuned_graph": graph_ms},
         "setup_s": setup_s, "gpu_launches_per_step": launches,
         "max_rel_diff_vs_plain_loop": worst,
         "distinct_tile_pairs": len(tiles),
