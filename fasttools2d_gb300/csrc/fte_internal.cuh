@@ -379,6 +379,8 @@ bool fte_near_uses_ff(const NearParamsHost& hp);
 size_t fte_near_ff_ws(int kind, int nv, int64_t nsrc);
 void fte_near_ff_attach(NearParamsHost* hp, int kind, int nv, int64_t nsrc, void* mem);
 int fte_near_ff_prep(fte_context* ctx, int kind, int nv, const NearParamsHost& hp);
+// the same for many descriptions (device array plist_dev, a warp per (description, box) item)
+int fte_near_ff_prep_batch(fte_context* ctx, int kind, int nv, const void* plist_dev, const int2* items, int nitems);
 // sources staged per chunk (ff: the description uses the float-float class)
 int fte_near_cap(const fte_context* ctx, int kind, int nv, bool ff);
 // nv (1..4) density vectors at q* + v*cl.qstride; outputs at ur + v*ustride
@@ -407,6 +409,18 @@ struct KspaceArgs {
     // spread / gather tile sizes (grid nodes a side); 0: the default rule
     int ts_spread = 0, ts_gather = 0;
 };
+// Work lists of many float-float k-space evaluations (batches): each added
+// evaluation (scratch carved from wc as fte_kspace_run carves it, tile bins
+// prebuilt) becomes an item of one launch per stage; *taken = false when its
+// form or shape needs the per-call path (FP64/FP32 k-space, long
+// transforms, untiled spread/gather, the FP64 multiplier).
+struct KMulti;
+int fte_kmulti_create(KMulti** out);
+int fte_kmulti_add(KMulti* km, fte_context* ctx, WsCarver& wc, const KspaceArgs& a, bool* taken);
+int fte_kmulti_finalize(KMulti* km, fte_context* ctx);
+int fte_kmulti_run(KMulti* km, fte_context* ctx);
+int fte_kmulti_items(const KMulti* km);
+void fte_kmulti_destroy(KMulti* km);
 size_t fte_kspace_ws(int kind, int form, int Mx, int My, int64_t nsrc, int64_t ntar);
 // float-float form: bytes of the sources' window records (0 for the other forms)
 size_t fte_kspace_rec_ws(int form, int64_t nsrc);

@@ -24,8 +24,12 @@
 // of the multiplier at (k1, k2) and at the Nyquist-mirrored wave vector
 // (k1', k2') (k' = -k on a Nyquist index, k' = k elsewhere); this reproduces
 // real(ifft2(.)) of the full-grid reference exactly.
+#include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <mutex>
+#include <new>
+#include <vector>
 
 #include "ff.cuh"
 #include "fft.cuh"
@@ -560,11 +564,12 @@ __global__ void k_fft_y_c2r(const double2* __restrict__ Hh, double* __restrict__
 // ---- the same three transforms in float-float (FFT lines of FfCx) --------------
 // (two CTAs of up to 512 threads per SM: registers capped at 64 so that a
 // second line's transform hides the first's barrier and load latency)
-__global__ void __launch_bounds__(512, 2) k_fft_y_r2c_ff(const double* __restrict__ H, float4* __restrict__ Hh, int Mx, int My, FftDev plan) {
-    extern __shared__ __align__(16) unsigned char shff[];
+// column pair c of grid g (the kernels: one pair per CTA; the work-list
+// kernels of batches read the evaluation's parameters first)
+__device__ __forceinline__ void fft_y_r2c_ff_line(const double* __restrict__ H, float4* __restrict__ Hh, int Mx,
+                                                  int My, const FftDev& plan, int c, int g, unsigned char* shff) {
     float4* A = reinterpret_cast<float4*>(shff);
     float4* B = A + plan.m;
-    const int c = blockIdx.x, g = blockIdx.y;
     const int Kh = My / 2 + 1;
     const double* h0 = H + ((size_t)g * Mx + 2 * c) * My;
     const double* h1 = h0 + My;
@@ -582,23 +587,33 @@ __global__ void __launch_bounds__(512, 2) k_fft_y_r2c_ff(const double* __restric
     }
 }
 
-__global__ void __launch_bounds__(512, 2) k_fft_x_ff(float4* __restrict__ Hh, int Mx, int Kh, FftDev plan, int inv) {
+__global__ void __launch_bounds__(512, 2) k_fft_y_r2c_ff(const double* __restrict__ H, float4* __restrict__ Hh, int Mx, int My, FftDev plan) {
     extern __shared__ __align__(16) unsigned char shff[];
+    fft_y_r2c_ff_line(H, Hh, Mx, My, plan, blockIdx.x, blockIdx.y, shff);
+}
+
+// line ky = k of grid g
+__device__ __forceinline__ void fft_x_ff_line(float4* __restrict__ Hh, int Mx, int Kh, const FftDev& plan, int inv,
+                                              int k, int g, unsigned char* shff) {
     float4* A = reinterpret_cast<float4*>(shff);
     float4* B = A + plan.m;
-    const int k = blockIdx.x, g = blockIdx.y;
     float4* base = Hh + ((size_t)g * Kh + k) * Mx;  // ky-major half spectra: line k is contiguous
     for (int x = threadIdx.x; x < Mx; x += blockDim.x) A[x] = base[x];
     float4* R = fft_block<FfCx>(A, B, plan, inv != 0);
     for (int x = threadIdx.x; x < Mx; x += blockDim.x) base[x] = R[x];
 }
 
-// half spectra -> real grids as float-float pairs (the gather's input)
-__global__ void __launch_bounds__(512, 2) k_fft_y_c2r_ff(const float4* __restrict__ Hh, float2* __restrict__ H, int Mx, int My, FftDev plan) {
+__global__ void __launch_bounds__(512, 2) k_fft_x_ff(float4* __restrict__ Hh, int Mx, int Kh, FftDev plan, int inv) {
     extern __shared__ __align__(16) unsigned char shff[];
+    fft_x_ff_line(Hh, Mx, Kh, plan, inv, blockIdx.x, blockIdx.y, shff);
+}
+
+// half spectra -> real grids as float-float pairs (the gather's input):
+// column pair c of grid g
+__device__ __forceinline__ void fft_y_c2r_ff_line(const float4* __restrict__ Hh, float2* __restrict__ H, int Mx,
+                                                  int My, const FftDev& plan, int c, int g, unsigned char* shff) {
     float4* A = reinterpret_cast<float4*>(shff);
     float4* B = A + plan.m;
-    const int c = blockIdx.x, g = blockIdx.y;
     const int Kh = My / 2 + 1;
     const float4* i0 = Hh + (size_t)g * Mx * Kh + 2 * c;  // ky-major: columns 2c, 2c + 1 adjacent
     for (int k = threadIdx.x; k < Kh; k += blockDim.x) {
@@ -619,6 +634,11 @@ __global__ void __launch_bounds__(512, 2) k_fft_y_c2r_ff(const float4* __restric
         o0[y] = ffc_re(z);
         o1[y] = ffc_im(z);
     }
+}
+
+__global__ void __launch_bounds__(512, 2) k_fft_y_c2r_ff(const float4* __restrict__ Hh, float2* __restrict__ H, int Mx, int My, FftDev plan) {
+    extern __shared__ __align__(16) unsigned char shff[];
+    fft_y_c2r_ff_line(Hh, H, Mx, My, plan, blockIdx.x, blockIdx.y, shff);
 }
 
 // ---- k-space multipliers ------------------------------------------------------
@@ -759,14 +779,13 @@ __device__ __forceinline__ float4 ffc_avg(float4 a, float4 b) {
     return ffc_mk(ff_scale2(ff_add(ffc_re(a), ffc_re(b)), 0.5f), ff_scale2(ff_add(ffc_im(a), ffc_im(b)), 0.5f));
 }
 
+// modes idx0, idx0 + stride, ... of the half spectra (etab loaded)
 template <int KIND>
-__global__ void k_filter_ff(float4* __restrict__ Hh, int Mx, int My, FfFilt f, int ng) {
-    __shared__ float2 etab[64];
-    for (int i = threadIdx.x; i < 64; i += blockDim.x) etab[i] = ff_split(exp2(-i / 64.0));
-    __syncthreads();
+__device__ __forceinline__ void filter_ff_run(float4* __restrict__ Hh, int Mx, int My, const FfFilt& f, int ng,
+                                              size_t idx0, size_t stride, const float2* etab) {
     const int Kh = My / 2 + 1;
     const size_t GS = (size_t)Mx * Kh;
-    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < GS; idx += (size_t)gridDim.x * blockDim.x) {
+    for (size_t idx = idx0; idx < GS; idx += stride) {
         const int k = (int)(idx / Mx), j = (int)(idx % Mx);  // ky-major half spectra
         float4* p0 = Hh + idx;
         if (j == 0 && k == 0) {
@@ -803,6 +822,15 @@ __global__ void k_filter_ff(float4* __restrict__ Hh, int Mx, int My, FfFilt f, i
         p0[0] = g1;
         p0[GS] = g2;
     }
+}
+
+template <int KIND>
+__global__ void k_filter_ff(float4* __restrict__ Hh, int Mx, int My, FfFilt f, int ng) {
+    __shared__ float2 etab[64];
+    for (int i = threadIdx.x; i < 64; i += blockDim.x) etab[i] = ff_split(exp2(-i / 64.0));
+    __syncthreads();
+    filter_ff_run<KIND>(Hh, Mx, My, f, ng, blockIdx.x * (size_t)blockDim.x + threadIdx.x,
+                        (size_t)gridDim.x * blockDim.x, etab);
 }
 
 FfFilt ff_filter_consts(double Lx, double Ly, double xi, double eta) {
@@ -1374,18 +1402,17 @@ __device__ __forceinline__ double e0_arg(double px, double py, const WinParams& 
     return wp.aniso ? px * px + py * py + 2 * (wp.w * px + wp.wy * py) : px * px + py * py + 2 * wp.w * (px + py);
 }
 
-// window records of the sources in tile order (k indexes perm)
-__global__ void k_ff_win(int kind, const double* __restrict__ p, const double* __restrict__ f,
-                         const double* __restrict__ nrm, const double* __restrict__ wts, const int* __restrict__ perm,
-                         int64_t n, WinParams wp, FfWin* __restrict__ out) {
-    // the three window factors as float-float exponentials of FP64 arguments:
-    // e0 = ex e4y = exp(t (px^2 + py^2 + 2 w (px + py))), e3x = exp(-2 t h px),
-    // e3y = exp(-2 t h py), t = -2 xi^2 / eta (the factors of window_of)
-    __shared__ float2 etab[64];
-    for (int j = threadIdx.x; j < 64; j += blockDim.x) etab[j] = ff_split(exp2(-j / 64.0));
-    __syncthreads();
+// the window record of the k-th source in tile order: the three window
+// factors as float-float exponentials of FP64 arguments, e0 = ex e4y =
+// exp(t (px^2 + py^2 + 2 w (px + py))), e3x = exp(-2 t h px), e3y =
+// exp(-2 t h py), t = -2 xi^2 / eta (the factors of window_of), and the
+// densities; etab = 2^(-j/64), j < 64, in float-float
+__device__ __forceinline__ void ff_win_rec(int kind, const double* __restrict__ p, const double* __restrict__ f,
+                                           const double* __restrict__ nrm, const double* __restrict__ wts,
+                                           const int* __restrict__ perm, int64_t k, const WinParams& wp,
+                                           const float2* etab, FfWin* __restrict__ out) {
     const double t = -2 * wp.xi * wp.xi / wp.eta;
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    {
         const int i = perm[k];
         int mx, my;
         double px, py;
@@ -1418,6 +1445,21 @@ __global__ void k_ff_win(int kind, const double* __restrict__ p, const double* _
     }
 }
 
+__device__ __forceinline__ void load_etab(float2* etab) {
+    for (int j = threadIdx.x; j < 64; j += blockDim.x) etab[j] = ff_split(exp2(-j / 64.0));
+}
+
+// window records of the sources in tile order (k indexes perm)
+__global__ void k_ff_win(int kind, const double* __restrict__ p, const double* __restrict__ f,
+                         const double* __restrict__ nrm, const double* __restrict__ wts, const int* __restrict__ perm,
+                         int64_t n, WinParams wp, FfWin* __restrict__ out) {
+    __shared__ float2 etab[64];
+    load_etab(etab);
+    __syncthreads();
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+        ff_win_rec(kind, p, f, nrm, wts, perm, k, wp, etab, out);
+}
+
 // Column-owned spread of grids (2 pass, 2 pass + 1) in float-float: the
 // scheme of k_spread_cols (warp w adds every region column c = w mod warps,
 // lane j window row j) with the first two grids' (sum, low parts) interleaved
@@ -1425,12 +1467,13 @@ __global__ void k_ff_win(int kind, const double* __restrict__ p, const double* _
 // region is flushed to the FP64 grids.  NG = 2 (Stokeslet: f1, f2) or 3
 // (stresslet: the symmetric products f1 n1, f1 n2 + f2 n1, f2 n2 -- the
 // stresslet multiplier sees the two mixed products only through their sum).
+// tiles tile0, tile0 + tstep, ... of one grid (the kernels below: a grid-
+// stride loop over one evaluation's tiles, or one tile of a work list)
 template <int NG>
-__global__ void __launch_bounds__(kColThreads) k_spread_ff(const FfWin* __restrict__ recs,
-                                                          const int* __restrict__ toff, int ts, int ntx, int nty,
-                                                          WinParams wp, double* __restrict__ H0,
-                                                          double* __restrict__ H1, double* __restrict__ H2) {
-    extern __shared__ __align__(16) unsigned char shraw[];
+__device__ __forceinline__ void spread_ff_run(const FfWin* __restrict__ recs, const int* __restrict__ toff, int ts,
+                                              int ntx, int nty, const WinParams& wp, double* __restrict__ H0,
+                                              double* __restrict__ H1, double* __restrict__ H2, int tile0, int tstep,
+                                              unsigned char* shraw) {
     const int P1 = wp.P + 1, W = tile_region(ts, wp.P), WW = W * W;
     const int P1e = (P1 + 1) & ~1;
     float4* buf = reinterpret_cast<float4*>(shraw);  // WW: (grid 0 sum, low, grid 1 sum, low)
@@ -1444,7 +1487,7 @@ __global__ void __launch_bounds__(kColThreads) k_spread_ff(const FfWin* __restri
     const float2* e1y = e1y_of(e1, wp);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     constexpr int nw = kColWarps;
-    for (int tile = blockIdx.x; tile < ntx * nty; tile += gridDim.x) {
+    for (int tile = tile0; tile < ntx * nty; tile += tstep) {
         const int k0 = toff[tile], k1 = toff[tile + 1];
         if (k0 == k1) continue;
         const int ox = (tile % ntx) * ts - wp.P / 2 - 2, oy = (tile / ntx) * ts - wp.P / 2 - 2;
@@ -1553,6 +1596,15 @@ __global__ void __launch_bounds__(kColThreads) k_spread_ff(const FfWin* __restri
     }
 }
 
+template <int NG>
+__global__ void __launch_bounds__(kColThreads) k_spread_ff(const FfWin* __restrict__ recs,
+                                                          const int* __restrict__ toff, int ts, int ntx, int nty,
+                                                          WinParams wp, double* __restrict__ H0,
+                                                          double* __restrict__ H1, double* __restrict__ H2) {
+    extern __shared__ __align__(16) unsigned char shraw[];
+    spread_ff_run<NG>(recs, toff, ts, ntx, nty, wp, H0, H1, H2, blockIdx.x, gridDim.x, shraw);
+}
+
 size_t spread_ff_smem(int ts, int P, int ng, int aniso = 0) {
     const int P1 = P + 1, W = tile_region(ts, P);
     const size_t third = ng == 3 ? ((size_t)W * W + (size_t)kColChunk * P1) * sizeof(float2) : 0;
@@ -1585,24 +1637,22 @@ __global__ void k_ff_join(double* __restrict__ H, int64_t n) {
 // shared-memory traffic for the weights); PM == 0: any support, the window
 // column in a per-thread shared-memory row.
 template <int PM>
-__global__ void __launch_bounds__(kTileThreads, 5) k_gather_ff(const double* __restrict__ p, const int* __restrict__ toff,
-                                                           const int* __restrict__ perm, int ts, int ntx, int nty,
-                                                           WinParams wp, const float2* __restrict__ G0,
-                                                           const float2* __restrict__ G1, double scale,
-                                                           double2* __restrict__ out) {
-    extern __shared__ __align__(16) unsigned char shraw[];
+__device__ __forceinline__ void gather_ff_run(const double* __restrict__ p, const int* __restrict__ toff,
+                                              const int* __restrict__ perm, int ts, int ntx, int nty,
+                                              const WinParams& wp, const float2* __restrict__ G0,
+                                              const float2* __restrict__ G1, double scale, double2* __restrict__ out,
+                                              int tile0, int tstep, unsigned char* shraw, float2* etab) {
     float2* shf = reinterpret_cast<float2*>(shraw);
     const int P1 = wp.P + 1, W = tile_region(ts, wp.P), WW = W * W;
     float2* r0 = shf;
     float2* r1 = r0 + WW;
     float2* e1 = r1 + WW;
     float2* wyb = e1 + e1_len(wp.P, wp.aniso) + threadIdx.x * P1;  // PM == 0 only
-    __shared__ float2 etab[64];  // 2^(-j/64) for the window factors (as in k_ff_win)
-    for (int j = threadIdx.x; j < 64; j += blockDim.x) etab[j] = ff_split(exp2(-j / 64.0));
+    load_etab(etab);  // 2^(-j/64) for the window factors (as in k_ff_win)
     load_e1_ff(e1, wp);
     const float2* e1y = e1y_of(e1, wp);
     const double tw = -2 * wp.xi * wp.xi / wp.eta;
-    for (int tile = blockIdx.x; tile < ntx * nty; tile += gridDim.x) {
+    for (int tile = tile0; tile < ntx * nty; tile += tstep) {
         const int k0 = toff[tile], k1 = toff[tile + 1];
         if (k0 == k1) continue;
         const int ox = (tile % ntx) * ts - wp.P / 2 - 2, oy = (tile / ntx) * ts - wp.P / 2 - 2;
@@ -1690,6 +1740,17 @@ __global__ void __launch_bounds__(kTileThreads, 5) k_gather_ff(const double* __r
             out[i] = make_double2(ff_join(a0, c0) * scale, ff_join(a1, c1) * scale);
         }
     }
+}
+
+template <int PM>
+__global__ void __launch_bounds__(kTileThreads, 5) k_gather_ff(const double* __restrict__ p, const int* __restrict__ toff,
+                                                           const int* __restrict__ perm, int ts, int ntx, int nty,
+                                                           WinParams wp, const float2* __restrict__ G0,
+                                                           const float2* __restrict__ G1, double scale,
+                                                           double2* __restrict__ out) {
+    extern __shared__ __align__(16) unsigned char shraw[];
+    __shared__ float2 etab[64];
+    gather_ff_run<PM>(p, toff, perm, ts, ntx, nty, wp, G0, G1, scale, out, blockIdx.x, gridDim.x, shraw, etab);
 }
 
 // the register form's support bound for window support P1 (0: none fits)
@@ -2264,6 +2325,358 @@ int fte_kspace_run(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, fte_info
     }
     FTE_TRY(fte_record(ctx, 5));
     (void)info;
+    return FTE_OK;
+}
+
+// ===========================================================================
+// Work lists of many float-float k-space evaluations (the batches of plans).
+//
+// A batch evaluates many (plan, density vector) pairs.  Where a plan's
+// k-space part is the float-float form on block transforms with tiled spread
+// and gather (what the tuned choice picks for batches at tol >= 1e-11), its
+// evaluations become items of one work list per stage instead of one launch
+// per stage and evaluation: grid clearing, window records, spread (Stokeslet
+// and stresslet), the y transforms, the x transforms, the multipliers, the
+// inverse transforms and the gather each run as one launch over every item's
+// blocks (a block reads its item's parameters from a device array; transforms
+// are grouped by line length so that a short line's block does not carry a
+// long line's shared memory).  The arithmetic is the per-call kernels' own
+// (the same device functions), so results match the per-plan path.
+// ===========================================================================
+namespace {
+
+struct KItem {
+    WinParams wp;
+    FftDev py, px;
+    FfFilt ffc;
+    int kind, ngs, Mx, My, Kh, PM;
+    int64_t nsrc, ntar;
+    double* H;    // the spread's FP64 grids, later the float-float grids of the gather
+    float4* Hf;   // float-float half spectra
+    FfWin* recs;  // window records of the sources in tile order
+    const double *psrc, *f, *nrm, *wts;
+    const int *toff_s, *perm_s;
+    int ts_s, ntx_s, nty_s;
+    const double* ptar;
+    const int *toff_g, *perm_g;
+    int ts_g, ntx_g, nty_g;
+    double scale;
+    double2* uk;
+};
+
+constexpr int kZeroPerThread = 8;
+constexpr int kFftClasses = 4;
+int fft_class(int m) { return m <= 256 ? 0 : (m <= 1024 ? 1 : (m <= 4096 ? 2 : 3)); }
+
+__global__ void k_zero_multi(const KItem* __restrict__ items, const int2* __restrict__ wl) {
+    const int2 w = wl[blockIdx.x];
+    const KItem& it = items[w.x];
+    const size_t n = (size_t)it.ngs * it.Mx * it.My;
+    const size_t base = (size_t)w.y * blockDim.x * kZeroPerThread;
+    for (int j = 0; j < kZeroPerThread; j++) {
+        const size_t i = base + (size_t)j * blockDim.x + threadIdx.x;
+        if (i < n) it.H[i] = 0.0;
+    }
+}
+
+__global__ void k_ff_win_multi(const KItem* __restrict__ items, const int2* __restrict__ wl) {
+    __shared__ float2 etab[64];
+    load_etab(etab);
+    __syncthreads();
+    const int2 w = wl[blockIdx.x];
+    const KItem& it = items[w.x];
+    const int64_t k = (int64_t)w.y * blockDim.x + threadIdx.x;
+    if (k < it.nsrc) {
+        const WinParams wp = it.wp;
+        ff_win_rec(it.kind, it.psrc, it.f, it.nrm, it.wts, it.perm_s, k, wp, etab, it.recs);
+    }
+}
+
+template <int NG>
+__global__ void __launch_bounds__(kColThreads) k_spread_ff_multi(const KItem* __restrict__ items,
+                                                                const int2* __restrict__ wl) {
+    extern __shared__ __align__(16) unsigned char shraw[];
+    const int2 w = wl[blockIdx.x];
+    const KItem& it = items[w.x];
+    const WinParams wp = it.wp;
+    const size_t G = (size_t)it.Mx * it.My;
+    spread_ff_run<NG>(it.recs, it.toff_s, it.ts_s, it.ntx_s, it.nty_s, wp, it.H, it.H + G,
+                      NG == 3 ? it.H + 2 * G : nullptr, w.y, it.ntx_s * it.nty_s, shraw);
+}
+
+__global__ void __launch_bounds__(512, 2) k_fft_y_r2c_ff_multi(const KItem* __restrict__ items,
+                                                               const int2* __restrict__ wl) {
+    extern __shared__ __align__(16) unsigned char shff[];
+    const int2 w = wl[blockIdx.x];
+    const KItem& it = items[w.x];
+    const FftDev plan = it.py;
+    const int half = it.Mx / 2;
+    fft_y_r2c_ff_line(it.H, it.Hf, it.Mx, it.My, plan, w.y % half, w.y / half, shff);
+}
+
+__global__ void __launch_bounds__(512, 2) k_fft_x_ff_multi(const KItem* __restrict__ items,
+                                                           const int2* __restrict__ wl, int inv) {
+    extern __shared__ __align__(16) unsigned char shff[];
+    const int2 w = wl[blockIdx.x];
+    const KItem& it = items[w.x];
+    const FftDev plan = it.px;
+    fft_x_ff_line(it.Hf, it.Mx, it.Kh, plan, inv, w.y % it.Kh, w.y / it.Kh, shff);
+}
+
+__global__ void __launch_bounds__(512, 2) k_fft_y_c2r_ff_multi(const KItem* __restrict__ items,
+                                                               const int2* __restrict__ wl) {
+    extern __shared__ __align__(16) unsigned char shff[];
+    const int2 w = wl[blockIdx.x];
+    const KItem& it = items[w.x];
+    const FftDev plan = it.py;
+    const int half = it.Mx / 2;
+    fft_y_c2r_ff_line(it.Hf, reinterpret_cast<float2*>(it.H), it.Mx, it.My, plan, w.y % half, w.y / half, shff);
+}
+
+template <int KIND>
+__global__ void k_filter_ff_multi(const KItem* __restrict__ items, const int2* __restrict__ wl) {
+    __shared__ float2 etab[64];
+    load_etab(etab);
+    __syncthreads();
+    const int2 w = wl[blockIdx.x];
+    const KItem& it = items[w.x];
+    const FfFilt f = it.ffc;
+    const size_t GS = (size_t)it.Mx * it.Kh;
+    filter_ff_run<KIND>(it.Hf, it.Mx, it.My, f, it.ngs, (size_t)w.y * blockDim.x + threadIdx.x, GS, etab);
+}
+
+template <int PM>
+__global__ void __launch_bounds__(kTileThreads, 5) k_gather_ff_multi(const KItem* __restrict__ items,
+                                                                     const int2* __restrict__ wl) {
+    extern __shared__ __align__(16) unsigned char shraw[];
+    __shared__ float2 etab[64];
+    const int2 w = wl[blockIdx.x];
+    const KItem& it = items[w.x];
+    const WinParams wp = it.wp;
+    const size_t G = (size_t)it.Mx * it.My;
+    const float2* Hf = reinterpret_cast<const float2*>(it.H);
+    gather_ff_run<PM>(it.ptar, it.toff_g, it.perm_g, it.ts_g, it.ntx_g, it.nty_g, wp, Hf, Hf + G, it.scale, it.uk, w.y,
+                      it.ntx_g * it.nty_g, shraw, etab);
+}
+
+}  // namespace
+
+struct KMulti {
+    struct List {
+        std::vector<int2> h;
+        int2* d = nullptr;
+        size_t smem = 0;
+        int threads = 0;
+        void add(int item, int n) {
+            for (int j = 0; j < n; j++) h.push_back(make_int2(item, j));
+        }
+    };
+    std::vector<KItem> items;
+    KItem* ditems = nullptr;
+    char* mem = nullptr;
+    List zero, win, spread[2], yr2c[kFftClasses], xf[kFftClasses], filt[2], xi[kFftClasses], yc2r[kFftClasses],
+        gather[3];
+    template <typename F>
+    void each(F fn) {
+        fn(zero);
+        fn(win);
+        for (auto& l : spread) fn(l);
+        for (auto& l : yr2c) fn(l);
+        for (auto& l : xf) fn(l);
+        for (auto& l : filt) fn(l);
+        for (auto& l : xi) fn(l);
+        for (auto& l : yc2r) fn(l);
+        for (auto& l : gather) fn(l);
+    }
+};
+
+int fte_kmulti_create(KMulti** out) {
+    *out = new (std::nothrow) KMulti();
+    if (!*out) {
+        fte_set_error("out of host memory");
+        return FTE_ERR_ALLOC;
+    }
+    return FTE_OK;
+}
+
+void fte_kmulti_destroy(KMulti* km) {
+    if (!km) return;
+    if (km->mem) cudaFree(km->mem);
+    delete km;
+}
+
+int fte_kmulti_add(KMulti* km, fte_context* ctx, WsCarver& wc, const KspaceArgs& a, bool* taken) {
+    *taken = false;
+    if (a.form != FTE_FORM_FF || !a.pre_src || !a.pre_tar) return FTE_OK;
+    const int Mx = a.Mx, My = a.My, Kh = My / 2 + 1;
+    if (!fte_fft_fits_block(My, sizeof(double2)) || !fte_fft_fits_block(Mx, sizeof(double2))) return FTE_OK;
+    const int PM = gather_ff_pm(a.P + 1);
+    if (!PM) return FTE_OK;
+    int ts_s = 0, ts_g = 0;
+    FTE_TRY(resolve_tiles(ctx, a, &ts_s, &ts_g));
+    if ((a.nsrc > 0 && (ts_s == 0 || a.pre_src->ts != ts_s)) || (a.ntar > 0 && (ts_g == 0 || a.pre_tar->ts != ts_g)))
+        return FTE_OK;
+    const double kmax = FTE_PI * (Mx / a.Lx > My / a.Ly ? Mx / a.Lx : My / a.Ly);
+    if (fabs(1.0 - a.eta) * 2.0 * kmax * kmax / (4.0 * a.xi * a.xi) >= 75.0) return FTE_OK;  // FP64 multiplier
+    KItem it;
+    std::memset(&it, 0, sizeof(it));
+    it.wp = win_params(a);
+    FTE_TRY(fte_get_plan(ctx, My, &it.py));
+    FTE_TRY(fte_get_plan(ctx, Mx, &it.px));
+    if (2 * (size_t)it.py.m * sizeof(float4) > (size_t)ctx->max_smem_optin ||
+        2 * (size_t)it.px.m * sizeof(float4) > (size_t)ctx->max_smem_optin)
+        return FTE_OK;
+    // the scratch as fte_kspace_run carves it: grids, half spectra, records
+    const int ng = a.kind == FTE_KIND_SLP ? 2 : 4;
+    const size_t G = (size_t)Mx * My;
+    it.H = wc.take<double>(ng * G);
+    it.Hf = reinterpret_cast<float4*>(wc.take<double2>(ng * (size_t)Mx * Kh));
+    it.recs = a.nsrc > 0 ? wc.take<FfWin>(a.nsrc) : nullptr;
+    FTE_WS_CHECK(wc);
+    it.ffc = ff_filter_consts(a.Lx, a.Ly, a.xi, a.eta);
+    it.kind = a.kind;
+    it.ngs = a.kind == FTE_KIND_SLP ? 2 : 3;
+    it.Mx = Mx;
+    it.My = My;
+    it.Kh = Kh;
+    it.PM = PM;
+    it.nsrc = a.nsrc;
+    it.ntar = a.ntar;
+    it.psrc = a.psrc;
+    it.f = a.f;
+    it.nrm = a.nrm;
+    it.wts = a.wts;
+    it.toff_s = a.pre_src->off;
+    it.perm_s = a.pre_src->perm;
+    it.ts_s = a.pre_src->ts;
+    it.ntx_s = a.nsrc > 0 ? a.pre_src->ntx : 0;
+    it.nty_s = a.nsrc > 0 ? a.pre_src->nty : 0;
+    it.ptar = a.ptar;
+    it.toff_g = a.pre_tar->off;
+    it.perm_g = a.pre_tar->perm;
+    it.ts_g = a.pre_tar->ts;
+    it.ntx_g = a.ntar > 0 ? a.pre_tar->ntx : 0;
+    it.nty_g = a.ntar > 0 ? a.pre_tar->nty : 0;
+    it.scale = gather_scale(a);
+    it.uk = a.uk;
+    const int i = (int)km->items.size();
+    km->items.push_back(it);
+    // work lists (blocks of every stage) and launch shapes
+    const int an = it.wp.aniso;
+    km->zero.add(i, (int)(((size_t)it.ngs * G + 256 * kZeroPerThread - 1) / (256 * kZeroPerThread)));
+    if (a.nsrc > 0) {
+        km->win.add(i, (int)((a.nsrc + 255) / 256));
+        KMulti::List& sp = km->spread[it.ngs == 2 ? 0 : 1];
+        sp.add(i, it.ntx_s * it.nty_s);
+        sp.smem = std::max(sp.smem, spread_ff_smem(it.ts_s, a.P, it.ngs, an));
+    }
+    const int cy = fft_class(it.py.m), cx = fft_class(it.px.m);
+    const size_t smy = 2 * (size_t)it.py.m * sizeof(float4), smx = 2 * (size_t)it.px.m * sizeof(float4);
+    auto shape = [](KMulti::List& l, size_t sm, int th) {
+        l.smem = std::max(l.smem, sm);
+        l.threads = std::max(l.threads, th);
+    };
+    km->yr2c[cy].add(i, (Mx / 2) * it.ngs);
+    shape(km->yr2c[cy], smy, fft_threads(it.py.m));
+    km->xf[cx].add(i, Kh * it.ngs);
+    shape(km->xf[cx], smx, fft_threads(it.px.m));
+    km->filt[a.kind == FTE_KIND_SLP ? 0 : 1].add(i, (int)(((size_t)Mx * Kh + 255) / 256));
+    km->xi[cx].add(i, Kh * 2);
+    shape(km->xi[cx], smx, fft_threads(it.px.m));
+    km->yc2r[cy].add(i, (Mx / 2) * 2);
+    shape(km->yc2r[cy], smy, fft_threads(it.py.m));
+    if (a.ntar > 0) {
+        KMulti::List& ga = km->gather[PM == 16 ? 0 : (PM == 24 ? 1 : 2)];
+        ga.add(i, it.ntx_g * it.nty_g);
+        ga.smem = std::max(ga.smem, gather_ff_smem(it.ts_g, a.P, an));
+    }
+    *taken = true;
+    return FTE_OK;
+}
+
+int fte_kmulti_finalize(KMulti* km, fte_context* ctx) {
+    if (km->items.empty()) return FTE_OK;
+    size_t need = ws_bytes(km->items.size() * sizeof(KItem), 1) + 4096;
+    km->each([&](KMulti::List& l) { need += ws_bytes(l.h.size() * sizeof(int2), 1); });
+    if (fte_alloc_should_fail() || cudaMalloc(&km->mem, need) != cudaSuccess) {
+        cudaGetLastError();
+        km->mem = nullptr;
+        fte_set_error("batch: %zu bytes of device memory for the k-space work lists not available", need);
+        return FTE_ERR_ALLOC;
+    }
+    WsCarver c{km->mem, 0, need};
+    km->ditems = c.take<KItem>(km->items.size());
+    km->each([&](KMulti::List& l) { l.d = l.h.empty() ? nullptr : c.take<int2>(l.h.size()); });
+    FTE_WS_CHECK(c);
+    FTE_CUDA_TRY(cudaMemcpyAsync(km->ditems, km->items.data(), km->items.size() * sizeof(KItem),
+                                 cudaMemcpyHostToDevice, ctx->stream));
+    cudaError_t e = cudaSuccess;
+    km->each([&](KMulti::List& l) {
+        if (l.d && e == cudaSuccess)
+            e = cudaMemcpyAsync(l.d, l.h.data(), l.h.size() * sizeof(int2), cudaMemcpyHostToDevice, ctx->stream);
+    });
+    FTE_CUDA_TRY(e);
+    FTE_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return FTE_OK;
+}
+
+int fte_kmulti_items(const KMulti* km) { return km ? (int)km->items.size() : 0; }
+
+int fte_kmulti_run(KMulti* km, fte_context* ctx) {
+    if (!km || km->items.empty()) return FTE_OK;
+    const KItem* it = km->ditems;
+    auto n = [](const KMulti::List& l) { return (int)l.h.size(); };
+    if (n(km->zero)) FTE_LAUNCH(ctx, k_zero_multi, n(km->zero), 256, 0, it, (const int2*)km->zero.d);
+    if (n(km->win)) FTE_LAUNCH(ctx, k_ff_win_multi, n(km->win), 256, 0, it, (const int2*)km->win.d);
+    if (n(km->spread[0])) {
+        FTE_CUDA_TRY(fte_smem_ceiling(k_spread_ff_multi<2>, km->spread[0].smem));
+        FTE_LAUNCH(ctx, k_spread_ff_multi<2>, n(km->spread[0]), kColThreads, km->spread[0].smem, it,
+                   (const int2*)km->spread[0].d);
+    }
+    if (n(km->spread[1])) {
+        FTE_CUDA_TRY(fte_smem_ceiling(k_spread_ff_multi<3>, km->spread[1].smem));
+        FTE_LAUNCH(ctx, k_spread_ff_multi<3>, n(km->spread[1]), kColThreads, km->spread[1].smem, it,
+                   (const int2*)km->spread[1].d);
+    }
+    for (auto& l : km->yr2c)
+        if (n(l)) {
+            FTE_CUDA_TRY(fte_smem_ceiling(k_fft_y_r2c_ff_multi, l.smem));
+            FTE_LAUNCH(ctx, k_fft_y_r2c_ff_multi, n(l), l.threads, l.smem, it, (const int2*)l.d);
+        }
+    for (auto& l : km->xf)
+        if (n(l)) {
+            FTE_CUDA_TRY(fte_smem_ceiling(k_fft_x_ff_multi, l.smem));
+            FTE_LAUNCH(ctx, k_fft_x_ff_multi, n(l), l.threads, l.smem, it, (const int2*)l.d, 0);
+        }
+    if (n(km->filt[0])) FTE_LAUNCH(ctx, k_filter_ff_multi<FTE_KIND_SLP>, n(km->filt[0]), 256, 0, it,
+                                   (const int2*)km->filt[0].d);
+    if (n(km->filt[1])) FTE_LAUNCH(ctx, k_filter_ff_multi<FTE_KIND_DLP>, n(km->filt[1]), 256, 0, it,
+                                   (const int2*)km->filt[1].d);
+    for (auto& l : km->xi)
+        if (n(l)) {
+            FTE_CUDA_TRY(fte_smem_ceiling(k_fft_x_ff_multi, l.smem));
+            FTE_LAUNCH(ctx, k_fft_x_ff_multi, n(l), l.threads, l.smem, it, (const int2*)l.d, 1);
+        }
+    for (auto& l : km->yc2r)
+        if (n(l)) {
+            FTE_CUDA_TRY(fte_smem_ceiling(k_fft_y_c2r_ff_multi, l.smem));
+            FTE_LAUNCH(ctx, k_fft_y_c2r_ff_multi, n(l), l.threads, l.smem, it, (const int2*)l.d);
+        }
+    if (n(km->gather[0])) {
+        FTE_CUDA_TRY(fte_smem_ceiling(k_gather_ff_multi<16>, km->gather[0].smem));
+        FTE_LAUNCH(ctx, k_gather_ff_multi<16>, n(km->gather[0]), kTileThreads, km->gather[0].smem, it,
+                   (const int2*)km->gather[0].d);
+    }
+    if (n(km->gather[1])) {
+        FTE_CUDA_TRY(fte_smem_ceiling(k_gather_ff_multi<24>, km->gather[1].smem));
+        FTE_LAUNCH(ctx, k_gather_ff_multi<24>, n(km->gather[1]), kTileThreads, km->gather[1].smem, it,
+                   (const int2*)km->gather[1].d);
+    }
+    if (n(km->gather[2])) {
+        FTE_CUDA_TRY(fte_smem_ceiling(k_gather_ff_multi<32>, km->gather[2].smem));
+        FTE_LAUNCH(ctx, k_gather_ff_multi<32>, n(km->gather[2]), kTileThreads, km->gather[2].smem, it,
+                   (const int2*)km->gather[2].d);
+    }
     return FTE_OK;
 }
 

@@ -1050,12 +1050,13 @@ __global__ void __launch_bounds__(NearCfg<FF>::threads, NearCfg<FF>::ctas) k_nea
 // relative to the centre of the source's own box, and the staged density
 // values (SLP: f1, f2; DLP: S11, (S12 + S21)/2, S22, S11 + S22) as
 // float-float.  A warp per box.
+// box b of one description, by one warp
 template <int KIND>
-__global__ void k_near_ff_prep(const NearParams prm, int nv, float4* __restrict__ sff, float2* __restrict__ qff) {
+__device__ __forceinline__ void near_ff_prep_box(const NearParams& prm, int nv, int b, float4* __restrict__ sff,
+                                                 float2* __restrict__ qff) {
     constexpr int kDen = KIND == FTE_KIND_SLP ? 2 : 4;
     const int lane = threadIdx.x & 31;
-    const int wpb = blockDim.x >> 5;
-    for (int b = blockIdx.x * wpb + (threadIdx.x >> 5); b < prm.nb; b += gridDim.x * wpb) {
+    {
         const int bx = b % prm.nsx, by = b / prm.nsx;
         const double2 bc = box_centre(prm, bx, by);
         const double cx = bc.x, cy = bc.y;
@@ -1080,6 +1081,25 @@ __global__ void k_near_ff_prep(const NearParams prm, int nv, float4* __restrict_
             }
         }
     }
+}
+
+template <int KIND>
+__global__ void k_near_ff_prep(const NearParams prm, int nv, float4* __restrict__ sff, float2* __restrict__ qff) {
+    const int wpb = blockDim.x >> 5;
+    for (int b = blockIdx.x * wpb + (threadIdx.x >> 5); b < prm.nb; b += gridDim.x * wpb)
+        near_ff_prep_box<KIND>(prm, nv, b, sff, qff);
+}
+
+// many descriptions at once: one warp per (description, box) work item
+template <int KIND>
+__global__ void k_near_ff_prep_batch(const unsigned char* __restrict__ plist, const int2* __restrict__ items,
+                                     int nitems, int nv) {
+    const int wpb = blockDim.x >> 5;
+    const int it = blockIdx.x * wpb + (threadIdx.x >> 5);
+    if (it >= nitems) return;
+    const int2 w = items[it];
+    const NearParams& prm = *reinterpret_cast<const NearParams*>(plist + (size_t)w.x * kParamStride);
+    near_ff_prep_box<KIND>(prm, nv, w.y, const_cast<float4*>(prm.sff), const_cast<float2*>(prm.qff));
 }
 
 template <int KIND, int NV>
@@ -1384,6 +1404,19 @@ void fte_near_ff_attach(NearParamsHost* hp, int kind, int nv, int64_t nsrc, void
     const float hx = (float)bx, hy = (float)by;
     p.bsxff = make_float2(hx, (float)(bx - (double)hx));
     p.bsyff = make_float2(hy, (float)(by - (double)hy));
+}
+
+int fte_near_ff_prep_batch(fte_context* ctx, int kind, int nv, const void* plist_dev, const int2* items,
+                           int nitems) {
+    if (nitems < 1) return FTE_OK;
+    const int grid = (nitems + 7) / 8;
+    if (kind == FTE_KIND_SLP)
+        FTE_LAUNCH(ctx, k_near_ff_prep_batch<FTE_KIND_SLP>, grid, 256, 0, (const unsigned char*)plist_dev, items,
+                   nitems, nv);
+    else
+        FTE_LAUNCH(ctx, k_near_ff_prep_batch<FTE_KIND_DLP>, grid, 256, 0, (const unsigned char*)plist_dev, items,
+                   nitems, nv);
+    return FTE_OK;
 }
 
 int fte_near_ff_prep(fte_context* ctx, int kind, int nv, const NearParamsHost& hp) {

@@ -25,13 +25,15 @@
 
 namespace {
 
-// sorted (cell-ordered) densities for nv vectors and packed f per vector
+// sorted (cell-ordered) densities for nv vectors and packed f per vector:
+// sorted source d
 template <int KIND>
-__global__ void k_plan_dens(const double* __restrict__ f1s, const double* __restrict__ f2s, int nv, int64_t n,
-                            const double* __restrict__ nrm, const double* __restrict__ wts,
-                            const int* __restrict__ sidx, double* __restrict__ q0, double* __restrict__ q1,
-                            double* __restrict__ q2, double* __restrict__ fv) {
-    for (int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; d < n; d += (int64_t)gridDim.x * blockDim.x) {
+__device__ __forceinline__ void plan_dens_one(const double* __restrict__ f1s, const double* __restrict__ f2s, int nv,
+                                              int64_t n, const double* __restrict__ nrm,
+                                              const double* __restrict__ wts, const int* __restrict__ sidx,
+                                              double* __restrict__ q0, double* __restrict__ q1,
+                                              double* __restrict__ q2, double* __restrict__ fv, int64_t d) {
+    {
         const int i = sidx[d];
         const double w = wts ? wts[i] : 1.0;
         for (int v = 0; v < nv; v++) {
@@ -53,11 +55,20 @@ __global__ void k_plan_dens(const double* __restrict__ f1s, const double* __rest
     }
 }
 
-// zero mode sum_s (f.n) x_s per vector (stresslet), one block per vector
-__global__ void k_plan_zero(const double* __restrict__ ps, const double* __restrict__ fv,
-                            const double* __restrict__ nrm, const double* __restrict__ wts, int64_t n,
-                            double* __restrict__ zero) {
-    const int v = blockIdx.x;
+template <int KIND>
+__global__ void k_plan_dens(const double* __restrict__ f1s, const double* __restrict__ f2s, int nv, int64_t n,
+                            const double* __restrict__ nrm, const double* __restrict__ wts,
+                            const int* __restrict__ sidx, double* __restrict__ q0, double* __restrict__ q1,
+                            double* __restrict__ q2, double* __restrict__ fv) {
+    for (int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; d < n; d += (int64_t)gridDim.x * blockDim.x)
+        plan_dens_one<KIND>(f1s, f2s, nv, n, nrm, wts, sidx, q0, q1, q2, fv, d);
+}
+
+// zero mode sum_s (f.n) x_s of vector v (stresslet), by one block of 256
+// threads
+__device__ __forceinline__ void plan_zero_vec(const double* __restrict__ ps, const double* __restrict__ fv,
+                                              const double* __restrict__ nrm, const double* __restrict__ wts,
+                                              int64_t n, double* __restrict__ zero, int v) {
     double zx = 0, zy = 0;
     for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
         const double w = wts ? wts[i] : 1.0;
@@ -82,16 +93,71 @@ __global__ void k_plan_zero(const double* __restrict__ ps, const double* __restr
     }
 }
 
+// one block per vector
+__global__ void k_plan_zero(const double* __restrict__ ps, const double* __restrict__ fv,
+                            const double* __restrict__ nrm, const double* __restrict__ wts, int64_t n,
+                            double* __restrict__ zero) {
+    plan_zero_vec(ps, fv, nrm, wts, n, zero, blockIdx.x);
+}
+
+// u = ur + uk (+ the zero mode) of target i for nv vectors
+__device__ __forceinline__ void plan_combine_one(const double2* __restrict__ ur, const double2* __restrict__ uk,
+                                                 int nv, int64_t n, const double* __restrict__ zero, double inv_area,
+                                                 double* __restrict__ u1s, double* __restrict__ u2s, int64_t i) {
+    for (int v = 0; v < nv; v++) {
+        double2 r = ur[v * n + i], k = uk[v * n + i];
+        double zx = zero ? zero[2 * v] * inv_area : 0.0, zy = zero ? zero[2 * v + 1] * inv_area : 0.0;
+        u1s[v * n + i] = r.x + k.x + zx;
+        u2s[v * n + i] = r.y + k.y + zy;
+    }
+}
+
 __global__ void k_plan_combine(const double2* __restrict__ ur, const double2* __restrict__ uk, int nv, int64_t n,
                                const double* __restrict__ zero, double inv_area, double* __restrict__ u1s,
                                double* __restrict__ u2s) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        for (int v = 0; v < nv; v++) {
-            double2 r = ur[v * n + i], k = uk[v * n + i];
-            double zx = zero ? zero[2 * v] * inv_area : 0.0, zy = zero ? zero[2 * v + 1] * inv_area : 0.0;
-            u1s[v * n + i] = r.x + k.x + zx;
-            u2s[v * n + i] = r.y + k.y + zy;
-        }
+        plan_combine_one(ur, uk, nv, n, zero, inv_area, u1s, u2s, i);
+}
+
+// ---- a batch's per-plan work as work lists (one launch for all plans) -----
+struct PItem {
+    int kind, nv;
+    int64_t nsrc, ntar;
+    const double *f1s, *f2s, *nrm, *wts, *ps;
+    const int* sidx;
+    double *q0, *q1, *q2, *fv, *zero;
+    const double2 *ur, *uk;
+    double *u1s, *u2s;
+    double inv_area;
+};
+
+// work items (plan, block of 256 sorted sources)
+__global__ void k_plan_dens_multi(const PItem* __restrict__ items, const int2* __restrict__ wl) {
+    const int2 w = wl[blockIdx.x];
+    const PItem& it = items[w.x];
+    const int64_t d = (int64_t)w.y * blockDim.x + threadIdx.x;
+    if (d >= it.nsrc) return;
+    if (it.kind == FTE_KIND_SLP)
+        plan_dens_one<FTE_KIND_SLP>(it.f1s, it.f2s, it.nv, it.nsrc, it.nrm, it.wts, it.sidx, it.q0, it.q1, it.q2,
+                                    it.fv, d);
+    else
+        plan_dens_one<FTE_KIND_DLP>(it.f1s, it.f2s, it.nv, it.nsrc, it.nrm, it.wts, it.sidx, it.q0, it.q1, it.q2,
+                                    it.fv, d);
+}
+
+// work items (stresslet plan, vector)
+__global__ void k_plan_zero_multi(const PItem* __restrict__ items, const int2* __restrict__ wl) {
+    const int2 w = wl[blockIdx.x];
+    const PItem& it = items[w.x];
+    plan_zero_vec(it.ps, it.fv, it.nrm, it.wts, it.nsrc, it.zero, w.y);
+}
+
+// work items (plan, block of 256 targets)
+__global__ void k_plan_combine_multi(const PItem* __restrict__ items, const int2* __restrict__ wl) {
+    const int2 w = wl[blockIdx.x];
+    const PItem& it = items[w.x];
+    const int64_t i = (int64_t)w.y * blockDim.x + threadIdx.x;
+    if (i < it.ntar) plan_combine_one(it.ur, it.uk, it.nv, it.ntar, it.zero, it.inv_area, it.u1s, it.u2s, i);
 }
 
 __global__ void k_plan_wrap(const double* __restrict__ x, const double* __restrict__ y, int64_t n, double Lx,
@@ -170,7 +236,45 @@ struct fte_batch {
     cudaGraphExec_t exec = nullptr;
     std::vector<cudaStream_t> streams;
     std::vector<cudaEvent_t> events;
+    // work lists: every plan's densities (dens); the k-space parts of the
+    // plans whose float-float k-space the work lists take (km, multi[i] = 1),
+    // their stresslet zero modes (zero) and combinations (comb); the other
+    // plans run their k-space per call on the forked streams
+    KMulti* km = nullptr;
+    std::vector<char> multi;
+    char* mem2 = nullptr;
+    PItem* pitems = nullptr;
+    int2 *wl_dens = nullptr, *wl_zero = nullptr, *wl_comb = nullptr;
+    int n_dens = 0, n_zero = 0, n_comb = 0;
 };
+
+// the k-space arguments of plan p's vector v in a batch
+static KspaceArgs batch_kspace_args(const fte_plan* p, int v) {
+    KspaceArgs a;
+    a.kind = p->kind;
+    a.form = p->prm.form;
+    a.nsrc = p->nsrc;
+    a.ntar = p->ntar;
+    a.psrc = p->ps;
+    a.ptar = p->pt;
+    a.f = p->fv + 2 * v * p->nsrc;
+    a.nrm = p->nrm;
+    a.wts = p->wts;
+    a.xi = p->prm.xi;
+    a.eta = p->prm.eta;
+    a.w = p->prm.w;
+    a.Lx = p->Lx;
+    a.Ly = p->Ly;
+    a.Mx = p->prm.Mx;
+    a.My = p->prm.My;
+    a.P = p->prm.P;
+    a.uk = p->uk + v * p->ntar;
+    a.pre_src = &p->tb_src;
+    a.pre_tar = &p->tb_tar;
+    a.ts_spread = p->prm.ts_spread;
+    a.ts_gather = p->prm.ts_gather;
+    return a;
+}
 
 // density-dependent work of one plan (device pointers; nv vectors)
 static int plan_exec_body(fte_plan* p, int nv, const double* f1s, const double* f2s, double* u1s, double* u2s,
@@ -495,59 +599,32 @@ extern "C" int fte_plan_destroy(fte_plan* p) {
 static int batch_run(fte_batch* b) {
     fte_context* c = b->ctx;
     cudaStream_t main = c->stream;
-    // densities into cell order, for every plan
-    for (size_t i = 0; i < b->plans.size(); i++) {
-        fte_plan* p = b->plans[i];
-        if (p->nsrc == 0) continue;
-        if (p->kind == FTE_KIND_SLP)
-            FTE_LAUNCH(c, k_plan_dens<FTE_KIND_SLP>, grid_of(c, p->nsrc), 256, 0, (const double*)b->f1[i],
-                       (const double*)b->f2[i], b->nv, p->nsrc, (const double*)p->nrm, (const double*)p->wts,
-                       (const int*)p->cl.sidx, p->q0, p->q1, p->q2, p->fv);
-        else
-            FTE_LAUNCH(c, k_plan_dens<FTE_KIND_DLP>, grid_of(c, p->nsrc), 256, 0, (const double*)b->f1[i],
-                       (const double*)b->f2[i], b->nv, p->nsrc, (const double*)p->nrm, (const double*)p->wts,
-                       (const int*)p->cl.sidx, p->q0, p->q1, p->q2, p->fv);
-        if (p->ffnear && p->ntar > 0) FTE_TRY(fte_near_ff_prep(c, p->kind, b->nv, p->near));
-    }
+    // densities into cell order, every plan in one launch; the float-float
+    // near data per kind
+    if (b->n_dens > 0)
+        FTE_LAUNCH(c, k_plan_dens_multi, b->n_dens, 256, 0, (const PItem*)b->pitems, (const int2*)b->wl_dens);
+    for (int kind = 0; kind < 2; kind++)
+        FTE_TRY(fte_near_ff_prep_batch(c, kind, b->nv, b->plist[kind * 2 + 1], b->items[kind * 2 + 1],
+                                       b->nitems[kind * 2 + 1]));
     // one persistent near-field launch per kind over all (plan, box) items
     for (int l = 0; l < 4; l++)
         if (b->nitems[l] > 0)
             FTE_TRY(fte_near_launch_batch(c, l / 2, b->nv, l % 2 == 1, b->plist[l], b->items[l], b->nitems[l]));
-    // k-space and combination of every plan on forked streams
-    const int S = (int)b->streams.size();
-    FTE_CUDA_TRY(cudaEventRecord(b->events[0], main));
-    for (int s = 0; s < S; s++) FTE_CUDA_TRY(cudaStreamWaitEvent(b->streams[s], b->events[0], 0));
+    // the k-space parts the work lists do not take: per plan on forked streams
+    bool percall = false;
+    for (size_t i = 0; i < b->plans.size(); i++) percall = percall || (!b->multi[i] && b->plans[i]->ntar > 0);
     int rc = FTE_OK;
-    for (size_t i = 0; i < b->plans.size() && rc == FTE_OK; i++) {
-        fte_plan* p = b->plans[i];
-        c->stream = b->streams[i % S];
-        // densities are already sorted; run the k-space part and the combination
-        if (p->ntar > 0) {
+    if (percall) {
+        const int S = (int)b->streams.size();
+        FTE_CUDA_TRY(cudaEventRecord(b->events[0], main));
+        for (int s = 0; s < S; s++) FTE_CUDA_TRY(cudaStreamWaitEvent(b->streams[s], b->events[0], 0));
+        for (size_t i = 0; i < b->plans.size() && rc == FTE_OK; i++) {
+            fte_plan* p = b->plans[i];
+            if (b->multi[i] || p->ntar == 0) continue;
+            c->stream = b->streams[i % S];
             for (int v = 0; v < b->nv && rc == FTE_OK; v++) {
                 WsCarver wc{p->kscratch, 0, p->kscratch_size};
-                KspaceArgs a;
-                a.kind = p->kind;
-                a.form = p->prm.form;
-                a.nsrc = p->nsrc;
-                a.ntar = p->ntar;
-                a.psrc = p->ps;
-                a.ptar = p->pt;
-                a.f = p->fv + 2 * v * p->nsrc;
-                a.nrm = p->nrm;
-                a.wts = p->wts;
-                a.xi = p->prm.xi;
-                a.eta = p->prm.eta;
-                a.w = p->prm.w;
-                a.Lx = p->Lx;
-                a.Ly = p->Ly;
-                a.Mx = p->prm.Mx;
-                a.My = p->prm.My;
-                a.P = p->prm.P;
-                a.uk = p->uk + v * p->ntar;
-                a.pre_src = &p->tb_src;
-                a.pre_tar = &p->tb_tar;
-                a.ts_spread = p->prm.ts_spread;
-                a.ts_gather = p->prm.ts_gather;
+                const KspaceArgs a = batch_kspace_args(p, v);
                 rc = fte_kspace_run(c, wc, a, nullptr);
             }
             if (rc == FTE_OK && p->kind == FTE_KIND_DLP && p->nsrc > 0) {
@@ -566,13 +643,122 @@ static int batch_run(fte_batch* b) {
                 }
             }
         }
+        c->stream = main;
+        for (int s = 0; s < S; s++) {
+            FTE_CUDA_TRY(cudaEventRecord(b->events[1 + s], b->streams[s]));
+            FTE_CUDA_TRY(cudaStreamWaitEvent(main, b->events[1 + s], 0));
+        }
+        FTE_TRY(rc);
     }
-    c->stream = main;
-    for (int s = 0; s < S; s++) {
-        FTE_CUDA_TRY(cudaEventRecord(b->events[1 + s], b->streams[s]));
-        FTE_CUDA_TRY(cudaStreamWaitEvent(main, b->events[1 + s], 0));
+    // the work lists' k-space parts, zero modes and combinations
+    FTE_TRY(fte_kmulti_run(b->km, c));
+    if (b->n_zero > 0)
+        FTE_LAUNCH(c, k_plan_zero_multi, b->n_zero, 256, 0, (const PItem*)b->pitems, (const int2*)b->wl_zero);
+    if (b->n_comb > 0)
+        FTE_LAUNCH(c, k_plan_combine_multi, b->n_comb, 256, 0, (const PItem*)b->pitems, (const int2*)b->wl_comb);
+    return FTE_OK;
+}
+
+// Work lists of a batch: the k-space items of every plan whose float-float
+// k-space they take (vector 0 in the plan's own scratch, the others in the
+// batch's), and the per-plan items of the densities, zero modes and
+// combinations.
+static int batch_build_lists(fte_batch* b) {
+    fte_context* c = b->ctx;
+    const int nv = b->nv;
+    const size_t np = b->plans.size();
+    b->multi.assign(np, 0);
+    FTE_TRY(fte_kmulti_create(&b->km));
+    // scratch of vectors 1..nv-1 of the float-float plans
+    size_t need = ws_bytes(np * sizeof(PItem), 1) + 4096;
+    for (size_t i = 0; i < np; i++) {
+        const fte_plan* p = b->plans[i];
+        if (p->prm.form == FTE_FORM_FF && p->ntar > 0) need += (size_t)(nv - 1) * ws_bytes(p->kscratch_size, 1);
     }
-    return rc;
+    std::vector<int2> dens, zero, comb;
+    for (size_t i = 0; i < np; i++) {
+        const fte_plan* p = b->plans[i];
+        if (p->nsrc > 0)
+            for (int j = 0; j < (int)((p->nsrc + 255) / 256); j++) dens.push_back(make_int2((int)i, j));
+    }
+    need += 3 * ws_bytes((dens.size() + np * (nv + 1) + 1) * sizeof(int2), 1);
+    for (size_t i = 0; i < np; i++) need += ws_bytes((size_t)(b->plans[i]->ntar + 255) / 256 * sizeof(int2), 1);
+    if (fte_alloc_should_fail() || cudaMalloc(&b->mem2, need) != cudaSuccess) {
+        cudaGetLastError();
+        b->mem2 = nullptr;
+        fte_set_error("fte_batch_create: %zu bytes of device memory not available", need);
+        return FTE_ERR_ALLOC;
+    }
+    WsCarver m{b->mem2, 0, need};
+    b->pitems = m.take<PItem>(np);
+    std::vector<PItem> hp(np);
+    for (size_t i = 0; i < np; i++) {
+        fte_plan* p = b->plans[i];
+        PItem& it = hp[i];
+        std::memset(&it, 0, sizeof(it));
+        it.kind = p->kind;
+        it.nv = nv;
+        it.nsrc = p->nsrc;
+        it.ntar = p->ntar;
+        it.f1s = b->f1[i];
+        it.f2s = b->f2[i];
+        it.nrm = p->nrm;
+        it.wts = p->wts;
+        it.ps = p->ps;
+        it.sidx = p->cl.sidx;
+        it.q0 = p->q0;
+        it.q1 = p->q1;
+        it.q2 = p->q2;
+        it.fv = p->fv;
+        // the stresslet's zero mode (none without sources)
+        it.zero = p->kind == FTE_KIND_DLP && p->nsrc > 0 ? p->zero : nullptr;
+        it.ur = p->ur;
+        it.uk = p->uk;
+        it.u1s = b->u1[i];
+        it.u2s = b->u2[i];
+        it.inv_area = 1.0 / (p->Lx * p->Ly);
+        if (p->ntar == 0) continue;
+        // the k-space items: all vectors of a plan or none
+        for (int v = 0; v < nv; v++) {
+            char* scr = v == 0 ? p->kscratch : m.take<char>(p->kscratch_size);
+            FTE_WS_CHECK(m);
+            WsCarver wc{scr, 0, p->kscratch_size};
+            bool taken = false;
+            FTE_TRY(fte_kmulti_add(b->km, c, wc, batch_kspace_args(p, v), &taken));
+            if (!taken) {
+                if (v > 0) {
+                    fte_set_error("internal: batch work list took vector 0 of plan %zu but not vector %d", i, v);
+                    return FTE_ERR_INVALID;
+                }
+                break;
+            }
+            b->multi[i] = 1;
+        }
+        if (!b->multi[i]) continue;
+        if (p->kind == FTE_KIND_DLP && p->nsrc > 0)
+            for (int v = 0; v < nv; v++) zero.push_back(make_int2((int)i, v));
+        for (int j = 0; j < (int)((p->ntar + 255) / 256); j++) comb.push_back(make_int2((int)i, j));
+    }
+    FTE_TRY(fte_kmulti_finalize(b->km, c));
+    b->n_dens = (int)dens.size();
+    b->n_zero = (int)zero.size();
+    b->n_comb = (int)comb.size();
+    b->wl_dens = m.take<int2>(dens.size() + 1);
+    b->wl_zero = m.take<int2>(zero.size() + 1);
+    b->wl_comb = m.take<int2>(comb.size() + 1);
+    FTE_WS_CHECK(m);
+    FTE_CUDA_TRY(cudaMemcpyAsync(b->pitems, hp.data(), np * sizeof(PItem), cudaMemcpyHostToDevice, c->stream));
+    if (!dens.empty())
+        FTE_CUDA_TRY(cudaMemcpyAsync(b->wl_dens, dens.data(), dens.size() * sizeof(int2), cudaMemcpyHostToDevice,
+                                     c->stream));
+    if (!zero.empty())
+        FTE_CUDA_TRY(cudaMemcpyAsync(b->wl_zero, zero.data(), zero.size() * sizeof(int2), cudaMemcpyHostToDevice,
+                                     c->stream));
+    if (!comb.empty())
+        FTE_CUDA_TRY(cudaMemcpyAsync(b->wl_comb, comb.data(), comb.size() * sizeof(int2), cudaMemcpyHostToDevice,
+                                     c->stream));
+    FTE_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return FTE_OK;
 }
 
 extern "C" int fte_batch_create(fte_context* c, fte_plan* const* plans, int nplans, int nv, fte_batch** out) {
@@ -654,6 +840,13 @@ extern "C" int fte_batch_create(fte_context* c, fte_plan* const* plans, int npla
                                      cudaMemcpyHostToDevice, c->stream));
     }
     FTE_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    {
+        const int st = batch_build_lists(b);
+        if (st != FTE_OK) {
+            fte_batch_destroy(b);
+            return st;
+        }
+    }
     const int S = nplans < 8 ? (nplans > 0 ? nplans : 1) : 8;
     b->streams.resize(S);
     b->events.resize(S + 1);
@@ -735,6 +928,8 @@ extern "C" int fte_batch_destroy(fte_batch* b) {
     for (auto s : b->streams) cudaStreamDestroy(s);
     for (auto e : b->events) cudaEventDestroy(e);
     cudaFree(b->mem);
+    if (b->mem2) cudaFree(b->mem2);
+    fte_kmulti_destroy(b->km);
     delete b;
     return FTE_OK;
 }

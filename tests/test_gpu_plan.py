@@ -213,3 +213,43 @@ def test_tuned_tiles_give_same_result(gpu_ctx, form, tol):
         t1, t2 = tuned.execute(f1s, f2s)
         bar = 1e-12 if pb.form == ft.FORM_PLAIN else tol
         assert rel_max(np.stack([t1, t2]), np.stack([b1, b2])) <= bar, (kind, pt.ts_spread, pt.ts_gather)
+
+
+def test_batch_work_lists_match_plans_in_few_launches(gpu_ctx):
+    """A batch of mixed-form plans (float-float k-space: every stage one
+    launch over all (plan, vector) items, the densities, zero modes and
+    combinations one launch over all plans) gives, plan by plan and vector by
+    vector, what the plans give one by one, in at most 100 kernel launches
+    per step however many plans it holds; a plain (FP64) plan in the same
+    batch takes the per-call path beside them."""
+    ft = _ft()
+    nv = 4
+    rng = np.random.default_rng(77)
+    plans, dens = [], []
+    for i in range(24):
+        n = int(np.exp(rng.uniform(np.log(1500), np.log(40000))))
+        Lx, Ly = [(1.0, 1.0), (2.0, 1.0), (1.0, 0.75), (1.0, np.sqrt(2.0))][i % 4]
+        g = _geom(900 + i, n, Lx, Ly)
+        f1s, f2s = _dens(950 + i, nv, n)
+        form, tol = (ft.FORM_PLAIN, 1e-10) if i == 5 else (ft.FORM_MIXED, 1e-8)
+        plans.append(ft.Plan(i % 2, *g[:4], f1s[0], f2s[0], Lx, Ly, n1=g[4], n2=g[5], tol=tol, form=form,
+                             nvmax=nv, ctx=gpu_ctx))
+        dens.append((f1s, f2s))
+    assert sum(p.params.form == ft.FORM_FF for p in plans) >= 20
+    batch = ft.Batch(plans, nv, ctx=gpu_ctx)
+    for i, (f1s, f2s) in enumerate(dens):
+        batch.set_density(i, f1s, f2s)
+    k0 = gpu_ctx.kernel_count
+    batch.launch(False)
+    launches = gpu_ctx.kernel_count - k0
+    # the plain plan alone launches ~10 kernels per vector on the per-call path
+    assert launches <= 100, launches
+    for use_graph in (True, False):
+        batch.launch(use_graph)
+        for i, p in enumerate(plans):
+            b1, b2 = batch.velocity(i)
+            e1, e2 = p.execute(*dens[i])
+            assert rel_max(np.stack([b1, b2]), np.stack([e1, e2])) <= 1e-12, (use_graph, i, p.params.form)
+    batch.close()
+    for p in plans:
+        p.close()
