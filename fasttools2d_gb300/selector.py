@@ -215,32 +215,35 @@ def _rational(T):
 
 
 def params_from(y, T):
-    """Valid driver options from network outputs y relative to T."""
-    P = int(np.clip(T.P + 2 * round(float(y[3])), 4, 24))
-    xi = float(T.xi * np.exp(y[1]))
+    """Driver options from network outputs y relative to the tuned choice T.
+    The cell-list scale and the window-support change are snapped to the
+    candidate set the labels come from; xi and the grid then follow from the
+    error estimates at that cutoff and support (the mixed form's chooser with
+    these overrides), exactly as for the labelled candidates, so that the four
+    parameters stay consistent.  (The network's xi and grid outputs, trained
+    on the labels' values, are not needed for that.)"""
+    sa = float(SCALES[int(np.argmin(np.abs(np.log(SCALES) - float(y[0]))))])
+    dp = int(DPS[int(np.argmin(np.abs(DPS - 2.0 * float(y[3]))))])
+    P = int(np.clip(T.P + dp, 4, 24))
     if _rational(T):
         A, B = int(T.A), int(T.B)
-        a = max(1, int(round(T.nside_x / A * np.exp(y[0]))))
-        t = max(2, int(round(T.Mx / A * np.exp(y[2]))))
-        while (A * t) % 2 or (B * t) % 2:
-            t += 1
-        while P + 1 > min(A * t, B * t):
-            t += 2
-        return dict(P=P, nside_x=A * a, nside_y=B * a, xi=xi, Mx=A * t, My=B * t)
+        a = max(1, int(round(T.nside_x / A * sa)))
+        return dict(P=P, nside_x=A * a, nside_y=B * a)
     # a box with its own step per axis: each count scaled on its own
-    s = np.exp(y[0])
-    nx, ny = max(1, int(round(T.nside_x * s))), max(1, int(round(T.nside_y * s)))
-    g = np.exp(y[2])
-    mx, my = max(2, int(round(T.Mx * g / 2)) * 2), max(2, int(round(T.My * g / 2)) * 2)
-    while P + 1 > min(mx, my):
-        mx, my = mx + 2, my + 2
-    return dict(P=P, nside_x=nx, nside_y=ny, xi=xi, Mx=mx, My=my)
+    return dict(P=P, nside_x=max(1, int(round(T.nside_x * sa))), nside_y=max(1, int(round(T.nside_y * sa))))
 
 
 # candidates around the tuned choice, the same for every configuration so that
 # labels are comparable: cell-list scale (xi and the grid follow from the
 # estimates) x window support change
 CANDIDATES = [(sa, dp) for sa in (0.7, 1.0, 1.4, 2.0) for dp in (-4, -2, 0, 2)]
+SCALES = np.array(sorted({sa for sa, _ in CANDIDATES}))
+DPS = np.array(sorted({dp for _, dp in CANDIDATES}))
+# a candidate other than the tuned choice becomes the label only where it
+# saves at least this fraction of the tuned choice's time: among near-equal
+# candidates the timing noise would otherwise pick the label, and the
+# network would learn to leave the tuned choice for nothing
+LABEL_GAIN = 0.05
 # a label must meet the tolerance with this margin
 LABEL_MARGIN = 0.5
 # the sampled check sees 64 targets, whose largest error is below the largest
@@ -435,12 +438,15 @@ def tuned_of(rec, **kw):
 
 def label_targets(rec):
     """(targets, t_best, t_T) of a record: the fastest candidate meeting the
-    tolerance, relative to the current tuned choice; None if none met it."""
+    tolerance (row 0, the tuned choice, unless another saves LABEL_GAIN of
+    its time), relative to the current tuned choice; None if none met it."""
     c = rec["cands"]
     ok = c[:, 8] <= LABEL_MARGIN * rec["tol"]
     if not ok.any():
         return None
     j = int(np.argmin(np.where(ok, c[:, 7], np.inf)))
+    if ok[0] and c[j, 7] > (1.0 - LABEL_GAIN) * c[0, 7]:
+        j = 0
     T = tuned_of(rec)
     y = np.array([np.log(c[j, 1] / T.nside_x), np.log(c[j, 5] / T.xi), np.log(c[j, 3] / T.Mx), (c[j, 0] - T.P) / 2])
     return y, float(c[j, 7]), float(c[0, 7])
@@ -455,13 +461,15 @@ def save_records(path, recs):
 
 
 def load_records(path):
-    z = np.load(path)
+    # read each array once (indexing the archive reads the whole member again)
+    with np.load(path) as zf:
+        z = {k: zf[k] for k in zf.files}
     recs, o = [], 0
     for i in range(len(z["kind"])):
         k = int(z["ncand"][i])
         recs.append({"feats": z["feats"][i], "kind": int(z["kind"][i]), "tol": float(z["tol"][i]), "n": int(z["n"][i]),
                      "ntar": int(z["ntar"][i]), "Lx": float(z["Lx"][i]), "Ly": float(z["Ly"][i]),
-                     "qsum": float(z["qsum"][i]), "cands": z["cands"][o:o + k]})
+                     "qsum": float(z["qsum"][i]), "cands": z["cands"][o:o + k].copy()})
         o += k
     return recs
 

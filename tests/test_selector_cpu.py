@@ -74,6 +74,10 @@ def test_features_on_known_layouts():
 
 
 def test_targets_and_params_round_trip():
+    """Network outputs map to the candidate set of the labels: zero
+    corrections give the tuned cells and support back; others snap to the
+    nearest candidate cell scale and support change (xi and the grid follow
+    from the chooser)."""
     ft = pytest.importorskip("fasttools2d_gb300")
     from fasttools2d_gb300 import selector
 
@@ -82,22 +86,19 @@ def test_targets_and_params_round_trip():
     f1, f2 = rng.standard_normal(n), rng.standard_normal(n)
     for Lx, Ly in ((1.0, 1.0), (2.75, 1.0), (1.0, 3.25)):
         T = ft.choose_params(0, f1, f2, n, Lx, Ly, tol=1e-8, form=ft.FORM_MIXED)
-        opts = selector.params_from(np.zeros(4), T)
-        assert (opts["P"], opts["nside_x"], opts["nside_y"], opts["Mx"], opts["My"]) == \
-            (T.P, T.nside_x, T.nside_y, T.Mx, T.My)
-        assert opts["xi"] == pytest.approx(T.xi)
-        y = np.array([0.2, -0.1, 0.15, 1.0])
-        o = selector.params_from(y, T)
         assert selector._rational(T)
-        assert o["nside_x"] % T.A == 0 and o["nside_y"] % T.B == 0
-        assert o["Mx"] * T.B == o["My"] * T.A and o["Mx"] % 2 == 0 and o["My"] % 2 == 0
-        assert o["P"] == min(T.P + 2, 24)
-        assert np.log(o["xi"] / T.xi) == pytest.approx(-0.1)
+        opts = selector.params_from(np.zeros(4), T)
+        assert opts == dict(P=T.P, nside_x=T.nside_x, nside_y=T.nside_y)
+        o = selector.params_from(np.array([0.3, -0.1, 0.15, 0.8]), T)  # scale 1.4, P + 2
+        a = max(1, round(T.nside_x / T.A * 1.4))
+        assert o == dict(P=min(T.P + 2, 24), nside_x=T.A * a, nside_y=T.B * a)
+        o = selector.params_from(np.array([-0.9, 0.0, 0.0, -3.0]), T)  # scale 0.7, P - 4
+        assert o["P"] == max(T.P - 4, 4) and o["nside_x"] == T.A * max(1, round(T.nside_x / T.A * 0.7))
 
 
 def test_params_round_trip_on_irrational_box():
     """Boxes with a step per axis: zero corrections give the tuned choice
-    back, and corrections scale each axis on its own (even grid sizes)."""
+    back, and a cell scale applies to each axis's count on its own."""
     ft = pytest.importorskip("fasttools2d_gb300")
     from fasttools2d_gb300 import selector
 
@@ -106,11 +107,9 @@ def test_params_round_trip_on_irrational_box():
     f1, f2 = rng.standard_normal(n), rng.standard_normal(n)
     T = ft.choose_params(1, f1, f2, n, 1.0, np.sqrt(2.0), tol=1e-8, form=ft.FORM_MIXED)
     assert not selector._rational(T)
-    o = selector.params_from(np.zeros(4), T)
-    assert (o["P"], o["nside_x"], o["nside_y"], o["Mx"], o["My"]) == (T.P, T.nside_x, T.nside_y, T.Mx, T.My)
+    assert selector.params_from(np.zeros(4), T) == dict(P=T.P, nside_x=T.nside_x, nside_y=T.nside_y)
     o = selector.params_from(np.array([0.3, 0.0, 0.2, -1.0]), T)
-    assert o["Mx"] % 2 == 0 and o["My"] % 2 == 0 and o["P"] == T.P - 2
-    assert o["nside_x"] == round(T.nside_x * np.exp(0.3)) and o["nside_y"] == round(T.nside_y * np.exp(0.3))
+    assert o == dict(P=T.P - 2, nside_x=round(T.nside_x * 1.4), nside_y=round(T.nside_y * 1.4))
 
 
 def test_committed_model_layout():
@@ -150,6 +149,11 @@ def test_records_round_trip_and_labels(tmp_path):
     y, tb, tT = selector.label_targets(rec)
     assert tb == 3.0 and tT == 5.0
     assert np.allclose(y, [np.log(2.0), np.log(1.5), np.log(2.0), -1.0])
+    # a candidate saving less than LABEL_GAIN leaves the label at the tuned choice
+    rec3 = dict(rec, cands=rec["cands"].copy())
+    rec3["cands"][2, 7] = 4.9
+    y3, tb3, _ = selector.label_targets(rec3)
+    assert tb3 == 5.0 and np.allclose(y3, [0.0, 0.0, 0.0, 0.0])
     rec2 = dict(rec, cands=rec["cands"][:2])
     rec2["cands"][0, 8] = 1e-7
     assert selector.label_targets(rec2) is None
