@@ -238,7 +238,8 @@ def batched_section(ft, wl, ctx, stream, steps, warmup, flush):
 
     ours:     one plan per (configuration, kernel) with the tuned parameter
               choice and autotuned spread/gather tiles, all bound into one
-              batch; a step is one replay of its CUDA graph.
+              batch (every stage one launch over all plans, with the work
+              lists' own tile sizes); a step is one replay of its CUDA graph.
     baseline: the untuned plain per-instance loop -- one FP64 driver call per
               (configuration, kernel, vector) with the analytic parameters.
     ablations, to separate what each part adds:
@@ -247,7 +248,8 @@ def batched_section(ft, wl, ctx, stream, steps, warmup, flush):
                      arithmetic and parameters; no plans, batch or graph)
       plans_loop     the batch's plans executed one after another (geometry
                      reused, all vectors per call; no batch or graph)
-      batch_untuned  the same batch with the default tile sizes (no autotuner)
+      plans_loop_untuned  the same, plans with the default tile sizes (what
+                     the autotuner adds to plans executed alone)
     All with inputs resident on the GPU; L2 flushed before every step."""
     import numpy as np
     import torch
@@ -370,21 +372,23 @@ def batched_section(ft, wl, ctx, stream, steps, warmup, flush):
     plans_loop()
     plans_loop_ms = device_ms(plans_loop, 2)
 
-    # ablation 3: the same batch with the default tiles (no autotuner)
+    # ablation 3: the plans one after another with the default tiles (what
+    # the autotuner adds to plans executed alone; a batch's work lists use
+    # their own tile sizes either way)
     plans_u = []
     for d in dev:
         for kind in kinds:
             plans_u.append(ft.Plan(kind, d["xsrc"], d["ysrc"], d["xsrc"], d["ysrc"], d["f1"][0], d["f2"][0], d["Lx"],
                                    d["Ly"], n1=d["n1"], n2=d["n2"], tol=tol, form=ft.FORM_MIXED, nvmax=nv, tune=False,
                                    ctx=ctx))
-    batch_u = ft.Batch(plans_u, nv, ctx=ctx)
-    for i in range(len(plans_u)):
-        d = dev[i // len(kinds)]
-        batch_u.set_density(i, d["f1"], d["f2"])
-    for _ in range(warmup):
-        batch_u.launch(True)
-    untuned_ms = device_ms(lambda: batch_u.launch(True), bsteps)
-    batch_u.close()
+
+    def plans_loop_untuned():
+        for i, p in enumerate(plans_u):
+            d = dev[i // len(kinds)]
+            p.execute(d["f1"], d["f2"])
+
+    plans_loop_untuned()
+    untuned_ms = device_ms(plans_loop_untuned, 2)
     for p in plans_u:
         p.close()
 
@@ -443,7 +447,7 @@ def batched_section(ft, wl, ctx, stream, steps, warmup, flush):
                        "calls_per_step": len(cfgs) * len(kinds) * nv},
         "speedup_vs_plain_loop": loop_ms / graph_ms,
         "ablation_ms_per_step": {"mixed_loop": mixed_loop_ms, "plans_loop": plans_loop_ms,
-                                 "batch_untuned": untuned_ms, "batch_tuned_graph": graph_ms},
+                                 "plans_loop_untuned": untuned_ms, "batch_tuned_graph": graph_ms},
         "setup_s": setup_s, "gpu_launches_per_step": launches,
         "max_rel_diff_vs_plain_loop": worst,
         "distinct_tile_pairs": len(tiles),

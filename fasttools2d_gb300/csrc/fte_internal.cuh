@@ -414,6 +414,11 @@ struct KspaceArgs {
 // prebuilt) becomes an item of one launch per stage; *taken = false when its
 // form or shape needs the per-call path (FP64/FP32 k-space, long
 // transforms, untiled spread/gather, the FP64 multiplier).
+// Tile sizes of an evaluation inside a batch's work lists: the default rule
+// without the small-grid shrink and without a plan's tuned sizes (many plans
+// share each launch, so the GPU is filled by the batch; tiles timed on one
+// plan alone, or shrunk to fill the GPU with one grid, only add halo work).
+int fte_kspace_batch_tiles(const fte_context* ctx, const KspaceArgs& a, int* ts_s, int* ts_g);
 struct KMulti;
 int fte_kmulti_create(KMulti** out);
 int fte_kmulti_add(KMulti* km, fte_context* ctx, WsCarver& wc, const KspaceArgs& a, bool* taken);

@@ -326,7 +326,6 @@ __global__ void __launch_bounds__(kColThreads) k_spread_cols(int mode, const dou
                                                             double* __restrict__ H1) {
     extern __shared__ double sh[];
     const int P1 = wp.P + 1, W = tile_region(ts, wp.P), WW = W * W;
-    const int P1e = (P1 + 1) & ~1;
     double* buf = sh;                     // 2 * WW
     double* e1 = buf + 2 * WW;            // e1_len (P1e, or 2 P1e with aniso)
     double* fw = e1 + e1_len(wp.P, wp.aniso);  // kColChunk * 2 * P1
@@ -1475,7 +1474,6 @@ __device__ __forceinline__ void spread_ff_run(const FfWin* __restrict__ recs, co
                                               double* __restrict__ H1, double* __restrict__ H2, int tile0, int tstep,
                                               unsigned char* shraw) {
     const int P1 = wp.P + 1, W = tile_region(ts, wp.P), WW = W * W;
-    const int P1e = (P1 + 1) & ~1;
     float4* buf = reinterpret_cast<float4*>(shraw);  // WW: (grid 0 sum, low, grid 1 sum, low)
     float4* fw = buf + WW;                            // kColChunk * P1: q0 wx, q1 wx (float-float each)
     float2* e1 = reinterpret_cast<float2*>(fw + kColChunk * P1);  // e1_len (P1e, 2 P1e with aniso)
@@ -1790,7 +1788,7 @@ bool gather_fits(const fte_context* ctx, int form, int ts, int P, int aniso = 0)
                 : (form == FTE_FORM_FF ? gather_ff_smem(ts, P, aniso) : gather64_smem(ts, P, aniso));
     return sm <= tile_budget(ctx);
 }
-int resolve_tiles(const fte_context* ctx, const KspaceArgs& a, int* ts_s, int* ts_g) {
+int resolve_tiles(const fte_context* ctx, const KspaceArgs& a, int* ts_s, int* ts_g, bool fill = true) {
     *ts_s = 0;
     *ts_g = 0;
     const int an = kspace_aniso(a);
@@ -1830,6 +1828,18 @@ int resolve_tiles(const fte_context* ctx, const KspaceArgs& a, int* ts_s, int* t
         for (int ts = 64; ts >= 8 && !*ts_g; ts -= 4)
             if (gather_fits(ctx, a.form, ts, a.P, an)) *ts_g = ts;
     }
+    // Small grids: a tile is one CTA, so that a grid of a few tiles leaves
+    // most SMs idle while each CTA walks its tile's points alone (48 x 108
+    // nodes at tile 64: two CTAs).  Default sizes shrink (by 4, not below 8)
+    // until the grid has two tiles per SM; the halo a smaller tile adds is
+    // small in absolute terms on such grids.
+    if (!fill) return FTE_OK;
+    auto tiles = [&](int ts) { return (int64_t)((a.Mx + ts - 1) / ts) * ((a.My + ts - 1) / ts); };
+    const int64_t want = 2 * (int64_t)(ctx->num_sms > 0 ? ctx->num_sms : 1);
+    if (a.ts_spread <= 0)
+        while (*ts_s > 8 && tiles(*ts_s) < want) *ts_s -= 4;
+    if (a.ts_gather <= 0)
+        while (*ts_g > 8 && tiles(*ts_g) < want) *ts_g -= 4;
     return FTE_OK;
 }
 
@@ -2025,6 +2035,12 @@ int kspace_run_mixed(fte_context* ctx, WsCarver& wc, const KspaceArgs& a) {
     return FTE_OK;
 }
 }  // namespace
+
+int fte_kspace_batch_tiles(const fte_context* ctx, const KspaceArgs& a, int* ts_s, int* ts_g) {
+    KspaceArgs d = a;
+    d.ts_spread = d.ts_gather = 0;
+    return resolve_tiles(ctx, d, ts_s, ts_g, false);
+}
 
 int fte_kspace_tiles(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, TileBins* src, TileBins* tar) {
     int ts_s = 0, ts_g = 0;
@@ -2367,6 +2383,16 @@ struct KItem {
 constexpr int kZeroPerThread = 8;
 constexpr int kFftClasses = 4;
 int fft_class(int m) { return m <= 256 ? 0 : (m <= 1024 ? 1 : (m <= 4096 ? 2 : 3)); }
+// Spread and gather items are grouped by the CTAs per SM their shared memory
+// allows (1..kOccClasses): a launch reserves its largest item's shared memory
+// for every block, so that plans with larger tiles (autotuned sizes differ per
+// plan) would otherwise lower every other plan's occupancy.
+constexpr int kOccClasses = 8;
+int occ_class(size_t smem) {
+    const size_t per_sm = 228 * 1024, reserved = 1024;  // per SM; per CTA
+    const size_t c = per_sm / (smem + reserved);
+    return (int)(c < 1 ? 0 : (c > kOccClasses ? kOccClasses - 1 : c - 1));
+}
 
 __global__ void k_zero_multi(const KItem* __restrict__ items, const int2* __restrict__ wl) {
     const int2 w = wl[blockIdx.x];
@@ -2474,19 +2500,22 @@ struct KMulti {
     std::vector<KItem> items;
     KItem* ditems = nullptr;
     char* mem = nullptr;
-    List zero, win, spread[2], yr2c[kFftClasses], xf[kFftClasses], filt[2], xi[kFftClasses], yc2r[kFftClasses],
-        gather[3];
+    // spread[grids 2/3][occupancy class], gather[support class][occupancy class]
+    List zero, win, spread[2][kOccClasses], yr2c[kFftClasses], xf[kFftClasses], filt[2], xi[kFftClasses],
+        yc2r[kFftClasses], gather[3][kOccClasses];
     template <typename F>
     void each(F fn) {
         fn(zero);
         fn(win);
-        for (auto& l : spread) fn(l);
+        for (auto& g : spread)
+            for (auto& l : g) fn(l);
         for (auto& l : yr2c) fn(l);
         for (auto& l : xf) fn(l);
         for (auto& l : filt) fn(l);
         for (auto& l : xi) fn(l);
         for (auto& l : yc2r) fn(l);
-        for (auto& l : gather) fn(l);
+        for (auto& g : gather)
+            for (auto& l : g) fn(l);
     }
 };
 
@@ -2566,9 +2595,10 @@ int fte_kmulti_add(KMulti* km, fte_context* ctx, WsCarver& wc, const KspaceArgs&
     km->zero.add(i, (int)(((size_t)it.ngs * G + 256 * kZeroPerThread - 1) / (256 * kZeroPerThread)));
     if (a.nsrc > 0) {
         km->win.add(i, (int)((a.nsrc + 255) / 256));
-        KMulti::List& sp = km->spread[it.ngs == 2 ? 0 : 1];
+        const size_t sm = spread_ff_smem(it.ts_s, a.P, it.ngs, an);
+        KMulti::List& sp = km->spread[it.ngs == 2 ? 0 : 1][occ_class(sm)];
         sp.add(i, it.ntx_s * it.nty_s);
-        sp.smem = std::max(sp.smem, spread_ff_smem(it.ts_s, a.P, it.ngs, an));
+        sp.smem = std::max(sp.smem, sm);
     }
     const int cy = fft_class(it.py.m), cx = fft_class(it.px.m);
     const size_t smy = 2 * (size_t)it.py.m * sizeof(float4), smx = 2 * (size_t)it.px.m * sizeof(float4);
@@ -2586,9 +2616,10 @@ int fte_kmulti_add(KMulti* km, fte_context* ctx, WsCarver& wc, const KspaceArgs&
     km->yc2r[cy].add(i, (Mx / 2) * 2);
     shape(km->yc2r[cy], smy, fft_threads(it.py.m));
     if (a.ntar > 0) {
-        KMulti::List& ga = km->gather[PM == 16 ? 0 : (PM == 24 ? 1 : 2)];
+        const size_t sm = gather_ff_smem(it.ts_g, a.P, an);
+        KMulti::List& ga = km->gather[PM == 16 ? 0 : (PM == 24 ? 1 : 2)][occ_class(sm)];
         ga.add(i, it.ntx_g * it.nty_g);
-        ga.smem = std::max(ga.smem, gather_ff_smem(it.ts_g, a.P, an));
+        ga.smem = std::max(ga.smem, sm);
     }
     *taken = true;
     return FTE_OK;
@@ -2628,16 +2659,16 @@ int fte_kmulti_run(KMulti* km, fte_context* ctx) {
     auto n = [](const KMulti::List& l) { return (int)l.h.size(); };
     if (n(km->zero)) FTE_LAUNCH(ctx, k_zero_multi, n(km->zero), 256, 0, it, (const int2*)km->zero.d);
     if (n(km->win)) FTE_LAUNCH(ctx, k_ff_win_multi, n(km->win), 256, 0, it, (const int2*)km->win.d);
-    if (n(km->spread[0])) {
-        FTE_CUDA_TRY(fte_smem_ceiling(k_spread_ff_multi<2>, km->spread[0].smem));
-        FTE_LAUNCH(ctx, k_spread_ff_multi<2>, n(km->spread[0]), kColThreads, km->spread[0].smem, it,
-                   (const int2*)km->spread[0].d);
-    }
-    if (n(km->spread[1])) {
-        FTE_CUDA_TRY(fte_smem_ceiling(k_spread_ff_multi<3>, km->spread[1].smem));
-        FTE_LAUNCH(ctx, k_spread_ff_multi<3>, n(km->spread[1]), kColThreads, km->spread[1].smem, it,
-                   (const int2*)km->spread[1].d);
-    }
+    for (auto& l : km->spread[0])
+        if (n(l)) {
+            FTE_CUDA_TRY(fte_smem_ceiling(k_spread_ff_multi<2>, l.smem));
+            FTE_LAUNCH(ctx, k_spread_ff_multi<2>, n(l), kColThreads, l.smem, it, (const int2*)l.d);
+        }
+    for (auto& l : km->spread[1])
+        if (n(l)) {
+            FTE_CUDA_TRY(fte_smem_ceiling(k_spread_ff_multi<3>, l.smem));
+            FTE_LAUNCH(ctx, k_spread_ff_multi<3>, n(l), kColThreads, l.smem, it, (const int2*)l.d);
+        }
     for (auto& l : km->yr2c)
         if (n(l)) {
             FTE_CUDA_TRY(fte_smem_ceiling(k_fft_y_r2c_ff_multi, l.smem));
@@ -2662,21 +2693,21 @@ int fte_kmulti_run(KMulti* km, fte_context* ctx) {
             FTE_CUDA_TRY(fte_smem_ceiling(k_fft_y_c2r_ff_multi, l.smem));
             FTE_LAUNCH(ctx, k_fft_y_c2r_ff_multi, n(l), l.threads, l.smem, it, (const int2*)l.d);
         }
-    if (n(km->gather[0])) {
-        FTE_CUDA_TRY(fte_smem_ceiling(k_gather_ff_multi<16>, km->gather[0].smem));
-        FTE_LAUNCH(ctx, k_gather_ff_multi<16>, n(km->gather[0]), kTileThreads, km->gather[0].smem, it,
-                   (const int2*)km->gather[0].d);
-    }
-    if (n(km->gather[1])) {
-        FTE_CUDA_TRY(fte_smem_ceiling(k_gather_ff_multi<24>, km->gather[1].smem));
-        FTE_LAUNCH(ctx, k_gather_ff_multi<24>, n(km->gather[1]), kTileThreads, km->gather[1].smem, it,
-                   (const int2*)km->gather[1].d);
-    }
-    if (n(km->gather[2])) {
-        FTE_CUDA_TRY(fte_smem_ceiling(k_gather_ff_multi<32>, km->gather[2].smem));
-        FTE_LAUNCH(ctx, k_gather_ff_multi<32>, n(km->gather[2]), kTileThreads, km->gather[2].smem, it,
-                   (const int2*)km->gather[2].d);
-    }
+    for (auto& l : km->gather[0])
+        if (n(l)) {
+            FTE_CUDA_TRY(fte_smem_ceiling(k_gather_ff_multi<16>, l.smem));
+            FTE_LAUNCH(ctx, k_gather_ff_multi<16>, n(l), kTileThreads, l.smem, it, (const int2*)l.d);
+        }
+    for (auto& l : km->gather[1])
+        if (n(l)) {
+            FTE_CUDA_TRY(fte_smem_ceiling(k_gather_ff_multi<24>, l.smem));
+            FTE_LAUNCH(ctx, k_gather_ff_multi<24>, n(l), kTileThreads, l.smem, it, (const int2*)l.d);
+        }
+    for (auto& l : km->gather[2])
+        if (n(l)) {
+            FTE_CUDA_TRY(fte_smem_ceiling(k_gather_ff_multi<32>, l.smem));
+            FTE_LAUNCH(ctx, k_gather_ff_multi<32>, n(l), kTileThreads, l.smem, it, (const int2*)l.d);
+        }
     return FTE_OK;
 }
 

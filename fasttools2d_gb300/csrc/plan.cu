@@ -243,6 +243,11 @@ struct fte_batch {
     KMulti* km = nullptr;
     std::vector<char> multi;
     char* mem2 = nullptr;
+    // the work lists' tile sizes and bins per plan (the plan's own bins where
+    // the sizes agree, else bins built into mem3)
+    std::vector<int2> wl_ts;
+    std::vector<TileBins> wl_src, wl_tar;
+    char* mem3 = nullptr;
     PItem* pitems = nullptr;
     int2 *wl_dens = nullptr, *wl_zero = nullptr, *wl_comb = nullptr;
     int n_dens = 0, n_zero = 0, n_comb = 0;
@@ -669,6 +674,45 @@ static int batch_build_lists(fte_batch* b) {
     const size_t np = b->plans.size();
     b->multi.assign(np, 0);
     FTE_TRY(fte_kmulti_create(&b->km));
+    // tile sizes for the work lists (fte_kspace_batch_tiles); bins where a
+    // plan's own differ (tuned or shrunk for its grid alone)
+    b->wl_ts.assign(np, make_int2(0, 0));
+    b->wl_src.resize(np);
+    b->wl_tar.resize(np);
+    std::vector<char> rebuild(np, 0);
+    size_t need3 = 4096;
+    for (size_t i = 0; i < np; i++) {
+        fte_plan* p = b->plans[i];
+        b->wl_src[i] = p->tb_src;
+        b->wl_tar[i] = p->tb_tar;
+        if (p->prm.form != FTE_FORM_FF || p->ntar == 0) continue;
+        int ts_s = 0, ts_g = 0;
+        FTE_TRY(fte_kspace_batch_tiles(c, batch_kspace_args(p, 0), &ts_s, &ts_g));
+        b->wl_ts[i] = make_int2(ts_s, ts_g);
+        if ((p->nsrc > 0 && ts_s != p->tb_src.ts) || ts_g != p->tb_tar.ts) {
+            rebuild[i] = 1;
+            const int M = p->prm.Mx, Mb = p->prm.My;
+            if (ts_s > 0) need3 += fte_tiles_ws(p->nsrc, ((M + ts_s - 1) / ts_s) * ((Mb + ts_s - 1) / ts_s));
+            if (ts_g > 0) need3 += fte_tiles_ws(p->ntar, ((M + ts_g - 1) / ts_g) * ((Mb + ts_g - 1) / ts_g));
+        }
+    }
+    if (need3 > 4096) {
+        if (fte_alloc_should_fail() || cudaMalloc(&b->mem3, need3) != cudaSuccess) {
+            cudaGetLastError();
+            b->mem3 = nullptr;
+            fte_set_error("fte_batch_create: %zu bytes of device memory for tile bins not available", need3);
+            return FTE_ERR_ALLOC;
+        }
+        WsCarver tb{b->mem3, 0, need3};
+        for (size_t i = 0; i < np; i++) {
+            if (!rebuild[i]) continue;
+            KspaceArgs a = batch_kspace_args(b->plans[i], 0);
+            a.ts_spread = b->wl_ts[i].x;
+            a.ts_gather = b->wl_ts[i].y;
+            FTE_TRY(fte_kspace_tiles(c, tb, a, &b->wl_src[i], &b->wl_tar[i]));
+            FTE_WS_CHECK(tb);
+        }
+    }
     // scratch of vectors 1..nv-1 of the float-float plans
     size_t need = ws_bytes(np * sizeof(PItem), 1) + 4096;
     for (size_t i = 0; i < np; i++) {
@@ -724,7 +768,14 @@ static int batch_build_lists(fte_batch* b) {
             FTE_WS_CHECK(m);
             WsCarver wc{scr, 0, p->kscratch_size};
             bool taken = false;
-            FTE_TRY(fte_kmulti_add(b->km, c, wc, batch_kspace_args(p, v), &taken));
+            KspaceArgs a = batch_kspace_args(p, v);
+            if (b->wl_ts[i].y > 0) {
+                a.ts_spread = b->wl_ts[i].x;
+                a.ts_gather = b->wl_ts[i].y;
+                a.pre_src = &b->wl_src[i];
+                a.pre_tar = &b->wl_tar[i];
+            }
+            FTE_TRY(fte_kmulti_add(b->km, c, wc, a, &taken));
             if (!taken) {
                 if (v > 0) {
                     fte_set_error("internal: batch work list took vector 0 of plan %zu but not vector %d", i, v);
@@ -929,6 +980,7 @@ extern "C" int fte_batch_destroy(fte_batch* b) {
     for (auto e : b->events) cudaEventDestroy(e);
     cudaFree(b->mem);
     if (b->mem2) cudaFree(b->mem2);
+    if (b->mem3) cudaFree(b->mem3);
     fte_kmulti_destroy(b->km);
     delete b;
     return FTE_OK;
