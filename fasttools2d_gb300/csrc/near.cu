@@ -275,6 +275,15 @@ struct NearSmem {
     // targets a warp keeps in flight (ring entries carry the slot): the
     // accumulators cost NSLOT * NV * 2 doubles per lane
     static constexpr int kSlots = NV == 1 ? 4 : (NV == 2 ? 2 : 1);
+    // the float-float kernel: the Stokeslet with one vector keeps four
+    // targets' sums in shared memory (a float4 per lane and slot: selecting
+    // among four register copies cost more than the loads; 1e6 points:
+    // near 3.31 -> 3.09 ms at tol 1e-10, 4.07 -> 2.87 ms at 1e-8); the
+    // others keep two (one beyond two vectors) in registers, since the
+    // stresslet's larger staged sources need that shared memory (its
+    // neighbourhoods then split into more chunks: 2.48 -> 3.03 ms)
+    static constexpr bool kAccSmem = KIND == FTE_KIND_SLP && NV == 1;
+    static constexpr int kSlotsFF = kAccSmem ? 4 : (NV <= 2 ? 2 : 1);
     // doubles before the staged sources: the FP64 kernel's K(x) and exp
     // tables, or the float-float kernel's K(x), exp and small-x E1 tables,
     // then the FP32 K(x) table
@@ -288,9 +297,12 @@ struct NearSmem {
         return ff ? 2 * sizeof(float2) + 2 * kDen * NV * sizeof(float)
                   : (2 + kDen * NV) * sizeof(double) + sizeof(float2) + kDen * NV * sizeof(float);
     }
+    __host__ __device__ static size_t acc_bytes(bool ff) {
+        return ff && kAccSmem ? (size_t)NearCfg<true>::warps * kSlotsFF * NV * 32 * sizeof(float4) + 16 : 0;
+    }
     __host__ __device__ static size_t bytes(int cap, bool ff) {
         return head(ff) * sizeof(double) + (size_t)cap * per_source(ff) +
-               (ff ? NearCfg<true>::warps : NearCfg<false>::warps) * 3 * kQueue * sizeof(int) + 64;
+               (ff ? NearCfg<true>::warps : NearCfg<false>::warps) * 3 * kQueue * sizeof(int) + acc_bytes(ff) + 64;
     }
 };
 
@@ -305,10 +317,12 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
     constexpr bool ffn = FF;
     constexpr int kNearThreads = NearCfg<ffn>::threads;
     constexpr int kNearWarps = NearCfg<ffn>::warps;
-    // targets in flight: the FP64 classes gain from four (partial FP64
-    // batches are what costs), the float-float ones from two (the slot
-    // selects are what costs); one beyond two density vectors (registers)
-    constexpr int NSLOT = ffn ? (NV <= 2 ? 2 : 1) : NearSmem<KIND, NV>::kSlots;
+    // targets in flight (up to four for one density vector): a target's
+    // sums stay open until the rings have evaluated its pairs, so that
+    // batches fill up with later targets' pairs instead of being drained
+    // half empty; the sums live in registers (selected per entry) except the
+    // float-float Stokeslet's with one vector (shared memory, NearSmem)
+    constexpr int NSLOT = ffn ? NearSmem<KIND, NV>::kSlotsFF : NearSmem<KIND, NV>::kSlots;
     const int cap = prm.cap;
     // tables: FP64 kernel: ktab, etab, ktab32; float-float kernel: ktabff,
     // etabff, rtabff, ktab32
@@ -329,6 +343,10 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
     float2* slo = reinterpret_cast<float2*>(den32 + (size_t)kDen * NV * cap);
     float* dlo = reinterpret_cast<float*>(slo + (ffn ? cap : 0));
     int* qbuf = reinterpret_cast<int*>(dlo + (ffn ? (size_t)kDen * NV * cap : 0));
+    // float-float class with sums in shared memory: [warp][slot][vector][lane]
+    // (16-byte aligned)
+    float4* const accs = reinterpret_cast<float4*>(
+        (reinterpret_cast<uintptr_t>(qbuf + kNearWarps * 3 * kQueue) + 15) & ~static_cast<uintptr_t>(15));
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     // per warp: ring 0 = pairs with x >= 1 (FP64, or float-float when ffn),
@@ -463,7 +481,11 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
         int Pf = 0, Ef = 0, Pn = 0, En = 0;  // pushed / evaluated counts of rings qf, qn
         int tailF[NSLOT], tailN[NSLOT];      // Pf, Pn after each slot's sweep
         double acc[NSLOT][NV][2];
-        float accf[NSLOT][NV][4];  // float-float class: (sum, low parts) per component
+        // float-float class: (sum, low parts) per component per slot, in
+        // registers or (kAccSmem) this lane's entries in shared memory
+        constexpr bool acc_smem = NearSmem<KIND, NV>::kAccSmem;
+        float4* const accw = accs + (size_t)warp * NSLOT * NV * 32 + lane;
+        float accf[acc_smem ? 1 : NSLOT][NV][4];
         float acc32[NV][2];
 #pragma unroll
         for (int j = 0; j < NSLOT; j++) {
@@ -471,7 +493,11 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
 #pragma unroll
             for (int v = 0; v < NV; v++) {
                 acc[j][v][0] = acc[j][v][1] = 0.0;
-                accf[j][v][0] = accf[j][v][1] = accf[j][v][2] = accf[j][v][3] = 0.0f;
+                if constexpr (acc_smem) {
+                    if (ffn) accw[(j * NV + v) * 32] = make_float4(0.f, 0.f, 0.f, 0.f);
+                } else {
+                    accf[j][v][0] = accf[j][v][1] = accf[j][v][2] = accf[j][v][3] = 0.0f;
+                }
             }
         }
 #pragma unroll
@@ -503,25 +529,37 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
                     acc[j][v][1] = m ? a1 : acc[j][v][1];
                 }
         };
+        // (each lane reads and writes only its own entries: no barrier)
+        // (selects written as conditional expressions, no branches)
         auto accf_get = [&](int tag, int v, float* a) {
+            if constexpr (acc_smem) {
+                const float4 t = accw[(tag * NV + v) * 32];
+                a[0] = t.x;
+                a[1] = t.y;
+                a[2] = t.z;
+                a[3] = t.w;
+            } else {
 #pragma unroll
-            for (int i = 0; i < 4; i++) a[i] = accf[0][v][i];
+                for (int i = 0; i < 4; i++) a[i] = accf[0][v][i];
 #pragma unroll
-            for (int j = 1; j < NSLOT; j++)
-                {
+                for (int j = 1; j < NSLOT; j++) {
                     const bool m = tag == j;
 #pragma unroll
                     for (int i = 0; i < 4; i++) a[i] = m ? accf[j][v][i] : a[i];
                 }
+            }
         };
         auto accf_put = [&](int tag, int v, const float* a) {
+            if constexpr (acc_smem) {
+                accw[(tag * NV + v) * 32] = make_float4(a[0], a[1], a[2], a[3]);
+            } else {
 #pragma unroll
-            for (int j = 0; j < NSLOT; j++)
-                {
+                for (int j = 0; j < NSLOT; j++) {
                     const bool m = tag == j;
 #pragma unroll
                     for (int i = 0; i < 4; i++) accf[j][v][i] = m ? a[i] : accf[j][v][i];
                 }
+            }
         };
 
         // FP32 class: the same pair terms in FP32 from box-relative
