@@ -806,18 +806,17 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
 
         // evaluate everything pending in ring qf (if df) and qn (if dn);
         // both hold fewer than 32 entries here
+        // (one call site per ring: each inlined copy of a pair evaluation
+        // is hundreds of instructions, and copies at several sites made
+        // the kernel wait on instruction fetch)
         auto drain = [&](bool df, bool dn) {
             const int cf = df ? Pf - Ef : 0, cn = dn ? Pn - En : 0;
-            // the two rings share one pass when they fit in a warp
-            if (cf + cn <= 32) {
-                if (lane < cf)
-                    evalF(qf[(Ef + lane) & (kQueue - 1)]);
-                else if (lane < cf + cn)
-                    evalN(qn[(En + lane - cf) & (kQueue - 1)]);
-            } else {
-                if (lane < cf) evalF(qf[(Ef + lane) & (kQueue - 1)]);
-                if (lane < cn) evalN(qn[(En + lane) & (kQueue - 1)]);
-            }
+            // the two rings share one pass when they fit in a warp (the two
+            // divergent halves run one after the other either way)
+            const bool one = cf + cn <= 32;
+            const int ln = one ? lane - cf : lane;
+            if (lane < cf) evalF(qf[(Ef + lane) & (kQueue - 1)]);
+            if (ln >= 0 && ln < cn) evalN(qn[(En + ln) & (kQueue - 1)]);
             Ef += cf;
             En += cn;
             __syncwarp();
@@ -890,136 +889,138 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
         // its lane
         double2 tpl = make_double2(0.0, 0.0);
         float4 tfl = make_float4(0.f, 0.f, 0.f, 0.f);
-        for (int k = 0; k < ntw; k++) {
-            const int slot = k & (NSLOT - 1);
-            if ((k & 31) == 0 && k + lane < ntw) {
-                tpl = prm.tpos[t0 + warp + (k + lane) * kNearWarps];
-                const double rx = tpl.x - cx, ry = tpl.y - cy;
-                if (ffn) {
-                    const float2 fx = ff_split(rx), fy = ff_split(ry);
-                    tfl = make_float4(fx.x, fx.y, fy.x, fy.y);
-                } else {
-                    tfl = make_float4((float)rx, 0.f, (float)ry, 0.f);
-                }
-            }
-            if (lane == (k & 31)) {
-                tsl[slot] = tpl;
-                tsf[slot] = tfl;
-            }
-            tx32 = __shfl_sync(0xffffffffu, tfl.x, k & 31);
-            ty32 = __shfl_sync(0xffffffffu, tfl.z, k & 31);
-            __syncwarp();
-            int hs = 0, cs = 0;  // FP32-class ring head and count
-
-            // candidate test of staged source s against the target being swept
-            auto test = [&](int s, bool& pass, bool& small_x, bool& single) {
-                pass = small_x = single = false;
-                if (s < clen) {
-                    const float2 q = s32[s];
-                    float dx = q.x - tx32, dy = q.y - ty32;
-                    float r2f = dx * dx + dy * dy;
-                    pass = (s < own_lim) || (r2f < prm.cut32);
-                    const float xf = r2f * xi2f;
-                    small_x = xf < xsplit;
-                    single = xf >= x32;
-                }
-            };
-            // NB = 2 batches of 32 candidates per step: independent tests in
-            // flight and one set of ring updates (measured at 1e6 points:
-            // stresslet near 8-9 % faster at tol 1e-10 and 1e-6, Stokeslet
-            // 9 % faster at 1e-6 and 2 % slower at 1e-10).  The rings hold up
-            // to 31 + 64 entries, and every full batch of 32 is evaluated
-            // before the next step from a single call site each.
-            constexpr int NB = 2;
-            for (int base = 0; base < clen; base += 32 * NB) {
-                const int s0 = base + lane, s1 = base + 32 + lane;
-                bool p0, x0, g0, p1 = false, x1 = false, g1 = false;
-                test(s0, p0, x0, g0);
-                if constexpr (NB == 2) test(s1, p1, x1, g1);
-                {
-                    const bool a0 = p0 && g0, a1 = p1 && g1;
-                    const unsigned m0 = __ballot_sync(0xffffffffu, a0), m1 = NB == 2 ? __ballot_sync(0xffffffffu, a1) : 0u;
-                    const int c0 = __popc(m0);
-                    if (a0) qs[(hs + cs + __popc(m0 & lt_mask)) & (kQueue - 1)] = s0;
-                    if (a1) qs[(hs + cs + c0 + __popc(m1 & lt_mask)) & (kQueue - 1)] = s1;
-                    cs += c0 + __popc(m1);
-                    p0 = p0 && !g0;
-                    p1 = p1 && !g1;
-                    __syncwarp();
-                    while (cs >= 32) {
-                        if (KIND == FTE_KIND_SLP)
-                            eval_slp32(qs[(hs + lane) & (kQueue - 1)]);
-                        else
-                            eval_dlp32(qs[(hs + lane) & (kQueue - 1)]);
-                        hs = (hs + 32) & (kQueue - 1);
-                        cs -= 32;
-                        __syncwarp();
+        // NSLOT - 1 steps past the last target finalize the targets still
+        // in flight (one finalize site; its drain evaluates what the rings
+        // still hold)
+        for (int k = 0; k < ntw + NSLOT - 1; k++) {
+            if (k < ntw) {
+                const int slot = k & (NSLOT - 1);
+                if ((k & 31) == 0 && k + lane < ntw) {
+                    tpl = prm.tpos[t0 + warp + (k + lane) * kNearWarps];
+                    const double rx = tpl.x - cx, ry = tpl.y - cy;
+                    if (ffn) {
+                        const float2 fx = ff_split(rx), fy = ff_split(ry);
+                        tfl = make_float4(fx.x, fx.y, fy.x, fy.y);
+                    } else {
+                        tfl = make_float4((float)rx, 0.f, (float)ry, 0.f);
                     }
                 }
-                const int e0 = (s0 << 2) | slot, e1 = (s1 << 2) | slot;
-                // the Stokeslet's pairs with x < 1 take ring qn (the series of
-                // E1); the stresslet has one pair formula
-                if constexpr (KIND == FTE_KIND_SLP) {
-                    const bool f0 = p0 && !x0, n0 = p0 && x0, f1 = p1 && !x1, n1 = p1 && x1;
-                    const unsigned mf0 = __ballot_sync(0xffffffffu, f0), mf1 = NB == 2 ? __ballot_sync(0xffffffffu, f1) : 0u;
-                    const unsigned mn0 = __ballot_sync(0xffffffffu, n0), mn1 = NB == 2 ? __ballot_sync(0xffffffffu, n1) : 0u;
-                    const int cf0 = __popc(mf0), cn0 = __popc(mn0);
-                    if (f0) qf[(Pf + __popc(mf0 & lt_mask)) & (kQueue - 1)] = e0;
-                    if (f1) qf[(Pf + cf0 + __popc(mf1 & lt_mask)) & (kQueue - 1)] = e1;
-                    if (n0) qn[(Pn + __popc(mn0 & lt_mask)) & (kQueue - 1)] = e0;
-                    if (n1) qn[(Pn + cn0 + __popc(mn1 & lt_mask)) & (kQueue - 1)] = e1;
-                    Pf += cf0 + __popc(mf1);
-                    Pn += cn0 + __popc(mn1);
-                } else {
-                    const unsigned mf0 = __ballot_sync(0xffffffffu, p0), mf1 = NB == 2 ? __ballot_sync(0xffffffffu, p1) : 0u;
-                    const int cf0 = __popc(mf0);
-                    if (p0) qf[(Pf + __popc(mf0 & lt_mask)) & (kQueue - 1)] = e0;
-                    if (p1) qf[(Pf + cf0 + __popc(mf1 & lt_mask)) & (kQueue - 1)] = e1;
-                    Pf += cf0 + __popc(mf1);
+                if (lane == (k & 31)) {
+                    tsl[slot] = tpl;
+                    tsf[slot] = tfl;
                 }
+                tx32 = __shfl_sync(0xffffffffu, tfl.x, k & 31);
+                ty32 = __shfl_sync(0xffffffffu, tfl.z, k & 31);
                 __syncwarp();
-                while (Pf - Ef >= 32) {
-                    evalF(qf[(Ef + lane) & (kQueue - 1)]);
-                    Ef += 32;
+                int hs = 0, cs = 0;  // FP32-class ring head and count
+
+                // candidate test of staged source s against the target being swept
+                auto test = [&](int s, bool& pass, bool& small_x, bool& single) {
+                    pass = small_x = single = false;
+                    if (s < clen) {
+                        const float2 q = s32[s];
+                        float dx = q.x - tx32, dy = q.y - ty32;
+                        float r2f = dx * dx + dy * dy;
+                        pass = (s < own_lim) || (r2f < prm.cut32);
+                        const float xf = r2f * xi2f;
+                        small_x = xf < xsplit;
+                        single = xf >= x32;
+                    }
+                };
+                // NB = 2 batches of 32 candidates per step: independent tests in
+                // flight and one set of ring updates (measured at 1e6 points:
+                // stresslet near 8-9 % faster at tol 1e-10 and 1e-6, Stokeslet
+                // 9 % faster at 1e-6 and 2 % slower at 1e-10).  The rings hold up
+                // to 31 + 64 entries, and every full batch of 32 is evaluated
+                // before the next step from a single call site each.
+                constexpr int NB = 2;
+                for (int base = 0; base < clen; base += 32 * NB) {
+                    const int s0 = base + lane, s1 = base + 32 + lane;
+                    bool p0, x0, g0, p1 = false, x1 = false, g1 = false;
+                    test(s0, p0, x0, g0);
+                    if constexpr (NB == 2) test(s1, p1, x1, g1);
+                    {
+                        const bool a0 = p0 && g0, a1 = p1 && g1;
+                        const unsigned m0 = __ballot_sync(0xffffffffu, a0), m1 = NB == 2 ? __ballot_sync(0xffffffffu, a1) : 0u;
+                        const int c0 = __popc(m0);
+                        if (a0) qs[(hs + cs + __popc(m0 & lt_mask)) & (kQueue - 1)] = s0;
+                        if (a1) qs[(hs + cs + c0 + __popc(m1 & lt_mask)) & (kQueue - 1)] = s1;
+                        cs += c0 + __popc(m1);
+                        p0 = p0 && !g0;
+                        p1 = p1 && !g1;
+                        __syncwarp();
+                        while (cs >= 32) {
+                            if (KIND == FTE_KIND_SLP)
+                                eval_slp32(qs[(hs + lane) & (kQueue - 1)]);
+                            else
+                                eval_dlp32(qs[(hs + lane) & (kQueue - 1)]);
+                            hs = (hs + 32) & (kQueue - 1);
+                            cs -= 32;
+                            __syncwarp();
+                        }
+                    }
+                    const int e0 = (s0 << 2) | slot, e1 = (s1 << 2) | slot;
+                    // the Stokeslet's pairs with x < 1 take ring qn (the series of
+                    // E1); the stresslet has one pair formula
+                    if constexpr (KIND == FTE_KIND_SLP) {
+                        const bool f0 = p0 && !x0, n0 = p0 && x0, f1 = p1 && !x1, n1 = p1 && x1;
+                        const unsigned mf0 = __ballot_sync(0xffffffffu, f0), mf1 = NB == 2 ? __ballot_sync(0xffffffffu, f1) : 0u;
+                        const unsigned mn0 = __ballot_sync(0xffffffffu, n0), mn1 = NB == 2 ? __ballot_sync(0xffffffffu, n1) : 0u;
+                        const int cf0 = __popc(mf0), cn0 = __popc(mn0);
+                        if (f0) qf[(Pf + __popc(mf0 & lt_mask)) & (kQueue - 1)] = e0;
+                        if (f1) qf[(Pf + cf0 + __popc(mf1 & lt_mask)) & (kQueue - 1)] = e1;
+                        if (n0) qn[(Pn + __popc(mn0 & lt_mask)) & (kQueue - 1)] = e0;
+                        if (n1) qn[(Pn + cn0 + __popc(mn1 & lt_mask)) & (kQueue - 1)] = e1;
+                        Pf += cf0 + __popc(mf1);
+                        Pn += cn0 + __popc(mn1);
+                    } else {
+                        const unsigned mf0 = __ballot_sync(0xffffffffu, p0), mf1 = NB == 2 ? __ballot_sync(0xffffffffu, p1) : 0u;
+                        const int cf0 = __popc(mf0);
+                        if (p0) qf[(Pf + __popc(mf0 & lt_mask)) & (kQueue - 1)] = e0;
+                        if (p1) qf[(Pf + cf0 + __popc(mf1 & lt_mask)) & (kQueue - 1)] = e1;
+                        Pf += cf0 + __popc(mf1);
+                    }
                     __syncwarp();
-                }
-                if constexpr (KIND == FTE_KIND_SLP) {
-                    while (Pn - En >= 32) {
-                        evalN(qn[(En + lane) & (kQueue - 1)]);
-                        En += 32;
+                    while (Pf - Ef >= 32) {
+                        evalF(qf[(Ef + lane) & (kQueue - 1)]);
+                        Ef += 32;
                         __syncwarp();
                     }
+                    if constexpr (KIND == FTE_KIND_SLP) {
+                        while (Pn - En >= 32) {
+                            evalN(qn[(En + lane) & (kQueue - 1)]);
+                            En += 32;
+                            __syncwarp();
+                        }
+                    }
                 }
-            }
-            // the target's FP32 class: last partial batch, then its sums
-            // (lanes 0-15 reduce component 0, lanes 16-31 component 1)
-            if (lane < cs) {
-                if (KIND == FTE_KIND_SLP)
-                    eval_slp32(qs[(hs + lane) & (kQueue - 1)]);
-                else
-                    eval_dlp32(qs[(hs + lane) & (kQueue - 1)]);
-            }
-            {
-                const bool hi = (lane & 16) != 0;
-#pragma unroll
-                for (int v = 0; v < NV; v++) {
-                    float keep = hi ? acc32[v][1] : acc32[v][0];
-                    keep += __shfl_xor_sync(0xffffffffu, hi ? acc32[v][0] : acc32[v][1], 16);
-#pragma unroll
-                    for (int o = 8; o > 0; o >>= 1) keep += __shfl_xor_sync(0xffffffffu, keep, o);
-                    if ((lane & 15) == 0) fsw[(slot * NV + v) * 2 + (hi ? 1 : 0)] = keep;
-                    acc32[v][0] = acc32[v][1] = 0.0f;
+                // the target's FP32 class: last partial batch, then its sums
+                // (lanes 0-15 reduce component 0, lanes 16-31 component 1)
+                if (lane < cs) {
+                    if (KIND == FTE_KIND_SLP)
+                        eval_slp32(qs[(hs + lane) & (kQueue - 1)]);
+                    else
+                        eval_dlp32(qs[(hs + lane) & (kQueue - 1)]);
                 }
-            }
+                {
+                    const bool hi = (lane & 16) != 0;
 #pragma unroll
-            for (int j = 0; j < NSLOT; j++)
-                if (slot == j) tailF[j] = Pf, tailN[j] = Pn;
+                    for (int v = 0; v < NV; v++) {
+                        float keep = hi ? acc32[v][1] : acc32[v][0];
+                        keep += __shfl_xor_sync(0xffffffffu, hi ? acc32[v][0] : acc32[v][1], 16);
+#pragma unroll
+                        for (int o = 8; o > 0; o >>= 1) keep += __shfl_xor_sync(0xffffffffu, keep, o);
+                        if ((lane & 15) == 0) fsw[(slot * NV + v) * 2 + (hi ? 1 : 0)] = keep;
+                        acc32[v][0] = acc32[v][1] = 0.0f;
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < NSLOT; j++)
+                    if (slot == j) tailF[j] = Pf, tailN[j] = Pn;
+            }
             // the oldest target in flight gives up its slot to target k + 1
             if (k >= NSLOT - 1) finalize(k - (NSLOT - 1));
         }
-        // end of the chunk: evaluate what the rings hold, store the rest
-        if (Pf > Ef || Pn > En) drain(true, true);
-        for (int kk = ntw - (NSLOT - 1) > 0 ? ntw - (NSLOT - 1) : 0; kk < ntw; kk++) finalize(kk);
         __syncwarp();
     }
 }
