@@ -64,13 +64,19 @@ __global__ void k_plan_dens(const double* __restrict__ f1s, const double* __rest
         plan_dens_one<KIND>(f1s, f2s, nv, n, nrm, wts, sidx, q0, q1, q2, fv, d);
 }
 
-// zero mode sum_s (f.n) x_s of vector v (stresslet), by one block of 256
-// threads
-__device__ __forceinline__ void plan_zero_vec(const double* __restrict__ ps, const double* __restrict__ fv,
-                                              const double* __restrict__ nrm, const double* __restrict__ wts,
-                                              int64_t n, double* __restrict__ zero, int v) {
+// zero mode sum_s (f.n) x_s of vector v (stresslet): block c of 256 threads
+// sums sources [c kZeroChunk, (c + 1) kZeroChunk) and adds its part to
+// zero[2v..2v+1] (zeroed before) with FP64 atomics, as the drivers' density
+// reduction does (one block per vector took 2 ms at 1e6 sources)
+constexpr int kZeroChunk = 8192;
+__host__ __device__ inline int zero_chunks(int64_t n) { return (int)((n + kZeroChunk - 1) / kZeroChunk); }
+
+__device__ __forceinline__ void plan_zero_part(const double* __restrict__ ps, const double* __restrict__ fv,
+                                               const double* __restrict__ nrm, const double* __restrict__ wts,
+                                               int64_t n, double* __restrict__ zero, int v, int c) {
     double zx = 0, zy = 0;
-    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    const int64_t i1 = (int64_t)(c + 1) * kZeroChunk < n ? (int64_t)(c + 1) * kZeroChunk : n;
+    for (int64_t i = (int64_t)c * kZeroChunk + threadIdx.x; i < i1; i += blockDim.x) {
         const double w = wts ? wts[i] : 1.0;
         const double fn = (fv[(v * n + i) * 2] * nrm[2 * i] + fv[(v * n + i) * 2 + 1] * nrm[2 * i + 1]) * w;
         zx += fn * ps[2 * i];
@@ -88,16 +94,16 @@ __device__ __forceinline__ void plan_zero_vec(const double* __restrict__ ps, con
         __syncthreads();
     }
     if (threadIdx.x == 0) {
-        zero[2 * v] = sx[0];
-        zero[2 * v + 1] = sy[0];
+        atomicAdd(&zero[2 * v], sx[0]);
+        atomicAdd(&zero[2 * v + 1], sy[0]);
     }
 }
 
-// one block per vector
+// grid (chunks, vectors)
 __global__ void k_plan_zero(const double* __restrict__ ps, const double* __restrict__ fv,
                             const double* __restrict__ nrm, const double* __restrict__ wts, int64_t n,
                             double* __restrict__ zero) {
-    plan_zero_vec(ps, fv, nrm, wts, n, zero, blockIdx.x);
+    plan_zero_part(ps, fv, nrm, wts, n, zero, blockIdx.y, blockIdx.x);
 }
 
 // u = ur + uk (+ the zero mode) of target i for nv vectors
@@ -135,6 +141,8 @@ struct PItem {
 __global__ void k_plan_dens_multi(const PItem* __restrict__ items, const int2* __restrict__ wl) {
     const int2 w = wl[blockIdx.x];
     const PItem& it = items[w.x];
+    // the zero-mode sums start from zero (their kernel runs after this one)
+    if (w.y == 0 && it.zero && threadIdx.x < 2 * it.nv) it.zero[threadIdx.x] = 0.0;
     const int64_t d = (int64_t)w.y * blockDim.x + threadIdx.x;
     if (d >= it.nsrc) return;
     if (it.kind == FTE_KIND_SLP)
@@ -145,11 +153,12 @@ __global__ void k_plan_dens_multi(const PItem* __restrict__ items, const int2* _
                                     it.fv, d);
 }
 
-// work items (stresslet plan, vector)
+// work items (stresslet plan, vector x chunks + chunk)
 __global__ void k_plan_zero_multi(const PItem* __restrict__ items, const int2* __restrict__ wl) {
     const int2 w = wl[blockIdx.x];
     const PItem& it = items[w.x];
-    plan_zero_vec(it.ps, it.fv, it.nrm, it.wts, it.nsrc, it.zero, w.y);
+    const int nch = zero_chunks(it.nsrc);
+    plan_zero_part(it.ps, it.fv, it.nrm, it.wts, it.nsrc, it.zero, w.y / nch, w.y % nch);
 }
 
 // work items (plan, block of 256 targets)
@@ -326,9 +335,11 @@ static int plan_exec_body(fte_plan* p, int nv, const double* f1s, const double* 
         a.ts_gather = p->prm.ts_gather;
         FTE_TRY(fte_kspace_run(c, wc, a, nullptr));
     }
-    if (p->kind == FTE_KIND_DLP && ns > 0)
-        FTE_LAUNCH(c, k_plan_zero, nv, 256, 0, (const double*)p->ps, (const double*)p->fv, (const double*)p->nrm,
-                   (const double*)p->wts, ns, p->zero);
+    if (p->kind == FTE_KIND_DLP && ns > 0) {
+        FTE_CUDA_TRY(cudaMemsetAsync(p->zero, 0, 2 * nv * sizeof(double), c->stream));
+        FTE_LAUNCH(c, k_plan_zero, dim3(zero_chunks(ns), nv), 256, 0, (const double*)p->ps, (const double*)p->fv,
+                   (const double*)p->nrm, (const double*)p->wts, ns, p->zero);
+    }
     FTE_LAUNCH(c, k_plan_combine, grid_of(c, nt), 256, 0, (const double2*)p->ur, (const double2*)p->uk, nv, nt,
                p->kind == FTE_KIND_DLP ? (const double*)p->zero : nullptr, 1.0 / (p->Lx * p->Ly), u1s, u2s);
     return FTE_OK;
@@ -633,7 +644,9 @@ static int batch_run(fte_batch* b) {
                 rc = fte_kspace_run(c, wc, a, nullptr);
             }
             if (rc == FTE_OK && p->kind == FTE_KIND_DLP && p->nsrc > 0) {
-                k_plan_zero<<<b->nv, 256, 0, c->stream>>>(p->ps, p->fv, p->nrm, p->wts, p->nsrc, p->zero);
+                cudaMemsetAsync(p->zero, 0, 2 * b->nv * sizeof(double), c->stream);
+                k_plan_zero<<<dim3(zero_chunks(p->nsrc), b->nv), 256, 0, c->stream>>>(p->ps, p->fv, p->nrm, p->wts,
+                                                                                      p->nsrc, p->zero);
                 c->kernels++;
             }
             if (rc == FTE_OK) {
@@ -787,7 +800,7 @@ static int batch_build_lists(fte_batch* b) {
         }
         if (!b->multi[i]) continue;
         if (p->kind == FTE_KIND_DLP && p->nsrc > 0)
-            for (int v = 0; v < nv; v++) zero.push_back(make_int2((int)i, v));
+            for (int v = 0; v < nv * zero_chunks(p->nsrc); v++) zero.push_back(make_int2((int)i, v));
         for (int j = 0; j < (int)((p->ntar + 255) / 256); j++) comb.push_back(make_int2((int)i, j));
     }
     FTE_TRY(fte_kmulti_finalize(b->km, c));
