@@ -41,6 +41,10 @@ struct NearCfg {
     static constexpr int warps = threads / 32;
     static constexpr int ctas = L ? 5 : 2;          // per SM
     static constexpr int grid_per_sm = L ? 32 : 16;  // grid-stride launch size
+    // dynamic shared memory per CTA; five float-float CTAs per SM fit with
+    // 0.8 KB to spare (dynamic + 464 B static + the 1 KB the runtime
+    // reserves per CTA, x 5, against 228 KB): more static shared memory in
+    // the kernel drops it to four CTAs unless this shrinks
     static constexpr size_t budget = L ? 44 * 1024 : 110 * 1024;
 };
 constexpr int kQueue = 128;  // ring entries per warp and class (a sweep step adds up to 64)
