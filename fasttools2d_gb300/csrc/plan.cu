@@ -644,7 +644,12 @@ static int batch_run(fte_batch* b) {
                 rc = fte_kspace_run(c, wc, a, nullptr);
             }
             if (rc == FTE_OK && p->kind == FTE_KIND_DLP && p->nsrc > 0) {
-                cudaMemsetAsync(p->zero, 0, 2 * b->nv * sizeof(double), c->stream);
+                const cudaError_t em = cudaMemsetAsync(p->zero, 0, 2 * b->nv * sizeof(double), c->stream);
+                if (em != cudaSuccess) {
+                    fte_set_error("batch: memset failed: %s", cudaGetErrorString(em));
+                    rc = FTE_ERR_CUDA;
+                    break;
+                }
                 k_plan_zero<<<dim3(zero_chunks(p->nsrc), b->nv), 256, 0, c->stream>>>(p->ps, p->fv, p->nrm, p->wts,
                                                                                       p->nsrc, p->zero);
                 c->kernels++;
