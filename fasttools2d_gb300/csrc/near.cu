@@ -1399,8 +1399,14 @@ __global__ void k_special_probe(int which, const double* __restrict__ x, double*
             }
             break;
         }
-        default:  // 1/x
+        case 3:  // 1/x
             r = fte_rcp(v);
+            break;
+        case 4:  // the drivers' coordinate wrap, box side 1
+            r = fte_wrap_coord(v, 1.0, 1.0);
+            break;
+        default:  // the same, box side 2.75
+            r = fte_wrap_coord(v, 2.75, 1.0 / 2.75);
             break;
     }
     out[i] = r;
@@ -1409,7 +1415,7 @@ __global__ void k_special_probe(int which, const double* __restrict__ x, double*
 
 extern "C" int fte_debug_special(int which, const double* x_dev, double* out_dev, int n) {
     if (n <= 0) return FTE_OK;
-    if (which < 0 || which > 3 || !x_dev || !out_dev) {
+    if (which < 0 || which > 5 || !x_dev || !out_dev) {
         fte_set_error("fte_debug_special: bad arguments");
         return FTE_ERR_INVALID;
     }

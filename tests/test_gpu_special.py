@@ -59,3 +59,23 @@ def test_e1_and_stokeslet_weight_against_scipy(gpu_ctx):
     # absolute accuracy relative to the larger of the two terms
     scale = np.maximum(0.5 * ref, np.exp(-x))
     assert np.max(np.abs(w - refw) / scale) <= 2e-15
+
+
+@pytest.mark.parametrize("which,L", [(4, 1.0), (5, 2.75)])
+def test_coordinate_wrap_is_the_drivers_formula_bit_for_bit(gpu_ctx, which, L):
+    """The device wrap (with its shortcut for points inside the box) equals
+    MATLAB's mod(x + L/2, L) - L/2 with mod's round-off compensation, as the
+    oracle restates it, bit for bit: random points in and around the box,
+    the box edges and their neighbouring doubles, multiples of L, and points
+    whose shifted coordinate lies just below L."""
+    from oracle import pyoracle as po
+
+    rng = np.random.default_rng(11)
+    edges = np.array([-L / 2, L / 2, 0.0, L, -L, 2.5 * L, -3.5 * L, 1e-300, -1e-300])
+    near = np.concatenate([np.nextafter(edges, np.inf), np.nextafter(edges, -np.inf)])
+    below = L / 2 - L * np.array([1e-16, 2e-16, 5e-16, 1e-15, 2e-15, 1e-14])
+    x = np.concatenate([(rng.random(20000) - 0.5) * L, (rng.random(20000) - 0.5) * 7 * L, edges, near, below,
+                        np.nextafter(below, np.inf), np.nextafter(below, -np.inf)])
+    mine, _ = _probe(which, x)
+    ref = po.matlab_wrap(x, L)
+    assert np.array_equal(mine.view(np.int64), ref.view(np.int64))
