@@ -48,8 +48,9 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--quick", action="store_true", help="headline only (for profiling runs)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched 64-configuration section")
-    ap.add_argument("--profile", choices=["plain", "mixed"], default=None,
-                    help="time only this form at tol 1e-10 (for profiler launch lists); no other sections")
+    ap.add_argument("--profile", choices=["plain", "mixed", "batched"], default=None,
+                    help="time only this form at tol 1e-10, or only the batched form's graph step (for profiler "
+                         "launch lists); no other sections")
     return ap.parse_args()
 
 
@@ -231,6 +232,58 @@ def cpu_baseline(n_full):
 # ---------------------------------------------------------------------------
 # our arm
 # ---------------------------------------------------------------------------
+def config4_device(ft, wl, nv):
+    """The 64-configuration workload on the device (positions, normals, nv
+    density vectors per configuration)."""
+    import numpy as np
+    import torch
+
+    dev = []
+    for c in wl.config4():
+        d = {k: torch.tensor(c[k], dtype=torch.float64, device="cuda") for k in ("xsrc", "ysrc", "n1", "n2")}
+        d["f1"] = torch.tensor(np.stack([f[0] for f in c["f"][:nv]]), dtype=torch.float64, device="cuda")
+        d["f2"] = torch.tensor(np.stack([f[1] for f in c["f"][:nv]]), dtype=torch.float64, device="cuda")
+        d["Lx"], d["Ly"] = c["Lx"], c["Ly"]
+        dev.append(d)
+    return dev
+
+
+def batched_profile(ft, wl, ctx, stream, steps, warmup, flush):
+    """The batched form's graph step alone (plans with autotuned tiles, one
+    batch, `warmup` untimed replays, then `steps` timed ones): for launch
+    lists of the batch's kernels."""
+    import torch
+
+    nv, tol = 4, 1e-8
+    kinds = (ft.KIND_SLP, ft.KIND_DLP)
+    dev = config4_device(ft, wl, nv)
+    plans = [ft.Plan(kind, d["xsrc"], d["ysrc"], d["xsrc"], d["ysrc"], d["f1"][0], d["f2"][0], d["Lx"], d["Ly"],
+                     n1=d["n1"], n2=d["n2"], tol=tol, form=ft.FORM_MIXED, nvmax=nv, tune=True, ctx=ctx)
+             for d in dev for kind in kinds]
+    batch = ft.Batch(plans, nv, ctx=ctx)
+    for i in range(len(plans)):
+        d = dev[i // len(kinds)]
+        batch.set_density(i, d["f1"], d["f2"])
+    k0 = ctx.kernel_count
+    batch.launch(False)  # one step outside the graph: its launches are counted
+    launches = ctx.kernel_count - k0
+    for _ in range(max(warmup, 1)):
+        batch.launch(True)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    torch.cuda.synchronize()
+    for i in range(steps):
+        flush.fill_(float(i))
+        ev[i][0].record(stream)
+        batch.launch(True)
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in ev) / steps
+    npts = sum(int(d["xsrc"].numel()) for d in dev)
+    return {"metric": "targets/s, 64-configuration batch (config 4), tol 1e-8", "profile": "batched",
+            "ms_per_step": ms, "value": npts * nv * len(kinds) / (ms / 1e3), "unit": "targets/s",
+            "gpu_launches_per_step": launches}
+
+
 def batched_section(ft, wl, ctx, stream, steps, warmup, flush):
     """Batched form on the 64-configuration workload (config 4): every
     configuration evaluated with the Stokeslet and the stresslet for 4
@@ -257,13 +310,7 @@ def batched_section(ft, wl, ctx, stream, steps, warmup, flush):
     cfgs = wl.config4()
     nv, tol = 4, 1e-8
     kinds = (ft.KIND_SLP, ft.KIND_DLP)
-    dev = []
-    for c in cfgs:
-        d = {k: torch.tensor(c[k], dtype=torch.float64, device="cuda") for k in ("xsrc", "ysrc", "n1", "n2")}
-        d["f1"] = torch.tensor(np.stack([f[0] for f in c["f"][:nv]]), dtype=torch.float64, device="cuda")
-        d["f2"] = torch.tensor(np.stack([f[1] for f in c["f"][:nv]]), dtype=torch.float64, device="cuda")
-        d["Lx"], d["Ly"] = c["Lx"], c["Ly"]
-        dev.append(d)
+    dev = config4_device(ft, wl, nv)
     npts = sum(len(c["xsrc"]) for c in cfgs)
     targets_per_step = npts * nv * len(kinds)
 
@@ -493,6 +540,12 @@ def main():
     dev = {k: torch.tensor(cfg[k], dtype=torch.float64, device="cuda") for k in keys}
     outs = [torch.empty(N, dtype=torch.float64, device="cuda") for _ in range(4)]
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
+    if args.profile == "batched":
+        line = batched_profile(ft, wl, ctx, stream, args.steps, args.warmup, flush)
+        if rank == 0:
+            print(json.dumps(line), flush=True)
+        reps.close()
+        return
 
     def step(tol, form, arrays=None, out=None):
         a = arrays or dev

@@ -314,8 +314,10 @@ struct NearSmem {
 // density vectors at once: the pair geometry and the special functions are
 // evaluated once per pair and shared by the vectors.
 template <int KIND, int NV, bool FF>
-__device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned char* smem_raw, int* nb_box,
-                                         int* nb_start, double* nb_shx, double* nb_shy) {
+// (part `part` of `nparts` of the box's targets: a problem with fewer boxes
+// than the GPU has CTA slots splits each box's targets over several CTAs)
+__device__ __forceinline__ void near_box(const NearParams& prm, int b, int part, int nparts, unsigned char* smem_raw,
+                                         int* nb_box, int* nb_start, double* nb_shx, double* nb_shy) {
     constexpr int kDen = NearSmem<KIND, NV>::kDen;
     // float-float class (FF)
     constexpr bool ffn = FF;
@@ -360,12 +362,16 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
     int* qn = qf + kQueue;
     int* qs = qn + kQueue;
     // per warp and target slot: the target's position and its FP32-class sums
+    // (ring entries carry the slot in two bits; the FP32-class sums of a
+    // warp hold two components per slot and vector)
+    static_assert(NSLOT >= 1 && NSLOT <= 4 && (NSLOT & (NSLOT - 1)) == 0, "target slots");
+    constexpr int kFsum = 2 * NSLOT * NV > 8 ? 2 * NSLOT * NV : 8;
     __shared__ double2 tslot[kNearWarps * 4];
     __shared__ float4 tslot_ff[kNearWarps * 4];  // box-relative (x hi, x lo, y hi, y lo)
-    __shared__ float fsum_all[kNearWarps * 8];
+    __shared__ float fsum_all[kNearWarps * kFsum];
     double2* tsl = tslot + warp * 4;
     float4* tsf = tslot_ff + warp * 4;
-    float* fsw = fsum_all + warp * 8;
+    float* fsw = fsum_all + warp * kFsum;
     const float x32 = prm.x32;
     const float cutf = (float)prm.cutoffsq;
     const float pf32 = (float)prm.pf;
@@ -373,8 +379,9 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, unsigned 
     const double inv4pi = 1.0 / (4.0 * FTE_PI);
     const float xi2f = (float)prm.xi2;
 
-    const int t0 = prm.tar_off[b];
-    const int nt = prm.tar_off[b + 1] - t0;
+    const int tb0 = prm.tar_off[b], ntb = prm.tar_off[b + 1] - tb0;
+    const int t0 = tb0 + (int)((long long)ntb * part / nparts);
+    const int nt = tb0 + (int)((long long)ntb * (part + 1) / nparts) - t0;
     if (nt == 0) return;
     const int bx = b % prm.nsx, by = b / prm.nsx;
     __syncthreads();  // the previous box is done with the staging buffers
@@ -1061,13 +1068,14 @@ __device__ __forceinline__ void near_load_tables(unsigned char* smem_raw) {
 
 // one problem: grid-stride over its boxes
 template <int KIND, int NV, bool FF>
-__global__ void __launch_bounds__(NearCfg<FF>::threads, NearCfg<FF>::ctas) k_near(const NearParams prm) {
+__global__ void __launch_bounds__(NearCfg<FF>::threads, NearCfg<FF>::ctas) k_near(const NearParams prm,
+                                                                                   int nparts) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int nb_box[9], nb_start[10];
     __shared__ double nb_shx[9], nb_shy[9];
     near_load_tables<KIND, NV, FF>(smem_raw);
-    for (int b = blockIdx.x; b < prm.nb; b += gridDim.x)
-        near_box<KIND, NV, FF>(prm, b, smem_raw, nb_box, nb_start, nb_shx, nb_shy);
+    for (int u = blockIdx.x; u < prm.nb * nparts; u += gridDim.x)
+        near_box<KIND, NV, FF>(prm, u / nparts, u % nparts, nparts, smem_raw, nb_box, nb_start, nb_shx, nb_shy);
 }
 
 // many problems: grid-stride over a (problem, box) work list; descriptions
@@ -1085,7 +1093,7 @@ __global__ void __launch_bounds__(NearCfg<FF>::threads, NearCfg<FF>::ctas) k_nea
         const int2 w = items[it];
         // read in place (a register copy of the description would spill)
         const NearParams& prm = *reinterpret_cast<const NearParams*>(plist + (size_t)w.x * kParamStride);
-        near_box<KIND, NV, FF>(prm, w.y, smem_raw, nb_box, nb_start, nb_shx, nb_shy);
+        near_box<KIND, NV, FF>(prm, w.y, 0, 1, smem_raw, nb_box, nb_start, nb_shx, nb_shy);
     }
 }
 
@@ -1254,18 +1262,31 @@ int near_launch_one(fte_context* ctx, NearParams p) {
     const bool ff = p.ffnear != 0;
     p.cap = near_cap<KIND, NV>(ctx, ff);
     size_t smem = NearSmem<KIND, NV>::bytes(p.cap, ff);
+    // boxes fewer than the CTAs the GPU holds at once: their targets split
+    // over up to 8 CTAs each (each stages the neighbourhood again)
+    auto parts = [&](int ctas) {
+        const long long slots = (long long)ctx->num_sms * ctas;
+        const long long q = p.nb > 0 ? (slots + p.nb - 1) / p.nb : 1;
+        return (int)(q < 1 ? 1 : (q > 8 ? 8 : q));
+    };
     if (ff) {
         using C = NearCfg<true>;
-        const int grid = p.nb < ctx->num_sms * C::grid_per_sm ? (p.nb > 0 ? p.nb : 1) : ctx->num_sms * C::grid_per_sm;
+        const int np = parts(C::ctas);
+        const long long units = (long long)p.nb * np;
+        const int grid = units < ctx->num_sms * C::grid_per_sm ? (units > 0 ? (int)units : 1)
+                                                                : ctx->num_sms * C::grid_per_sm;
         FTE_CUDA_TRY(
             fte_smem_ceiling(k_near<KIND, NV, true>, (int)smem));
-        FTE_LAUNCH(ctx, (k_near<KIND, NV, true>), grid, C::threads, smem, p);
+        FTE_LAUNCH(ctx, (k_near<KIND, NV, true>), grid, C::threads, smem, p, np);
     } else {
         using C = NearCfg<false>;
-        const int grid = p.nb < ctx->num_sms * C::grid_per_sm ? (p.nb > 0 ? p.nb : 1) : ctx->num_sms * C::grid_per_sm;
+        const int np = parts(C::ctas);
+        const long long units = (long long)p.nb * np;
+        const int grid = units < ctx->num_sms * C::grid_per_sm ? (units > 0 ? (int)units : 1)
+                                                                : ctx->num_sms * C::grid_per_sm;
         FTE_CUDA_TRY(
             fte_smem_ceiling(k_near<KIND, NV, false>, (int)smem));
-        FTE_LAUNCH(ctx, (k_near<KIND, NV, false>), grid, C::threads, smem, p);
+        FTE_LAUNCH(ctx, (k_near<KIND, NV, false>), grid, C::threads, smem, p, np);
     }
     return FTE_OK;
 }
