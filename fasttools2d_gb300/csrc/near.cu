@@ -380,8 +380,11 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, int part,
     const float xi2f = (float)prm.xi2;
 
     const int tb0 = prm.tar_off[b], ntb = prm.tar_off[b + 1] - tb0;
-    const int t0 = tb0 + (int)((long long)ntb * part / nparts);
-    const int nt = tb0 + (int)((long long)ntb * (part + 1) / nparts) - t0;
+    int t0 = tb0, nt = ntb;
+    if (nparts > 1) {
+        t0 = tb0 + (int)((long long)ntb * part / nparts);
+        nt = tb0 + (int)((long long)ntb * (part + 1) / nparts) - t0;
+    }
     if (nt == 0) return;
     const int bx = b % prm.nsx, by = b / prm.nsx;
     __syncthreads();  // the previous box is done with the staging buffers
@@ -1074,8 +1077,10 @@ __global__ void __launch_bounds__(NearCfg<FF>::threads, NearCfg<FF>::ctas) k_nea
     __shared__ int nb_box[9], nb_start[10];
     __shared__ double nb_shx[9], nb_shy[9];
     near_load_tables<KIND, NV, FF>(smem_raw);
-    for (int u = blockIdx.x; u < prm.nb * nparts; u += gridDim.x)
-        near_box<KIND, NV, FF>(prm, u / nparts, u % nparts, nparts, smem_raw, nb_box, nb_start, nb_shx, nb_shy);
+    for (int u = blockIdx.x; u < prm.nb * nparts; u += gridDim.x) {
+        const int b = nparts > 1 ? u / nparts : u, part = nparts > 1 ? u % nparts : 0;
+        near_box<KIND, NV, FF>(prm, b, part, nparts, smem_raw, nb_box, nb_start, nb_shx, nb_shy);
+    }
 }
 
 // many problems: grid-stride over a (problem, box) work list; descriptions
