@@ -2376,8 +2376,10 @@ int fte_kspace_run(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, fte_info
 // inverse transforms and the gather each run as one launch over every item's
 // blocks (a block reads its item's parameters from a device array; transforms
 // are grouped by line length so that a short line's block does not carry a
-// long line's shared memory).  The arithmetic is the per-call kernels' own
-// (the same device functions), so results match the per-plan path.
+// long line's shared memory, spread and gather items by the CTAs per SM their
+// tile allows and the gather's by window support).  The arithmetic is the
+// per-call kernels' own (the same device functions), so results match the
+// per-plan path.
 // ===========================================================================
 namespace {
 

@@ -213,11 +213,13 @@ int fte_plan_destroy(fte_plan* plan);
 /* No counterpart in the reference.  A batch binds plans of one context (any
  * sizes, both kinds) and nv density vectors each to device buffers
  * (fte_batch_buffers: plan i's f1s, f2s, u1s, u2s, laid out as in
- * fte_plan_execute).  fte_batch_launch evaluates all of them: one persistent
- * real-space launch per kind over every plan's cells, the k-space parts on
- * forked streams; with use_graph = 1 it replays the CUDA graph captured at
- * creation (one graph launch per step of an iterative solver).  Asynchronous
- * on the context's stream. */
+ * fte_plan_execute).  fte_batch_launch evaluates all of them, every stage as
+ * one launch over a work list of all plans: densities, the real-space sum
+ * (per kind, over every plan's cells), and the float-float k-space stages of
+ * every (plan, vector) (plans with another k-space form run theirs on forked
+ * streams beside them); with use_graph = 1 it replays the CUDA graph captured
+ * at creation (one graph launch per step of an iterative solver).
+ * Asynchronous on the context's stream. */
 typedef struct fte_batch fte_batch;
 int fte_batch_create(fte_context* ctx, fte_plan* const* plans, int nplans, int nv, fte_batch** batch);
 int fte_batch_buffers(const fte_batch* batch, int i, double** f1s, double** f2s, double** u1s, double** u2s);
