@@ -458,12 +458,15 @@ def batched_section(ft, wl, ctx, stream, steps, warmup, flush):
     lib = ft.lib()
 
     def e2e_step():
+        # pinned host buffers: the copies are queued without a synchronisation
+        # each; the step ends when the stream has delivered every velocity
         for i in range(len(plans)):
-            batch.set_density(i, hf[i][0].numpy(), hf[i][1].numpy())
+            batch.set_density(i, hf[i][0].numpy(), hf[i][1].numpy(), pinned_async=True)
         batch.launch(True)
         for i in range(len(plans)):
             ft._check(lib.fte_batch_get_velocity(batch.h, i, C.c_void_p(hu[i].data_ptr()),
-                                                 C.c_void_p(hu2[i].data_ptr()), 0))
+                                                 C.c_void_p(hu2[i].data_ptr()), ft.FTE_HOST_ASYNC))
+        stream.synchronize()
 
     e2e_step()
     torch.cuda.synchronize()

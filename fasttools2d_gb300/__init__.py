@@ -35,6 +35,7 @@ FTE_ERR_ALLOC = 3
 FTE_ERR_UNSUPPORTED = 4
 FTE_ERR_DEVICE = 5
 FTE_DEVICE_POINTERS = 1
+FTE_HOST_ASYNC = 2
 FORM_PLAIN = 0
 FORM_MIXED = 1
 FORM_FF = 2  # fte_params.form only: float-float spread and gather
@@ -535,11 +536,20 @@ class Batch:
         _check(lib().fte_batch_create(self.ctx.h, arr, len(self.plans), self.nv, C.byref(h)))
         self.h = h
 
-    def set_density(self, i, f1s, f2s):
+    def set_density(self, i, f1s, f2s, pinned_async=False):
+        """Copy plan i's density vectors in.  pinned_async: f1s, f2s are
+        page-locked host arrays; the copy is queued without synchronising
+        (synchronise the context's stream before reusing them)."""
+        if pinned_async and not _is_cuda_tensor(f1s):
+            # the copy outlives the call: no temporary conversions allowed
+            for a in (f1s, f2s):
+                if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.flags.c_contiguous):
+                    raise ValueError("pinned_async needs contiguous float64 numpy arrays (page-locked)")
         A = _Args()
         pf1, _ = A.arr(f1s, 1)
         pf2, _ = A.arr(f2s, 1)
-        _check(lib().fte_batch_set_density(self.h, int(i), pf1, pf2, A.flags))
+        flags = A.flags | (FTE_HOST_ASYNC if pinned_async and not (A.flags & FTE_DEVICE_POINTERS) else 0)
+        _check(lib().fte_batch_set_density(self.h, int(i), pf1, pf2, flags))
 
     def launch(self, use_graph: bool = True):
         _check(lib().fte_batch_launch(self.h, 1 if use_graph else 0))

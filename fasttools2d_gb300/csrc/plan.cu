@@ -1017,7 +1017,7 @@ extern "C" int fte_batch_set_density(fte_batch* b, int i, const double* f1s, con
         FTE_CUDA_TRY(cudaMemcpyAsync(b->f1[i], f1s, bytes, k, c->stream));
         FTE_CUDA_TRY(cudaMemcpyAsync(b->f2[i], f2s, bytes, k, c->stream));
     }
-    if (!(flags & FTE_DEVICE_POINTERS)) FTE_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    if (!(flags & (FTE_DEVICE_POINTERS | FTE_HOST_ASYNC))) FTE_CUDA_TRY(cudaStreamSynchronize(c->stream));
     return FTE_OK;
 }
 
@@ -1034,6 +1034,6 @@ extern "C" int fte_batch_get_velocity(fte_batch* b, int i, double* u1s, double* 
         FTE_CUDA_TRY(cudaMemcpyAsync(u1s, b->u1[i], bytes, k, c->stream));
         FTE_CUDA_TRY(cudaMemcpyAsync(u2s, b->u2[i], bytes, k, c->stream));
     }
-    if (!(flags & FTE_DEVICE_POINTERS)) FTE_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    if (!(flags & (FTE_DEVICE_POINTERS | FTE_HOST_ASYNC))) FTE_CUDA_TRY(cudaStreamSynchronize(c->stream));
     return FTE_OK;
 }

@@ -53,6 +53,12 @@ extern "C" {
 
 /* flags */
 #define FTE_DEVICE_POINTERS 1u /* all array arguments are device pointers */
+/* fte_batch_set_density / fte_batch_get_velocity: the host arrays are
+ * page-locked (pinned); the copies are queued on the context's stream and the
+ * call returns without synchronising -- the caller synchronises the stream
+ * before reusing the density arrays or reading the velocities.  Many plans'
+ * copies then cost one synchronisation instead of one each. */
+#define FTE_HOST_ASYNC 2u
 
 /* arithmetic forms */
 /* fte_options.form: FTE_FORM_PLAIN = the drivers' parameters, FP64
@@ -226,7 +232,8 @@ int fte_batch_buffers(const fte_batch* batch, int i, double** f1s, double** f2s,
 int fte_batch_launch(fte_batch* batch, int use_graph);
 int fte_batch_destroy(fte_batch* batch);
 /* copy plan i's nv density vectors in / velocities out (host or, with
- * FTE_DEVICE_POINTERS, device arrays; host copies synchronise) */
+ * FTE_DEVICE_POINTERS, device arrays; host copies synchronise unless
+ * FTE_HOST_ASYNC) */
 int fte_batch_set_density(fte_batch* batch, int i, const double* f1s, const double* f2s, unsigned flags);
 int fte_batch_get_velocity(fte_batch* batch, int i, double* u1s, double* u2s, unsigned flags);
 

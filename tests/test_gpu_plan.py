@@ -253,3 +253,44 @@ def test_batch_work_lists_match_plans_in_few_launches(gpu_ctx):
     batch.close()
     for p in plans:
         p.close()
+
+
+def test_batch_pinned_async_copies_match_synchronous(gpu_ctx):
+    """Densities in and velocities out through page-locked host buffers with
+    FTE_HOST_ASYNC (one stream synchronisation for all plans) give what the
+    synchronising copies give."""
+    import ctypes as C
+
+    import torch
+
+    ft = _ft()
+    nv = 2
+    plans, dens = [], []
+    for i, (n, Lx, Ly) in enumerate([(3000, 1.0, 1.0), (5000, 2.0, 1.0), (2500, 1.0, 0.75)]):
+        g = _geom(700 + i, n, Lx, Ly)
+        f1s, f2s = _dens(750 + i, nv, n)
+        plans.append(ft.Plan(i % 2, *g[:4], f1s[0], f2s[0], Lx, Ly, n1=g[4], n2=g[5], tol=1e-8, form=ft.FORM_MIXED,
+                             nvmax=nv, ctx=gpu_ctx))
+        dens.append((f1s, f2s))
+    batch = ft.Batch(plans, nv, ctx=gpu_ctx)
+    for i, (f1s, f2s) in enumerate(dens):
+        batch.set_density(i, f1s, f2s)
+    batch.launch(False)
+    want = [batch.velocity(i) for i in range(len(plans))]
+    pin_in = [(torch.tensor(np.ascontiguousarray(f1s)).pin_memory(), torch.tensor(np.ascontiguousarray(f2s)).pin_memory())
+              for f1s, f2s in dens]
+    pin_out = [(torch.zeros((nv, p.ntar), dtype=torch.float64).pin_memory(),
+                torch.zeros((nv, p.ntar), dtype=torch.float64).pin_memory()) for p in plans]
+    for i, (a, b) in enumerate(pin_in):
+        batch.set_density(i, a.numpy(), b.numpy(), pinned_async=True)
+    batch.launch(True)
+    lib = ft.lib()
+    for i, (u1, u2) in enumerate(pin_out):
+        ft._check(lib.fte_batch_get_velocity(batch.h, i, C.c_void_p(u1.data_ptr()), C.c_void_p(u2.data_ptr()),
+                                             ft.FTE_HOST_ASYNC))
+    torch.cuda.synchronize()
+    for i, (u1, u2) in enumerate(pin_out):
+        assert rel_max(np.stack([u1.numpy(), u2.numpy()]), np.stack(want[i])) <= 1e-12, i
+    batch.close()
+    for p in plans:
+        p.close()
