@@ -501,7 +501,7 @@ def batched_section(ft, wl, ctx, stream, steps, warmup, flush):
         "setup_s": setup_s, "gpu_launches_per_step": launches,
         "max_rel_diff_vs_plain_loop": worst,
         "distinct_tile_pairs": len(tiles),
-        "kspace_forms": {{ft.FORM_MIXED: "fp32", ft.FORM_FF: "float-float"}.get(k, "fp64"): v
+        "kspace_forms": {{ft.FORM_MIXED: "fp32", ft.FORM_FF: "float-float", ft.FORM_FF32: "float-float/fp32"}.get(k, "fp64"): v
                          for k, v in forms.items()},
         "e2e": {"targets_per_s": targets_per_step / (e2e_ms / 1e3), "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},

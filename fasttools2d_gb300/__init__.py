@@ -39,7 +39,8 @@ FTE_HOST_ASYNC = 2
 FORM_PLAIN = 0
 FORM_MIXED = 1
 FORM_FF = 2  # fte_params.form only: float-float spread and gather
-KSPACE_AUTO, KSPACE_FP64, KSPACE_FP32, KSPACE_FF = 0, 1, 2, 3
+FORM_FF32 = 3  # fte_params.form only: float-float transforms, FP32 spread and gather products
+KSPACE_AUTO, KSPACE_FP64, KSPACE_FP32, KSPACE_FF, KSPACE_FF32 = 0, 1, 2, 3, 4
 NEAR_AUTO, NEAR_FP64, NEAR_FF = 0, 1, 2
 KIND_SLP = 0
 KIND_DLP = 1

@@ -882,6 +882,7 @@ static const double kCostBox = 28e-9;          // per box of the cell list
 static const double kCostWin64 = 3.2e-12;      // one window node x grid, FP64 spread/gather
 static const double kCostWin32 = 2.5e-12;      // same in FP32 (an exponential per node)
 static const double kCostWinFF = 1.31e-12;     // same in float-float (FP32 pipe), window records included
+static const double kCostWinFS = 0.83e-12;     // same with FP32 products and compensated sums (FTE_FORM_FF32)
 static const double kCostGridFF = 16e-12;      // float-float: per grid node x grid (tile staging, flushes)
 static const double kCostFft64 = 9e-12;        // per unit of fft_work, 7-smooth FP64 block transforms
 static const double kCostFftFF = 2.3e-12;      // same in float-float (filter included)
@@ -900,6 +901,8 @@ static const double kTolSlack[2] = {1.0, 3.0};
 // taken at the tolerance times this factor (the grid grows ~4 % per side).
 static const double kKinfSlack[2] = {0.1, 1.0};
 static const double kWinRatio[2] = {3000.0, 300.0};
+// (also the floor of FTE_FORM_FF32: its FP32 products left 1.6e-7 / 1.6e-8
+// at 1e6 uniform points on the parameters of tol 1e-11)
 static const double kFp32Floor[2] = {1e-6, 2e-7};
 // float-float spread and gather (~48-bit values) hold their ~1e-13 relative
 // error well below tolerances from 1e-11 up
@@ -912,7 +915,7 @@ static int choose_params_tuned(int kind, int64_t nsrc, int64_t ntar, double Q, d
     const double tol = o->tol;
     const double tol_e = tol * (opt && opt->slack > 0 ? opt->slack : kTolSlack[kind]);
     const int force = opt ? opt->kspace : FTE_KSPACE_AUTO;
-    if (force < FTE_KSPACE_AUTO || force > FTE_KSPACE_FF) {
+    if (force < FTE_KSPACE_AUTO || force > FTE_KSPACE_FF32) {
         fte_set_error("unknown k-space arithmetic %d", force);
         return FTE_ERR_INVALID;
     }
@@ -1007,18 +1010,24 @@ static int choose_params_tuned(int kind, int64_t nsrc, int64_t ntar, double Q, d
                             kCostBox * (double)nsx * (double)nsy;
         int kf = -1;
         double cost = 1e300;
-        for (int f : {FTE_FORM_MIXED, FTE_FORM_FF, FTE_FORM_PLAIN}) {
-            const bool allowed = force == FTE_KSPACE_AUTO
-                                     ? (f == FTE_FORM_MIXED ? fp32 && fits32 : (f == FTE_FORM_FF ? ffok : true))
-                                     : (force == FTE_KSPACE_FP32 ? f == FTE_FORM_MIXED && fits32
-                                                                 : f == (force == FTE_KSPACE_FF ? FTE_FORM_FF
-                                                                                                : FTE_FORM_PLAIN));
+        for (int f : {FTE_FORM_MIXED, FTE_FORM_FF32, FTE_FORM_FF, FTE_FORM_PLAIN}) {
+            bool allowed;
+            if (force == FTE_KSPACE_AUTO)
+                allowed = f == FTE_FORM_MIXED ? fp32 && fits32
+                                              : (f == FTE_FORM_FF32 ? fp32 && ffok : (f == FTE_FORM_FF ? ffok : true));
+            else if (force == FTE_KSPACE_FP32)
+                allowed = f == FTE_FORM_MIXED && fits32;
+            else
+                allowed = f == (force == FTE_KSPACE_FF     ? FTE_FORM_FF
+                                : force == FTE_KSPACE_FF32 ? FTE_FORM_FF32
+                                                           : FTE_FORM_PLAIN);
             if (!allowed) continue;
             double c;
             if (f == FTE_FORM_MIXED)
                 c = kCostWin32 * win + kCostFft32 * fftw;
-            else if (f == FTE_FORM_FF)
-                c = kCostWinFF * winff + kCostGridFF * (double)Mx * My * (kind == FTE_KIND_SLP ? 4 : 5) +
+            else if (fte_form_ff(f))
+                c = (f == FTE_FORM_FF32 ? kCostWinFS : kCostWinFF) * winff +
+                    kCostGridFF * (double)Mx * My * (kind == FTE_KIND_SLP ? 4 : 5) +
                     (long64 ? 2.5 * kCostFft64 : kCostFftFF) * fftwff;
             else
                 c = kCostWin64 * win + (long64 ? 2.5 : 1.0) * kCostFft64 * fftw;

@@ -61,6 +61,17 @@ __device__ __forceinline__ void ff_mac(float2 a, float2 b, float& s, float& c) {
     s = t;
     c = __fadd_rn(c, __fadd_rn(err, e));
 }
+// (s, c) += a b for FP32 a, b with Kahan's compensated summation (Kahan
+// 1965, "Further remarks on reducing truncation errors"): the product rounded
+// once together with the carried compensation, s + c the running sum; the
+// sum's error stays near one rounding of the total while each product keeps
+// its own FP32 rounding
+__device__ __forceinline__ void fs_mac(float a, float b, float& s, float& c) {
+    const float y = __fmaf_rn(a, b, c);
+    const float t = __fadd_rn(s, y);
+    c = __fadd_rn(__fsub_rn(s, t), y);
+    s = t;
+}
 // (s, c) += a
 __device__ __forceinline__ void ff_acc(float2 a, float& s, float& c) {
     const float t = __fadd_rn(s, a.x);

@@ -10,6 +10,9 @@
 
 #include "../../include/fasttools2d.h"
 
+// the k-space forms with float-float window factors and transforms
+__host__ __device__ inline bool fte_form_ff(int form) { return form == FTE_FORM_FF || form == FTE_FORM_FF32; }
+
 #define FTE_PI 3.14159265358979323846
 #define FTE_EULER 0.57721566490153286060651209008240243
 

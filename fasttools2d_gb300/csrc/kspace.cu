@@ -1467,8 +1467,13 @@ __global__ void k_ff_win(int kind, const double* __restrict__ p, const double* _
 // (stresslet: the symmetric products f1 n1, f1 n2 + f2 n1, f2 n2 -- the
 // stresslet multiplier sees the two mixed products only through their sum).
 // tiles tile0, tile0 + tstep, ... of one grid (the kernels below: a grid-
-// stride loop over one evaluation's tiles, or one tile of a work list)
-template <int NG>
+// stride loop over one evaluation's tiles, or one tile of a work list).
+// C32 (FTE_FORM_FF32, loose tolerances): the window factors as above, but
+// the products in FP32 (high parts of the float-float rows and columns) and
+// the region's sums Kahan-compensated (fs_mac): four FP32 operations per node
+// and grid instead of eleven; the region keeps its (sum, compensation) pairs
+// and is flushed as for float-float.
+template <int NG, bool C32 = false>
 __device__ __forceinline__ void spread_ff_run(const FfWin* __restrict__ recs, const int* __restrict__ toff, int ts,
                                               int ntx, int nty, const WinParams& wp, double* __restrict__ H0,
                                               double* __restrict__ H1, double* __restrict__ H2, int tile0, int tstep,
@@ -1481,6 +1486,10 @@ __device__ __forceinline__ void spread_ff_run(const FfWin* __restrict__ recs, co
     float2* buf2 = wy + kColChunk * P1;                            // NG == 3: WW (grid 2 sum, low)
     float2* fw2 = buf2 + (NG == 3 ? WW : 0);                       // NG == 3: kColChunk * P1 (q2 wx)
     int* org = reinterpret_cast<int*>(fw2 + (NG == 3 ? kColChunk * P1 : 0));  // kColChunk * 2 (lx, ly)
+    // C32: the same arrays hold FP32 values (q0 wx, q1 wx pairs; wy; q2 wx)
+    float2* fwc = reinterpret_cast<float2*>(fw);
+    float* wyc = reinterpret_cast<float*>(wy);
+    float* fw2c = reinterpret_cast<float*>(fw2);
     load_e1_ff(e1, wp);
     const float2* e1y = e1y_of(e1, wp);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1509,7 +1518,11 @@ __device__ __forceinline__ void spread_ff_run(const FfWin* __restrict__ recs, co
                         const float2 e3 = r.ey3;
                         float2 ey = ff_powi(e3, j0);
                         for (int j = j0; j < j1; j++) {
-                            wy[lane * P1 + j] = ff_mul(e1y[j], ey);
+                            const float2 w = ff_mul(e1y[j], ey);
+                            if constexpr (C32)
+                                wyc[lane * P1 + j] = w.x;
+                            else
+                                wy[lane * P1 + j] = w;
                             ey = ff_mul(ey, e3);
                         }
                         if (seg == 0) {
@@ -1523,50 +1536,89 @@ __device__ __forceinline__ void spread_ff_run(const FfWin* __restrict__ recs, co
                         for (int a = j0; a < j1; a++) {
                             const float2 wxa = ff_mul(ex, e1[a]);
                             const float2 u = ff_mul(q0, wxa), v = ff_mul(q1, wxa);
-                            fa[a] = make_float4(u.x, u.y, v.x, v.y);
-                            if constexpr (NG == 3) fw2[lane * P1 + a] = ff_mul(q2, wxa);
+                            if constexpr (C32) {
+                                fwc[lane * P1 + a] = make_float2(u.x, v.x);
+                                if constexpr (NG == 3) fw2c[lane * P1 + a] = ff_mul(q2, wxa).x;
+                            } else {
+                                fa[a] = make_float4(u.x, u.y, v.x, v.y);
+                                if constexpr (NG == 3) fw2[lane * P1 + a] = ff_mul(q2, wxa);
+                            }
                             ex = ff_mul(ex, e3);
                         }
                     }
                 }
             }
             __syncthreads();
-            if (lane < P1) {
+            // supports of at most 16 nodes: the warp's two halves take
+            // alternate owned columns of a window (row j = lane mod 16), one
+            // pass per two columns instead of half the lanes idle
+            const bool split = P1 <= 16;
+            const int j = split ? (lane & 15) : lane;
+            const int cstep = split ? 2 * nw : nw;
+            if (j < P1) {
                 for (int s = 0; s < cn; s++) {
                     const int2 o = *reinterpret_cast<const int2*>(org + 2 * s);
                     const int lx = o.x, ly = o.y;
-                    const float2 wyj = wy[s * P1 + lane];
+                    const float2 wyj = C32 ? make_float2(wyc[s * P1 + j], 0.f) : wy[s * P1 + j];
                     const float4* fa = fw + s * P1;
                     const float2* fa2 = fw2 + s * P1;
-                    // first column >= lx owned by this warp
-                    int c = lx + ((warp - lx) & (nw - 1));
+                    const float2* fac = fwc + s * P1;
+                    const float* fa2c = fw2c + s * P1;
+                    // first column >= lx owned by this warp (by this half)
+                    int c = lx + ((warp - lx) & (nw - 1)) + (split ? (lane >> 4) * nw : 0);
                     if (lx >= 0 && ly >= 0 && lx + wp.P < W && ly + wp.P < W) {
-                        float4* b = buf + ly + lane;
-                        float2* b2 = buf2 + ly + lane;
-                        for (; c <= lx + wp.P; c += nw) {
-                            const float4 f = fa[c - lx];
-                            float4 v = b[c * W];
-                            ff_mac(make_float2(f.x, f.y), wyj, v.x, v.y);
-                            ff_mac(make_float2(f.z, f.w), wyj, v.z, v.w);
-                            b[c * W] = v;
-                            if constexpr (NG == 3) {
-                                float2 v2 = b2[c * W];
-                                ff_mac(fa2[c - lx], wyj, v2.x, v2.y);
-                                b2[c * W] = v2;
+                        float4* b = buf + ly + j;
+                        float2* b2 = buf2 + ly + j;
+                        if constexpr (C32) {
+                            for (; c <= lx + wp.P; c += cstep) {
+                                const float2 f = fac[c - lx];
+                                float4 v = b[c * W];
+                                fs_mac(f.x, wyj.x, v.x, v.y);
+                                fs_mac(f.y, wyj.x, v.z, v.w);
+                                b[c * W] = v;
+                                if constexpr (NG == 3) {
+                                    float2 v2 = b2[c * W];
+                                    fs_mac(fa2c[c - lx], wyj.x, v2.x, v2.y);
+                                    b2[c * W] = v2;
+                                }
+                            }
+                        } else {
+                            for (; c <= lx + wp.P; c += cstep) {
+                                const float4 f = fa[c - lx];
+                                float4 v = b[c * W];
+                                ff_mac(make_float2(f.x, f.y), wyj, v.x, v.y);
+                                ff_mac(make_float2(f.z, f.w), wyj, v.z, v.w);
+                                b[c * W] = v;
+                                if constexpr (NG == 3) {
+                                    float2 v2 = b2[c * W];
+                                    ff_mac(fa2[c - lx], wyj, v2.x, v2.y);
+                                    b2[c * W] = v2;
+                                }
                             }
                         }
                     } else {
                         // window outside the region: straight into the global grids
-                        const size_t row = fte_wrap_index(oy + ly + lane, wp.My);
-                        for (; c <= lx + wp.P; c += nw) {
-                            const size_t at = (size_t)fte_wrap_index(ox + c, wp.Mx) * wp.My + row;
-                            const float4 f = fa[c - lx];
-                            const float2 p0 = ff_mul(make_float2(f.x, f.y), wyj), p1 = ff_mul(make_float2(f.z, f.w), wyj);
-                            atomicAdd(&H0[at], ff_join(p0.x, p0.y));
-                            atomicAdd(&H1[at], ff_join(p1.x, p1.y));
-                            if constexpr (NG == 3) {
-                                const float2 p2 = ff_mul(fa2[c - lx], wyj);
-                                atomicAdd(&H2[at], ff_join(p2.x, p2.y));
+                        const size_t row = fte_wrap_index(oy + ly + j, wp.My);
+                        if constexpr (C32) {
+                            for (; c <= lx + wp.P; c += cstep) {
+                                const size_t at = (size_t)fte_wrap_index(ox + c, wp.Mx) * wp.My + row;
+                                const float2 f = fac[c - lx];
+                                atomicAdd(&H0[at], (double)__fmul_rn(f.x, wyj.x));
+                                atomicAdd(&H1[at], (double)__fmul_rn(f.y, wyj.x));
+                                if constexpr (NG == 3) atomicAdd(&H2[at], (double)__fmul_rn(fa2c[c - lx], wyj.x));
+                            }
+                        } else {
+                            for (; c <= lx + wp.P; c += cstep) {
+                                const size_t at = (size_t)fte_wrap_index(ox + c, wp.Mx) * wp.My + row;
+                                const float4 f = fa[c - lx];
+                                const float2 p0 = ff_mul(make_float2(f.x, f.y), wyj);
+                                const float2 p1 = ff_mul(make_float2(f.z, f.w), wyj);
+                                atomicAdd(&H0[at], ff_join(p0.x, p0.y));
+                                atomicAdd(&H1[at], ff_join(p1.x, p1.y));
+                                if constexpr (NG == 3) {
+                                    const float2 p2 = ff_mul(fa2[c - lx], wyj);
+                                    atomicAdd(&H2[at], ff_join(p2.x, p2.y));
+                                }
                             }
                         }
                     }
@@ -1594,13 +1646,13 @@ __device__ __forceinline__ void spread_ff_run(const FfWin* __restrict__ recs, co
     }
 }
 
-template <int NG>
+template <int NG, bool C32>
 __global__ void __launch_bounds__(kColThreads) k_spread_ff(const FfWin* __restrict__ recs,
                                                           const int* __restrict__ toff, int ts, int ntx, int nty,
                                                           WinParams wp, double* __restrict__ H0,
                                                           double* __restrict__ H1, double* __restrict__ H2) {
     extern __shared__ __align__(16) unsigned char shraw[];
-    spread_ff_run<NG>(recs, toff, ts, ntx, nty, wp, H0, H1, H2, blockIdx.x, gridDim.x, shraw);
+    spread_ff_run<NG, C32>(recs, toff, ts, ntx, nty, wp, H0, H1, H2, blockIdx.x, gridDim.x, shraw);
 }
 
 size_t spread_ff_smem(int ts, int P, int ng, int aniso = 0) {
@@ -1633,8 +1685,11 @@ __global__ void k_ff_join(double* __restrict__ H, int64_t n) {
 // supports of at most PM nodes, the target's window column held in registers
 // and the node loops unrolled to PM (independent products in flight, no
 // shared-memory traffic for the weights); PM == 0: any support, the window
-// column in a per-thread shared-memory row.
-template <int PM>
+// column in a per-thread shared-memory row.  C32 (FTE_FORM_FF32, loose
+// tolerances): the region holds the grids' high parts only (FP32), each
+// window column is summed with FP32 FMAs and the column sums are added with
+// Kahan's compensation (fs_mac); the window factors are the float-float ones.
+template <int PM, bool C32 = false>
 __device__ __forceinline__ void gather_ff_run(const double* __restrict__ p, const int* __restrict__ toff,
                                               const int* __restrict__ perm, int ts, int ntx, int nty,
                                               const WinParams& wp, const float2* __restrict__ G0,
@@ -1646,10 +1701,15 @@ __device__ __forceinline__ void gather_ff_run(const double* __restrict__ p, cons
     float2* r1 = r0 + WW;
     float2* e1 = r1 + WW;
     float2* wyb = e1 + e1_len(wp.P, wp.aniso) + threadIdx.x * P1;  // PM == 0 only
+    // C32: FP32 regions and window rows in the same space
+    float* r0f = reinterpret_cast<float*>(shf);
+    float* r1f = r0f + WW;
+    float* wybf = reinterpret_cast<float*>(e1 + e1_len(wp.P, wp.aniso)) + threadIdx.x * P1;
     load_etab(etab);  // 2^(-j/64) for the window factors (as in k_ff_win)
     load_e1_ff(e1, wp);
     const float2* e1y = e1y_of(e1, wp);
     const double tw = -2 * wp.xi * wp.xi / wp.eta;
+    constexpr int NW = PM > 0 ? PM : 1;
     for (int tile = tile0; tile < ntx * nty; tile += tstep) {
         const int k0 = toff[tile], k1 = toff[tile + 1];
         if (k0 == k1) continue;
@@ -1658,8 +1718,13 @@ __device__ __forceinline__ void gather_ff_run(const double* __restrict__ p, cons
         for (int idx = threadIdx.x; idx < WW; idx += blockDim.x) {
             int xx = idx / W, yy = idx - xx * W;
             size_t at = (size_t)fte_wrap_index(ox + xx, wp.Mx) * wp.My + fte_wrap_index(oy + yy, wp.My);
-            r0[idx] = G0[at];
-            r1[idx] = G1[at];
+            if constexpr (C32) {
+                r0f[idx] = G0[at].x;
+                r1f[idx] = G1[at].x;
+            } else {
+                r0[idx] = G0[at];
+                r1[idx] = G1[at];
+            }
         }
         __syncthreads();
         for (int k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
@@ -1668,19 +1733,28 @@ __device__ __forceinline__ void gather_ff_run(const double* __restrict__ p, cons
             double px, py;
             fte_closest_node(p[2 * i], p[2 * i + 1], wp.Lx, wp.Ly, wp.h, wp.rh, wp.hy, wp.rhy, wp.P, &mx, &my, &px,
                              &py);
-            float2 wy[PM > 0 ? PM : 1];
+            float2 wy[C32 ? 1 : NW];
+            float wyf[C32 ? NW : 1];
             {
                 const float2 e3 = fte_expm_ff(ff_split(2 * tw * wp.hy * py), etab);
                 float2 ey = make_float2(1.f, 0.f);
                 if constexpr (PM > 0) {
 #pragma unroll
                     for (int j = 0; j < PM; j++) {
-                        wy[j] = j < P1 ? ff_mul(e1y[j], ey) : make_float2(0.f, 0.f);
+                        const float2 w = j < P1 ? ff_mul(e1y[j], ey) : make_float2(0.f, 0.f);
+                        if constexpr (C32)
+                            wyf[j] = w.x;
+                        else
+                            wy[j] = w;
                         ey = ff_mul(ey, e3);
                     }
                 } else {
                     for (int j = 0; j < P1; j++) {
-                        wyb[j] = ff_mul(e1y[j], ey);
+                        const float2 w = ff_mul(e1y[j], ey);
+                        if constexpr (C32)
+                            wybf[j] = w.x;
+                        else
+                            wyb[j] = w;
                         ey = ff_mul(ey, e3);
                     }
                 }
@@ -1693,54 +1767,98 @@ __device__ __forceinline__ void gather_ff_run(const double* __restrict__ p, cons
             for (int a = 0; a < P1; a++) {
                 const float2 wxa = ff_mul(ex, e1[a]);
                 ex = ff_mul(ex, e3x);
-                float s0 = 0.f, t0 = 0.f, s1 = 0.f, t1 = 0.f;
-                if (inside) {
-                    const float2* g0 = r0 + (lx + a) * W + ly;
-                    const float2* g1 = r1 + (lx + a) * W + ly;
-                    if constexpr (PM > 0) {
+                if constexpr (C32) {
+                    float s0 = 0.f, s1 = 0.f;
+                    if (inside) {
+                        const float* g0 = r0f + (lx + a) * W + ly;
+                        const float* g1 = r1f + (lx + a) * W + ly;
+                        if constexpr (PM > 0) {
 #pragma unroll
-                        for (int j = 0; j < PM; j++) {
-                            if (j < P1) {
-                                ff_mac(wy[j], g0[j], s0, t0);
-                                ff_mac(wy[j], g1[j], s1, t1);
+                            for (int j = 0; j < PM; j++) {
+                                if (j < P1) {
+                                    s0 = __fmaf_rn(wyf[j], g0[j], s0);
+                                    s1 = __fmaf_rn(wyf[j], g1[j], s1);
+                                }
+                            }
+                        } else {
+                            for (int j = 0; j < P1; j++) {
+                                const float w = wybf[j];
+                                s0 = __fmaf_rn(w, g0[j], s0);
+                                s1 = __fmaf_rn(w, g1[j], s1);
                             }
                         }
                     } else {
-                        for (int j = 0; j < P1; j++) {
-                            const float2 w = wyb[j];
-                            ff_mac(w, g0[j], s0, t0);
-                            ff_mac(w, g1[j], s1, t1);
-                        }
-                    }
-                } else {
-                    const size_t base = (size_t)fte_wrap_index(mx + a, wp.Mx) * wp.My;
-                    if constexpr (PM > 0) {
+                        const size_t base = (size_t)fte_wrap_index(mx + a, wp.Mx) * wp.My;
+                        if constexpr (PM > 0) {
 #pragma unroll
-                        for (int j = 0; j < PM; j++) {
-                            if (j < P1) {
+                            for (int j = 0; j < PM; j++) {
+                                if (j < P1) {
+                                    const size_t at = base + fte_wrap_index(my + j, wp.My);
+                                    s0 = __fmaf_rn(wyf[j], G0[at].x, s0);
+                                    s1 = __fmaf_rn(wyf[j], G1[at].x, s1);
+                                }
+                            }
+                        } else {
+                            for (int j = 0; j < P1; j++) {
                                 const size_t at = base + fte_wrap_index(my + j, wp.My);
-                                ff_mac(wy[j], G0[at], s0, t0);
-                                ff_mac(wy[j], G1[at], s1, t1);
+                                const float w = wybf[j];
+                                s0 = __fmaf_rn(w, G0[at].x, s0);
+                                s1 = __fmaf_rn(w, G1[at].x, s1);
+                            }
+                        }
+                    }
+                    fs_mac(wxa.x, s0, a0, c0);
+                    fs_mac(wxa.x, s1, a1, c1);
+                } else {
+                    float s0 = 0.f, t0 = 0.f, s1 = 0.f, t1 = 0.f;
+                    if (inside) {
+                        const float2* g0 = r0 + (lx + a) * W + ly;
+                        const float2* g1 = r1 + (lx + a) * W + ly;
+                        if constexpr (PM > 0) {
+#pragma unroll
+                            for (int j = 0; j < PM; j++) {
+                                if (j < P1) {
+                                    ff_mac(wy[j], g0[j], s0, t0);
+                                    ff_mac(wy[j], g1[j], s1, t1);
+                                }
+                            }
+                        } else {
+                            for (int j = 0; j < P1; j++) {
+                                const float2 w = wyb[j];
+                                ff_mac(w, g0[j], s0, t0);
+                                ff_mac(w, g1[j], s1, t1);
                             }
                         }
                     } else {
-                        for (int j = 0; j < P1; j++) {
-                            const size_t at = base + fte_wrap_index(my + j, wp.My);
-                            const float2 w = wyb[j];
-                            ff_mac(w, G0[at], s0, t0);
-                            ff_mac(w, G1[at], s1, t1);
+                        const size_t base = (size_t)fte_wrap_index(mx + a, wp.Mx) * wp.My;
+                        if constexpr (PM > 0) {
+#pragma unroll
+                            for (int j = 0; j < PM; j++) {
+                                if (j < P1) {
+                                    const size_t at = base + fte_wrap_index(my + j, wp.My);
+                                    ff_mac(wy[j], G0[at], s0, t0);
+                                    ff_mac(wy[j], G1[at], s1, t1);
+                                }
+                            }
+                        } else {
+                            for (int j = 0; j < P1; j++) {
+                                const size_t at = base + fte_wrap_index(my + j, wp.My);
+                                const float2 w = wyb[j];
+                                ff_mac(w, G0[at], s0, t0);
+                                ff_mac(w, G1[at], s1, t1);
+                            }
                         }
                     }
+                    ff_mac(wxa, ff_norm(s0, t0), a0, c0);
+                    ff_mac(wxa, ff_norm(s1, t1), a1, c1);
                 }
-                ff_mac(wxa, ff_norm(s0, t0), a0, c0);
-                ff_mac(wxa, ff_norm(s1, t1), a1, c1);
             }
             out[i] = make_double2(ff_join(a0, c0) * scale, ff_join(a1, c1) * scale);
         }
     }
 }
 
-template <int PM>
+template <int PM, bool C32>
 __global__ void __launch_bounds__(kTileThreads, 5) k_gather_ff(const double* __restrict__ p, const int* __restrict__ toff,
                                                            const int* __restrict__ perm, int ts, int ntx, int nty,
                                                            WinParams wp, const float2* __restrict__ G0,
@@ -1748,7 +1866,7 @@ __global__ void __launch_bounds__(kTileThreads, 5) k_gather_ff(const double* __r
                                                            double2* __restrict__ out) {
     extern __shared__ __align__(16) unsigned char shraw[];
     __shared__ float2 etab[64];
-    gather_ff_run<PM>(p, toff, perm, ts, ntx, nty, wp, G0, G1, scale, out, blockIdx.x, gridDim.x, shraw, etab);
+    gather_ff_run<PM, C32>(p, toff, perm, ts, ntx, nty, wp, G0, G1, scale, out, blockIdx.x, gridDim.x, shraw, etab);
 }
 
 // the register form's support bound for window support P1 (0: none fits)
@@ -1793,14 +1911,14 @@ int kspace_aniso(const KspaceArgs& a) { return kspace_aniso(a.Lx, a.Mx, a.Ly, a.
 bool spread_fits(const fte_context* ctx, int form, int kind, int ts, int P, int aniso = 0) {
     if (ts < 8 || ts > 256) return false;
     size_t sm = form == FTE_FORM_MIXED ? spread_cols32_smem(ts, P)
-                : (form == FTE_FORM_FF ? spread_ff_smem(ts, P, kind == FTE_KIND_SLP ? 2 : 3, aniso)
+                : (fte_form_ff(form) ? spread_ff_smem(ts, P, kind == FTE_KIND_SLP ? 2 : 3, aniso)
                                        : spread_cols_smem(ts, P, aniso));
     return sm <= tile_budget(ctx);
 }
 bool gather_fits(const fte_context* ctx, int form, int ts, int P, int aniso = 0) {
     if (ts < 8 || ts > 256) return false;
     size_t sm = form == FTE_FORM_MIXED ? gather32_smem(ts, P)
-                : (form == FTE_FORM_FF ? gather_ff_smem(ts, P, aniso) : gather64_smem(ts, P, aniso));
+                : (fte_form_ff(form) ? gather_ff_smem(ts, P, aniso) : gather64_smem(ts, P, aniso));
     return sm <= tile_budget(ctx);
 }
 int resolve_tiles(const fte_context* ctx, const KspaceArgs& a, int* ts_s, int* ts_g, bool fill = true) {
@@ -1817,7 +1935,7 @@ int resolve_tiles(const fte_context* ctx, const KspaceArgs& a, int* ts_s, int* t
         // float-float: three CTAs per SM where that still leaves tiles of at
         // least 28 nodes a side (else the halo flushes cost more than the
         // occupancy gains: measured at 1e6 points, P 14..22)
-        if (a.form == FTE_FORM_FF) {
+        if (fte_form_ff(a.form)) {
             const int ngf = a.kind == FTE_KIND_SLP ? 2 : 3;
             for (int ts = 64; ts >= 28 && !*ts_s; ts -= 4)
                 if (spread_ff_smem(ts, a.P, ngf, an) <= tile_budget(ctx) * 2 / 3) *ts_s = ts;
@@ -1831,7 +1949,7 @@ int resolve_tiles(const fte_context* ctx, const KspaceArgs& a, int* ts_s, int* t
             return FTE_ERR_INVALID;
         }
         *ts_g = a.ts_gather;
-    } else if (a.form == FTE_FORM_FF && gather_ff_pm(a.P + 1)) {
+    } else if (fte_form_ff(a.form) && gather_ff_pm(a.P + 1)) {
         // register form: tiles small enough for four CTAs per SM (more warps
         // to hide the products' latency; the region re-reads cost little),
         // at most 28 nodes a side (fewer idle threads in a tile's last round
@@ -1898,7 +2016,7 @@ int launch_spread_tiled(fte_context* ctx, const KspaceArgs& a, const TileBins& t
     const size_t sm = f32 ? spread_cols32_smem(tb.ts, a.P) : spread_cols_smem(tb.ts, a.P, wp.aniso);
     const int nt = tb.ntx * tb.nty;
     const int grid = nt < ctx->num_sms * 8 ? nt : ctx->num_sms * 8;
-    if (a.form == FTE_FORM_FF) {
+    if (fte_form_ff(a.form)) {
         if (!recs) {
             fte_set_error("internal: float-float spread without window records");
             return FTE_ERR_INVALID;
@@ -1910,15 +2028,16 @@ int launch_spread_tiled(fte_context* ctx, const KspaceArgs& a, const TileBins& t
         const size_t smf = spread_ff_smem(tb.ts, a.P, ngf, wp.aniso);
         FTE_LAUNCH(ctx, k_ff_win, ew_grid(ctx, a.nsrc), 256, 0, a.kind, a.psrc, a.f, a.nrm, a.wts, (const int*)tb.perm,
                    a.nsrc, wp, recs);
-        if (ngf == 2) {
-            FTE_CUDA_TRY(fte_smem_ceiling(k_spread_ff<2>, (int)smf));
-            FTE_LAUNCH(ctx, k_spread_ff<2>, grid, kColThreads, smf, (const FfWin*)recs, (const int*)tb.off, tb.ts,
-                       tb.ntx, tb.nty, wp, Hd, Hd + G, nullptr);
-        } else {
-            FTE_CUDA_TRY(fte_smem_ceiling(k_spread_ff<3>, (int)smf));
-            FTE_LAUNCH(ctx, k_spread_ff<3>, grid, kColThreads, smf, (const FfWin*)recs, (const int*)tb.off, tb.ts,
-                       tb.ntx, tb.nty, wp, Hd, Hd + G, Hd + 2 * G);
-        }
+        auto go = [&](auto kern) -> int {
+            FTE_CUDA_TRY(fte_smem_ceiling(kern, (int)smf));
+            FTE_LAUNCH(ctx, kern, grid, kColThreads, smf, (const FfWin*)recs, (const int*)tb.off, tb.ts, tb.ntx,
+                       tb.nty, wp, Hd, Hd + G, ngf == 3 ? Hd + 2 * G : nullptr);
+            return FTE_OK;
+        };
+        if (a.form == FTE_FORM_FF32)
+            FTE_TRY(ngf == 2 ? go(k_spread_ff<2, true>) : go(k_spread_ff<3, true>));
+        else
+            FTE_TRY(ngf == 2 ? go(k_spread_ff<2, false>) : go(k_spread_ff<3, false>));
     } else if (f32) {
         float* Hf = static_cast<float*>(H);
         FTE_CUDA_TRY(fte_smem_ceiling(k_spread_cols32, (int)sm));
@@ -1948,7 +2067,7 @@ int launch_gather_tiled(fte_context* ctx, const KspaceArgs& a, const TileBins& t
     const size_t G = (size_t)a.Mx * a.My;
     const int nt = tb.ntx * tb.nty;
     const int grid = nt < ctx->num_sms * 8 ? nt : ctx->num_sms * 8;
-    if (a.form == FTE_FORM_FF) {
+    if (fte_form_ff(a.form)) {
         const float2* Hf = static_cast<const float2*>(H);
         size_t sm = gather_ff_smem(tb.ts, a.P, wp.aniso);
         auto go = [&](auto kern) -> int {
@@ -1957,16 +2076,29 @@ int launch_gather_tiled(fte_context* ctx, const KspaceArgs& a, const TileBins& t
                        tb.ntx, tb.nty, wp, Hf, Hf + G, scale, a.uk);
             return FTE_OK;
         };
-        switch (gather_ff_pm(a.P + 1)) {
-            case 16: FTE_TRY(go(k_gather_ff<16>)); break;
-            case 17: FTE_TRY(go(k_gather_ff<17>)); break;
-            case 19: FTE_TRY(go(k_gather_ff<19>)); break;
-            case 21: FTE_TRY(go(k_gather_ff<21>)); break;
-            case 23: FTE_TRY(go(k_gather_ff<23>)); break;
-            case 24: FTE_TRY(go(k_gather_ff<24>)); break;
-            case 25: FTE_TRY(go(k_gather_ff<25>)); break;
-            case 32: FTE_TRY(go(k_gather_ff<32>)); break;
-            default: FTE_TRY(go(k_gather_ff<0>)); break;
+        if (a.form == FTE_FORM_FF32) {
+            // FP32 products: the instances for 16, 24 and 32 nodes
+            const int pm = gather_ff_pm(a.P + 1);
+            if (pm == 0)
+                FTE_TRY(go(k_gather_ff<0, true>));
+            else if (pm <= 16)
+                FTE_TRY(go(k_gather_ff<16, true>));
+            else if (pm <= 24)
+                FTE_TRY(go(k_gather_ff<24, true>));
+            else
+                FTE_TRY(go(k_gather_ff<32, true>));
+        } else {
+            switch (gather_ff_pm(a.P + 1)) {
+                case 16: FTE_TRY(go(k_gather_ff<16, false>)); break;
+                case 17: FTE_TRY(go(k_gather_ff<17, false>)); break;
+                case 19: FTE_TRY(go(k_gather_ff<19, false>)); break;
+                case 21: FTE_TRY(go(k_gather_ff<21, false>)); break;
+                case 23: FTE_TRY(go(k_gather_ff<23, false>)); break;
+                case 24: FTE_TRY(go(k_gather_ff<24, false>)); break;
+                case 25: FTE_TRY(go(k_gather_ff<25, false>)); break;
+                case 32: FTE_TRY(go(k_gather_ff<32, false>)); break;
+                default: FTE_TRY(go(k_gather_ff<0, false>)); break;
+            }
         }
     } else if (a.form == FTE_FORM_MIXED) {
         const float* Hf = static_cast<const float*>(H);
@@ -2117,7 +2249,7 @@ int fte_kspace_tune(fte_context* ctx, void* grid, WsCarver bins, KspaceArgs& a, 
         TileBins tb;
         rc = fte_tiles_build(ctx, w, a.psrc, a.nsrc, a.Lx, a.Ly, wp.h, wp.hy, ts, (a.Mx + ts - 1) / ts,
                              (a.My + ts - 1) / ts, &tb);
-        FfWin* recs = a.form == FTE_FORM_FF ? w.take<FfWin>(a.nsrc) : nullptr;
+        FfWin* recs = fte_form_ff(a.form) ? w.take<FfWin>(a.nsrc) : nullptr;
         if (!rc && !w.ok()) {
             fte_set_error("internal: tuner bin scratch too small");
             rc = FTE_ERR_ALLOC;
@@ -2163,7 +2295,7 @@ int fte_kspace_tune(fte_context* ctx, void* grid, WsCarver bins, KspaceArgs& a, 
 }
 
 size_t fte_kspace_rec_ws(int form, int64_t nsrc) {
-    return form == FTE_FORM_FF ? ws_bytes((size_t)nsrc + 1, sizeof(FfWin)) : 0;
+    return fte_form_ff(form) ? ws_bytes((size_t)nsrc + 1, sizeof(FfWin)) : 0;
 }
 
 size_t fte_kspace_ws(int kind, int form, int Mx, int My, int64_t nsrc, int64_t ntar) {
@@ -2247,7 +2379,7 @@ int fte_kspace_run(fte_context* ctx, WsCarver& wc, const KspaceArgs& a, fte_info
         return FTE_ERR_INVALID;
     }
     // float-float form: window records of the sources (tiled spread only)
-    const bool ff = a.form == FTE_FORM_FF;
+    const bool ff = fte_form_ff(a.form);
     FfWin* recs = ff && a.nsrc > 0 && ts_s > 0 ? wc.take<FfWin>(a.nsrc) : nullptr;
     FTE_WS_CHECK(wc);
 

@@ -69,13 +69,17 @@ extern "C" {
  *   FTE_FORM_MIXED  FP32 spread (Kahan-compensated), transforms and gather,
  *                   the multiplier in FP64 (tol >= 1e-6 SLP, 2e-7 DLP);
  *   FTE_FORM_FF     float-float (pairs of FP32 numbers, ~48 bits) spread,
- *                   transforms, multiplier and gather (tol >= 1e-11).
+ *                   transforms, multiplier and gather (tol >= 1e-11);
+ *   FTE_FORM_FF32   float-float window factors, transforms and multiplier,
+ *                   FP32 products with Kahan-compensated sums in the spread
+ *                   and gather (tol >= 1e-6 SLP, 2e-7 DLP).
  * The real-space pairs of the mixed form are FP32 for pairs whose terms lie
  * far below the tolerance, float-float for the others from tol 1e-11, and
  * FP64 below (fte_options.near). */
 #define FTE_FORM_PLAIN 0
 #define FTE_FORM_MIXED 1
 #define FTE_FORM_FF 2
+#define FTE_FORM_FF32 3
 
 /* fte_options.kspace (FTE_FORM_MIXED): the k-space arithmetic of the tuned
  * choice; AUTO lets the chooser pick by tolerance and cost */
@@ -83,6 +87,7 @@ extern "C" {
 #define FTE_KSPACE_FP64 1
 #define FTE_KSPACE_FP32 2
 #define FTE_KSPACE_FF 3
+#define FTE_KSPACE_FF32 4
 
 /* fte_options.near (FTE_FORM_MIXED): the arithmetic of the real-space pairs;
  * AUTO: FP32 for pairs whose terms are below the tolerance's reach of FP32
@@ -112,8 +117,9 @@ typedef struct {
     int Mx, My;     /* grid size */
     double w;       /* window half-width P*h/2 */
     double eta;     /* window shape (2 xi w / m)^2, m = 0.95 sqrt(pi P) */
-    int form;       /* arithmetic of the k-space part: FTE_FORM_PLAIN (FP64), FTE_FORM_MIXED (FP32) or
-                       FTE_FORM_FF (float-float spread, transforms, multiplier and gather) */
+    int form;       /* arithmetic of the k-space part: FTE_FORM_PLAIN (FP64), FTE_FORM_MIXED (FP32),
+                       FTE_FORM_FF (float-float spread, transforms, multiplier and gather) or
+                       FTE_FORM_FF32 (float-float transforms, FP32 spread and gather products) */
     int ts_spread;  /* k-space spread / gather tile sizes in grid nodes (plans; 0: the default rule) */
     int ts_gather;
 } fte_params;

@@ -1,0 +1,165 @@
+"""Float-float window factors and transforms with FP32 spread and gather
+products (FTE_FORM_FF32), the tuned choice at loose tolerances.
+
+The products are rounded to FP32 and the sums carried with Kahan's
+compensation, so the k-space part sits ~1e-7 (Stokeslet) / ~1e-8
+(stresslet) of its maximum from the FP64 k-space on the same parameters --
+the FP32 form's floor -- and the form is only chosen where the tolerance is
+at least 1e-6 (SLP) / 2e-7 (DLP).
+
+* against the FP64 k-space on the same parameters, on square, wide and tall
+  boxes, every gather instance (window supports 9..35 nodes: the register
+  forms for 16, 24, 32 nodes and the shared-memory form) and around the long
+  transforms (windows wrapping a 32-node axis: the spread's and gather's
+  out-of-region paths);
+* the tuned choice picks it at tol 1e-6 and 1e-5 and meets the tolerance
+  against converged FP64 Ewald sums;
+* plans give the driver's result to the FP32 products' rounding (their tile
+  bins order a tile's points by atomic counters, the driver's call builds
+  its own), batches of such plans the plans' result.
+"""
+import numpy as np
+import pytest
+
+from oracle import pyoracle as po
+
+pytestmark = pytest.mark.gpu
+
+# FP32 products: the k-space part's distance from FP64 on the same parameters
+KS_BOUND = 1e-6
+
+
+def _ft():
+    import fasttools2d_gb300 as ft
+
+    return ft
+
+
+def _case(seed, n, Lx, Ly):
+    rng = np.random.default_rng(seed)
+    xs, ys = (rng.random(n) - 0.5) * Lx, (rng.random(n) - 0.5) * Ly
+    xt, yt = (rng.random(n) - 0.5) * Lx, (rng.random(n) - 0.5) * Ly
+    f1, f2 = rng.standard_normal(n), rng.standard_normal(n)
+    f1 -= f1.mean()
+    f2 -= f2.mean()
+    th = rng.random(n) * 2 * np.pi
+    return xs, ys, xt, yt, f1, f2, np.cos(th), np.sin(th)
+
+
+def _run(ft, ctx, kind, d, Lx, Ly, **kw):
+    xs, ys, xt, yt, f1, f2, n1, n2 = d
+    if kind == "slp":
+        return ft.StokesSLP_ewald_2p(xs, ys, xt, yt, f1, f2, Lx, Ly, form=ft.FORM_MIXED, ctx=ctx, return_info=True,
+                                     **kw)
+    return ft.StokesDLP_ewald_2p(xs, ys, xt, yt, n1, n2, f1, f2, Lx, Ly, form=ft.FORM_MIXED, ctx=ctx,
+                                 return_info=True, **kw)
+
+
+def _vs_fp64(ft, ctx, kind, d, Lx, Ly, **kw):
+    out_f, info_f = _run(ft, ctx, kind, d, Lx, Ly, kspace=ft.KSPACE_FF32, **kw)
+    p = info_f.params
+    assert p.form == ft.FORM_FF32
+    same = dict(P=p.P, xi=p.xi, Mx=p.Mx, My=p.My, nside_x=p.nside_x, nside_y=p.nside_y)
+    kw = {k: v for k, v in kw.items() if k not in same}
+    out_d, info_d = _run(ft, ctx, kind, d, Lx, Ly, kspace=ft.KSPACE_FP64, **same, **kw)
+    assert info_d.params.form == ft.FORM_PLAIN
+    return np.max(np.abs(out_f[3] - out_d[3])) / np.max(np.abs(out_d[3])), p
+
+
+@pytest.mark.parametrize("kind", ["slp", "dlp"])
+@pytest.mark.parametrize("geom", [(20000, 1.0, 1.0, 141), (12000, 2.0, 1.0, 142), (9000, 1.0, 2.75, 143)])
+def test_ff32_kspace_near_fp64(gpu_ctx, kind, geom):
+    ft = _ft()
+    n, Lx, Ly, seed = geom
+    rel, _ = _vs_fp64(ft, gpu_ctx, kind, _case(seed, n, Lx, Ly), Lx, Ly, tol=1e-6)
+    assert rel <= KS_BOUND, rel
+
+
+@pytest.mark.parametrize("kind", ["slp", "dlp"])
+@pytest.mark.parametrize("P", [8, 12, 16, 24, 30, 34])
+def test_ff32_gather_supports(gpu_ctx, kind, P):
+    """Window supports of every gather instance: 9 and 13 nodes (the
+    16-node form), 17 (24), 25 and 31 (32) and 35 (shared-memory rows)."""
+    ft = _ft()
+    Lx, Ly = 1.0, 1.5
+    rel, p = _vs_fp64(ft, gpu_ctx, kind, _case(160 + P, 6000, Lx, Ly), Lx, Ly, tol=1e-6, P=P)
+    assert p.P == P
+    assert rel <= KS_BOUND, rel
+
+
+@pytest.mark.parametrize("kind", ["slp", "dlp"])
+def test_ff32_around_long_transforms(gpu_ctx, kind):
+    """An 8000 x 32 grid of a 250 x 1 box: FP64 long transforms between the
+    FP32-product spread and gather, most windows wrapping the 32-node axis
+    (the out-of-region atomics of the spread, global reads of the gather)."""
+    ft = _ft()
+    Lx, Ly = 250.0, 1.0
+    same = dict(P=16, xi=10.0, Mx=8000, My=32, nside_x=500, nside_y=2)
+    rel, _ = _vs_fp64(ft, gpu_ctx, kind, _case(177, 3000, Lx, Ly), Lx, Ly, tol=1e-6, **same)
+    assert rel <= KS_BOUND, rel
+
+
+@pytest.mark.parametrize("tol", [1e-6, 1e-5])
+@pytest.mark.parametrize("geom", [(20000, 1.0, 1.0, 151), (12000, 3.75, 1.0, 152)])
+def test_ff32_chosen_and_meets_tolerance(gpu_ctx, tol, geom):
+    ft = _ft()
+    n, Lx, Ly, seed = geom
+    d = _case(seed, n, Lx, Ly)
+    xs, ys, xt, yt, f1, f2, n1, n2 = d
+    idx = np.arange(0, n, 40)
+    for kind in ("slp", "dlp"):
+        out, info = _run(ft, gpu_ctx, kind, d, Lx, Ly, tol=tol)
+        assert info.params.form == ft.FORM_FF32, info.params.as_dict()
+        if kind == "slp":
+            truth = po.ewald_truth(po.KIND_SLP, xs, ys, xt[idx], yt[idx], f1, f2, Lx, Ly)
+        else:
+            truth = po.ewald_truth(po.KIND_DLP, xs, ys, xt[idx], yt[idx], f1, f2, Lx, Ly, n1=n1, n2=n2)
+        u = np.stack([out[0][idx], out[1][idx]], 1)
+        err = np.max(np.abs(u - truth)) / np.max(np.abs(truth))
+        assert err <= tol, (kind, err, info.params.as_dict())
+
+
+def test_ff32_plans_and_batch_match_driver(gpu_ctx):
+    """Plans at tol 1e-6 (FP32-product k-space, window records and tile bins
+    built once) against the driver on the same parameters, and a batch of
+    them (their k-space parts on the per-plan path) against the plans."""
+    ft = _ft()
+    n, Lx, Ly = 15000, 2.0, 1.0
+    xs, ys, xt, yt, f1, f2, n1, n2 = _case(161, n, Lx, Ly)
+    rng = np.random.default_rng(162)
+    fs1, fs2 = rng.standard_normal((2, n)), rng.standard_normal((2, n))
+    plans = []
+    for kind in (ft.KIND_SLP, ft.KIND_DLP):
+        plan = ft.Plan(kind, xs, ys, xt, yt, f1, f2, Lx, Ly, n1=n1, n2=n2, tol=1e-6, form=ft.FORM_MIXED, nvmax=2,
+                       ctx=gpu_ctx)
+        p = plan.params
+        assert p.form == ft.FORM_FF32
+        u1s, u2s = plan.execute(fs1, fs2)
+        for v in range(2):
+            kw = dict(tol=1e-6, form=ft.FORM_MIXED, kspace=ft.KSPACE_FF32, P=p.P, xi=p.xi, Mx=p.Mx, My=p.My,
+                      nside_x=p.nside_x, nside_y=p.nside_y, ctx=gpu_ctx)
+            if kind == ft.KIND_SLP:
+                o = ft.StokesSLP_ewald_2p(xs, ys, xt, yt, fs1[v], fs2[v], Lx, Ly, **kw)
+            else:
+                o = ft.StokesDLP_ewald_2p(xs, ys, xt, yt, n1, n2, fs1[v], fs2[v], Lx, Ly, **kw)
+            ref = np.stack([o[0], o[1]], 1)
+            got = np.stack([np.asarray(u1s[v]), np.asarray(u2s[v])], 1)
+            # same kernels and tile sizes, but the plan's tile bins are its
+            # own build: the order of the points within a tile comes from
+            # atomic counters, and with FP32 products another order moves
+            # the rounding (the batch below reuses the plan's bins)
+            assert np.max(np.abs(got - ref)) <= KS_BOUND * np.max(np.abs(ref)), (kind, v)
+        plans.append(plan)
+    batch = ft.Batch(plans, 2, ctx=gpu_ctx)
+    for i in range(len(plans)):
+        batch.set_density(i, fs1, fs2)
+    for use_graph in (True, False):
+        batch.launch(use_graph)
+        for i, p in enumerate(plans):
+            b1, b2 = batch.velocity(i)
+            e1, e2 = p.execute(fs1, fs2)
+            got, ref = np.stack([np.asarray(b1), np.asarray(b2)]), np.stack([np.asarray(e1), np.asarray(e2)])
+            assert np.max(np.abs(got - ref)) <= 1e-12 * np.max(np.abs(ref)), (use_graph, i)
+    batch.close()
+    for p in plans:
+        p.close()

@@ -86,4 +86,4 @@ def test_tuned_parameters_are_cheaper(gpu_ctx):
     tuned = ft.choose_params(ft.KIND_SLP, f1, f2, n, 1.0, 1.0, tol=1e-6, form=ft.FORM_MIXED)
     assert tuned.P < plain.P
     assert tuned.nside_x > plain.nside_x  # smaller cutoff: fewer FP64 near pairs
-    assert tuned.form in (ft.FORM_MIXED, ft.FORM_FF)  # FP32 or float-float k-space, by cost
+    assert tuned.form in (ft.FORM_MIXED, ft.FORM_FF, ft.FORM_FF32)  # FP32 or float-float k-space, by cost
