@@ -1701,9 +1701,10 @@ __device__ __forceinline__ void gather_ff_run(const double* __restrict__ p, cons
     float2* r1 = r0 + WW;
     float2* e1 = r1 + WW;
     float2* wyb = e1 + e1_len(wp.P, wp.aniso) + threadIdx.x * P1;  // PM == 0 only
-    // C32: FP32 regions and window rows in the same space
-    float* r0f = reinterpret_cast<float*>(shf);
-    float* r1f = r0f + WW;
+    // C32: the grids' high parts interleaved per node (one 8-byte read gives
+    // both grids' values; the tile bins' order of the targets keeps a half
+    // warp's rows on distinct banks for 8-byte values) and FP32 window rows
+    float2* rc = shf;
     float* wybf = reinterpret_cast<float*>(e1 + e1_len(wp.P, wp.aniso)) + threadIdx.x * P1;
     load_etab(etab);  // 2^(-j/64) for the window factors (as in k_ff_win)
     load_e1_ff(e1, wp);
@@ -1719,8 +1720,7 @@ __device__ __forceinline__ void gather_ff_run(const double* __restrict__ p, cons
             int xx = idx / W, yy = idx - xx * W;
             size_t at = (size_t)fte_wrap_index(ox + xx, wp.Mx) * wp.My + fte_wrap_index(oy + yy, wp.My);
             if constexpr (C32) {
-                r0f[idx] = G0[at].x;
-                r1f[idx] = G1[at].x;
+                rc[idx] = make_float2(G0[at].x, G1[at].x);
             } else {
                 r0[idx] = G0[at];
                 r1[idx] = G1[at];
@@ -1770,21 +1770,22 @@ __device__ __forceinline__ void gather_ff_run(const double* __restrict__ p, cons
                 if constexpr (C32) {
                     float s0 = 0.f, s1 = 0.f;
                     if (inside) {
-                        const float* g0 = r0f + (lx + a) * W + ly;
-                        const float* g1 = r1f + (lx + a) * W + ly;
+                        const float2* g = rc + (lx + a) * W + ly;
                         if constexpr (PM > 0) {
 #pragma unroll
                             for (int j = 0; j < PM; j++) {
                                 if (j < P1) {
-                                    s0 = __fmaf_rn(wyf[j], g0[j], s0);
-                                    s1 = __fmaf_rn(wyf[j], g1[j], s1);
+                                    const float2 v = g[j];
+                                    s0 = __fmaf_rn(wyf[j], v.x, s0);
+                                    s1 = __fmaf_rn(wyf[j], v.y, s1);
                                 }
                             }
                         } else {
                             for (int j = 0; j < P1; j++) {
                                 const float w = wybf[j];
-                                s0 = __fmaf_rn(w, g0[j], s0);
-                                s1 = __fmaf_rn(w, g1[j], s1);
+                                const float2 v = g[j];
+                                s0 = __fmaf_rn(w, v.x, s0);
+                                s1 = __fmaf_rn(w, v.y, s1);
                             }
                         }
                     } else {
