@@ -492,6 +492,9 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, int part,
         const int ntw = warp < nt ? (nt - warp + kNearWarps - 1) / kNearWarps : 0;
         // x below which a Stokeslet pair takes ring qn
         const float xsplit = 1.0f;
+        // Stokeslet with the FP32 class from x = 1 (tol >= ~7e-8): ring qf
+        // (1 <= x < x32) stays empty, its ballots and stores are skipped
+        const bool slp_no_f = KIND == FTE_KIND_SLP && x32 <= xsplit;
         int Pf = 0, Ef = 0, Pn = 0, En = 0;  // pushed / evaluated counts of rings qf, qn
         int tailF[NSLOT], tailN[NSLOT];      // Pf, Pn after each slot's sweep
         double acc[NSLOT][NV][2];
@@ -978,14 +981,18 @@ __device__ __forceinline__ void near_box(const NearParams& prm, int b, int part,
                     // E1); the stresslet has one pair formula
                     if constexpr (KIND == FTE_KIND_SLP) {
                         const bool f0 = p0 && !x0, n0 = p0 && x0, f1 = p1 && !x1, n1 = p1 && x1;
-                        const unsigned mf0 = __ballot_sync(0xffffffffu, f0), mf1 = NB == 2 ? __ballot_sync(0xffffffffu, f1) : 0u;
+                        if (!slp_no_f) {
+                            const unsigned mf0 = __ballot_sync(0xffffffffu, f0);
+                            const unsigned mf1 = NB == 2 ? __ballot_sync(0xffffffffu, f1) : 0u;
+                            const int cf0 = __popc(mf0);
+                            if (f0) qf[(Pf + __popc(mf0 & lt_mask)) & (kQueue - 1)] = e0;
+                            if (f1) qf[(Pf + cf0 + __popc(mf1 & lt_mask)) & (kQueue - 1)] = e1;
+                            Pf += cf0 + __popc(mf1);
+                        }
                         const unsigned mn0 = __ballot_sync(0xffffffffu, n0), mn1 = NB == 2 ? __ballot_sync(0xffffffffu, n1) : 0u;
-                        const int cf0 = __popc(mf0), cn0 = __popc(mn0);
-                        if (f0) qf[(Pf + __popc(mf0 & lt_mask)) & (kQueue - 1)] = e0;
-                        if (f1) qf[(Pf + cf0 + __popc(mf1 & lt_mask)) & (kQueue - 1)] = e1;
+                        const int cn0 = __popc(mn0);
                         if (n0) qn[(Pn + __popc(mn0 & lt_mask)) & (kQueue - 1)] = e0;
                         if (n1) qn[(Pn + cn0 + __popc(mn1 & lt_mask)) & (kQueue - 1)] = e1;
-                        Pf += cf0 + __popc(mf1);
                         Pn += cn0 + __popc(mn1);
                     } else {
                         const unsigned mf0 = __ballot_sync(0xffffffffu, p0), mf1 = NB == 2 ? __ballot_sync(0xffffffffu, p1) : 0u;

@@ -16,7 +16,9 @@ at least 1e-6 (SLP) / 2e-7 (DLP).
   against converged FP64 Ewald sums;
 * plans give the driver's result to the FP32 products' rounding (their tile
   bins order a tile's points by atomic counters, the driver's call builds
-  its own), batches of such plans the plans' result.
+  its own), batches of such plans the plans' result to the same rounding
+  (the gather rounds FP64 grid values, whose last bits follow the order of
+  the spread's atomic flushes, to FP32).
 """
 import numpy as np
 import pytest
@@ -159,7 +161,10 @@ def test_ff32_plans_and_batch_match_driver(gpu_ctx):
             b1, b2 = batch.velocity(i)
             e1, e2 = p.execute(fs1, fs2)
             got, ref = np.stack([np.asarray(b1), np.asarray(b2)]), np.stack([np.asarray(e1), np.asarray(e2)])
-            assert np.max(np.abs(got - ref)) <= 1e-12 * np.max(np.abs(ref)), (use_graph, i)
+            # same bins and kernels; the FP64 grids' last bits depend on the
+            # order of the tiles' atomic flushes, and the gather's FP32 high
+            # parts of a grid value can round either way on such a bit
+            assert np.max(np.abs(got - ref)) <= KS_BOUND * np.max(np.abs(ref)), (use_graph, i)
     batch.close()
     for p in plans:
         p.close()
