@@ -40,6 +40,26 @@ def test_library_exports_declared_symbols():
     assert L.fte_version() >= 100
 
 
+def test_python_constants_match_header():
+    """Every status, flag, form, arithmetic and kind code of the public header
+    has the same value in the Python mirror (FTE_FORM_FF -> FORM_FF, ...)."""
+    import fasttools2d_gb300 as ft
+
+    text = open(os.path.join(ROOT, "include", "fasttools2d.h")).read()
+    defs = dict(re.findall(r"^#define (FTE_[A-Z0-9_]+) (\d+)u?\b", text, flags=re.M))
+    checked = 0
+    for name, val in defs.items():
+        short = name[4:]
+        if short.startswith(("OK", "ERR_", "DEVICE_POINTERS", "HOST_ASYNC")):
+            assert getattr(ft, name) == int(val), name  # status codes and flags keep the prefix
+        elif short.startswith(("FORM_", "KSPACE_", "NEAR_", "KIND_")):
+            assert getattr(ft, short) == int(val), name
+        else:
+            continue
+        checked += 1
+    assert checked >= 20
+
+
 @pytest.mark.parametrize("kind", [0, 1])
 @pytest.mark.parametrize("case", [(1000, 1000, 1.0, 1.0, 1e-10), (20, 20, 1.0, 1.0, 1e-16), (500, 300, 2.0, 1.0, 1e-8),
                                   (2000, 2000, 1.0, 2.0, 1e-12), (10240, 534528, 2.0, 1.0, 1e-10),
