@@ -84,15 +84,15 @@ def test_irrational_box_meets_tolerance(gpu_ctx, tol, geom):
 
 
 def test_forced_kspace_arithmetic_on_irrational_box(gpu_ctx):
-    """FP64, FP32 and float-float k-space on the same unequal-step grid agree
-    (the FP32 form to its own floor)."""
+    """FP64, FP32, float-float and FP32-product k-space on the same
+    unequal-step grid agree (the FP32 forms to their own floor)."""
     import fasttools2d_gb300 as ft
 
     n, Lx, Ly = 12000, 1.0, np.sqrt(2.0)
     xs, ys, xt, yt, f1, f2, n1, n2 = _case(n, Lx, Ly, 45)
     res = {}
     over = {}
-    for ks in (ft.KSPACE_FP64, ft.KSPACE_FF, ft.KSPACE_FP32):
+    for ks in (ft.KSPACE_FP64, ft.KSPACE_FF, ft.KSPACE_FP32, ft.KSPACE_FF32):
         # the same parameters for every arithmetic (those of the first call)
         out, info = ft.StokesDLP_ewald_2p(xs, ys, xt, yt, n1, n2, f1, f2, Lx, Ly, tol=1e-6, form=ft.FORM_MIXED,
                                           kspace=ks, near=ft.NEAR_FP64, ctx=gpu_ctx, return_info=True, **over)
@@ -106,6 +106,7 @@ def test_forced_kspace_arithmetic_on_irrational_box(gpu_ctx):
     scale = np.abs(res[ft.KSPACE_FP64]).max()
     assert np.abs(res[ft.KSPACE_FF] - res[ft.KSPACE_FP64]).max() <= 1e-11 * scale
     assert np.abs(res[ft.KSPACE_FP32] - res[ft.KSPACE_FP64]).max() <= 1e-6 * scale
+    assert np.abs(res[ft.KSPACE_FF32] - res[ft.KSPACE_FP64]).max() <= 1e-6 * scale
 
 
 def test_plans_on_irrational_box(gpu_ctx):
