@@ -148,6 +148,7 @@ extern "C" int fte_create(fte_context** out, int device) {
     FTE_CUDA_TRY(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking));
     c->stream = c->own_stream;
     for (int i = 0; i < 8; i++) FTE_CUDA_TRY(cudaEventCreate(&c->ev[i]));
+    FTE_CUDA_TRY(cudaEventCreateWithFlags(&c->ev_q, cudaEventDisableTiming));
     FTE_CUDA_TRY(cudaMallocHost(&c->host_scalars, 64 * sizeof(double)));
     FTE_CUDA_TRY(cudaMalloc(&c->dev_flags, 64));
     *out = c;
@@ -185,6 +186,7 @@ extern "C" int fte_destroy(fte_context* c) {
     if (c->dev_flags) cudaFree(c->dev_flags);
     for (int i = 0; i < 8; i++)
         if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+    if (c->ev_q) cudaEventDestroy(c->ev_q);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
     delete c;
     return FTE_OK;
@@ -1119,21 +1121,9 @@ __global__ void k_pack(const double* __restrict__ a, const double* __restrict__ 
     }
 }
 
-// acc[0] += sum (w f1)^2 + (w f2)^2 ;  DLP also acc[1..2] += sum (f.n) (xs, ys)
-template <int KIND>
-__global__ void k_reduce(const double* __restrict__ p, const double* __restrict__ f, const double* __restrict__ nrm,
-                         const double* __restrict__ wts, int64_t n, double* __restrict__ acc) {
-    double q = 0, zx = 0, zy = 0;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        double w = wts ? wts[i] : 1.0;
-        double f1 = f[2 * i] * w, f2 = f[2 * i + 1] * w;
-        q += f1 * f1 + f2 * f2;
-        if (KIND == FTE_KIND_DLP) {
-            double fn = f1 * nrm[2 * i] + f2 * nrm[2 * i + 1];
-            zx += fn * p[2 * i];
-            zy += fn * p[2 * i + 1];
-        }
-    }
+// block sums of up to three values added to acc[0 .. count-1] (one atomic
+// each per block)
+__device__ __forceinline__ void block_acc3(double q, double zx, double zy, double* __restrict__ acc, int count) {
     for (int o = 16; o > 0; o >>= 1) {
         q += __shfl_down_sync(0xffffffffu, q, o);
         zx += __shfl_down_sync(0xffffffffu, zx, o);
@@ -1159,12 +1149,39 @@ __global__ void k_reduce(const double* __restrict__ p, const double* __restrict_
         }
         if (lane == 0) {
             atomicAdd(&acc[0], q);
-            if (KIND == FTE_KIND_DLP) {
-                atomicAdd(&acc[1], zx);
-                atomicAdd(&acc[2], zy);
-            }
+            if (count > 1) atomicAdd(&acc[1], zx);
+            if (count > 2) atomicAdd(&acc[2], zy);
         }
     }
+}
+
+// acc[0] += sum (w f1)^2 + (w f2)^2, the estimates' Q, from the caller's
+// (staged) density and weight arrays: it needs no packing, so the host can
+// read it back while the wrapping kernels run
+__global__ void k_reduce_q(const double* __restrict__ f1, const double* __restrict__ f2,
+                           const double* __restrict__ wts, int64_t n, double* __restrict__ acc) {
+    double q = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double w = wts ? wts[i] : 1.0;
+        const double a = f1[i] * w, b = f2[i] * w;
+        q += a * a + b * b;
+    }
+    block_acc3(q, 0.0, 0.0, acc, 1);
+}
+
+// acc[1..2] += sum (w f . n) (xs, ys) over the wrapped sources: the
+// stresslet's zero mode
+__global__ void k_reduce_zero(const double* __restrict__ p, const double* __restrict__ f,
+                              const double* __restrict__ nrm, const double* __restrict__ wts, int64_t n,
+                              double* __restrict__ acc) {
+    double zx = 0, zy = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double w = wts ? wts[i] : 1.0;
+        const double fn = f[2 * i] * w * nrm[2 * i] + f[2 * i + 1] * w * nrm[2 * i + 1];
+        zx += fn * p[2 * i];
+        zy += fn * p[2 * i + 1];
+    }
+    block_acc3(zx, zy, 0.0, acc + 1, 2);
 }
 
 // u = ur + uk (+ zero mode); optional interleaved copies of ur and uk (with the zero mode in uk)
@@ -1617,24 +1634,23 @@ static int ewald_entry(fte_context* c, int kind, const double* xsrc, const doubl
     for (const double* a : {dxs, dys, df1, df2, dn1, dn2, dw}) fin.add(a, nsrc);
     fin.add(dxt, ntar);
     fin.add(dyt, ntar);
+    // the input check and Q first: the host reads them back (event ev_q)
+    // and chooses the parameters while the wrapping and packing kernels run
     FTE_TRY(fte_finite_launch(c, fin));
+    FTE_CUDA_TRY(cudaMemsetAsync(acc, 0, 8 * sizeof(double), c->stream));
+    if (nsrc > 0) FTE_LAUNCH(c, k_reduce_q, grid1d(c, nsrc), 256, 0, df1, df2, dw, nsrc, acc);
+    FTE_CUDA_TRY(cudaMemcpyAsync(c->host_scalars, acc, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    FTE_CUDA_TRY(cudaEventRecord(c->ev_q, c->stream));
     if (nsrc > 0) {
         FTE_LAUNCH(c, k_wrap_pack, grid1d(c, nsrc), 256, 0, dxs, dys, nsrc, Lx, Ly, ps);
         FTE_LAUNCH(c, k_pack, grid1d(c, nsrc), 256, 0, df1, df2, nsrc, pf);
         if (pn) FTE_LAUNCH(c, k_pack, grid1d(c, nsrc), 256, 0, dn1, dn2, nsrc, pn);
     }
     if (ntar > 0) FTE_LAUNCH(c, k_wrap_pack, grid1d(c, ntar), 256, 0, dxt, dyt, ntar, Lx, Ly, pt);
-    FTE_CUDA_TRY(cudaMemsetAsync(acc, 0, 8 * sizeof(double), c->stream));
-    if (nsrc > 0) {
-        if (kind == FTE_KIND_SLP)
-            FTE_LAUNCH(c, k_reduce<FTE_KIND_SLP>, grid1d(c, nsrc), 256, 0, (const double*)ps, (const double*)pf,
-                       (const double*)pn, dw, nsrc, acc);
-        else
-            FTE_LAUNCH(c, k_reduce<FTE_KIND_DLP>, grid1d(c, nsrc), 256, 0, (const double*)ps, (const double*)pf,
-                       (const double*)pn, dw, nsrc, acc);
-    }
-    FTE_CUDA_TRY(cudaMemcpyAsync(c->host_scalars, acc, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-    FTE_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    if (nsrc > 0 && kind == FTE_KIND_DLP)
+        FTE_LAUNCH(c, k_reduce_zero, grid1d(c, nsrc), 256, 0, (const double*)ps, (const double*)pf,
+                   (const double*)pn, dw, nsrc, acc);
+    FTE_CUDA_TRY(cudaEventSynchronize(c->ev_q));
     FTE_TRY(fte_finite_result(c, kind == FTE_KIND_SLP ? "fte_stokes_slp_ewald_2p" : "fte_stokes_dlp_ewald_2p"));
     double Q = c->host_scalars[0] + 1.0;
     fte_params prm;

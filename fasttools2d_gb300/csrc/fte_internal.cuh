@@ -145,6 +145,7 @@ struct fte_context {
     std::map<int, FftPlan*> plans;
     std::map<int, LongPlan*> lplans;
     cudaEvent_t ev[8] = {nullptr};
+    cudaEvent_t ev_q = nullptr;  // the drivers' Q read-back (no timing)
     int max_smem_optin = 0;
     int num_sms = 0;
     unsigned int* dev_flags = nullptr;  // device counters of the input checks
