@@ -1936,10 +1936,16 @@ int resolve_tiles(const fte_context* ctx, const KspaceArgs& a, int* ts_s, int* t
         // float-float: three CTAs per SM where that still leaves tiles of at
         // least 28 nodes a side (else the halo flushes cost more than the
         // occupancy gains: measured at 1e6 points, P 14..22)
+        // FP32 products (four operations per node instead of eleven): four
+        // CTAs per SM, tiles down to 16 nodes (1e6 points, tol 1e-6: the
+        // tuner's picks, 32 / 16 nodes for the two / three grids, were 2 %
+        // faster than the three-CTA tiles)
         if (fte_form_ff(a.form)) {
             const int ngf = a.kind == FTE_KIND_SLP ? 2 : 3;
-            for (int ts = 64; ts >= 28 && !*ts_s; ts -= 4)
-                if (spread_ff_smem(ts, a.P, ngf, an) <= tile_budget(ctx) * 2 / 3) *ts_s = ts;
+            const bool c32 = a.form == FTE_FORM_FF32;
+            const size_t cap = c32 ? tile_budget(ctx) / 2 : tile_budget(ctx) * 2 / 3;
+            for (int ts = 64; ts >= (c32 ? 16 : 28) && !*ts_s; ts -= 4)
+                if (spread_ff_smem(ts, a.P, ngf, an) <= cap) *ts_s = ts;
         }
         for (int ts = 64; ts >= 8 && !*ts_s; ts -= 4)
             if (spread_fits(ctx, a.form, a.kind, ts, a.P, an)) *ts_s = ts;
@@ -1955,7 +1961,8 @@ int resolve_tiles(const fte_context* ctx, const KspaceArgs& a, int* ts_s, int* t
         // to hide the products' latency; the region re-reads cost little),
         // at most 28 nodes a side (fewer idle threads in a tile's last round
         // of targets; 28 was the fastest of 24..48 at 1e6 points)
-        for (int ts = 28; ts >= 8 && !*ts_g; ts -= 4)
+        // (FP32 products: up to 32, the tuner's pick at tol 1e-6)
+        for (int ts = a.form == FTE_FORM_FF32 ? 32 : 28; ts >= 8 && !*ts_g; ts -= 4)
             if (gather_ff_smem(ts, a.P, an) <= tile_budget(ctx) / 2) *ts_g = ts;
         if (!*ts_g) *ts_g = 8;
     } else {
