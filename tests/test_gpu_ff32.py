@@ -14,6 +14,7 @@ at least 1e-6 (SLP) / 2e-7 (DLP).
   out-of-region paths);
 * the tuned choice picks it at tol 1e-6 and 1e-5 and meets the tolerance
   against converged FP64 Ewald sums;
+* a handful of points and no sources at all;
 * plans give the driver's result to the FP32 products' rounding (their tile
   bins order a tile's points by atomic counters, the driver's call builds
   its own), batches of such plans the plans' result to the same rounding
@@ -168,3 +169,37 @@ def test_ff32_plans_and_batch_match_driver(gpu_ctx):
     batch.close()
     for p in plans:
         p.close()
+
+
+@pytest.mark.parametrize("kind", ["slp", "dlp"])
+@pytest.mark.parametrize("n", [1, 3, 50])
+def test_ff32_few_points(gpu_ctx, kind, n):
+    """A handful of points (grids of a few tiles, windows wrapping the whole
+    box): the FP32-product k-space against FP64 on the same parameters."""
+    ft = _ft()
+    d = list(_case(170 + n, n, 1.0, 1.0))
+    if n == 1:  # one source: keep its density (a zero-mean single density is 0)
+        rng = np.random.default_rng(171)
+        d[4], d[5] = rng.standard_normal(1), rng.standard_normal(1)
+    out_f, info_f = _run(ft, gpu_ctx, kind, tuple(d), 1.0, 1.0, tol=1e-6, kspace=ft.KSPACE_FF32)
+    p = info_f.params
+    assert p.form == ft.FORM_FF32
+    same = dict(P=p.P, xi=p.xi, Mx=p.Mx, My=p.My, nside_x=p.nside_x, nside_y=p.nside_y)
+    out_d, _ = _run(ft, gpu_ctx, kind, tuple(d), 1.0, 1.0, tol=1e-6, kspace=ft.KSPACE_FP64, **same)
+    scale = np.max(np.abs(out_d[3]))
+    assert np.max(np.abs(out_f[3] - out_d[3])) <= KS_BOUND * scale + 1e-300, (kind, n)
+
+
+def test_ff32_without_sources(gpu_ctx):
+    """No sources: zero velocities at the targets (the Q read-back, the
+    zero mode and the k-space part all see empty inputs)."""
+    ft = _ft()
+    rng = np.random.default_rng(181)
+    xt, yt = rng.random(40) - 0.5, rng.random(40) - 0.5
+    e = np.zeros(0)
+    for kind in ("slp", "dlp"):
+        if kind == "slp":
+            out = ft.StokesSLP_ewald_2p(e, e, xt, yt, e, e, 1.0, 1.0, tol=1e-6, form=ft.FORM_MIXED, ctx=gpu_ctx)
+        else:
+            out = ft.StokesDLP_ewald_2p(e, e, xt, yt, e, e, e, e, 1.0, 1.0, tol=1e-6, form=ft.FORM_MIXED, ctx=gpu_ctx)
+        assert out[0].shape == (40,) and np.all(out[0] == 0) and np.all(out[1] == 0), kind
