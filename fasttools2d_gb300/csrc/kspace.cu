@@ -1699,7 +1699,7 @@ __device__ __forceinline__ void gather_ff_run(const double* __restrict__ p, cons
     const int P1 = wp.P + 1, W = tile_region(ts, wp.P), WW = W * W;
     float2* r0 = shf;
     float2* r1 = r0 + WW;
-    float2* e1 = r1 + WW;
+    float2* e1 = C32 ? shf + WW : r1 + WW;  // C32: one pair region (below)
     float2* wyb = e1 + e1_len(wp.P, wp.aniso) + threadIdx.x * P1;  // PM == 0 only
     // C32: the grids' high parts interleaved per node (one 8-byte read gives
     // both grids' values; the tile bins' order of the targets keeps a half
@@ -1860,7 +1860,7 @@ __device__ __forceinline__ void gather_ff_run(const double* __restrict__ p, cons
 }
 
 template <int PM, bool C32>
-__global__ void __launch_bounds__(kTileThreads, 5) k_gather_ff(const double* __restrict__ p, const int* __restrict__ toff,
+__global__ void __launch_bounds__(kTileThreads, C32 ? 8 : 5) k_gather_ff(const double* __restrict__ p, const int* __restrict__ toff,
                                                            const int* __restrict__ perm, int ts, int ntx, int nty,
                                                            WinParams wp, const float2* __restrict__ G0,
                                                            const float2* __restrict__ G1, double scale,
@@ -1888,9 +1888,13 @@ inline int gather_pm_class(int PM) {
     return -1;
 }
 
-size_t gather_ff_smem(int ts, int P, int aniso = 0) {
+// c32: the FP32-product gather's region holds one (grid 0, grid 1) pair of
+// high parts per node and its window rows are FP32
+size_t gather_ff_smem(int ts, int P, int aniso = 0, bool c32 = false) {
     const int P1 = P + 1, W = tile_region(ts, P);
     const size_t rows = gather_ff_pm(P1) ? 0 : (size_t)kTileThreads * P1;  // per-thread window columns
+    if (c32)
+        return (size_t)W * W * sizeof(float2) + (size_t)e1_len(P, aniso) * sizeof(float2) + rows * sizeof(float);
     return 2 * (size_t)W * W * sizeof(float2) + (size_t)(e1_len(P, aniso) + rows) * sizeof(float2);
 }
 
@@ -1919,7 +1923,8 @@ bool spread_fits(const fte_context* ctx, int form, int kind, int ts, int P, int 
 bool gather_fits(const fte_context* ctx, int form, int ts, int P, int aniso = 0) {
     if (ts < 8 || ts > 256) return false;
     size_t sm = form == FTE_FORM_MIXED ? gather32_smem(ts, P)
-                : (fte_form_ff(form) ? gather_ff_smem(ts, P, aniso) : gather64_smem(ts, P, aniso));
+                : (fte_form_ff(form) ? gather_ff_smem(ts, P, aniso, form == FTE_FORM_FF32)
+                                       : gather64_smem(ts, P, aniso));
     return sm <= tile_budget(ctx);
 }
 int resolve_tiles(const fte_context* ctx, const KspaceArgs& a, int* ts_s, int* ts_g, bool fill = true) {
@@ -1961,9 +1966,11 @@ int resolve_tiles(const fte_context* ctx, const KspaceArgs& a, int* ts_s, int* t
         // to hide the products' latency; the region re-reads cost little),
         // at most 28 nodes a side (fewer idle threads in a tile's last round
         // of targets; 28 was the fastest of 24..48 at 1e6 points)
-        // (FP32 products: up to 32, the tuner's pick at tol 1e-6)
-        for (int ts = a.form == FTE_FORM_FF32 ? 32 : 28; ts >= 8 && !*ts_g; ts -= 4)
-            if (gather_ff_smem(ts, a.P, an) <= tile_budget(ctx) / 2) *ts_g = ts;
+        // (FP32 products: up to 32 nodes, the tuner's pick at tol 1e-6, and
+        // a half-size region: eight CTAs per SM, registers capped at 64)
+        const bool c32 = a.form == FTE_FORM_FF32;
+        for (int ts = c32 ? 32 : 28; ts >= 8 && !*ts_g; ts -= 4)
+            if (gather_ff_smem(ts, a.P, an, c32) <= tile_budget(ctx) / (c32 ? 4 : 2)) *ts_g = ts;
         if (!*ts_g) *ts_g = 8;
     } else {
         for (int ts = 64; ts >= 8 && !*ts_g; ts -= 4)
@@ -2077,7 +2084,7 @@ int launch_gather_tiled(fte_context* ctx, const KspaceArgs& a, const TileBins& t
     const int grid = nt < ctx->num_sms * 8 ? nt : ctx->num_sms * 8;
     if (fte_form_ff(a.form)) {
         const float2* Hf = static_cast<const float2*>(H);
-        size_t sm = gather_ff_smem(tb.ts, a.P, wp.aniso);
+        size_t sm = gather_ff_smem(tb.ts, a.P, wp.aniso, a.form == FTE_FORM_FF32);
         auto go = [&](auto kern) -> int {
             FTE_CUDA_TRY(fte_smem_ceiling(kern, (int)sm));
             FTE_LAUNCH(ctx, kern, grid, kTileThreads, sm, a.ptar, (const int*)tb.off, (const int*)tb.perm, tb.ts,
