@@ -263,10 +263,15 @@ struct fte_batch {
 };
 
 // the k-space arguments of plan p's vector v in a batch
-static KspaceArgs batch_kspace_args(const fte_plan* p, int v) {
+// multi: arguments for the batch work lists, which evaluate an FP32-product
+// plan with the float-float kernels (the same parameters, window records and
+// grids; the result is the float-float one, within the FP32 products'
+// rounding of the plan's own), so that it joins the work lists instead of
+// running per plan.  A plan the work lists do not take keeps its own form.
+static KspaceArgs batch_kspace_args(const fte_plan* p, int v, bool multi = false) {
     KspaceArgs a;
     a.kind = p->kind;
-    a.form = p->prm.form;
+    a.form = multi && p->prm.form == FTE_FORM_FF32 ? FTE_FORM_FF : p->prm.form;
     a.nsrc = p->nsrc;
     a.ntar = p->ntar;
     a.psrc = p->ps;
@@ -703,9 +708,9 @@ static int batch_build_lists(fte_batch* b) {
         fte_plan* p = b->plans[i];
         b->wl_src[i] = p->tb_src;
         b->wl_tar[i] = p->tb_tar;
-        if (p->prm.form != FTE_FORM_FF || p->ntar == 0) continue;
+        if (!fte_form_ff(p->prm.form) || p->ntar == 0) continue;
         int ts_s = 0, ts_g = 0;
-        FTE_TRY(fte_kspace_batch_tiles(c, batch_kspace_args(p, 0), &ts_s, &ts_g));
+        FTE_TRY(fte_kspace_batch_tiles(c, batch_kspace_args(p, 0, true), &ts_s, &ts_g));
         b->wl_ts[i] = make_int2(ts_s, ts_g);
         if ((p->nsrc > 0 && ts_s != p->tb_src.ts) || ts_g != p->tb_tar.ts) {
             rebuild[i] = 1;
@@ -724,7 +729,7 @@ static int batch_build_lists(fte_batch* b) {
         WsCarver tb{b->mem3, 0, need3};
         for (size_t i = 0; i < np; i++) {
             if (!rebuild[i]) continue;
-            KspaceArgs a = batch_kspace_args(b->plans[i], 0);
+            KspaceArgs a = batch_kspace_args(b->plans[i], 0, true);
             a.ts_spread = b->wl_ts[i].x;
             a.ts_gather = b->wl_ts[i].y;
             FTE_TRY(fte_kspace_tiles(c, tb, a, &b->wl_src[i], &b->wl_tar[i]));
@@ -735,7 +740,7 @@ static int batch_build_lists(fte_batch* b) {
     size_t need = ws_bytes(np * sizeof(PItem), 1) + 4096;
     for (size_t i = 0; i < np; i++) {
         const fte_plan* p = b->plans[i];
-        if (p->prm.form == FTE_FORM_FF && p->ntar > 0) need += (size_t)(nv - 1) * ws_bytes(p->kscratch_size, 1);
+        if (fte_form_ff(p->prm.form) && p->ntar > 0) need += (size_t)(nv - 1) * ws_bytes(p->kscratch_size, 1);
     }
     std::vector<int2> dens, zero, comb;
     for (size_t i = 0; i < np; i++) {
@@ -786,7 +791,7 @@ static int batch_build_lists(fte_batch* b) {
             FTE_WS_CHECK(m);
             WsCarver wc{scr, 0, p->kscratch_size};
             bool taken = false;
-            KspaceArgs a = batch_kspace_args(p, v);
+            KspaceArgs a = batch_kspace_args(p, v, true);
             if (b->wl_ts[i].y > 0) {
                 a.ts_spread = b->wl_ts[i].x;
                 a.ts_gather = b->wl_ts[i].y;
