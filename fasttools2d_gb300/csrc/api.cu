@@ -906,6 +906,13 @@ static const double kWinRatio[2] = {3000.0, 300.0};
 // (also the floor of FTE_FORM_FF32: its FP32 products left 1.6e-7 / 1.6e-8
 // at 1e6 uniform points on the parameters of tol 1e-11)
 static const double kFp32Floor[2] = {1e-6, 2e-7};
+// FTE_FORM_FF32 only up to this window support: measured at 6000 points
+// against FP64 on the same parameters, the k-space part stays at the FP32
+// floor (~1e-7) up to P = 36 and then loses accuracy in the Stokeslet spread
+// (5e-6 at P = 40, 5e-3 at P = 44); the float-float spread with the FP32
+// gather stays at the floor there, the FP32-product spread is the part that
+// degrades.  The tuned choice reaches FTE_FORM_FF32 at P <= 16.
+static const int kFf32MaxP = 30;
 // float-float spread and gather (~48-bit values) hold their ~1e-13 relative
 // error well below tolerances from 1e-11 up
 static const double kFfFloor[2] = {1e-11, 1e-11};
@@ -920,6 +927,11 @@ static int choose_params_tuned(int kind, int64_t nsrc, int64_t ntar, double Q, d
     if (force < FTE_KSPACE_AUTO || force > FTE_KSPACE_FF32) {
         fte_set_error("unknown k-space arithmetic %d", force);
         return FTE_ERR_INVALID;
+    }
+    if (force == FTE_KSPACE_FF32 && opt && opt->P > kFf32MaxP) {
+        fte_set_error("FP32-product k-space: window support P=%d above %d (its Stokeslet spread loses accuracy "
+                      "beyond that)", opt->P, kFf32MaxP);
+        return FTE_ERR_UNSUPPORTED;
     }
     const bool fp32 = tol >= kFp32Floor[kind];
     const bool ffok = tol >= kFfFloor[kind];
@@ -1016,7 +1028,8 @@ static int choose_params_tuned(int kind, int64_t nsrc, int64_t ntar, double Q, d
             bool allowed;
             if (force == FTE_KSPACE_AUTO)
                 allowed = f == FTE_FORM_MIXED ? fp32 && fits32
-                                              : (f == FTE_FORM_FF32 ? fp32 && ffok : (f == FTE_FORM_FF ? ffok : true));
+                                              : (f == FTE_FORM_FF32 ? fp32 && ffok && P <= kFf32MaxP
+                                                                    : (f == FTE_FORM_FF ? ffok : true));
             else if (force == FTE_KSPACE_FP32)
                 allowed = f == FTE_FORM_MIXED && fits32;
             else

@@ -395,14 +395,15 @@ __global__ void __launch_bounds__(kColThreads) k_spread_cols(int mode, const dou
                 const int lx = org[2 * s];
                 if (lx < 0) continue;
                 const int ly = org[2 * s + 1];
-                // first column >= lx owned by this warp
-                int c = lx + ((warp - lx) & (nw - 1));
-                if (lane < P1) {
-                    const double wyj = wy[s * P1 + lane];
+                // first column >= lx owned by this warp; window rows in
+                // blocks of 32 (P up to 64)
+                const int c0 = lx + ((warp - lx) & (nw - 1));
+                for (int j = lane; j < P1; j += 32) {
+                    const double wyj = wy[s * P1 + j];
                     const double* fa = fw + (s * 2) * P1;
                     const double* fb = fa + P1;
-                    for (; c <= lx + wp.P; c += nw) {
-                        double* b0 = buf + c * W + ly + lane;
+                    for (int c = c0; c <= lx + wp.P; c += nw) {
+                        double* b0 = buf + c * W + ly + j;
                         b0[0] = fma(fa[c - lx], wyj, b0[0]);
                         b0[WW] = fma(fb[c - lx], wyj, b0[WW]);
                     }
@@ -1164,12 +1165,13 @@ __global__ void __launch_bounds__(kColThreads) k_spread_cols32(int mode, const d
                 const int lx = org[2 * s];
                 if (lx < 0) continue;
                 const int ly = org[2 * s + 1];
-                int c = lx + ((warp - lx) & (nw - 1));
-                if (lane < P1) {
-                    const float wyj = wy[s * P1 + lane];
+                // window rows in blocks of 32 (P up to 64)
+                const int c0 = lx + ((warp - lx) & (nw - 1));
+                for (int j = lane; j < P1; j += 32) {
+                    const float wyj = wy[s * P1 + j];
                     const float* fa = fw + (s * 2) * P1;
-                    for (; c <= lx + wp.P; c += nw) {
-                        const int at = c * W + ly + lane;
+                    for (int c = c0; c <= lx + wp.P; c += nw) {
+                        const int at = c * W + ly + j;
 #pragma unroll
                         for (int g = 0; g < 2; g++) {
                             // Kahan: sum += v with carry
@@ -1553,9 +1555,11 @@ __device__ __forceinline__ void spread_ff_run(const FfWin* __restrict__ recs, co
             // alternate owned columns of a window (row j = lane mod 16), one
             // pass per two columns instead of half the lanes idle
             const bool split = P1 <= 16;
-            const int j = split ? (lane & 15) : lane;
             const int cstep = split ? 2 * nw : nw;
-            if (j < P1) {
+            // window rows in blocks of 32 (P up to 64; one block when split)
+            for (int jb = 0; jb < P1; jb += 32) {
+                const int j = split ? (lane & 15) : jb + lane;
+                if (j >= P1) continue;
                 for (int s = 0; s < cn; s++) {
                     const int2 o = *reinterpret_cast<const int2*>(org + 2 * s);
                     const int lx = o.x, ly = o.y;
@@ -2092,11 +2096,13 @@ int launch_gather_tiled(fte_context* ctx, const KspaceArgs& a, const TileBins& t
             return FTE_OK;
         };
         if (a.form == FTE_FORM_FF32) {
-            // FP32 products: the instances for 16, 24 and 32 nodes
+            // FP32 products: the instances for 16, 24 and 32 nodes (the
+            // form is confined to P <= 30)
             const int pm = gather_ff_pm(a.P + 1);
-            if (pm == 0)
-                FTE_TRY(go(k_gather_ff<0, true>));
-            else if (pm <= 16)
+            if (pm == 0) {
+                fte_set_error("internal: FP32-product gather with a support of %d nodes", a.P + 1);
+                return FTE_ERR_INVALID;
+            } else if (pm <= 16)
                 FTE_TRY(go(k_gather_ff<16, true>));
             else if (pm <= 24)
                 FTE_TRY(go(k_gather_ff<24, true>));

@@ -72,7 +72,8 @@ extern "C" {
  *                   transforms, multiplier and gather (tol >= 1e-11);
  *   FTE_FORM_FF32   float-float window factors, transforms and multiplier,
  *                   FP32 products with Kahan-compensated sums in the spread
- *                   and gather (tol >= 1e-6 SLP, 2e-7 DLP).
+ *                   and gather (tol >= 1e-6 SLP, 2e-7 DLP; window supports
+ *                   P <= 30, FTE_ERR_UNSUPPORTED when forced beyond).
  * The real-space pairs of the mixed form are FP32 for pairs whose terms lie
  * far below the tolerance, float-float for the others from tol 1e-11, and
  * FP64 below (fte_options.near). */

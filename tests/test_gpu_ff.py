@@ -67,10 +67,11 @@ def test_ff_kspace_matches_fp64(gpu_ctx, kind, geom):
 
 
 @pytest.mark.parametrize("kind", ["slp", "dlp"])
-@pytest.mark.parametrize("P", [12, 16, 24, 32])
+@pytest.mark.parametrize("P", [12, 16, 24, 32, 48])
 def test_ff_gather_supports(gpu_ctx, kind, P):
     """Window supports on either side of the gather's register bounds (16, 24
-    and 32 nodes) and beyond them (the shared-memory form)."""
+    and 32 nodes) and beyond them (the shared-memory form; 49 nodes: the
+    spread's rows in two blocks of 32)."""
     ft = _ft()
     Lx, Ly = 1.0, 1.5
     d = _case(60 + P, 6000, Lx, Ly)

@@ -8,8 +8,8 @@ the FP32 form's floor -- and the form is only chosen where the tolerance is
 at least 1e-6 (SLP) / 2e-7 (DLP).
 
 * against the FP64 k-space on the same parameters, on square, wide and tall
-  boxes, every gather instance (window supports 9..35 nodes: the register
-  forms for 16, 24, 32 nodes and the shared-memory form) and around the long
+  boxes, every gather instance (window supports 9..31 nodes: the register
+  forms for 16, 24, 32 nodes; the form is confined to P <= 30) and around the long
   transforms (windows wrapping a 32-node axis: the spread's and gather's
   out-of-region paths);
 * the tuned choice picks it at tol 1e-6 and 1e-5 and meets the tolerance
@@ -78,15 +78,27 @@ def test_ff32_kspace_near_fp64(gpu_ctx, kind, geom):
 
 
 @pytest.mark.parametrize("kind", ["slp", "dlp"])
-@pytest.mark.parametrize("P", [8, 12, 16, 24, 30, 34])
+@pytest.mark.parametrize("P", [8, 12, 16, 24, 30])
 def test_ff32_gather_supports(gpu_ctx, kind, P):
     """Window supports of every gather instance: 9 and 13 nodes (the
-    16-node form), 17 (24), 25 and 31 (32) and 35 (shared-memory rows)."""
+    16-node form), 17 (24), 25 and 31 (32)."""
     ft = _ft()
     Lx, Ly = 1.0, 1.5
     rel, p = _vs_fp64(ft, gpu_ctx, kind, _case(160 + P, 6000, Lx, Ly), Lx, Ly, tol=1e-6, P=P)
     assert p.P == P
     assert rel <= KS_BOUND, rel
+
+
+def test_ff32_rejects_wide_windows(gpu_ctx):
+    """The form is confined to P <= 30: forcing it with a wider window is
+    refused, and the tuned choice takes another arithmetic."""
+    ft = _ft()
+    d = _case(190, 3000, 1.0, 1.0)
+    with pytest.raises(ft.FteError) as e:
+        _run(ft, gpu_ctx, "slp", d, 1.0, 1.0, tol=1e-6, kspace=ft.KSPACE_FF32, P=34)
+    assert e.value.code == ft.FTE_ERR_UNSUPPORTED
+    _, info = _run(ft, gpu_ctx, "slp", d, 1.0, 1.0, tol=1e-6, P=34)
+    assert info.params.form != ft.FORM_FF32
 
 
 @pytest.mark.parametrize("kind", ["slp", "dlp"])

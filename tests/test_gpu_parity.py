@@ -129,6 +129,32 @@ def test_kspace_gateway_points_outside_box(gpu_ctx, kind):
     assert rel_max(out, ref) <= TOL_FP64
 
 
+@pytest.mark.parametrize("kind", ["slp", "dlp"])
+@pytest.mark.parametrize("P", [32, 40, 48, 64])
+def test_kspace_gateway_wide_windows(gpu_ctx, kind, P):
+    """Window supports of 33 to 65 nodes (the gateways accept P up to 64):
+    the tiled spread covers a window's rows in blocks of 32 lanes."""
+    ft = _ft()
+    rng = np.random.default_rng(22 + P)
+    ns, nt = 1500, 800
+    ps = rng.random((ns, 2)) - 0.5
+    pt = rng.random((nt, 2)) - 0.5
+    f = rng.standard_normal((ns, 2))
+    th = rng.random(ns) * 2 * np.pi
+    n = np.stack([np.cos(th), np.sin(th)], 1)
+    Mx = My = 128
+    xi = 30.0
+    w = P * (1.0 / Mx) / 2
+    eta = (2 * xi * w / (0.95 * np.sqrt(np.pi * P))) ** 2
+    if kind == "slp":
+        ref = po.slp_kspace(ps, pt, xi, eta, f, Mx, My, 1.0, 1.0, w, P)
+        out = ft.mex_stokes_slp_kspace(ps, pt, xi, eta, f, Mx, My, 1.0, 1.0, w, P, ctx=gpu_ctx)
+    else:
+        ref = po.dlp_kspace(ps, pt, xi, eta, f, n, Mx, My, 1.0, 1.0, w, P)
+        out = ft.mex_stokes_dlp_kspace(ps, pt, xi, eta, f, n, Mx, My, 1.0, 1.0, w, P, ctx=gpu_ctx)
+    assert rel_max(out, ref) <= TOL_FP64
+
+
 def test_device_pointers_match_host(gpu_ctx):
     import torch
 
