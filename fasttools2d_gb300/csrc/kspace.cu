@@ -397,12 +397,12 @@ __global__ void __launch_bounds__(kColThreads) k_spread_cols(int mode, const dou
                 const int ly = org[2 * s + 1];
                 // first column >= lx owned by this warp; window rows in
                 // blocks of 32 (P up to 64)
-                const int c0 = lx + ((warp - lx) & (nw - 1));
+                const int cfirst = lx + ((warp - lx) & (nw - 1));
                 for (int j = lane; j < P1; j += 32) {
                     const double wyj = wy[s * P1 + j];
                     const double* fa = fw + (s * 2) * P1;
                     const double* fb = fa + P1;
-                    for (int c = c0; c <= lx + wp.P; c += nw) {
+                    for (int c = cfirst; c <= lx + wp.P; c += nw) {
                         double* b0 = buf + c * W + ly + j;
                         b0[0] = fma(fa[c - lx], wyj, b0[0]);
                         b0[WW] = fma(fb[c - lx], wyj, b0[WW]);
@@ -1166,11 +1166,11 @@ __global__ void __launch_bounds__(kColThreads) k_spread_cols32(int mode, const d
                 if (lx < 0) continue;
                 const int ly = org[2 * s + 1];
                 // window rows in blocks of 32 (P up to 64)
-                const int c0 = lx + ((warp - lx) & (nw - 1));
+                const int cfirst = lx + ((warp - lx) & (nw - 1));
                 for (int j = lane; j < P1; j += 32) {
                     const float wyj = wy[s * P1 + j];
                     const float* fa = fw + (s * 2) * P1;
-                    for (int c = c0; c <= lx + wp.P; c += nw) {
+                    for (int c = cfirst; c <= lx + wp.P; c += nw) {
                         const int at = c * W + ly + j;
 #pragma unroll
                         for (int g = 0; g < 2; g++) {
